@@ -1,0 +1,310 @@
+#!/usr/bin/env python
+"""Spin-flip throughput on one GB300 (and N independent replicas on N GPUs).
+
+Workload (the 2-D configuration the headline metric is quoted on): Ising, L=4096
+periodic, J=1, h=0, int8 spins, +/-1 start from seed 7, Metropolis checkerboard
+sweeps at beta=0.4407, energy and magnetisation recorded every sweep.  One step is
+one mcx_sweep call of --sweeps-per-step sweeps.  The lattice (16 MiB) fits in L2,
+so L2 is flushed (256 MiB write) between timed steps.
+
+  value      attempts/ns with the lattice resident in HBM, CUDA events on the
+             library's stream (torch's current stream is handed to the context)
+  e2e        the same metric through the public C ABI with host buffers: every step
+             uploads the lattice from pinned host memory (mcx_set_spins) and reads
+             the per-sweep (pair, spin, spin2) series back (mcx_sweep obs_series)
+  roofline   the half-sweep kernel: algorithmic bytes 1.5*N per launch (reads both
+             colour arrays, writes its own) over the average launch time
+  cpu_baseline  the oracle's sequential random-site mode (the reference's
+             spin_flip! order, FP64 exp decisions), one chain per host core
+
+`--impl reference` times that CPU path alone on every host core.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "montecarlox.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+L_SIDE = 4096
+BETA = 0.4407
+SEED = 7
+METRIC = "spin-flip attempts/ns"
+UNIT = "attempts/ns"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mcx", "reference"], default="mcx")
+    ap.add_argument("--sweeps-per-step", type=int, default=200)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per half-sweep launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ising_cb_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_full_size")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            os.unlink(self.path)
+        except Exception:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(seconds, nthreads):
+    """Oracle sequential random-site mode on `nthreads` chains, sized to ~`seconds`."""
+    import oracle as O
+
+    L = [L_SIDE, L_SIDE]
+    pilot = 200_000
+    t = O.bench_seq(O.ISING, L, O.METROPOLIS, BETA, SEED, nthreads, pilot)
+    rate = nthreads * pilot / max(t, 1e-6)
+    per_thread = max(pilot, int(rate * seconds / nthreads))
+    t = O.bench_seq(O.ISING, L, O.METROPOLIS, BETA, SEED, nthreads, per_thread)
+    return nthreads * per_thread / (t * 1e9), t, per_thread
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    ncores = os.cpu_count() or 1
+    secs = max(1.0, min(5.0, 120.0 / max(1, args.steps + args.warmup)))
+    vals, times, per = [], [], 0
+    for k in range(args.warmup + args.steps):
+        v, t, per = cpu_sample(secs, ncores)
+        if k >= args.warmup:
+            vals.append(v)
+            times.append(t)
+    value = statistics.mean(vals)
+    sample = "%d host threads x %d sequential random-site Metropolis attempts on an L=%d lattice each" % (
+        ncores, per, L_SIDE)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "ising2d_L4096_metropolis", "L": L_SIDE, "beta": BETA, "seed": SEED,
+                   "order": "sequential random-site (spin_flip! order)", "precision": "fp64 exp decisions"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_mcx(args):
+    import numpy as np
+    import torch
+
+    import mcx
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    ctx = mcx.Context(device=local, stream=stream.cuda_stream)
+    S = args.sweeps_per_step
+    L = [L_SIDE, L_SIDE]
+    N = L_SIDE * L_SIDE
+    lat = mcx.Ising(L, ctx=ctx)
+    mcx.init_(lat, "random", rng=mcx.Philox(SEED, rank))
+    alg = mcx.Metropolis(mcx.Philox(SEED, rank), beta=BETA)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def enqueue_step():
+        rng = alg.rng._c()
+        mcx._check(mcx._lib.load().mcx_sweep(lat.handle, alg.ALG, BETA, mcx.C.byref(rng), S, None, None))
+        alg.rng.counter = rng.counter
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        enqueue_step()
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches()
+    barrier()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        enqueue_step()
+        ev[k][1].record(stream)
+    barrier()
+    launches = ctx.launches() - launches0
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    attempts = N * S * args.steps * ws
+    value = attempts / (total_ms * 1e6)
+
+    # roofline of the half-sweep kernel (2 launches per sweep)
+    avg_launch_s = total_ms * 1e-3 / (2 * S * args.steps)
+    alg_bytes = 1.5 * N
+    achieved = alg_bytes / avg_launch_s / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # end to end through the C ABI with pinned host buffers
+    host_spins = torch.empty(N, dtype=torch.int8).pin_memory()
+    host_spins.numpy()[:] = lat.spins
+    host_obs = torch.empty((S, 3), dtype=torch.int64).pin_memory()
+    lib = mcx._lib.load()
+    e2e_times = []
+    barrier()
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mcx._check(lib.mcx_set_spins(lat.handle, host_spins.data_ptr(), N))
+        rng = alg.rng._c()
+        cnt = mcx._lib.mcx_counters(0, 0)
+        mcx._check(lib.mcx_sweep(lat.handle, alg.ALG, BETA, mcx.C.byref(rng), S, host_obs.data_ptr(),
+                                 mcx.C.byref(cnt)))
+        alg.rng.counter = rng.counter
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e_s = sum(e2e_times)
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
+    barrier()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        ncores = os.cpu_count() or 1
+        v, t, per = cpu_sample(args.cpu_seconds, ncores)
+        cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
+               "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
+                         "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
+    tr = traffic_per_launch()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+        "config": {"workload": "ising2d_L4096_metropolis_int8", "L": L_SIDE, "beta": BETA, "seed": SEED,
+                   "layout": "int8 colour-split", "sweeps_per_step": S, "record": "E,M every sweep",
+                   "l2": "flushed between timed steps (256 MiB write)", "replicas_per_gpu": 1,
+                   "parallelism": "replicas"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
+                     "kernel": "k_ising_cb<2,16,false>", "alg_bytes_per_launch": alg_bytes},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
+                "d2h_bytes_per_step": S * 3 * 8 + 8},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mcx(args)
+
+
+if __name__ == "__main__":
+    main()

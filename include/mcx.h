@@ -1,0 +1,162 @@
+/*
+ * mcx.h -- C ABI of libmcx_cuda, the GB300 (sm_103a) spin-flip library.
+ *
+ * The library accelerates one hot path of MonteCarloX.jl + SpinSystems: the
+ * single-spin-flip Metropolis / Glauber / HeatBath sweep over Ising and
+ * Blume-Capel lattices, the Multicanonical / Wang-Landau histogram-and-weight
+ * update, and the replica-exchange step of parallel tempering.  Every entry
+ * point names the reference interface it replaces (paths inside MonteCarloX.jl).
+ *
+ * Conventions
+ *   - Plain C types only; handles are opaque.  Device memory is owned by the
+ *     library; host buffers are owned by the caller.
+ *   - Spins cross the boundary in the SpinSystems linear order: site
+ *     i = x + Lx*(y + Ly*z) (0-based), the Graphs.grid vertex order used by
+ *     Ising(dims)/BlumeCapel(dims) (SpinSystems/src/ising.jl:523-534) and by
+ *     IsingLatticeOptim (ising.jl:550-571).  Values are int8 in {-1,+1} (Ising)
+ *     or {-1,0,+1} (Blume-Capel), as SpinSystems' `spins::Vector{Int8}`.
+ *   - A context owns one CUDA stream; calls on one context are ordered on it.
+ *     A context is not thread-safe; distinct contexts are independent.
+ *   - Every call returns an mcx_status; mcx_last_error_string() gives details
+ *     for the calling thread.  MCX_ERR_OUT_OF_RANGE is the BoundsError of the
+ *     reference (an energy outside the histogram bins).
+ *   - Lattices on the device need every side even and >= 4 (checkerboard order).
+ */
+#ifndef MCX_H
+#define MCX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MCX_API __attribute__((visibility("default")))
+#else
+#define MCX_API
+#endif
+
+typedef enum mcx_status {
+    MCX_OK = 0,
+    MCX_ERR_INVALID_ARG = 1,
+    MCX_ERR_OUT_OF_RANGE = 2, /* energy left the bin range (reference: BoundsError) */
+    MCX_ERR_OOM = 3,          /* cudaMalloc failed                                  */
+    MCX_ERR_BUDGET = 4,       /* the context's HBM budget would be exceeded          */
+    MCX_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up                  */
+    MCX_ERR_CUDA = 6,         /* any other CUDA runtime error                        */
+    MCX_ERR_NOT_READY = 7,    /* a request has not finished yet                      */
+    MCX_ERR_NOT_FOUND = 8     /* unknown request / handle                            */
+} mcx_status;
+
+typedef enum mcx_model { MCX_ISING = 0, MCX_BLUME_CAPEL = 1 } mcx_model;
+
+/* Metropolis: src/algorithms/metropolis.jl:124-127, Glauber: :231-237,
+ * HeatBath: src/algorithms/heat_bath.jl + SpinSystems ising.jl:153-168 /
+ * blume_capel.jl:61-85. */
+typedef enum mcx_algorithm { MCX_METROPOLIS = 0, MCX_GLAUBER = 1, MCX_HEATBATH = 2 } mcx_algorithm;
+
+/* INT8: one byte per site.  MSC64: 64 same-colour sites per uint64 word
+ * (Ising only; needs Lx a multiple of 128). */
+typedef enum mcx_layout { MCX_LAYOUT_INT8 = 0, MCX_LAYOUT_MSC64 = 1 } mcx_layout;
+
+/* Flat-histogram mode: Multicanonical (src/algorithms/multicanonical.jl) or
+ * Wang-Landau (src/algorithms/wang_landau.jl). */
+typedef enum mcx_flathist_mode { MCX_MUCA = 0, MCX_WANG_LANDAU = 1 } mcx_flathist_mode;
+
+typedef struct mcx_config {
+    int device;          /* CUDA device ordinal                                  */
+    void* stream;        /* cudaStream_t to run on; NULL = a library-owned stream */
+    uint64_t hbm_budget; /* bytes this context may allocate on the device; 0 = none */
+} mcx_config;
+
+/* Counter-based random stream: Philox4x32-10 keyed by `seed`; `counter` is the
+ * next sweep index and advances by the number of sweeps run; `stream` separates
+ * independent chains with the same seed.  Stands in for the `rng` field of the
+ * reference's algorithm objects (src/algorithms/metropolis.jl:173-178). */
+typedef struct mcx_rng {
+    uint64_t seed;
+    uint64_t counter;
+    uint32_t stream;
+    uint32_t reserved;
+} mcx_rng;
+
+/* `steps` / `accepted` of the reference's algorithm objects
+ * (src/algorithms/importance_sampling.jl:23-28); accumulated, never reset. */
+typedef struct mcx_counters {
+    uint64_t attempts;
+    uint64_t accepted;
+} mcx_counters;
+
+typedef struct mcx_ctx mcx_ctx;
+typedef struct mcx_lattice mcx_lattice;
+typedef struct mcx_flathist mcx_flathist;
+typedef struct mcx_pt mcx_pt;
+typedef struct mcx_server mcx_server;
+
+/* ---------------------------------------------------------------- errors -- */
+MCX_API const char* mcx_status_string(mcx_status status);
+MCX_API const char* mcx_last_error_string(void);
+MCX_API int mcx_version(void);
+
+/* --------------------------------------------------------------- context -- */
+MCX_API mcx_status mcx_ctx_create(const mcx_config* config, mcx_ctx** out);
+MCX_API mcx_status mcx_ctx_destroy(mcx_ctx* ctx);
+MCX_API mcx_status mcx_sync(mcx_ctx* ctx);
+MCX_API mcx_status mcx_ctx_stream(mcx_ctx* ctx, void** stream);
+MCX_API mcx_status mcx_ctx_memory(mcx_ctx* ctx, uint64_t* used, uint64_t* budget);
+/* Number of kernels this context has launched so far (for launch accounting). */
+MCX_API mcx_status mcx_ctx_launches(mcx_ctx* ctx, uint64_t* launches);
+
+/* --------------------------------------------------------------- lattice -- */
+/* Replaces Ising(dims; J, periodic=true, h) (SpinSystems/src/ising.jl:523-534),
+ * IsingLatticeOptim(Lx, Ly) (ising.jl:550-571) and BlumeCapel(dims; J, D, h)
+ * (SpinSystems/src/blume_capel.jl:500-511).  All spins start at +1, like the
+ * reference constructors. */
+MCX_API mcx_status mcx_lattice_create(mcx_ctx* ctx, mcx_model model, int dim,
+                                      const int32_t* L, mcx_layout layout, double J,
+                                      double D, double h, mcx_lattice** out);
+MCX_API mcx_status mcx_lattice_destroy(mcx_lattice* lat);
+MCX_API mcx_status mcx_lattice_info(const mcx_lattice* lat, int64_t* nsites,
+                                    int64_t* device_bytes);
+
+/* The `spins` field of the reference systems (copy in / copy out). */
+MCX_API mcx_status mcx_set_spins(mcx_lattice* lat, const int8_t* host, size_t n);
+MCX_API mcx_status mcx_get_spins(mcx_lattice* lat, int8_t* host, size_t n);
+
+/* init!(sys, :random; rng) (ising.jl:170-188, blume_capel.jl:87-109), fed by Philox. */
+MCX_API mcx_status mcx_init_random(mcx_lattice* lat, uint64_t seed, uint32_t stream);
+/* init!(sys, :up / :down / :zero): every site set to `value`. */
+MCX_API mcx_status mcx_init_uniform(mcx_lattice* lat, int8_t value);
+
+/* Cached bookkeeping of the reference systems (sum_pair_interactions without J,
+ * sum_spins, sum_spins2; ising.jl:196-203, blume_capel.jl:117-127).  Waits for
+ * the stream. */
+MCX_API mcx_status mcx_observables(mcx_lattice* lat, int64_t* pair_sum, int64_t* spin_sum,
+                                   int64_t* spin2_sum);
+/* energy(sys; full=true) / magnetization(sys; full=true): recompute the bookkeeping
+ * from the spins (ising.jl:127-128, _recompute_cached! :251-269); waits. */
+MCX_API mcx_status mcx_recompute_observables(mcx_lattice* lat, int64_t* pair_sum,
+                                             int64_t* spin_sum, int64_t* spin2_sum);
+/* energy(sys), magnetization(sys) (ising.jl:127-128, blume_capel.jl:18-19):
+ * E = -J*pair_sum - h*spin_sum + D*spin2_sum. */
+MCX_API mcx_status mcx_energy(mcx_lattice* lat, double* energy, int64_t* magnetization);
+
+/* N x spin_flip!(sys, alg) per sweep in checkerboard order, `nsweeps` sweeps
+ * (replaces the user loop `for _ in 1:N; spin_flip!(sys, alg); end`, e.g.
+ * docs/src/examples/spin_systems/importance_Ising2D.jl:105-122, over
+ * spin_flip! ising.jl:145-168 / blume_capel.jl:52-85).
+ *   obs_series: host int64[nsweeps*3] of (pair_sum, spin_sum, spin2_sum) after each
+ *               sweep, or NULL.  counters: accumulated, or NULL.
+ * With both NULL the call only enqueues work on the context stream. */
+MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
+                             mcx_rng* rng, int64_t nsweeps, int64_t* obs_series,
+                             mcx_counters* counters);
+/* Copy the per-sweep series of the last mcx_sweep call (first n sweeps). */
+MCX_API mcx_status mcx_read_series(mcx_lattice* lat, int64_t* obs_series, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCX_H */

@@ -1,0 +1,135 @@
+// mcx_device.cuh -- device helpers: Philox4x32-10, 53-bit uniforms, the project
+// log, warp/block integer reductions.  Compiled with --fmad=false so that every
+// FP64 expression is evaluated exactly as written.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+namespace mcx {
+
+__host__ __device__ __forceinline__ double bits_to_double(long long b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(b);
+#else
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ long long double_to_bits(double d) {
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(d);
+#else
+    long long b;
+    std::memcpy(&b, &d, 8);
+    return b;
+#endif
+}
+
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+__device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += kPhiloxW0;
+            k1 += kPhiloxW1;
+        }
+        unsigned long long p0 = (unsigned long long)kPhiloxM0 * c.x;
+        unsigned long long p1 = (unsigned long long)kPhiloxM1 * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1,
+                       (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0);
+    }
+    return c;
+}
+
+// word 2 of a checkerboard counter
+__device__ __forceinline__ uint32_t ctr_word2(unsigned long long sweep, int colour,
+                                              uint32_t purpose) {
+    return ((uint32_t)(sweep >> 32) & 0xFFFFu) | ((uint32_t)colour << 16) | (purpose << 24);
+}
+
+__device__ __forceinline__ uint32_t pick4(uint4 w, int lane) {
+    return lane == 0 ? w.x : lane == 1 ? w.y : lane == 2 ? w.z : w.w;
+}
+
+__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
+    unsigned long long k = ((unsigned long long)hi << 21) | (unsigned long long)(lo >> 11);
+    return (double)k * 1.1102230246251565404236316680908203125e-16;  // 2^-53
+}
+
+// log(x) from log(m) = 2 atanh((m-1)/(m+1)) after x = 2^k m, m in [sqrt(1/2), sqrt(2)).
+// Plain multiplies and adds, in a fixed order, so host and device agree bit for bit.
+__host__ __device__ __forceinline__ double mcx_log(double x) {
+    if (x != x) return x;
+    if (x < 0.0) return bits_to_double(0x7FF8000000000000ll);
+    if (x == 0.0) return bits_to_double(0xFFF0000000000000ll);
+    if (x == bits_to_double(0x7FF0000000000000ll)) return x;
+    long long b = double_to_bits(x);
+    long long k = 0;
+    if ((b >> 52) == 0) {
+        double y = x * 18014398509481984.0;  // 2^54
+        b = double_to_bits(y);
+        k = -54;
+    }
+    k += (b >> 52) - 1023;
+    double m = bits_to_double((b & 0x000FFFFFFFFFFFFFll) | 0x3FF0000000000000ll);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        k += 1;
+    }
+    double f = m - 1.0;
+    double s = f / (m + 1.0);
+    double s2 = s * s;
+    double p = 1.0 / 23.0;
+    p = p * s2 + 1.0 / 21.0;
+    p = p * s2 + 1.0 / 19.0;
+    p = p * s2 + 1.0 / 17.0;
+    p = p * s2 + 1.0 / 15.0;
+    p = p * s2 + 1.0 / 13.0;
+    p = p * s2 + 1.0 / 11.0;
+    p = p * s2 + 1.0 / 9.0;
+    p = p * s2 + 1.0 / 7.0;
+    p = p * s2 + 1.0 / 5.0;
+    p = p * s2 + 1.0 / 3.0;
+    double two_s = s + s;
+    double lm = two_s + two_s * (s2 * p);
+    double kd = (double)k;
+    const double ln2_hi = 6.93147180369123816490e-01;
+    const double ln2_lo = 1.90821492927058770002e-10;
+    return kd * ln2_hi + (lm + kd * ln2_lo);
+}
+
+// Block-wide sum of up to 4 int64 values, one atomicAdd per value per block.
+template <int NV>
+__device__ __forceinline__ void block_add_atomic(long long (&v)[NV], unsigned long long* const (&dst)[NV]) {
+    __shared__ long long red[32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        long long x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if (lane == 0) red[warp][j] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            long long x = lane < nw ? red[lane][j] : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+            if (lane == 0 && x != 0 && dst[j] != nullptr) atomicAdd(dst[j], (unsigned long long)x);
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace mcx

@@ -1,0 +1,97 @@
+// mcx_internal.h -- host-side internals shared by the libmcx_cuda translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/mcx.h"
+
+namespace mcx {
+
+// Philox counter word 2 carries (sweep hi16 | colour<<16 | purpose<<24).
+enum Purpose : uint32_t {
+    P_ACCEPT = 0,   // acceptance / heat-bath word of a site
+    P_PROPOSE = 1,  // Blume-Capel proposal bit (top bit of the word)
+    P_LOW = 2,      // low word of a 53-bit uniform (flat-histogram decisions)
+    P_INIT = 3,     // init!(sys, :random)
+    P_EXCHANGE = 4  // replica-exchange uniform
+};
+
+void set_error(const char* fmt, ...);
+mcx_status fail(mcx_status st, const char* fmt, ...);
+mcx_status cuda_fail(cudaError_t e, const char* what);
+
+#define MCX_CUDA(call)                                             \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return ::mcx::cuda_fail(_e, #call); \
+    } while (0)
+
+#define MCX_CHECK(expr)                       \
+    do {                                      \
+        mcx_status _s = (expr);               \
+        if (_s != MCX_OK) return _s;          \
+    } while (0)
+
+// Largest acceptance table: Blume-Capel Metropolis in 3-D has 3*2*13 entries.
+constexpr int kMaxTable = 80;
+
+struct Table {
+    uint64_t thr[kMaxTable];  // 2^32 means "always"
+    int n;
+};
+
+// Host-side table construction (same rules as the reference; see mcx_tables.cu).
+mcx_status build_ising_table(int dim, mcx_algorithm alg, double beta, double J, double h,
+                             Table* t);
+mcx_status build_bc_table(int dim, mcx_algorithm alg, double beta, double J, double D,
+                          double h, Table* t);
+
+}  // namespace mcx
+
+struct mcx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t budget = 0;
+    uint64_t used = 0;
+    uint64_t launches = 0;
+    int num_sms = 0;
+};
+
+struct mcx_lattice {
+    mcx_ctx* ctx = nullptr;
+    mcx_model model = MCX_ISING;
+    mcx_layout layout = MCX_LAYOUT_INT8;
+    int dim = 2;
+    int64_t L[3] = {1, 1, 1};
+    double J = 1, D = 0, h = 0;
+    int64_t N = 0;       // sites
+    int64_t W = 0;       // sites of one colour per row (Lx/2)
+    int64_t rows = 0;    // Ly*Lz
+    // INT8 layout: colour-split arrays, row r = y + Ly*z, entry k <-> x = 2k + ((y+z+c)&1)
+    int8_t* d_col[2] = {nullptr, nullptr};
+    // MSC64 layout: same order, bit b of word w <-> k = 64*w + b
+    unsigned long long* d_msc[2] = {nullptr, nullptr};
+    int8_t* d_lin = nullptr;       // staging buffer in linear order (set/get)
+    int64_t* d_state = nullptr;    // current (pair_sum, spin_sum, spin2_sum)
+    unsigned long long* d_acc = nullptr;  // accepted-move counter
+    int64_t* d_series = nullptr;   // per-sweep deltas, then the running series
+    int64_t series_cap = 0;        // in sweeps
+    int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
+    int64_t device_bytes = 0;
+};
+
+namespace mcx {
+mcx_status dev_alloc(mcx_ctx* ctx, void** p, size_t bytes);
+void dev_free(mcx_ctx* ctx, void* p, size_t bytes);
+// launch accounting helper
+inline void count_launch(mcx_ctx* ctx, uint64_t n = 1) { ctx->launches += n; }
+mcx_status ensure_series(mcx_lattice* lat, int64_t nsweeps);
+mcx_status recompute_state(mcx_lattice* lat);
+// enqueue kernels that finish a run: prefix-sum the per-sweep deltas into the series
+mcx_status finish_series(mcx_lattice* lat, int64_t nsweeps);
+}  // namespace mcx

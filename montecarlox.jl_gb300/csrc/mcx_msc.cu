@@ -1,0 +1,208 @@
+// mcx_msc.cu -- multi-spin-coded (MSC64) Ising sweeps: 64 same-colour sites per
+// uint64 word (bit b of word w of a colour row <-> entry k = 64w + b of the int8
+// colour-split layout; bit set = spin up).  Neighbour counts are formed for 64
+// sites at once with bit-sliced adders; every site still draws its own Philox word,
+// so results are bit-identical to the int8 kernels.
+#include "mcx_device.cuh"
+#include "mcx_internal.h"
+
+namespace mcx {
+
+struct MscArgs {
+    unsigned long long* cur;
+    const unsigned long long* oth;
+    int nw;  // words per row
+    int W, Ly, Lz, rows, colour;
+    uint32_t k0, k1, stream;
+    unsigned long long sweep;
+    unsigned long long* dst[2];
+    unsigned long long* acc;
+    unsigned long long thr[14];
+};
+
+__global__ void k_msc_pack(const int8_t* __restrict__ col, unsigned long long* __restrict__ msc,
+                           long long nwords) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nwords;
+         q += (long long)gridDim.x * blockDim.x) {
+        const uint4* p = reinterpret_cast<const uint4*>(col + q * 64);
+        unsigned long long word = 0;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const uint4 x = p[v];
+            const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    if (((xs[i] >> (8 * b)) & 0xFF) == 1) word |= 1ull << (16 * v + 4 * i + b);
+        }
+        msc[q] = word;
+    }
+}
+
+__global__ void k_msc_unpack(int8_t* __restrict__ col, const unsigned long long* __restrict__ msc,
+                             long long nwords) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nwords;
+         q += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long word = msc[q];
+        uint4* p = reinterpret_cast<uint4*>(col + q * 64);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            uint32_t xs[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                uint32_t x = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    x |= ((word >> (16 * v + 4 * i + b)) & 1ull ? 0x01u : 0xFFu) << (8 * b);
+                xs[i] = x;
+            }
+            p[v] = make_uint4(xs[0], xs[1], xs[2], xs[3]);
+        }
+    }
+}
+
+// Bit-sliced count of set bits over Z words: (b0, b1, b2) with n = b0 + 2 b1 + 4 b2.
+template <int Z>
+__device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], unsigned long long& b0,
+                                           unsigned long long& b1, unsigned long long& b2) {
+    b0 = 0; b1 = 0; b2 = 0;
+#pragma unroll
+    for (int d = 0; d < Z; ++d) {
+        const unsigned long long c0 = b0 & x[d];
+        b0 ^= x[d];
+        const unsigned long long c1 = b1 & c0;
+        b1 ^= c0;
+        b2 ^= c1;  // n <= 6 never overflows three bits
+    }
+}
+
+template <int DIM, bool HB>
+__global__ void __launch_bounds__(256) k_msc_cb(const MscArgs a) {
+    constexpr int Z = 2 * DIM;
+    constexpr int NT = 2 * (Z + 1);
+    __shared__ unsigned long long s_thr[NT];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
+    __syncthreads();
+    const long long nwords = (long long)a.nw * a.rows;
+    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
+    int nacc = 0, asum = 0, nup = 0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nwords;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(g / a.nw);
+        const int w = (int)(g - (long long)r * a.nw);
+        const int y = r % a.Ly, z = r / a.Ly;
+        const int p = (y + z + a.colour) & 1;
+        const long long ryp = (y + 1 == a.Ly ? 0 : y + 1) + (long long)a.Ly * z;
+        const long long rym = (y == 0 ? a.Ly - 1 : y - 1) + (long long)a.Ly * z;
+        unsigned long long nb[Z];
+        const unsigned long long mid = a.oth[g];
+        nb[0] = mid;
+        nb[1] = a.oth[ryp * a.nw + w];
+        nb[2] = a.oth[rym * a.nw + w];
+        if (p == 0) {
+            const unsigned long long prev = a.oth[(long long)r * a.nw + (w == 0 ? a.nw - 1 : w - 1)];
+            nb[3] = (mid << 1) | (prev >> 63);
+        } else {
+            const unsigned long long next = a.oth[(long long)r * a.nw + (w == a.nw - 1 ? 0 : w + 1)];
+            nb[3] = (mid >> 1) | (next << 63);
+        }
+        if constexpr (DIM == 3) {
+            const long long rzp = y + (long long)a.Ly * (z + 1 == a.Lz ? 0 : z + 1);
+            const long long rzm = y + (long long)a.Ly * (z == 0 ? a.Lz - 1 : z - 1);
+            nb[4] = a.oth[rzp * a.nw + w];
+            nb[5] = a.oth[rzm * a.nw + w];
+        }
+        unsigned long long b0, b1, b2;
+        count_bits<Z>(nb, b0, b1, b2);
+        const unsigned long long own = a.cur[g];
+        unsigned long long fm = 0;
+        const uint32_t cbase = (uint32_t)(((unsigned long long)r * a.W + 64ull * w) >> 2);
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+            const uint4 rnd = philox10(make_uint4(cbase + q, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int bit = 4 * q + b;
+                const int n = (int)((b0 >> bit) & 1) + 2 * (int)((b1 >> bit) & 1) + 4 * (int)((b2 >> bit) & 1);
+                const int up = (int)((own >> bit) & 1);
+                const int al = up ? n : Z - n;
+                uint32_t u = b == 0 ? rnd.x : b == 1 ? rnd.y : b == 2 ? rnd.z : rnd.w;
+                if (HB && up) u = ~u;
+                if ((unsigned long long)u < s_thr[al + (Z + 1) * up]) {
+                    fm |= 1ull << bit;
+                    ++nacc;
+                    asum += al;
+                    nup += up;
+                }
+            }
+        }
+        a.cur[g] = own ^ fm;
+    }
+    long long v[3] = {2ll * Z * nacc - 4ll * asum, 2ll * nacc - 4ll * nup, (long long)nacc};
+    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
+    block_add_atomic<3>(v, dst);
+}
+
+static int grid_cap(const mcx_ctx* ctx, long long work) {
+    long long g = (work + 255) / 256;
+    const long long cap = (long long)ctx->num_sms * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+mcx_status msc_pack(mcx_lattice* lat) {
+    mcx_ctx* ctx = lat->ctx;
+    const long long nwords = lat->N / 2 / 64;
+    for (int c = 0; c < 2; ++c)
+        k_msc_pack<<<grid_cap(ctx, nwords), 256, 0, ctx->stream>>>(lat->d_col[c], lat->d_msc[c], nwords);
+    count_launch(ctx, 2);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+mcx_status msc_unpack(mcx_lattice* lat) {
+    mcx_ctx* ctx = lat->ctx;
+    const long long nwords = lat->N / 2 / 64;
+    for (int c = 0; c < 2; ++c)
+        k_msc_unpack<<<grid_cap(ctx, nwords), 256, 0, ctx->stream>>>(lat->d_col[c], lat->d_msc[c], nwords);
+    count_launch(ctx, 2);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
+                     int64_t nsweeps) {
+    mcx_ctx* ctx = lat->ctx;
+    MscArgs a;
+    a.nw = (int)(lat->W / 64);
+    a.W = (int)lat->W;
+    a.Ly = (int)lat->L[1];
+    a.Lz = (int)lat->L[2];
+    a.rows = (int)lat->rows;
+    a.k0 = (uint32_t)rng->seed;
+    a.k1 = (uint32_t)(rng->seed >> 32);
+    a.stream = rng->stream;
+    a.acc = lat->d_acc;
+    for (int i = 0; i < t.n && i < 14; ++i) a.thr[i] = t.thr[i];
+    const bool hb = alg == MCX_HEATBATH;
+    void (*fn)(const MscArgs) = lat->dim == 2 ? (hb ? k_msc_cb<2, true> : k_msc_cb<2, false>)
+                                              : (hb ? k_msc_cb<3, true> : k_msc_cb<3, false>);
+    const int grid = grid_cap(ctx, (long long)a.nw * a.rows);
+    for (int64_t s = 0; s < nsweeps; ++s) {
+        a.sweep = rng->counter + (uint64_t)s;
+        for (int c = 0; c < 2; ++c) {
+            a.colour = c;
+            a.cur = lat->d_msc[c];
+            a.oth = lat->d_msc[1 - c];
+            a.dst[0] = (unsigned long long*)(lat->d_series + 3 * s);
+            a.dst[1] = (unsigned long long*)(lat->d_series + 3 * s + 1);
+            fn<<<grid, 256, 0, ctx->stream>>>(a);
+        }
+    }
+    count_launch(ctx, 2 * (uint64_t)nsweeps);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+}  // namespace mcx

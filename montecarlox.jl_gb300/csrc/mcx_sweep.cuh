@@ -1,0 +1,29 @@
+// mcx_sweep.cuh -- launch arguments of the checkerboard half-sweep kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "mcx_internal.h"
+
+namespace mcx {
+
+struct SweepArgs {
+    int8_t* cur;        // colour being updated
+    const int8_t* oth;  // the other colour
+    int W, Ly, Lz, rows, colour;
+    uint32_t k0, k1, stream;
+    unsigned long long sweep;
+    unsigned long long* dst[3];  // this sweep's (pair, spin, spin2) delta slots
+    unsigned long long* acc;     // accepted-move counter
+    unsigned long long thr[kMaxTable];
+};
+
+using HalfSweepFn = void (*)(const SweepArgs);
+
+HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V);
+int vec_width(int64_t W);
+int half_sweep_grid(const mcx_ctx* ctx, int64_t W, int64_t rows, int V);
+mcx_status build_table(const mcx_lattice* lat, mcx_algorithm alg, double beta, Table* t);
+void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const mcx_rng* rng);
+
+}  // namespace mcx

@@ -1,0 +1,412 @@
+"""Host-side mirror of the MonteCarloX.jl / SpinSystems API for the GB300 path.
+
+Every compute call goes through the C ABI of ``libmcx_cuda.so`` (``include/mcx.h``);
+there is no CPU fallback.  Names follow the reference with Julia's ``!`` written as
+a trailing underscore (``init!`` -> ``init_``, ``spin_flip!`` -> ``spin_flip_``).
+
+Reference API mirrored here (paths inside MonteCarloX.jl):
+  BoltzmannEnsemble           src/ensembles/boltzmann.jl:7-30
+  Metropolis / Glauber        src/algorithms/metropolis.jl:173-237
+  HeatBath                    src/algorithms/heat_bath.jl:11-17
+  acceptance_rate / reset!    src/algorithms/importance_sampling.jl:95-110
+  Ising / IsingLatticeOptim   SpinSystems/src/ising.jl:523-571
+  BlumeCapel                  SpinSystems/src/blume_capel.jl:500-511
+  init! / energy / magnetization  ising.jl:127-188, blume_capel.jl:18-109
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = [
+    "MCXError", "ArgumentError", "BoundsError", "OutOfMemoryError", "BudgetError", "DeviceTimeoutError",
+    "CudaError", "Context", "default_context", "Philox", "BoltzmannEnsemble", "logweight", "Metropolis",
+    "Glauber", "HeatBath", "ensemble", "acceptance_rate", "reset_", "AbstractSystem", "AbstractSpinSystem",
+    "Ising", "IsingLatticeOptim", "BlumeCapel", "init_", "energy", "magnetization", "observables",
+    "sweep_", "spin_flip_", "set_spins_", "logistic",
+]
+
+
+# --------------------------------------------------------------------- errors --
+class MCXError(RuntimeError):
+    status = None
+
+
+class ArgumentError(MCXError, ValueError):
+    status = L.MCX_ERR_INVALID_ARG
+
+
+class BoundsError(MCXError, IndexError):
+    """An energy left the histogram range (the reference's BoundsError)."""
+    status = L.MCX_ERR_OUT_OF_RANGE
+
+
+class OutOfMemoryError(MCXError, MemoryError):
+    status = L.MCX_ERR_OOM
+
+
+class BudgetError(MCXError):
+    status = L.MCX_ERR_BUDGET
+
+
+class DeviceTimeoutError(MCXError, TimeoutError):
+    status = L.MCX_ERR_TIMEOUT
+
+
+class CudaError(MCXError):
+    status = L.MCX_ERR_CUDA
+
+
+class NotReadyError(MCXError):
+    status = L.MCX_ERR_NOT_READY
+
+
+class NotFoundError(MCXError, KeyError):
+    status = L.MCX_ERR_NOT_FOUND
+
+
+_ERRORS = {e.status: e for e in (ArgumentError, BoundsError, OutOfMemoryError, BudgetError,
+                                 DeviceTimeoutError, CudaError, NotReadyError, NotFoundError)}
+
+
+def _check(status):
+    if status != L.MCX_OK:
+        raise _ERRORS.get(status, MCXError)("%s: %s" % (L.load().mcx_status_string(status).decode(),
+                                                        L.error_string()))
+
+
+# -------------------------------------------------------------------- context --
+class Context:
+    """One CUDA stream plus the device memory owned through it (mcx_ctx)."""
+
+    def __init__(self, device=0, stream=None, hbm_budget=0):
+        lib = L.load()
+        cfg = L.mcx_config(int(device), C.c_void_p(int(stream) if stream else 0), int(hbm_budget))
+        h = C.c_void_p()
+        _check(lib.mcx_ctx_create(C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def sync(self):
+        _check(L.load().mcx_sync(self.handle))
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(L.load().mcx_ctx_stream(self.handle, C.byref(s)))
+        return s.value or 0
+
+    def memory(self):
+        used, budget = C.c_uint64(), C.c_uint64()
+        _check(L.load().mcx_ctx_memory(self.handle, C.byref(used), C.byref(budget)))
+        return used.value, budget.value
+
+    def launches(self) -> int:
+        n = C.c_uint64()
+        _check(L.load().mcx_ctx_launches(self.handle, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.load().mcx_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context()
+    return _default_ctx
+
+
+# ------------------------------------------------------------------------ rng --
+class Philox:
+    """Counter-based Philox4x32-10 stream: (seed, stream) key, counter = next sweep.
+
+    Plays the role of the ``rng`` objects (Xoshiro / MersenneTwister) the reference
+    algorithms carry; the counter advances by the number of sweeps run, so a run
+    can be resumed or replayed exactly."""
+
+    def __init__(self, seed=0, stream=0, counter=0):
+        self.seed = int(seed) & (2 ** 64 - 1)
+        self.stream = int(stream) & 0xFFFFFFFF
+        self.counter = int(counter)
+
+    def _c(self):
+        return L.mcx_rng(self.seed, self.counter, self.stream, 0)
+
+    def __repr__(self):
+        return "Philox(seed=%d, stream=%d, counter=%d)" % (self.seed, self.stream, self.counter)
+
+
+# ------------------------------------------------------------------ ensembles --
+def logistic(x):
+    """src/infrastructure/utils.jl:82-88"""
+    if x >= 0:
+        return 1.0 / (1.0 + math.exp(-x))
+    ex = math.exp(x)
+    return ex / (1.0 + ex)
+
+
+class BoltzmannEnsemble:
+    """logweight(E) = -beta*E; exactly one of beta / β / T (src/ensembles/boltzmann.jl:7-22)."""
+
+    def __init__(self, *, beta=None, T=None, **kw):
+        b2 = kw.pop("β", None)
+        if kw:
+            raise TypeError("unexpected keyword(s) %s" % list(kw))
+        if beta is not None and b2 is not None:
+            raise ArgumentError("Specify only one of `beta` or `β`")
+        b = beta if beta is not None else b2
+        if (b is None) == (T is None):
+            raise ArgumentError("Specify exactly one of `beta`/`β` or `T`")
+        self.beta = b if b is not None else 1.0 / T
+
+    def logweight(self, E):
+        return -self.beta * E
+
+    def __call__(self, E):
+        return self.logweight(E)
+
+    def __eq__(self, other):
+        return type(other) is type(self) and other.beta == self.beta
+
+
+def logweight(ens, x=None):
+    f = ens.logweight if hasattr(ens, "logweight") else ens
+    return f if x is None else f(x)
+
+
+# ----------------------------------------------------------------- algorithms --
+class _ImportanceSampling:
+    ALG = None
+
+    def __init__(self, rng, ensemble=None, *, beta=None, **kw):
+        b2 = kw.pop("β", None)
+        if kw:
+            raise TypeError("unexpected keyword(s) %s" % list(kw))
+        if ensemble is None:
+            if beta is None and b2 is None:
+                raise ArgumentError("give an ensemble or beta")
+            ensemble = BoltzmannEnsemble(beta=beta if beta is not None else b2)
+        self.rng = rng if isinstance(rng, Philox) else Philox(rng)
+        self.ensemble = ensemble
+        self.steps = 0
+        self.accepted = 0
+
+    @property
+    def beta(self):
+        return self.ensemble.beta
+
+
+class Metropolis(_ImportanceSampling):
+    """Metropolis(rng; β) -- accept iff lr > 0 || U < exp(lr)."""
+    ALG = L.METROPOLIS
+
+
+class Glauber(_ImportanceSampling):
+    """Glauber(rng; β) -- accept iff U < logistic(lr)."""
+    ALG = L.GLAUBER
+
+
+class HeatBath:
+    """HeatBath(rng; β): fields rng, β (as ``beta``), steps (src/algorithms/heat_bath.jl:11-17).
+
+    ``flips`` counts state changes, which the reference does not keep."""
+    ALG = L.HEATBATH
+
+    def __init__(self, rng, *, beta=None, **kw):
+        b2 = kw.pop("β", None)
+        if kw:
+            raise TypeError("unexpected keyword(s) %s" % list(kw))
+        b = beta if beta is not None else b2
+        if b is None:
+            raise ArgumentError("HeatBath needs β")
+        self.rng = rng if isinstance(rng, Philox) else Philox(rng)
+        self.beta = b
+        self.steps = 0
+        self.flips = 0
+
+
+def ensemble(alg):
+    return alg.ensemble
+
+
+def acceptance_rate(alg):
+    """accepted/steps, 0.0 before the first step (importance_sampling.jl:95-96)."""
+    return alg.accepted / alg.steps if alg.steps > 0 else 0.0
+
+
+def reset_(alg):
+    """Zero the step / acceptance counters (importance_sampling.jl:106-110)."""
+    alg.steps = 0
+    if hasattr(alg, "accepted"):
+        alg.accepted = 0
+    if hasattr(alg, "flips"):
+        alg.flips = 0
+    if hasattr(alg, "_reset_hook"):
+        alg._reset_hook()
+
+
+# -------------------------------------------------------------------- systems --
+class AbstractSystem:
+    pass
+
+
+class AbstractSpinSystem(AbstractSystem):
+    pass
+
+
+class DeviceLattice(AbstractSpinSystem):
+    MODEL = None
+    STATES = ()
+
+    def __init__(self, dims, *, J=1, D=0, h=0, periodic=True, layout="int8", ctx=None):
+        if not periodic:
+            raise ArgumentError("the device lattices are periodic")
+        if not isinstance(h, (int, float)):
+            raise ArgumentError("the device lattices take a uniform field h")
+        self.ctx = ctx or default_context()
+        self.dims = [int(d) for d in dims]
+        self.J, self.D, self.h = J, D, h
+        self.layout = layout
+        lay = {"int8": L.LAYOUT_INT8, "msc64": L.LAYOUT_MSC64}[layout]
+        Ls = (C.c_int32 * 3)(*(self.dims + [1] * (3 - len(self.dims))))
+        hdl = C.c_void_p()
+        _check(L.load().mcx_lattice_create(self.ctx.handle, self.MODEL, len(self.dims), Ls, lay, float(J),
+                                           float(D), float(h), C.byref(hdl)))
+        self.handle = hdl
+        self.N = int(np.prod(self.dims))
+
+    def __len__(self):
+        return self.N
+
+    @property
+    def spins(self):
+        """Copy of the spins in SpinSystems linear order (int8)."""
+        out = np.empty(self.N, np.int8)
+        _check(L.load().mcx_get_spins(self.handle, out.ctypes.data, self.N))
+        return out
+
+    @spins.setter
+    def spins(self, values):
+        set_spins_(self, values)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.load().mcx_lattice_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class IsingDevice(DeviceLattice):
+    MODEL = L.ISING
+    STATES = (-1, 1)
+
+
+class BlumeCapelDevice(DeviceLattice):
+    MODEL = L.BLUME_CAPEL
+    STATES = (-1, 0, 1)
+
+
+def Ising(dims, *, J=1, periodic=True, h=0, layout="int8", ctx=None):
+    """Ising(dims; J=1, periodic=true, h=0): all spins up (SpinSystems/src/ising.jl:523-534)."""
+    return IsingDevice(dims, J=J, h=h, periodic=periodic, layout=layout, ctx=ctx)
+
+
+def IsingLatticeOptim(Lx, Ly, *, layout="int8", ctx=None):
+    """2-D periodic J=1 Ising (SpinSystems/src/ising.jl:550-571)."""
+    return IsingDevice([Lx, Ly], J=1, h=0, layout=layout, ctx=ctx)
+
+
+def BlumeCapel(dims, *, J=1, D=0, periodic=True, h=0, ctx=None):
+    """BlumeCapel(dims; J=1, D=0, periodic=true, h=0) (SpinSystems/src/blume_capel.jl:500-511)."""
+    return BlumeCapelDevice(dims, J=J, D=D, h=h, periodic=periodic, ctx=ctx)
+
+
+def set_spins_(sys, values):
+    arr = np.ascontiguousarray(values, dtype=np.int8).reshape(-1)
+    if arr.size != sys.N:
+        raise ArgumentError("expected %d spins, got %d" % (sys.N, arr.size))
+    _check(L.load().mcx_set_spins(sys.handle, arr.ctypes.data, sys.N))
+
+
+def init_(sys, type, rng=None):
+    """init!(sys, :up | :down | :zero | :random; rng)."""
+    t = type.lstrip(":") if isinstance(type, str) else type
+    if t == "random":
+        if rng is None:
+            raise ArgumentError("Random initialization requires rng")
+        r = rng if isinstance(rng, Philox) else Philox(rng)
+        _check(L.load().mcx_init_random(sys.handle, r.seed, r.stream))
+    elif t in ("up", "down", "zero"):
+        v = {"up": 1, "down": -1, "zero": 0}[t]
+        if v not in sys.STATES:
+            raise ArgumentError("Unknown initialization type: %s" % type)
+        _check(L.load().mcx_init_uniform(sys.handle, v))
+    else:
+        raise ArgumentError("Unknown initialization type: %s" % type)
+    return sys
+
+
+def observables(sys, full=False):
+    """(pair_sum, spin_sum, spin2_sum); ``full=True`` recomputes them from the spins."""
+    P, M, Q = C.c_int64(), C.c_int64(), C.c_int64()
+    fn = L.load().mcx_recompute_observables if full else L.load().mcx_observables
+    _check(fn(sys.handle, C.byref(P), C.byref(M), C.byref(Q)))
+    return P.value, M.value, Q.value
+
+
+def energy(sys, full=False):
+    """energy(sys; full): -J*pair - h*M (+ D*sum s^2 for Blume-Capel)."""
+    P, M, Q = observables(sys, full)
+    E = (-(sys.J * P)) - (sys.h * M)
+    if isinstance(sys, BlumeCapelDevice):
+        E = E + sys.D * Q
+    return E
+
+
+def magnetization(sys, full=False):
+    return observables(sys, full)[1]
+
+
+def sweep_(sys, alg, nsweeps=1, record=False):
+    """``nsweeps`` checkerboard sweeps (N spin_flip! attempts each) on the device.
+
+    Updates ``alg.steps`` / ``alg.accepted`` (HeatBath: ``steps``, ``flips``) and the
+    rng counter.  With ``record=True`` returns the per-sweep (pair, spin, spin2) series
+    as an int64 array of shape (nsweeps, 3)."""
+    beta = alg.beta
+    rng = alg.rng._c()
+    cnt = L.mcx_counters(0, 0)
+    obs = np.zeros((nsweeps, 3), np.int64) if record else None
+    _check(L.load().mcx_sweep(sys.handle, alg.ALG, float(beta), C.byref(rng), int(nsweeps),
+                              obs.ctypes.data if record else None, C.byref(cnt)))
+    alg.rng.counter = rng.counter
+    alg.steps += cnt.attempts
+    if isinstance(alg, HeatBath):
+        alg.flips += cnt.accepted
+    else:
+        alg.accepted += cnt.accepted
+    return obs
+
+
+def spin_flip_(sys, alg):
+    """Single random-site updates are not run on the device; use sweep_ (checkerboard)."""
+    raise NotImplementedError("spin_flip_ on a device lattice: use sweep_(sys, alg, n)")

@@ -1,0 +1,98 @@
+"""ctypes binding of libmcx_cuda (the C ABI declared in include/mcx.h).
+
+The library is built in-tree by ``montecarlox.jl_gb300/build.py``.  There is no
+CPU fallback: if the shared library is missing, importing any compute entry point
+raises.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libmcx_cuda.so")
+
+MCX_OK = 0
+MCX_ERR_INVALID_ARG = 1
+MCX_ERR_OUT_OF_RANGE = 2
+MCX_ERR_OOM = 3
+MCX_ERR_BUDGET = 4
+MCX_ERR_TIMEOUT = 5
+MCX_ERR_CUDA = 6
+MCX_ERR_NOT_READY = 7
+MCX_ERR_NOT_FOUND = 8
+
+ISING, BLUME_CAPEL = 0, 1
+METROPOLIS, GLAUBER, HEATBATH = 0, 1, 2
+LAYOUT_INT8, LAYOUT_MSC64 = 0, 1
+MUCA, WANG_LANDAU = 0, 1
+
+
+class mcx_config(C.Structure):
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("hbm_budget", C.c_uint64)]
+
+
+class mcx_rng(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("counter", C.c_uint64), ("stream", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class mcx_counters(C.Structure):
+    _fields_ = [("attempts", C.c_uint64), ("accepted", C.c_uint64)]
+
+
+_P = C.c_void_p
+_i64p = C.POINTER(C.c_int64)
+_u64p = C.POINTER(C.c_uint64)
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "mcx_status_string": (C.c_char_p, [C.c_int]),
+    "mcx_last_error_string": (C.c_char_p, []),
+    "mcx_version": (C.c_int, []),
+    "mcx_ctx_create": (C.c_int, [C.POINTER(mcx_config), C.POINTER(_P)]),
+    "mcx_ctx_destroy": (C.c_int, [_P]),
+    "mcx_sync": (C.c_int, [_P]),
+    "mcx_ctx_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "mcx_ctx_memory": (C.c_int, [_P, _u64p, _u64p]),
+    "mcx_ctx_launches": (C.c_int, [_P, _u64p]),
+    "mcx_lattice_create": (C.c_int, [_P, C.c_int, C.c_int, _i32p, C.c_int, C.c_double, C.c_double,
+                                     C.c_double, C.POINTER(_P)]),
+    "mcx_lattice_destroy": (C.c_int, [_P]),
+    "mcx_lattice_info": (C.c_int, [_P, _i64p, _i64p]),
+    "mcx_set_spins": (C.c_int, [_P, _P, C.c_size_t]),
+    "mcx_get_spins": (C.c_int, [_P, _P, C.c_size_t]),
+    "mcx_init_random": (C.c_int, [_P, C.c_uint64, C.c_uint32]),
+    "mcx_init_uniform": (C.c_int, [_P, C.c_int8]),
+    "mcx_observables": (C.c_int, [_P, _i64p, _i64p, _i64p]),
+    "mcx_recompute_observables": (C.c_int, [_P, _i64p, _i64p, _i64p]),
+    "mcx_energy": (C.c_int, [_P, _f64p, _i64p]),
+    "mcx_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P,
+                            C.POINTER(mcx_counters)]),
+    "mcx_read_series": (C.c_int, [_P, _P, C.c_int64]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libmcx_cuda.so; raises OSError (no fallback) when it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("libmcx_cuda.so not found at %s: build it with montecarlox.jl_gb300/build.py "
+                      "(there is no CPU fallback)" % path)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def error_string() -> str:
+    return load().mcx_last_error_string().decode(errors="replace")

@@ -1,0 +1,181 @@
+"""CPU oracle for the spin-flip hot path -- TEST INFRASTRUCTURE ONLY.
+
+The C restatement in ``mcx_oracle.c`` is the checker for the CUDA library.  Only
+``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+may import this package.  The product library never calls it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ISING, BC = 0, 1
+METROPOLIS, GLAUBER, HEATBATH = 0, 1, 2
+MUCA, WL = 0, 1
+OK, ERR_INVALID, ERR_RANGE = 0, 1, 2
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags="C")
+        u64p = np.ctypeslib.ndpointer(np.uint64, flags="C")
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
+        i8p = np.ctypeslib.ndpointer(np.int8, flags="C")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
+        u8p = np.ctypeslib.ndpointer(np.uint8, flags="C")
+        L.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        L.orc_site_word.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_int, C.c_uint64]
+        L.orc_site_word.restype = C.c_uint32
+        L.orc_log.argtypes = [C.c_double]
+        L.orc_log.restype = C.c_double
+        L.orc_table_ising.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, u64p, u32p]
+        L.orc_table_bc.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, u64p]
+        L.orc_init_random.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_uint64, C.c_uint32]
+        L.orc_init_random.restype = None
+        L.orc_observables.argtypes = [i8p, C.c_int, i32p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]
+        L.orc_observables.restype = None
+        L.orc_cb_sweep.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64, C.c_void_p,
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_seq_attempts.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_flathist_sweep.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_double, C.c_double, C.c_double,
+                                         C.c_int, f64p, i64p, C.c_int64, C.c_int64, C.c_int64, C.c_double,
+                                         C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64, C.c_void_p,
+                                         C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_muca_update.argtypes = [f64p, i64p, C.c_int64]
+        L.orc_muca_update.restype = None
+        L.orc_wl_flat.argtypes = [i64p, u8p, C.c_int64, C.c_double, C.POINTER(C.c_double)]
+        L.orc_pt_exchange.argtypes = [C.c_int, f64p, i32p, C.POINTER(C.c_int32), f64p, C.c_uint64,
+                                      C.c_uint32, C.c_uint64, u64p, u64p]
+        L.orc_bench_seq.argtypes = [C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_uint64, C.c_int, C.c_int64, C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def _dims(L):
+    L = [int(v) for v in L]
+    return len(L), np.array(L + [1] * (3 - len(L)), dtype=np.int32)
+
+
+def philox(ctr, key):
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(np.asarray(ctr, np.uint32), np.asarray(key, np.uint32), out)
+    return out
+
+
+def site_word(seed, stream, sweep, colour, purpose, site):
+    return int(lib().orc_site_word(seed, stream, sweep, colour, purpose, site))
+
+
+def log(x):
+    return float(lib().orc_log(float(x)))
+
+
+def table_ising(dim, alg, beta, J=1.0, h=0.0):
+    n = 2 * (2 * dim + 1)
+    thr = np.zeros(n, np.uint64)
+    xm = np.zeros(n, np.uint32)
+    rc = lib().orc_table_ising(dim, alg, beta, J, h, thr, xm)
+    assert rc == OK
+    return thr, xm
+
+
+def table_bc(dim, alg, beta, J=1.0, D=1.0, h=0.0):
+    n = 3 * 2 * (4 * dim + 1)
+    thr = np.zeros(n, np.uint64)
+    rc = lib().orc_table_bc(dim, alg, beta, J, D, h, thr)
+    assert rc == OK
+    return thr
+
+
+def init_random(model, L, seed, stream=0):
+    dim, Lv = _dims(L)
+    s = np.zeros(int(np.prod(L)), np.int8)
+    lib().orc_init_random(s, model, dim, Lv, seed, stream)
+    return s
+
+
+def observables(s, L):
+    dim, Lv = _dims(L)
+    P, M, Q = C.c_int64(), C.c_int64(), C.c_int64()
+    lib().orc_observables(np.ascontiguousarray(s, np.int8), dim, Lv, C.byref(P), C.byref(M), C.byref(Q))
+    return P.value, M.value, Q.value
+
+
+def cb_sweep(s, model, L, alg, beta, seed, stream=0, sweep0=0, nsweeps=1, J=1.0, D=0.0, h=0.0,
+             record=True):
+    """Checkerboard sweeps in place on ``s``; returns (obs[nsweeps,3] or None, attempts, accepts)."""
+    dim, Lv = _dims(L)
+    obs = np.zeros((nsweeps, 3), np.int64) if record else None
+    att, acc = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_cb_sweep(s, model, dim, Lv, alg, beta, J, D, h, seed, stream, sweep0, nsweeps,
+                            obs.ctypes.data if record else None, C.byref(att), C.byref(acc))
+    if rc != OK:
+        raise ValueError("oracle cb_sweep failed: %d" % rc)
+    return obs, att.value, acc.value
+
+
+def seq_attempts(s, model, L, alg, beta, seed, stream=0, attempt0=0, nattempts=1, J=1.0, D=0.0, h=0.0):
+    dim, Lv = _dims(L)
+    st, ac = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_seq_attempts(s, model, dim, Lv, alg, beta, J, D, h, seed, stream, attempt0, nattempts,
+                                C.byref(st), C.byref(ac))
+    if rc != OK:
+        raise ValueError("oracle seq_attempts failed: %d" % rc)
+    return st.value, ac.value
+
+
+def flathist_sweep(s, model, L, mode, lnw, H, start, step, logf, seed, stream=0, sweep0=0, nsweeps=1,
+                   J=1.0, D=0.0, h=0.0, record=True):
+    """Returns (rc, obs, steps, accepted); lnw/H/s are updated in place."""
+    dim, Lv = _dims(L)
+    obs = np.zeros((nsweeps, 3), np.int64) if record else None
+    st, ac = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_flathist_sweep(s, model, dim, Lv, J, D, h, mode, lnw, H, start, step, len(lnw), logf,
+                                  seed, stream, sweep0, nsweeps, obs.ctypes.data if record else None,
+                                  C.byref(st), C.byref(ac))
+    return rc, obs, st.value, ac.value
+
+
+def muca_update(lnw, H):
+    lib().orc_muca_update(lnw, H, len(lnw))
+
+
+def wl_flat(H, visited, flatness):
+    r = C.c_double(0)
+    f = lib().orc_wl_flat(np.ascontiguousarray(H, np.int64), np.ascontiguousarray(visited, np.uint8), len(H),
+                          flatness, C.byref(r))
+    return bool(f), r.value
+
+
+def pt_exchange(betas, pos, stage, x, seed, ladder, t, steps, accepted):
+    """One exchange stage; ``pos``, ``steps``, ``accepted`` update in place; returns the new stage."""
+    st = C.c_int32(stage)
+    rc = lib().orc_pt_exchange(len(betas), np.ascontiguousarray(betas, np.float64), pos, C.byref(st),
+                               np.ascontiguousarray(x, np.float64), seed, ladder, t, steps, accepted)
+    assert rc == OK
+    return st.value
+
+
+def bench_seq(model, L, alg, beta, seed, nthreads, attempts_per_thread, J=1.0, D=0.0, h=0.0):
+    dim, Lv = _dims(L)
+    sec = C.c_double(0)
+    rc = lib().orc_bench_seq(model, dim, Lv, alg, beta, J, D, h, seed, nthreads, attempts_per_thread,
+                             C.byref(sec))
+    assert rc == OK
+    return sec.value
+
+
+__all__ = [n for n in dir() if not n.startswith("_")]

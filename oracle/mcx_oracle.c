@@ -1,0 +1,628 @@
+/*
+ * mcx_oracle.c -- CPU oracle for the spin-flip hot path (TEST INFRASTRUCTURE ONLY).
+ *
+ * Restates, in plain C, the MonteCarloX.jl / SpinSystems algorithms that the CUDA
+ * library accelerates.  Used only as the checker by the tests, smoke() and the
+ * CPU-baseline leg of bench.py.  Compile with -ffp-contract=off: every FP64
+ * decision must be evaluated with exactly the operations written here.
+ *
+ * Reference citations are paths inside the MonteCarloX.jl repository.
+ */
+#include "mcx_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* Philox purposes (counter word 2, bits 24..31) */
+enum { P_ACCEPT = 0, P_PROPOSE = 1, P_LOW = 2, P_INIT = 3, P_EXCHANGE = 4, P_SEQ = 5, P_SEQ2 = 6 };
+
+/* ---------------------------------------------------------------------------
+ * Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
+ * SC'11): 10 rounds of two 32x32->64 multiplies with a Weyl key schedule.
+ * ------------------------------------------------------------------------- */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* The checkerboard stream: key = seed, counter = (site>>3, sweep lo, sweep hi16 |
+ * colour<<16 | purpose<<24, stream); the site takes word (site>>1)&3.  Eight
+ * consecutive linear sites hold four sites of each colour, so one call feeds four
+ * same-colour sites. */
+uint32_t orc_site_word(uint64_t seed, uint32_t stream, uint64_t sweep, int colour,
+                       int purpose, uint64_t site) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t ctr[4] = {(uint32_t)(site >> 3), (uint32_t)sweep,
+                       ((uint32_t)(sweep >> 32) & 0xFFFFu) | ((uint32_t)colour << 16) |
+                           ((uint32_t)purpose << 24),
+                       stream};
+    uint32_t out[4];
+    orc_philox4x32_10(ctr, key, out);
+    return out[(site >> 1) & 3];
+}
+
+static double u53(uint32_t hi, uint32_t lo) {
+    uint64_t k = ((uint64_t)hi << 21) | (uint64_t)(lo >> 11);
+    return (double)k * 0x1p-53;
+}
+
+/* ---------------------------------------------------------------------------
+ * log(x) from the series log(m) = 2 atanh(s), s = (m-1)/(m+1), after splitting
+ * x = 2^k m with m in [sqrt(1/2), sqrt(2)).  Plain multiplies and adds only.
+ * ------------------------------------------------------------------------- */
+double orc_log(double x) {
+    if (x != x) return x;
+    if (x < 0.0) return NAN;
+    if (x == 0.0) return -INFINITY;
+    if (x == INFINITY) return x;
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    int64_t k = 0;
+    if ((b >> 52) == 0) { /* subnormal: scale by 2^54 */
+        double y = x * 0x1p54;
+        memcpy(&b, &y, 8);
+        k = -54;
+    }
+    k += (int64_t)(b >> 52) - 1023;
+    uint64_t mb = (b & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull;
+    double m;
+    memcpy(&m, &mb, 8);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        k += 1;
+    }
+    double f = m - 1.0;
+    double s = f / (m + 1.0);
+    double s2 = s * s;
+    double p = 1.0 / 23.0;
+    p = p * s2 + 1.0 / 21.0;
+    p = p * s2 + 1.0 / 19.0;
+    p = p * s2 + 1.0 / 17.0;
+    p = p * s2 + 1.0 / 15.0;
+    p = p * s2 + 1.0 / 13.0;
+    p = p * s2 + 1.0 / 11.0;
+    p = p * s2 + 1.0 / 9.0;
+    p = p * s2 + 1.0 / 7.0;
+    p = p * s2 + 1.0 / 5.0;
+    p = p * s2 + 1.0 / 3.0;
+    double two_s = s + s;
+    double lm = two_s + two_s * (s2 * p);
+    double kd = (double)k;
+    const double ln2_hi = 6.93147180369123816490e-01; /* 0x3FE62E42FEE00000 */
+    const double ln2_lo = 1.90821492927058770002e-10; /* ln2 - ln2_hi */
+    return kd * ln2_hi + (lm + kd * ln2_lo);
+}
+
+/* logistic, src/infrastructure/utils.jl:82-88 */
+static double logistic(double x) {
+    if (x >= 0) return 1.0 / (1.0 + exp(-x));
+    double ex = exp(x);
+    return ex / (1.0 + ex);
+}
+
+static uint64_t prob_to_thr(double p) {
+    if (!(p > 0.0)) return 0;
+    if (p >= 1.0) return 1ull << 32;
+    double v = floor(p * 4294967296.0);
+    if (v >= 4294967296.0) return 1ull << 32;
+    return (uint64_t)v;
+}
+
+/* Metropolis rule, src/algorithms/metropolis.jl:124-127 and
+ * src/algorithms/importance_sampling.jl:80-85: accept iff lr > 0 || U < exp(lr),
+ * with lr = logweight(BoltzmannEnsemble, dE) = -beta*dE (src/ensembles/boltzmann.jl:28). */
+static uint64_t metropolis_thr(double beta, double dE) {
+    double lr = (-beta) * dE;
+    if (lr >= 0.0) return 1ull << 32;
+    return prob_to_thr(exp(lr));
+}
+
+/* Glauber rule, src/algorithms/metropolis.jl:231-237: accept iff U < logistic(lr). */
+static uint64_t glauber_thr(double beta, double dE) {
+    double lr = (-beta) * dE;
+    return prob_to_thr(logistic(lr));
+}
+
+/* Ising tables.  Entry idx = a + (2d+1)*up, a = number of neighbours aligned with the
+ * site, up = (s == +1).  A flip happens iff (u ^ xmask) < thr. */
+int orc_table_ising(int dim, int alg, double beta, double J, double h, uint64_t* thr,
+                    uint32_t* xmask) {
+    if (dim != 2 && dim != 3) return ORC_ERR_INVALID;
+    int z = 2 * dim;
+    for (int up = 0; up < 2; ++up) {
+        for (int a = 0; a <= z; ++a) {
+            int idx = a + (z + 1) * up;
+            double s = up ? 1.0 : -1.0;
+            double lpi = (double)(2 * a - z);            /* s_i * sum_j s_j  */
+            double dpair = ((-2.0) * J) * lpi;            /* ising.jl:297-301 */
+            double dspin = -2.0 * s;
+            double dE = (-dpair) - (h * dspin);           /* ising.jl:308     */
+            if (alg == ORC_METROPOLIS) {
+                thr[idx] = metropolis_thr(beta, dE);
+                xmask[idx] = 0;
+            } else if (alg == ORC_GLAUBER) {
+                thr[idx] = glauber_thr(beta, dE);
+                xmask[idx] = 0;
+            } else if (alg == ORC_HEATBATH) {
+                /* ising.jl:153-168: p_plus = logistic(beta*s_old*dE), s_new = U<p_plus ? +1:-1 */
+                uint64_t tp = prob_to_thr(logistic((beta * s) * dE));
+                if (up) { thr[idx] = (1ull << 32) - tp; xmask[idx] = 0xFFFFFFFFu; }
+                else    { thr[idx] = tp;                xmask[idx] = 0; }
+            } else {
+                return ORC_ERR_INVALID;
+            }
+        }
+    }
+    return ORC_OK;
+}
+
+/* _propose_state, SpinSystems/src/blume_capel.jl:21-30 */
+static int bc_propose(int s_old, int b) {
+    if (s_old == -1) return b ? 0 : 1;
+    if (s_old == 0) return b ? -1 : 1;
+    return b ? -1 : 0;
+}
+
+/* Blume-Capel tables.  Metropolis/Glauber: idx = (s_old+1)*2*(4d+1) + b*(4d+1) + (c+2d),
+ * accept iff u < thr.  HeatBath: per c two cumulative thresholds (T1, T12) at
+ * [2*(c+2d)], [2*(c+2d)+1]. */
+int orc_table_bc(int dim, int alg, double beta, double J, double D, double h, uint64_t* thr) {
+    if (dim != 2 && dim != 3) return ORC_ERR_INVALID;
+    int z = 2 * dim, nc = 2 * z + 1;
+    if (alg == ORC_HEATBATH) {
+        for (int c = -z; c <= z; ++c) {
+            /* blume_capel.jl:61-85 */
+            double coupling = J * (double)c;
+            double e1 = (coupling - (h * -1.0)) + D;
+            double e3 = ((-coupling) - (h * 1.0)) + D;
+            double w1 = exp((-beta) * e1);
+            double w2 = exp((-beta) * 0.0);
+            double w3 = exp((-beta) * e3);
+            double zz = (w1 + w2) + w3;
+            thr[2 * (c + z)] = prob_to_thr(w1 / zz);
+            thr[2 * (c + z) + 1] = prob_to_thr((w1 + w2) / zz);
+        }
+        return ORC_OK;
+    }
+    if (alg != ORC_METROPOLIS && alg != ORC_GLAUBER) return ORC_ERR_INVALID;
+    for (int so = -1; so <= 1; ++so)
+        for (int b = 0; b < 2; ++b)
+            for (int c = -z; c <= z; ++c) {
+                int sn = bc_propose(so, b);
+                double ds = (double)(sn - so);
+                double ds2 = (double)(sn * sn - so * so);
+                double dpair = ds * (J * (double)c);          /* blume_capel.jl:235-241 */
+                double dE = ((-dpair) - (h * ds)) + (D * ds2); /* blume_capel.jl:247-248 */
+                int idx = (so + 1) * 2 * nc + b * nc + (c + z);
+                thr[idx] = alg == ORC_METROPOLIS ? metropolis_thr(beta, dE) : glauber_thr(beta, dE);
+            }
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * geometry: SpinSystems linear order (Graphs.grid vertex order, first dim fastest),
+ * periodic, i = x + Lx*(y + Ly*z); colour = (x+y+z) & 1.
+ * ------------------------------------------------------------------------- */
+typedef struct { int dim; int64_t Lx, Ly, Lz, N; } geom_t;
+
+static int geom_init(geom_t* g, int dim, const int32_t* L) {
+    if (dim != 2 && dim != 3) return ORC_ERR_INVALID;
+    g->dim = dim;
+    g->Lx = L[0]; g->Ly = L[1]; g->Lz = dim == 3 ? L[2] : 1;
+    for (int d = 0; d < dim; ++d)
+        if (L[d] < 4 || (L[d] & 1)) return ORC_ERR_INVALID;
+    g->N = g->Lx * g->Ly * g->Lz;
+    return ORC_OK;
+}
+
+static inline int colour_of(const geom_t* g, int64_t i) {
+    int64_t x = i % g->Lx, y = (i / g->Lx) % g->Ly, z = i / (g->Lx * g->Ly);
+    return (int)((x + y + z) & 1);
+}
+
+static inline int nbr_sum(const geom_t* g, const int8_t* s, int64_t i) {
+    int64_t x = i % g->Lx, y = (i / g->Lx) % g->Ly, z = i / (g->Lx * g->Ly);
+    int64_t Lx = g->Lx, Ly = g->Ly, Lz = g->Lz;
+    int64_t base = i - x;
+    int acc = s[base + (x + 1) % Lx] + s[base + (x + Lx - 1) % Lx];
+    int64_t rowbase = i - y * Lx;
+    acc += s[rowbase + ((y + 1) % Ly) * Lx] + s[rowbase + ((y + Ly - 1) % Ly) * Lx];
+    if (g->dim == 3) {
+        int64_t plane = Lx * Ly, zb = i - z * plane;
+        acc += s[zb + ((z + 1) % Lz) * plane] + s[zb + ((z + Lz - 1) % Lz) * plane];
+    }
+    return acc;
+}
+
+void orc_observables(const int8_t* s, int dim, const int32_t* L, int64_t* P, int64_t* M,
+                     int64_t* Q) {
+    geom_t g;
+    if (geom_init(&g, dim, L)) { *P = *M = *Q = 0; return; }
+    int64_t p = 0, m = 0, q = 0;
+    for (int64_t i = 0; i < g.N; ++i) {
+        int64_t x = i % g.Lx, y = (i / g.Lx) % g.Ly, z = i / (g.Lx * g.Ly);
+        int si = s[i];
+        int64_t xp = i - x + (x + 1) % g.Lx;
+        int64_t yp = i - y * g.Lx + ((y + 1) % g.Ly) * g.Lx;
+        p += si * s[xp] + si * s[yp];
+        if (dim == 3) {
+            int64_t pl = g.Lx * g.Ly;
+            int64_t zp = i - z * pl + ((z + 1) % g.Lz) * pl;
+            p += si * s[zp];
+        }
+        m += si;
+        q += si * si;
+    }
+    *P = p; *M = m; *Q = q;
+}
+
+/* init!(sys, :random), ising.jl:170-188 / blume_capel.jl:87-109, fed by Philox */
+void orc_init_random(int8_t* s, int model, int dim, const int32_t* L, uint64_t seed,
+                     uint32_t stream) {
+    geom_t g;
+    if (geom_init(&g, dim, L)) return;
+    for (int64_t i = 0; i < g.N; ++i) {
+        uint32_t r = orc_site_word(seed, stream, 0, colour_of(&g, i), P_INIT, (uint64_t)i);
+        if (model == ORC_ISING) s[i] = (r & 0x80000000u) ? 1 : -1;
+        else s[i] = (int8_t)((int)(((uint64_t)r * 3u) >> 32) - 1);
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * Mode (i): checkerboard sweeps.  One sweep = colour 0 then colour 1; within a
+ * colour every site sees only the other colour, so visiting the sites of one colour
+ * in any order equals the simultaneous update the device performs.
+ *   Ising: spin_flip!(::AbstractIsing, ::AbstractMetropolis / ::AbstractHeatBath),
+ *          SpinSystems/src/ising.jl:145-168, modify! :310-315.
+ *   Blume-Capel: spin_flip! blume_capel.jl:52-85, modify! :250-256.
+ * ------------------------------------------------------------------------- */
+int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                 double J, double D, double h, uint64_t seed, uint32_t stream,
+                 uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
+                 uint64_t* accepts) {
+    geom_t g;
+    if (geom_init(&g, dim, L)) return ORC_ERR_INVALID;
+    int z = 2 * dim, nc = 2 * z + 1;
+    uint64_t thr[3 * 2 * 13];
+    uint32_t xm[14];
+    int rc = model == ORC_ISING ? orc_table_ising(dim, alg, beta, J, h, thr, xm)
+                                : orc_table_bc(dim, alg, beta, J, D, h, thr);
+    if (rc) return rc;
+    int64_t P, M, Q;
+    orc_observables(s, dim, L, &P, &M, &Q);
+    uint64_t att = 0, acc = 0;
+    for (int64_t k = 0; k < nsweeps; ++k) {
+        uint64_t t = sweep0 + (uint64_t)k;
+        for (int c = 0; c < 2; ++c) {
+            for (int64_t i = 0; i < g.N; ++i) {
+                if (colour_of(&g, i) != c) continue;
+                int so = s[i];
+                int S = nbr_sum(&g, s, i);
+                ++att;
+                if (model == ORC_ISING) {
+                    int sigma = so * S;
+                    int a = (sigma + z) / 2;
+                    int idx = a + (z + 1) * (so > 0);
+                    uint32_t u = orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i);
+                    if ((uint64_t)(u ^ xm[idx]) < thr[idx]) {
+                        s[i] = (int8_t)(-so);
+                        P += -2 * sigma;
+                        M += -2 * so;
+                        ++acc;
+                    }
+                } else {
+                    int sn;
+                    if (alg == ORC_HEATBATH) {
+                        uint32_t u = orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i);
+                        sn = (u < thr[2 * (S + z)]) ? -1 : ((u < thr[2 * (S + z) + 1]) ? 0 : 1);
+                        if (sn == so) continue;
+                    } else {
+                        int b = (int)(orc_site_word(seed, stream, t, c, P_PROPOSE, (uint64_t)i) >> 31);
+                        int idx = (so + 1) * 2 * nc + b * nc + (S + z);
+                        uint32_t u = orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i);
+                        if (!((uint64_t)u < thr[idx])) continue;
+                        sn = bc_propose(so, b);
+                    }
+                    int ds = sn - so;
+                    s[i] = (int8_t)sn;
+                    P += (int64_t)ds * S;
+                    M += ds;
+                    Q += sn * sn - so * so;
+                    ++acc;
+                }
+            }
+        }
+        if (obs) { obs[3 * k] = P; obs[3 * k + 1] = M; obs[3 * k + 2] = Q; }
+    }
+    if (attempts) *attempts += att;
+    if (accepts) *accepts += acc;
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * Mode (ii): the reference's sequential random-site order with FP64 decisions.
+ *   pick_site:   SpinSystems/src/abstractions.jl:19 (rand(rng, UInt) % N + 1)
+ *   Metropolis:  ising.jl:145-151 -> metropolis.jl:124-127 -> importance_sampling.jl:80-85
+ *   Glauber:     metropolis.jl:231-237
+ *   HeatBath:    ising.jl:153-168, blume_capel.jl:61-85
+ *   BC proposal: blume_capel.jl:21-30, 52-59
+ * Attempt a draws Philox(seed, (a lo, a hi, P_SEQ<<24, stream)) -> site from words
+ * 0,1 and U from words 2,3; Blume-Capel proposals take the top bit of word 0 of
+ * Philox(seed, (a lo, a hi, P_SEQ2<<24, stream)).
+ * ------------------------------------------------------------------------- */
+int orc_seq_attempts(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                     double J, double D, double h, uint64_t seed, uint32_t stream,
+                     uint64_t attempt0, int64_t nattempts, uint64_t* steps,
+                     uint64_t* accepted) {
+    geom_t g;
+    if (geom_init(&g, dim, L)) return ORC_ERR_INVALID;
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint64_t st = 0, ac = 0;
+    for (int64_t k = 0; k < nattempts; ++k) {
+        uint64_t a = attempt0 + (uint64_t)k;
+        uint32_t ctr[4] = {(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)P_SEQ << 24, stream};
+        uint32_t w[4];
+        orc_philox4x32_10(ctr, key, w);
+        int64_t i = (int64_t)((((uint64_t)w[0] << 32) | w[1]) % (uint64_t)g.N);
+        double U = u53(w[2], w[3]);
+        int so = s[i];
+        int S = nbr_sum(&g, s, i);
+        ++st;
+        if (model == ORC_ISING) {
+            double lpi = (double)(so * S);
+            double dpair = ((-2.0) * J) * lpi;
+            double dspin = -2.0 * so;
+            double dE = (-dpair) - (h * dspin);
+            int flip;
+            if (alg == ORC_METROPOLIS) {
+                double lr = (-beta) * dE;
+                flip = (lr > 0) || (U < exp(lr));
+            } else if (alg == ORC_GLAUBER) {
+                double lr = (-beta) * dE;
+                flip = U < logistic(lr);
+            } else {
+                double pp = logistic((beta * (double)so) * dE);
+                int sn = U < pp ? 1 : -1;
+                flip = sn != so;
+            }
+            if (flip) { s[i] = (int8_t)(-so); ++ac; }
+        } else {
+            int sn;
+            if (alg == ORC_HEATBATH) {
+                double coupling = J * (double)S;
+                double e1 = (coupling - (h * -1.0)) + D;
+                double e3 = ((-coupling) - (h * 1.0)) + D;
+                double w1 = exp((-beta) * e1), w2 = exp((-beta) * 0.0), w3 = exp((-beta) * e3);
+                double zz = (w1 + w2) + w3;
+                double r = U * zz;
+                sn = r < w1 ? -1 : (r < (w1 + w2) ? 0 : 1);
+                if (sn != so) { s[i] = (int8_t)sn; ++ac; }
+            } else {
+                uint32_t c2[4] = {(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)P_SEQ2 << 24, stream};
+                uint32_t w2[4];
+                orc_philox4x32_10(c2, key, w2);
+                int b = (int)(w2[0] >> 31);
+                sn = bc_propose(so, b);
+                double ds = (double)(sn - so), ds2 = (double)(sn * sn - so * so);
+                double dE = ((-(ds * (J * (double)S))) - (h * ds)) + (D * ds2);
+                double lr = (-beta) * dE;
+                int acc = alg == ORC_METROPOLIS ? ((lr > 0) || (U < exp(lr))) : (U < logistic(lr));
+                if (acc) { s[i] = (int8_t)sn; ++ac; }
+            }
+        }
+    }
+    if (steps) *steps += st;
+    if (accepted) *accepted += ac;
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * Flat-histogram sweeps in checkerboard order.
+ *   generic importance-sampling spin flip: ising.jl:135-143, blume_capel.jl:41-50
+ *   accept!(alg, x_new, x_old):  src/algorithms/importance_sampling.jl:69-85
+ *   MUCA record_visit!:          src/ensembles/multicanonical.jl:25-30 (h[x] += 1)
+ *   WangLandau accept!:          src/algorithms/wang_landau.jl:29-37 (lw[x_vis] -= logf)
+ *   BinnedObject integer index:  src/infrastructure/binned_object.jl:22-24 (div(x-start,step)+1)
+ * The decision lr > 0 || U < exp(lr) is evaluated as lr > 0 || log(U) < lr.  An
+ * energy outside the bins stops the run before the attempt is counted (the
+ * reference throws BoundsError from lw(x_new) with the counters unchanged,
+ * test/test_multicanonical.jl:39-43).  Energies must be integers: J, D, h integral.
+ * The Wang-Landau run also counts visits in H (for the flatness test).
+ * ------------------------------------------------------------------------- */
+static int bin_of(int64_t E, int64_t start, int64_t step, int64_t nbins, int64_t* b) {
+    int64_t q = (E - start) / step; /* truncating, as Julia div */
+    if (q < 0 || q >= nbins) return 0;
+    *b = q;
+    return 1;
+}
+
+int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
+                       double h, int mode, double* lnw, int64_t* H, int64_t start,
+                       int64_t step, int64_t nbins, double logf, uint64_t seed,
+                       uint32_t stream, uint64_t sweep0, int64_t nsweeps, int64_t* obs,
+                       uint64_t* steps, uint64_t* accepted) {
+    geom_t g;
+    if (geom_init(&g, dim, L)) return ORC_ERR_INVALID;
+    if (step <= 0 || nbins <= 0) return ORC_ERR_INVALID;
+    int64_t Ji = (int64_t)J, Di = (int64_t)D, hi = (int64_t)h;
+    if ((double)Ji != J || (double)Di != D || (double)hi != h) return ORC_ERR_INVALID;
+    int64_t P, M, Q;
+    orc_observables(s, dim, L, &P, &M, &Q);
+    int64_t E = -Ji * P + Di * Q - hi * M;
+    int64_t bo;
+    if (!bin_of(E, start, step, nbins, &bo)) return ORC_ERR_RANGE;
+    uint64_t st = 0, ac = 0;
+    int rc = ORC_OK;
+    for (int64_t k = 0; k < nsweeps && rc == ORC_OK; ++k) {
+        uint64_t t = sweep0 + (uint64_t)k;
+        for (int c = 0; c < 2 && rc == ORC_OK; ++c) {
+            for (int64_t i = 0; i < g.N; ++i) {
+                if (colour_of(&g, i) != c) continue;
+                int so = s[i];
+                int S = nbr_sum(&g, s, i);
+                int sn;
+                if (model == ORC_ISING) sn = -so;
+                else sn = bc_propose(so, (int)(orc_site_word(seed, stream, t, c, P_PROPOSE, (uint64_t)i) >> 31));
+                int64_t ds = sn - so, dq = sn * sn - so * so, dp = ds * S;
+                int64_t dE = -Ji * dp + Di * dq - hi * ds;
+                int64_t En = E + dE, bn;
+                if (!bin_of(En, start, step, nbins, &bn)) { rc = ORC_ERR_RANGE; break; }
+                double lr = lnw[bn] - lnw[bo];
+                double U = u53(orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i),
+                               orc_site_word(seed, stream, t, c, P_LOW, (uint64_t)i));
+                int acc = (lr > 0) || (orc_log(U) < lr);
+                ++st;
+                if (acc) {
+                    ++ac;
+                    s[i] = (int8_t)sn;
+                    P += dp; M += ds; Q += dq;
+                    E = En;
+                    bo = bn;
+                }
+                if (mode == ORC_WL) lnw[bo] -= logf;
+                H[bo] += 1;
+            }
+        }
+        if (rc == ORC_OK && obs) { obs[3 * k] = P; obs[3 * k + 1] = M; obs[3 * k + 2] = Q; }
+    }
+    if (steps) *steps += st;
+    if (accepted) *accepted += ac;
+    return rc;
+}
+
+/* update!(::MulticanonicalEnsemble; mode=:simple), src/ensembles/multicanonical.jl:32-43 */
+void orc_muca_update(double* lnw, const int64_t* H, int64_t nbins) {
+    for (int64_t b = 0; b < nbins; ++b) {
+        double logh = H[b] > 0 ? orc_log((double)H[b]) : 0.0;
+        lnw[b] -= logh;
+    }
+}
+
+/* Wang-Landau flatness (Wang & Landau, PRL 86, 2050 (2001)): over the bins visited
+ * at least once in the run, min H >= flatness * mean H. */
+int orc_wl_flat(const int64_t* H, const uint8_t* visited, int64_t nbins, double flatness,
+                double* ratio) {
+    int64_t mn = INT64_MAX, sum = 0, cnt = 0;
+    for (int64_t b = 0; b < nbins; ++b) {
+        if (!visited[b]) continue;
+        if (H[b] < mn) mn = H[b];
+        sum += H[b];
+        ++cnt;
+    }
+    if (cnt == 0 || sum == 0) { if (ratio) *ratio = 0.0; return 0; }
+    double mean = (double)sum / (double)cnt;
+    double r = (double)mn / mean;
+    if (ratio) *ratio = r;
+    return r >= flatness;
+}
+
+/* ---------------------------------------------------------------------------
+ * Replica exchange, src/algorithms/replica_exchange.jl:110-178 (threads update!):
+ * even/odd neighbour pairs by stage, lr = exchange_log_ratio, accept iff
+ * lr > 0 || U < exp(lr) (evaluated as log(U) < lr), swap the ladder positions.
+ * pos[r] = 0-based ladder position held by replica r (the reference's indices - 1).
+ * U for pair p after sweep t: Philox(seed, (p, t lo, t hi16 | P_EXCHANGE<<24, ladder))
+ * words 0 and 1.
+ * ------------------------------------------------------------------------- */
+int orc_pt_exchange(int n, const double* betas, int32_t* pos, int32_t* stage,
+                    const double* x, uint64_t seed, uint32_t ladder, uint64_t t,
+                    uint64_t* steps, uint64_t* accepted) {
+    if (n < 2) return ORC_ERR_INVALID;
+    int32_t* rep = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    for (int r = 0; r < n; ++r) rep[pos[r]] = r;
+    int first = (*stage % 2 == 0) ? 0 : 1;
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int p = first; p < n - 1; p += 2) {
+        int ri = rep[p], rj = rep[p + 1];
+        steps[p] += 1;
+        uint32_t ctr[4] = {(uint32_t)p, (uint32_t)t,
+                           ((uint32_t)(t >> 32) & 0xFFFFu) | ((uint32_t)P_EXCHANGE << 24), ladder};
+        uint32_t w[4];
+        orc_philox4x32_10(ctr, key, w);
+        double U = u53(w[0], w[1]);
+        double bi = betas[p], bj = betas[p + 1];
+        double xi = x[ri], xj = x[rj];
+        double lr = (((-bi) * xj) - ((-bi) * xi)) + (((-bj) * xi) - ((-bj) * xj));
+        if ((lr > 0) || (orc_log(U) < lr)) {
+            accepted[p] += 1;
+            pos[ri] = p + 1;
+            pos[rj] = p;
+        }
+    }
+    *stage = 1 - *stage;
+    free(rep);
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * CPU baseline harness: one independent chain per thread (the reference's
+ * ParallelChains threads pattern, src/infrastructure/parallel_chains.jl:99-105).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    int model, dim, alg;
+    int32_t L[3];
+    double beta, J, D, h;
+    uint64_t seed;
+    uint32_t stream;
+    int64_t attempts;
+    int8_t* s;
+    int rc;
+} bench_arg_t;
+
+static void* bench_thread(void* p) {
+    bench_arg_t* a = (bench_arg_t*)p;
+    uint64_t st = 0, ac = 0;
+    a->rc = orc_seq_attempts(a->s, a->model, a->dim, a->L, a->alg, a->beta, a->J, a->D, a->h,
+                             a->seed, a->stream, 0, a->attempts, &st, &ac);
+    return NULL;
+}
+
+int orc_bench_seq(int model, int dim, const int32_t* L, int alg, double beta, double J,
+                  double D, double h, uint64_t seed, int nthreads, int64_t attempts_per_thread,
+                  double* seconds) {
+    geom_t g;
+    if (geom_init(&g, dim, L) || nthreads < 1) return ORC_ERR_INVALID;
+    bench_arg_t* args = (bench_arg_t*)calloc((size_t)nthreads, sizeof(bench_arg_t));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int k = 0; k < nthreads; ++k) {
+        bench_arg_t* a = &args[k];
+        a->model = model; a->dim = dim; a->alg = alg;
+        a->L[0] = L[0]; a->L[1] = L[1]; a->L[2] = dim == 3 ? L[2] : 1;
+        a->beta = beta; a->J = J; a->D = D; a->h = h;
+        a->seed = seed; a->stream = (uint32_t)k; a->attempts = attempts_per_thread;
+        a->s = (int8_t*)malloc((size_t)g.N);
+        orc_init_random(a->s, model, dim, L, seed, (uint32_t)k);
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int k = 0; k < nthreads; ++k) pthread_create(&th[k], NULL, bench_thread, &args[k]);
+    int rc = ORC_OK;
+    for (int k = 0; k < nthreads; ++k) {
+        pthread_join(th[k], NULL);
+        if (args[k].rc) rc = args[k].rc;
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    *seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    for (int k = 0; k < nthreads; ++k) free(args[k].s);
+    free(args);
+    free(th);
+    return rc;
+}

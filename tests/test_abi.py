@@ -1,0 +1,76 @@
+"""C-ABI surface and host-side logic (CPU only; no compute call needs a GPU)."""
+import ctypes
+import glob
+import math
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        names += re.findall(r"MCX_API\s+[\w\s\*]+?\b(mcx_\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for n in ("mcx_ctx_create", "mcx_lattice_create", "mcx_sweep", "mcx_observables"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(mcxlib):
+    lib = ctypes.CDLL(mcxlib._lib.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    # every binding in the Python mirror names an exported symbol
+    for n in mcxlib._lib.SIGNATURES:
+        assert hasattr(lib, n), n
+
+
+def test_status_strings_need_no_gpu(mcxlib):
+    lib = mcxlib._lib.load()
+    assert lib.mcx_status_string(0) == b"ok"
+    assert b"range" in lib.mcx_status_string(2)
+    assert lib.mcx_version() >= 1
+
+
+def test_boltzmann_ensemble_rules(mcxlib):
+    # test/test_ensembles.jl:22-57
+    B = mcxlib.BoltzmannEnsemble
+    with pytest.raises(mcxlib.ArgumentError):
+        B(beta=1.0, **{"β": 2.0})
+    with pytest.raises(mcxlib.ArgumentError):
+        B()
+    with pytest.raises(mcxlib.ArgumentError):
+        B(beta=1.0, T=2.0)
+    assert B(T=2.0).beta == 0.5
+    assert B(**{"β": 2.0}).logweight(1.0) == -2.0
+    assert B(beta=2.0) == B(**{"β": 2.0})
+
+
+def test_logistic(mcxlib):
+    # test/test_utils.jl:56-67
+    f = mcxlib.logistic
+    assert f(0.0) == 0.5
+    for x in (0.1, 1.0, 5.0, 40.0):
+        assert abs(f(x) + f(-x) - 1.0) < 1e-15
+
+
+def test_algorithm_objects(mcxlib):
+    m = mcxlib.Metropolis(mcxlib.Philox(42), beta=0.4407)
+    assert m.steps == 0 and m.accepted == 0 and mcxlib.acceptance_rate(m) == 0.0
+    assert mcxlib.ensemble(m).beta == 0.4407
+    g = mcxlib.Glauber(7, **{"β": 0.3})
+    assert g.beta == 0.3 and g.rng.seed == 7
+    hb = mcxlib.HeatBath(mcxlib.Philox(1), beta=0.6)
+    assert hb.steps == 0 and hb.beta == 0.6
+    m.steps, m.accepted = 10, 4
+    assert mcxlib.acceptance_rate(m) == 0.4
+    mcxlib.reset_(m)
+    assert m.steps == 0 and m.accepted == 0

@@ -1,0 +1,166 @@
+"""Device checkerboard sweeps against the oracle, bit for bit (GPU)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ALG = {"metropolis": O.METROPOLIS, "glauber": O.GLAUBER, "heatbath": O.HEATBATH}
+
+
+def _alg(mcx, name, seed, beta, stream=0):
+    rng = mcx.Philox(seed, stream)
+    return {"metropolis": mcx.Metropolis, "glauber": mcx.Glauber, "heatbath": mcx.HeatBath}[name](rng, beta=beta)
+
+
+def _run_pair(mcx, model, L, alg, beta, seed=42, stream=0, nsweeps=6, D=0.0, h=0.0, J=1.0, layout="int8",
+              init="random"):
+    if model == O.ISING:
+        sys_ = mcx.Ising(L, J=J, h=h, layout=layout)
+    else:
+        sys_ = mcx.BlumeCapel(L, J=J, D=D, h=h)
+    if init == "random":
+        mcx.init_(sys_, "random", rng=mcx.Philox(seed, stream))
+        s = O.init_random(model, L, seed, stream)
+    else:
+        s = np.ones(int(np.prod(L)), np.int8)
+    assert np.array_equal(sys_.spins, s)
+    a = _alg(mcx, alg, seed, beta, stream)
+    obs = mcx.sweep_(sys_, a, nsweeps, record=True)
+    oobs, att, acc = O.cb_sweep(s, model, L, ALG[alg], beta, seed, stream=stream, nsweeps=nsweeps, J=J, D=D, h=h)
+    return sys_, a, obs, s, oobs, att, acc
+
+
+ISING_CASES = [
+    ([4, 4], "metropolis", 0.4407, 0.0),
+    ([6, 8], "glauber", 0.3, 0.0),          # W=3: per-site kernel
+    ([8, 8], "heatbath", 0.6, 0.0),         # W=4: 4-site words
+    ([16, 12], "metropolis", 0.4407, 0.3),  # field
+    ([32, 32], "metropolis", 0.4407, 0.0),  # W=16: 128-bit rows
+    ([64, 64], "glauber", 0.4407, 0.0),
+    ([64, 48], "heatbath", 0.3, -0.2),
+    ([4, 4, 4], "metropolis", 0.22, 0.0),
+    ([24, 24, 24], "metropolis", 0.2216, 0.0),
+    ([32, 8, 6], "heatbath", 0.25, 0.1),
+    ([16, 16, 16], "glauber", 0.2, 0.0),
+]
+
+
+@pytest.mark.parametrize("L,alg,beta,h", ISING_CASES)
+def test_ising_parity(gpu, L, alg, beta, h):
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.ISING, L, alg, beta, h=h)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.steps == att
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    assert gpu.observables(sys_) == gpu.observables(sys_, full=True)
+
+
+BC_CASES = [
+    ([4, 4], "metropolis", 0.5, 1.0, 0.0),
+    ([8, 6], "heatbath", 0.7, 0.5, 0.1),
+    ([32, 32], "metropolis", 0.6, 1.0, 0.0),
+    ([64, 64], "heatbath", 0.6, 1.0, 0.0),
+    ([64, 40], "glauber", 0.45, 0.5, 0.2),
+    ([8, 8, 8], "metropolis", 0.3, 1.0, 0.0),
+    ([32, 16, 8], "heatbath", 0.35, 0.7, 0.0),
+]
+
+
+@pytest.mark.parametrize("L,alg,beta,D,h", BC_CASES)
+def test_blume_capel_parity(gpu, L, alg, beta, D, h):
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.BC, L, alg, beta, D=D, h=h)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    assert gpu.observables(sys_) == gpu.observables(sys_, full=True)
+
+
+@pytest.mark.parametrize("L,alg", [([128, 128], "metropolis"), ([256, 64], "glauber"), ([128, 8, 8], "heatbath")])
+def test_msc64_matches_int8_and_oracle(gpu, L, alg):
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.ISING, L, alg, 0.4407 if len(L) == 2 else 0.22,
+                                                layout="msc64")
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+
+
+def test_l4096_two_sweeps_bit_exact(gpu):
+    """configs: 2-D L=4096, seed 7, Metropolis at beta 0.4407, int8 and MSC64."""
+    L = [4096, 4096]
+    s0 = O.init_random(O.ISING, L, 7)
+    s = s0.copy()
+    oobs, _, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.4407, 7, nsweeps=2)
+    for layout in ("int8", "msc64"):
+        sys_ = gpu.Ising(L, layout=layout)
+        gpu.init_(sys_, "random", rng=gpu.Philox(7))
+        a = gpu.Metropolis(gpu.Philox(7), beta=0.4407)
+        obs = gpu.sweep_(sys_, a, 2, record=True)
+        assert np.array_equal(obs, oobs)
+        assert a.accepted == acc
+        assert np.array_equal(sys_.spins, s)
+        sys_.close()
+
+
+def test_sweeps_compose_and_replay(gpu):
+    """Counter-based stream: 3+5 sweeps equal 8 sweeps; a replay from the same
+    counter reproduces the run."""
+    L = [64, 32]
+    a1 = gpu.Ising(L)
+    gpu.init_(a1, "random", rng=gpu.Philox(1))
+    m1 = gpu.Metropolis(gpu.Philox(5), beta=0.5)
+    gpu.sweep_(a1, m1, 3)
+    gpu.sweep_(a1, m1, 5)
+    a2 = gpu.Ising(L)
+    gpu.init_(a2, "random", rng=gpu.Philox(1))
+    m2 = gpu.Metropolis(gpu.Philox(5), beta=0.5)
+    gpu.sweep_(a2, m2, 8)
+    assert np.array_equal(a1.spins, a2.spins)
+    assert m1.accepted == m2.accepted and m1.rng.counter == 8
+
+
+def test_known_answers_through_the_abi(gpu):
+    # SpinSystems/test/test_ising.jl:8-35
+    sys_ = gpu.Ising([4, 4])
+    assert gpu.energy(sys_) == -32 and gpu.magnetization(sys_) == 16
+    sp = sys_.spins
+    sp[0] = -1
+    sys_.spins = sp
+    assert gpu.energy(sys_) == -24 and gpu.magnetization(sys_) == 14
+    # SpinSystems/test/test_blume_capel.jl:8-31
+    bc = gpu.BlumeCapel([4, 4], J=1.0, D=0.5)
+    assert gpu.energy(bc) == -24.0 and gpu.magnetization(bc) == 16
+    sp = bc.spins
+    sp[0] = 0
+    bc.spins = sp
+    assert gpu.energy(bc) == -24.0 + 3.5 and gpu.magnetization(bc) == 15
+    gpu.init_(bc, "zero")
+    assert gpu.magnetization(bc) == 0 and gpu.energy(bc) == 0.0
+    gpu.init_(bc, "down")
+    assert np.all(bc.spins == -1)
+
+
+def test_argument_errors(gpu):
+    with pytest.raises(gpu.ArgumentError):
+        gpu.Ising([5, 8])
+    with pytest.raises(gpu.ArgumentError):
+        gpu.Ising([2, 8])
+    with pytest.raises(gpu.ArgumentError):
+        gpu.Ising([64, 64], layout="msc64")  # Lx must be a multiple of 128
+    sys_ = gpu.Ising([8, 8])
+    with pytest.raises(gpu.ArgumentError):
+        sys_.spins = np.zeros(64, np.int8)  # 0 is not an Ising state
+    with pytest.raises(gpu.ArgumentError):
+        gpu.init_(sys_, "zero")
+    with pytest.raises(gpu.ArgumentError):
+        gpu.init_(sys_, "random")
+
+
+def test_hbm_budget(gpu):
+    ctx = gpu.Context(hbm_budget=1 << 20)
+    with pytest.raises(gpu.BudgetError):
+        gpu.Ising([2048, 2048], ctx=ctx)
+    small = gpu.Ising([64, 64], ctx=ctx)
+    used, budget = ctx.memory()
+    assert 0 < used <= budget
+    small.close()
