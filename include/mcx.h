@@ -156,6 +156,95 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
 /* Copy the per-sweep series of the last mcx_sweep call (first n sweeps). */
 MCX_API mcx_status mcx_read_series(mcx_lattice* lat, int64_t* obs_series, int64_t n);
 
+
+/* --------------------------------------------------------- flat histogram -- */
+/* A 1-D integer binning [start, start + step*nbins) of the total energy with an FP64
+ * log-weight table (ln g) and an int64 visit histogram: the BinnedObject pair of
+ * MulticanonicalEnsemble / WangLandauEnsemble (src/ensembles/multicanonical.jl:1-23,
+ * src/ensembles/wang_landau.jl:1-21, src/infrastructure/binned_object.jl:13-24).
+ * The bin of E is div(E - start, step) (truncating); bins outside [0, nbins) are the
+ * reference's BoundsError.  ln g starts at 0, H at 0. */
+MCX_API mcx_status mcx_flathist_create(mcx_ctx* ctx, int64_t start, int64_t step, int64_t nbins,
+                                       mcx_flathist** out);
+MCX_API mcx_status mcx_flathist_destroy(mcx_flathist* fh);
+MCX_API mcx_status mcx_flathist_set_logweight(mcx_flathist* fh, const double* host, int64_t n);
+MCX_API mcx_status mcx_flathist_get_logweight(mcx_flathist* fh, double* host, int64_t n);
+MCX_API mcx_status mcx_flathist_set_histogram(mcx_flathist* fh, const int64_t* host, int64_t n);
+MCX_API mcx_status mcx_flathist_get_histogram(mcx_flathist* fh, int64_t* host, int64_t n);
+/* reset!(::Multicanonical) histogram part (src/algorithms/multicanonical.jl:27-33): H := 0. */
+MCX_API mcx_status mcx_flathist_reset(mcx_flathist* fh);
+/* update!(::MulticanonicalEnsemble; mode=:simple) (multicanonical.jl:32-43):
+ * ln g[b] -= log(H[b]) where H[b] > 0. */
+MCX_API mcx_status mcx_flathist_update_muca(mcx_flathist* fh);
+/* Wang-Landau flatness (the reference has none; Wang & Landau 2001): marks every bin
+ * with H > 0 as visited (the mark persists across resets), then is_flat = min H >=
+ * threshold * mean H over the visited bins; ratio = min H / mean H. */
+MCX_API mcx_status mcx_flathist_flatness(mcx_flathist* fh, double threshold, int* is_flat,
+                                         double* ratio);
+/* merge_histograms! (src/algorithms/parallel_multicanonical.jl:38-47): dst.H += src[i].H. */
+MCX_API mcx_status mcx_flathist_merge(mcx_flathist* dst, mcx_flathist* const* src, int nsrc);
+/* distribute_logweight! (parallel_multicanonical.jl:59-68): dst.lnw := src.lnw. */
+MCX_API mcx_status mcx_flathist_copy_logweight(mcx_flathist* dst, const mcx_flathist* src);
+/* `nsweeps` checkerboard sweeps of N importance-sampling spin flips
+ * (ising.jl:135-143, blume_capel.jl:41-50) for each of `nwalkers` walkers, with
+ * accept!(alg, E_new, E_old) of a Multicanonical (importance_sampling.jl:69-78) or
+ * Wang-Landau (wang_landau.jl:29-37) algorithm; the decision lr > 0 || U < exp(lr)
+ * is evaluated as log(U) < lr.  fhs: one table shared by all walkers (nfh = 1;
+ * Multicanonical only: H adds up over walkers like merge_histograms!) or one per
+ * walker (nfh = nwalkers).  Walker i draws from rngs[i].  Lattices must be int8, of
+ * one shape and model, with integer J, D, h.  A walker whose energy leaves the bins
+ * stops at that attempt with its counters unchanged; the call then returns
+ * MCX_ERR_OUT_OF_RANGE.  The per-sweep (pair, spin, spin2) series of each walker is
+ * readable with mcx_read_series. */
+MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lattices, int nwalkers,
+                                      mcx_flathist* const* fhs, int nfh, mcx_flathist_mode mode,
+                                      double logf, mcx_rng* rngs, int64_t nsweeps,
+                                      mcx_counters* counters);
+
+/* ------------------------------------------------------ parallel tempering -- */
+/* Batched replica exchange over `nladders` independent ladders: ladder l holds
+ * nreplicas[l] Ising replicas (J, h) of side sides[l] (dim 2 or 3, side a multiple
+ * of 8) at the inverse temperatures betas[...] listed ladder after ladder by ladder
+ * position.  Replaces ParallelTempering(betas; seed, rng)
+ * (src/algorithms/parallel_tempering.jl:24-53) over ReplicaExchange
+ * (src/algorithms/replica_exchange.jl:13-19, 52-58) with one system per replica.
+ * Replica r (0-based, ladder after ladder) draws its sweep stream with stream id r. */
+typedef enum mcx_pt_mode {
+    MCX_PT_PERSISTENT = 0, /* one cooperative launch for all sweeps of all replicas */
+    MCX_PT_PLAIN = 1       /* one launch per replica and colour, one per exchange   */
+} mcx_pt_mode;
+
+MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int32_t* sides,
+                                 const int32_t* nreplicas, const double* betas, double J,
+                                 double h, mcx_pt** out);
+MCX_API mcx_status mcx_pt_destroy(mcx_pt* pt);
+MCX_API mcx_status mcx_pt_info(const mcx_pt* pt, int32_t* nreplicas, int64_t* sites,
+                               int64_t* device_bytes);
+/* init!(sys, :random) of every replica (replica r uses stream r). */
+MCX_API mcx_status mcx_pt_init_random(mcx_pt* pt, uint64_t seed);
+MCX_API mcx_status mcx_pt_set_spins(mcx_pt* pt, int32_t replica, const int8_t* host, size_t n);
+MCX_API mcx_status mcx_pt_get_spins(mcx_pt* pt, int32_t replica, int8_t* host, size_t n);
+/* `nsweeps` checkerboard sweeps of every replica at its current ladder beta; after
+ * every sweep t with (t+1) % exchange_every == 0, update!(rx, energies)
+ * (replica_exchange.jl:158-178) on every ladder.  series: host
+ * int64[nsweeps][nreplicas][2] of (pair_sum, spin_sum) after each sweep, or NULL. */
+MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64_t nsweeps,
+                              int32_t exchange_every, mcx_pt_mode mode, int64_t* series);
+/* index(rx) (replica_exchange.jl:48-50), 0-based: ladder position of each replica;
+ * and the stage. */
+MCX_API mcx_status mcx_pt_indices(mcx_pt* pt, int32_t* positions, int32_t* stage);
+/* rx.steps / rx.accepted per ladder edge, ladder after ladder (n_l - 1 each). */
+MCX_API mcx_status mcx_pt_exchange_counters(mcx_pt* pt, uint64_t* steps, uint64_t* accepted);
+/* Cached (pair_sum, spin_sum) of every replica. */
+MCX_API mcx_status mcx_pt_observables(mcx_pt* pt, int64_t* pair_sum, int64_t* spin_sum);
+/* Accepted spin flips of every replica during the last mcx_pt_run. */
+MCX_API mcx_status mcx_pt_replica_accepted(mcx_pt* pt, uint64_t* accepted);
+/* Poll limit of the grid barrier waits (default 2^24 polls of ~100 ns). */
+MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls);
+/* Failure-detection check: a bounded wait on a device flag that nothing sets;
+ * returns MCX_ERR_TIMEOUT after `polls` polls, with the context still usable. */
+MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,190 @@
+// mcx_cb.cuh -- device building blocks of the checkerboard kernels, shared by the
+// single-lattice sweeps (mcx_sweep.cu) and the batched replica kernels (mcx_pt.cu).
+#pragma once
+
+#include <cstdint>
+
+#include "mcx_device.cuh"
+
+namespace mcx {
+
+__device__ __forceinline__ uint32_t upbits(uint32_t w) { return (~w >> 1) & 0x01010101u; }
+// per byte: v + 1 for v in {-1, 0, +1}
+__device__ __forceinline__ uint32_t plus1(uint32_t w) {
+    return ((w & 0x7F7F7F7Fu) + 0x01010101u) & 0x03030303u;
+}
+
+template <int V>
+__device__ __forceinline__ void load_row(const int8_t* p, uint32_t (&w)[V / 4]) {
+    if constexpr (V == 16) {
+        const uint4 v = *reinterpret_cast<const uint4*>(p);
+        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    } else if constexpr (V == 8) {
+        const uint2 v = *reinterpret_cast<const uint2*>(p);
+        w[0] = v.x; w[1] = v.y;
+    } else {
+        w[0] = *reinterpret_cast<const uint32_t*>(p);
+    }
+}
+
+template <int V>
+__device__ __forceinline__ void store_row(int8_t* p, const uint32_t (&w)[V / 4]) {
+    if constexpr (V == 16) {
+        *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    } else if constexpr (V == 8) {
+        *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+    } else {
+        *reinterpret_cast<uint32_t*>(p) = w[0];
+    }
+}
+
+__device__ __forceinline__ int bc_propose(int so, int bit) {
+    return bit ? (so == -1 ? 0 : -1) : (so == 1 ? 0 : 1);
+}
+
+// Row bookkeeping shared by all kernels: neighbour rows and the in-row parity.
+struct RowInfo {
+    int p;                   // (y + z + colour) & 1
+    long long ryp, rym, rzp, rzm;
+};
+
+__device__ __forceinline__ RowInfo row_info(int r, int Ly, int Lz, int colour, int dim) {
+    RowInfo ri;
+    const int y = r % Ly, z = r / Ly;
+    ri.p = (y + z + colour) & 1;
+    ri.ryp = (long long)((y + 1 == Ly ? 0 : y + 1) + Ly * z);
+    ri.rym = (long long)((y == 0 ? Ly - 1 : y - 1) + Ly * z);
+    if (dim == 3) {
+        ri.rzp = (long long)(y + Ly * (z + 1 == Lz ? 0 : z + 1));
+        ri.rzm = (long long)(y + Ly * (z == 0 ? Lz - 1 : z - 1));
+    } else {
+        ri.rzp = ri.rzm = 0;
+    }
+    return ri;
+}
+
+// Walks the chunks (row y + Ly*z, chunk q of the row) of one colour in grid-stride
+// order; the stride is decomposed once, so the loop itself has no divisions.
+struct ChunkIter {
+    int q, y, z;
+    int cpr, Ly, Lz;
+    int sq, sy, sz;
+    __device__ __forceinline__ ChunkIter(long long g0, long long stride, int cpr_, int Ly_, int Lz_)
+        : cpr(cpr_), Ly(Ly_), Lz(Lz_) {
+        const long long r0 = g0 / cpr;
+        q = (int)(g0 - r0 * cpr);
+        y = (int)(r0 % Ly);
+        z = (int)(r0 / Ly);
+        const long long sr = stride / cpr;
+        sq = (int)(stride - sr * cpr);
+        sy = (int)(sr % Ly);
+        sz = (int)(sr / Ly);
+    }
+    __device__ __forceinline__ bool valid() const { return z < Lz; }
+    __device__ __forceinline__ void next() {
+        q += sq;
+        int c = 0;
+        if (q >= cpr) { q -= cpr; c = 1; }
+        y += sy + c;
+        c = 0;
+        if (y >= Ly) { y -= Ly; c = 1; }
+        z += sz + c;
+    }
+    __device__ __forceinline__ int row() const { return y + Ly * z; }
+};
+
+__device__ __forceinline__ RowInfo row_info_yz(int y, int z, int Ly, int Lz, int colour, int dim) {
+    RowInfo ri;
+    ri.p = (y + z + colour) & 1;
+    ri.ryp = (long long)((y + 1 == Ly ? 0 : y + 1) + Ly * z);
+    ri.rym = (long long)((y == 0 ? Ly - 1 : y - 1) + Ly * z);
+    if (dim == 3) {
+        ri.rzp = (long long)(y + Ly * (z + 1 == Lz ? 0 : z + 1));
+        ri.rzm = (long long)(y + Ly * (z == 0 ? Lz - 1 : z - 1));
+    } else {
+        ri.rzp = ri.rzm = 0;
+    }
+    return ri;
+}
+
+// Gathers the V-site word groups of one chunk: own spins and the 2*DIM neighbour
+// words, with `side` the in-row neighbour shifted by one site.
+template <int DIM, int V>
+struct Chunk {
+    static constexpr int NW = V / 4;
+    uint32_t own[NW];
+    uint32_t nb[2 * DIM][NW];
+
+    __device__ __forceinline__ void load(const int8_t* cur, const int8_t* oth, int W, int r, int k0,
+                                         const RowInfo& ri) {
+        const long long base = (long long)r * W + k0;
+        load_row<V>(cur + base, own);
+        uint32_t mid[NW];
+        load_row<V>(oth + base, mid);
+        load_row<V>(oth + ri.ryp * W + k0, nb[1]);
+        load_row<V>(oth + ri.rym * W + k0, nb[2]);
+        if constexpr (DIM == 3) {
+            load_row<V>(oth + ri.rzp * W + k0, nb[4]);
+            load_row<V>(oth + ri.rzm * W + k0, nb[5]);
+        }
+        if (ri.p == 0) {
+            const int ke = k0 == 0 ? W - 1 : k0 - 1;
+            const uint32_t edge = (uint32_t)(uint8_t)oth[(long long)r * W + ke];
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                nb[3][w] = __funnelshift_l(w == 0 ? (edge << 24) : mid[w - 1], mid[w], 8);
+        } else {
+            const int ke = k0 + V == W ? 0 : k0 + V;
+            const uint32_t edge = (uint32_t)(uint8_t)oth[(long long)r * W + ke];
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                nb[3][w] = __funnelshift_r(mid[w], w == NW - 1 ? edge : mid[w + 1], 8);
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) nb[0][w] = mid[w];
+    }
+};
+
+// Ising decision for the four sites of one 32-bit word (bytes 0x01 = up, 0xFF = down).
+// Per byte: cnt2 = 2 * (down neighbours) from one AND per neighbour word; U1 = 1 for
+// an up site; idx2 = 2 * (a + (Z+1)*up) with a = aligned neighbours, which is
+// cnt2 for a down site and 2(2Z+1) - cnt2 for an up site, formed byte-parallel with
+// (cnt2 ^ 30) = 30 - cnt2 (cnt2 even, <= 12).  4*idx2 is the byte offset of the
+// 8-byte table entry.  One Philox call feeds the four 64-bit threshold compares.
+// Returns the flip bits (0/1 per byte); accumulates flips, flipped up spins and the
+// sum of idx2 over flips (sum a = (isum - (2Z+2)*nup) / 2).
+template <int Z, bool HB>
+__device__ __forceinline__ uint32_t ising_word(const uint32_t (&nbw)[Z], uint32_t own, uint4 rnd,
+                                               const unsigned long long* s_thr, int& nacc, int& nup,
+                                               int& isum) {
+    uint32_t cnt2 = 0;
+#pragma unroll
+    for (int d = 0; d < Z; ++d) cnt2 += nbw[d] & 0x02020202u;
+    const uint32_t U1 = (~own & 0x02020202u) >> 1;
+    const uint32_t idx2 = (cnt2 ^ (U1 * 30u)) - U1 * (uint32_t)(30 - 2 * (2 * Z + 1));
+    const uint32_t off = idx2 << 2;
+    const char* tb = reinterpret_cast<const char*>(s_thr);
+    const uint32_t us[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+    uint32_t fb = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        uint32_t u = us[b];
+        if (HB) u ^= 0u - ((U1 >> (8 * b)) & 1u);
+        const uint32_t o = __byte_perm(off, 0u, 0x4440u + b);
+        const unsigned long long t = *reinterpret_cast<const unsigned long long*>(tb + o);
+        if ((unsigned long long)u < t) fb |= 1u << (8 * b);
+    }
+    nacc += __popc(fb);
+    nup += __popc(fb & U1);
+    isum += (int)(((idx2 & (fb * 0xFFu)) * 0x01010101u) >> 24);
+    return fb;
+}
+
+// (pair, spin) deltas of a block of Ising flips from the word accumulators
+template <int Z>
+__device__ __forceinline__ void ising_deltas(int nacc, int nup, int isum, long long& dP, long long& dM) {
+    dP = 2ll * Z * nacc - 2ll * ((long long)isum - (2ll * Z + 2) * nup);
+    dM = 2ll * nacc - 4ll * nup;
+}
+
+}  // namespace mcx

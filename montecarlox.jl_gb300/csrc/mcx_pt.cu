@@ -1,0 +1,874 @@
+// mcx_pt.cu -- batched parallel tempering: many Ising replicas of uneven size, their
+// checkerboard sweeps and the replica-exchange step.
+//
+// Two forms with bit-identical results:
+//   PERSISTENT: one cooperative launch runs all sweeps of all replicas.  Replicas are
+//     cut into tiles of ~4096 same-colour sites; tiles are assigned to blocks by a
+//     longest-processing-time schedule built on the host.  A bounded grid barrier
+//     separates the two colours of a sweep and the sweep from the exchange; every
+//     block then evaluates the (tiny) exchange step itself, so the new ladder
+//     positions need no further barrier.  Per-replica energy deltas are triple
+//     buffered so that one sweep's accumulation never meets another's reads.
+//   PLAIN: one launch per replica and colour plus one exchange launch per sweep.
+//
+// Exchange rule: src/algorithms/replica_exchange.jl:110-178 (threads update!): pairs
+// (p, p+1) with p = first, first+2, ... where first = stage even ? 0 : 1 (0-based);
+// lr = (lw_i(x_j) - lw_i(x_i)) + (lw_j(x_i) - lw_j(x_j)) with lw(x) = -beta*x;
+// accept iff lr > 0 || U < exp(lr), evaluated as log(U) < lr with the project log;
+// on acceptance the two replicas swap ladder positions (their betas); the stage
+// toggles after every exchange step.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <queue>
+#include <vector>
+
+#include "mcx_cb.cuh"
+#include "mcx_device.cuh"
+#include "mcx_internal.h"
+#include "mcx_sweep.cuh"
+
+namespace mcx {
+
+struct PTReplica {
+    long long off[2];  // colour arrays inside the arena
+    int W, Ly, Lz, cpr, V, rows;
+    int ladder, gpos0, n;  // ladder id, first global position of the ladder, ladder size
+    uint32_t m_cpr, m_Ly;  // round-up reciprocals for exact division of small integers
+};
+
+struct PTTile {
+    int rep, c_begin, c_end, sites;
+};
+
+struct PTArgs {
+    int8_t* arena;
+    const PTReplica* reps;
+    const PTTile* tiles;
+    const int* block_tiles;  // CSR over blocks (persistent form)
+    const int* block_off;
+    int nrep, npos;
+    const unsigned long long* tables;  // [npos][16] for the algorithm of this run
+    const double* betas;               // [npos]
+    const int* pos_ladder;             // [npos]
+    const int* pos_local;              // [npos]
+    const int* ladder_n;               // [nladders]
+    int32_t* pos;                      // [nrep] ladder position of each replica
+    int32_t* stage;
+    long long* state;                  // [nrep][2] pair sum, spin sum
+    long long* delta;                  // [3][nrep][2]
+    unsigned long long* acc;           // [nrep]
+    unsigned long long* ex_steps;      // [npos] edge (p, p+1) counted at the global position of p
+    unsigned long long* ex_acc;        // [npos]
+    long long* series;                 // [nsweeps][nrep][2] or null
+    unsigned int* bar;                 // count, generation, error
+    double J, h;
+    uint32_t k0, k1;
+    unsigned long long sweep0;
+    long long nsweeps;
+    int every;
+    long long spin_limit;
+};
+
+// n / d for small n, d: m = ceil(2^32 / d) (exact while n < 2^32 / d); m = 0 encodes d = 1
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m) { return m ? __umulhi(n, m) : n; }
+
+// One tile of one replica: chunks [c_begin, c_end) of colour `colour`.
+template <int DIM, int V, bool HB>
+__device__ __forceinline__ void pt_tile(const PTArgs& a, const PTReplica& R, int rep, int c_begin, int c_end,
+                                        int colour, unsigned long long sweep, const unsigned long long* s_thr,
+                                        int& nacc, int& nup, int& isum) {
+    constexpr int Z = 2 * DIM;
+    constexpr int NW = V / 4;
+    int8_t* cur = a.arena + R.off[colour];
+    const int8_t* oth = a.arena + R.off[1 - colour];
+    const uint32_t w2 = ctr_word2(sweep, colour, P_ACCEPT);
+    for (int g = c_begin + (int)threadIdx.x; g < c_end; g += blockDim.x) {
+        const int r = (int)fdiv((uint32_t)g, R.m_cpr);
+        const int q = g - r * R.cpr;
+        const int z = (int)fdiv((uint32_t)r, R.m_Ly);
+        const int y = r - z * R.Ly;
+        const RowInfo ri = row_info_yz(y, z, R.Ly, R.Lz, colour, DIM);
+        Chunk<DIM, V> ch;
+        ch.load(cur, oth, R.W, r, q * V, ri);
+        const uint32_t c0 = (uint32_t)(((unsigned long long)r * R.W + q * V) >> 2);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            uint32_t nbw[Z];
+#pragma unroll
+            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
+            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, (uint32_t)rep), a.k0, a.k1);
+            const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
+            ch.own[w] ^= fb * 0xFEu;
+        }
+        store_row<V>(cur + (long long)r * R.W + q * V, ch.own);
+    }
+}
+
+template <int DIM, bool HB>
+__device__ __forceinline__ void pt_run_tile(const PTArgs& a, const PTTile& tl, int colour,
+                                            unsigned long long sweep, int ladder_pos, long long* dcur,
+                                            unsigned long long* s_thr) {
+    const PTReplica R = a.reps[tl.rep];
+    __syncthreads();  // previous tile is done with s_thr
+    if (threadIdx.x < 16) s_thr[threadIdx.x] = a.tables[(size_t)(R.gpos0 + ladder_pos) * 16 + threadIdx.x];
+    __syncthreads();
+    int nacc = 0, nup = 0, isum = 0;
+    if (R.V == 16) pt_tile<DIM, 16, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
+    else if (R.V == 8) pt_tile<DIM, 8, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
+    else pt_tile<DIM, 4, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
+    constexpr int Z = 2 * DIM;
+    long long dP, dM;
+    ising_deltas<Z>(nacc, nup, isum, dP, dM);
+    long long v[3] = {dP, dM, (long long)nacc};
+    unsigned long long* const dst[3] = {(unsigned long long*)&dcur[2 * tl.rep],
+                                        (unsigned long long*)&dcur[2 * tl.rep + 1], &a.acc[tl.rep]};
+    block_add_atomic<3>(v, dst);
+}
+
+// The exchange step on block-local copies: pos (replica -> position), rep_at
+// (global position -> replica), energies from (P, M).  Every thread handles the
+// pairs whose lower global position it owns; pairs are disjoint, so the position
+// updates never collide.  `count` adds the edge counters (done by one block only).
+__device__ void pt_exchange(const PTArgs& a, int* s_pos, int* s_rep, const long long* s_P, const long long* s_M,
+                            int stage, unsigned long long t, bool count) {
+    for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) s_rep[a.reps[r].gpos0 + s_pos[r]] = r;
+    __syncthreads();
+    const int first = (stage & 1) ? 1 : 0;
+    for (int gp = threadIdx.x; gp < a.npos; gp += blockDim.x) {
+        const int p = a.pos_local[gp];
+        const int l = a.pos_ladder[gp];
+        if (p < first || ((p - first) & 1) || p + 1 >= a.ladder_n[l]) continue;
+        const int ri = s_rep[gp], rj = s_rep[gp + 1];
+        const uint4 w = philox10(make_uint4((uint32_t)p, (uint32_t)t, ctr_word2(t, 0, P_EXCHANGE), (uint32_t)l),
+                                 a.k0, a.k1);
+        const double U = u53(w.x, w.y);
+        const double bi = a.betas[gp], bj = a.betas[gp + 1];
+        const double xi = (-(a.J * (double)s_P[ri])) - (a.h * (double)s_M[ri]);
+        const double xj = (-(a.J * (double)s_P[rj])) - (a.h * (double)s_M[rj]);
+        const double lr = (((-bi) * xj) - ((-bi) * xi)) + (((-bj) * xi) - ((-bj) * xj));
+        const bool acc = (lr > 0.0) || (mcx_log(U) < lr);
+        if (count) {
+            a.ex_steps[gp] += 1ull;
+            if (acc) a.ex_acc[gp] += 1ull;
+        }
+        if (acc) {
+            s_pos[ri] = p + 1;
+            s_pos[rj] = p;
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier with a bounded wait: bar[0] arrivals, bar[1] generation,
+// bar[2] error flag.  A wait that exceeds `limit` polls sets the error flag; every
+// block then leaves at its next barrier and the host reports MCX_ERR_TIMEOUT.
+__device__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long long limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned g = gen;
+        if (atomicAdd(&bar[0], 1u) == nblocks - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            st_release(&bar[1], g + 1);
+        } else {
+            long long n = 0;
+            while (ld_acquire(&bar[1]) == g) {
+                if (ld_acquire(&bar[2]) != 0u) { ok = 0; break; }
+                if (++n > limit) { atomicExch(&bar[2], 1u); ok = 0; break; }
+                __nanosleep(100);
+            }
+        }
+        gen = g + 1;
+        s_ok = ok && ld_acquire(&bar[2]) == 0u;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int DIM, bool HB>
+__global__ void __launch_bounds__(256) k_pt_persistent(const PTArgs a) {
+    extern __shared__ long long smem[];
+    long long* s_P = smem;
+    long long* s_M = s_P + a.nrep;
+    int* s_pos = reinterpret_cast<int*>(s_M + a.nrep);
+    int* s_rep = s_pos + a.nrep;
+    __shared__ unsigned long long s_thr[16];
+    __shared__ unsigned s_gen;
+    for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
+        s_P[r] = a.state[2 * r];
+        s_M[r] = a.state[2 * r + 1];
+        s_pos[r] = a.pos[r];
+    }
+    if (threadIdx.x == 0) s_gen = ld_acquire(&a.bar[1]);
+    int stage = *a.stage;
+    __syncthreads();
+    unsigned gen = s_gen;
+    const int t_begin = a.block_off[blockIdx.x], t_end = a.block_off[blockIdx.x + 1];
+    const size_t dsz = (size_t)a.nrep * 2;
+    for (long long s = 0; s < a.nsweeps; ++s) {
+        const unsigned long long t = a.sweep0 + (unsigned long long)s;
+        long long* dcur = a.delta + (size_t)(s % 3) * dsz;
+        if (blockIdx.x == 0) {
+            long long* dnext = a.delta + (size_t)((s + 1) % 3) * dsz;
+            for (size_t i = threadIdx.x; i < dsz; i += blockDim.x) dnext[i] = 0;
+        }
+        for (int colour = 0; colour < 2; ++colour) {
+            for (int k = t_begin; k < t_end; ++k) {
+                const PTTile tl = a.tiles[a.block_tiles[k]];
+                pt_run_tile<DIM, HB>(a, tl, colour, t, s_pos[tl.rep], dcur, s_thr);
+            }
+            if (!grid_sync(a.bar, gridDim.x, gen, a.spin_limit)) return;
+        }
+        for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
+            s_P[r] += dcur[2 * r];
+            s_M[r] += dcur[2 * r + 1];
+        }
+        __syncthreads();
+        if (a.series && blockIdx.x == 0)
+            for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
+                a.series[((size_t)s * a.nrep + r) * 2] = s_P[r];
+                a.series[((size_t)s * a.nrep + r) * 2 + 1] = s_M[r];
+            }
+        if ((t + 1) % (unsigned long long)a.every == 0) {
+            pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, blockIdx.x == 0);
+            stage ^= 1;
+        }
+    }
+    if (blockIdx.x == 0) {
+        for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
+            a.pos[r] = s_pos[r];
+            a.state[2 * r] = s_P[r];
+            a.state[2 * r + 1] = s_M[r];
+        }
+        if (threadIdx.x == 0) *a.stage = stage;
+    }
+}
+
+// Plain form: one launch per replica and colour (blocks = that replica's tiles).
+template <int DIM, bool HB>
+__global__ void __launch_bounds__(256) k_pt_plain_half(const PTArgs a, int tile0, int colour,
+                                                       unsigned long long sweep) {
+    __shared__ unsigned long long s_thr[16];
+    const PTTile tl = a.tiles[tile0 + blockIdx.x];
+    pt_run_tile<DIM, HB>(a, tl, colour, sweep, a.pos[tl.rep], a.delta, s_thr);
+}
+
+// Plain form: fold the sweep's deltas into the state, record, exchange (one block).
+__global__ void __launch_bounds__(256) k_pt_plain_exchange(const PTArgs a, long long s, unsigned long long t) {
+    extern __shared__ long long smem[];
+    long long* s_P = smem;
+    long long* s_M = s_P + a.nrep;
+    int* s_pos = reinterpret_cast<int*>(s_M + a.nrep);
+    int* s_rep = s_pos + a.nrep;
+    for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
+        s_P[r] = a.state[2 * r] + a.delta[2 * r];
+        s_M[r] = a.state[2 * r + 1] + a.delta[2 * r + 1];
+        a.delta[2 * r] = 0;
+        a.delta[2 * r + 1] = 0;
+        a.state[2 * r] = s_P[r];
+        a.state[2 * r + 1] = s_M[r];
+        s_pos[r] = a.pos[r];
+        if (a.series) {
+            a.series[((size_t)s * a.nrep + r) * 2] = s_P[r];
+            a.series[((size_t)s * a.nrep + r) * 2 + 1] = s_M[r];
+        }
+    }
+    __syncthreads();
+    if ((t + 1) % (unsigned long long)a.every != 0) return;
+    const int stage = *a.stage;
+    pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, true);
+    for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) a.pos[r] = s_pos[r];
+    if (threadIdx.x == 0) *a.stage = stage ^ 1;
+}
+
+// Bounded wait on a flag nothing sets: the failure-detection path of the barriers,
+// testable without faulting or hanging the GPU.
+__global__ void k_wait_flag(unsigned* flag, long long limit, unsigned* result) {
+    long long n = 0;
+    while (ld_acquire(flag) == 0u) {
+        if (++n > limit) {
+            *result = 1u;
+            return;
+        }
+        __nanosleep(100);
+    }
+    *result = 0u;
+}
+
+}  // namespace mcx
+
+using namespace mcx;
+
+struct mcx_pt {
+    mcx_ctx* ctx = nullptr;
+    int dim = 3;
+    double J = 1, h = 0;
+    int nladders = 0, nrep = 0, npos = 0;
+    std::vector<int> ladder_n, ladder_side, ladder_gpos0, rep_ladder;
+    std::vector<double> betas;
+    std::vector<PTReplica> reps;
+    std::vector<PTTile> tiles;
+    std::vector<int> rep_tile0, rep_ntiles;
+    int64_t sites = 0;
+    size_t arena_bytes = 0;
+    int8_t* d_arena = nullptr;
+    PTReplica* d_reps = nullptr;
+    PTTile* d_tiles = nullptr;
+    int* d_block_tiles = nullptr;
+    int* d_block_off = nullptr;
+    int grid = 0;  // persistent grid size the schedule was built for
+    unsigned long long* d_tables = nullptr;  // [3 algs][npos][16]
+    double* d_betas = nullptr;
+    int* d_pos_ladder = nullptr;
+    int* d_pos_local = nullptr;
+    int* d_ladder_n = nullptr;
+    int32_t* d_pos = nullptr;
+    int32_t* d_stage = nullptr;
+    long long* d_state = nullptr;
+    long long* d_delta = nullptr;
+    unsigned long long* d_acc = nullptr;
+    unsigned long long* d_ex_steps = nullptr;
+    unsigned long long* d_ex_acc = nullptr;
+    long long* d_series = nullptr;
+    int64_t series_cap = 0;
+    unsigned int* d_bar = nullptr;
+    int8_t* d_lin = nullptr;
+    size_t lin_bytes = 0;
+    std::vector<std::pair<void*, size_t>> allocs;
+    long long spin_limit = 1ll << 24;
+};
+
+namespace mcx {
+
+static uint32_t roundup_recip(uint32_t d) { return d <= 1 ? 0u : (uint32_t)(((1ull << 32) + d - 1) / d); }
+
+static mcx_status pt_alloc(mcx_pt* pt, void** p, size_t bytes) {
+    MCX_CHECK(dev_alloc(pt->ctx, p, bytes));
+    pt->allocs.emplace_back(*p, bytes);
+    return MCX_OK;
+}
+
+template <typename T>
+static mcx_status pt_upload(mcx_pt* pt, T** dst, const std::vector<T>& v) {
+    void* p = nullptr;
+    MCX_CHECK(pt_alloc(pt, &p, std::max<size_t>(1, v.size()) * sizeof(T)));
+    if (!v.empty()) MCX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *dst = (T*)p;
+    return MCX_OK;
+}
+
+using PersistentFn = void (*)(const PTArgs);
+using PlainFn = void (*)(const PTArgs, int, int, unsigned long long);
+
+static PersistentFn persistent_fn(int dim, bool hb) {
+    if (dim == 2) return hb ? k_pt_persistent<2, true> : k_pt_persistent<2, false>;
+    return hb ? k_pt_persistent<3, true> : k_pt_persistent<3, false>;
+}
+
+static PlainFn plain_fn(int dim, bool hb) {
+    if (dim == 2) return hb ? k_pt_plain_half<2, true> : k_pt_plain_half<2, false>;
+    return hb ? k_pt_plain_half<3, true> : k_pt_plain_half<3, false>;
+}
+
+static size_t pt_smem(const mcx_pt* pt) {
+    return (size_t)pt->nrep * (2 * sizeof(long long) + sizeof(int)) + (size_t)pt->npos * sizeof(int);
+}
+
+// Longest-processing-time assignment of tiles to `grid` blocks, stored as CSR.
+static mcx_status pt_schedule(mcx_pt* pt, int grid) {
+    std::vector<int> order(pt->tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return pt->tiles[x].sites > pt->tiles[y].sites; });
+    using Item = std::pair<long long, int>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (int b = 0; b < grid; ++b) heap.push({0, b});
+    std::vector<std::vector<int>> per(grid);
+    for (int t : order) {
+        Item it = heap.top();
+        heap.pop();
+        per[it.second].push_back(t);
+        heap.push({it.first + pt->tiles[t].sites, it.second});
+    }
+    std::vector<int> off(grid + 1, 0), list;
+    for (int b = 0; b < grid; ++b) {
+        std::sort(per[b].begin(), per[b].end());
+        off[b + 1] = off[b] + (int)per[b].size();
+        list.insert(list.end(), per[b].begin(), per[b].end());
+    }
+    MCX_CHECK(pt_upload(pt, &pt->d_block_tiles, list));
+    MCX_CHECK(pt_upload(pt, &pt->d_block_off, off));
+    pt->grid = grid;
+    return MCX_OK;
+}
+
+static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
+    std::memset(a, 0, sizeof(*a));
+    a->arena = pt->d_arena;
+    a->reps = pt->d_reps;
+    a->tiles = pt->d_tiles;
+    a->block_tiles = pt->d_block_tiles;
+    a->block_off = pt->d_block_off;
+    a->nrep = pt->nrep;
+    a->npos = pt->npos;
+    a->tables = pt->d_tables + (size_t)alg * pt->npos * 16;
+    a->betas = pt->d_betas;
+    a->pos_ladder = pt->d_pos_ladder;
+    a->pos_local = pt->d_pos_local;
+    a->ladder_n = pt->d_ladder_n;
+    a->pos = pt->d_pos;
+    a->stage = pt->d_stage;
+    a->state = pt->d_state;
+    a->delta = pt->d_delta;
+    a->acc = pt->d_acc;
+    a->ex_steps = pt->d_ex_steps;
+    a->ex_acc = pt->d_ex_acc;
+    a->bar = pt->d_bar;
+    a->J = pt->J;
+    a->h = pt->h;
+    a->spin_limit = pt->spin_limit;
+}
+
+// colour-split layout conversion for one replica (reuses the lattice kernels' rule)
+__global__ void k_pt_scatter(int8_t* __restrict__ lin, int8_t* __restrict__ c0, int8_t* __restrict__ c1,
+                             int Lx, int Ly, int Lz, int W, int to_device) {
+    const long long N = (long long)Lx * Ly * Lz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % Lx);
+        const long long rr = i / Lx;
+        const int y = (int)(rr % Ly), z = (int)(rr / Ly);
+        const long long e = (long long)(y + Ly * z) * W + (x >> 1);
+        int8_t* col = ((x + y + z) & 1) ? c1 : c0;
+        if (to_device) col[e] = lin[i];
+        else lin[i] = col[e];
+    }
+}
+
+__global__ void k_pt_init_random(int8_t* arena, const PTReplica* reps, int nrep, uint32_t k0, uint32_t k1) {
+    const int r = blockIdx.y;
+    if (r >= nrep) return;
+    const PTReplica R = reps[r];
+    const int Lx = 2 * R.W;
+    const long long N = (long long)Lx * R.rows;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % Lx);
+        const long long rr = i / Lx;
+        const int y = (int)(rr % R.Ly), z = (int)(rr / R.Ly);
+        const int c = (x + y + z) & 1;
+        const uint4 w = philox10(make_uint4((uint32_t)(i >> 3), 0u, ctr_word2(0ull, c, P_INIT), (uint32_t)r), k0, k1);
+        const uint32_t u = pick4(w, (int)((i >> 1) & 3));
+        arena[R.off[c] + rr * R.W + (x >> 1)] = (int8_t)((u & 0x80000000u) ? 1 : -1);
+    }
+}
+
+// per-replica (pair_sum, spin_sum) recompute
+__global__ void k_pt_observables(const int8_t* arena, const PTReplica* reps, int nrep, int dim, long long* state) {
+    const int r = blockIdx.y;
+    if (r >= nrep) return;
+    const PTReplica R = reps[r];
+    const int8_t* c0 = arena + R.off[0];
+    const int8_t* c1 = arena + R.off[1];
+    long long P = 0, M = 0;
+    const long long half = (long long)R.W * R.rows;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < half;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int row = (int)(e / R.W), k = (int)(e - (long long)row * R.W);
+        const int y = row % R.Ly, z = row / R.Ly;
+        const int p = (y + z) & 1;
+        const int s = c0[e];
+        const int km = k == 0 ? R.W - 1 : k - 1, kp = k == R.W - 1 ? 0 : k + 1;
+        const long long rb = (long long)row * R.W;
+        int S = c1[rb + k] + c1[rb + (p ? kp : km)];
+        const int yp = y + 1 == R.Ly ? 0 : y + 1, ym = y == 0 ? R.Ly - 1 : y - 1;
+        S += c1[(long long)(yp + R.Ly * z) * R.W + k] + c1[(long long)(ym + R.Ly * z) * R.W + k];
+        if (dim == 3) {
+            const int zp = z + 1 == R.Lz ? 0 : z + 1, zm = z == 0 ? R.Lz - 1 : z - 1;
+            S += c1[(long long)(y + R.Ly * zp) * R.W + k] + c1[(long long)(y + R.Ly * zm) * R.W + k];
+        }
+        P += s * S;
+        M += s + c1[e];
+    }
+    long long v[2] = {P, M};
+    unsigned long long* const dst[2] = {(unsigned long long*)&state[2 * r], (unsigned long long*)&state[2 * r + 1]};
+    block_add_atomic<2>(v, dst);
+}
+
+static mcx_status pt_recompute(mcx_pt* pt) {
+    mcx_ctx* ctx = pt->ctx;
+    MCX_CUDA(cudaMemsetAsync(pt->d_state, 0, (size_t)pt->nrep * 2 * sizeof(long long), ctx->stream));
+    dim3 grid(8, pt->nrep);
+    k_pt_observables<<<grid, 256, 0, ctx->stream>>>(pt->d_arena, pt->d_reps, pt->nrep, pt->dim, pt->d_state);
+    count_launch(ctx);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+}  // namespace mcx
+
+extern "C" {
+
+MCX_API mcx_status mcx_pt_destroy(mcx_pt* pt) {
+    if (!pt) return MCX_OK;
+    cudaStreamSynchronize(pt->ctx->stream);
+    for (auto& a : pt->allocs) dev_free(pt->ctx, a.first, a.second);
+    delete pt;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int32_t* sides,
+                                 const int32_t* nreplicas, const double* betas, double J, double h,
+                                 mcx_pt** out) {
+    if (!ctx || !sides || !nreplicas || !betas || !out) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return fail(MCX_ERR_INVALID_ARG, "dim must be 2 or 3");
+    if (nladders < 1) return fail(MCX_ERR_INVALID_ARG, "need at least one ladder");
+    if (!std::isfinite(J) || !std::isfinite(h)) return fail(MCX_ERR_INVALID_ARG, "J and h must be finite");
+    mcx_pt* pt = new mcx_pt();
+    pt->ctx = ctx;
+    pt->dim = dim;
+    pt->J = J;
+    pt->h = h;
+    pt->nladders = nladders;
+    std::vector<int> pos_ladder, pos_local;
+    for (int l = 0; l < nladders; ++l) {
+        const int L = sides[l], n = nreplicas[l];
+        if (n < 2) {
+            delete pt;
+            return fail(MCX_ERR_INVALID_ARG, "ladder %d: need at least 2 replicas", l);
+        }
+        if (L < 8 || L % 8) {
+            delete pt;
+            return fail(MCX_ERR_INVALID_ARG, "ladder %d: side %d must be a multiple of 8", l, L);
+        }
+        pt->ladder_n.push_back(n);
+        pt->ladder_side.push_back(L);
+        pt->ladder_gpos0.push_back(pt->npos);
+        for (int p = 0; p < n; ++p) {
+            const double b = betas[pt->npos + p];
+            if (!std::isfinite(b)) {
+                delete pt;
+                return fail(MCX_ERR_INVALID_ARG, "beta must be finite");
+            }
+            pt->betas.push_back(b);
+            pos_ladder.push_back(l);
+            pos_local.push_back(p);
+            pt->rep_ladder.push_back(l);
+        }
+        pt->npos += n;
+    }
+    pt->nrep = pt->npos;
+    if (pt->nrep > 2048) {
+        delete pt;
+        return fail(MCX_ERR_INVALID_ARG, "at most 2048 replicas");
+    }
+    // arena layout: replica r (ladder order), colour 0 then colour 1, 256-byte aligned
+    size_t off = 0;
+    for (int r = 0; r < pt->nrep; ++r) {
+        const int l = pt->rep_ladder[r];
+        const int L = pt->ladder_side[l];
+        PTReplica R;
+        std::memset(&R, 0, sizeof(R));
+        R.W = L / 2;
+        R.Ly = L;
+        R.Lz = dim == 3 ? L : 1;
+        R.rows = R.Ly * R.Lz;
+        R.V = R.W % 16 == 0 ? 16 : (R.W % 8 == 0 ? 8 : 4);
+        R.cpr = R.W / R.V;
+        R.ladder = l;
+        R.gpos0 = pt->ladder_gpos0[l];
+        R.n = pt->ladder_n[l];
+        R.m_cpr = roundup_recip((uint32_t)R.cpr);
+        R.m_Ly = roundup_recip((uint32_t)R.Ly);
+        const size_t half = (size_t)R.W * R.rows;
+        R.off[0] = (long long)off;
+        off += (half + 255) / 256 * 256;
+        R.off[1] = (long long)off;
+        off += (half + 255) / 256 * 256;
+        pt->sites += 2 * (int64_t)half;
+        pt->lin_bytes = std::max(pt->lin_bytes, 2 * half);
+        pt->reps.push_back(R);
+        // tiles of ~4096 same-colour sites
+        const int nchunks = R.cpr * R.rows;
+        const int per = 256 * (16 / R.V);
+        pt->rep_tile0.push_back((int)pt->tiles.size());
+        for (int c = 0; c < nchunks; c += per) {
+            PTTile t;
+            t.rep = r;
+            t.c_begin = c;
+            t.c_end = std::min(nchunks, c + per);
+            t.sites = (t.c_end - t.c_begin) * R.V;
+            pt->tiles.push_back(t);
+        }
+        pt->rep_ntiles.push_back((int)pt->tiles.size() - pt->rep_tile0.back());
+    }
+    pt->arena_bytes = off;
+    mcx_status st = MCX_OK;
+    auto run = [&](mcx_status s) {
+        if (st == MCX_OK) st = s;
+    };
+    void* p = nullptr;
+    run(pt_alloc(pt, &p, pt->arena_bytes));
+    pt->d_arena = (int8_t*)p;
+    run(pt_upload(pt, &pt->d_reps, pt->reps));
+    run(pt_upload(pt, &pt->d_tiles, pt->tiles));
+    run(pt_upload(pt, &pt->d_betas, pt->betas));
+    run(pt_upload(pt, &pt->d_pos_ladder, pos_ladder));
+    run(pt_upload(pt, &pt->d_pos_local, pos_local));
+    run(pt_upload(pt, &pt->d_ladder_n, pt->ladder_n));
+    // acceptance tables for the three algorithms at every ladder position
+    std::vector<unsigned long long> tabs((size_t)3 * pt->npos * 16, 0);
+    for (int alg = 0; alg < 3 && st == MCX_OK; ++alg)
+        for (int gp = 0; gp < pt->npos; ++gp) {
+            Table t;
+            run(build_ising_table(dim, (mcx_algorithm)alg, pt->betas[gp], J, h, &t));
+            for (int i = 0; i < t.n; ++i) tabs[((size_t)alg * pt->npos + gp) * 16 + i] = t.thr[i];
+        }
+    run(pt_upload(pt, &pt->d_tables, tabs));
+    std::vector<int32_t> pos0(pt->nrep);
+    for (int r = 0; r < pt->nrep; ++r) pos0[r] = r - pt->ladder_gpos0[pt->rep_ladder[r]];
+    run(pt_upload(pt, &pt->d_pos, pos0));
+    run(pt_upload(pt, &pt->d_stage, std::vector<int32_t>(1, 0)));
+    run(pt_upload(pt, &pt->d_state, std::vector<long long>((size_t)pt->nrep * 2, 0)));
+    run(pt_upload(pt, &pt->d_delta, std::vector<long long>((size_t)pt->nrep * 6, 0)));
+    run(pt_upload(pt, &pt->d_acc, std::vector<unsigned long long>(pt->nrep, 0)));
+    run(pt_upload(pt, &pt->d_ex_steps, std::vector<unsigned long long>(pt->npos, 0)));
+    run(pt_upload(pt, &pt->d_ex_acc, std::vector<unsigned long long>(pt->npos, 0)));
+    run(pt_upload(pt, &pt->d_bar, std::vector<unsigned int>(4, 0)));
+    run(pt_alloc(pt, &p, pt->lin_bytes));
+    pt->d_lin = (int8_t*)p;
+    if (st == MCX_OK) {
+        // schedule for the persistent grid
+        int bps = 0;
+        const size_t smem = pt_smem(pt);
+        const PersistentFn fn = persistent_fn(dim, false);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(persistent_fn(dim, true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_pt_plain_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, smem) != cudaSuccess || bps < 1) bps = 1;
+        int grid = ctx->num_sms * bps;
+        if (grid > (int)pt->tiles.size()) grid = (int)pt->tiles.size();
+        run(pt_schedule(pt, grid));
+    }
+    if (st == MCX_OK) {
+        // all spins up, like the reference constructors
+        MCX_CUDA(cudaMemset(pt->d_arena, 1, pt->arena_bytes));
+        run(pt_recompute(pt));
+    }
+    if (st != MCX_OK) {
+        mcx_pt_destroy(pt);
+        return st;
+    }
+    *out = pt;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_info(const mcx_pt* pt, int32_t* nreplicas, int64_t* sites, int64_t* device_bytes) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (nreplicas) *nreplicas = pt->nrep;
+    if (sites) *sites = pt->sites;
+    if (device_bytes) {
+        int64_t b = 0;
+        for (auto& a : pt->allocs) b += (int64_t)a.second;
+        *device_bytes = b;
+    }
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_init_random(mcx_pt* pt, uint64_t seed) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    mcx_ctx* ctx = pt->ctx;
+    dim3 grid(16, pt->nrep);
+    k_pt_init_random<<<grid, 256, 0, ctx->stream>>>(pt->d_arena, pt->d_reps, pt->nrep, (uint32_t)seed,
+                                                     (uint32_t)(seed >> 32));
+    count_launch(ctx);
+    MCX_CUDA(cudaGetLastError());
+    return pt_recompute(pt);
+}
+
+static mcx_status pt_copy_spins(mcx_pt* pt, int32_t r, int8_t* host, size_t n, bool to_device) {
+    if (!pt || !host) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (r < 0 || r >= pt->nrep) return fail(MCX_ERR_INVALID_ARG, "replica %d out of range", r);
+    const PTReplica& R = pt->reps[r];
+    const size_t N = (size_t)2 * R.W * R.rows;
+    if (n != N) return fail(MCX_ERR_INVALID_ARG, "replica %d has %zu sites, got %zu", r, N, n);
+    mcx_ctx* ctx = pt->ctx;
+    if (to_device) {
+        for (size_t i = 0; i < n; ++i)
+            if (host[i] != 1 && host[i] != -1) return fail(MCX_ERR_INVALID_ARG, "spin %zu is %d", i, (int)host[i]);
+        MCX_CUDA(cudaMemcpyAsync(pt->d_lin, host, n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    k_pt_scatter<<<64, 256, 0, ctx->stream>>>(pt->d_lin, pt->d_arena + R.off[0], pt->d_arena + R.off[1], 2 * R.W,
+                                              R.Ly, R.Lz, R.W, to_device ? 1 : 0);
+    count_launch(ctx);
+    MCX_CUDA(cudaGetLastError());
+    if (to_device) return pt_recompute(pt);
+    MCX_CUDA(cudaMemcpyAsync(host, pt->d_lin, n, cudaMemcpyDeviceToHost, ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_set_spins(mcx_pt* pt, int32_t replica, const int8_t* host, size_t n) {
+    return pt_copy_spins(pt, replica, const_cast<int8_t*>(host), n, true);
+}
+
+MCX_API mcx_status mcx_pt_get_spins(mcx_pt* pt, int32_t replica, int8_t* host, size_t n) {
+    return pt_copy_spins(pt, replica, host, n, false);
+}
+
+MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64_t nsweeps,
+                              int32_t exchange_every, mcx_pt_mode mode, int64_t* series) {
+    if (!pt || !rng) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (alg != MCX_METROPOLIS && alg != MCX_GLAUBER && alg != MCX_HEATBATH)
+        return fail(MCX_ERR_INVALID_ARG, "unknown algorithm");
+    if (nsweeps < 0 || exchange_every < 1) return fail(MCX_ERR_INVALID_ARG, "nsweeps >= 0 and exchange_every >= 1");
+    if (mode != MCX_PT_PERSISTENT && mode != MCX_PT_PLAIN) return fail(MCX_ERR_INVALID_ARG, "unknown mode");
+    if (rng->counter + (uint64_t)nsweeps >= (1ull << 48)) return fail(MCX_ERR_INVALID_ARG, "sweep counter beyond 2^48");
+    if (nsweeps == 0) return MCX_OK;
+    mcx_ctx* ctx = pt->ctx;
+    if (series) {
+        if (nsweeps > pt->series_cap) {
+            void* p = nullptr;
+            MCX_CHECK(dev_alloc(ctx, &p, (size_t)nsweeps * pt->nrep * 2 * sizeof(long long)));
+            for (auto it = pt->allocs.begin(); it != pt->allocs.end(); ++it)
+                if (it->first == pt->d_series) {
+                    dev_free(ctx, it->first, it->second);
+                    pt->allocs.erase(it);
+                    break;
+                }
+            pt->allocs.emplace_back(p, (size_t)nsweeps * pt->nrep * 2 * sizeof(long long));
+            pt->d_series = (long long*)p;
+            pt->series_cap = nsweeps;
+        }
+    }
+    PTArgs a;
+    pt_args(pt, &a, alg);
+    a.series = series ? pt->d_series : nullptr;
+    a.k0 = (uint32_t)rng->seed;
+    a.k1 = (uint32_t)(rng->seed >> 32);
+    a.sweep0 = rng->counter;
+    a.nsweeps = nsweeps;
+    a.every = exchange_every;
+    const bool hb = alg == MCX_HEATBATH;
+    const size_t smem = pt_smem(pt);
+    MCX_CUDA(cudaMemsetAsync(pt->d_acc, 0, (size_t)pt->nrep * sizeof(unsigned long long), ctx->stream));
+    if (mode == MCX_PT_PERSISTENT) {
+        MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 6 * sizeof(long long), ctx->stream));
+        MCX_CUDA(cudaMemsetAsync(pt->d_bar, 0, sizeof(unsigned int), ctx->stream));
+        MCX_CUDA(cudaMemsetAsync(pt->d_bar + 2, 0, sizeof(unsigned int), ctx->stream));
+        const PersistentFn fn = persistent_fn(pt->dim, hb);
+        void* args[] = {&a};
+        MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem, ctx->stream));
+        count_launch(ctx);
+        unsigned int err = 0;
+        MCX_CUDA(cudaMemcpyAsync(&err, pt->d_bar + 2, sizeof(err), cudaMemcpyDeviceToHost, ctx->stream));
+        MCX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (err) return fail(MCX_ERR_TIMEOUT, "grid barrier wait exceeded its limit");
+    } else {
+        MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 2 * sizeof(long long), ctx->stream));
+        const PlainFn fn = plain_fn(pt->dim, hb);
+        for (int64_t s = 0; s < nsweeps; ++s) {
+            const unsigned long long t = rng->counter + (unsigned long long)s;
+            for (int r = 0; r < pt->nrep; ++r)
+                for (int c = 0; c < 2; ++c)
+                    fn<<<pt->rep_ntiles[r], 256, 0, ctx->stream>>>(a, pt->rep_tile0[r], c, t);
+            k_pt_plain_exchange<<<1, 256, smem, ctx->stream>>>(a, s, t);
+        }
+        count_launch(ctx, (uint64_t)nsweeps * (2 * pt->nrep + 1));
+        MCX_CUDA(cudaGetLastError());
+    }
+    rng->counter += (uint64_t)nsweeps;
+    if (series) {
+        MCX_CUDA(cudaMemcpyAsync(series, pt->d_series, (size_t)nsweeps * pt->nrep * 2 * sizeof(long long),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+        MCX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_indices(mcx_pt* pt, int32_t* pos, int32_t* stage) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (pos) MCX_CUDA(cudaMemcpyAsync(pos, pt->d_pos, pt->nrep * sizeof(int32_t), cudaMemcpyDeviceToHost, pt->ctx->stream));
+    if (stage) MCX_CUDA(cudaMemcpyAsync(stage, pt->d_stage, sizeof(int32_t), cudaMemcpyDeviceToHost, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_exchange_counters(mcx_pt* pt, uint64_t* steps, uint64_t* accepted) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    std::vector<unsigned long long> s(pt->npos), a(pt->npos);
+    MCX_CUDA(cudaMemcpyAsync(s.data(), pt->d_ex_steps, pt->npos * 8, cudaMemcpyDeviceToHost, pt->ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(a.data(), pt->d_ex_acc, pt->npos * 8, cudaMemcpyDeviceToHost, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    // edges of ladder l are its positions 0..n_l-2, packed ladder after ladder
+    int k = 0;
+    for (int l = 0; l < pt->nladders; ++l)
+        for (int p = 0; p + 1 < pt->ladder_n[l]; ++p, ++k) {
+            if (steps) steps[k] = s[pt->ladder_gpos0[l] + p];
+            if (accepted) accepted[k] = a[pt->ladder_gpos0[l] + p];
+        }
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_observables(mcx_pt* pt, int64_t* pair_sum, int64_t* spin_sum) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    std::vector<long long> st((size_t)pt->nrep * 2);
+    MCX_CUDA(cudaMemcpyAsync(st.data(), pt->d_state, st.size() * 8, cudaMemcpyDeviceToHost, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    for (int r = 0; r < pt->nrep; ++r) {
+        if (pair_sum) pair_sum[r] = st[2 * r];
+        if (spin_sum) spin_sum[r] = st[2 * r + 1];
+    }
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_replica_accepted(mcx_pt* pt, uint64_t* accepted) {
+    if (!pt || !accepted) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    MCX_CUDA(cudaMemcpyAsync(accepted, pt->d_acc, pt->nrep * 8, cudaMemcpyDeviceToHost, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls) {
+    if (!pt || polls < 1) return fail(MCX_ERR_INVALID_ARG, "bad argument");
+    pt->spin_limit = polls;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls) {
+    if (!ctx || polls < 1) return fail(MCX_ERR_INVALID_ARG, "bad argument");
+    void* p = nullptr;
+    MCX_CHECK(dev_alloc(ctx, &p, 2 * sizeof(unsigned int)));
+    unsigned int* d = (unsigned int*)p;
+    unsigned int res = 2;
+    cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned int), ctx->stream);
+    if (e == cudaSuccess) {
+        k_wait_flag<<<1, 1, 0, ctx->stream>>>(d, polls, d + 1);
+        count_launch(ctx);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&res, d + 1, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, p, 2 * sizeof(unsigned int));
+    if (e != cudaSuccess) return cuda_fail(e, "wait-flag test");
+    return res == 1 ? fail(MCX_ERR_TIMEOUT, "flag wait exceeded %lld polls", (long long)polls) : MCX_OK;
+}
+
+}  // extern "C"

@@ -10,104 +10,18 @@
 // Per-sweep energy / magnetisation deltas are reduced per block (warp shuffles)
 // and added with one 64-bit atomic per block into the sweep's slot of the series.
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
 #include "mcx_sweep.cuh"
+#include "mcx_cb.cuh"
 
 namespace mcx {
 
-__device__ __forceinline__ uint32_t upbits(uint32_t w) { return (~w >> 1) & 0x01010101u; }
-// per byte: v + 1 for v in {-1, 0, +1}
-__device__ __forceinline__ uint32_t plus1(uint32_t w) {
-    return ((w & 0x7F7F7F7Fu) + 0x01010101u) & 0x03030303u;
-}
-
-template <int V>
-__device__ __forceinline__ void load_row(const int8_t* p, uint32_t (&w)[V / 4]) {
-    if constexpr (V == 16) {
-        const uint4 v = *reinterpret_cast<const uint4*>(p);
-        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
-    } else {
-        w[0] = *reinterpret_cast<const uint32_t*>(p);
-    }
-}
-
-template <int V>
-__device__ __forceinline__ void store_row(int8_t* p, const uint32_t (&w)[V / 4]) {
-    if constexpr (V == 16) {
-        *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
-    } else {
-        *reinterpret_cast<uint32_t*>(p) = w[0];
-    }
-}
-
-__device__ __forceinline__ int bc_propose(int so, int bit) {
-    return bit ? (so == -1 ? 0 : -1) : (so == 1 ? 0 : 1);
-}
-
-// Row bookkeeping shared by all kernels: neighbour rows and the in-row parity.
-struct RowInfo {
-    int p;                   // (y + z + colour) & 1
-    long long ryp, rym, rzp, rzm;
-};
-
-__device__ __forceinline__ RowInfo row_info(int r, int Ly, int Lz, int colour, int dim) {
-    RowInfo ri;
-    const int y = r % Ly, z = r / Ly;
-    ri.p = (y + z + colour) & 1;
-    ri.ryp = (long long)((y + 1 == Ly ? 0 : y + 1) + Ly * z);
-    ri.rym = (long long)((y == 0 ? Ly - 1 : y - 1) + Ly * z);
-    if (dim == 3) {
-        ri.rzp = (long long)(y + Ly * (z + 1 == Lz ? 0 : z + 1));
-        ri.rzm = (long long)(y + Ly * (z == 0 ? Lz - 1 : z - 1));
-    } else {
-        ri.rzp = ri.rzm = 0;
-    }
-    return ri;
-}
-
-// Gathers the V-site word groups of one chunk: own spins and the 2*DIM neighbour
-// words, with `side` the in-row neighbour shifted by one site.
-template <int DIM, int V>
-struct Chunk {
-    static constexpr int NW = V / 4;
-    uint32_t own[NW];
-    uint32_t nb[2 * DIM][NW];
-
-    __device__ __forceinline__ void load(const int8_t* cur, const int8_t* oth, int W, int r, int k0,
-                                         const RowInfo& ri) {
-        const long long base = (long long)r * W + k0;
-        load_row<V>(cur + base, own);
-        uint32_t mid[NW];
-        load_row<V>(oth + base, mid);
-        load_row<V>(oth + ri.ryp * W + k0, nb[1]);
-        load_row<V>(oth + ri.rym * W + k0, nb[2]);
-        if constexpr (DIM == 3) {
-            load_row<V>(oth + ri.rzp * W + k0, nb[4]);
-            load_row<V>(oth + ri.rzm * W + k0, nb[5]);
-        }
-        if (ri.p == 0) {
-            const int ke = k0 == 0 ? W - 1 : k0 - 1;
-            const uint32_t edge = (uint32_t)(uint8_t)oth[(long long)r * W + ke];
-#pragma unroll
-            for (int w = 0; w < NW; ++w)
-                nb[3][w] = __funnelshift_l(w == 0 ? (edge << 24) : mid[w - 1], mid[w], 8);
-        } else {
-            const int ke = k0 + V == W ? 0 : k0 + V;
-            const uint32_t edge = (uint32_t)(uint8_t)oth[(long long)r * W + ke];
-#pragma unroll
-            for (int w = 0; w < NW; ++w)
-                nb[3][w] = __funnelshift_r(mid[w], w == NW - 1 ? edge : mid[w + 1], 8);
-        }
-#pragma unroll
-        for (int w = 0; w < NW; ++w) nb[0][w] = mid[w];
-    }
-};
-
-// ------------------------------------------------------------------ Ising --
 template <int DIM, int V, bool HB>
-__global__ void __launch_bounds__(256) k_ising_cb(const SweepArgs a) {
+__global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int NT = 2 * (Z + 1);
     constexpr int NW = V / 4;
@@ -115,44 +29,31 @@ __global__ void __launch_bounds__(256) k_ising_cb(const SweepArgs a) {
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
     const int cpr = a.W / V;
-    const long long nchunk = (long long)cpr * a.rows;
     const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
-    int nacc = 0, asum = 0, nup = 0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nchunk;
-         g += (long long)gridDim.x * blockDim.x) {
-        const int r = (int)(g / cpr);
-        const int k0 = (int)(g - (long long)r * cpr) * V;
-        const RowInfo ri = row_info(r, a.Ly, a.Lz, a.colour, DIM);
+    int nacc = 0, isum = 0, nup = 0;
+    for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
+                      a.Ly, a.Lz);
+         it.valid(); it.next()) {
+        const int r = it.row();
+        const int k0 = it.q * V;
+        const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
-        const unsigned long long j0 = (unsigned long long)r * a.W + k0;
+        const uint32_t c0 = (uint32_t)(((unsigned long long)r * a.W + k0) >> 2);
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
-            uint32_t cnt = 0;
+            uint32_t nbw[Z];
 #pragma unroll
-            for (int d = 0; d < Z; ++d) cnt += upbits(ch.nb[d][w]);
-            const uint32_t ob = upbits(ch.own[w]);
-            const uint4 rnd = philox10(make_uint4((uint32_t)(j0 >> 2) + w, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
-            uint32_t fm = 0;
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int n = (cnt >> (8 * b)) & 0xFF;
-                const int up = (ob >> (8 * b)) & 1;
-                const int al = up ? n : Z - n;
-                uint32_t u = b == 0 ? rnd.x : b == 1 ? rnd.y : b == 2 ? rnd.z : rnd.w;
-                if (HB && up) u = ~u;
-                if ((unsigned long long)u < s_thr[al + (Z + 1) * up]) {
-                    fm |= 0xFEu << (8 * b);
-                    ++nacc;
-                    asum += al;
-                    nup += up;
-                }
-            }
-            ch.own[w] ^= fm;
+            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
+            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
+            const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
+            ch.own[w] ^= fb * 0xFEu;
         }
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
-    long long v[3] = {2ll * Z * nacc - 4ll * asum, 2ll * nacc - 4ll * nup, (long long)nacc};
+    long long dP, dM;
+    ising_deltas<Z>(nacc, nup, isum, dP, dM);
+    long long v[3] = {dP, dM, (long long)nacc};
     unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
     block_add_atomic<3>(v, dst);
 }
@@ -195,7 +96,7 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
 
 // ------------------------------------------------------------ Blume-Capel --
 template <int DIM, int V, bool HB>
-__global__ void __launch_bounds__(256) k_bc_cb(const SweepArgs a) {
+__global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int NC = 2 * Z + 1;
     constexpr int NT = HB ? 2 * NC : 6 * NC;
@@ -204,15 +105,15 @@ __global__ void __launch_bounds__(256) k_bc_cb(const SweepArgs a) {
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
     const int cpr = a.W / V;
-    const long long nchunk = (long long)cpr * a.rows;
     const uint32_t w2a = ctr_word2(a.sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(a.sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nchunk;
-         g += (long long)gridDim.x * blockDim.x) {
-        const int r = (int)(g / cpr);
-        const int k0 = (int)(g - (long long)r * cpr) * V;
-        const RowInfo ri = row_info(r, a.Ly, a.Lz, a.colour, DIM);
+    for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
+                      a.Ly, a.Lz);
+         it.valid(); it.next()) {
+        const int r = it.row();
+        const int k0 = it.q * V;
+        const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
         const unsigned long long j0 = (unsigned long long)r * a.W + k0;
@@ -327,12 +228,30 @@ HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V) 
 
 int vec_width(int64_t W) { return W % 16 == 0 ? 16 : (W % 4 == 0 ? 4 : 1); }
 
-int half_sweep_grid(const mcx_ctx* ctx, int64_t W, int64_t rows, int V) {
-    const long long work = (long long)(W / V) * rows;
-    long long g = (work + 255) / 256;
-    const long long cap = (long long)ctx->num_sms * 8;
+// Grid = min(work, SMs x resident blocks per SM): one wave of a grid-stride kernel.
+int occupancy_grid(const mcx_ctx* ctx, const void* fn, long long work, int block, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> cache;
+    int bps = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto key = std::make_pair(fn, block);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            bps = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, block, smem) != cudaSuccess) bps = 1;
+            cache[key] = bps;
+        }
+    }
+    long long g = (work + block - 1) / block;
+    const long long cap = (long long)ctx->num_sms * (bps > 0 ? bps : 1);
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
+}
+
+int half_sweep_grid(const mcx_ctx* ctx, HalfSweepFn fn, int64_t W, int64_t rows, int V) {
+    return occupancy_grid(ctx, (const void*)fn, (long long)(W / V) * rows, 256, 0);
 }
 
 mcx_status build_table(const mcx_lattice* lat, mcx_algorithm alg, double beta, Table* t) {
@@ -381,7 +300,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         a.acc = lat->d_acc;
         const int V = vec_width(lat->W);
         const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
-        const int grid = half_sweep_grid(ctx, lat->W, lat->rows, V);
+        const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         for (int64_t s = 0; s < nsweeps; ++s) {
             a.sweep = rng->counter + (uint64_t)s;
             for (int c = 0; c < 2; ++c) {

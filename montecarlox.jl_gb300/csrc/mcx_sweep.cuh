@@ -22,7 +22,8 @@ using HalfSweepFn = void (*)(const SweepArgs);
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V);
 int vec_width(int64_t W);
-int half_sweep_grid(const mcx_ctx* ctx, int64_t W, int64_t rows, int V);
+int half_sweep_grid(const mcx_ctx* ctx, HalfSweepFn fn, int64_t W, int64_t rows, int V);
+int occupancy_grid(const mcx_ctx* ctx, const void* fn, long long work, int block, size_t smem);
 mcx_status build_table(const mcx_lattice* lat, mcx_algorithm alg, double beta, Table* t);
 void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const mcx_rng* rng);
 

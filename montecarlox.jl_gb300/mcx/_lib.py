@@ -70,7 +70,36 @@ SIGNATURES = {
     "mcx_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P,
                             C.POINTER(mcx_counters)]),
     "mcx_read_series": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_create": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(_P)]),
+    "mcx_flathist_destroy": (C.c_int, [_P]),
+    "mcx_flathist_set_logweight": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_get_logweight": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_set_histogram": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_get_histogram": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_reset": (C.c_int, [_P]),
+    "mcx_flathist_update_muca": (C.c_int, [_P]),
+    "mcx_flathist_flatness": (C.c_int, [_P, C.c_double, C.POINTER(C.c_int), _f64p]),
+    "mcx_flathist_merge": (C.c_int, [_P, C.POINTER(_P), C.c_int]),
+    "mcx_flathist_copy_logweight": (C.c_int, [_P, _P]),
+    "mcx_flathist_sweep": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P), C.c_int, C.c_int, C.c_double,
+                                     C.POINTER(mcx_rng), C.c_int64, C.POINTER(mcx_counters)]),
+    "mcx_pt_create": (C.c_int, [_P, C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_double, C.c_double,
+                                C.POINTER(_P)]),
+    "mcx_pt_destroy": (C.c_int, [_P]),
+    "mcx_pt_info": (C.c_int, [_P, _i32p, _i64p, _i64p]),
+    "mcx_pt_init_random": (C.c_int, [_P, C.c_uint64]),
+    "mcx_pt_set_spins": (C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    "mcx_pt_get_spins": (C.c_int, [_P, C.c_int32, _P, C.c_size_t]),
+    "mcx_pt_run": (C.c_int, [_P, C.c_int, C.POINTER(mcx_rng), C.c_int64, C.c_int32, C.c_int, _P]),
+    "mcx_pt_indices": (C.c_int, [_P, _P, _i32p]),
+    "mcx_pt_exchange_counters": (C.c_int, [_P, _P, _P]),
+    "mcx_pt_observables": (C.c_int, [_P, _P, _P]),
+    "mcx_pt_replica_accepted": (C.c_int, [_P, _P]),
+    "mcx_pt_set_wait_limit": (C.c_int, [_P, C.c_int64]),
+    "mcx_wait_flag_test": (C.c_int, [_P, C.c_int64]),
 }
+
+PT_PERSISTENT, PT_PLAIN = 0, 1
 
 _lib = None
 

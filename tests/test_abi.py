@@ -74,3 +74,15 @@ def test_algorithm_objects(mcxlib):
     assert mcxlib.acceptance_rate(m) == 0.4
     mcxlib.reset_(m)
     assert m.steps == 0 and m.accepted == 0
+
+
+def test_set_betas(mcxlib):
+    # test/test_parallel_ensembles.jl:164-170
+    from mcx.pt import set_betas
+    assert set_betas(4, 0.4, 1.0, ":uniform") == [1.0, 0.8, 0.6, 0.4]
+    b2 = set_betas(4, 0.5, 1.0, ":geometric")
+    assert abs(b2[0] - 1.0) < 1e-15 and abs(b2[-1] - 0.5) < 1e-15
+    with pytest.raises(mcxlib.ArgumentError):
+        set_betas(1, 0.1, 0.2, ":uniform")
+    with pytest.raises(mcxlib.ArgumentError):
+        set_betas(4, 0.1, 0.2, ":linear")

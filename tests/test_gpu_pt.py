@@ -1,0 +1,90 @@
+"""Batched parallel tempering on the device against the oracle (GPU)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ALG = {"metropolis": O.METROPOLIS, "glauber": O.GLAUBER, "heatbath": O.HEATBATH}
+
+
+def oracle_pt(ladders, dim, alg, seed, nsweeps, every, J=1.0, h=0.0):
+    reps = [(L, l, k) for l, (L, b) in enumerate(ladders) for k in range(len(b))]
+    spins = [O.init_random(O.ISING, [L] * dim, seed, r) for r, (L, l, k) in enumerate(reps)]
+    pos = [np.arange(len(b), dtype=np.int32) for _, b in ladders]
+    steps = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
+    acc = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
+    stage = 0
+    series = np.zeros((nsweeps, len(reps), 2), np.int64)
+    for t in range(nsweeps):
+        for r, (L, l, k) in enumerate(reps):
+            beta = ladders[l][1][pos[l][k]]
+            O.cb_sweep(spins[r], O.ISING, [L] * dim, ALG[alg], beta, seed, stream=r, sweep0=t, nsweeps=1, J=J, h=h,
+                       record=False)
+            P, M, _ = O.observables(spins[r], [L] * dim)
+            series[t, r] = (P, M)
+        if (t + 1) % every == 0:
+            new_stage = stage
+            first = 0
+            for l, (L, b) in enumerate(ladders):
+                idx = [r for r, rr in enumerate(reps) if rr[1] == l]
+                x = np.array([(-(J * float(series[t, r, 0]))) - (h * float(series[t, r, 1])) for r in idx])
+                new_stage = O.pt_exchange(np.array(b), pos[l], stage, x, seed, l, t, steps[l], acc[l])
+            stage = new_stage
+    positions = np.concatenate(pos)
+    return spins, series, positions, stage, np.concatenate(steps), np.concatenate(acc)
+
+
+CASES = [
+    (3, [(8, [0.25, 0.235, 0.22]), (16, [0.25, 0.24, 0.23, 0.2])], "metropolis", 7, 1),
+    (3, [(24, [0.23, 0.22, 0.21]), (48, [0.22, 0.2])], "glauber", 5, 1),
+    (2, [(16, [0.6, 0.5, 0.45, 0.4, 0.3]), (32, [0.5, 0.44])], "heatbath", 8, 2),
+    (2, [(64, [0.45, 0.44, 0.43, 0.42]), (8, [0.9, 0.1])], "metropolis", 9, 1),
+]
+
+
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("dim,ladders,alg,nsweeps,every", CASES)
+def test_pt_parity(gpu, mode, dim, ladders, alg, nsweeps, every):
+    from mcx.pt import ParallelTempering
+    seed = 123
+    pt = ParallelTempering(ladders, dim=dim, seed=seed)
+    pt.init_(seed)
+    series = pt.sweep_(nsweeps, alg=alg, exchange_every=every, mode=mode, record=True)
+    spins, oseries, opos, ostage, osteps, oacc = oracle_pt(ladders, dim, alg, seed, nsweeps, every)
+    assert np.array_equal(series, oseries)
+    assert np.array_equal(pt.positions, opos)
+    assert pt.stage == ostage
+    s, a = pt.counters()
+    assert np.array_equal(s, osteps) and np.array_equal(a, oacc)
+    for r in range(pt.nrep):
+        assert np.array_equal(pt.spins(r), spins[r]), r
+    P, M = pt.observables()
+    assert np.array_equal(P, oseries[-1, :, 0]) and np.array_equal(M, oseries[-1, :, 1])
+
+
+def test_pt_runs_compose(gpu):
+    """3 + 4 sweeps in two calls equal 7 sweeps in one (stage and counters carry over)."""
+    from mcx.pt import ParallelTempering
+    lad = [(16, [0.25, 0.23, 0.21]), (8, [0.3, 0.2])]
+    a = ParallelTempering(lad, dim=3, seed=5)
+    a.init_(5)
+    a.sweep_(3)
+    a.sweep_(4, mode="plain")
+    b = ParallelTempering(lad, dim=3, seed=5)
+    b.init_(5)
+    b.sweep_(7)
+    assert np.array_equal(a.positions, b.positions) and a.stage == b.stage
+    assert np.array_equal(a.counters()[1], b.counters()[1])
+    for r in range(a.nrep):
+        assert np.array_equal(a.spins(r), b.spins(r))
+
+
+def test_bounded_wait_reports_timeout(gpu):
+    """A device wait on a flag nothing sets gives up and reports, context intact."""
+    ctx = gpu.default_context()
+    with pytest.raises(gpu.DeviceTimeoutError):
+        gpu._check(gpu._lib.load().mcx_wait_flag_test(ctx.handle, 1000))
+    sys_ = gpu.Ising([8, 8])
+    assert gpu.energy(sys_) == -128
