@@ -245,6 +245,31 @@ MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls);
  * returns MCX_ERR_TIMEOUT after `polls` polls, with the context still usable. */
 MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls);
 
+/* ----------------------------------------------------------- no allocation -- */
+/* mcx_sweep_noalloc has no counterpart in the reference.  It runs the same sweeps as
+ * mcx_sweep for callers that must not have device memory allocated during the call:
+ * programs whose GPU memory all belongs to another allocator (CUDA.jl's pool in Julia,
+ * PyTorch's caching allocator) or a service that reserved its HBM up front.  For them
+ * a library-side cudaMalloc bypasses the owner's accounting and can fail at run time,
+ * and cudaFree waits for the whole device.  This call uses no cudaMalloc, cudaFree or
+ * other allocating routine: its scratch (the per-sweep partial sums and the accepted
+ * counter) is one fixed device array of MCX_NOALLOC_MAX_SWEEPS sweeps (96 KiB) that
+ * every GPU which loads the library holds until the process exits; a call with more
+ * sweeps returns MCX_ERR_INVALID_ARG.  int8 lattices only.
+ *   obs_series_dev: caller-owned device int64[nsweeps*3], written with the per-sweep
+ *                   (pair_sum, spin_sum, spin2_sum), or NULL.
+ *   accepted_dev:   caller-owned device uint64, set to this call's accepted moves, or NULL.
+ * The call only enqueues work on the context stream; the lattice's cached bookkeeping
+ * (mcx_observables) is updated, mcx_read_series is not.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call shares the array and clears the part it
+ * uses; calls whose work overlaps on the GPU (other streams or contexts on the same
+ * device) race on it and must be serialized by the caller. */
+#define MCX_NOALLOC_MAX_SWEEPS 4096
+MCX_API mcx_status mcx_sweep_noalloc(mcx_lattice* lat, mcx_algorithm alg, double beta,
+                                     mcx_rng* rng, int64_t nsweeps, int64_t* obs_series_dev,
+                                     uint64_t* accepted_dev);
+
 #ifdef __cplusplus
 }
 #endif
