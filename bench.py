@@ -49,7 +49,10 @@ def parse_args():
     ap.add_argument("--impl", choices=["mcx", "reference"], default="mcx")
     ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
+    ap.add_argument("--profile", choices=["pt", "flathist", "serve"], default=None,
+                    help="run one short workload for a profiler capture and exit (no JSON line)")
     return ap.parse_args()
 
 
@@ -174,6 +177,76 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+PT_SIZES = [16, 24, 32, 48, 64]
+PT_COUNTS = [52, 51, 51, 51, 51]
+
+
+def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, plain_sweeps=2):
+    """3-D parallel tempering, 256 replicas of uneven size (L 16..64, ~51 each),
+    geometric beta 0.20 -> 0.25 per size, exchange every sweep: the persistent batched
+    form against the plain one-lattice-per-launch form (same results bit for bit)."""
+    from mcx.pt import ParallelTempering, set_betas
+
+    ladders = [(L, set_betas(n, 0.20, 0.25, ":geometric")) for L, n in zip(PT_SIZES, PT_COUNTS)]
+    pt = ParallelTempering(ladders, dim=3, seed=SEED, ctx=ctx)
+    pt.init_(SEED)
+    sites = sum(L ** 3 * n for L, n in zip(PT_SIZES, PT_COUNTS))
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for mode, nsw in (("persistent", sweeps_per_step), ("plain", plain_sweeps)):
+        for _ in range(warmup):
+            flush.zero_()
+            pt.sweep_(nsw, mode=mode)
+        torch.cuda.synchronize()
+        l0 = ctx.launches()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            pt.sweep_(nsw, mode=mode)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        out[mode] = {"attempts_per_ns": sites * nsw * steps / (tot * 1e6), "ms_per_sweep": tot / (nsw * steps),
+                     "sweeps_per_step": nsw, "gpu_launches": ctx.launches() - l0}
+    peak, _ = measured_peaks()
+    per = out["persistent"]
+    achieved = 3.0 * sites / (per["ms_per_sweep"] * 1e-3) / 1e9
+    return {
+        "workload": "pt3d_ising_256replicas_L16-64_exchange_every_sweep", "replicas": pt.nrep, "sites": sites,
+        "persistent": per, "plain": out["plain"],
+        "speedup_vs_plain": per["attempts_per_ns"] / out["plain"]["attempts_per_ns"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "alg_bytes_per_sweep": 3 * sites, "kernel": "k_pt_persistent<3,false>"},
+        "exchange_acceptance": float(pt.acceptance_rate()),
+    }
+
+
+def bench_serve(mcx, ctx, njobs=40):
+    """Poisson arrivals (200 / s, seed 11) of Metropolis and Multicanonical jobs on 2-D
+    Ising / Blume-Capel, L log-uniform in [32, 512] (Multicanonical jobs, whose walker
+    is serial, capped at 128), sweeps log-uniform in [100, 1000] (the configured
+    [32, 2048] x [1e3, 1e5] stream would hold one GPU for hours), HBM budget 8 GiB,
+    64 slots, 25-sweep chunks."""
+    from mcx.serve import Server, poisson_jobs, run_load
+
+    srv = Server(hbm_budget=8 << 30, max_jobs=64, chunk=25, ctx=ctx)
+    # warm the kernels once
+    srv.submit(model="ising", L=(64, 64), nsweeps=30)
+    srv.run_until_idle()
+    stream = poisson_jobs(njobs, rate=200.0, seed=11, L_range=(32, 512), sweeps_range=(100, 1000), muca_L_max=128)
+    r = run_load(srv, stream)
+    st = srv.stats()
+    srv.close()
+    r.update({"workload": "poisson200_ising_bc_metropolis_muca_L32-512_muca_L<=128_sweeps100-1000",
+              "rate_per_s": 200.0,
+              "peak_bytes": st["peak_bytes"], "iterations": st["iterations"]})
+    return r
+
+
 def run_mcx(args):
     import numpy as np
     import torch
@@ -266,6 +339,10 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
+    pt_res = srv_res = None
+    if not args.no_extras:
+        pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
+        srv_res = bench_serve(mcx, ctx)
     if rank != 0:
         return
     cpu = None
@@ -292,14 +369,49 @@ def run_mcx(args):
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "batched_pt": pt_res,
+        "serving": srv_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
+def run_profile_target(args):
+    """Short, fixed workloads for ncu captures (small enough for ~40 replays)."""
+    import torch
+
+    import mcx
+
+    ctx = mcx.Context(device=0, stream=torch.cuda.current_stream().cuda_stream)
+    if args.profile == "pt":
+        from mcx.pt import ParallelTempering, set_betas
+        ladders = [(L, set_betas(n, 0.20, 0.25, ":geometric")) for L, n in zip(PT_SIZES, PT_COUNTS)]
+        pt = ParallelTempering(ladders, dim=3, seed=SEED, ctx=ctx)
+        pt.init_(SEED)
+        pt.sweep_(3)
+        pt.sweep_(10)
+    elif args.profile == "flathist":
+        from mcx import flathist as F
+        L = [128, 128]
+        walkers = []
+        for i in range(64):
+            s = mcx.BlumeCapel(L, D=1.0, ctx=ctx)
+            mcx.init_(s, "random", rng=mcx.Philox(SEED, i))
+            walkers.append(s)
+        N = L[0] * L[1]
+        ens = F.MulticanonicalEnsemble((-N, 1, 4 * N + 1), ctx=ctx)
+        alg = F.Multicanonical(mcx.Philox(SEED), ens)
+        F.sweep_walkers_(walkers, alg, 1)
+        F.sweep_walkers_(walkers, alg, 2)
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse_args()
+    if args.profile:
+        run_profile_target(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -153,6 +153,12 @@ MCX_API mcx_status mcx_energy(mcx_lattice* lat, double* energy, int64_t* magneti
 MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
                              mcx_rng* rng, int64_t nsweeps, int64_t* obs_series,
                              mcx_counters* counters);
+/* Times the admissible kernel shapes (sites per thread: 16, 8, 4) for this lattice
+ * and algorithm on a scratch copy of the spins and keeps the fastest for later
+ * mcx_sweep calls; results never depend on the choice.  chosen / ns_per_site may be
+ * NULL. */
+MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, double beta,
+                                int32_t* chosen, double* ns_per_site);
 /* Copy the per-sweep series of the last mcx_sweep call (first n sweeps). */
 MCX_API mcx_status mcx_read_series(mcx_lattice* lat, int64_t* obs_series, int64_t n);
 
@@ -244,6 +250,69 @@ MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls);
 /* Failure-detection check: a bounded wait on a device flag that nothing sets;
  * returns MCX_ERR_TIMEOUT after `polls` polls, with the context still usable. */
 MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls);
+
+/* ----------------------------------------------------------------- serving -- */
+/* Continuous batching of simulation jobs (no counterpart in the reference, whose
+ * users run one loop per system).  A job is a 2-D Ising or Blume-Capel lattice
+ * started with init!(sys, :random) from (seed, stream) and run for nsweeps
+ * checkerboard sweeps, canonically (alg, beta) or with fixed Multicanonical weights
+ * over integer energy bins.  Jobs are admitted in arrival order while the server's
+ * HBM budget and job slots allow, stay on the device until they finish, and share
+ * every launch with the other active jobs.  A job's result does not depend on the
+ * other jobs in the mix. */
+typedef enum mcx_job_kind { MCX_JOB_CANONICAL = 0, MCX_JOB_MULTICANONICAL = 1 } mcx_job_kind;
+
+typedef struct mcx_job {
+    int32_t model;   /* mcx_model */
+    int32_t dim;     /* 2 */
+    int32_t L[3];    /* sides, multiples of 8 */
+    int32_t kind;    /* mcx_job_kind */
+    int32_t alg;     /* mcx_algorithm (canonical jobs) */
+    int32_t reserved0;
+    double beta, J, D, h;
+    uint64_t seed;
+    uint32_t stream;
+    uint32_t reserved1;
+    int64_t nsweeps;
+    /* Multicanonical jobs: bins and initial log-weights (copied at submit, may be NULL) */
+    int64_t bin_start, bin_step, nbins;
+    const double* logweight;
+    /* caller-owned host outputs, filled when the job finishes (each may be NULL) */
+    int64_t* obs_series;    /* int64[nsweeps*3]: (pair, spin, spin2) after each sweep */
+    int64_t* histogram;     /* int64[nbins] (Multicanonical) */
+    double* logweight_out;  /* double[nbins] (Multicanonical) */
+    int8_t* final_spins;    /* int8[L0*L1] in SpinSystems order */
+} mcx_job;
+
+typedef struct mcx_job_result {
+    int32_t state;   /* 0 queued, 1 running, 2 done, 3 cancelled, 4 failed */
+    int32_t status;  /* mcx_status of the job (MCX_ERR_OUT_OF_RANGE: left the bins) */
+    int64_t pair_sum, spin_sum, spin2_sum;
+    uint64_t attempts, accepted;
+    int64_t sweeps_done;
+    double submit_s, admit_s, finish_s; /* server clock, seconds since creation */
+} mcx_job_result;
+
+typedef struct mcx_server_stats {
+    int32_t active, pending;
+    uint64_t iterations, jobs_done, attempts_done;
+    uint64_t bytes_in_use, peak_bytes;
+    double now_s;
+} mcx_server_stats;
+
+/* hbm_budget: bytes the server's jobs may hold at once (0 = no limit); max_jobs: job
+ * slots; chunk_sweeps: sweeps every active job advances per step. */
+MCX_API mcx_status mcx_server_create(mcx_ctx* ctx, uint64_t hbm_budget, int32_t max_jobs,
+                                     int32_t chunk_sweeps, mcx_server** out);
+MCX_API mcx_status mcx_server_destroy(mcx_server* server);
+/* Queue a job (MCX_ERR_BUDGET if it alone exceeds the budget). */
+MCX_API mcx_status mcx_server_submit(mcx_server* server, const mcx_job* job, uint64_t* job_id);
+/* One scheduling iteration: admit, advance every active job one chunk, retire. */
+MCX_API mcx_status mcx_server_step(mcx_server* server, int32_t* active, int32_t* pending);
+/* MCX_ERR_NOT_READY while queued or running; MCX_OK with the result once finished. */
+MCX_API mcx_status mcx_server_poll(mcx_server* server, uint64_t job_id, mcx_job_result* result);
+MCX_API mcx_status mcx_server_cancel(mcx_server* server, uint64_t job_id);
+MCX_API mcx_status mcx_server_get_stats(mcx_server* server, mcx_server_stats* stats);
 
 /* ----------------------------------------------------------- no allocation -- */
 /* mcx_sweep_noalloc has no counterpart in the reference.  It runs the same sweeps as

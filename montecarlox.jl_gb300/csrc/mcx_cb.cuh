@@ -180,6 +180,48 @@ __device__ __forceinline__ uint32_t ising_word(const uint32_t (&nbw)[Z], uint32_
     return fb;
 }
 
+// Blume-Capel decision for the four sites of one word (bytes 0xFF, 0x00, 0x01).
+// Neighbour sums per byte S = c + Z from (v + 1) per neighbour word.  Metropolis /
+// Glauber: proposal bit from the top bit of the proposal word (the reference's
+// rand(rng, Bool)), table entry (s_old+1)*2*NC + bit*NC + S.  Heat bath: cumulative
+// thresholds (T1, T12) at 2S, 2S+1.  Returns the new word.
+template <int Z, bool HB>
+__device__ __forceinline__ uint32_t bc_word(const uint32_t (&nbw)[Z], uint32_t word, uint4 ra, uint4 rp,
+                                            const unsigned long long* s_thr, int& nacc, int& dP, int& dM,
+                                            int& dQ) {
+    constexpr int NC = 2 * Z + 1;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int d = 0; d < Z; ++d) cnt += plus1(nbw[d]);
+    const uint32_t ua[4] = {ra.x, ra.y, ra.z, ra.w};
+    const uint32_t up[4] = {rp.x, rp.y, rp.z, rp.w};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int S = (cnt >> (8 * b)) & 0xFF;
+        const int so = (int)(int8_t)(word >> (8 * b));
+        const uint32_t u = ua[b];
+        int sn;
+        bool acc;
+        if (HB) {
+            sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
+            acc = sn != so;
+        } else {
+            const int bit = (int)(up[b] >> 31);
+            acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
+            sn = bc_propose(so, bit);
+        }
+        if (acc) {
+            const int ds = sn - so;
+            word = (word & ~(0xFFu << (8 * b))) | ((uint32_t)(uint8_t)(int8_t)sn << (8 * b));
+            ++nacc;
+            dP += ds * (S - Z);
+            dM += ds;
+            dQ += sn * sn - so * so;
+        }
+    }
+    return word;
+}
+
 // (pair, spin) deltas of a block of Ising flips from the word accumulators
 template <int Z>
 __device__ __forceinline__ void ising_deltas(int nacc, int nup, int isum, long long& dP, long long& dM) {

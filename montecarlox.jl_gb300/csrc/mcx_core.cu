@@ -6,6 +6,7 @@
 // the site x = 2k + ((y+z+c)&1).  A checkerboard half-sweep then reads one whole
 // array (the other colour), reads and writes the other (its own colour) with dense
 // 128-bit accesses.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -190,6 +191,67 @@ __global__ void k_gather(int8_t* __restrict__ lin, const int8_t* __restrict__ c0
     }
 }
 
+// Number of bytes that are not spin states of the model (Ising {-1,+1}, BC {-1,0,+1}).
+__global__ void k_validate(const int8_t* __restrict__ lin, long long n, int bc, unsigned long long* bad) {
+    unsigned long long cnt = 0;
+    const long long n16 = n / 16;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n16; q += stride) {
+        const uint4 v = reinterpret_cast<const uint4*>(lin)[q];
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            uint32_t ok = __vcmpeq4(w[i], 0x01010101u) | __vcmpeq4(w[i], 0xFFFFFFFFu);
+            if (bc) ok |= __vcmpeq4(w[i], 0u);
+            cnt += __popc(~ok) >> 3;
+        }
+    }
+    for (long long i = n16 * 16 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int v = lin[i];
+        cnt += !(v == 1 || v == -1 || (bc && v == 0));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(bad, cnt);
+}
+
+// Layout conversion 16 linear sites at a time (rows a multiple of 16 long): the even
+// bytes of a chunk belong to one colour, the odd bytes to the other, and land as 8
+// consecutive bytes in each colour array.
+__global__ void k_scatter16(const uint4* __restrict__ lin, int8_t* __restrict__ c0, int8_t* __restrict__ c1, Geo g) {
+    const long long cpr = g.Lx / 16, nq = g.N / 16;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nq;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long r = q / cpr;
+        const int x0 = (int)(q - r * cpr) * 16;
+        const int y = (int)(r % g.Ly), z = (int)(r / g.Ly);
+        const int p0 = (y + z) & 1;  // colour of the even bytes
+        const uint4 v = lin[q];
+        const uint2 ev = make_uint2(__byte_perm(v.x, v.y, 0x6420), __byte_perm(v.z, v.w, 0x6420));
+        const uint2 od = make_uint2(__byte_perm(v.x, v.y, 0x7531), __byte_perm(v.z, v.w, 0x7531));
+        const long long e = r * g.W + (x0 >> 1);
+        *reinterpret_cast<uint2*>((p0 ? c1 : c0) + e) = ev;
+        *reinterpret_cast<uint2*>((p0 ? c0 : c1) + e) = od;
+    }
+}
+
+__global__ void k_gather16(uint4* __restrict__ lin, const int8_t* __restrict__ c0, const int8_t* __restrict__ c1,
+                           Geo g) {
+    const long long cpr = g.Lx / 16, nq = g.N / 16;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nq;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long r = q / cpr;
+        const int x0 = (int)(q - r * cpr) * 16;
+        const int y = (int)(r % g.Ly), z = (int)(r / g.Ly);
+        const int p0 = (y + z) & 1;
+        const long long e = r * g.W + (x0 >> 1);
+        const uint2 ev = *reinterpret_cast<const uint2*>((p0 ? c1 : c0) + e);
+        const uint2 od = *reinterpret_cast<const uint2*>((p0 ? c0 : c1) + e);
+        lin[q] = make_uint4(__byte_perm(ev.x, od.x, 0x5140), __byte_perm(ev.x, od.x, 0x7362),
+                            __byte_perm(ev.y, od.y, 0x5140), __byte_perm(ev.y, od.y, 0x7362));
+    }
+}
+
 // init!(sys, :random): Ising s = top bit ? +1 : -1; Blume-Capel s = floor(3u/2^32) - 1.
 __global__ void k_init_random(int8_t* __restrict__ c0, int8_t* __restrict__ c1, Geo g,
                               uint32_t k0, uint32_t k1, uint32_t stream, int bc) {
@@ -209,30 +271,32 @@ __global__ void k_init_random(int8_t* __restrict__ c0, int8_t* __restrict__ c1, 
 
 // Full recompute of (pair_sum, spin_sum, spin2_sum).  Every bond joins the two
 // colours, so pair_sum = sum over colour-0 sites of s_i * (sum of its neighbours).
+// Grid: x over the entries of a row, y over rows.
 __global__ void k_observables(const int8_t* __restrict__ c0, const int8_t* __restrict__ c1,
                               Geo g, int dim, unsigned long long* state) {
     long long P = 0, M = 0, Q = 0;
-    const long long half = g.N / 2;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < half;
-         e += (long long)gridDim.x * blockDim.x) {
-        const long long r = e / g.W;
-        const int k = (int)(e - r * g.W);
-        const int y = (int)(r % g.Ly), z = (int)(r / g.Ly);
-        const int p = (y + z) & 1;  // colour-0 parity of this row
-        const int s = c0[e];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rows = g.Ly * g.Lz;
+    if (k < g.W) {
         const int km = k == 0 ? g.W - 1 : k - 1, kp = k == g.W - 1 ? 0 : k + 1;
-        const long long rowb = r * (long long)g.W;
-        int S = c1[rowb + k] + c1[rowb + (p ? kp : km)];
-        const int yp = y + 1 == g.Ly ? 0 : y + 1, ym = y == 0 ? g.Ly - 1 : y - 1;
-        S += c1[(long long)(yp + g.Ly * z) * g.W + k] + c1[(long long)(ym + g.Ly * z) * g.W + k];
-        if (dim == 3) {
-            const int zp = z + 1 == g.Lz ? 0 : z + 1, zm = z == 0 ? g.Lz - 1 : z - 1;
-            S += c1[(long long)(y + g.Ly * zp) * g.W + k] + c1[(long long)(y + g.Ly * zm) * g.W + k];
+        for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+            const int y = r % g.Ly, z = r / g.Ly;
+            const int p = (y + z) & 1;  // colour-0 parity of this row
+            const long long rowb = (long long)r * g.W;
+            const long long e = rowb + k;
+            const int s = c0[e];
+            int S = c1[e] + c1[rowb + (p ? kp : km)];
+            const int yp = y + 1 == g.Ly ? 0 : y + 1, ym = y == 0 ? g.Ly - 1 : y - 1;
+            S += c1[(long long)(yp + g.Ly * z) * g.W + k] + c1[(long long)(ym + g.Ly * z) * g.W + k];
+            if (dim == 3) {
+                const int zp = z + 1 == g.Lz ? 0 : z + 1, zm = z == 0 ? g.Lz - 1 : z - 1;
+                S += c1[(long long)(y + g.Ly * zp) * g.W + k] + c1[(long long)(y + g.Ly * zm) * g.W + k];
+            }
+            const int s1 = c1[e];
+            P += s * S;
+            M += s + s1;
+            Q += s * s + s1 * s1;
         }
-        const int s1 = c1[e];
-        P += s * S;
-        M += s + s1;
-        Q += s * s + s1 * s1;
     }
     long long v[3] = {P, M, Q};
     unsigned long long* const dst[3] = {state, state + 1, state + 2};
@@ -298,8 +362,11 @@ mcx_status recompute_state(mcx_lattice* lat) {
     if (lat->layout == MCX_LAYOUT_MSC64) MCX_CHECK(msc_unpack(lat));
     MCX_CUDA(cudaMemsetAsync(lat->d_state, 0, 3 * sizeof(int64_t), ctx->stream));
     const Geo g = geo_of(lat);
-    k_observables<<<grid_for(ctx, lat->N / 2, 256), 256, 0, ctx->stream>>>(
-        lat->d_col[0], lat->d_col[1], g, lat->dim, (unsigned long long*)lat->d_state);
+    const int bx = (int)((lat->W + 255) / 256);
+    int by = (int)std::min<int64_t>(lat->rows, 65535);
+    by = std::max(1, std::min(by, (ctx->num_sms * 16 + bx - 1) / bx));
+    k_observables<<<dim3(bx, by), 256, 0, ctx->stream>>>(lat->d_col[0], lat->d_col[1], g, lat->dim,
+                                                          (unsigned long long*)lat->d_state);
     count_launch(ctx);
     MCX_CUDA(cudaGetLastError());
     return MCX_OK;
@@ -484,15 +551,24 @@ MCX_API mcx_status mcx_lattice_info(const mcx_lattice* lat, int64_t* nsites, int
 MCX_API mcx_status mcx_set_spins(mcx_lattice* lat, const int8_t* host, size_t n) {
     if (!lat || !host) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
     if ((int64_t)n != lat->N) return fail(MCX_ERR_INVALID_ARG, "expected %lld spins, got %zu", (long long)lat->N, n);
-    for (size_t i = 0; i < n; ++i) {
-        const int8_t v = host[i];
-        const bool ok = lat->model == MCX_ISING ? (v == 1 || v == -1) : (v >= -1 && v <= 1);
-        if (!ok) return fail(MCX_ERR_INVALID_ARG, "spin %zu has value %d", i, (int)v);
-    }
     mcx_ctx* ctx = lat->ctx;
     MCX_CUDA(cudaMemcpyAsync(lat->d_lin, host, n, cudaMemcpyHostToDevice, ctx->stream));
+    // validate on the device before the lattice is touched (the counter word is free here)
+    unsigned long long bad = 0;
+    MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
+    k_validate<<<grid_for(ctx, lat->N / 16 + 1, 256), 256, 0, ctx->stream>>>(lat->d_lin, lat->N,
+                                                                             lat->model == MCX_BLUME_CAPEL, lat->d_acc);
+    count_launch(ctx);
+    MCX_CUDA(cudaGetLastError());
+    MCX_CUDA(cudaMemcpyAsync(&bad, lat->d_acc, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (bad) return fail(MCX_ERR_INVALID_ARG, "%llu values are not spin states of this model", bad);
     const Geo g = geo_of(lat);
-    k_scatter<<<grid_for(ctx, lat->N, 256), 256, 0, ctx->stream>>>(lat->d_lin, lat->d_col[0], lat->d_col[1], g);
+    if (lat->L[0] % 16 == 0)
+        k_scatter16<<<grid_for(ctx, lat->N / 16, 256), 256, 0, ctx->stream>>>(
+            reinterpret_cast<const uint4*>(lat->d_lin), lat->d_col[0], lat->d_col[1], g);
+    else
+        k_scatter<<<grid_for(ctx, lat->N, 256), 256, 0, ctx->stream>>>(lat->d_lin, lat->d_col[0], lat->d_col[1], g);
     count_launch(ctx);
     MCX_CUDA(cudaGetLastError());
     if (lat->layout == MCX_LAYOUT_MSC64) MCX_CHECK(msc_pack(lat));
@@ -505,7 +581,11 @@ MCX_API mcx_status mcx_get_spins(mcx_lattice* lat, int8_t* host, size_t n) {
     mcx_ctx* ctx = lat->ctx;
     if (lat->layout == MCX_LAYOUT_MSC64) MCX_CHECK(msc_unpack(lat));
     const Geo g = geo_of(lat);
-    k_gather<<<grid_for(ctx, lat->N, 256), 256, 0, ctx->stream>>>(lat->d_lin, lat->d_col[0], lat->d_col[1], g);
+    if (lat->L[0] % 16 == 0)
+        k_gather16<<<grid_for(ctx, lat->N / 16, 256), 256, 0, ctx->stream>>>(reinterpret_cast<uint4*>(lat->d_lin),
+                                                                             lat->d_col[0], lat->d_col[1], g);
+    else
+        k_gather<<<grid_for(ctx, lat->N, 256), 256, 0, ctx->stream>>>(lat->d_lin, lat->d_col[0], lat->d_col[1], g);
     count_launch(ctx);
     MCX_CUDA(cudaGetLastError());
     MCX_CUDA(cudaMemcpyAsync(host, lat->d_lin, n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -27,43 +27,12 @@
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
 #include "mcx_sweep.cuh"
+#include "mcx_flathist.cuh"
 
-struct mcx_flathist {
-    mcx_ctx* ctx = nullptr;
-    int64_t start = 0, step = 1, nbins = 0;
-    double* d_lnw = nullptr;
-    unsigned long long* d_H = nullptr;
-    uint8_t* d_visited = nullptr;
-    unsigned long long* d_red = nullptr;  // min, sum, count
-};
 
 namespace mcx {
 
-struct FHWalker {
-    int8_t* col[2];
-    double* lnw;
-    unsigned long long* H;
-    long long* series;  // [nsweeps][3] or null
-    long long P, M, Q;
-    unsigned long long steps, accepted;
-    unsigned long long sweep0;
-    uint32_t k0, k1, stream;
-    int status;  // 0 ok, 2 out of range
-};
-
-struct FHArgs {
-    FHWalker* walkers;
-    int nwalkers;
-    int W, Ly, Lz, dim, model;
-    long long J, D, h;
-    long long start, step, nbins;
-    int shift;  // log2(step) if step is a power of two, else -1
-    int mode;   // 0 MUCA, 1 Wang-Landau
-    double logf;
-    long long nsweeps;
-};
-
-__device__ __forceinline__ bool fh_bin(long long E, const FHArgs& a, long long& b) {
+__device__ __forceinline__ bool fh_bin(long long E, const FHGeom& a, long long& b) {
     const long long x = E - a.start;
     long long q;
     if (a.shift >= 0) q = x >= 0 ? (x >> a.shift) : -((-x) >> a.shift);  // truncating, as Julia div
@@ -74,13 +43,43 @@ __device__ __forceinline__ bool fh_bin(long long E, const FHArgs& a, long long& 
 
 constexpr int kFHWarps = 4;
 
+// Each warp keeps a window of kFHWin log-weights around the walker's current bin in
+// shared memory, so the serial scan never waits on a global load; the window moves
+// when a proposed bin falls outside it (Wang-Landau writes the window back first).
+constexpr int kFHWin = 1024;
+// Bound on |logf(float(U)) - 53 ln 2 (in float) - log(U)|: float(k) is within 2^-24
+// relative of k, logf within 1 ulp (<= 2^-18 for results below 64 in magnitude), the
+// float constant and subtraction within 2^-18 each: far below 2^-14.
+constexpr double kLogMargin = 6.103515625e-05;  // 2^-14
+
+__device__ __forceinline__ long long fh_window_base(long long b, long long nbins) {
+    long long wb = b - kFHWin / 2;
+    if (wb > nbins - kFHWin) wb = nbins - kFHWin;
+    return wb < 0 ? 0 : wb;
+}
+
+__device__ __forceinline__ void fh_window_load(double* win, const double* lnw, long long wb, long long nbins, int lane) {
+    for (int i = lane; i < kFHWin; i += 32) win[i] = wb + i < nbins ? lnw[wb + i] : 0.0;
+    __syncwarp();
+}
+
+__device__ __forceinline__ void fh_window_store(const double* win, double* lnw, long long wb, long long nbins, int lane) {
+    for (int i = lane; i < kFHWin; i += 32)
+        if (wb + i < nbins) lnw[wb + i] = win[i];
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
     __shared__ long long s_dE[kFHWarps][32];
-    __shared__ double s_lu[kFHWarps][32];
+    __shared__ unsigned long long s_k[kFHWarps][32];  // U = k * 2^-53
+    __shared__ double s_lo[kFHWarps][32];             // log(U) lies in [lo, hi]
+    __shared__ double s_hi[kFHWarps][32];
+    __shared__ double s_win[kFHWarps][kFHWin];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int wid = blockIdx.x * kFHWarps + wl;
     if (wid >= a.nwalkers) return;  // whole warp
     FHWalker& w = a.walkers[wid];
+    const FHGeom g = w.g;
     int8_t* const col0 = w.col[0];
     int8_t* const col1 = w.col[1];
     double* const lnw = w.lnw;
@@ -89,15 +88,18 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
     const uint32_t k0 = w.k0, k1 = w.k1, stream = w.stream;
     const unsigned long long sweep0 = w.sweep0;
     long long P = w.P, M = w.M, Q = w.Q;
-    long long E = -a.J * P + a.D * Q - a.h * M;
+    long long E = -g.J * P + g.D * Q - g.h * M;
     long long bo = 0;
     int status = 0;
-    if (!fh_bin(E, a, bo)) status = 2;
-    double lwo = status ? 0.0 : lnw[bo];
+    if (!fh_bin(E, g, bo)) status = 2;
+    double* const win = s_win[wl];
+    long long wb = fh_window_base(status ? 0 : bo, g.nbins);
+    fh_window_load(win, lnw, wb, g.nbins, lane);
+    double lwo = status ? 0.0 : win[bo - wb];
     unsigned long long steps = 0, accepted = 0;
-    const long long ncol = (long long)a.W * a.Ly * a.Lz;
-    const int Z = 2 * a.dim;
-    for (long long s = 0; s < a.nsweeps && status == 0; ++s) {
+    const long long ncol = (long long)g.W * g.Ly * g.Lz;
+    const int Z = 2 * g.dim;
+    for (long long s = 0; s < g.nsweeps && status == 0; ++s) {
         const unsigned long long t = sweep0 + (unsigned long long)s;
         long long dP = 0, dM = 0, dQ = 0;
         for (int c = 0; c < 2 && status == 0; ++c) {
@@ -110,59 +112,86 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
                 const bool valid = j < ncol;
                 int sn = 0, ds = 0, dq = 0, dp = 0;
                 long long dE = 0;
-                double lu = 0.0;
+                unsigned long long k53 = 0;
+                double lo = 0.0, hi = 0.0;
                 if (valid) {
-                    const int r = (int)(j / a.W), k = (int)(j - (long long)r * a.W);
-                    const int y = r % a.Ly, z = r / a.Ly;
-                    const RowInfo ri = row_info_yz(y, z, a.Ly, a.Lz, c, a.dim);
+                    const int r = (int)(j / g.W), k = (int)(j - (long long)r * g.W);
+                    const int y = r % g.Ly, z = r / g.Ly;
+                    const RowInfo ri = row_info_yz(y, z, g.Ly, g.Lz, c, g.dim);
                     const int so = cur[j];
-                    const int ks = ri.p == 0 ? (k == 0 ? a.W - 1 : k - 1) : (k == a.W - 1 ? 0 : k + 1);
-                    int S = oth[j] + oth[(long long)r * a.W + ks] + oth[ri.ryp * a.W + k] + oth[ri.rym * a.W + k];
-                    if (Z == 6) S += oth[ri.rzp * a.W + k] + oth[ri.rzm * a.W + k];
+                    const int ks = ri.p == 0 ? (k == 0 ? g.W - 1 : k - 1) : (k == g.W - 1 ? 0 : k + 1);
+                    int S = oth[j] + oth[(long long)r * g.W + ks] + oth[ri.ryp * g.W + k] + oth[ri.rym * g.W + k];
+                    if (Z == 6) S += oth[ri.rzp * g.W + k] + oth[ri.rzm * g.W + k];
                     const uint32_t cj = (uint32_t)(j >> 2);
                     const int lj = (int)(j & 3);
-                    if (a.model == 0) sn = -so;
+                    if (g.model == 0) sn = -so;
                     else sn = bc_propose(so, (int)(pick4(philox10(make_uint4(cj, (uint32_t)t, w2p, stream), k0, k1), lj) >> 31));
                     ds = sn - so;
                     dq = sn * sn - so * so;
                     dp = ds * S;
-                    dE = -a.J * dp + a.D * dq - a.h * ds;
-                    const uint32_t hi = pick4(philox10(make_uint4(cj, (uint32_t)t, w2a, stream), k0, k1), lj);
-                    const uint32_t lo = pick4(philox10(make_uint4(cj, (uint32_t)t, w2l, stream), k0, k1), lj);
-                    lu = mcx_log(u53(hi, lo));
+                    dE = -g.J * dp + g.D * dq - g.h * ds;
+                    const uint32_t whi = pick4(philox10(make_uint4(cj, (uint32_t)t, w2a, stream), k0, k1), lj);
+                    const uint32_t wlo = pick4(philox10(make_uint4(cj, (uint32_t)t, w2l, stream), k0, k1), lj);
+                    k53 = ((unsigned long long)whi << 21) | (unsigned long long)(wlo >> 11);
+                    // single-precision log(U) and a margin that bounds its distance to the
+                    // FP64 log of the decision rule (logf: <= 1 ulp, |log U| < 37.5)
+                    const float l32 = logf(__ull2float_rn(k53)) - 36.7368005696771f;  // 53 ln 2
+                    lo = (double)l32 - kLogMargin;
+                    hi = (double)l32 + kLogMargin;
                 }
                 s_dE[wl][lane] = dE;
-                s_lu[wl][lane] = lu;
+                s_k[wl][lane] = k53;
+                s_lo[wl][lane] = lo;
+                s_hi[wl][lane] = hi;
                 __syncwarp();
                 unsigned int accmask = 0;
-                int stop = 32;
-                if (lane == 0) {
-                    const int n = (int)((ncol - j0) < 32 ? (ncol - j0) : 32);
-                    for (int i = 0; i < n; ++i) {
-                        const long long En = E + s_dE[wl][i];
-                        long long bn;
-                        if (!fh_bin(En, a, bn)) {
-                            status = 2;
-                            stop = i;
-                            break;
+                int i = 0;
+                const int n = (int)((ncol - j0) < 32 ? (ncol - j0) : 32);
+                for (;;) {
+                    long long need = -1;
+                    if (lane == 0) {
+                        for (; i < n; ++i) {
+                            const long long En = E + s_dE[wl][i];
+                            long long bn;
+                            if (!fh_bin(En, g, bn)) {
+                                status = 2;
+                                break;
+                            }
+                            if (bn < wb || bn >= wb + kFHWin) {
+                                need = bn;
+                                break;
+                            }
+                            const double lwn = win[bn - wb];
+                            const double lr = lwn - lwo;
+                            // lr > 0 || log(U) < lr, deciding from the single-precision
+                            // bracket and computing the FP64 log only inside it
+                            bool acc;
+                            if (lr > 0.0 || lr > s_hi[wl][i]) acc = true;
+                            else if (lr <= s_lo[wl][i]) acc = false;
+                            else acc = mcx_log((double)s_k[wl][i] * 1.1102230246251565404236316680908203125e-16) < lr;
+                            ++steps;
+                            if (acc) {
+                                ++accepted;
+                                accmask |= 1u << i;
+                                E = En;
+                                bo = bn;
+                                lwo = lwn;
+                            }
+                            if (g.mode == 1) {
+                                lwo = lwo - g.logf;
+                                win[bo - wb] = lwo;
+                            }
+                            atomicAdd(&H[bo], 1ull);
                         }
-                        const double lwn = bn == bo ? lwo : lnw[bn];
-                        const double lr = lwn - lwo;
-                        const bool acc = (lr > 0.0) || (s_lu[wl][i] < lr);
-                        ++steps;
-                        if (acc) {
-                            ++accepted;
-                            accmask |= 1u << i;
-                            E = En;
-                            bo = bn;
-                            lwo = lwn;
-                        }
-                        if (a.mode == 1) {
-                            lwo = lwo - a.logf;
-                            lnw[bo] = lwo;
-                        }
-                        atomicAdd(&H[bo], 1ull);
                     }
+                    need = __shfl_sync(0xFFFFFFFFu, need, 0);
+                    if (need < 0) break;
+                    // move the window around the proposed bin (the current bin stays inside:
+                    // one move changes the bin by far less than half the window)
+                    __syncwarp();
+                    if (g.mode == 1) fh_window_store(win, lnw, wb, g.nbins, lane);
+                    wb = fh_window_base(need, g.nbins);
+                    fh_window_load(win, lnw, wb, g.nbins, lane);
                 }
                 accmask = __shfl_sync(0xFFFFFFFFu, accmask, 0);
                 status = __shfl_sync(0xFFFFFFFFu, status, 0);
@@ -195,6 +224,7 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
         M = __shfl_sync(0xFFFFFFFFu, M, 0);
         Q = __shfl_sync(0xFFFFFFFFu, Q, 0);
     }
+    if (g.mode == 1) fh_window_store(win, lnw, wb, g.nbins, lane);
     if (lane == 0) {
         // a stopped sweep still folds the accepted moves made before the stop
         w.P = P;
@@ -251,6 +281,28 @@ __global__ void k_add_hist(unsigned long long* dst, const unsigned long long* sr
     for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n;
          b += (long long)gridDim.x * blockDim.x)
         dst[b] += src[b];
+}
+
+mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers) {
+    FHArgs a;
+    a.walkers = d_walkers;
+    a.nwalkers = nwalkers;
+    k_flathist<<<(nwalkers + kFHWarps - 1) / kFHWarps, 32 * kFHWarps, 0, ctx->stream>>>(a);
+    count_launch(ctx);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+bool fh_window_ok(int dim, long long J, long long D, long long h, long long step) {
+    const long long z = 2 * dim;
+    const long long maxde = 2 * (J < 0 ? -J : J) * z + 2 * (h < 0 ? -h : h) + (D < 0 ? -D : D);
+    return maxde / step + 2 < kFHWin / 2;
+}
+
+int fh_shift(long long step) {
+    for (int sft = 0; sft < 62; ++sft)
+        if ((1ll << sft) == step) return sft;
+    return -1;
 }
 
 static int small_grid(const mcx_ctx* ctx, long long n) {
@@ -409,6 +461,8 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
     const long long Ji = (long long)L0->J, Di = (long long)L0->D, hi = (long long)L0->h;
     if ((double)Ji != L0->J || (double)Di != L0->D || (double)hi != L0->h)
         return fail(MCX_ERR_INVALID_ARG, "flat-histogram sweeps need integer J, D and h (integer energies)");
+    if (!fh_window_ok(L0->dim, Ji, Di, hi, F0->step))
+        return fail(MCX_ERR_INVALID_ARG, "one move may change the energy by more than the ln g window holds");
     if (nsweeps == 0) return MCX_OK;
     std::vector<FHWalker> hw(nwalkers);
     for (int i = 0; i < nwalkers; ++i) {
@@ -438,28 +492,28 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
     }
     void* dw = nullptr;
     MCX_CHECK(dev_alloc(ctx, &dw, hw.size() * sizeof(FHWalker)));
+    FHGeom g;
+    std::memset(&g, 0, sizeof(g));
+    g.W = (int)L0->W;
+    g.Ly = (int)L0->L[1];
+    g.Lz = (int)L0->L[2];
+    g.dim = L0->dim;
+    g.model = L0->model == MCX_ISING ? 0 : 1;
+    g.J = Ji;
+    g.D = Di;
+    g.h = hi;
+    g.start = F0->start;
+    g.step = F0->step;
+    g.nbins = F0->nbins;
+    g.shift = fh_shift(F0->step);
+    g.mode = mode == MCX_MUCA ? 0 : 1;
+    g.logf = logf;
+    g.nsweeps = nsweeps;
+    for (auto& w : hw) w.g = g;
     cudaError_t e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(FHWalker), cudaMemcpyHostToDevice, ctx->stream);
     FHArgs a;
-    std::memset(&a, 0, sizeof(a));
     a.walkers = (FHWalker*)dw;
     a.nwalkers = nwalkers;
-    a.W = (int)L0->W;
-    a.Ly = (int)L0->L[1];
-    a.Lz = (int)L0->L[2];
-    a.dim = L0->dim;
-    a.model = L0->model == MCX_ISING ? 0 : 1;
-    a.J = Ji;
-    a.D = Di;
-    a.h = hi;
-    a.start = F0->start;
-    a.step = F0->step;
-    a.nbins = F0->nbins;
-    a.shift = -1;
-    for (int sft = 0; sft < 62; ++sft)
-        if ((1ll << sft) == F0->step) a.shift = sft;
-    a.mode = mode == MCX_MUCA ? 0 : 1;
-    a.logf = logf;
-    a.nsweeps = nsweeps;
     if (e == cudaSuccess) {
         k_flathist<<<(nwalkers + kFHWarps - 1) / kFHWarps, 32 * kFHWarps, 0, ctx->stream>>>(a);
         count_launch(ctx);

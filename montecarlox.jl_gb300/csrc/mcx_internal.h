@@ -83,6 +83,7 @@ struct mcx_lattice {
     int64_t series_cap = 0;        // in sweeps
     int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
     int64_t device_bytes = 0;
+    int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
 };
 
 namespace mcx {

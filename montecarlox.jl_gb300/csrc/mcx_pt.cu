@@ -3,8 +3,9 @@
 //
 // Two forms with bit-identical results:
 //   PERSISTENT: one cooperative launch runs all sweeps of all replicas.  Replicas are
-//     cut into tiles of ~4096 same-colour sites; tiles are assigned to blocks by a
-//     longest-processing-time schedule built on the host.  A bounded grid barrier
+//     cut into tiles of ~4096 same-colour sites; in every phase the blocks claim tiles,
+//     largest first, from an atomic ticket counter (dynamic balancing of tiles of
+//     unequal cost).  A bounded grid barrier
 //     separates the two colours of a sweep and the sweep from the exchange; every
 //     block then evaluates the (tiny) exchange step itself, so the new ladder
 //     positions need no further barrier.  Per-replica energy deltas are triple
@@ -46,9 +47,9 @@ struct PTArgs {
     int8_t* arena;
     const PTReplica* reps;
     const PTTile* tiles;
-    const int* block_tiles;  // CSR over blocks (persistent form)
-    const int* block_off;
-    int nrep, npos;
+    const int* order;        // tiles in claiming order, largest first (persistent form)
+    unsigned int* claim;     // [3] per-phase tile tickets (persistent form)
+    int nrep, npos, ntiles;
     const unsigned long long* tables;  // [npos][16] for the algorithm of this run
     const double* betas;               // [npos]
     const int* pos_ladder;             // [npos]
@@ -63,6 +64,7 @@ struct PTArgs {
     unsigned long long* ex_acc;        // [npos]
     long long* series;                 // [nsweeps][nrep][2] or null
     unsigned int* bar;                 // count, generation, error
+    double* logu;                      // [2][npos] exchange log-uniforms (persistent form)
     double J, h;
     uint32_t k0, k1;
     unsigned long long sweep0;
@@ -106,25 +108,49 @@ __device__ __forceinline__ void pt_tile(const PTArgs& a, const PTReplica& R, int
     }
 }
 
+// Warp-level sum of N int64 values and one atomic per value per warp (no block
+// barrier, so a block can move from tile to tile without synchronising).
+template <int N>
+__device__ __forceinline__ void warp_add_atomic(long long (&v)[N], unsigned long long* const (&dst)[N]) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        long long x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if ((threadIdx.x & 31) == 0 && x != 0) atomicAdd(dst[j], (unsigned long long)x);
+    }
+}
+
+// One tile with its acceptance table `thr` (shared memory); per-warp atomics.
 template <int DIM, bool HB>
 __device__ __forceinline__ void pt_run_tile(const PTArgs& a, const PTTile& tl, int colour,
-                                            unsigned long long sweep, int ladder_pos, long long* dcur,
-                                            unsigned long long* s_thr) {
+                                            unsigned long long sweep, long long* dcur,
+                                            const unsigned long long* thr) {
     const PTReplica R = a.reps[tl.rep];
-    __syncthreads();  // previous tile is done with s_thr
-    if (threadIdx.x < 16) s_thr[threadIdx.x] = a.tables[(size_t)(R.gpos0 + ladder_pos) * 16 + threadIdx.x];
-    __syncthreads();
     int nacc = 0, nup = 0, isum = 0;
-    if (R.V == 16) pt_tile<DIM, 16, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
-    else if (R.V == 8) pt_tile<DIM, 8, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
-    else pt_tile<DIM, 4, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, s_thr, nacc, nup, isum);
+    if (R.V == 16) pt_tile<DIM, 16, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
+    else if (R.V == 8) pt_tile<DIM, 8, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
+    else pt_tile<DIM, 4, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
     constexpr int Z = 2 * DIM;
     long long dP, dM;
     ising_deltas<Z>(nacc, nup, isum, dP, dM);
     long long v[3] = {dP, dM, (long long)nacc};
     unsigned long long* const dst[3] = {(unsigned long long*)&dcur[2 * tl.rep],
                                         (unsigned long long*)&dcur[2 * tl.rep + 1], &a.acc[tl.rep]};
-    block_add_atomic<3>(v, dst);
+    warp_add_atomic<3>(v, dst);
+}
+
+// log(U) of the exchange uniform of pair (p, p+1) of ladder l after sweep t
+__device__ __forceinline__ double pt_exchange_logu(const PTArgs& a, int p, int l, unsigned long long t) {
+    const uint4 w = philox10(make_uint4((uint32_t)p, (uint32_t)t, ctr_word2(t, 0, P_EXCHANGE), (uint32_t)l), a.k0, a.k1);
+    return mcx_log(u53(w.x, w.y));
+}
+
+__device__ __forceinline__ bool pt_pair_active(const PTArgs& a, int gp, int stage, int& p, int& l) {
+    p = a.pos_local[gp];
+    l = a.pos_ladder[gp];
+    const int first = (stage & 1) ? 1 : 0;
+    return !(p < first || ((p - first) & 1) || p + 1 >= a.ladder_n[l]);
 }
 
 // The exchange step on block-local copies: pos (replica -> position), rep_at
@@ -132,23 +158,19 @@ __device__ __forceinline__ void pt_run_tile(const PTArgs& a, const PTTile& tl, i
 // pairs whose lower global position it owns; pairs are disjoint, so the position
 // updates never collide.  `count` adds the edge counters (done by one block only).
 __device__ void pt_exchange(const PTArgs& a, int* s_pos, int* s_rep, const long long* s_P, const long long* s_M,
-                            int stage, unsigned long long t, bool count) {
+                            int stage, unsigned long long t, bool count, const double* logu) {
     for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) s_rep[a.reps[r].gpos0 + s_pos[r]] = r;
     __syncthreads();
-    const int first = (stage & 1) ? 1 : 0;
     for (int gp = threadIdx.x; gp < a.npos; gp += blockDim.x) {
-        const int p = a.pos_local[gp];
-        const int l = a.pos_ladder[gp];
-        if (p < first || ((p - first) & 1) || p + 1 >= a.ladder_n[l]) continue;
+        int p, l;
+        if (!pt_pair_active(a, gp, stage, p, l)) continue;
         const int ri = s_rep[gp], rj = s_rep[gp + 1];
-        const uint4 w = philox10(make_uint4((uint32_t)p, (uint32_t)t, ctr_word2(t, 0, P_EXCHANGE), (uint32_t)l),
-                                 a.k0, a.k1);
-        const double U = u53(w.x, w.y);
+        const double lu = logu ? logu[gp] : pt_exchange_logu(a, p, l, t);
         const double bi = a.betas[gp], bj = a.betas[gp + 1];
         const double xi = (-(a.J * (double)s_P[ri])) - (a.h * (double)s_M[ri]);
         const double xj = (-(a.J * (double)s_P[rj])) - (a.h * (double)s_M[rj]);
         const double lr = (((-bi) * xj) - ((-bi) * xi)) + (((-bj) * xi) - ((-bj) * xj));
-        const bool acc = (lr > 0.0) || (mcx_log(U) < lr);
+        const bool acc = (lr > 0.0) || (lu < lr);
         if (count) {
             a.ex_steps[gp] += 1ull;
             if (acc) a.ex_acc[gp] += 1ull;
@@ -201,14 +223,15 @@ __device__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long l
 }
 
 template <int DIM, bool HB>
-__global__ void __launch_bounds__(256) k_pt_persistent(const PTArgs a) {
+__global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
     extern __shared__ long long smem[];
-    long long* s_P = smem;
+    unsigned long long* s_tab = reinterpret_cast<unsigned long long*>(smem);  // [npos][16]
+    long long* s_P = smem + (size_t)a.npos * 16;
     long long* s_M = s_P + a.nrep;
     int* s_pos = reinterpret_cast<int*>(s_M + a.nrep);
     int* s_rep = s_pos + a.nrep;
-    __shared__ unsigned long long s_thr[16];
     __shared__ unsigned s_gen;
+    for (int i = threadIdx.x; i < a.npos * 16; i += blockDim.x) s_tab[i] = a.tables[i];
     for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
         s_P[r] = a.state[2 * r];
         s_M[r] = a.state[2 * r + 1];
@@ -218,19 +241,42 @@ __global__ void __launch_bounds__(256) k_pt_persistent(const PTArgs a) {
     int stage = *a.stage;
     __syncthreads();
     unsigned gen = s_gen;
-    const int t_begin = a.block_off[blockIdx.x], t_end = a.block_off[blockIdx.x + 1];
+    __shared__ unsigned s_ticket;
+    const unsigned ntiles = (unsigned)a.ntiles;
     const size_t dsz = (size_t)a.nrep * 2;
     for (long long s = 0; s < a.nsweeps; ++s) {
         const unsigned long long t = a.sweep0 + (unsigned long long)s;
         long long* dcur = a.delta + (size_t)(s % 3) * dsz;
+        const bool exch = (t + 1) % (unsigned long long)a.every == 0;
+        double* logu = a.logu + (size_t)(s & 1) * a.npos;
         if (blockIdx.x == 0) {
             long long* dnext = a.delta + (size_t)((s + 1) % 3) * dsz;
             for (size_t i = threadIdx.x; i < dsz; i += blockDim.x) dnext[i] = 0;
         }
+        if (exch)  // the exchange uniforms' logs, each computed once, read after the barriers
+            for (int gp = blockIdx.x * blockDim.x + threadIdx.x; gp < a.npos; gp += gridDim.x * blockDim.x) {
+                int p, l;
+                if (pt_pair_active(a, gp, stage, p, l)) logu[gp] = pt_exchange_logu(a, p, l, t);
+            }
         for (int colour = 0; colour < 2; ++colour) {
-            for (int k = t_begin; k < t_end; ++k) {
-                const PTTile tl = a.tiles[a.block_tiles[k]];
-                pt_run_tile<DIM, HB>(a, tl, colour, t, s_pos[tl.rep], dcur, s_thr);
+            // phase h = 2s + colour claims tiles from ticket counter h % 3; the counter of
+            // phase h + 1 was last used in phase h - 2 and is cleared now
+            const long long h = 2 * s + colour;
+            if (blockIdx.x == 0 && threadIdx.x == 0) a.claim[(h + 1) % 3] = 0u;
+            unsigned* ctr = a.claim + (h % 3);
+            if (threadIdx.x == 0) s_ticket = atomicAdd(ctr, 1u);
+            __syncthreads();
+            unsigned k = s_ticket;
+            while (k < ntiles) {
+                unsigned nk = 0;
+                if (threadIdx.x == 0) nk = atomicAdd(ctr, 1u);  // the next claim flies during this tile
+                const PTTile tl = a.tiles[a.order[k]];
+                const int gpos = a.reps[tl.rep].gpos0 + s_pos[tl.rep];
+                pt_run_tile<DIM, HB>(a, tl, colour, t, dcur, s_tab + (size_t)gpos * 16);
+                __syncthreads();
+                if (threadIdx.x == 0) s_ticket = nk;
+                __syncthreads();
+                k = s_ticket;
             }
             if (!grid_sync(a.bar, gridDim.x, gen, a.spin_limit)) return;
         }
@@ -244,8 +290,8 @@ __global__ void __launch_bounds__(256) k_pt_persistent(const PTArgs a) {
                 a.series[((size_t)s * a.nrep + r) * 2] = s_P[r];
                 a.series[((size_t)s * a.nrep + r) * 2 + 1] = s_M[r];
             }
-        if ((t + 1) % (unsigned long long)a.every == 0) {
-            pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, blockIdx.x == 0);
+        if (exch) {
+            pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, blockIdx.x == 0, logu);
             stage ^= 1;
         }
     }
@@ -265,7 +311,10 @@ __global__ void __launch_bounds__(256) k_pt_plain_half(const PTArgs a, int tile0
                                                        unsigned long long sweep) {
     __shared__ unsigned long long s_thr[16];
     const PTTile tl = a.tiles[tile0 + blockIdx.x];
-    pt_run_tile<DIM, HB>(a, tl, colour, sweep, a.pos[tl.rep], a.delta, s_thr);
+    if (threadIdx.x < 16)
+        s_thr[threadIdx.x] = a.tables[(size_t)(a.reps[tl.rep].gpos0 + a.pos[tl.rep]) * 16 + threadIdx.x];
+    __syncthreads();
+    pt_run_tile<DIM, HB>(a, tl, colour, sweep, a.delta, s_thr);
 }
 
 // Plain form: fold the sweep's deltas into the state, record, exchange (one block).
@@ -291,7 +340,7 @@ __global__ void __launch_bounds__(256) k_pt_plain_exchange(const PTArgs a, long 
     __syncthreads();
     if ((t + 1) % (unsigned long long)a.every != 0) return;
     const int stage = *a.stage;
-    pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, true);
+    pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, true, nullptr);
     for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) a.pos[r] = s_pos[r];
     if (threadIdx.x == 0) *a.stage = stage ^ 1;
 }
@@ -329,9 +378,9 @@ struct mcx_pt {
     int8_t* d_arena = nullptr;
     PTReplica* d_reps = nullptr;
     PTTile* d_tiles = nullptr;
-    int* d_block_tiles = nullptr;
-    int* d_block_off = nullptr;
-    int grid = 0;  // persistent grid size the schedule was built for
+    int* d_order = nullptr;          // tiles in claiming order (largest first)
+    unsigned int* d_claim = nullptr; // per-phase tile tickets
+    int grid = 0;                    // persistent grid size
     unsigned long long* d_tables = nullptr;  // [3 algs][npos][16]
     double* d_betas = nullptr;
     int* d_pos_ladder = nullptr;
@@ -347,6 +396,7 @@ struct mcx_pt {
     long long* d_series = nullptr;
     int64_t series_cap = 0;
     unsigned int* d_bar = nullptr;
+    double* d_logu = nullptr;
     int8_t* d_lin = nullptr;
     size_t lin_bytes = 0;
     std::vector<std::pair<void*, size_t>> allocs;
@@ -389,30 +439,21 @@ static size_t pt_smem(const mcx_pt* pt) {
     return (size_t)pt->nrep * (2 * sizeof(long long) + sizeof(int)) + (size_t)pt->npos * sizeof(int);
 }
 
-// Longest-processing-time assignment of tiles to `grid` blocks, stored as CSR.
+static size_t pt_smem_persistent(const mcx_pt* pt) { return pt_smem(pt) + (size_t)pt->npos * 16 * 8; }
+
+// Claiming order of the persistent form: tiles sorted by estimated cost, largest
+// first (blocks then take tiles from a ticket counter, which balances the phase).
 static mcx_status pt_schedule(mcx_pt* pt, int grid) {
     std::vector<int> order(pt->tiles.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return pt->tiles[x].sites > pt->tiles[y].sites; });
-    using Item = std::pair<long long, int>;
-    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
-    for (int b = 0; b < grid; ++b) heap.push({0, b});
-    std::vector<std::vector<int>> per(grid);
-    for (int t : order) {
-        Item it = heap.top();
-        heap.pop();
-        per[it.second].push_back(t);
-        heap.push({it.first + pt->tiles[t].sites, it.second});
-    }
-    std::vector<int> off(grid + 1, 0), list;
-    for (int b = 0; b < grid; ++b) {
-        std::sort(per[b].begin(), per[b].end());
-        off[b + 1] = off[b] + (int)per[b].size();
-        list.insert(list.end(), per[b].begin(), per[b].end());
-    }
-    MCX_CHECK(pt_upload(pt, &pt->d_block_tiles, list));
-    MCX_CHECK(pt_upload(pt, &pt->d_block_off, off));
+    auto cost = [&](int t) {
+        const PTTile& T = pt->tiles[t];
+        const int V = pt->reps[T.rep].V;
+        return (double)T.sites * (V == 16 ? 1.0 : (V == 8 ? 1.15 : 1.4));
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    MCX_CHECK(pt_upload(pt, &pt->d_order, order));
+    MCX_CHECK(pt_upload(pt, &pt->d_claim, std::vector<unsigned int>(3, 0u)));
     pt->grid = grid;
     return MCX_OK;
 }
@@ -422,9 +463,10 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->arena = pt->d_arena;
     a->reps = pt->d_reps;
     a->tiles = pt->d_tiles;
-    a->block_tiles = pt->d_block_tiles;
-    a->block_off = pt->d_block_off;
+    a->order = pt->d_order;
+    a->claim = pt->d_claim;
     a->nrep = pt->nrep;
+    a->ntiles = (int)pt->tiles.size();
     a->npos = pt->npos;
     a->tables = pt->d_tables + (size_t)alg * pt->npos * 16;
     a->betas = pt->d_betas;
@@ -439,6 +481,7 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->ex_steps = pt->d_ex_steps;
     a->ex_acc = pt->d_ex_acc;
     a->bar = pt->d_bar;
+    a->logu = pt->d_logu;
     a->J = pt->J;
     a->h = pt->h;
     a->spin_limit = pt->spin_limit;
@@ -574,9 +617,9 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
         pt->npos += n;
     }
     pt->nrep = pt->npos;
-    if (pt->nrep > 2048) {
+    if (pt->nrep > 1024) {
         delete pt;
-        return fail(MCX_ERR_INVALID_ARG, "at most 2048 replicas");
+        return fail(MCX_ERR_INVALID_ARG, "at most 1024 replicas");
     }
     // arena layout: replica r (ladder order), colour 0 then colour 1, 256-byte aligned
     size_t off = 0;
@@ -651,21 +694,19 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
     run(pt_upload(pt, &pt->d_ex_steps, std::vector<unsigned long long>(pt->npos, 0)));
     run(pt_upload(pt, &pt->d_ex_acc, std::vector<unsigned long long>(pt->npos, 0)));
     run(pt_upload(pt, &pt->d_bar, std::vector<unsigned int>(4, 0)));
+    run(pt_upload(pt, &pt->d_logu, std::vector<double>((size_t)2 * pt->npos, 0.0)));
     run(pt_alloc(pt, &p, pt->lin_bytes));
     pt->d_lin = (int8_t*)p;
     if (st == MCX_OK) {
         // schedule for the persistent grid
         int bps = 0;
-        const size_t smem = pt_smem(pt);
+        const size_t smem = pt_smem_persistent(pt);
         const PersistentFn fn = persistent_fn(dim, false);
-        if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(persistent_fn(dim, true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_pt_plain_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_pt_plain_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pt_smem(pt));
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, smem) != cudaSuccess || bps < 1) bps = 1;
-        int grid = ctx->num_sms * bps;
-        if (grid > (int)pt->tiles.size()) grid = (int)pt->tiles.size();
-        run(pt_schedule(pt, grid));
+        run(pt_schedule(pt, ctx->num_sms * bps));
     }
     if (st == MCX_OK) {
         // all spins up, like the reference constructors
@@ -768,14 +809,17 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
     a.every = exchange_every;
     const bool hb = alg == MCX_HEATBATH;
     const size_t smem = pt_smem(pt);
+    const size_t smem_persistent = pt_smem_persistent(pt);
     MCX_CUDA(cudaMemsetAsync(pt->d_acc, 0, (size_t)pt->nrep * sizeof(unsigned long long), ctx->stream));
     if (mode == MCX_PT_PERSISTENT) {
         MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 6 * sizeof(long long), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar, 0, sizeof(unsigned int), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar + 2, 0, sizeof(unsigned int), ctx->stream));
+        MCX_CUDA(cudaMemsetAsync(pt->d_claim, 0, 3 * sizeof(unsigned int), ctx->stream));
         const PersistentFn fn = persistent_fn(pt->dim, hb);
         void* args[] = {&a};
-        MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem, ctx->stream));
+        MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem_persistent,
+                                             ctx->stream));
         count_launch(ctx);
         unsigned int err = 0;
         MCX_CUDA(cudaMemcpyAsync(&err, pt->d_bar + 2, sizeof(err), cudaMemcpyDeviceToHost, ctx->stream));

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
@@ -119,39 +120,14 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
         const unsigned long long j0 = (unsigned long long)r * a.W + k0;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
-            uint32_t cnt = 0;
+            uint32_t nbw[Z];
 #pragma unroll
-            for (int d = 0; d < Z; ++d) cnt += plus1(ch.nb[d][w]);
+            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
             const uint32_t c0 = (uint32_t)(j0 >> 2) + w;
             const uint4 ra = philox10(make_uint4(c0, (uint32_t)a.sweep, w2a, a.stream), a.k0, a.k1);
             uint4 rp = make_uint4(0, 0, 0, 0);
             if (!HB) rp = philox10(make_uint4(c0, (uint32_t)a.sweep, w2p, a.stream), a.k0, a.k1);
-            uint32_t word = ch.own[w];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int S = (cnt >> (8 * b)) & 0xFF;  // c + Z
-                const int so = (int)(int8_t)(word >> (8 * b));
-                const uint32_t u = b == 0 ? ra.x : b == 1 ? ra.y : b == 2 ? ra.z : ra.w;
-                int sn;
-                bool acc;
-                if (HB) {
-                    sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
-                    acc = sn != so;
-                } else {
-                    const uint32_t pw = b == 0 ? rp.x : b == 1 ? rp.y : b == 2 ? rp.z : rp.w;
-                    const int bit = (int)(pw >> 31);
-                    acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
-                    sn = bc_propose(so, bit);
-                }
-                if (acc) {
-                    const int ds = sn - so;
-                    word = (word & ~(0xFFu << (8 * b))) | ((uint32_t)(uint8_t)(int8_t)sn << (8 * b));
-                    ++nacc;
-                    dP += ds * (S - Z);
-                    dM += ds;
-                    dQ += sn * sn - so * so;
-                }
-            }
+            const uint32_t word = bc_word<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, dP, dM, dQ);
             ch.own[w] = word;
         }
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
@@ -214,10 +190,12 @@ static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V) {
     const bool hb = alg == MCX_HEATBATH;
     if (model == MCX_ISING) {
         if (V == 16) return hb ? k_ising_cb<DIM, 16, true> : k_ising_cb<DIM, 16, false>;
+        if (V == 8) return hb ? k_ising_cb<DIM, 8, true> : k_ising_cb<DIM, 8, false>;
         if (V == 4) return hb ? k_ising_cb<DIM, 4, true> : k_ising_cb<DIM, 4, false>;
         return hb ? k_ising_cb_site<DIM, true> : k_ising_cb_site<DIM, false>;
     }
     if (V == 16) return hb ? k_bc_cb<DIM, 16, true> : k_bc_cb<DIM, 16, false>;
+    if (V == 8) return hb ? k_bc_cb<DIM, 8, true> : k_bc_cb<DIM, 8, false>;
     if (V == 4) return hb ? k_bc_cb<DIM, 4, true> : k_bc_cb<DIM, 4, false>;
     return hb ? k_bc_cb_site<DIM, true> : k_bc_cb_site<DIM, false>;
 }
@@ -226,7 +204,12 @@ HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V) 
     return dim == 2 ? pick_kernel_dim<2>(model, alg, V) : pick_kernel_dim<3>(model, alg, V);
 }
 
-int vec_width(int64_t W) { return W % 16 == 0 ? 16 : (W % 4 == 0 ? 4 : 1); }
+int vec_width(int64_t W) { return W % 16 == 0 ? 16 : (W % 8 == 0 ? 8 : (W % 4 == 0 ? 4 : 1)); }
+
+int lattice_width(const mcx_lattice* lat) {
+    const int V = lat->tuned_V;
+    return (V > 0 && lat->W % V == 0) ? V : vec_width(lat->W);
+}
 
 // Grid = min(work, SMs x resident blocks per SM): one wave of a grid-stride kernel.
 int occupancy_grid(const mcx_ctx* ctx, const void* fn, long long work, int block, size_t smem) {
@@ -298,7 +281,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         SweepArgs a;
         fill_sweep_args(&a, lat, t, rng);
         a.acc = lat->d_acc;
-        const int V = vec_width(lat->W);
+        const int V = lattice_width(lat);
         const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
         const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         for (int64_t s = 0; s < nsweeps; ++s) {
@@ -328,5 +311,81 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     } else if (obs) {
         MCX_CUDA(cudaStreamSynchronize(ctx->stream));
     }
+    return MCX_OK;
+}
+
+// ------------------------------------------------------------- autotuning --
+// Times every admissible row width (16, 8, 4 sites per thread; 1 only when nothing
+// else fits) on a scratch copy of the lattice and keeps the fastest for later
+// mcx_sweep calls.  The choice never changes results: every width applies the same
+// stream to the same sites.
+extern "C" MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, double beta, int32_t* chosen,
+                                           double* ns_per_site) {
+    if (!lat) return fail(MCX_ERR_INVALID_ARG, "lattice is NULL");
+    if (!std::isfinite(beta)) return fail(MCX_ERR_INVALID_ARG, "beta must be finite");
+    if (alg != MCX_METROPOLIS && alg != MCX_GLAUBER && alg != MCX_HEATBATH)
+        return fail(MCX_ERR_INVALID_ARG, "unknown algorithm %d", (int)alg);
+    if (lat->layout != MCX_LAYOUT_INT8) {
+        if (chosen) *chosen = 64;
+        if (ns_per_site) *ns_per_site = 0.0;
+        return MCX_OK;
+    }
+    mcx_ctx* ctx = lat->ctx;
+    std::vector<int> cands;
+    for (int V : {16, 8, 4})
+        if (lat->W % V == 0) cands.push_back(V);
+    if (cands.empty()) cands.push_back(1);
+    Table t;
+    MCX_CHECK(build_table(lat, alg, beta, &t));
+    const size_t half = (size_t)(lat->N / 2);
+    void* scratch = nullptr;
+    const size_t bytes = 2 * ((half + 255) / 256 * 256) + 3 * 8 + 8;
+    MCX_CHECK(dev_alloc(ctx, &scratch, bytes));
+    int8_t* col[2] = {(int8_t*)scratch, (int8_t*)scratch + (half + 255) / 256 * 256};
+    unsigned long long* acc = (unsigned long long*)(col[1] + (half + 255) / 256 * 256);
+    unsigned long long* dst = acc + 1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    int best = cands[0];
+    float best_ms = 0.f;
+    mcx_rng r{0x5EEDull, 0, 0, 0};
+    for (size_t ci = 0; ci < cands.size() && err == cudaSuccess; ++ci) {
+        const int V = cands[ci];
+        err = cudaMemcpyAsync(col[0], lat->d_col[0], half, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(col[1], lat->d_col[1], half, cudaMemcpyDeviceToDevice, ctx->stream);
+        SweepArgs a;
+        fill_sweep_args(&a, lat, t, &r);
+        a.acc = acc;
+        for (int j = 0; j < 3; ++j) a.dst[j] = dst + j;
+        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
+        const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
+        const int warm = 2, reps = 8;
+        for (int k = 0; k < warm + reps && err == cudaSuccess; ++k) {
+            if (k == warm) err = cudaEventRecord(e0, ctx->stream);
+            a.sweep = (unsigned long long)(k / 2);
+            a.colour = k & 1;
+            a.cur = col[a.colour];
+            a.oth = col[1 - a.colour];
+            fn<<<grid, 256, 0, ctx->stream>>>(a);
+            count_launch(ctx);
+        }
+        if (err == cudaSuccess) err = cudaEventRecord(e1, ctx->stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        if (err == cudaSuccess && (ci == 0 || ms < best_ms)) {
+            best_ms = ms;
+            best = V;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, scratch, bytes);
+    if (err != cudaSuccess) return cuda_fail(err, "autotune");
+    lat->tuned_V = best;
+    if (chosen) *chosen = best;
+    if (ns_per_site) *ns_per_site = (double)best_ms * 1e6 / (8.0 * (double)half);
     return MCX_OK;
 }

@@ -22,6 +22,7 @@ using HalfSweepFn = void (*)(const SweepArgs);
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V);
 int vec_width(int64_t W);
+int lattice_width(const mcx_lattice* lat);
 int half_sweep_grid(const mcx_ctx* ctx, HalfSweepFn fn, int64_t W, int64_t rows, int V);
 int occupancy_grid(const mcx_ctx* ctx, const void* fn, long long work, int block, size_t smem);
 mcx_status build_table(const mcx_lattice* lat, mcx_algorithm alg, double beta, Table* t);

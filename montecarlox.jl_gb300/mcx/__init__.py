@@ -25,7 +25,7 @@ __all__ = [
     "CudaError", "Context", "default_context", "Philox", "BoltzmannEnsemble", "logweight", "Metropolis",
     "Glauber", "HeatBath", "ensemble", "acceptance_rate", "reset_", "AbstractSystem", "AbstractSpinSystem",
     "Ising", "IsingLatticeOptim", "BlumeCapel", "init_", "energy", "magnetization", "observables",
-    "sweep_", "spin_flip_", "set_spins_", "logistic",
+    "sweep_", "spin_flip_", "set_spins_", "logistic", "autotune_",
 ]
 
 
@@ -405,6 +405,15 @@ def sweep_(sys, alg, nsweeps=1, record=False):
     else:
         alg.accepted += cnt.accepted
     return obs
+
+
+def autotune_(sys, alg):
+    """Pick the fastest kernel shape for this lattice and algorithm (results unchanged).
+    Returns (sites per thread, ns per site per half-sweep)."""
+    v = C.c_int32()
+    ns = C.c_double()
+    _check(L.load().mcx_autotune(sys.handle, alg.ALG, float(alg.beta), C.byref(v), C.byref(ns)))
+    return v.value, ns.value
 
 
 def spin_flip_(sys, alg):

@@ -70,6 +70,7 @@ SIGNATURES = {
     "mcx_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P,
                             C.POINTER(mcx_counters)]),
     "mcx_read_series": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_autotune": (C.c_int, [_P, C.c_int, C.c_double, _i32p, _f64p]),
     "mcx_flathist_create": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "mcx_flathist_destroy": (C.c_int, [_P]),
     "mcx_flathist_set_logweight": (C.c_int, [_P, _P, C.c_int64]),
@@ -83,6 +84,14 @@ SIGNATURES = {
     "mcx_flathist_copy_logweight": (C.c_int, [_P, _P]),
     "mcx_flathist_sweep": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P), C.c_int, C.c_int, C.c_double,
                                      C.POINTER(mcx_rng), C.c_int64, C.POINTER(mcx_counters)]),
+    "mcx_server_create": (C.c_int, [_P, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(_P)]),
+    "mcx_server_destroy": (C.c_int, [_P]),
+    "mcx_server_submit": (C.c_int, [_P, _P, _u64p]),
+    "mcx_server_step": (C.c_int, [_P, _i32p, _i32p]),
+    "mcx_server_poll": (C.c_int, [_P, C.c_uint64, _P]),
+    "mcx_server_cancel": (C.c_int, [_P, C.c_uint64]),
+    "mcx_server_get_stats": (C.c_int, [_P, _P]),
+    "mcx_sweep_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P, _P]),
     "mcx_pt_create": (C.c_int, [_P, C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_double, C.c_double,
                                 C.POINTER(_P)]),
     "mcx_pt_destroy": (C.c_int, [_P]),
@@ -100,6 +109,30 @@ SIGNATURES = {
 }
 
 PT_PERSISTENT, PT_PLAIN = 0, 1
+JOB_CANONICAL, JOB_MULTICANONICAL = 0, 1
+
+
+class mcx_job(C.Structure):
+    _fields_ = [("model", C.c_int32), ("dim", C.c_int32), ("L", C.c_int32 * 3), ("kind", C.c_int32),
+                ("alg", C.c_int32), ("reserved0", C.c_int32), ("beta", C.c_double), ("J", C.c_double),
+                ("D", C.c_double), ("h", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32),
+                ("reserved1", C.c_uint32), ("nsweeps", C.c_int64), ("bin_start", C.c_int64),
+                ("bin_step", C.c_int64), ("nbins", C.c_int64), ("logweight", C.c_void_p),
+                ("obs_series", C.c_void_p), ("histogram", C.c_void_p), ("logweight_out", C.c_void_p),
+                ("final_spins", C.c_void_p)]
+
+
+class mcx_job_result(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("pair_sum", C.c_int64), ("spin_sum", C.c_int64),
+                ("spin2_sum", C.c_int64), ("attempts", C.c_uint64), ("accepted", C.c_uint64),
+                ("sweeps_done", C.c_int64), ("submit_s", C.c_double), ("admit_s", C.c_double),
+                ("finish_s", C.c_double)]
+
+
+class mcx_server_stats(C.Structure):
+    _fields_ = [("active", C.c_int32), ("pending", C.c_int32), ("iterations", C.c_uint64),
+                ("jobs_done", C.c_uint64), ("attempts_done", C.c_uint64), ("bytes_in_use", C.c_uint64),
+                ("peak_bytes", C.c_uint64), ("now_s", C.c_double)]
 
 _lib = None
 

@@ -164,3 +164,17 @@ def test_hbm_budget(gpu):
     used, budget = ctx.memory()
     assert 0 < used <= budget
     small.close()
+
+
+@pytest.mark.parametrize("L,alg", [([4096, 64], "metropolis"), ([48, 48, 48], "heatbath"), ([96, 80], "glauber")])
+def test_autotune_keeps_results(gpu, L, alg):
+    """The autotuner only picks a kernel shape; results stay bit-identical to the oracle."""
+    sys_ = gpu.Ising(L)
+    gpu.init_(sys_, "random", rng=gpu.Philox(4))
+    a = _alg(gpu, alg, 4, 0.3 if len(L) == 2 else 0.22)
+    width, ns = gpu.autotune_(sys_, a)
+    assert width in (4, 8, 16) and ns > 0
+    obs = gpu.sweep_(sys_, a, 3, record=True)
+    s = O.init_random(O.ISING, L, 4)
+    oobs, _, acc = O.cb_sweep(s, O.ISING, L, ALG[alg], 0.3 if len(L) == 2 else 0.22, 4, nsweeps=3)
+    assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s)

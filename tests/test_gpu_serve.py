@@ -1,0 +1,103 @@
+"""Serving: continuous batching, HBM-budget admission, same result alone and in the mix (GPU)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+JOBS = [
+    dict(model="ising", L=(64, 64), kind="canonical", alg="metropolis", beta=0.44, seed=5, stream=0, nsweeps=37),
+    dict(model="bc", L=(48, 40), kind="canonical", alg="heatbath", beta=0.6, D=1.0, seed=5, stream=1, nsweeps=23),
+    dict(model="ising", L=(16, 24), kind="canonical", alg="glauber", beta=0.3, seed=9, stream=2, nsweeps=61),
+    dict(model="ising", L=(32, 32), kind="multicanonical", beta=0.4, seed=5, stream=3, nsweeps=15,
+         bins=(-2048, 4, 1025)),
+    dict(model="bc", L=(16, 16), kind="multicanonical", beta=0.5, D=1.0, seed=5, stream=4, nsweeps=12,
+         bins=(-256, 1, 1025)),
+    dict(model="ising", L=(128, 64), kind="canonical", alg="metropolis", beta=0.6, h=0.25, seed=1, stream=5,
+         nsweeps=19),
+]
+
+
+def _spec(j):
+    j = dict(j)
+    if j["kind"] == "multicanonical":
+        start, step, nb = j["bins"]
+        j["logweight"] = -j["beta"] * (start + step * np.arange(nb)).astype(np.float64)
+    return j
+
+
+def _snapshot(job):
+    r = job.result
+    return (r["state"], r["status"], r["pair_sum"], r["spin_sum"], r["spin2_sum"], r["attempts"], r["accepted"],
+            job.series.tobytes(), job.spins.tobytes(),
+            None if job.histogram is None else job.histogram.tobytes(),
+            None if job.logweight is None else job.logweight.tobytes())
+
+
+def test_same_result_alone_and_in_the_mix(gpu):
+    from mcx.serve import Server
+    alone = []
+    for j in JOBS:
+        srv = Server(chunk=7)
+        job = srv.submit(spins=True, **_spec(j))
+        srv.run_until_idle()
+        assert srv.poll(job) is not None and job.result["state"] == 2
+        alone.append(_snapshot(job))
+        srv.close()
+    # in the mix: staggered arrivals, a budget that holds only some jobs at once
+    srv = Server(hbm_budget=30_000, max_jobs=4, chunk=5)
+    jobs = []
+    for k, j in enumerate(JOBS):
+        jobs.append(srv.submit(spins=True, **_spec(j)))
+        if k % 2 == 1:
+            srv.step()
+    srv.run_until_idle()
+    st = srv.stats()
+    assert st["peak_bytes"] <= 30_000 and st["jobs_done"] == len(JOBS)
+    for job, ref in zip(jobs, alone):
+        assert srv.poll(job) is not None
+        assert _snapshot(job) == ref  # bit for bit
+
+
+def test_canonical_job_matches_oracle(gpu):
+    from mcx.serve import Server
+    srv = Server(chunk=4)
+    job = srv.submit(spins=True, **JOBS[0])
+    srv.run_until_idle()
+    srv.poll(job)
+    L = [64, 64]
+    s = O.init_random(O.ISING, L, 5, 0)
+    obs, att, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.44, 5, stream=0, nsweeps=37)
+    assert np.array_equal(job.series, obs)
+    assert np.array_equal(job.spins, s)
+    assert (job.result["attempts"], job.result["accepted"]) == (att, acc)
+
+
+def test_multicanonical_job_matches_oracle(gpu):
+    from mcx.serve import Server
+    spec = _spec(JOBS[3])
+    srv = Server(chunk=6)
+    job = srv.submit(spins=True, **spec)
+    srv.run_until_idle()
+    srv.poll(job)
+    L = [32, 32]
+    s = O.init_random(O.ISING, L, 5, 3)
+    lnw = spec["logweight"].copy()
+    H = np.zeros(len(lnw), np.int64)
+    rc, obs, st, ac = O.flathist_sweep(s, O.ISING, L, O.MUCA, lnw, H, -2048, 4, 0.0, 5, stream=3, nsweeps=15)
+    assert rc == O.OK
+    assert np.array_equal(job.series, obs) and np.array_equal(job.spins, s)
+    assert np.array_equal(job.histogram, H)
+    assert (job.result["attempts"], job.result["accepted"]) == (st, ac)
+
+
+def test_budget_rejects_oversized_job_and_cancel(gpu):
+    from mcx.serve import Server
+    srv = Server(hbm_budget=10_000, max_jobs=2, chunk=5)
+    with pytest.raises(gpu.BudgetError):
+        srv.submit(model="ising", L=(256, 256), nsweeps=10)
+    small = srv.submit(model="ising", L=(16, 16), nsweeps=50)
+    srv.cancel(small)
+    srv.run_until_idle()
+    assert srv.poll(small)["state"] == 3
