@@ -225,6 +225,38 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
     }
 
 
+def bench_flathist(torch, mcx, ctx, dev, nwalkers=512, L=1024):
+    """Multicanonical production on 2-D Blume-Capel L=1024, J=1, D=1 (integer energies,
+    4,194,305 bins of FP64 ln g and int64 H shared by the walkers): one sweep of
+    `nwalkers` independent walkers (one warp each).  The walker itself is serial, so the
+    throughput comes from the number of walkers."""
+    from mcx import flathist as F
+
+    N = L * L
+    walkers = []
+    for i in range(nwalkers):
+        s = mcx.BlumeCapel([L, L], D=1.0, ctx=ctx)
+        mcx.init_(s, "random", rng=mcx.Philox(SEED, i))
+        walkers.append(s)
+    ens = F.MulticanonicalEnsemble((-N, 1, 4 * N + 1), ctx=ctx)
+    alg = F.Multicanonical(mcx.Philox(SEED), ens)
+    stream = torch.cuda.current_stream(dev)
+    F.sweep_walkers_(walkers[:8], alg, 1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    F.sweep_walkers_(walkers, alg, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    for s in walkers:
+        s.close()
+    return {"workload": "bc2d_L1024_D1_muca_production_%d_walkers_1_sweep" % nwalkers, "walkers": nwalkers,
+            "bins": 4 * N + 1, "attempts_per_ns": nwalkers * N / (ms * 1e6),
+            "ns_per_attempt_per_walker": ms * 1e6 / N, "ms": ms}
+
+
 def bench_serve(mcx, ctx, njobs=40):
     """Poisson arrivals (200 / s, seed 11) of Metropolis and Multicanonical jobs on 2-D
     Ising / Blume-Capel, L log-uniform in [32, 512] (Multicanonical jobs, whose walker
@@ -339,10 +371,11 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = None
+    pt_res = srv_res = fh_res = None
     if not args.no_extras:
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
+        fh_res = bench_flathist(torch, mcx, ctx, dev)
     if rank != 0:
         return
     cpu = None
@@ -371,6 +404,7 @@ def run_mcx(args):
         "cpu_baseline": cpu,
         "batched_pt": pt_res,
         "serving": srv_res,
+        "flat_histogram": fh_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

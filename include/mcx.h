@@ -187,6 +187,9 @@ MCX_API mcx_status mcx_flathist_update_muca(mcx_flathist* fh);
  * threshold * mean H over the visited bins; ratio = min H / mean H. */
 MCX_API mcx_status mcx_flathist_flatness(mcx_flathist* fh, double threshold, int* is_flat,
                                          double* ratio);
+/* The visited-bin marks of the flatness test (for checkpoint / resume). */
+MCX_API mcx_status mcx_flathist_get_visited(mcx_flathist* fh, uint8_t* host, int64_t n);
+MCX_API mcx_status mcx_flathist_set_visited(mcx_flathist* fh, const uint8_t* host, int64_t n);
 /* merge_histograms! (src/algorithms/parallel_multicanonical.jl:38-47): dst.H += src[i].H. */
 MCX_API mcx_status mcx_flathist_merge(mcx_flathist* dst, mcx_flathist* const* src, int nsrc);
 /* distribute_logweight! (parallel_multicanonical.jl:59-68): dst.lnw := src.lnw. */
@@ -241,6 +244,11 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
 MCX_API mcx_status mcx_pt_indices(mcx_pt* pt, int32_t* positions, int32_t* stage);
 /* rx.steps / rx.accepted per ladder edge, ladder after ladder (n_l - 1 each). */
 MCX_API mcx_status mcx_pt_exchange_counters(mcx_pt* pt, uint64_t* steps, uint64_t* accepted);
+/* Restore ladder positions (a permutation within every ladder), the stage and the
+ * edge counters, e.g. from a checkpoint (src/infrastructure/checkpointing.jl:95-100). */
+MCX_API mcx_status mcx_pt_set_indices(mcx_pt* pt, const int32_t* positions, int32_t stage);
+MCX_API mcx_status mcx_pt_set_exchange_counters(mcx_pt* pt, const uint64_t* steps,
+                                                const uint64_t* accepted);
 /* Cached (pair_sum, spin_sum) of every replica. */
 MCX_API mcx_status mcx_pt_observables(mcx_pt* pt, int64_t* pair_sum, int64_t* spin_sum);
 /* Accepted spin flips of every replica during the last mcx_pt_run. */

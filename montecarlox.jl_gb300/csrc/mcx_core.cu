@@ -338,6 +338,7 @@ mcx_status ensure_series(mcx_lattice* lat, int64_t nsweeps) {
     while (cap < nsweeps) cap *= 2;
     void* p = nullptr;
     MCX_CHECK(dev_alloc(lat->ctx, &p, (size_t)cap * 3 * sizeof(int64_t)));
+    clear_graphs(lat);  // captured sweep sequences point at the old buffer
     dev_free(lat->ctx, lat->d_series, (size_t)lat->series_cap * 3 * sizeof(int64_t));
     lat->device_bytes += (cap - lat->series_cap) * 3 * (int64_t)sizeof(int64_t);
     lat->d_series = (int64_t*)p;
@@ -345,13 +346,22 @@ mcx_status ensure_series(mcx_lattice* lat, int64_t nsweeps) {
     return MCX_OK;
 }
 
-mcx_status finish_series(mcx_lattice* lat, int64_t nsweeps) {
-    k_prefix_series<<<1, 32, 0, lat->ctx->stream>>>((long long*)lat->d_series,
-                                                    (long long*)lat->d_state, nsweeps);
+mcx_status launch_prefix(mcx_lattice* lat, int64_t nsweeps, cudaStream_t stream) {
+    k_prefix_series<<<1, 32, 0, stream>>>((long long*)lat->d_series, (long long*)lat->d_state, nsweeps);
     count_launch(lat->ctx);
     MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+mcx_status finish_series(mcx_lattice* lat, int64_t nsweeps) {
+    MCX_CHECK(launch_prefix(lat, nsweeps, lat->ctx->stream));
     lat->series_len = nsweeps;
     return MCX_OK;
+}
+
+void clear_graphs(mcx_lattice* lat) {
+    for (auto& g : lat->graphs) cudaGraphExecDestroy(g.exec);
+    lat->graphs.clear();
 }
 
 mcx_status msc_pack(mcx_lattice* lat);    // mcx_msc.cu
@@ -432,6 +442,7 @@ MCX_API mcx_status mcx_ctx_create(const mcx_config* cfg, mcx_ctx** out) {
 MCX_API mcx_status mcx_ctx_destroy(mcx_ctx* ctx) {
     if (!ctx) return MCX_OK;
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MCX_OK;
@@ -515,6 +526,8 @@ MCX_API mcx_status mcx_lattice_create(mcx_ctx* ctx, mcx_model model, int dim, co
     grab((void**)&lat->d_state, 3 * sizeof(int64_t));
     grab(&p, sizeof(unsigned long long));
     lat->d_acc = (unsigned long long*)p;
+    grab(&p, sizeof(unsigned long long));
+    lat->d_sweep_base = (unsigned long long*)p;
     if (st == MCX_OK) st = ensure_series(lat, 64);
     if (st != MCX_OK) {
         mcx_lattice_destroy(lat);
@@ -536,6 +549,8 @@ MCX_API mcx_status mcx_lattice_destroy(mcx_lattice* lat) {
     dev_free(ctx, lat->d_lin, (size_t)lat->N);
     dev_free(ctx, lat->d_state, 3 * sizeof(int64_t));
     dev_free(ctx, lat->d_acc, sizeof(unsigned long long));
+    dev_free(ctx, lat->d_sweep_base, sizeof(unsigned long long));
+    clear_graphs(lat);
     dev_free(ctx, lat->d_series, (size_t)lat->series_cap * 3 * sizeof(int64_t));
     delete lat;
     return MCX_OK;

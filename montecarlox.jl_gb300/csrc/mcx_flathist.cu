@@ -46,7 +46,7 @@ constexpr int kFHWarps = 4;
 // Each warp keeps a window of kFHWin log-weights around the walker's current bin in
 // shared memory, so the serial scan never waits on a global load; the window moves
 // when a proposed bin falls outside it (Wang-Landau writes the window back first).
-constexpr int kFHWin = 1024;
+constexpr int kFHWin = 512;
 // Bound on |logf(float(U)) - 53 ln 2 (in float) - log(U)|: float(k) is within 2^-24
 // relative of k, logf within 1 ulp (<= 2^-18 for results below 64 in magnitude), the
 // float constant and subtraction within 2^-18 each: far below 2^-14.
@@ -58,8 +58,17 @@ __device__ __forceinline__ long long fh_window_base(long long b, long long nbins
     return wb < 0 ? 0 : wb;
 }
 
-__device__ __forceinline__ void fh_window_load(double* win, const double* lnw, long long wb, long long nbins, int lane) {
-    for (int i = lane; i < kFHWin; i += 32) win[i] = wb + i < nbins ? lnw[wb + i] : 0.0;
+// FP64 window plus a single-precision copy relative to a centre value c (finite),
+// which the serial scan uses to decide without FP64 arithmetic in the common case.
+__device__ __forceinline__ void fh_window_load(double* win, float* fwin, const double* lnw, long long wb,
+                                               long long nbins, long long centre, int lane, double& c) {
+    const double v = lnw[centre];
+    c = (v - v == 0.0) ? v : 0.0;  // v finite ? v : 0
+    for (int i = lane; i < kFHWin; i += 32) {
+        const double x = wb + i < nbins ? lnw[wb + i] : 0.0;
+        win[i] = x;
+        fwin[i] = (float)(x - c);
+    }
     __syncwarp();
 }
 
@@ -72,9 +81,10 @@ __device__ __forceinline__ void fh_window_store(const double* win, double* lnw, 
 __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
     __shared__ long long s_dE[kFHWarps][32];
     __shared__ unsigned long long s_k[kFHWarps][32];  // U = k * 2^-53
-    __shared__ double s_lo[kFHWarps][32];             // log(U) lies in [lo, hi]
-    __shared__ double s_hi[kFHWarps][32];
+    __shared__ float s_lo[kFHWarps][32];              // log(U) lies in [lo, hi]
+    __shared__ float s_hi[kFHWarps][32];
     __shared__ double s_win[kFHWarps][kFHWin];
+    __shared__ float s_fwin[kFHWarps][kFHWin];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int wid = blockIdx.x * kFHWarps + wl;
     if (wid >= a.nwalkers) return;  // whole warp
@@ -93,9 +103,11 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
     int status = 0;
     if (!fh_bin(E, g, bo)) status = 2;
     double* const win = s_win[wl];
+    float* const fwin = s_fwin[wl];
     long long wb = fh_window_base(status ? 0 : bo, g.nbins);
-    fh_window_load(win, lnw, wb, g.nbins, lane);
-    double lwo = status ? 0.0 : win[bo - wb];
+    double cw = 0.0;
+    fh_window_load(win, fwin, lnw, wb, g.nbins, status ? 0 : bo, lane, cw);
+    float flwo = status ? 0.f : fwin[bo - wb];
     unsigned long long steps = 0, accepted = 0;
     const long long ncol = (long long)g.W * g.Ly * g.Lz;
     const int Z = 2 * g.dim;
@@ -113,7 +125,7 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
                 int sn = 0, ds = 0, dq = 0, dp = 0;
                 long long dE = 0;
                 unsigned long long k53 = 0;
-                double lo = 0.0, hi = 0.0;
+                float lo = 0.f, hi = 0.f;
                 if (valid) {
                     const int r = (int)(j / g.W), k = (int)(j - (long long)r * g.W);
                     const int y = r % g.Ly, z = r / g.Ly;
@@ -136,8 +148,8 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
                     // single-precision log(U) and a margin that bounds its distance to the
                     // FP64 log of the decision rule (logf: <= 1 ulp, |log U| < 37.5)
                     const float l32 = logf(__ull2float_rn(k53)) - 36.7368005696771f;  // 53 ln 2
-                    lo = (double)l32 - kLogMargin;
-                    hi = (double)l32 + kLogMargin;
+                    lo = l32 - (float)kLogMargin;
+                    hi = l32 + (float)kLogMargin;
                 }
                 s_dE[wl][lane] = dE;
                 s_k[wl][lane] = k53;
@@ -161,25 +173,33 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
                                 need = bn;
                                 break;
                             }
-                            const double lwn = win[bn - wb];
-                            const double lr = lwn - lwo;
-                            // lr > 0 || log(U) < lr, deciding from the single-precision
-                            // bracket and computing the FP64 log only inside it
+                            // lr = lnw[bn] - lnw[bo] in FP64, decided from the float copy:
+                            // |lr32 - lr| <= 2^-23 (|fa| + |fb| + |lr32|) (two roundings of
+                            // the centred values, one of the difference), doubled below
+                            const float fa = fwin[bn - wb];
+                            const float lr32 = fa - flwo;
+                            const float e = (fabsf(fa) + fabsf(flwo) + fabsf(lr32)) * 2.384185791015625e-07f + 1e-30f;
                             bool acc;
-                            if (lr > 0.0 || lr > s_hi[wl][i]) acc = true;
-                            else if (lr <= s_lo[wl][i]) acc = false;
-                            else acc = mcx_log((double)s_k[wl][i] * 1.1102230246251565404236316680908203125e-16) < lr;
+                            if (lr32 - e > 0.f || lr32 - e > s_hi[wl][i]) acc = true;
+                            else if (lr32 + e <= s_lo[wl][i]) acc = false;
+                            else {
+                                const double lr = win[bn - wb] - win[bo - wb];
+                                acc = (lr > 0.0) ||
+                                      (mcx_log((double)s_k[wl][i] * 1.1102230246251565404236316680908203125e-16) < lr);
+                            }
                             ++steps;
                             if (acc) {
                                 ++accepted;
                                 accmask |= 1u << i;
                                 E = En;
                                 bo = bn;
-                                lwo = lwn;
+                                flwo = fa;
                             }
                             if (g.mode == 1) {
-                                lwo = lwo - g.logf;
-                                win[bo - wb] = lwo;
+                                const double v = win[bo - wb] - g.logf;
+                                win[bo - wb] = v;
+                                flwo = (float)(v - cw);
+                                fwin[bo - wb] = flwo;
                             }
                             atomicAdd(&H[bo], 1ull);
                         }
@@ -190,8 +210,10 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
                     // one move changes the bin by far less than half the window)
                     __syncwarp();
                     if (g.mode == 1) fh_window_store(win, lnw, wb, g.nbins, lane);
+                    const long long bo_all = __shfl_sync(0xFFFFFFFFu, bo, 0);
                     wb = fh_window_base(need, g.nbins);
-                    fh_window_load(win, lnw, wb, g.nbins, lane);
+                    fh_window_load(win, fwin, lnw, wb, g.nbins, need, lane, cw);
+                    if (lane == 0) flwo = fwin[bo_all - wb];
                 }
                 accmask = __shfl_sync(0xFFFFFFFFu, accmask, 0);
                 status = __shfl_sync(0xFFFFFFFFu, status, 0);
@@ -382,6 +404,22 @@ MCX_API mcx_status mcx_flathist_set_histogram(mcx_flathist* fh, const int64_t* h
 MCX_API mcx_status mcx_flathist_get_histogram(mcx_flathist* fh, int64_t* host, int64_t n) {
     if (!fh || !host || n != fh->nbins) return fail(MCX_ERR_INVALID_ARG, "expected %lld bins", (long long)(fh ? fh->nbins : 0));
     MCX_CUDA(cudaMemcpyAsync(host, fh->d_H, (size_t)n * 8, cudaMemcpyDeviceToHost, fh->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(fh->ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_flathist_get_visited(mcx_flathist* fh, uint8_t* host, int64_t n) {
+    if (!fh || !host || n != fh->nbins) return fail(MCX_ERR_INVALID_ARG, "expected %lld bins", (long long)(fh ? fh->nbins : 0));
+    MCX_CUDA(cudaMemcpyAsync(host, fh->d_visited, (size_t)n, cudaMemcpyDeviceToHost, fh->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(fh->ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_flathist_set_visited(mcx_flathist* fh, const uint8_t* host, int64_t n) {
+    if (!fh || !host || n != fh->nbins) return fail(MCX_ERR_INVALID_ARG, "expected %lld bins", (long long)(fh ? fh->nbins : 0));
+    for (int64_t i = 0; i < n; ++i)
+        if (host[i] > 1) return fail(MCX_ERR_INVALID_ARG, "visited marks are 0 or 1");
+    MCX_CUDA(cudaMemcpyAsync(fh->d_visited, host, (size_t)n, cudaMemcpyHostToDevice, fh->ctx->stream));
     MCX_CUDA(cudaStreamSynchronize(fh->ctx->stream));
     return MCX_OK;
 }

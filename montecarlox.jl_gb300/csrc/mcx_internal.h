@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/mcx.h"
 
@@ -60,6 +61,7 @@ struct mcx_ctx {
     uint64_t used = 0;
     uint64_t launches = 0;
     int num_sms = 0;
+    cudaStream_t capture_stream = nullptr;  // private stream for CUDA-graph capture
 };
 
 struct mcx_lattice {
@@ -84,6 +86,16 @@ struct mcx_lattice {
     int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
+    unsigned long long* d_sweep_base = nullptr;  // first sweep index read by captured graphs
+    struct Graph {
+        int alg;
+        double beta;
+        int64_t nsweeps;
+        int V;
+        const int64_t* series;
+        cudaGraphExec_t exec;
+    };
+    std::vector<Graph> graphs;     // instantiated sweep sequences (most recent last)
 };
 
 namespace mcx {
@@ -95,4 +107,6 @@ mcx_status ensure_series(mcx_lattice* lat, int64_t nsweeps);
 mcx_status recompute_state(mcx_lattice* lat);
 // enqueue kernels that finish a run: prefix-sum the per-sweep deltas into the series
 mcx_status finish_series(mcx_lattice* lat, int64_t nsweeps);
+mcx_status launch_prefix(mcx_lattice* lat, int64_t nsweeps, cudaStream_t stream);
+void clear_graphs(mcx_lattice* lat);
 }  // namespace mcx

@@ -890,6 +890,39 @@ MCX_API mcx_status mcx_pt_replica_accepted(mcx_pt* pt, uint64_t* accepted) {
     return MCX_OK;
 }
 
+MCX_API mcx_status mcx_pt_set_indices(mcx_pt* pt, const int32_t* positions, int32_t stage) {
+    if (!pt || !positions) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (stage != 0 && stage != 1) return fail(MCX_ERR_INVALID_ARG, "stage must be 0 or 1");
+    // every ladder must hold a permutation of its positions
+    std::vector<int> seen(pt->npos, 0);
+    for (int r = 0; r < pt->nrep; ++r) {
+        const int l = pt->rep_ladder[r];
+        const int p = positions[r];
+        if (p < 0 || p >= pt->ladder_n[l] || seen[pt->ladder_gpos0[l] + p]++)
+            return fail(MCX_ERR_INVALID_ARG, "positions are not a permutation within each ladder");
+    }
+    MCX_CUDA(cudaMemcpyAsync(pt->d_pos, positions, pt->nrep * sizeof(int32_t), cudaMemcpyHostToDevice, pt->ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(pt->d_stage, &stage, sizeof(int32_t), cudaMemcpyHostToDevice, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_set_exchange_counters(mcx_pt* pt, const uint64_t* steps, const uint64_t* accepted) {
+    if (!pt || !steps || !accepted) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    std::vector<unsigned long long> s(pt->npos, 0), a(pt->npos, 0);
+    int k = 0;
+    for (int l = 0; l < pt->nladders; ++l)
+        for (int p = 0; p + 1 < pt->ladder_n[l]; ++p, ++k) {
+            if (accepted[k] > steps[k]) return fail(MCX_ERR_INVALID_ARG, "accepted exceeds steps on edge %d", k);
+            s[pt->ladder_gpos0[l] + p] = steps[k];
+            a[pt->ladder_gpos0[l] + p] = accepted[k];
+        }
+    MCX_CUDA(cudaMemcpyAsync(pt->d_ex_steps, s.data(), pt->npos * 8, cudaMemcpyHostToDevice, pt->ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(pt->d_ex_acc, a.data(), pt->npos * 8, cudaMemcpyHostToDevice, pt->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));
+    return MCX_OK;
+}
+
 MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls) {
     if (!pt || polls < 1) return fail(MCX_ERR_INVALID_ARG, "bad argument");
     pt->spin_limit = polls;

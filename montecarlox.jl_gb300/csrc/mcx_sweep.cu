@@ -29,8 +29,9 @@ __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
     const int cpr = a.W / V;
-    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
+    const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, isum = 0, nup = 0;
     for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
                       a.Ly, a.Lz);
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
             uint32_t nbw[Z];
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
-            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
+            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, a.stream), a.k0, a.k1);
             const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
             ch.own[w] ^= fb * 0xFEu;
         }
@@ -67,8 +68,9 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
     const long long n = (long long)a.W * a.rows;
-    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
+    const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, asum = 0, nup = 0;
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
          j += (long long)gridDim.x * blockDim.x) {
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
         if (DIM == 3) S += a.oth[ri.rzp * a.W + k] + a.oth[ri.rzm * a.W + k];
         const int up = s > 0;
         const int al = (s * S + Z) / 2;
-        const uint4 rnd = philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
+        const uint4 rnd = philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2, a.stream), a.k0, a.k1);
         uint32_t u = pick4(rnd, (int)(j & 3));
         if (HB && up) u = ~u;
         if ((unsigned long long)u < s_thr[al + (Z + 1) * up]) {
@@ -105,9 +107,10 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
     const int cpr = a.W / V;
-    const uint32_t w2a = ctr_word2(a.sweep, a.colour, P_ACCEPT);
-    const uint32_t w2p = ctr_word2(a.sweep, a.colour, P_PROPOSE);
+    const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
+    const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
     for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
                       a.Ly, a.Lz);
@@ -124,9 +127,9 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
             const uint32_t c0 = (uint32_t)(j0 >> 2) + w;
-            const uint4 ra = philox10(make_uint4(c0, (uint32_t)a.sweep, w2a, a.stream), a.k0, a.k1);
+            const uint4 ra = philox10(make_uint4(c0, (uint32_t)sweep, w2a, a.stream), a.k0, a.k1);
             uint4 rp = make_uint4(0, 0, 0, 0);
-            if (!HB) rp = philox10(make_uint4(c0, (uint32_t)a.sweep, w2p, a.stream), a.k0, a.k1);
+            if (!HB) rp = philox10(make_uint4(c0, (uint32_t)sweep, w2p, a.stream), a.k0, a.k1);
             const uint32_t word = bc_word<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, dP, dM, dQ);
             ch.own[w] = word;
         }
@@ -145,9 +148,10 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
     const long long n = (long long)a.W * a.rows;
-    const uint32_t w2a = ctr_word2(a.sweep, a.colour, P_ACCEPT);
-    const uint32_t w2p = ctr_word2(a.sweep, a.colour, P_PROPOSE);
+    const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
+    const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
          j += (long long)gridDim.x * blockDim.x) {
@@ -158,14 +162,14 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
         int c = a.oth[j] + a.oth[(long long)r * a.W + ks] + a.oth[ri.ryp * a.W + k] + a.oth[ri.rym * a.W + k];
         if (DIM == 3) c += a.oth[ri.rzp * a.W + k] + a.oth[ri.rzm * a.W + k];
         const int S = c + Z;
-        const uint32_t u = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)a.sweep, w2a, a.stream), a.k0, a.k1), (int)(j & 3));
+        const uint32_t u = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2a, a.stream), a.k0, a.k1), (int)(j & 3));
         int sn;
         bool acc;
         if (HB) {
             sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
             acc = sn != so;
         } else {
-            const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)a.sweep, w2p, a.stream), a.k0, a.k1), (int)(j & 3));
+            const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2p, a.stream), a.k0, a.k1), (int)(j & 3));
             const int bit = (int)(pw >> 31);
             acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
             sn = bc_propose(so, bit);
@@ -243,6 +247,7 @@ mcx_status build_table(const mcx_lattice* lat, mcx_algorithm alg, double beta, T
 }
 
 void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const mcx_rng* rng) {
+    a->sweep_base = nullptr;
     a->W = (int)lat->W;
     a->Ly = (int)lat->L[1];
     a->Lz = (int)lat->L[2];
@@ -255,6 +260,63 @@ void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const
 
 mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
                      int64_t nsweeps);  // mcx_msc.cu
+
+__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// The whole sweep sequence of one call (zero the series and counter, 2*nsweeps
+// half-sweeps, prefix sum) captured once into a CUDA graph on a private stream; the
+// kernels read the first sweep index from lat->d_sweep_base, so the instantiated
+// graph is replayed for every later call with the same algorithm, beta and length.
+static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, const Table& t, int V,
+                              int64_t nsweeps, cudaGraphExec_t* out) {
+    for (auto& g : lat->graphs)
+        if (g.alg == (int)alg && g.beta == beta && g.nsweeps == nsweeps && g.V == V && g.series == lat->d_series) {
+            *out = g.exec;
+            return MCX_OK;
+        }
+    mcx_ctx* ctx = lat->ctx;
+    if (!ctx->capture_stream) MCX_CUDA(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
+    cudaStream_t cs = ctx->capture_stream;
+    SweepArgs a;
+    mcx_rng r0{0, 0, 0, 0};
+    fill_sweep_args(&a, lat, t, &r0);
+    a.sweep_base = lat->d_sweep_base;
+    a.acc = lat->d_acc;
+    const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
+    const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
+    MCX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), cs);
+    for (int64_t s = 0; s < nsweeps && e == cudaSuccess; ++s) {
+        a.sweep = (uint64_t)s;
+        for (int c = 0; c < 2; ++c) {
+            a.colour = c;
+            a.cur = lat->d_col[c];
+            a.oth = lat->d_col[1 - c];
+            for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
+            fn<<<grid, 256, 0, cs>>>(a);
+        }
+    }
+    if (e == cudaSuccess) {
+        const mcx_status ps = launch_prefix(lat, nsweeps, cs);
+        if (ps != MCX_OK) e = cudaErrorUnknown;
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "sweep graph capture");
+    if (lat->graphs.size() >= 4) {
+        cudaGraphExecDestroy(lat->graphs.front().exec);
+        lat->graphs.erase(lat->graphs.begin());
+    }
+    lat->graphs.push_back({(int)alg, beta, nsweeps, V, lat->d_series, exec});
+    *out = exec;
+    return MCX_OK;
+}
 
 }  // namespace mcx
 
@@ -273,10 +335,24 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     Table t;
     MCX_CHECK(build_table(lat, alg, beta, &t));
     MCX_CHECK(ensure_series(lat, nsweeps > 0 ? nsweeps : 1));
-    MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
-    MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
+    // sequences of two or more sweeps replay a captured CUDA graph (which zeroes the
+    // series and counter and ends with the prefix sum itself)
+    const bool graph = lat->layout == MCX_LAYOUT_INT8 && nsweeps >= 2;
+    if (!graph) {
+        MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
+        MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
+    }
     if (lat->layout == MCX_LAYOUT_MSC64) {
         MCX_CHECK(msc_sweep(lat, alg, t, rng, nsweeps));
+    } else if (graph) {
+        const int V = lattice_width(lat);
+        cudaGraphExec_t exec = nullptr;
+        MCX_CHECK(sweep_graph(lat, alg, beta, t, V, nsweeps, &exec));
+        k_set_u64<<<1, 1, 0, ctx->stream>>>(lat->d_sweep_base, (unsigned long long)rng->counter);
+        MCX_CUDA(cudaGetLastError());
+        MCX_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        count_launch(ctx, 2 * (uint64_t)nsweeps + 2);
+        lat->series_len = nsweeps;
     } else {
         SweepArgs a;
         fill_sweep_args(&a, lat, t, rng);
@@ -297,7 +373,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         count_launch(ctx, 2 * (uint64_t)nsweeps);
         MCX_CUDA(cudaGetLastError());
     }
-    MCX_CHECK(finish_series(lat, nsweeps));
+    if (!graph) MCX_CHECK(finish_series(lat, nsweeps));
     rng->counter += (uint64_t)nsweeps;
     if (obs && nsweeps > 0)
         MCX_CUDA(cudaMemcpyAsync(obs, lat->d_series, (size_t)nsweeps * 3 * sizeof(int64_t),

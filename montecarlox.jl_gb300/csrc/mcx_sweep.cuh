@@ -12,7 +12,8 @@ struct SweepArgs {
     const int8_t* oth;  // the other colour
     int W, Ly, Lz, rows, colour;
     uint32_t k0, k1, stream;
-    unsigned long long sweep;
+    unsigned long long sweep;    // sweep index (added to *sweep_base when that is set)
+    const unsigned long long* sweep_base;  // device-resident first sweep index, or null
     unsigned long long* dst[3];  // this sweep's (pair, spin, spin2) delta slots
     unsigned long long* acc;     // accepted-move counter
     unsigned long long thr[kMaxTable];

@@ -105,6 +105,10 @@ SIGNATURES = {
     "mcx_pt_observables": (C.c_int, [_P, _P, _P]),
     "mcx_pt_replica_accepted": (C.c_int, [_P, _P]),
     "mcx_pt_set_wait_limit": (C.c_int, [_P, C.c_int64]),
+    "mcx_pt_set_indices": (C.c_int, [_P, _P, C.c_int32]),
+    "mcx_pt_set_exchange_counters": (C.c_int, [_P, _P, _P]),
+    "mcx_flathist_get_visited": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_flathist_set_visited": (C.c_int, [_P, _P, C.c_int64]),
     "mcx_wait_flag_test": (C.c_int, [_P, C.c_int64]),
 }
 

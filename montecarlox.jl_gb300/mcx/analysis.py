@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 __all__ = ["binning_error", "binned_mean", "binder_cumulant", "jackknife", "onsager_energy_per_site",
-           "onsager_magnetization", "BETA_C"]
+           "onsager_magnetization", "BETA_C", "log_sum", "distribution_from_logdos"]
 
 BETA_C = 0.5 * math.log(1.0 + math.sqrt(2.0))
 
@@ -80,3 +80,31 @@ def onsager_magnetization(beta, J=1.0):
     if b <= BETA_C:
         return 0.0
     return (1.0 - math.sinh(2 * b) ** -4) ** 0.125
+
+
+def log_sum(values):
+    """log(sum(exp(values))) reduced pairwise as the reference's log_sum
+    (src/infrastructure/utils.jl:54-73): c = max + log1p(exp(min - max))."""
+    vals = [float(v) for v in values]
+    if not vals:
+        raise ValueError("values must be non-empty")
+    acc = vals[0]
+    for b in vals[1:]:
+        a = acc
+        acc = a + math.log1p(math.exp(b - a)) if a > b else b + math.log1p(math.exp(a - b))
+    return acc
+
+
+def distribution_from_logdos(centers, logdos, beta):
+    """Canonical distribution at beta from a log density of states: reweight with
+    exp(-beta E) over the finite entries and normalise (reweighting,
+    src/infrastructure/utils.jl:95-105).  Entries that are not finite get 0."""
+    E = np.asarray(centers, np.float64)
+    lw = np.asarray(logdos, np.float64) - beta * E
+    mask = np.isfinite(lw)
+    if not mask.any():
+        raise ValueError("logdos must contain at least one finite entry")
+    lz = log_sum(lw[mask])
+    out = np.zeros_like(lw)
+    out[mask] = np.exp(lw[mask] - lz)
+    return out

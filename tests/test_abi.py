@@ -86,3 +86,31 @@ def test_set_betas(mcxlib):
         set_betas(1, 0.1, 0.2, ":uniform")
     with pytest.raises(mcxlib.ArgumentError):
         set_betas(4, 0.1, 0.2, ":linear")
+
+
+def test_analysis_helpers(mcxlib):
+    import json
+    import math
+    import os
+    import numpy as np
+    from mcx.analysis import (binning_error, binder_cumulant, distribution_from_logdos, log_sum,
+                              onsager_energy_per_site, onsager_magnetization, BETA_C)
+    # utils.jl docstring: exp(log_sum(log 2, log 3)) == 5
+    assert abs(math.exp(log_sum([math.log(2.0), math.log(3.0)])) - 5.0) < 1e-12
+    # exact DOS fixture reweighted: normalised, mean energy finite and below zero at beta 0.4
+    d = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ising2d_8x8_logdos.json")))
+    E = np.arange(-128, 129, 4)
+    tab = dict((e, v) for e, v in d["energy_logdos"])
+    ld = np.array([tab.get(int(e), np.nan) for e in E])
+    p = distribution_from_logdos(E, ld, 0.4)
+    assert abs(p.sum() - 1) < 1e-12 and p[1] == 0.0 and (E * p).sum() < 0
+    # Onsager: known values
+    assert abs(onsager_magnetization(0.6) - 0.97360866744) < 1e-9
+    assert onsager_magnetization(0.4) == 0.0
+    assert abs(BETA_C - 0.44068679350977147) < 1e-15
+    assert abs(onsager_energy_per_site(0.3) + 0.70449907083) < 1e-9
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=65536)
+    assert abs(binning_error(x) - 1 / 256) < 0.001
+    u, eu = binder_cumulant(rng.normal(size=65536))
+    assert abs(u) < 4 * eu + 1e-3
