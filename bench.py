@@ -291,8 +291,12 @@ def run_mcx(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # an explicit stream shared by torch (flush, events) and the library: a context
+    # given no stream (handle 0) would run on a private stream the events do not see
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     ctx = mcx.Context(device=local, stream=stream.cuda_stream)
+    assert ctx.stream == stream.cuda_stream
     S = args.sweeps_per_step
     L = [L_SIDE, L_SIDE]
     N = L_SIDE * L_SIDE
@@ -417,7 +421,9 @@ def run_profile_target(args):
 
     import mcx
 
-    ctx = mcx.Context(device=0, stream=torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = mcx.Context(device=0, stream=stream.cuda_stream)
     if args.profile == "pt":
         from mcx.pt import ParallelTempering, set_betas
         ladders = [(L, set_betas(n, 0.20, 0.25, ":geometric")) for L, n in zip(PT_SIZES, PT_COUNTS)]

@@ -102,6 +102,9 @@ MCX_API int mcx_version(void);
 
 /* --------------------------------------------------------------- context -- */
 MCX_API mcx_status mcx_ctx_create(const mcx_config* config, mcx_ctx** out);
+/* Releases the caller's handle.  Lattices, ensembles, ladders and servers created on
+ * the context each hold it too: its stream and memory accounting are freed when the
+ * last of them is destroyed, so the handles may be destroyed in any order. */
 MCX_API mcx_status mcx_ctx_destroy(mcx_ctx* ctx);
 MCX_API mcx_status mcx_sync(mcx_ctx* ctx);
 MCX_API mcx_status mcx_ctx_stream(mcx_ctx* ctx, void** stream);

@@ -38,6 +38,15 @@ mcx_status cuda_fail(cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? MCX_ERR_OOM : MCX_ERR_CUDA;
 }
 
+void ctx_release(mcx_ctx* ctx) {
+    if (ctx->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
 mcx_status dev_alloc(mcx_ctx* ctx, void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return MCX_OK;
@@ -442,9 +451,7 @@ MCX_API mcx_status mcx_ctx_create(const mcx_config* cfg, mcx_ctx** out) {
 MCX_API mcx_status mcx_ctx_destroy(mcx_ctx* ctx) {
     if (!ctx) return MCX_OK;
     cudaStreamSynchronize(ctx->stream);
-    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
-    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    ctx_release(ctx);
     return MCX_OK;
 }
 
@@ -496,6 +503,7 @@ MCX_API mcx_status mcx_lattice_create(mcx_ctx* ctx, mcx_model model, int dim, co
     }
     mcx_lattice* lat = new mcx_lattice();
     lat->ctx = ctx;
+    lat->hold.set(ctx);
     lat->model = model;
     lat->layout = layout;
     lat->dim = dim;
@@ -526,7 +534,7 @@ MCX_API mcx_status mcx_lattice_create(mcx_ctx* ctx, mcx_model model, int dim, co
     grab((void**)&lat->d_state, 3 * sizeof(int64_t));
     grab(&p, sizeof(unsigned long long));
     lat->d_acc = (unsigned long long*)p;
-    grab(&p, sizeof(unsigned long long));
+    grab(&p, 4 * sizeof(unsigned long long));
     lat->d_sweep_base = (unsigned long long*)p;
     if (st == MCX_OK) st = ensure_series(lat, 64);
     if (st != MCX_OK) {
@@ -549,7 +557,7 @@ MCX_API mcx_status mcx_lattice_destroy(mcx_lattice* lat) {
     dev_free(ctx, lat->d_lin, (size_t)lat->N);
     dev_free(ctx, lat->d_state, 3 * sizeof(int64_t));
     dev_free(ctx, lat->d_acc, sizeof(unsigned long long));
-    dev_free(ctx, lat->d_sweep_base, sizeof(unsigned long long));
+    dev_free(ctx, lat->d_sweep_base, 4 * sizeof(unsigned long long));
     clear_graphs(lat);
     dev_free(ctx, lat->d_series, (size_t)lat->series_cap * 3 * sizeof(int64_t));
     delete lat;

@@ -357,6 +357,7 @@ MCX_API mcx_status mcx_flathist_create(mcx_ctx* ctx, int64_t start, int64_t step
     if (step <= 0 || nbins <= 0) return fail(MCX_ERR_INVALID_ARG, "need step > 0 and nbins > 0");
     mcx_flathist* fh = new mcx_flathist();
     fh->ctx = ctx;
+    fh->hold.set(ctx);
     fh->start = start;
     fh->step = step;
     fh->nbins = nbins;

@@ -8,6 +8,7 @@
 
 struct mcx_flathist {
     mcx_ctx* ctx = nullptr;
+    mcx::CtxHold hold;  // keeps ctx alive while this object exists
     int64_t start = 0, step = 1, nbins = 0;
     double* d_lnw = nullptr;
     unsigned long long* d_H = nullptr;

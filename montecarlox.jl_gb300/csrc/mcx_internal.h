@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -62,10 +63,35 @@ struct mcx_ctx {
     uint64_t launches = 0;
     int num_sms = 0;
     cudaStream_t capture_stream = nullptr;  // private stream for CUDA-graph capture
+    // the caller's handle plus one per live object created on this context: the
+    // streams and the accounting stay valid until the last of them is destroyed, in
+    // whatever order a garbage collector finalises them
+    std::atomic<int> refs{1};
 };
+
+namespace mcx {
+void ctx_release(mcx_ctx* ctx);
+
+// Reference to the context held by every object created on it.
+struct CtxHold {
+    mcx_ctx* p = nullptr;
+    CtxHold() = default;
+    CtxHold(const CtxHold&) = delete;
+    CtxHold& operator=(const CtxHold&) = delete;
+    void set(mcx_ctx* c) {
+        if (c) c->refs.fetch_add(1);
+        if (p) ctx_release(p);
+        p = c;
+    }
+    ~CtxHold() {
+        if (p) ctx_release(p);
+    }
+};
+}  // namespace mcx
 
 struct mcx_lattice {
     mcx_ctx* ctx = nullptr;
+    mcx::CtxHold hold;  // keeps ctx alive while the lattice exists
     mcx_model model = MCX_ISING;
     mcx_layout layout = MCX_LAYOUT_INT8;
     int dim = 2;
@@ -86,7 +112,7 @@ struct mcx_lattice {
     int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
-    unsigned long long* d_sweep_base = nullptr;  // first sweep index read by captured graphs
+    unsigned long long* d_sweep_base = nullptr;  // {first sweep, seed, stream} read by captured graphs
     struct Graph {
         int alg;
         double beta;

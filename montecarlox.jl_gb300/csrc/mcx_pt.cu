@@ -365,6 +365,7 @@ using namespace mcx;
 
 struct mcx_pt {
     mcx_ctx* ctx = nullptr;
+    mcx::CtxHold hold;  // keeps ctx alive while this object exists
     int dim = 3;
     double J = 1, h = 0;
     int nladders = 0, nrep = 0, npos = 0;
@@ -585,6 +586,7 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
     if (!std::isfinite(J) || !std::isfinite(h)) return fail(MCX_ERR_INVALID_ARG, "J and h must be finite");
     mcx_pt* pt = new mcx_pt();
     pt->ctx = ctx;
+    pt->hold.set(ctx);
     pt->dim = dim;
     pt->J = J;
     pt->h = h;

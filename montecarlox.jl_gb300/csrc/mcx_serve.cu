@@ -162,6 +162,7 @@ double now_s(std::chrono::steady_clock::time_point t0) {
 
 struct mcx_server {
     mcx_ctx* ctx = nullptr;
+    mcx::CtxHold hold;  // keeps ctx alive while this object exists
     uint64_t budget = 0, used = 0, peak = 0;
     int max_jobs = 0, chunk = 0;
     uint64_t next_id = 1;
@@ -460,6 +461,7 @@ MCX_API mcx_status mcx_server_create(mcx_ctx* ctx, uint64_t hbm_budget, int32_t 
     if (max_jobs < 1 || chunk_sweeps < 1) return fail(MCX_ERR_INVALID_ARG, "max_jobs and chunk_sweeps must be >= 1");
     mcx_server* s = new mcx_server();
     s->ctx = ctx;
+    s->hold.set(ctx);
     s->budget = hbm_budget;
     s->max_jobs = max_jobs;
     s->chunk = chunk_sweeps;

@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
-    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
+    const SweepKey key = sweep_key(a);
+    const unsigned long long sweep = key.sweep;
     const int cpr = a.W / V;
     const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, isum = 0, nup = 0;
@@ -47,7 +48,7 @@ __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
             uint32_t nbw[Z];
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
-            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, a.stream), a.k0, a.k1);
+            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, key.stream), key.k0, key.k1);
             const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
             ch.own[w] ^= fb * 0xFEu;
         }
@@ -68,7 +69,8 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
-    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
+    const SweepKey key = sweep_key(a);
+    const unsigned long long sweep = key.sweep;
     const long long n = (long long)a.W * a.rows;
     const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, asum = 0, nup = 0;
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
         if (DIM == 3) S += a.oth[ri.rzp * a.W + k] + a.oth[ri.rzm * a.W + k];
         const int up = s > 0;
         const int al = (s * S + Z) / 2;
-        const uint4 rnd = philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2, a.stream), a.k0, a.k1);
+        const uint4 rnd = philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2, key.stream), key.k0, key.k1);
         uint32_t u = pick4(rnd, (int)(j & 3));
         if (HB && up) u = ~u;
         if ((unsigned long long)u < s_thr[al + (Z + 1) * up]) {
@@ -107,7 +109,8 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
-    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
+    const SweepKey key = sweep_key(a);
+    const unsigned long long sweep = key.sweep;
     const int cpr = a.W / V;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
@@ -127,9 +130,9 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
             const uint32_t c0 = (uint32_t)(j0 >> 2) + w;
-            const uint4 ra = philox10(make_uint4(c0, (uint32_t)sweep, w2a, a.stream), a.k0, a.k1);
+            const uint4 ra = philox10(make_uint4(c0, (uint32_t)sweep, w2a, key.stream), key.k0, key.k1);
             uint4 rp = make_uint4(0, 0, 0, 0);
-            if (!HB) rp = philox10(make_uint4(c0, (uint32_t)sweep, w2p, a.stream), a.k0, a.k1);
+            if (!HB) rp = philox10(make_uint4(c0, (uint32_t)sweep, w2p, key.stream), key.k0, key.k1);
             const uint32_t word = bc_word<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, dP, dM, dQ);
             ch.own[w] = word;
         }
@@ -148,7 +151,8 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
-    const unsigned long long sweep = a.sweep_base ? *a.sweep_base + a.sweep : a.sweep;
+    const SweepKey key = sweep_key(a);
+    const unsigned long long sweep = key.sweep;
     const long long n = (long long)a.W * a.rows;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
@@ -162,14 +166,14 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
         int c = a.oth[j] + a.oth[(long long)r * a.W + ks] + a.oth[ri.ryp * a.W + k] + a.oth[ri.rym * a.W + k];
         if (DIM == 3) c += a.oth[ri.rzp * a.W + k] + a.oth[ri.rzm * a.W + k];
         const int S = c + Z;
-        const uint32_t u = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2a, a.stream), a.k0, a.k1), (int)(j & 3));
+        const uint32_t u = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2a, key.stream), key.k0, key.k1), (int)(j & 3));
         int sn;
         bool acc;
         if (HB) {
             sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
             acc = sn != so;
         } else {
-            const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2p, a.stream), a.k0, a.k1), (int)(j & 3));
+            const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2p, key.stream), key.k0, key.k1), (int)(j & 3));
             const int bit = (int)(pw >> 31);
             acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
             sn = bc_propose(so, bit);
@@ -261,12 +265,18 @@ void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const
 mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
                      int64_t nsweeps);  // mcx_msc.cu
 
-__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+__global__ void k_set_key(unsigned long long* p, unsigned long long sweep, unsigned long long seed,
+                          unsigned long long stream) {
+    p[0] = sweep;
+    p[1] = seed;
+    p[2] = stream;
+}
 
 // The whole sweep sequence of one call (zero the series and counter, 2*nsweeps
 // half-sweeps, prefix sum) captured once into a CUDA graph on a private stream; the
-// kernels read the first sweep index from lat->d_sweep_base, so the instantiated
-// graph is replayed for every later call with the same algorithm, beta and length.
+// kernels read the first sweep index and the Philox key from lat->d_sweep_base, so the
+// instantiated graph is replayed for every later call with the same algorithm, beta and
+// length, whatever the random stream.
 static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, const Table& t, int V,
                               int64_t nsweeps, cudaGraphExec_t* out) {
     for (auto& g : lat->graphs)
@@ -348,7 +358,8 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         const int V = lattice_width(lat);
         cudaGraphExec_t exec = nullptr;
         MCX_CHECK(sweep_graph(lat, alg, beta, t, V, nsweeps, &exec));
-        k_set_u64<<<1, 1, 0, ctx->stream>>>(lat->d_sweep_base, (unsigned long long)rng->counter);
+        k_set_key<<<1, 1, 0, ctx->stream>>>(lat->d_sweep_base, (unsigned long long)rng->counter,
+                                            (unsigned long long)rng->seed, (unsigned long long)rng->stream);
         MCX_CUDA(cudaGetLastError());
         MCX_CUDA(cudaGraphLaunch(exec, ctx->stream));
         count_launch(ctx, 2 * (uint64_t)nsweeps + 2);

@@ -12,12 +12,27 @@ struct SweepArgs {
     const int8_t* oth;  // the other colour
     int W, Ly, Lz, rows, colour;
     uint32_t k0, k1, stream;
-    unsigned long long sweep;    // sweep index (added to *sweep_base when that is set)
-    const unsigned long long* sweep_base;  // device-resident first sweep index, or null
+    unsigned long long sweep;    // sweep index (added to sweep_base[0] when that is set)
+    // device-resident {first sweep index, seed, stream} that replace (0, k0|k1<<32,
+    // stream) when set (captured CUDA graphs), or null
+    const unsigned long long* sweep_base;
     unsigned long long* dst[3];  // this sweep's (pair, spin, spin2) delta slots
     unsigned long long* acc;     // accepted-move counter
     unsigned long long thr[kMaxTable];
 };
+
+struct SweepKey {
+    unsigned long long sweep;
+    uint32_t k0, k1, stream;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ SweepKey sweep_key(const SweepArgs& a) {
+    if (!a.sweep_base) return SweepKey{a.sweep, a.k0, a.k1, a.stream};
+    const unsigned long long seed = a.sweep_base[1];
+    return SweepKey{a.sweep_base[0] + a.sweep, (uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)a.sweep_base[2]};
+}
+#endif
 
 using HalfSweepFn = void (*)(const SweepArgs);
 

@@ -119,6 +119,39 @@ def test_sweeps_compose_and_replay(gpu):
     assert m1.accepted == m2.accepted and m1.rng.counter == 8
 
 
+def test_replayed_sequence_follows_each_calls_stream(gpu):
+    """Multi-sweep calls replay one captured sequence per (algorithm, beta, length):
+    every replay must still use its own call's seed, stream and counter."""
+    L = [32, 32]
+    s0 = O.init_random(O.ISING, L, 1, 0)
+    sys_ = gpu.Ising(L)
+    for seed, stream, counter in ((11, 0, 0), (12, 3, 0), (11, 0, 40), (99, 7, 5)):
+        sys_.spins = s0
+        a = gpu.Metropolis(gpu.Philox(seed, stream, counter), beta=0.45)
+        obs = gpu.sweep_(sys_, a, 4, record=True)
+        s = s0.copy()
+        oobs, att, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.45, seed, stream=stream, nsweeps=4,
+                                    sweep0=counter)
+        assert np.array_equal(obs, oobs), (seed, stream, counter)
+        assert np.array_equal(sys_.spins, s)
+        assert a.accepted == acc
+
+
+def test_context_outlives_its_objects(gpu):
+    """Destroying the context handle first leaves its lattices usable; the stream and
+    accounting go away with the last object (finalisers may run in any order)."""
+    ctx = gpu.Context()
+    sys_ = gpu.Ising([16, 16], ctx=ctx)
+    gpu.init_(sys_, "random", rng=gpu.Philox(3))
+    s = O.init_random(O.ISING, [16, 16], 3)
+    ctx.close()
+    a = gpu.Metropolis(gpu.Philox(3), beta=0.4)
+    obs = gpu.sweep_(sys_, a, 3, record=True)
+    oobs, _, _ = O.cb_sweep(s, O.ISING, [16, 16], O.METROPOLIS, 0.4, 3, nsweeps=3)
+    assert np.array_equal(obs, oobs)
+    sys_.close()
+
+
 def test_known_answers_through_the_abi(gpu):
     # SpinSystems/test/test_ising.jl:8-35
     sys_ = gpu.Ising([4, 4])
