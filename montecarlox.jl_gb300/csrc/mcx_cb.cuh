@@ -145,12 +145,21 @@ struct Chunk {
     }
 };
 
+// Table entry of ising_word: heat-bath entries of up sites (idx >= Z+1) hold 2^32 - thr,
+// the probability of staying up; the decision is inverted for up sites once per word,
+// so the uniforms need no per-site complement.
+__host__ __device__ __forceinline__ unsigned long long ising_tab_entry(unsigned long long thr, int idx, int Z,
+                                                                      bool hb) {
+    return (hb && idx >= Z + 1) ? (1ull << 32) - thr : thr;
+}
+
 // Ising decision for the four sites of one 32-bit word (bytes 0x01 = up, 0xFF = down).
 // Per byte: cnt2 = 2 * (down neighbours) from one AND per neighbour word; U1 = 1 for
 // an up site; idx2 = 2 * (a + (Z+1)*up) with a = aligned neighbours, which is
 // cnt2 for a down site and 2(2Z+1) - cnt2 for an up site, formed byte-parallel with
 // (cnt2 ^ 30) = 30 - cnt2 (cnt2 even, <= 12).  4*idx2 is the byte offset of the
-// 8-byte table entry.  One Philox call feeds the four 64-bit threshold compares.
+// 8-byte table entry (ising_tab_entry form).  One Philox call feeds the four 64-bit
+// threshold compares.
 // Returns the flip bits (0/1 per byte); accumulates flips, flipped up spins and the
 // sum of idx2 over flips (sum a = (isum - (2Z+2)*nup) / 2).
 template <int Z, bool HB>
@@ -168,16 +177,59 @@ __device__ __forceinline__ uint32_t ising_word(const uint32_t (&nbw)[Z], uint32_
     uint32_t fb = 0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        uint32_t u = us[b];
-        if (HB) u ^= 0u - ((U1 >> (8 * b)) & 1u);
         const uint32_t o = __byte_perm(off, 0u, 0x4440u + b);
         const unsigned long long t = *reinterpret_cast<const unsigned long long*>(tb + o);
-        if ((unsigned long long)u < t) fb |= 1u << (8 * b);
+        if ((unsigned long long)us[b] < t) fb |= 1u << (8 * b);
     }
+    // heat bath: an up site's entry is 2^32 - thr, and u below it keeps the spin up
+    if (HB) fb ^= U1;
     nacc += __popc(fb);
     nup += __popc(fb & U1);
     isum += (int)(((idx2 & (fb * 0xFFu)) * 0x01010101u) >> 24);
     return fb;
+}
+
+// ising_word with 32-bit thresholds: entry t - 1 for the ising_tab_entry value t, usable
+// when no entry is 0 (then u < t <=> u <= t - 1 for every t in [1, 2^32]): one 32-bit
+// compare per site.  Flip counts go to byte-lane counters of the caller's chunk (at most
+// four words: af, au <= 4 and ai <= 4 * 26 per byte), summed once per chunk.
+template <int Z, bool HB>
+__device__ __forceinline__ uint32_t ising_word32(const uint32_t (&nbw)[Z], uint32_t own, uint4 rnd,
+                                                 const uint32_t* s_t32, uint32_t& af, uint32_t& au, uint32_t& ai) {
+    uint32_t cnt2 = 0;
+#pragma unroll
+    for (int d = 0; d < Z; ++d) cnt2 += nbw[d] & 0x02020202u;
+    const uint32_t U1 = (~own & 0x02020202u) >> 1;
+    const uint32_t idx2 = (cnt2 ^ (U1 * 30u)) - U1 * (uint32_t)(30 - 2 * (2 * Z + 1));
+    const uint32_t off = idx2 << 1;  // 4 * idx
+    const char* tb = reinterpret_cast<const char*>(s_t32);
+    const uint32_t us[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+    uint32_t fb = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const uint32_t o = __byte_perm(off, 0u, 0x4440u + b);
+        if (us[b] <= *reinterpret_cast<const uint32_t*>(tb + o)) fb |= 1u << (8 * b);
+    }
+    if (HB) fb ^= U1;
+    af += fb;
+    au += fb & U1;
+    ai += idx2 & (fb * 0xFFu);
+    return fb;
+}
+
+// sums of the byte lanes of x (total below 256) and of x with bytes below 256 (any total)
+__device__ __forceinline__ int hsum8(uint32_t x) { return (int)((x * 0x01010101u) >> 24); }
+__device__ __forceinline__ int hsum16(uint32_t x) {
+    x = (x & 0x00FF00FFu) + ((x >> 8) & 0x00FF00FFu);
+    return (int)((x * 0x00010001u) >> 16);
+}
+
+// Whether every Ising table entry (ising_tab_entry form) is at least 1, so the 32-bit
+// form of ising_word32 applies.
+inline bool ising_table_fits32(const uint64_t* thr, int n, int Z, bool hb) {
+    for (int i = 0; i < n; ++i)
+        if (ising_tab_entry(thr[i], i, Z, hb) == 0) return false;
+    return true;
 }
 
 // Blume-Capel decision for the four sites of one word (bytes 0xFF, 0x00, 0x01).

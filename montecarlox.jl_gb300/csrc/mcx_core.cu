@@ -43,8 +43,28 @@ void ctx_release(mcx_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+mcx_status ctx_scratch(mcx_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->scratch_bytes) {
+        size_t cap = ctx->scratch_bytes ? ctx->scratch_bytes : 4096;
+        while (cap < bytes) cap *= 2;
+        if (ctx->budget && ctx->used - ctx->scratch_bytes + cap > ctx->budget)
+            return fail(MCX_ERR_BUDGET, "HBM budget exceeded by %zu scratch bytes", cap);
+        MCX_CUDA(cudaStreamSynchronize(ctx->stream));  // the old scratch may still be read
+        if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+        ctx->used -= ctx->scratch_bytes;
+        ctx->d_scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        MCX_CUDA(cudaMalloc(&ctx->d_scratch, cap));
+        ctx->scratch_bytes = cap;
+        ctx->used += cap;
+    }
+    *out = ctx->d_scratch;
+    return MCX_OK;
 }
 
 mcx_status dev_alloc(mcx_ctx* ctx, void** p, size_t bytes) {

@@ -14,11 +14,11 @@
 // The acceptance of a site depends on the running total energy and, for
 // Wang-Landau, on ln g as modified by the previous attempt, so one walker is
 // serial.  Within one colour of a checkerboard sweep, however, every site's energy
-// change is fixed in advance (its neighbours are all of the other colour): a warp
-// computes 32 proposals, energy changes and log-uniforms in parallel, then lane 0
-// runs the short dependent scan over them in site order.  Throughput comes from
-// many walkers (one warp each), the pattern of the reference's parallel
-// multicanonical walkers.
+// change is fixed in advance (its neighbours are all of the other colour): one warp
+// of the walker's block produces proposals, energy changes and log-uniforms for
+// batches of 32 sites while the other warp's lane 0 runs the short dependent scan
+// over the previous batches in site order.  Throughput comes from many walkers (one
+// block each), the pattern of the reference's parallel multicanonical walkers.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -41,16 +41,48 @@ __device__ __forceinline__ bool fh_bin(long long E, const FHGeom& a, long long& 
     return q >= 0 && q < a.nbins;
 }
 
-constexpr int kFHWarps = 4;
+// Each walker is one block of two warps.  The producer warp computes, for batches of
+// 32 consecutive sites of the current colour, the proposals, energy changes and
+// single-precision brackets of log(U) into a ring of kFHSlots shared-memory slots;
+// the consumer warp's lane 0 runs the dependent scan over each batch in site order,
+// then its 32 lanes write the accepted spins.  Within one colour every energy change
+// is fixed in advance (all neighbours are of the other colour), so the producer runs
+// ahead of the scan; at a colour boundary it waits until the consumer has written the
+// last batch.  Hand-offs use named barriers (FULL / EMPTY per slot, COL per colour)
+// that both warps pass in the same sequence whatever happens, so none can wait forever.
+constexpr int kFHSlots = 4;
+constexpr int kFHBarFull = 1, kFHBarEmpty = 5, kFHBarCol = 9;
 
-// Each warp keeps a window of kFHWin log-weights around the walker's current bin in
-// shared memory, so the serial scan never waits on a global load; the window moves
-// when a proposed bin falls outside it (Wang-Landau writes the window back first).
+// Each walker keeps a window of kFHWin log-weights around its current bin in shared
+// memory (FP64 and a single-precision copy relative to a centre value), so the scan
+// never waits on a global load; the window moves when a proposed bin falls outside
+// it (Wang-Landau writes the window back first).  Histogram counts of the window
+// accumulate in shared memory and go to global memory when the window moves.
 constexpr int kFHWin = 512;
 // Bound on |logf(float(U)) - 53 ln 2 (in float) - log(U)|: float(k) is within 2^-24
 // relative of k, logf within 1 ulp (<= 2^-18 for results below 64 in magnitude), the
 // float constant and subtraction within 2^-18 each: far below 2^-14.
 constexpr double kLogMargin = 6.103515625e-05;  // 2^-14
+
+struct FHSlot {
+    int4 cand[32];                // dE, lo, hacc (float bits), packed (sn, ds, dq, dp)
+    unsigned long long k53[32];   // U = k * 2^-53
+};
+
+struct FHShared {
+    FHSlot slot[kFHSlots];
+    double win[kFHWin];
+    float fwin[kFHWin];
+    unsigned long long hwin[kFHWin];
+    uint32_t rnd[3][8][4];  // producer: Philox blocks of one batch by purpose
+    uint16_t binrec[32];    // consumer: window bin after each attempt of the batch
+    uint8_t accf[32];       // consumer: 1 where the batch's attempt was accepted
+    float2 thr2[32];        // consumer: (hacc + ew, lo - ew) of the batch's sites
+    int stop;
+};
+
+__device__ __forceinline__ void fh_bar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void fh_bar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
 
 __device__ __forceinline__ long long fh_window_base(long long b, long long nbins) {
     long long wb = b - kFHWin / 2;
@@ -58,173 +90,451 @@ __device__ __forceinline__ long long fh_window_base(long long b, long long nbins
     return wb < 0 ? 0 : wb;
 }
 
-// FP64 window plus a single-precision copy relative to a centre value c (finite),
-// which the serial scan uses to decide without FP64 arithmetic in the common case.
-__device__ __forceinline__ void fh_window_load(double* win, float* fwin, const double* lnw, long long wb,
-                                               long long nbins, long long centre, int lane, double& c) {
+// Absolute margin for the single-precision decision: with B >= |fwin[i]| over the
+// window, d = fl(fa - fb) is within 2^-22 * B of the FP64 difference lr (two rounded
+// conversions and one rounded subtraction), and forming the thresholds fl(h +- ew)
+// rounds by at most 2^-24 (|h| + ew) with |h| < 40.  So d > fl(hacc + ew) proves
+// lr > hacc and d <= fl(lo - ew) proves lr < lo whenever ew >= 2^-21 (B + 40);
+// (B + 64) 2^-20 is used.  A window holding a value that is not finite in single
+// precision gets NaN, which sends every decision to FP64.
+__device__ __forceinline__ float fh_margin(float B) {
+    return B <= 3.0e38f ? (B + 64.0f) * 9.5367431640625e-07f : __int_as_float(0x7FC00000);
+}
+
+// Loads the window at wb (all lanes of the consumer); returns the margin.
+__device__ __forceinline__ float fh_window_load(FHShared& sh, const double* lnw, long long wb, long long nbins,
+                                                long long centre, int lane, double& c) {
     const double v = lnw[centre];
     c = (v - v == 0.0) ? v : 0.0;  // v finite ? v : 0
+    unsigned int m = 0;
     for (int i = lane; i < kFHWin; i += 32) {
         const double x = wb + i < nbins ? lnw[wb + i] : 0.0;
-        win[i] = x;
-        fwin[i] = (float)(x - c);
+        const float f = (float)(x - c);
+        sh.win[i] = x;
+        sh.fwin[i] = f;
+        const unsigned int a = __float_as_uint(f) & 0x7FFFFFFFu;  // |f|; NaN / inf above every finite
+        m = a > m ? a : m;
+    }
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    __syncwarp();
+    return fh_margin(__uint_as_float(m));
+}
+
+// Adds the window's histogram counts to H and clears them (all lanes of the consumer).
+__device__ __forceinline__ void fh_hist_flush(FHShared& sh, unsigned long long* H, long long wb, long long nbins,
+                                              int lane) {
+    __syncwarp();
+    for (int i = lane; i < kFHWin; i += 32) {
+        const unsigned long long h = sh.hwin[i];
+        if (h) {
+            if (wb + i < nbins) atomicAdd(&H[wb + i], h);
+            sh.hwin[i] = 0;
+        }
     }
     __syncwarp();
 }
 
-__device__ __forceinline__ void fh_window_store(const double* win, double* lnw, long long wb, long long nbins, int lane) {
+__device__ __forceinline__ void fh_window_store(const FHShared& sh, double* lnw, long long wb, long long nbins,
+                                                int lane) {
+    __syncwarp();
     for (int i = lane; i < kFHWin; i += 32)
-        if (wb + i < nbins) lnw[wb + i] = win[i];
+        if (wb + i < nbins) lnw[wb + i] = sh.win[i];
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
-    __shared__ long long s_dE[kFHWarps][32];
-    __shared__ unsigned long long s_k[kFHWarps][32];  // U = k * 2^-53
-    __shared__ float s_lo[kFHWarps][32];              // log(U) lies in [lo, hi]
-    __shared__ float s_hi[kFHWarps][32];
-    __shared__ double s_win[kFHWarps][kFHWin];
-    __shared__ float s_fwin[kFHWarps][kFHWin];
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const int wid = blockIdx.x * kFHWarps + wl;
-    if (wid >= a.nwalkers) return;  // whole warp
+// Producer, stage 1: the raw spins one lane needs for site j0 + lane of colour c (own
+// spin and 2*dim neighbours), loaded one batch ahead so that their latency overlaps the
+// previous batch's arithmetic and the wait for a free slot.
+struct FHLoad {
+    int so;
+    int nb[6];
+};
+
+__device__ __forceinline__ FHLoad fh_load(const FHGeom& g, const int8_t* cur, const int8_t* oth, int c, long long j0,
+                                          int r0, int q0, long long ncol, int lane) {
+    FHLoad L;
+    L.so = 0;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) L.nb[d] = 0;
+    const long long j = j0 + lane;
+    if (j < ncol) {
+        int q = q0 + lane, r = r0;
+        while (q >= g.W) {
+            q -= g.W;
+            ++r;
+        }
+        int y = r, z = 0;
+        if (g.dim == 3) {
+            z = r / g.Ly;
+            y = r - z * g.Ly;
+        }
+        const RowInfo ri = row_info_yz(y, z, g.Ly, g.Lz, c, g.dim);
+        const int qs = ri.p == 0 ? (q == 0 ? g.W - 1 : q - 1) : (q == g.W - 1 ? 0 : q + 1);
+        L.so = cur[j];
+        L.nb[0] = oth[j];
+        L.nb[1] = oth[(long long)r * g.W + qs];
+        L.nb[2] = oth[ri.ryp * g.W + q];
+        L.nb[3] = oth[ri.rym * g.W + q];
+        if (g.dim == 3) {
+            L.nb[4] = oth[ri.rzp * g.W + q];
+            L.nb[5] = oth[ri.rzm * g.W + q];
+        }
+    }
+    return L;
+}
+
+// Producer, stage 2: candidates of one batch (32 sites of colour c from site j0).
+__device__ __forceinline__ void fh_produce(FHShared& sh, FHSlot& sl, const FHGeom& g, const FHLoad& L, int c,
+                                           unsigned long long t, long long j0, long long ncol, uint32_t k0,
+                                           uint32_t k1, uint32_t stream, int lane) {
+    // one Philox block per lane: purpose lane / 8 (accept, low word, proposal), group lane % 8
+    {
+        const int pur = lane >> 3, grp = lane & 7;
+        if (pur < 2 + g.model) {
+            const uint32_t p = pur == 0 ? P_ACCEPT : (pur == 1 ? P_LOW : P_PROPOSE);
+            const uint4 v = philox10(make_uint4((uint32_t)((j0 >> 2) + grp), (uint32_t)t, ctr_word2(t, c, p), stream),
+                                     k0, k1);
+            sh.rnd[pur][grp][0] = v.x;
+            sh.rnd[pur][grp][1] = v.y;
+            sh.rnd[pur][grp][2] = v.z;
+            sh.rnd[pur][grp][3] = v.w;
+        }
+    }
+    __syncwarp();
+    int4 cd = make_int4(0, 0, 0, 0);
+    unsigned long long k53 = 0;
+    if (j0 + lane < ncol) {
+        const int so = L.so;
+        const int S = L.nb[0] + L.nb[1] + L.nb[2] + L.nb[3] + L.nb[4] + L.nb[5];
+        const int grp = lane >> 2, wd = lane & 3;
+        const int sn = g.model == 0 ? -so : bc_propose(so, (int)(sh.rnd[2][grp][wd] >> 31));
+        const int ds = sn - so, dq = sn * sn - so * so, dp = ds * S;
+        const long long dE = -g.J * dp + g.D * dq - g.h * ds;
+        k53 = ((unsigned long long)sh.rnd[0][grp][wd] << 21) | (unsigned long long)(sh.rnd[1][grp][wd] >> 11);
+        // single-precision log(U) and a margin that bounds its distance to the FP64
+        // log of the decision rule (logf: <= 1 ulp, |log U| < 37.5)
+        const float l32 = logf(__ull2float_rn(k53)) - 36.7368005696771f;  // 53 ln 2
+        const float lo = l32 - (float)kLogMargin;
+        const float hacc = fminf(l32 + (float)kLogMargin, 0.0f);  // accept when lr > min(0, log U)
+        cd = make_int4((int)dE, __float_as_int(lo), __float_as_int(hacc),
+                       (int)((uint32_t)(uint8_t)sn | ((uint32_t)(uint8_t)ds << 8) | ((uint32_t)(uint8_t)dq << 16) |
+                             ((uint32_t)(uint8_t)dp << 24)));
+    }
+    sl.cand[lane] = cd;
+    sl.k53[lane] = k53;
+    __syncwarp();
+}
+
+// Consumer lane-0 state of one walker.
+struct FHScan {
+    long long E;   // energy (tracked when !FAST)
+    long long Ewb; // start + wb * step
+    int er;        // E - Ewb (tracked when FAST)
+    int bi;        // current bin, relative to wb
+    float flwo;    // fwin[bi]
+    float ew;      // decision margin of the window
+    double cw;     // centre of the single-precision window copy
+    unsigned long long steps;
+};
+
+// Scans sites i..n-1 of one batch (consumer lane 0).  Stops early with `need` set to
+// the bin that must come into the window, or with status 2 (energy out of range).
+template <bool FAST>
+__device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FHGeom& g, long long wb, int lim,
+                                        FHScan& st, int& i, int n, long long& need, int& status) {
+    const bool wl = g.mode == 1;
+    int4 nx = sl.cand[i < n ? i : 0];
+    for (; i < n; ++i) {
+        const int4 cd = nx;
+        if (i + 1 < n) nx = sl.cand[i + 1];  // prefetch: keeps the load off the dependent chain
+        int bn;
+        long long En = 0;
+        int en = 0;
+        if (FAST) {
+            en = st.er + cd.x;
+            if ((unsigned)en < (unsigned)lim) {
+                bn = en >> g.shift;
+            } else {
+                long long b;
+                if (!fh_bin(st.Ewb + en, g, b)) {
+                    status = 2;
+                    break;
+                }
+                if (b < wb || b >= wb + kFHWin) {
+                    need = b;
+                    break;
+                }
+                bn = (int)(b - wb);
+            }
+        } else {
+            En = st.E + cd.x;
+            long long b;
+            if (!fh_bin(En, g, b)) {
+                status = 2;
+                break;
+            }
+            if (b < wb || b >= wb + kFHWin) {
+                need = b;
+                break;
+            }
+            bn = (int)(b - wb);
+        }
+        // lr = lnw[bn] - lnw[bo] against log(U), decided in single precision when the
+        // margins allow, else in FP64 with the project's log
+        const float fa = sh.fwin[bn];
+        const float d = fa - st.flwo;
+        bool acc;
+        if (d > __int_as_float(cd.z) + st.ew) acc = true;
+        else if (d <= __int_as_float(cd.y) - st.ew) acc = false;
+        else {
+            const double lr = sh.win[bn] - sh.win[st.bi];
+            acc = (lr > 0.0) || (mcx_log((double)sl.k53[i] * 1.1102230246251565404236316680908203125e-16) < lr);
+        }
+        if (acc) {
+            sh.accf[i] = 1;
+            st.bi = bn;
+            if (FAST) st.er = en;
+            else st.E = En;
+            st.flwo = fa;
+        }
+        if (wl) {
+            const double v = sh.win[st.bi] - g.logf;
+            sh.win[st.bi] = v;
+            const float f = (float)(v - st.cw);
+            sh.fwin[st.bi] = f;
+            st.flwo = f;
+            // keep the margin valid for the changed value (NaN stays NaN)
+            const float m = fh_margin(fabsf(f));
+            if (st.ew == st.ew && !(m <= st.ew)) st.ew = m;
+        }
+        sh.binrec[i] = (uint16_t)st.bi;
+    }
+}
+
+// Multicanonical scan with power-of-two bins (consumer lane 0): straight-line code while
+// every proposed bin is inside the window and the single-precision decision is clear
+// (thresholds precomputed in thr2), with the weight and weight difference of the next
+// site formed for both outcomes of the current decision, so the shared-memory latency
+// leaves the dependent chain.  Returns at the first site that needs fh_scan (window
+// miss, range end, FP64 decision) or at the end of the batch.
+__device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int shift, int lim, FHScan& st, int& i,
+                                             int n) {
+    if (i >= n) return;
+    int er = st.er, bi = st.bi;
+    float flwo = st.flwo;
+    int k = i;
+    int en = er + sl.cand[k].x;
+    bool ok = (unsigned)en < (unsigned)lim;
+    float fa = sh.fwin[ok ? (en >> shift) : bi];
+    float d = fa - flwo;
+    bool go = true;
+    while (go) {
+        const int dn = sl.cand[k + 1 < 32 ? k + 1 : 31].x;
+        const float tx = sh.thr2[k].x, ty = sh.thr2[k].y;
+        const int en_r = er + dn, en_a = en + dn;
+        const bool ok_r = (unsigned)en_r < (unsigned)lim, ok_a = (unsigned)en_a < (unsigned)lim;
+        const float fa_r = sh.fwin[ok_r ? (en_r >> shift) : 0];
+        const float fa_a = sh.fwin[ok_a ? (en_a >> shift) : 0];
+        const float d_r = fa_r - flwo, d_a = fa_a - fa;
+        const bool acc = d > tx;
+        const bool clear = ok && (acc || d <= ty);
+        if (clear) {
+            if (acc) {
+                er = en;
+                bi = en >> shift;
+                flwo = fa;
+            }
+            sh.accf[k] = (uint8_t)acc;
+            sh.binrec[k] = (uint16_t)bi;
+            ++k;
+            en = acc ? en_a : en_r;
+            ok = acc ? ok_a : ok_r;
+            fa = acc ? fa_a : fa_r;
+            d = acc ? d_a : d_r;
+        }
+        go = clear && k < n;
+    }
+    i = k;
+    st.er = er;
+    st.bi = bi;
+    st.flwo = flwo;
+}
+
+// Decision thresholds of the batch for the current window margin (all lanes).
+__device__ __forceinline__ void fh_thresholds(FHShared& sh, const FHSlot& sl, float ew, int lane) {
+    const int4 c = sl.cand[lane];
+    sh.thr2[lane] = make_float2(__int_as_float(c.z) + ew, __int_as_float(c.y) - ew);
+    __syncwarp();
+}
+
+// Histogram counts of sites [h0, h1) of the batch (all lanes of the consumer): lanes
+// holding the same bin add once, as a group.
+__device__ __forceinline__ void fh_hist_batch(FHShared& sh, int h0, int h1, int lane) {
+    __syncwarp();
+    const bool act = lane >= h0 && lane < h1;
+    const unsigned int am = __ballot_sync(0xFFFFFFFFu, act);
+    if (act) {
+        const int b = sh.binrec[lane];
+        const unsigned int grp = __match_any_sync(am, b);
+        if (lane == __ffs(grp) - 1) sh.hwin[b] += (unsigned long long)__popc(grp);
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
+    __shared__ FHShared sh;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wid = blockIdx.x;
+    if (wid >= a.nwalkers) return;  // whole block
     FHWalker& w = a.walkers[wid];
     const FHGeom g = w.g;
     int8_t* const col0 = w.col[0];
     int8_t* const col1 = w.col[1];
+    const long long ncol = (long long)g.W * g.Ly * g.Lz;
+    const long long nb = (ncol + 31) / 32;                // batches per colour
+    const long long total = g.nsweeps * 2 * nb;          // batches of the launch
+    const unsigned long long sweep0 = w.sweep0;
+    if (warp == 0 && lane == 0) sh.stop = 0;
+    for (int i = threadIdx.x; i < kFHWin; i += 64) sh.hwin[i] = 0;
+    __syncthreads();
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer --
+        const uint32_t k0 = w.k0, k1 = w.k1, stream = w.stream;
+        long long qb = 0;
+        for (long long s = 0; s < g.nsweeps; ++s) {
+            const unsigned long long t = sweep0 + (unsigned long long)s;
+            for (int c = 0; c < 2; ++c) {
+                if (s > 0 || c > 0) fh_bar_sync(kFHBarCol);
+                const int8_t* cur = c ? col1 : col0;
+                const int8_t* oth = c ? col0 : col1;
+                int r0 = 0, q0 = 0;
+                FHLoad ld = fh_load(g, cur, oth, c, 0, 0, 0, ncol, lane);
+                for (long long b = 0; b < nb; ++b, ++qb) {
+                    const int sl = (int)(qb % kFHSlots);
+                    // next batch's loads first (sites the consumer has not reached)
+                    int r1 = r0, q1 = q0 + 32;
+                    while (q1 >= g.W) {
+                        q1 -= g.W;
+                        ++r1;
+                    }
+                    const FHLoad nx = fh_load(g, cur, oth, c, (b + 1) * 32, r1, q1, ncol, lane);
+                    if (qb >= kFHSlots) fh_bar_sync(kFHBarEmpty + sl);
+                    if (!*(volatile int*)&sh.stop)
+                        fh_produce(sh, sh.slot[sl], g, ld, c, t, b * 32, ncol, k0, k1, stream, lane);
+                    __threadfence_block();
+                    fh_bar_arrive(kFHBarFull + sl);
+                    ld = nx;
+                    r0 = r1;
+                    q0 = q1;
+                }
+            }
+        }
+        return;
+    }
+
+    // ---------------------------------------------------------------- consumer --
     double* const lnw = w.lnw;
     unsigned long long* const H = w.H;
     long long* const series = w.series;
-    const uint32_t k0 = w.k0, k1 = w.k1, stream = w.stream;
-    const unsigned long long sweep0 = w.sweep0;
     long long P = w.P, M = w.M, Q = w.Q;
-    long long E = -g.J * P + g.D * Q - g.h * M;
-    long long bo = 0;
+    if (w.state) {
+        P = w.state[0];
+        M = w.state[1];
+        Q = w.state[2];
+    }
     int status = 0;
-    if (!fh_bin(E, g, bo)) status = 2;
-    double* const win = s_win[wl];
-    float* const fwin = s_fwin[wl];
+    FHScan st;
+    st.E = -g.J * P + g.D * Q - g.h * M;
+    long long bo = 0;
+    if (!fh_bin(st.E, g, bo)) status = 2;
+    const bool fast = g.shift >= 0 && g.shift <= 20;
     long long wb = fh_window_base(status ? 0 : bo, g.nbins);
-    double cw = 0.0;
-    fh_window_load(win, fwin, lnw, wb, g.nbins, status ? 0 : bo, lane, cw);
-    float flwo = status ? 0.f : fwin[bo - wb];
-    unsigned long long steps = 0, accepted = 0;
-    const long long ncol = (long long)g.W * g.Ly * g.Lz;
-    const int Z = 2 * g.dim;
-    for (long long s = 0; s < g.nsweeps && status == 0; ++s) {
-        const unsigned long long t = sweep0 + (unsigned long long)s;
+    st.ew = fh_window_load(sh, lnw, wb, g.nbins, status ? 0 : bo, lane, st.cw);
+    st.Ewb = g.start + wb * g.step;
+    st.er = (int)(st.E - st.Ewb);
+    st.bi = status ? 0 : (int)(bo - wb);
+    st.flwo = sh.fwin[st.bi];
+    st.steps = 0;
+    const bool muca_fast = fast && g.mode == 0;
+    if (status && lane == 0) sh.stop = 1;
+    unsigned long long accepted = 0;
+    long long qb = 0;
+    for (long long s = 0; s < g.nsweeps; ++s) {
         long long dP = 0, dM = 0, dQ = 0;
-        for (int c = 0; c < 2 && status == 0; ++c) {
+        for (int c = 0; c < 2; ++c) {
             int8_t* cur = c ? col1 : col0;
-            const int8_t* oth = c ? col0 : col1;
-            const uint32_t w2a = ctr_word2(t, c, P_ACCEPT), w2l = ctr_word2(t, c, P_LOW),
-                           w2p = ctr_word2(t, c, P_PROPOSE);
-            for (long long j0 = 0; j0 < ncol && status == 0; j0 += 32) {
-                const long long j = j0 + lane;
-                const bool valid = j < ncol;
-                int sn = 0, ds = 0, dq = 0, dp = 0;
-                long long dE = 0;
-                unsigned long long k53 = 0;
-                float lo = 0.f, hi = 0.f;
-                if (valid) {
-                    const int r = (int)(j / g.W), k = (int)(j - (long long)r * g.W);
-                    const int y = r % g.Ly, z = r / g.Ly;
-                    const RowInfo ri = row_info_yz(y, z, g.Ly, g.Lz, c, g.dim);
-                    const int so = cur[j];
-                    const int ks = ri.p == 0 ? (k == 0 ? g.W - 1 : k - 1) : (k == g.W - 1 ? 0 : k + 1);
-                    int S = oth[j] + oth[(long long)r * g.W + ks] + oth[ri.ryp * g.W + k] + oth[ri.rym * g.W + k];
-                    if (Z == 6) S += oth[ri.rzp * g.W + k] + oth[ri.rzm * g.W + k];
-                    const uint32_t cj = (uint32_t)(j >> 2);
-                    const int lj = (int)(j & 3);
-                    if (g.model == 0) sn = -so;
-                    else sn = bc_propose(so, (int)(pick4(philox10(make_uint4(cj, (uint32_t)t, w2p, stream), k0, k1), lj) >> 31));
-                    ds = sn - so;
-                    dq = sn * sn - so * so;
-                    dp = ds * S;
-                    dE = -g.J * dp + g.D * dq - g.h * ds;
-                    const uint32_t whi = pick4(philox10(make_uint4(cj, (uint32_t)t, w2a, stream), k0, k1), lj);
-                    const uint32_t wlo = pick4(philox10(make_uint4(cj, (uint32_t)t, w2l, stream), k0, k1), lj);
-                    k53 = ((unsigned long long)whi << 21) | (unsigned long long)(wlo >> 11);
-                    // single-precision log(U) and a margin that bounds its distance to the
-                    // FP64 log of the decision rule (logf: <= 1 ulp, |log U| < 37.5)
-                    const float l32 = logf(__ull2float_rn(k53)) - 36.7368005696771f;  // 53 ln 2
-                    lo = l32 - (float)kLogMargin;
-                    hi = l32 + (float)kLogMargin;
-                }
-                s_dE[wl][lane] = dE;
-                s_k[wl][lane] = k53;
-                s_lo[wl][lane] = lo;
-                s_hi[wl][lane] = hi;
-                __syncwarp();
-                unsigned int accmask = 0;
-                int i = 0;
-                const int n = (int)((ncol - j0) < 32 ? (ncol - j0) : 32);
-                for (;;) {
-                    long long need = -1;
-                    if (lane == 0) {
-                        for (; i < n; ++i) {
-                            const long long En = E + s_dE[wl][i];
-                            long long bn;
-                            if (!fh_bin(En, g, bn)) {
-                                status = 2;
-                                break;
-                            }
-                            if (bn < wb || bn >= wb + kFHWin) {
-                                need = bn;
-                                break;
-                            }
-                            // lr = lnw[bn] - lnw[bo] in FP64, decided from the float copy:
-                            // |lr32 - lr| <= 2^-23 (|fa| + |fb| + |lr32|) (two roundings of
-                            // the centred values, one of the difference), doubled below
-                            const float fa = fwin[bn - wb];
-                            const float lr32 = fa - flwo;
-                            const float e = (fabsf(fa) + fabsf(flwo) + fabsf(lr32)) * 2.384185791015625e-07f + 1e-30f;
-                            bool acc;
-                            if (lr32 - e > 0.f || lr32 - e > s_hi[wl][i]) acc = true;
-                            else if (lr32 + e <= s_lo[wl][i]) acc = false;
-                            else {
-                                const double lr = win[bn - wb] - win[bo - wb];
-                                acc = (lr > 0.0) ||
-                                      (mcx_log((double)s_k[wl][i] * 1.1102230246251565404236316680908203125e-16) < lr);
-                            }
-                            ++steps;
-                            if (acc) {
-                                ++accepted;
-                                accmask |= 1u << i;
-                                E = En;
-                                bo = bn;
-                                flwo = fa;
-                            }
-                            if (g.mode == 1) {
-                                const double v = win[bo - wb] - g.logf;
-                                win[bo - wb] = v;
-                                flwo = (float)(v - cw);
-                                fwin[bo - wb] = flwo;
-                            }
-                            atomicAdd(&H[bo], 1ull);
-                        }
-                    }
-                    need = __shfl_sync(0xFFFFFFFFu, need, 0);
-                    if (need < 0) break;
-                    // move the window around the proposed bin (the current bin stays inside:
-                    // one move changes the bin by far less than half the window)
+            for (long long b = 0; b < nb; ++b, ++qb) {
+                const int slot = (int)(qb % kFHSlots);
+                fh_bar_sync(kFHBarFull + slot);
+                const FHSlot& sl = sh.slot[slot];
+                if (status == 0) {
+                    const int n = (int)((ncol - b * 32) < 32 ? (ncol - b * 32) : 32);
+                    int i = 0, h0 = 0;
+                    sh.accf[lane] = 0;
+                    if (muca_fast) fh_thresholds(sh, sl, __shfl_sync(0xFFFFFFFFu, st.ew, 0), lane);
                     __syncwarp();
-                    if (g.mode == 1) fh_window_store(win, lnw, wb, g.nbins, lane);
-                    const long long bo_all = __shfl_sync(0xFFFFFFFFu, bo, 0);
-                    wb = fh_window_base(need, g.nbins);
-                    fh_window_load(win, fwin, lnw, wb, g.nbins, need, lane, cw);
-                    if (lane == 0) flwo = fwin[bo_all - wb];
+                    for (;;) {
+                        long long need = -1;
+                        if (lane == 0) {
+                            const long long vis = wb + kFHWin < g.nbins ? kFHWin : g.nbins - wb;
+                            const int lim = (int)(vis << (fast ? g.shift : 0));
+                            const int i0 = i;
+                            if (muca_fast) {
+                                for (;;) {
+                                    fh_scan_fast(sh, sl, g.shift, lim, st, i, n);
+                                    if (i >= n) break;
+                                    fh_scan<true>(sh, sl, g, wb, lim, st, i, i + 1, need, status);
+                                    if (need >= 0 || status) break;
+                                }
+                            } else if (fast) {
+                                fh_scan<true>(sh, sl, g, wb, lim, st, i, n, need, status);
+                            } else {
+                                fh_scan<false>(sh, sl, g, wb, lim, st, i, n, need, status);
+                            }
+                            st.steps += (unsigned long long)(i - i0);
+                        }
+                        need = __shfl_sync(0xFFFFFFFFu, need, 0);
+                        i = __shfl_sync(0xFFFFFFFFu, i, 0);
+                        fh_hist_batch(sh, h0, i, lane);
+                        h0 = i;
+                        if (need < 0) break;
+                        // move the window around the proposed bin (the current bin stays
+                        // inside: one move changes the bin by far less than half the window)
+                        fh_hist_flush(sh, H, wb, g.nbins, lane);
+                        if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
+                        const long long bo_all = __shfl_sync(0xFFFFFFFFu, wb + st.bi, 0);
+                        const long long wb_new = fh_window_base(need, g.nbins);
+                        const float ew = fh_window_load(sh, lnw, wb_new, g.nbins, need, lane, st.cw);
+                        if (lane == 0) {
+                            st.ew = ew;
+                            st.er += (int)((wb - wb_new) * g.step);  // FAST only (wb moves < 2^11 bins)
+                            st.Ewb = g.start + wb_new * g.step;
+                            st.bi = (int)(bo_all - wb_new);
+                            st.flwo = sh.fwin[st.bi];
+                        }
+                        wb = wb_new;
+                        if (muca_fast) fh_thresholds(sh, sl, ew, lane);
+                    }
+                    __syncwarp();
+                    const unsigned int accmask = __ballot_sync(0xFFFFFFFFu, sh.accf[lane] != 0);
+                    status = __shfl_sync(0xFFFFFFFFu, status, 0);
+                    if ((accmask >> lane) & 1u) {
+                        const uint32_t pk = (uint32_t)sl.cand[lane].w;
+                        cur[b * 32 + lane] = (int8_t)(pk & 0xFFu);
+                        dP += (int8_t)(pk >> 24);
+                        dM += (int8_t)((pk >> 8) & 0xFFu);
+                        dQ += (int8_t)((pk >> 16) & 0xFFu);
+                    }
+                    if (lane == 0) {
+                        accepted += __popc(accmask);
+                        if (status) sh.stop = 1;
+                    }
                 }
-                accmask = __shfl_sync(0xFFFFFFFFu, accmask, 0);
-                status = __shfl_sync(0xFFFFFFFFu, status, 0);
-                if (valid && ((accmask >> lane) & 1u)) {
-                    cur[j] = (int8_t)sn;
-                    dP += dp;
-                    dM += ds;
-                    dQ += dq;
-                }
-                __syncwarp();
+                __threadfence_block();
+                if (qb + kFHSlots < total) fh_bar_arrive(kFHBarEmpty + slot);
             }
+            if (s + 1 < g.nsweeps || c == 0) fh_bar_arrive(kFHBarCol);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -246,13 +556,19 @@ __global__ void __launch_bounds__(32 * kFHWarps) k_flathist(const FHArgs a) {
         M = __shfl_sync(0xFFFFFFFFu, M, 0);
         Q = __shfl_sync(0xFFFFFFFFu, Q, 0);
     }
-    if (g.mode == 1) fh_window_store(win, lnw, wb, g.nbins, lane);
+    fh_hist_flush(sh, H, wb, g.nbins, lane);
+    if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
     if (lane == 0) {
         // a stopped sweep still folds the accepted moves made before the stop
         w.P = P;
         w.M = M;
         w.Q = Q;
-        w.steps = steps;
+        if (w.state) {
+            w.state[0] = P;
+            w.state[1] = M;
+            w.state[2] = Q;
+        }
+        w.steps = st.steps;
         w.accepted = accepted;
         w.status = status;
     }
@@ -309,7 +625,7 @@ mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers) {
     FHArgs a;
     a.walkers = d_walkers;
     a.nwalkers = nwalkers;
-    k_flathist<<<(nwalkers + kFHWarps - 1) / kFHWarps, 32 * kFHWarps, 0, ctx->stream>>>(a);
+    k_flathist<<<nwalkers, 64, 0, ctx->stream>>>(a);
     count_launch(ctx);
     MCX_CUDA(cudaGetLastError());
     return MCX_OK;
@@ -318,7 +634,7 @@ mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers) {
 bool fh_window_ok(int dim, long long J, long long D, long long h, long long step) {
     const long long z = 2 * dim;
     const long long maxde = 2 * (J < 0 ? -J : J) * z + 2 * (h < 0 ? -h : h) + (D < 0 ? -D : D);
-    return maxde / step + 2 < kFHWin / 2;
+    return maxde < (1ll << 30) && maxde / step + 2 < kFHWin / 2;
 }
 
 int fh_shift(long long step) {
@@ -507,11 +823,6 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
     for (int i = 0; i < nwalkers; ++i) {
         MCX_CHECK(ensure_series(lats[i], nsweeps));
     }
-    // current bookkeeping of every walker
-    std::vector<long long> st((size_t)nwalkers * 3);
-    for (int i = 0; i < nwalkers; ++i)
-        MCX_CUDA(cudaMemcpyAsync(&st[3 * i], lats[i]->d_state, 24, cudaMemcpyDeviceToHost, ctx->stream));
-    MCX_CUDA(cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < nwalkers; ++i) {
         FHWalker& w = hw[i];
         std::memset(&w, 0, sizeof(w));
@@ -521,16 +832,14 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
         w.lnw = f->d_lnw;
         w.H = f->d_H;
         w.series = (long long*)lats[i]->d_series;
-        w.P = st[3 * i];
-        w.M = st[3 * i + 1];
-        w.Q = st[3 * i + 2];
+        w.state = (long long*)lats[i]->d_state;  // the kernel reads and updates (P, M, Q) in place
         w.sweep0 = rngs[i].counter;
         w.k0 = (uint32_t)rngs[i].seed;
         w.k1 = (uint32_t)(rngs[i].seed >> 32);
         w.stream = rngs[i].stream;
     }
     void* dw = nullptr;
-    MCX_CHECK(dev_alloc(ctx, &dw, hw.size() * sizeof(FHWalker)));
+    MCX_CHECK(ctx_scratch(ctx, hw.size() * sizeof(FHWalker), &dw));
     FHGeom g;
     std::memset(&g, 0, sizeof(g));
     g.W = (int)L0->W;
@@ -554,20 +863,16 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
     a.walkers = (FHWalker*)dw;
     a.nwalkers = nwalkers;
     if (e == cudaSuccess) {
-        k_flathist<<<(nwalkers + kFHWarps - 1) / kFHWarps, 32 * kFHWarps, 0, ctx->stream>>>(a);
+        k_flathist<<<nwalkers, 64, 0, ctx->stream>>>(a);
         count_launch(ctx);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(hw.data(), dw, hw.size() * sizeof(FHWalker), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    dev_free(ctx, dw, hw.size() * sizeof(FHWalker));
     if (e != cudaSuccess) return cuda_fail(e, "flat-histogram sweep");
     bool range = false;
     for (int i = 0; i < nwalkers; ++i) {
         const FHWalker& w = hw[i];
-        long long s3[3] = {w.P, w.M, w.Q};
-        MCX_CUDA(cudaMemcpyAsync(lats[i]->d_state, s3, 24, cudaMemcpyHostToDevice, ctx->stream));
-        MCX_CUDA(cudaStreamSynchronize(ctx->stream));
         lats[i]->series_len = w.status ? 0 : nsweeps;
         rngs[i].counter += (uint64_t)nsweeps;
         if (counters) {

@@ -36,7 +36,8 @@ struct FHWalker {
     double* lnw;
     unsigned long long* H;
     long long* series;  // [nsweeps][3] or null
-    long long P, M, Q;
+    long long* state;   // device (P, M, Q), read at the start and written back at the end, or null
+    long long P, M, Q;  // used when state is null; always written back
     unsigned long long steps, accepted;
     unsigned long long sweep0;
     uint32_t k0, k1, stream;

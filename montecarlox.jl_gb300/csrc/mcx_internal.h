@@ -63,6 +63,8 @@ struct mcx_ctx {
     uint64_t launches = 0;
     int num_sms = 0;
     cudaStream_t capture_stream = nullptr;  // private stream for CUDA-graph capture
+    void* d_scratch = nullptr;              // per-call descriptors (walkers), grown on demand
+    size_t scratch_bytes = 0;
     // the caller's handle plus one per live object created on this context: the
     // streams and the accounting stay valid until the last of them is destroyed, in
     // whatever order a garbage collector finalises them
@@ -71,6 +73,9 @@ struct mcx_ctx {
 
 namespace mcx {
 void ctx_release(mcx_ctx* ctx);
+// Device scratch of at least `bytes` owned by the context (valid until the next call on
+// the same context; contexts are used by one thread at a time).
+mcx_status ctx_scratch(mcx_ctx* ctx, size_t bytes, void** out);
 
 // Reference to the context held by every object created on it.
 struct CtxHold {

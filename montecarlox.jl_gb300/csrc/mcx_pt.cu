@@ -50,7 +50,7 @@ struct PTArgs {
     const int* order;        // tiles in claiming order, largest first (persistent form)
     unsigned int* claim;     // [3] per-phase tile tickets (persistent form)
     int nrep, npos, ntiles;
-    const unsigned long long* tables;  // [npos][16] for the algorithm of this run
+    const unsigned long long* tables;  // [npos][16] for the algorithm of this run (ising_tab_entry form)
     const double* betas;               // [npos]
     const int* pos_ladder;             // [npos]
     const int* pos_local;              // [npos]
@@ -683,7 +683,9 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
         for (int gp = 0; gp < pt->npos; ++gp) {
             Table t;
             run(build_ising_table(dim, (mcx_algorithm)alg, pt->betas[gp], J, h, &t));
-            for (int i = 0; i < t.n; ++i) tabs[((size_t)alg * pt->npos + gp) * 16 + i] = t.thr[i];
+            for (int i = 0; i < t.n; ++i)
+                tabs[((size_t)alg * pt->npos + gp) * 16 + i] =
+                    ising_tab_entry(t.thr[i], i, 2 * dim, alg == MCX_HEATBATH);
         }
     run(pt_upload(pt, &pt->d_tables, tabs));
     std::vector<int32_t> pos0(pt->nrep);

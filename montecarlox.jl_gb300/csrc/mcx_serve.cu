@@ -94,7 +94,10 @@ __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const S
         const SrvJobDev J = jobs[tl.job];
         if (s >= J.todo) continue;  // uniform over the block
         __syncthreads();
-        for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) s_thr[i] = tables[(size_t)tl.job * kMaxTable + i];
+        for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
+            const unsigned long long x = tables[(size_t)tl.job * kMaxTable + i];
+            s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
+        }
         __syncthreads();
         const unsigned long long t = J.t0 + (unsigned long long)s;
         int nacc = 0, a1 = 0, a2 = 0, a3 = 0;

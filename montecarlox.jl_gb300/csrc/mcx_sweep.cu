@@ -21,13 +21,18 @@
 
 namespace mcx {
 
-template <int DIM, int V, bool HB>
+template <int DIM, int V, bool HB, bool T32>
 __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int NT = 2 * (Z + 1);
     constexpr int NW = V / 4;
     __shared__ unsigned long long s_thr[NT];
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
+    __shared__ uint32_t s_t32[NT];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+        const unsigned long long e = ising_tab_entry(a.thr[t], t, Z, HB);
+        if (T32) s_t32[t] = (uint32_t)(e - 1);
+        else s_thr[t] = e;
+    }
     __syncthreads();
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
@@ -43,14 +48,22 @@ __global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
         const uint32_t c0 = (uint32_t)(((unsigned long long)r * a.W + k0) >> 2);
+        uint32_t af = 0, au = 0, ai = 0;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
             uint32_t nbw[Z];
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
             const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, key.stream), key.k0, key.k1);
-            const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
+            uint32_t fb;
+            if (T32) fb = ising_word32<Z, HB>(nbw, ch.own[w], rnd, s_t32, af, au, ai);
+            else fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
             ch.own[w] ^= fb * 0xFEu;
+        }
+        if (T32) {
+            nacc += hsum8(af);
+            nup += hsum8(au);
+            isum += hsum16(ai);
         }
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
@@ -193,13 +206,20 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
 }
 
 // ----------------------------------------------------------- dispatching --
+template <int DIM, bool T32>
+static HalfSweepFn pick_ising_word(bool hb, int V) {
+    if (V == 16) return hb ? k_ising_cb<DIM, 16, true, T32> : k_ising_cb<DIM, 16, false, T32>;
+    if (V == 8) return hb ? k_ising_cb<DIM, 8, true, T32> : k_ising_cb<DIM, 8, false, T32>;
+    return hb ? k_ising_cb<DIM, 4, true, T32> : k_ising_cb<DIM, 4, false, T32>;
+}
+
 template <int DIM>
-static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V) {
+static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, const Table& t) {
     const bool hb = alg == MCX_HEATBATH;
     if (model == MCX_ISING) {
-        if (V == 16) return hb ? k_ising_cb<DIM, 16, true> : k_ising_cb<DIM, 16, false>;
-        if (V == 8) return hb ? k_ising_cb<DIM, 8, true> : k_ising_cb<DIM, 8, false>;
-        if (V == 4) return hb ? k_ising_cb<DIM, 4, true> : k_ising_cb<DIM, 4, false>;
+        if (V == 16 || V == 8 || V == 4)
+            return ising_table_fits32(t.thr, t.n, 2 * DIM, hb) ? pick_ising_word<DIM, true>(hb, V)
+                                                               : pick_ising_word<DIM, false>(hb, V);
         return hb ? k_ising_cb_site<DIM, true> : k_ising_cb_site<DIM, false>;
     }
     if (V == 16) return hb ? k_bc_cb<DIM, 16, true> : k_bc_cb<DIM, 16, false>;
@@ -208,8 +228,8 @@ static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V) {
     return hb ? k_bc_cb_site<DIM, true> : k_bc_cb_site<DIM, false>;
 }
 
-HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V) {
-    return dim == 2 ? pick_kernel_dim<2>(model, alg, V) : pick_kernel_dim<3>(model, alg, V);
+HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t) {
+    return dim == 2 ? pick_kernel_dim<2>(model, alg, V, t) : pick_kernel_dim<3>(model, alg, V, t);
 }
 
 int vec_width(int64_t W) { return W % 16 == 0 ? 16 : (W % 8 == 0 ? 8 : (W % 4 == 0 ? 4 : 1)); }
@@ -292,7 +312,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
     fill_sweep_args(&a, lat, t, &r0);
     a.sweep_base = lat->d_sweep_base;
     a.acc = lat->d_acc;
-    const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
+    const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
     const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
     MCX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), cs);
@@ -369,7 +389,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         fill_sweep_args(&a, lat, t, rng);
         a.acc = lat->d_acc;
         const int V = lattice_width(lat);
-        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
+        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
         const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         for (int64_t s = 0; s < nsweeps; ++s) {
             a.sweep = rng->counter + (uint64_t)s;
@@ -445,7 +465,7 @@ extern "C" MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, 
         fill_sweep_args(&a, lat, t, &r);
         a.acc = acc;
         for (int j = 0; j < 3; ++j) a.dst[j] = dst + j;
-        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V);
+        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
         const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         const int warm = 2, reps = 8;
         for (int k = 0; k < warm + reps && err == cudaSuccess; ++k) {

@@ -36,7 +36,7 @@ __device__ __forceinline__ SweepKey sweep_key(const SweepArgs& a) {
 
 using HalfSweepFn = void (*)(const SweepArgs);
 
-HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V);
+HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);
 int lattice_width(const mcx_lattice* lat);
 int half_sweep_grid(const mcx_ctx* ctx, HalfSweepFn fn, int64_t W, int64_t rows, int V);

@@ -32,6 +32,12 @@ CASES = [
     (O.ISING, [4, 4, 4], 0.0, (-192, 4, 97), "muca", 2, False, 0.0, 15, "beta"),
     (O.BC, [8, 8], 1.0, (-64, 1, 257), "wl", 2, False, 0.5, 12, "flat"),
     (O.BC, [12, 8], 1.0, (-96, 1, 385), "muca", 3, True, 0.0, 10, "beta"),
+    # more bins than the 512-bin shared-memory window: the energy drifts and the window moves
+    (O.BC, [32, 32], 1.0, (-1024, 1, 4097), "muca", 4, True, 0.0, 20, "beta"),
+    (O.ISING, [32, 32], 0.0, (-2048, 1, 4097), "wl", 2, False, 0.05, 10, "beta"),
+    (O.ISING, [8, 8, 8], 0.0, (-1536, 2, 1537), "muca", 3, True, 0.0, 6, "beta"),
+    # bin width not a power of two: the general 64-bit binning path
+    (O.ISING, [16, 16], 0.0, (-512, 12, 86), "muca", 2, True, 0.0, 10, "beta"),
 ]
 
 

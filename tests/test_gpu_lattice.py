@@ -44,6 +44,9 @@ ISING_CASES = [
     ([24, 24, 24], "metropolis", 0.2216, 0.0),
     ([32, 8, 6], "heatbath", 0.25, 0.1),
     ([16, 16, 16], "glauber", 0.2, 0.0),
+    # beta so large that some acceptance thresholds are 0: the 64-bit threshold kernels
+    ([32, 32], "metropolis", 3.0, 0.0),
+    ([16, 16, 16], "heatbath", 3.0, 0.0),
 ]
 
 
