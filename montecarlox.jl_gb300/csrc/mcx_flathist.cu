@@ -59,6 +59,10 @@ constexpr int kFHBarFull = 1, kFHBarEmpty = 5, kFHBarCol = 9;
 // it (Wang-Landau writes the window back first).  Histogram counts of the window
 // accumulate in shared memory and go to global memory when the window moves.
 constexpr int kFHWin = 512;
+// Guard entries on both sides of the single-precision window: one move changes the bin
+// by less than kFHWin / 2 (fh_window_ok), so a proposal from a bin inside the window
+// indexes fwin(sh) within [-kFHGuard, kFHWin + kFHGuard) without a bounds select.
+constexpr int kFHGuard = kFHWin / 2;
 // Bound on |logf(float(U)) - 53 ln 2 (in float) - log(U)|: float(k) is within 2^-24
 // relative of k, logf within 1 ulp (<= 2^-18 for results below 64 in magnitude), the
 // float constant and subtraction within 2^-18 each: far below 2^-14.
@@ -72,7 +76,7 @@ struct FHSlot {
 struct FHShared {
     FHSlot slot[kFHSlots];
     double win[kFHWin];
-    float fwin[kFHWin];
+    float fwin_g[kFHGuard + kFHWin + kFHGuard];  // fwin(sh)[-kFHGuard, kFHWin + kFHGuard)
     unsigned long long hwin[kFHWin];
     uint32_t rnd[3][8][4];  // producer: Philox blocks of one batch by purpose
     uint16_t binrec[32];    // consumer: window bin after each attempt of the batch
@@ -80,6 +84,8 @@ struct FHShared {
     float2 thr2[32];        // consumer: (hacc + ew, lo - ew) of the batch's sites
     int stop;
 };
+
+__device__ __forceinline__ float* fwin(FHShared& sh) { return sh.fwin_g + kFHGuard; }
 
 __device__ __forceinline__ void fh_bar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
 __device__ __forceinline__ void fh_bar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
@@ -111,7 +117,7 @@ __device__ __forceinline__ float fh_window_load(FHShared& sh, const double* lnw,
         const double x = wb + i < nbins ? lnw[wb + i] : 0.0;
         const float f = (float)(x - c);
         sh.win[i] = x;
-        sh.fwin[i] = f;
+        fwin(sh)[i] = f;
         const unsigned int a = __float_as_uint(f) & 0x7FFFFFFFu;  // |f|; NaN / inf above every finite
         m = a > m ? a : m;
     }
@@ -281,7 +287,7 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FH
         }
         // lr = lnw[bn] - lnw[bo] against log(U), decided in single precision when the
         // margins allow, else in FP64 with the project's log
-        const float fa = sh.fwin[bn];
+        const float fa = fwin(sh)[bn];
         const float d = fa - st.flwo;
         bool acc;
         if (d > __int_as_float(cd.z) + st.ew) acc = true;
@@ -301,7 +307,7 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FH
             const double v = sh.win[st.bi] - g.logf;
             sh.win[st.bi] = v;
             const float f = (float)(v - st.cw);
-            sh.fwin[st.bi] = f;
+            fwin(sh)[st.bi] = f;
             st.flwo = f;
             // keep the margin valid for the changed value (NaN stays NaN)
             const float m = fh_margin(fabsf(f));
@@ -313,44 +319,42 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FH
 
 // Multicanonical scan with power-of-two bins (consumer lane 0): straight-line code while
 // every proposed bin is inside the window and the single-precision decision is clear
-// (thresholds precomputed in thr2), with the weight and weight difference of the next
-// site formed for both outcomes of the current decision, so the shared-memory latency
-// leaves the dependent chain.  Returns at the first site that needs fh_scan (window
-// miss, range end, FP64 decision) or at the end of the batch.
+// (thresholds precomputed in thr2); the next site's energy change and thresholds are
+// loaded one site ahead, so the dependent chain per site is one shared-memory load of
+// the weight plus a handful of integer and float operations.  Returns at the first
+// site that needs fh_scan (window miss, range end, FP64 decision) or at the end of the
+// batch.
 __device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int shift, int lim, FHScan& st, int& i,
                                              int n) {
     if (i >= n) return;
     int er = st.er, bi = st.bi;
     float flwo = st.flwo;
     int k = i;
-    int en = er + sl.cand[k].x;
-    bool ok = (unsigned)en < (unsigned)lim;
-    float fa = sh.fwin[ok ? (en >> shift) : bi];
-    float d = fa - flwo;
+    int dn = sl.cand[k].x;
+    float2 t = sh.thr2[k];
     bool go = true;
     while (go) {
-        const int dn = sl.cand[k + 1 < 32 ? k + 1 : 31].x;
-        const float tx = sh.thr2[k].x, ty = sh.thr2[k].y;
-        const int en_r = er + dn, en_a = en + dn;
-        const bool ok_r = (unsigned)en_r < (unsigned)lim, ok_a = (unsigned)en_a < (unsigned)lim;
-        const float fa_r = sh.fwin[ok_r ? (en_r >> shift) : 0];
-        const float fa_a = sh.fwin[ok_a ? (en_a >> shift) : 0];
-        const float d_r = fa_r - flwo, d_a = fa_a - fa;
-        const bool acc = d > tx;
-        const bool clear = ok && (acc || d <= ty);
+        const int en = er + dn;
+        const bool ok = (unsigned)en < (unsigned)lim;
+        const int b = ok ? (en >> shift) : bi;
+        const float fa = fwin(sh)[b];
+        const int kn = k + 1 < 32 ? k + 1 : 31;
+        const int dn2 = sl.cand[kn].x;
+        const float2 t2 = sh.thr2[kn];
+        const float d = fa - flwo;
+        const bool acc = d > t.x;
+        const bool clear = ok && (acc || d <= t.y);
         if (clear) {
             if (acc) {
                 er = en;
-                bi = en >> shift;
+                bi = b;
                 flwo = fa;
             }
             sh.accf[k] = (uint8_t)acc;
             sh.binrec[k] = (uint16_t)bi;
             ++k;
-            en = acc ? en_a : en_r;
-            ok = acc ? ok_a : ok_r;
-            fa = acc ? fa_a : fa_r;
-            d = acc ? d_a : d_r;
+            dn = dn2;
+            t = t2;
         }
         go = clear && k < n;
     }
@@ -358,6 +362,49 @@ __device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int
     st.er = er;
     st.bi = bi;
     st.flwo = flwo;
+}
+
+// Branch-free Multicanonical pass over a whole batch (consumer lane 0), used while the
+// current bin is inside the window: every site is decided in single precision with
+// fa > fl(flwo + hacc + ew) (accept) or fa <= fl(flwo + lo - ew) (reject), which the same
+// margin proves equal to the FP64 rule.  No site depends on a branch, so the dependent
+// chain per site is an add, the window load, a compare and a select.  A site that falls
+// outside the window or is not clear in single precision makes the pass report false;
+// the caller then redoes the batch with fh_scan_fast / fh_scan, which overwrite
+// everything this pass wrote.  Moves are taken only inside the window, so every load
+// stays within the guard entries.
+__device__ __forceinline__ bool fh_batch_fast(FHShared& sh, const FHSlot& sl, int shift, int lim, FHScan& st, int n,
+                                              unsigned int& mask_out) {
+    const float* fw = fwin(sh);
+    int er = st.er, bi = st.bi;
+    float flwo = st.flwo;
+    unsigned int mask = 0;
+    bool clear = true;
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+        if (q < n) {
+            const int en = er + sl.cand[q].x;
+            const int b = en >> shift;
+            const float fa = fw[b];
+            const float2 t = sh.thr2[q];
+            const float ta = flwo + t.x, tr = flwo + t.y;
+            const bool ok = (unsigned)en < (unsigned)lim;
+            const bool up = fa > ta;
+            const bool acc = up & ok;
+            clear = clear & ok & (up | (fa <= tr));
+            er = acc ? en : er;
+            bi = acc ? b : bi;
+            flwo = acc ? fa : flwo;
+            mask |= acc ? (1u << q) : 0u;
+            sh.binrec[q] = (uint16_t)bi;
+        }
+    }
+    if (!clear) return false;
+    st.er = er;
+    st.bi = bi;
+    st.flwo = flwo;
+    mask_out = mask;
+    return true;
 }
 
 // Decision thresholds of the batch for the current window margin (all lanes).
@@ -396,6 +443,7 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     const unsigned long long sweep0 = w.sweep0;
     if (warp == 0 && lane == 0) sh.stop = 0;
     for (int i = threadIdx.x; i < kFHWin; i += 64) sh.hwin[i] = 0;
+    for (int i = threadIdx.x; i < kFHGuard + kFHWin + kFHGuard; i += 64) sh.fwin_g[i] = 0.0f;
     __syncthreads();
 
     if (warp == 0) {
@@ -454,7 +502,7 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     st.Ewb = g.start + wb * g.step;
     st.er = (int)(st.E - st.Ewb);
     st.bi = status ? 0 : (int)(bo - wb);
-    st.flwo = sh.fwin[st.bi];
+    st.flwo = fwin(sh)[st.bi];
     st.steps = 0;
     const bool muca_fast = fast && g.mode == 0;
     if (status && lane == 0) sh.stop = 1;
@@ -471,6 +519,7 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                 if (status == 0) {
                     const int n = (int)((ncol - b * 32) < 32 ? (ncol - b * 32) : 32);
                     int i = 0, h0 = 0;
+                    unsigned int fastmask = 0;  // acceptances of a successful fh_batch_fast (lane 0)
                     sh.accf[lane] = 0;
                     if (muca_fast) fh_thresholds(sh, sl, __shfl_sync(0xFFFFFFFFu, st.ew, 0), lane);
                     __syncwarp();
@@ -480,7 +529,10 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                             const long long vis = wb + kFHWin < g.nbins ? kFHWin : g.nbins - wb;
                             const int lim = (int)(vis << (fast ? g.shift : 0));
                             const int i0 = i;
-                            if (muca_fast) {
+                            if (muca_fast && i == 0 && (unsigned)st.er < (unsigned)lim &&
+                                fh_batch_fast(sh, sl, g.shift, lim, st, n, fastmask)) {
+                                i = n;
+                            } else if (muca_fast) {
                                 for (;;) {
                                     fh_scan_fast(sh, sl, g.shift, lim, st, i, n);
                                     if (i >= n) break;
@@ -511,13 +563,14 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                             st.er += (int)((wb - wb_new) * g.step);  // FAST only (wb moves < 2^11 bins)
                             st.Ewb = g.start + wb_new * g.step;
                             st.bi = (int)(bo_all - wb_new);
-                            st.flwo = sh.fwin[st.bi];
+                            st.flwo = fwin(sh)[st.bi];
                         }
                         wb = wb_new;
                         if (muca_fast) fh_thresholds(sh, sl, ew, lane);
                     }
                     __syncwarp();
-                    const unsigned int accmask = __ballot_sync(0xFFFFFFFFu, sh.accf[lane] != 0);
+                    const unsigned int accmask =
+                        __ballot_sync(0xFFFFFFFFu, sh.accf[lane] != 0) | __shfl_sync(0xFFFFFFFFu, fastmask, 0);
                     status = __shfl_sync(0xFFFFFFFFu, status, 0);
                     if ((accmask >> lane) & 1u) {
                         const uint32_t pk = (uint32_t)sl.cand[lane].w;

@@ -51,6 +51,7 @@ struct PTArgs {
     unsigned int* claim;     // [3] per-phase tile tickets (persistent form)
     int nrep, npos, ntiles;
     const unsigned long long* tables;  // [npos][16] for the algorithm of this run (ising_tab_entry form)
+    const uint32_t* tables32;          // the same minus 1 (32-bit form, when no entry is 0)
     const double* betas;               // [npos]
     const int* pos_ladder;             // [npos]
     const int* pos_local;              // [npos]
@@ -76,11 +77,12 @@ struct PTArgs {
 // n / d for small n, d: m = ceil(2^32 / d) (exact while n < 2^32 / d); m = 0 encodes d = 1
 __device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m) { return m ? __umulhi(n, m) : n; }
 
-// One tile of one replica: chunks [c_begin, c_end) of colour `colour`.
-template <int DIM, int V, bool HB>
+// One tile of one replica: chunks [c_begin, c_end) of colour `colour`; `tab` is the
+// replica's table in shared memory (64-bit, or 32-bit when T32).
+template <int DIM, int V, bool HB, bool T32>
 __device__ __forceinline__ void pt_tile(const PTArgs& a, const PTReplica& R, int rep, int c_begin, int c_end,
-                                        int colour, unsigned long long sweep, const unsigned long long* s_thr,
-                                        int& nacc, int& nup, int& isum) {
+                                        int colour, unsigned long long sweep, const void* tab, int& nacc, int& nup,
+                                        int& isum) {
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
     int8_t* cur = a.arena + R.off[colour];
@@ -95,14 +97,22 @@ __device__ __forceinline__ void pt_tile(const PTArgs& a, const PTReplica& R, int
         Chunk<DIM, V> ch;
         ch.load(cur, oth, R.W, r, q * V, ri);
         const uint32_t c0 = (uint32_t)(((unsigned long long)r * R.W + q * V) >> 2);
+        uint32_t af = 0, au = 0, ai = 0;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
             uint32_t nbw[Z];
 #pragma unroll
             for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
             const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, (uint32_t)rep), a.k0, a.k1);
-            const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
+            uint32_t fb;
+            if (T32) fb = ising_word32<Z, HB>(nbw, ch.own[w], rnd, (const uint32_t*)tab, af, au, ai);
+            else fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, (const unsigned long long*)tab, nacc, nup, isum);
             ch.own[w] ^= fb * 0xFEu;
+        }
+        if (T32) {
+            nacc += hsum8(af);
+            nup += hsum8(au);
+            isum += hsum16(ai);
         }
         store_row<V>(cur + (long long)r * R.W + q * V, ch.own);
     }
@@ -122,15 +132,14 @@ __device__ __forceinline__ void warp_add_atomic(long long (&v)[N], unsigned long
 }
 
 // One tile with its acceptance table `thr` (shared memory); per-warp atomics.
-template <int DIM, bool HB>
+template <int DIM, bool HB, bool T32>
 __device__ __forceinline__ void pt_run_tile(const PTArgs& a, const PTTile& tl, int colour,
-                                            unsigned long long sweep, long long* dcur,
-                                            const unsigned long long* thr) {
+                                            unsigned long long sweep, long long* dcur, const void* thr) {
     const PTReplica R = a.reps[tl.rep];
     int nacc = 0, nup = 0, isum = 0;
-    if (R.V == 16) pt_tile<DIM, 16, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
-    else if (R.V == 8) pt_tile<DIM, 8, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
-    else pt_tile<DIM, 4, HB>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
+    if (R.V == 16) pt_tile<DIM, 16, HB, T32>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
+    else if (R.V == 8) pt_tile<DIM, 8, HB, T32>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
+    else pt_tile<DIM, 4, HB, T32>(a, R, tl.rep, tl.c_begin, tl.c_end, colour, sweep, thr, nacc, nup, isum);
     constexpr int Z = 2 * DIM;
     long long dP, dM;
     ising_deltas<Z>(nacc, nup, isum, dP, dM);
@@ -222,16 +231,21 @@ __device__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long l
     return s_ok != 0;
 }
 
-template <int DIM, bool HB>
+template <int DIM, bool HB, bool T32>
 __global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
     extern __shared__ long long smem[];
-    unsigned long long* s_tab = reinterpret_cast<unsigned long long*>(smem);  // [npos][16]
-    long long* s_P = smem + (size_t)a.npos * 16;
+    // [npos][16] tables (8 or 4 bytes per entry), then the per-replica state
+    unsigned long long* s_tab = reinterpret_cast<unsigned long long*>(smem);
+    uint32_t* s_tab32 = reinterpret_cast<uint32_t*>(smem);
+    long long* s_P = smem + (size_t)a.npos * (T32 ? 8 : 16);
     long long* s_M = s_P + a.nrep;
     int* s_pos = reinterpret_cast<int*>(s_M + a.nrep);
     int* s_rep = s_pos + a.nrep;
     __shared__ unsigned s_gen;
-    for (int i = threadIdx.x; i < a.npos * 16; i += blockDim.x) s_tab[i] = a.tables[i];
+    for (int i = threadIdx.x; i < a.npos * 16; i += blockDim.x) {
+        if (T32) s_tab32[i] = a.tables32[i];
+        else s_tab[i] = a.tables[i];
+    }
     for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
         s_P[r] = a.state[2 * r];
         s_M[r] = a.state[2 * r + 1];
@@ -272,7 +286,8 @@ __global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
                 if (threadIdx.x == 0) nk = atomicAdd(ctr, 1u);  // the next claim flies during this tile
                 const PTTile tl = a.tiles[a.order[k]];
                 const int gpos = a.reps[tl.rep].gpos0 + s_pos[tl.rep];
-                pt_run_tile<DIM, HB>(a, tl, colour, t, dcur, s_tab + (size_t)gpos * 16);
+                const void* tab = T32 ? (const void*)(s_tab32 + (size_t)gpos * 16) : (const void*)(s_tab + (size_t)gpos * 16);
+                pt_run_tile<DIM, HB, T32>(a, tl, colour, t, dcur, tab);
                 __syncthreads();
                 if (threadIdx.x == 0) s_ticket = nk;
                 __syncthreads();
@@ -306,15 +321,19 @@ __global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
 }
 
 // Plain form: one launch per replica and colour (blocks = that replica's tiles).
-template <int DIM, bool HB>
+template <int DIM, bool HB, bool T32>
 __global__ void __launch_bounds__(256) k_pt_plain_half(const PTArgs a, int tile0, int colour,
                                                        unsigned long long sweep) {
     __shared__ unsigned long long s_thr[16];
+    __shared__ uint32_t s_thr32[16];
     const PTTile tl = a.tiles[tile0 + blockIdx.x];
-    if (threadIdx.x < 16)
-        s_thr[threadIdx.x] = a.tables[(size_t)(a.reps[tl.rep].gpos0 + a.pos[tl.rep]) * 16 + threadIdx.x];
+    if (threadIdx.x < 16) {
+        const size_t e = (size_t)(a.reps[tl.rep].gpos0 + a.pos[tl.rep]) * 16 + threadIdx.x;
+        if (T32) s_thr32[threadIdx.x] = a.tables32[e];
+        else s_thr[threadIdx.x] = a.tables[e];
+    }
     __syncthreads();
-    pt_run_tile<DIM, HB>(a, tl, colour, sweep, a.delta, s_thr);
+    pt_run_tile<DIM, HB, T32>(a, tl, colour, sweep, a.delta, T32 ? (const void*)s_thr32 : (const void*)s_thr);
 }
 
 // Plain form: fold the sweep's deltas into the state, record, exchange (one block).
@@ -383,6 +402,8 @@ struct mcx_pt {
     unsigned int* d_claim = nullptr; // per-phase tile tickets
     int grid = 0;                    // persistent grid size
     unsigned long long* d_tables = nullptr;  // [3 algs][npos][16]
+    uint32_t* d_tables32 = nullptr;          // [3 algs][npos][16], entry - 1
+    bool fits32[3] = {false, false, false};  // every entry of the algorithm's tables >= 1
     double* d_betas = nullptr;
     int* d_pos_ladder = nullptr;
     int* d_pos_local = nullptr;
@@ -426,21 +447,33 @@ static mcx_status pt_upload(mcx_pt* pt, T** dst, const std::vector<T>& v) {
 using PersistentFn = void (*)(const PTArgs);
 using PlainFn = void (*)(const PTArgs, int, int, unsigned long long);
 
-static PersistentFn persistent_fn(int dim, bool hb) {
-    if (dim == 2) return hb ? k_pt_persistent<2, true> : k_pt_persistent<2, false>;
-    return hb ? k_pt_persistent<3, true> : k_pt_persistent<3, false>;
+template <int DIM, bool T32>
+static PersistentFn persistent_fn_t(bool hb) {
+    return hb ? k_pt_persistent<DIM, true, T32> : k_pt_persistent<DIM, false, T32>;
 }
 
-static PlainFn plain_fn(int dim, bool hb) {
-    if (dim == 2) return hb ? k_pt_plain_half<2, true> : k_pt_plain_half<2, false>;
-    return hb ? k_pt_plain_half<3, true> : k_pt_plain_half<3, false>;
+static PersistentFn persistent_fn(int dim, bool hb, bool t32) {
+    if (dim == 2) return t32 ? persistent_fn_t<2, true>(hb) : persistent_fn_t<2, false>(hb);
+    return t32 ? persistent_fn_t<3, true>(hb) : persistent_fn_t<3, false>(hb);
+}
+
+template <int DIM, bool T32>
+static PlainFn plain_fn_t(bool hb) {
+    return hb ? k_pt_plain_half<DIM, true, T32> : k_pt_plain_half<DIM, false, T32>;
+}
+
+static PlainFn plain_fn(int dim, bool hb, bool t32) {
+    if (dim == 2) return t32 ? plain_fn_t<2, true>(hb) : plain_fn_t<2, false>(hb);
+    return t32 ? plain_fn_t<3, true>(hb) : plain_fn_t<3, false>(hb);
 }
 
 static size_t pt_smem(const mcx_pt* pt) {
     return (size_t)pt->nrep * (2 * sizeof(long long) + sizeof(int)) + (size_t)pt->npos * sizeof(int);
 }
 
-static size_t pt_smem_persistent(const mcx_pt* pt) { return pt_smem(pt) + (size_t)pt->npos * 16 * 8; }
+static size_t pt_smem_persistent(const mcx_pt* pt, bool t32) {
+    return pt_smem(pt) + (size_t)pt->npos * 16 * (t32 ? 4 : 8);
+}
 
 // Claiming order of the persistent form: tiles sorted by estimated cost, largest
 // first (blocks then take tiles from a ticket counter, which balances the phase).
@@ -470,6 +503,7 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->ntiles = (int)pt->tiles.size();
     a->npos = pt->npos;
     a->tables = pt->d_tables + (size_t)alg * pt->npos * 16;
+    a->tables32 = pt->d_tables32 + (size_t)alg * pt->npos * 16;
     a->betas = pt->d_betas;
     a->pos_ladder = pt->d_pos_ladder;
     a->pos_local = pt->d_pos_local;
@@ -688,6 +722,17 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
                     ising_tab_entry(t.thr[i], i, 2 * dim, alg == MCX_HEATBATH);
         }
     run(pt_upload(pt, &pt->d_tables, tabs));
+    std::vector<uint32_t> tabs32(tabs.size());
+    for (int alg = 0; alg < 3; ++alg) {
+        pt->fits32[alg] = true;
+        for (int gp = 0; gp < pt->npos; ++gp)
+            for (int i = 0; i < 16; ++i) {
+                const size_t e = ((size_t)alg * pt->npos + gp) * 16 + i;
+                if (i < 2 * (2 * dim + 1) && tabs[e] == 0) pt->fits32[alg] = false;
+                tabs32[e] = (uint32_t)(tabs[e] - 1);
+            }
+    }
+    run(pt_upload(pt, &pt->d_tables32, tabs32));
     std::vector<int32_t> pos0(pt->nrep);
     for (int r = 0; r < pt->nrep; ++r) pos0[r] = r - pt->ladder_gpos0[pt->rep_ladder[r]];
     run(pt_upload(pt, &pt->d_pos, pos0));
@@ -703,13 +748,18 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
     pt->d_lin = (int8_t*)p;
     if (st == MCX_OK) {
         // schedule for the persistent grid
-        int bps = 0;
-        const size_t smem = pt_smem_persistent(pt);
-        const PersistentFn fn = persistent_fn(dim, false);
-        cudaFuncSetAttribute(persistent_fn(dim, true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        // one grid for every variant: the smallest co-resident block count among them
+        int bps = 1 << 30;
+        for (int v = 0; v < 4; ++v) {
+            const bool hb = v & 1, t32 = v >> 1;
+            const size_t smem = pt_smem_persistent(pt, t32);
+            const PersistentFn fn = persistent_fn(dim, hb, t32);
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, smem) != cudaSuccess || b < 1) b = 1;
+            bps = std::min(bps, b);
+        }
         cudaFuncSetAttribute(k_pt_plain_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pt_smem(pt));
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, smem) != cudaSuccess || bps < 1) bps = 1;
         run(pt_schedule(pt, ctx->num_sms * bps));
     }
     if (st == MCX_OK) {
@@ -812,15 +862,16 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
     a.nsweeps = nsweeps;
     a.every = exchange_every;
     const bool hb = alg == MCX_HEATBATH;
+    const bool t32 = pt->fits32[alg];
     const size_t smem = pt_smem(pt);
-    const size_t smem_persistent = pt_smem_persistent(pt);
+    const size_t smem_persistent = pt_smem_persistent(pt, t32);
     MCX_CUDA(cudaMemsetAsync(pt->d_acc, 0, (size_t)pt->nrep * sizeof(unsigned long long), ctx->stream));
     if (mode == MCX_PT_PERSISTENT) {
         MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 6 * sizeof(long long), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar, 0, sizeof(unsigned int), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar + 2, 0, sizeof(unsigned int), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_claim, 0, 3 * sizeof(unsigned int), ctx->stream));
-        const PersistentFn fn = persistent_fn(pt->dim, hb);
+        const PersistentFn fn = persistent_fn(pt->dim, hb, t32);
         void* args[] = {&a};
         MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem_persistent,
                                              ctx->stream));
@@ -831,7 +882,7 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
         if (err) return fail(MCX_ERR_TIMEOUT, "grid barrier wait exceeded its limit");
     } else {
         MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 2 * sizeof(long long), ctx->stream));
-        const PlainFn fn = plain_fn(pt->dim, hb);
+        const PlainFn fn = plain_fn(pt->dim, hb, t32);
         for (int64_t s = 0; s < nsweeps; ++s) {
             const unsigned long long t = rng->counter + (unsigned long long)s;
             for (int r = 0; r < pt->nrep; ++r)
