@@ -69,17 +69,24 @@ constexpr int kFHGuard = kFHWin / 2;
 constexpr double kLogMargin = 6.103515625e-05;  // 2^-14
 
 struct FHSlot {
+    // producer -> consumer
     int4 cand[32];                // dE, lo, hacc (float bits), packed (sn, ds, dq, dp)
     unsigned long long k53[32];   // U = k * 2^-53
+    long long j0;                 // first site of the batch in its colour
+    int colour;
+    // consumer -> producer (applied when the slot is next reused or at a colour end)
+    int bin[32];                  // bin after each attempt, relative to base
+    long long base;
+    unsigned int accmask;         // accepted attempts
+    int nproc;                    // attempts made (fewer than the batch after a range stop)
+    int pending;                  // results not applied yet
 };
 
 struct FHShared {
     FHSlot slot[kFHSlots];
     double win[kFHWin];
     float fwin_g[kFHGuard + kFHWin + kFHGuard];  // fwin(sh)[-kFHGuard, kFHWin + kFHGuard)
-    unsigned long long hwin[kFHWin];
     uint32_t rnd[3][8][4];  // producer: Philox blocks of one batch by purpose
-    uint16_t binrec[32];    // consumer: window bin after each attempt of the batch
     uint8_t accf[32];       // consumer: 1 where the batch's attempt was accepted
     float2 thr2[32];        // consumer: (hacc + ew, lo - ew) of the batch's sites
     int stop;
@@ -126,19 +133,6 @@ __device__ __forceinline__ float fh_window_load(FHShared& sh, const double* lnw,
     return fh_margin(__uint_as_float(m));
 }
 
-// Adds the window's histogram counts to H and clears them (all lanes of the consumer).
-__device__ __forceinline__ void fh_hist_flush(FHShared& sh, unsigned long long* H, long long wb, long long nbins,
-                                              int lane) {
-    __syncwarp();
-    for (int i = lane; i < kFHWin; i += 32) {
-        const unsigned long long h = sh.hwin[i];
-        if (h) {
-            if (wb + i < nbins) atomicAdd(&H[wb + i], h);
-            sh.hwin[i] = 0;
-        }
-    }
-    __syncwarp();
-}
 
 __device__ __forceinline__ void fh_window_store(const FHShared& sh, double* lnw, long long wb, long long nbins,
                                                 int lane) {
@@ -246,7 +240,7 @@ struct FHScan {
 // Scans sites i..n-1 of one batch (consumer lane 0).  Stops early with `need` set to
 // the bin that must come into the window, or with status 2 (energy out of range).
 template <bool FAST>
-__device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FHGeom& g, long long wb, int lim,
+__device__ __forceinline__ void fh_scan(FHShared& sh, FHSlot& sl, const FHGeom& g, long long wb, int lim,
                                         FHScan& st, int& i, int n, long long& need, int& status) {
     const bool wl = g.mode == 1;
     int4 nx = sl.cand[i < n ? i : 0];
@@ -313,7 +307,7 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FH
             const float m = fh_margin(fabsf(f));
             if (st.ew == st.ew && !(m <= st.ew)) st.ew = m;
         }
-        sh.binrec[i] = (uint16_t)st.bi;
+        sl.bin[i] = st.bi;
     }
 }
 
@@ -324,7 +318,7 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, const FHSlot& sl, const FH
 // the weight plus a handful of integer and float operations.  Returns at the first
 // site that needs fh_scan (window miss, range end, FP64 decision) or at the end of the
 // batch.
-__device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int shift, int lim, FHScan& st, int& i,
+__device__ __forceinline__ void fh_scan_fast(FHShared& sh, FHSlot& sl, int shift, int lim, FHScan& st, int& i,
                                              int n) {
     if (i >= n) return;
     int er = st.er, bi = st.bi;
@@ -351,7 +345,7 @@ __device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int
                 flwo = fa;
             }
             sh.accf[k] = (uint8_t)acc;
-            sh.binrec[k] = (uint16_t)bi;
+            sl.bin[k] = bi;
             ++k;
             dn = dn2;
             t = t2;
@@ -364,7 +358,7 @@ __device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int
     st.flwo = flwo;
 }
 
-// Branch-free Multicanonical pass over a whole batch (consumer lane 0), used while the
+// Branch-free Multicanonical pass over a full batch of 32 sites (consumer lane 0), used while the
 // current bin is inside the window: every site is decided in single precision with
 // fa > fl(flwo + hacc + ew) (accept) or fa <= fl(flwo + lo - ew) (reject), which the same
 // margin proves equal to the FP64 rule.  No site depends on a branch, so the dependent
@@ -373,7 +367,7 @@ __device__ __forceinline__ void fh_scan_fast(FHShared& sh, const FHSlot& sl, int
 // the caller then redoes the batch with fh_scan_fast / fh_scan, which overwrite
 // everything this pass wrote.  Moves are taken only inside the window, so every load
 // stays within the guard entries.
-__device__ __forceinline__ bool fh_batch_fast(FHShared& sh, const FHSlot& sl, int shift, int lim, FHScan& st, int n,
+__device__ __forceinline__ bool fh_batch_fast(FHShared& sh, FHSlot& sl, int shift, int lim, FHScan& st,
                                               unsigned int& mask_out) {
     const float* fw = fwin(sh);
     int er = st.er, bi = st.bi;
@@ -382,7 +376,7 @@ __device__ __forceinline__ bool fh_batch_fast(FHShared& sh, const FHSlot& sl, in
     bool clear = true;
 #pragma unroll
     for (int q = 0; q < 32; ++q) {
-        if (q < n) {
+        {
             const int en = er + sl.cand[q].x;
             const int b = en >> shift;
             const float fa = fw[b];
@@ -396,7 +390,7 @@ __device__ __forceinline__ bool fh_batch_fast(FHShared& sh, const FHSlot& sl, in
             bi = acc ? b : bi;
             flwo = acc ? fa : flwo;
             mask |= acc ? (1u << q) : 0u;
-            sh.binrec[q] = (uint16_t)bi;
+            sl.bin[q] = bi;
         }
     }
     if (!clear) return false;
@@ -414,17 +408,27 @@ __device__ __forceinline__ void fh_thresholds(FHShared& sh, const FHSlot& sl, fl
     __syncwarp();
 }
 
-// Histogram counts of sites [h0, h1) of the batch (all lanes of the consumer): lanes
-// holding the same bin add once, as a group.
-__device__ __forceinline__ void fh_hist_batch(FHShared& sh, int h0, int h1, int lane) {
-    __syncwarp();
-    const bool act = lane >= h0 && lane < h1;
+// Producer: applies the consumer's results of one batch (all lanes): histogram counts
+// of the bins after each attempt (lanes holding the same bin add once, as a group), the
+// accepted spins and the observable deltas.
+__device__ __forceinline__ void fh_apply(FHSlot& sl, int8_t* col0, int8_t* col1, unsigned long long* H, long long& dP,
+                                         long long& dM, long long& dQ, int lane) {
+    const bool act = lane < sl.nproc;
     const unsigned int am = __ballot_sync(0xFFFFFFFFu, act);
     if (act) {
-        const int b = sh.binrec[lane];
-        const unsigned int grp = __match_any_sync(am, b);
-        if (lane == __ffs(grp) - 1) sh.hwin[b] += (unsigned long long)__popc(grp);
+        const long long bin = sl.base + sl.bin[lane];
+        const unsigned int grp = __match_any_sync(am, bin);
+        if (lane == __ffs(grp) - 1) atomicAdd(&H[bin], (unsigned long long)__popc(grp));
+        if ((sl.accmask >> lane) & 1u) {
+            const uint32_t pk = (uint32_t)sl.cand[lane].w;
+            (sl.colour ? col1 : col0)[sl.j0 + lane] = (int8_t)(pk & 0xFFu);
+            dP += (int8_t)(pk >> 24);
+            dM += (int8_t)((pk >> 8) & 0xFFu);
+            dQ += (int8_t)((pk >> 16) & 0xFFu);
+        }
     }
+    __syncwarp();
+    if (lane == 0) sl.pending = 0;
     __syncwarp();
 }
 
@@ -442,40 +446,113 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     const long long total = g.nsweeps * 2 * nb;          // batches of the launch
     const unsigned long long sweep0 = w.sweep0;
     if (warp == 0 && lane == 0) sh.stop = 0;
-    for (int i = threadIdx.x; i < kFHWin; i += 64) sh.hwin[i] = 0;
+    if (threadIdx.x < kFHSlots) sh.slot[threadIdx.x].pending = 0;
     for (int i = threadIdx.x; i < kFHGuard + kFHWin + kFHGuard; i += 64) sh.fwin_g[i] = 0.0f;
     __syncthreads();
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer --
+        // Prepares batches, and applies the consumer's results of a batch when its slot
+        // is reused or at the end of a colour: histogram counts, accepted spins and the
+        // running (pair, spin, spin2) sums with the per-sweep series.
         const uint32_t k0 = w.k0, k1 = w.k1, stream = w.stream;
+        unsigned long long* const H = w.H;
+        long long* const series = w.series;
+        long long P = w.P, M = w.M, Q = w.Q;
+        if (w.state) {
+            P = w.state[0];
+            M = w.state[1];
+            Q = w.state[2];
+        }
+        long long dP = 0, dM = 0, dQ = 0;
+        bool stopped = false;
+        // every slot with results not applied yet (the consumer has finished the colour)
+        auto apply_all = [&]() {
+            for (int k = 0; k < kFHSlots; ++k)
+                if (sh.slot[k].pending) fh_apply(sh.slot[k], col0, col1, H, dP, dM, dQ, lane);
+        };
+        // fold the sweep's deltas; the series records sweeps that ran to the end
+        auto end_sweep = [&](long long s) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                dP += __shfl_down_sync(0xFFFFFFFFu, dP, o);
+                dM += __shfl_down_sync(0xFFFFFFFFu, dM, o);
+                dQ += __shfl_down_sync(0xFFFFFFFFu, dQ, o);
+            }
+            dP = __shfl_sync(0xFFFFFFFFu, dP, 0);
+            dM = __shfl_sync(0xFFFFFFFFu, dM, 0);
+            dQ = __shfl_sync(0xFFFFFFFFu, dQ, 0);
+            P += dP;
+            M += dM;
+            Q += dQ;
+            dP = dM = dQ = 0;
+            stopped = stopped || *(volatile int*)&sh.stop;
+            if (lane == 0 && !stopped && series) {
+                series[3 * s] = P;
+                series[3 * s + 1] = M;
+                series[3 * s + 2] = Q;
+            }
+        };
         long long qb = 0;
         for (long long s = 0; s < g.nsweeps; ++s) {
             const unsigned long long t = sweep0 + (unsigned long long)s;
             for (int c = 0; c < 2; ++c) {
-                if (s > 0 || c > 0) fh_bar_sync(kFHBarCol);
+                if (s > 0 || c > 0) {
+                    fh_bar_sync(kFHBarCol);
+                    apply_all();
+                    if (c == 0) end_sweep(s - 1);
+                }
                 const int8_t* cur = c ? col1 : col0;
                 const int8_t* oth = c ? col0 : col1;
-                int r0 = 0, q0 = 0;
-                FHLoad ld = fh_load(g, cur, oth, c, 0, 0, 0, ncol, lane);
+                // spins of batches b and b + 1 are in registers or in flight; the loads of
+                // batch b + 2 are issued after batch b is handed over, so the fence before
+                // the hand-over never waits on them (sites the consumer has not reached)
+                int r2 = 0, q2 = 0;  // row and column of the first site of the batch loaded next
+                auto advance = [&]() {
+                    q2 += 32;
+                    while (q2 >= g.W) {
+                        q2 -= g.W;
+                        ++r2;
+                    }
+                };
+                FHLoad ld0 = fh_load(g, cur, oth, c, 0, r2, q2, ncol, lane);
+                advance();
+                FHLoad ld1 = fh_load(g, cur, oth, c, 32, r2, q2, ncol, lane);
+                advance();
                 for (long long b = 0; b < nb; ++b, ++qb) {
                     const int sl = (int)(qb % kFHSlots);
-                    // next batch's loads first (sites the consumer has not reached)
-                    int r1 = r0, q1 = q0 + 32;
-                    while (q1 >= g.W) {
-                        q1 -= g.W;
-                        ++r1;
+                    if (qb >= kFHSlots) {
+                        fh_bar_sync(kFHBarEmpty + sl);
+                        if (sh.slot[sl].pending) fh_apply(sh.slot[sl], col0, col1, H, dP, dM, dQ, lane);
                     }
-                    const FHLoad nx = fh_load(g, cur, oth, c, (b + 1) * 32, r1, q1, ncol, lane);
-                    if (qb >= kFHSlots) fh_bar_sync(kFHBarEmpty + sl);
                     if (!*(volatile int*)&sh.stop)
-                        fh_produce(sh, sh.slot[sl], g, ld, c, t, b * 32, ncol, k0, k1, stream, lane);
+                        fh_produce(sh, sh.slot[sl], g, ld0, c, t, b * 32, ncol, k0, k1, stream, lane);
+                    if (lane == 0) {
+                        sh.slot[sl].j0 = b * 32;
+                        sh.slot[sl].colour = c;
+                    }
                     __threadfence_block();
                     fh_bar_arrive(kFHBarFull + sl);
-                    ld = nx;
-                    r0 = r1;
-                    q0 = q1;
+                    ld0 = ld1;
+                    ld1 = fh_load(g, cur, oth, c, (b + 2) * 32, r2, q2, ncol, lane);
+                    advance();
                 }
+            }
+        }
+        if (g.nsweeps > 0) {
+            fh_bar_sync(kFHBarCol);  // the consumer has finished the last colour
+            apply_all();
+            end_sweep(g.nsweeps - 1);
+        }
+        if (lane == 0) {
+            // a stopped sweep still folds the accepted moves made before the stop
+            w.P = P;
+            w.M = M;
+            w.Q = Q;
+            if (w.state) {
+                w.state[0] = P;
+                w.state[1] = M;
+                w.state[2] = Q;
             }
         }
         return;
@@ -483,17 +560,17 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
 
     // ---------------------------------------------------------------- consumer --
     double* const lnw = w.lnw;
-    unsigned long long* const H = w.H;
-    long long* const series = w.series;
-    long long P = w.P, M = w.M, Q = w.Q;
-    if (w.state) {
-        P = w.state[0];
-        M = w.state[1];
-        Q = w.state[2];
-    }
     int status = 0;
     FHScan st;
-    st.E = -g.J * P + g.D * Q - g.h * M;
+    {
+        long long P = w.P, M = w.M, Q = w.Q;
+        if (w.state) {
+            P = w.state[0];
+            M = w.state[1];
+            Q = w.state[2];
+        }
+        st.E = -g.J * P + g.D * Q - g.h * M;
+    }
     long long bo = 0;
     if (!fh_bin(st.E, g, bo)) status = 2;
     const bool fast = g.shift >= 0 && g.shift <= 20;
@@ -509,16 +586,15 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     unsigned long long accepted = 0;
     long long qb = 0;
     for (long long s = 0; s < g.nsweeps; ++s) {
-        long long dP = 0, dM = 0, dQ = 0;
         for (int c = 0; c < 2; ++c) {
-            int8_t* cur = c ? col1 : col0;
             for (long long b = 0; b < nb; ++b, ++qb) {
                 const int slot = (int)(qb % kFHSlots);
                 fh_bar_sync(kFHBarFull + slot);
-                const FHSlot& sl = sh.slot[slot];
+                FHSlot& sl = sh.slot[slot];
+                int i = 0;
+                unsigned int accmask = 0;
                 if (status == 0) {
                     const int n = (int)((ncol - b * 32) < 32 ? (ncol - b * 32) : 32);
-                    int i = 0, h0 = 0;
                     unsigned int fastmask = 0;  // acceptances of a successful fh_batch_fast (lane 0)
                     sh.accf[lane] = 0;
                     if (muca_fast) fh_thresholds(sh, sl, __shfl_sync(0xFFFFFFFFu, st.ew, 0), lane);
@@ -529,8 +605,8 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                             const long long vis = wb + kFHWin < g.nbins ? kFHWin : g.nbins - wb;
                             const int lim = (int)(vis << (fast ? g.shift : 0));
                             const int i0 = i;
-                            if (muca_fast && i == 0 && (unsigned)st.er < (unsigned)lim &&
-                                fh_batch_fast(sh, sl, g.shift, lim, st, n, fastmask)) {
+                            if (muca_fast && i == 0 && n == 32 && (unsigned)st.er < (unsigned)lim &&
+                                fh_batch_fast(sh, sl, g.shift, lim, st, fastmask)) {
                                 i = n;
                             } else if (muca_fast) {
                                 for (;;) {
@@ -548,15 +624,16 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                         }
                         need = __shfl_sync(0xFFFFFFFFu, need, 0);
                         i = __shfl_sync(0xFFFFFFFFu, i, 0);
-                        fh_hist_batch(sh, h0, i, lane);
-                        h0 = i;
                         if (need < 0) break;
                         // move the window around the proposed bin (the current bin stays
-                        // inside: one move changes the bin by far less than half the window)
-                        fh_hist_flush(sh, H, wb, g.nbins, lane);
+                        // inside: one move changes the bin by far less than half the window);
+                        // the bins recorded so far in this batch are rebased on the new window
                         if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
                         const long long bo_all = __shfl_sync(0xFFFFFFFFu, wb + st.bi, 0);
                         const long long wb_new = fh_window_base(need, g.nbins);
+                        __syncwarp();
+                        if (lane < i) sl.bin[lane] += (int)(wb - wb_new);
+                        __syncwarp();
                         const float ew = fh_window_load(sh, lnw, wb_new, g.nbins, need, lane, st.cw);
                         if (lane == 0) {
                             st.ew = ew;
@@ -569,58 +646,26 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                         if (muca_fast) fh_thresholds(sh, sl, ew, lane);
                     }
                     __syncwarp();
-                    const unsigned int accmask =
-                        __ballot_sync(0xFFFFFFFFu, sh.accf[lane] != 0) | __shfl_sync(0xFFFFFFFFu, fastmask, 0);
+                    accmask = __ballot_sync(0xFFFFFFFFu, sh.accf[lane] != 0) | __shfl_sync(0xFFFFFFFFu, fastmask, 0);
                     status = __shfl_sync(0xFFFFFFFFu, status, 0);
-                    if ((accmask >> lane) & 1u) {
-                        const uint32_t pk = (uint32_t)sl.cand[lane].w;
-                        cur[b * 32 + lane] = (int8_t)(pk & 0xFFu);
-                        dP += (int8_t)(pk >> 24);
-                        dM += (int8_t)((pk >> 8) & 0xFFu);
-                        dQ += (int8_t)((pk >> 16) & 0xFFu);
-                    }
-                    if (lane == 0) {
-                        accepted += __popc(accmask);
-                        if (status) sh.stop = 1;
-                    }
                 }
+                if (lane == 0) {
+                    accepted += __popc(accmask);
+                    if (status) sh.stop = 1;
+                    sl.accmask = accmask;
+                    sl.nproc = i;
+                    sl.base = wb;
+                    sl.pending = 1;
+                }
+                __syncwarp();
                 __threadfence_block();
                 if (qb + kFHSlots < total) fh_bar_arrive(kFHBarEmpty + slot);
             }
-            if (s + 1 < g.nsweeps || c == 0) fh_bar_arrive(kFHBarCol);
+            fh_bar_arrive(kFHBarCol);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            dP += __shfl_down_sync(0xFFFFFFFFu, dP, o);
-            dM += __shfl_down_sync(0xFFFFFFFFu, dM, o);
-            dQ += __shfl_down_sync(0xFFFFFFFFu, dQ, o);
-        }
-        if (lane == 0) {
-            P += dP;
-            M += dM;
-            Q += dQ;
-            if (status == 0 && series) {
-                series[3 * s] = P;
-                series[3 * s + 1] = M;
-                series[3 * s + 2] = Q;
-            }
-        }
-        P = __shfl_sync(0xFFFFFFFFu, P, 0);
-        M = __shfl_sync(0xFFFFFFFFu, M, 0);
-        Q = __shfl_sync(0xFFFFFFFFu, Q, 0);
     }
-    fh_hist_flush(sh, H, wb, g.nbins, lane);
     if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
     if (lane == 0) {
-        // a stopped sweep still folds the accepted moves made before the stop
-        w.P = P;
-        w.M = M;
-        w.Q = Q;
-        if (w.state) {
-            w.state[0] = P;
-            w.state[1] = M;
-            w.state[2] = Q;
-        }
         w.steps = st.steps;
         w.accepted = accepted;
         w.status = status;
