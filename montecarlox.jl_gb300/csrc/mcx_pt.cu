@@ -2,10 +2,10 @@
 // checkerboard sweeps and the replica-exchange step.
 //
 // Two forms with bit-identical results:
-//   PERSISTENT: one cooperative launch runs all sweeps of all replicas.  Replicas are
-//     cut into tiles of ~4096 same-colour sites; in every phase the blocks claim tiles,
-//     largest first, from an atomic ticket counter (dynamic balancing of tiles of
-//     unequal cost).  A bounded grid barrier
+//   PERSISTENT: one cooperative launch runs all sweeps of all replicas.  Every warp of
+//     the grid owns one chunk range of one replica (built on the host: warps are handed
+//     to replicas by cost, and a replica's chunks are split evenly among its warps), so
+//     a phase needs no block barrier and no atomic claiming.  A bounded grid barrier
 //     separates the two colours of a sweep and the sweep from the exchange; every
 //     block then evaluates the (tiny) exchange step itself, so the new ladder
 //     positions need no further barrier.  Per-replica energy deltas are triple
@@ -46,9 +46,8 @@ struct PTTile {
 struct PTArgs {
     int8_t* arena;
     const PTReplica* reps;
-    const PTTile* tiles;
-    const int* order;        // tiles in claiming order, largest first (persistent form)
-    unsigned int* claim;     // [3] per-phase tile tickets (persistent form)
+    const PTTile* tiles;     // per-block tiles of one replica-colour (plain form)
+    const PTTile* spans;     // one chunk range of one replica per warp of the grid (persistent form)
     int nrep, npos, ntiles;
     const unsigned long long* tables;  // [npos][16] for the algorithm of this run (ising_tab_entry form)
     const uint32_t* tables32;          // the same minus 1 (32-bit form, when no entry is 0)
@@ -129,6 +128,64 @@ __device__ __forceinline__ void warp_add_atomic(long long (&v)[N], unsigned long
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
         if ((threadIdx.x & 31) == 0 && x != 0) atomicAdd(dst[j], (unsigned long long)x);
     }
+}
+
+// One warp's chunk range [c_begin, c_end) of one replica: lanes take consecutive chunks
+// (coalesced rows), no block barrier; deltas reduced over the warp.
+template <int DIM, int V, bool HB, bool T32>
+__device__ __forceinline__ void pt_span(const PTArgs& a, const PTReplica& R, int rep, int c_begin, int c_end,
+                                        int colour, unsigned long long sweep, const void* tab, int lane, int& nacc,
+                                        int& nup, int& isum) {
+    constexpr int Z = 2 * DIM;
+    constexpr int NW = V / 4;
+    int8_t* cur = a.arena + R.off[colour];
+    const int8_t* oth = a.arena + R.off[1 - colour];
+    const uint32_t w2 = ctr_word2(sweep, colour, P_ACCEPT);
+    for (int g = c_begin + lane; g < c_end; g += 32) {
+        const int r = (int)fdiv((uint32_t)g, R.m_cpr);
+        const int q = g - r * R.cpr;
+        const int z = (int)fdiv((uint32_t)r, R.m_Ly);
+        const int y = r - z * R.Ly;
+        const RowInfo ri = row_info_yz(y, z, R.Ly, R.Lz, colour, DIM);
+        Chunk<DIM, V> ch;
+        ch.load(cur, oth, R.W, r, q * V, ri);
+        const uint32_t c0 = (uint32_t)(((unsigned long long)r * R.W + q * V) >> 2);
+        uint32_t af = 0, au = 0, ai = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            uint32_t nbw[Z];
+#pragma unroll
+            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
+            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, (uint32_t)rep), a.k0, a.k1);
+            uint32_t fb;
+            if (T32) fb = ising_word32<Z, HB>(nbw, ch.own[w], rnd, (const uint32_t*)tab, af, au, ai);
+            else fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, (const unsigned long long*)tab, nacc, nup, isum);
+            ch.own[w] ^= fb * 0xFEu;
+        }
+        if (T32) {
+            nacc += hsum8(af);
+            nup += hsum8(au);
+            isum += hsum16(ai);
+        }
+        store_row<V>(cur + (long long)r * R.W + q * V, ch.own);
+    }
+}
+
+template <int DIM, bool HB, bool T32>
+__device__ __forceinline__ void pt_run_span(const PTArgs& a, const PTTile& sp, int colour, unsigned long long sweep,
+                                            long long* dcur, const void* thr, int lane) {
+    const PTReplica R = a.reps[sp.rep];
+    int nacc = 0, nup = 0, isum = 0;
+    if (R.V == 16) pt_span<DIM, 16, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    else if (R.V == 8) pt_span<DIM, 8, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    else pt_span<DIM, 4, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    constexpr int Z = 2 * DIM;
+    long long dP, dM;
+    ising_deltas<Z>(nacc, nup, isum, dP, dM);
+    long long v[3] = {dP, dM, (long long)nacc};
+    unsigned long long* const dst[3] = {(unsigned long long*)&dcur[2 * sp.rep],
+                                        (unsigned long long*)&dcur[2 * sp.rep + 1], &a.acc[sp.rep]};
+    warp_add_atomic<3>(v, dst);
 }
 
 // One tile with its acceptance table `thr` (shared memory); per-warp atomics.
@@ -255,8 +312,8 @@ __global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
     int stage = *a.stage;
     __syncthreads();
     unsigned gen = s_gen;
-    __shared__ unsigned s_ticket;
-    const unsigned ntiles = (unsigned)a.ntiles;
+    const int lane = threadIdx.x & 31;
+    const PTTile span = a.spans[blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)];  // this warp's share
     const size_t dsz = (size_t)a.nrep * 2;
     for (long long s = 0; s < a.nsweeps; ++s) {
         const unsigned long long t = a.sweep0 + (unsigned long long)s;
@@ -273,25 +330,12 @@ __global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
                 if (pt_pair_active(a, gp, stage, p, l)) logu[gp] = pt_exchange_logu(a, p, l, t);
             }
         for (int colour = 0; colour < 2; ++colour) {
-            // phase h = 2s + colour claims tiles from ticket counter h % 3; the counter of
-            // phase h + 1 was last used in phase h - 2 and is cleared now
-            const long long h = 2 * s + colour;
-            if (blockIdx.x == 0 && threadIdx.x == 0) a.claim[(h + 1) % 3] = 0u;
-            unsigned* ctr = a.claim + (h % 3);
-            if (threadIdx.x == 0) s_ticket = atomicAdd(ctr, 1u);
-            __syncthreads();
-            unsigned k = s_ticket;
-            while (k < ntiles) {
-                unsigned nk = 0;
-                if (threadIdx.x == 0) nk = atomicAdd(ctr, 1u);  // the next claim flies during this tile
-                const PTTile tl = a.tiles[a.order[k]];
-                const int gpos = a.reps[tl.rep].gpos0 + s_pos[tl.rep];
+            // every warp sweeps its own chunk range (static, balanced on the host), so
+            // the phase needs no block barrier and no claiming; one grid barrier ends it
+            if (span.c_end > span.c_begin) {
+                const int gpos = a.reps[span.rep].gpos0 + s_pos[span.rep];
                 const void* tab = T32 ? (const void*)(s_tab32 + (size_t)gpos * 16) : (const void*)(s_tab + (size_t)gpos * 16);
-                pt_run_tile<DIM, HB, T32>(a, tl, colour, t, dcur, tab);
-                __syncthreads();
-                if (threadIdx.x == 0) s_ticket = nk;
-                __syncthreads();
-                k = s_ticket;
+                pt_run_span<DIM, HB, T32>(a, span, colour, t, dcur, tab, lane);
             }
             if (!grid_sync(a.bar, gridDim.x, gen, a.spin_limit)) return;
         }
@@ -398,8 +442,7 @@ struct mcx_pt {
     int8_t* d_arena = nullptr;
     PTReplica* d_reps = nullptr;
     PTTile* d_tiles = nullptr;
-    int* d_order = nullptr;          // tiles in claiming order (largest first)
-    unsigned int* d_claim = nullptr; // per-phase tile tickets
+    PTTile* d_spans = nullptr;       // [grid * 8] warp chunk ranges of the persistent form
     int grid = 0;                    // persistent grid size
     unsigned long long* d_tables = nullptr;  // [3 algs][npos][16]
     uint32_t* d_tables32 = nullptr;          // [3 algs][npos][16], entry - 1
@@ -475,19 +518,46 @@ static size_t pt_smem_persistent(const mcx_pt* pt, bool t32) {
     return pt_smem(pt) + (size_t)pt->npos * 16 * (t32 ? 4 : 8);
 }
 
-// Claiming order of the persistent form: tiles sorted by estimated cost, largest
-// first (blocks then take tiles from a ticket counter, which balances the phase).
+// Warp spans of the persistent form: every warp of the grid sweeps one chunk range of
+// one replica per phase.  Replica r gets k_r warps, handed out one at a time to the
+// replica whose cost per warp is largest (costs per site: 1.0 for 16-site rows chunks,
+// 1.15 for 8, 1.4 for 4), and its chunks are split evenly among them.
 static mcx_status pt_schedule(mcx_pt* pt, int grid) {
-    std::vector<int> order(pt->tiles.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    auto cost = [&](int t) {
-        const PTTile& T = pt->tiles[t];
-        const int V = pt->reps[T.rep].V;
-        return (double)T.sites * (V == 16 ? 1.0 : (V == 8 ? 1.15 : 1.4));
-    };
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
-    MCX_CHECK(pt_upload(pt, &pt->d_order, order));
-    MCX_CHECK(pt_upload(pt, &pt->d_claim, std::vector<unsigned int>(3, 0u)));
+    const int nwarps = grid * 8;
+    const int R = pt->nrep;
+    if (nwarps < R) return fail(MCX_ERR_INVALID_ARG, "%d replicas need at least as many resident warps", R);
+    std::vector<double> cost(R);
+    std::vector<int> nch(R), k(R, 1);
+    std::priority_queue<std::pair<double, int>> heap;
+    for (int r = 0; r < R; ++r) {
+        const PTReplica& P = pt->reps[r];
+        nch[r] = P.cpr * P.rows;
+        cost[r] = (double)nch[r] * P.V * (P.V == 16 ? 1.0 : (P.V == 8 ? 1.15 : 1.4));
+        heap.push({cost[r], r});
+    }
+    for (int left = nwarps - R; left > 0 && !heap.empty();) {
+        const int r = heap.top().second;
+        heap.pop();
+        if (k[r] >= nch[r]) continue;  // one chunk per warp at most
+        ++k[r];
+        --left;
+        heap.push({cost[r] / k[r], r});
+    }
+    std::vector<PTTile> spans;
+    spans.reserve(nwarps);
+    for (int r = 0; r < R; ++r)
+        for (int j = 0; j < k[r]; ++j) {
+            PTTile t;
+            t.rep = r;
+            t.c_begin = (int)((long long)j * nch[r] / k[r]);
+            t.c_end = (int)((long long)(j + 1) * nch[r] / k[r]);
+            t.sites = (t.c_end - t.c_begin) * pt->reps[r].V;
+            spans.push_back(t);
+        }
+    PTTile idle;
+    std::memset(&idle, 0, sizeof(idle));
+    spans.resize(nwarps, idle);
+    MCX_CHECK(pt_upload(pt, &pt->d_spans, spans));
     pt->grid = grid;
     return MCX_OK;
 }
@@ -497,8 +567,7 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->arena = pt->d_arena;
     a->reps = pt->d_reps;
     a->tiles = pt->d_tiles;
-    a->order = pt->d_order;
-    a->claim = pt->d_claim;
+    a->spans = pt->d_spans;
     a->nrep = pt->nrep;
     a->ntiles = (int)pt->tiles.size();
     a->npos = pt->npos;
@@ -870,7 +939,6 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
         MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 6 * sizeof(long long), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar, 0, sizeof(unsigned int), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar + 2, 0, sizeof(unsigned int), ctx->stream));
-        MCX_CUDA(cudaMemsetAsync(pt->d_claim, 0, 3 * sizeof(unsigned int), ctx->stream));
         const PersistentFn fn = persistent_fn(pt->dim, hb, t32);
         void* args[] = {&a};
         MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem_persistent,
