@@ -289,7 +289,7 @@ __device__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long l
 }
 
 template <int DIM, bool HB, bool T32>
-__global__ void __launch_bounds__(256, 4) k_pt_persistent(const PTArgs a) {
+__global__ void __launch_bounds__(256, 2) k_pt_persistent(const PTArgs a) {
     extern __shared__ long long smem[];
     // [npos][16] tables (8 or 4 bytes per entry), then the per-replica state
     unsigned long long* s_tab = reinterpret_cast<unsigned long long*>(smem);

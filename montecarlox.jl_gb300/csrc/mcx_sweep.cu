@@ -22,7 +22,7 @@
 namespace mcx {
 
 template <int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(256, 4) k_ising_cb(const SweepArgs a) {
+__global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int NT = 2 * (Z + 1);
     constexpr int NW = V / 4;
