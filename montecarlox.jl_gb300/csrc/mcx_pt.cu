@@ -5,8 +5,9 @@
 //   PERSISTENT: one cooperative launch runs all sweeps of all replicas.  Every warp of
 //     the grid owns one chunk range of one replica (built on the host: warps are handed
 //     to replicas by cost, and a replica's chunks are split evenly among its warps), so
-//     a phase needs no block barrier and no atomic claiming.  A bounded grid barrier
-//     separates the two colours of a sweep and the sweep from the exchange; every
+//     a phase needs no block barrier and no atomic claiming.  Between the colours of
+//     a sweep a replica's warps wait only for one another (arrival counter); a
+//     bounded grid barrier separates the sweep from the exchange; every
 //     block then evaluates the (tiny) exchange step itself, so the new ladder
 //     positions need no further barrier.  Per-replica energy deltas are triple
 //     buffered so that one sweep's accumulation never meets another's reads.
@@ -41,6 +42,7 @@ struct PTReplica {
 
 struct PTTile {
     int rep, c_begin, c_end, sites;
+    int nw;  // persistent spans: warps sharing this replica
 };
 
 struct PTArgs {
@@ -64,6 +66,7 @@ struct PTArgs {
     unsigned long long* ex_acc;        // [npos]
     long long* series;                 // [nsweeps][nrep][2] or null
     unsigned int* bar;                 // count, generation, error
+    unsigned long long* repbar;        // [nrep] colour-0 arrivals of each replica's warps (persistent form)
     double* logu;                      // [2][npos] exchange log-uniforms (persistent form)
     double J, h;
     uint32_t k0, k1;
@@ -255,6 +258,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -329,15 +338,40 @@ __global__ void __launch_bounds__(256, 2) k_pt_persistent(const PTArgs a) {
                 int p, l;
                 if (pt_pair_active(a, gp, stage, p, l)) logu[gp] = pt_exchange_logu(a, p, l, t);
             }
+        bool ok = true;
         for (int colour = 0; colour < 2; ++colour) {
             // every warp sweeps its own chunk range (static, balanced on the host), so
-            // the phase needs no block barrier and no claiming; one grid barrier ends it
-            if (span.c_end > span.c_begin) {
+            // the phase needs no block barrier and no claiming
+            if (span.c_end > span.c_begin && ok) {
                 const int gpos = a.reps[span.rep].gpos0 + s_pos[span.rep];
                 const void* tab = T32 ? (const void*)(s_tab32 + (size_t)gpos * 16) : (const void*)(s_tab + (size_t)gpos * 16);
                 pt_run_span<DIM, HB, T32>(a, span, colour, t, dcur, tab, lane);
             }
-            if (!grid_sync(a.bar, gridDim.x, gen, a.spin_limit)) return;
+            if (colour == 0) {
+                // colour 1 of a replica needs only that replica's colour 0: its warps
+                // count their arrivals (bounded wait; a timeout flags the error that
+                // the grid barrier below reports)
+                if (span.c_end > span.c_begin) {
+                    __syncwarp();
+                    if (lane == 0) {
+                        __threadfence();
+                        atomicAdd(&a.repbar[span.rep], 1ull);
+                        const unsigned long long target = (unsigned long long)span.nw * (unsigned long long)(s + 1);
+                        long long n = 0;
+                        while (ld_acquire64(&a.repbar[span.rep]) < target) {
+                            if (ld_acquire(&a.bar[2]) != 0u || ++n > a.spin_limit) {
+                                atomicExch(&a.bar[2], 1u);
+                                ok = false;
+                                break;
+                            }
+                            __nanosleep(32);
+                        }
+                    }
+                    ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+                }
+            } else if (!grid_sync(a.bar, gridDim.x, gen, a.spin_limit)) {
+                return;
+            }
         }
         for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
             s_P[r] += dcur[2 * r];
@@ -461,6 +495,7 @@ struct mcx_pt {
     long long* d_series = nullptr;
     int64_t series_cap = 0;
     unsigned int* d_bar = nullptr;
+    unsigned long long* d_repbar = nullptr;  // [nrep] per-replica arrival counters (persistent form)
     double* d_logu = nullptr;
     int8_t* d_lin = nullptr;
     size_t lin_bytes = 0;
@@ -552,6 +587,7 @@ static mcx_status pt_schedule(mcx_pt* pt, int grid) {
             t.c_begin = (int)((long long)j * nch[r] / k[r]);
             t.c_end = (int)((long long)(j + 1) * nch[r] / k[r]);
             t.sites = (t.c_end - t.c_begin) * pt->reps[r].V;
+            t.nw = k[r];
             spans.push_back(t);
         }
     PTTile idle;
@@ -585,6 +621,7 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->ex_steps = pt->d_ex_steps;
     a->ex_acc = pt->d_ex_acc;
     a->bar = pt->d_bar;
+    a->repbar = pt->d_repbar;
     a->logu = pt->d_logu;
     a->J = pt->J;
     a->h = pt->h;
@@ -759,6 +796,7 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
         for (int c = 0; c < nchunks; c += per) {
             PTTile t;
             t.rep = r;
+            t.nw = 0;
             t.c_begin = c;
             t.c_end = std::min(nchunks, c + per);
             t.sites = (t.c_end - t.c_begin) * R.V;
@@ -812,6 +850,7 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
     run(pt_upload(pt, &pt->d_ex_steps, std::vector<unsigned long long>(pt->npos, 0)));
     run(pt_upload(pt, &pt->d_ex_acc, std::vector<unsigned long long>(pt->npos, 0)));
     run(pt_upload(pt, &pt->d_bar, std::vector<unsigned int>(4, 0)));
+    run(pt_upload(pt, &pt->d_repbar, std::vector<unsigned long long>(pt->nrep, 0ull)));
     run(pt_upload(pt, &pt->d_logu, std::vector<double>((size_t)2 * pt->npos, 0.0)));
     run(pt_alloc(pt, &p, pt->lin_bytes));
     pt->d_lin = (int8_t*)p;
@@ -939,6 +978,7 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
         MCX_CUDA(cudaMemsetAsync(pt->d_delta, 0, (size_t)pt->nrep * 6 * sizeof(long long), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar, 0, sizeof(unsigned int), ctx->stream));
         MCX_CUDA(cudaMemsetAsync(pt->d_bar + 2, 0, sizeof(unsigned int), ctx->stream));
+        MCX_CUDA(cudaMemsetAsync(pt->d_repbar, 0, (size_t)pt->nrep * sizeof(unsigned long long), ctx->stream));
         const PersistentFn fn = persistent_fn(pt->dim, hb, t32);
         void* args[] = {&a};
         MCX_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(pt->grid), dim3(256), args, smem_persistent,
