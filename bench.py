@@ -220,7 +220,7 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
         "persistent": per, "plain": out["plain"],
         "speedup_vs_plain": per["attempts_per_ns"] / out["plain"]["attempts_per_ns"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "alg_bytes_per_sweep": 3 * sites, "kernel": "k_pt_persistent<3,false>"},
+                     "alg_bytes_per_sweep": 3 * sites, "kernel": "k_pt_persistent<3,false,true>"},
         "exchange_acceptance": float(pt.acceptance_rate()),
     }
 
@@ -400,7 +400,7 @@ def run_mcx(args):
                    "parallelism": "replicas"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                     "kernel": "k_ising_cb<2,16,false>", "alg_bytes_per_launch": alg_bytes},
+                     "kernel": "k_ising_cb<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
         "gpu_launches": launches,
