@@ -225,6 +225,41 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
     }
 
 
+def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
+    """The headline workload on the 64-spins-per-word layout (same Philox stream, results
+    bit-identical to int8): device-timed, L2 flushed between steps."""
+    L = [L_SIDE, L_SIDE]
+    N = L_SIDE * L_SIDE
+    lat = mcx.Ising(L, layout="msc64", ctx=ctx)
+    mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+    alg = mcx.Metropolis(mcx.Philox(SEED), beta=BETA)
+    lib = mcx._lib.load()
+
+    def step():
+        rng = alg.rng._c()
+        mcx._check(lib.mcx_sweep(lat.handle, alg.ALG, BETA, mcx.C.byref(rng), sweeps_per_step, None, None))
+        alg.rng.counter = rng.counter
+
+    for _ in range(warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    lat.close()
+    return {"workload": "ising2d_L4096_metropolis_msc64", "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6),
+            "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2>",
+            "alg_bytes_per_launch": 1.5 * N / 8}
+
+
 def bench_flathist(torch, mcx, ctx, dev, nwalkers=512, L=1024):
     """Multicanonical production on 2-D Blume-Capel L=1024, J=1, D=1 (integer energies,
     4,194,305 bins of FP64 ln g and int64 H shared by the walkers): one sweep of
@@ -375,11 +410,12 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = None
+    pt_res = srv_res = fh_res = msc_res = None
     if not args.no_extras:
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
+        msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
     if rank != 0:
         return
     cpu = None
@@ -409,6 +445,7 @@ def run_mcx(args):
         "batched_pt": pt_res,
         "serving": srv_res,
         "flat_histogram": fh_res,
+        "msc64": msc_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -5,6 +5,7 @@
 // so results are bit-identical to the int8 kernels.
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
+#include "mcx_sweep.cuh"
 
 namespace mcx {
 
@@ -144,6 +145,113 @@ __global__ void __launch_bounds__(256) k_msc_cb(const MscArgs a) {
     block_add_atomic<3>(v, dst);
 }
 
+// Metropolis-type rule in rank form (no field): every class with at most Z/2 aligned
+// neighbours is always accepted, and the threshold t_k of a site with Z/2 + k aligned
+// neighbours is the same for both spin states and non-increasing in k.  Aligned
+// neighbours are counted bit-sliced (c0, c1, c2) for 64 sites at once; each site's
+// uniform is compared with the K = Z/2 thresholds into bit masks A_k (u < t_k), and the
+// flips are the always-class sites plus, per class k, the sites whose A_k bit is set.
+// Same Philox word per site as every other kernel, so results are bit-identical.
+template <int DIM>
+__global__ void __launch_bounds__(256, 2) k_msc_metro(const MscArgs a) {
+    constexpr int Z = 2 * DIM;
+    constexpr int K = Z / 2;
+    uint32_t tk[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) tk[k] = (uint32_t)a.thr[Z / 2 + 1 + k];  // < 2^32 for these classes
+    const int nwords = a.nw * a.rows;  // < 2^28 words (N <= 2^34 sites)
+    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
+    unsigned long long nacc = 0, asum = 0, nup = 0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < nwords; g += gridDim.x * blockDim.x) {
+        const int r = g / a.nw;
+        const int w = g - r * a.nw;
+        const int z = DIM == 3 ? r / a.Ly : 0;
+        const int y = r - z * a.Ly;
+        const int p = (y + z + a.colour) & 1;
+        const long long ryp = (y + 1 == a.Ly ? 0 : y + 1) + (long long)a.Ly * z;
+        const long long rym = (y == 0 ? a.Ly - 1 : y - 1) + (long long)a.Ly * z;
+        const unsigned long long own = a.cur[g];
+        unsigned long long al[Z];  // 1 where neighbour d is aligned with the site
+        const unsigned long long mid = a.oth[g];
+        al[0] = mid;
+        al[1] = a.oth[ryp * a.nw + w];
+        al[2] = a.oth[rym * a.nw + w];
+        if (p == 0) {
+            const unsigned long long prev = a.oth[(long long)r * a.nw + (w == 0 ? a.nw - 1 : w - 1)];
+            al[3] = (mid << 1) | (prev >> 63);
+        } else {
+            const unsigned long long next = a.oth[(long long)r * a.nw + (w == a.nw - 1 ? 0 : w + 1)];
+            al[3] = (mid >> 1) | (next << 63);
+        }
+        if constexpr (DIM == 3) {
+            const long long rzp = y + (long long)a.Ly * (z + 1 == a.Lz ? 0 : z + 1);
+            const long long rzm = y + (long long)a.Ly * (z == 0 ? a.Lz - 1 : z - 1);
+            al[4] = a.oth[rzp * a.nw + w];
+            al[5] = a.oth[rzm * a.nw + w];
+        }
+#pragma unroll
+        for (int d = 0; d < Z; ++d) al[d] = ~(al[d] ^ own);
+        unsigned long long c0, c1, c2;
+        count_bits<Z>(al, c0, c1, c2);
+        // class masks of Z/2 + k aligned neighbours, k = 1..K (the rest always flips)
+        unsigned long long m[K];
+        if constexpr (DIM == 2) {
+            m[0] = c0 & c1;  // 3 = 011
+            m[1] = c2;       // 4 = 100
+        } else {
+            m[0] = c2 & ~c1 & ~c0;  // 4 = 100
+            m[1] = c2 & c0;         // 5 = 101
+            m[2] = c2 & c1;         // 6 = 110
+        }
+        unsigned long long flip = ~c2;
+        if constexpr (DIM == 2) flip = ~(m[0] | m[1]);
+        // u < t_k for the 64 sites of the word (16 Philox blocks of four words)
+        uint32_t A[K][2];
+#pragma unroll
+        for (int k = 0; k < K; ++k) A[k][0] = A[k][1] = 0u;
+        const uint32_t cbase = (uint32_t)(((unsigned long long)r * a.W + 64ull * w) >> 2);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const uint4 rnd = philox10(make_uint4(cbase + q, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
+            const uint32_t us[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int j = 4 * q + b;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (us[b] < tk[k]) A[k][j >> 5] |= 1u << (j & 31);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            flip |= m[k] & (((unsigned long long)A[k][1] << 32) | A[k][0]);
+        a.cur[g] = own ^ flip;
+        nacc += __popcll(flip);
+        nup += __popcll(flip & own);
+        asum += __popcll(flip & c0) + 2ull * __popcll(flip & c1) + 4ull * __popcll(flip & c2);
+    }
+    long long v[3] = {2ll * Z * (long long)nacc - 4ll * (long long)asum, 2ll * (long long)nacc - 4ll * (long long)nup,
+                      (long long)nacc};
+    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
+    block_add_atomic<3>(v, dst);
+}
+
+// Whether a table has the rank form of k_msc_metro: always for <= Z/2 aligned
+// neighbours, equal for both spin states above, non-increasing in the aligned count.
+static bool msc_rank_form(const Table& t, int Z) {
+    const unsigned long long always = 1ull << 32;
+    for (int al = 0; al <= Z; ++al) {
+        const unsigned long long dn = t.thr[al], upv = t.thr[al + Z + 1];
+        if (al <= Z / 2) {
+            if (dn != always || upv != always) return false;
+        } else {
+            if (dn != upv || dn >= always) return false;
+            if (al > Z / 2 + 1 && dn > t.thr[al - 1]) return false;
+        }
+    }
+    return true;
+}
+
 static int grid_cap(const mcx_ctx* ctx, long long work) {
     long long g = (work + 255) / 256;
     const long long cap = (long long)ctx->num_sms * 8;
@@ -188,7 +296,11 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const 
     const bool hb = alg == MCX_HEATBATH;
     void (*fn)(const MscArgs) = lat->dim == 2 ? (hb ? k_msc_cb<2, true> : k_msc_cb<2, false>)
                                               : (hb ? k_msc_cb<3, true> : k_msc_cb<3, false>);
-    const int grid = grid_cap(ctx, (long long)a.nw * a.rows);
+    int grid = grid_cap(ctx, (long long)a.nw * a.rows);
+    if (!hb && msc_rank_form(t, 2 * lat->dim)) {
+        fn = lat->dim == 2 ? k_msc_metro<2> : k_msc_metro<3>;
+        grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 256, 0);  // one wave
+    }
     for (int64_t s = 0; s < nsweeps; ++s) {
         a.sweep = rng->counter + (uint64_t)s;
         for (int c = 0; c < 2; ++c) {

@@ -88,6 +88,16 @@ def test_msc64_matches_int8_and_oracle(gpu, L, alg):
     assert np.array_equal(sys_.spins, s)
 
 
+@pytest.mark.parametrize("L,beta,h", [([128, 16, 8], 0.22, 0.0), ([256, 32], 0.5, 0.25), ([128, 64], 3.0, 0.0)])
+def test_msc64_metropolis_forms(gpu, L, beta, h):
+    """MSC64 Metropolis: the rank-form kernel (no field; also with thresholds of 0 at large
+    beta) and the general kernel (field) against the oracle."""
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.ISING, L, "metropolis", beta, h=h, layout="msc64")
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.accepted == acc
+
+
 def test_l4096_two_sweeps_bit_exact(gpu):
     """configs: 2-D L=4096, seed 7, Metropolis at beta 0.4407, int8 and MSC64."""
     L = [4096, 4096]
