@@ -719,14 +719,18 @@ __global__ void k_add_hist(unsigned long long* dst, const unsigned long long* sr
         dst[b] += src[b];
 }
 
-mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers) {
+mcx_status launch_flathist_on(mcx_ctx* ctx, cudaStream_t stream, FHWalker* d_walkers, int nwalkers) {
     FHArgs a;
     a.walkers = d_walkers;
     a.nwalkers = nwalkers;
-    k_flathist<<<nwalkers, 64, 0, ctx->stream>>>(a);
+    k_flathist<<<nwalkers, 64, 0, stream>>>(a);
     count_launch(ctx);
     MCX_CUDA(cudaGetLastError());
     return MCX_OK;
+}
+
+mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers) {
+    return launch_flathist_on(ctx, ctx->stream, d_walkers, nwalkers);
 }
 
 bool fh_window_ok(int dim, long long J, long long D, long long h, long long step) {

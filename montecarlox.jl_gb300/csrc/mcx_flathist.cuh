@@ -49,8 +49,10 @@ struct FHArgs {
     int nwalkers;
 };
 
-// Enqueue one flat-histogram launch over `nwalkers` device walker descriptors.
+// Enqueue one flat-histogram launch over `nwalkers` device walker descriptors (on the
+// context's stream, or on `stream`).
 mcx_status launch_flathist(mcx_ctx* ctx, FHWalker* d_walkers, int nwalkers);
+mcx_status launch_flathist_on(mcx_ctx* ctx, cudaStream_t stream, FHWalker* d_walkers, int nwalkers);
 int fh_shift(long long step);
 // whether one move's energy change stays well inside the walker's ln g window
 bool fh_window_ok(int dim, long long J, long long D, long long h, long long step);

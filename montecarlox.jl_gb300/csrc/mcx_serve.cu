@@ -21,6 +21,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <thread>
 #include <vector>
 
 #include "mcx_cb.cuh"
@@ -155,6 +156,8 @@ struct SrvJob {
     mcx_status status = MCX_OK;
     uint64_t bytes = 0;
     Table table{};
+    int inflight = 0;       // sweeps of the Multicanonical launch in flight (0: none)
+    bool cancel_req = false;
 };
 
 double now_s(std::chrono::steady_clock::time_point t0) {
@@ -183,6 +186,14 @@ struct mcx_server {
     FHWalker* d_walkers = nullptr;
     size_t cap_walkers = 0;
     uint64_t iterations = 0, jobs_done = 0, attempts_done = 0;
+    // Multicanonical jobs run on their own stream, one launch in flight at a time, so
+    // that canonical jobs never wait for the (serial, long) walker chains
+    cudaStream_t mstream = nullptr;
+    cudaEvent_t mdone = nullptr;
+    bool minflight = false;
+    std::vector<FHWalker> mwalk;
+    std::vector<SrvJob*> mjobs;
+    std::vector<SrvJob*> deferred;  // finished jobs whose memory is freed when no walker launch runs
 };
 
 namespace {
@@ -306,7 +317,111 @@ mcx_status finish(mcx_server* s, SrvJob* j) {
     j->state = j->status == MCX_OK ? JOB_DONE : JOB_FAILED;
     s->jobs_done += 1;
     s->attempts_done += j->steps;
-    release(s, j);
+    // freeing synchronises the device, which would wait for a walker launch in flight
+    if (s->minflight) s->deferred.push_back(j);
+    else release(s, j);
+    return MCX_OK;
+}
+
+// Results of the walker launch in flight, when it has completed: job bookkeeping,
+// completion of finished (or cancelled) jobs.  Returns MCX_OK while it still runs.
+mcx_status collect_muca(mcx_server* s) {
+    if (!s->minflight) return MCX_OK;
+    const cudaError_t q = cudaEventQuery(s->mdone);
+    if (q == cudaErrorNotReady) return MCX_OK;
+    if (q != cudaSuccess) return cuda_fail(q, "walker launch");
+    MCX_CUDA(cudaMemcpy(s->mwalk.data(), s->d_walkers, s->mwalk.size() * sizeof(FHWalker), cudaMemcpyDeviceToHost));
+    s->minflight = false;
+    for (size_t i = 0; i < s->mjobs.size(); ++i) {
+        SrvJob* j = s->mjobs[i];
+        const FHWalker& w = s->mwalk[i];
+        j->P = w.P;
+        j->M = w.M;
+        j->Q = w.Q;
+        j->steps += w.steps;
+        j->accepted += w.accepted;
+        j->done += j->inflight;
+        j->inflight = 0;
+        if (w.status) {
+            j->status = MCX_ERR_OUT_OF_RANGE;
+            j->done = j->spec.nsweeps;  // stops here, like the reference's BoundsError
+        }
+        long long st[3] = {j->P, j->M, j->Q};
+        MCX_CUDA(cudaMemcpy(j->lat->d_state, st, 24, cudaMemcpyHostToDevice));
+    }
+    std::vector<SrvJob*> still;
+    for (SrvJob* j : s->active) {
+        if (j->spec.kind == MCX_JOB_CANONICAL) {
+            still.push_back(j);
+        } else if (j->cancel_req) {
+            j->state = JOB_CANCELLED;
+            j->t_finish = now_s(s->t0);
+            release(s, j);
+        } else if (j->done >= j->spec.nsweeps) {
+            MCX_CHECK(finish(s, j));
+        } else {
+            still.push_back(j);
+        }
+    }
+    s->active.swap(still);
+    s->mjobs.clear();
+    return MCX_OK;
+}
+
+// Starts one walker launch (chunk sweeps) for every active Multicanonical job.
+mcx_status launch_muca(mcx_server* s) {
+    if (s->minflight) return MCX_OK;
+    s->mwalk.clear();
+    s->mjobs.clear();
+    for (SrvJob* j : s->active) {
+        if (j->spec.kind != MCX_JOB_MULTICANONICAL || j->done >= j->spec.nsweeps) continue;
+        const int todo = (int)std::min<int64_t>(s->chunk, j->spec.nsweeps - j->done);
+        const mcx_lattice* L = j->lat;
+        FHWalker w;
+        std::memset(&w, 0, sizeof(w));
+        w.g.W = (int)L->W;
+        w.g.Ly = (int)L->L[1];
+        w.g.Lz = 1;
+        w.g.dim = 2;
+        w.g.model = L->model == MCX_ISING ? 0 : 1;
+        w.g.J = (long long)L->J;
+        w.g.D = (long long)L->D;
+        w.g.h = (long long)L->h;
+        w.g.start = j->spec.bin_start;
+        w.g.step = j->spec.bin_step;
+        w.g.nbins = j->spec.nbins;
+        w.g.shift = fh_shift(j->spec.bin_step);
+        w.g.mode = 0;
+        w.g.nsweeps = todo;
+        w.col[0] = L->d_col[0];
+        w.col[1] = L->d_col[1];
+        w.lnw = j->fh->d_lnw;
+        w.H = j->fh->d_H;
+        w.series = (long long*)L->d_series + 3 * j->done;
+        w.P = j->P;
+        w.M = j->M;
+        w.Q = j->Q;
+        w.sweep0 = (unsigned long long)j->done;
+        w.k0 = (uint32_t)j->spec.seed;
+        w.k1 = (uint32_t)(j->spec.seed >> 32);
+        w.stream = j->spec.stream;
+        j->inflight = todo;
+        s->mwalk.push_back(w);
+        s->mjobs.push_back(j);
+    }
+    if (s->mjobs.empty()) return MCX_OK;
+    if (!s->mstream) {
+        MCX_CUDA(cudaStreamCreateWithFlags(&s->mstream, cudaStreamNonBlocking));
+        MCX_CUDA(cudaEventCreateWithFlags(&s->mdone, cudaEventDisableTiming));
+    }
+    // the walkers' lattices were initialised on the context stream
+    MCX_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    MCX_CHECK(grow(s, &s->d_walkers, &s->cap_walkers, s->mwalk.size()));
+    MCX_CUDA(cudaMemcpyAsync(s->d_walkers, s->mwalk.data(), s->mwalk.size() * sizeof(FHWalker), cudaMemcpyHostToDevice,
+                             s->mstream));
+    MCX_CHECK(launch_flathist_on(s->ctx, s->mstream, s->d_walkers, (int)s->mwalk.size()));
+    MCX_CUDA(cudaEventRecord(s->mdone, s->mstream));
+    s->minflight = true;
     return MCX_OK;
 }
 
@@ -328,127 +443,81 @@ mcx_status step(mcx_server* s) {
         }
         s->active.push_back(j);
     }
-    if (s->active.empty()) return MCX_OK;
-    // 2. one chunk for every active job
+    // 2. Multicanonical jobs: collect a completed walker launch, free deferred memory
+    //    while nothing runs on the walker stream, start the next launch
+    MCX_CHECK(collect_muca(s));
+    if (!s->minflight) {
+        for (SrvJob* j : s->deferred) release(s, j);
+        s->deferred.clear();
+    }
+    MCX_CHECK(launch_muca(s));
+    // 3. one chunk for every active canonical job
     std::vector<SrvJobDev> jd;
     std::vector<SrvTile> tiles;
     std::vector<unsigned long long> tabs;
-    std::vector<FHWalker> walkers;
-    std::vector<SrvJob*> canon, muca;
+    std::vector<SrvJob*> canon;
     int chunk = 0;
     for (SrvJob* j : s->active) {
+        if (j->spec.kind != MCX_JOB_CANONICAL) continue;
         const int todo = (int)std::min<int64_t>(s->chunk, j->spec.nsweeps - j->done);
         chunk = std::max(chunk, todo);
-        if (j->spec.kind == MCX_JOB_CANONICAL) {
-            const mcx_lattice* L = j->lat;
-            SrvJobDev d;
-            std::memset(&d, 0, sizeof(d));
-            d.col[0] = L->d_col[0];
-            d.col[1] = L->d_col[1];
-            d.series = (long long*)L->d_series + 3 * j->done;
-            d.acc = L->d_acc;
-            d.W = (int)L->W;
-            d.Ly = (int)L->L[1];
-            d.rows = (int)L->rows;
-            d.V = L->W % 16 == 0 ? 16 : (L->W % 8 == 0 ? 8 : 4);
-            d.cpr = d.W / d.V;
-            d.model = L->model == MCX_ISING ? 0 : 1;
-            d.hb = j->spec.alg == MCX_HEATBATH;
-            d.todo = todo;
-            d.k0 = (uint32_t)j->spec.seed;
-            d.k1 = (uint32_t)(j->spec.seed >> 32);
-            d.stream = j->spec.stream;
-            d.m_cpr = d.cpr <= 1 ? 0u : (uint32_t)(((1ull << 32) + d.cpr - 1) / d.cpr);
-            d.t0 = (unsigned long long)j->done;
-            const int idx = (int)jd.size();
-            jd.push_back(d);
-            for (int i = 0; i < kMaxTable; ++i) tabs.push_back(i < j->table.n ? j->table.thr[i] : 0ull);
-            const int nch = d.cpr * d.rows, per = 256 * (16 / d.V);
-            for (int c = 0; c < nch; c += per) tiles.push_back(SrvTile{idx, c, std::min(nch, c + per), 0});
-            canon.push_back(j);
-        } else {
-            const mcx_lattice* L = j->lat;
-            FHWalker w;
-            std::memset(&w, 0, sizeof(w));
-            w.g.W = (int)L->W;
-            w.g.Ly = (int)L->L[1];
-            w.g.Lz = 1;
-            w.g.dim = 2;
-            w.g.model = L->model == MCX_ISING ? 0 : 1;
-            w.g.J = (long long)L->J;
-            w.g.D = (long long)L->D;
-            w.g.h = (long long)L->h;
-            w.g.start = j->spec.bin_start;
-            w.g.step = j->spec.bin_step;
-            w.g.nbins = j->spec.nbins;
-            w.g.shift = fh_shift(j->spec.bin_step);
-            w.g.mode = 0;
-            w.g.nsweeps = todo;
-            w.col[0] = L->d_col[0];
-            w.col[1] = L->d_col[1];
-            w.lnw = j->fh->d_lnw;
-            w.H = j->fh->d_H;
-            w.series = (long long*)L->d_series + 3 * j->done;
-            w.P = j->P;
-            w.M = j->M;
-            w.Q = j->Q;
-            w.sweep0 = (unsigned long long)j->done;
-            w.k0 = (uint32_t)j->spec.seed;
-            w.k1 = (uint32_t)(j->spec.seed >> 32);
-            w.stream = j->spec.stream;
-            walkers.push_back(w);
-            muca.push_back(j);
-        }
+        const mcx_lattice* L = j->lat;
+        SrvJobDev d;
+        std::memset(&d, 0, sizeof(d));
+        d.col[0] = L->d_col[0];
+        d.col[1] = L->d_col[1];
+        d.series = (long long*)L->d_series + 3 * j->done;
+        d.acc = L->d_acc;
+        d.W = (int)L->W;
+        d.Ly = (int)L->L[1];
+        d.rows = (int)L->rows;
+        d.V = L->W % 16 == 0 ? 16 : (L->W % 8 == 0 ? 8 : 4);
+        d.cpr = d.W / d.V;
+        d.model = L->model == MCX_ISING ? 0 : 1;
+        d.hb = j->spec.alg == MCX_HEATBATH;
+        d.todo = todo;
+        d.k0 = (uint32_t)j->spec.seed;
+        d.k1 = (uint32_t)(j->spec.seed >> 32);
+        d.stream = j->spec.stream;
+        d.m_cpr = d.cpr <= 1 ? 0u : (uint32_t)(((1ull << 32) + d.cpr - 1) / d.cpr);
+        d.t0 = (unsigned long long)j->done;
+        const int idx = (int)jd.size();
+        jd.push_back(d);
+        for (int i = 0; i < kMaxTable; ++i) tabs.push_back(i < j->table.n ? j->table.thr[i] : 0ull);
+        const int nch = d.cpr * d.rows, per = 256 * (16 / d.V);
+        for (int c = 0; c < nch; c += per) tiles.push_back(SrvTile{idx, c, std::min(nch, c + per), 0});
+        canon.push_back(j);
     }
-    if (!canon.empty()) {
-        MCX_CHECK(grow(s, &s->d_jobs, &s->cap_jobs, jd.size()));
-        MCX_CHECK(grow(s, &s->d_tiles, &s->cap_tiles, tiles.size()));
-        MCX_CHECK(grow(s, &s->d_tables, &s->cap_tables, tabs.size()));
-        MCX_CUDA(cudaMemcpyAsync(s->d_jobs, jd.data(), jd.size() * sizeof(SrvJobDev), cudaMemcpyHostToDevice, ctx->stream));
-        MCX_CUDA(cudaMemcpyAsync(s->d_tiles, tiles.data(), tiles.size() * sizeof(SrvTile), cudaMemcpyHostToDevice,
-                                 ctx->stream));
-        MCX_CUDA(cudaMemcpyAsync(s->d_tables, tabs.data(), tabs.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
-        const int grid = occupancy_grid(ctx, (const void*)k_srv_half, (long long)tiles.size() * 256, 256, 0);
-        for (int sw = 0; sw < chunk; ++sw)
-            for (int c = 0; c < 2; ++c)
-                k_srv_half<<<grid, 256, 0, ctx->stream>>>(s->d_jobs, s->d_tiles, (int)tiles.size(), s->d_tables, c, sw);
-        count_launch(ctx, 2 * (uint64_t)chunk);
-        MCX_CUDA(cudaGetLastError());
+    if (canon.empty()) {
+        if (s->minflight) std::this_thread::sleep_for(std::chrono::microseconds(50));  // walkers only: do not spin
+        return MCX_OK;
     }
-    if (!muca.empty()) {
-        MCX_CHECK(grow(s, &s->d_walkers, &s->cap_walkers, walkers.size()));
-        MCX_CUDA(cudaMemcpyAsync(s->d_walkers, walkers.data(), walkers.size() * sizeof(FHWalker), cudaMemcpyHostToDevice,
-                                 ctx->stream));
-        MCX_CHECK(launch_flathist(ctx, s->d_walkers, (int)walkers.size()));
-        MCX_CUDA(cudaMemcpyAsync(walkers.data(), s->d_walkers, walkers.size() * sizeof(FHWalker), cudaMemcpyDeviceToHost,
-                                 ctx->stream));
-    }
+    MCX_CHECK(grow(s, &s->d_jobs, &s->cap_jobs, jd.size()));
+    MCX_CHECK(grow(s, &s->d_tiles, &s->cap_tiles, tiles.size()));
+    MCX_CHECK(grow(s, &s->d_tables, &s->cap_tables, tabs.size()));
+    MCX_CUDA(cudaMemcpyAsync(s->d_jobs, jd.data(), jd.size() * sizeof(SrvJobDev), cudaMemcpyHostToDevice, ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(s->d_tiles, tiles.data(), tiles.size() * sizeof(SrvTile), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(s->d_tables, tabs.data(), tabs.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    const int grid = occupancy_grid(ctx, (const void*)k_srv_half, (long long)tiles.size() * 256, 256, 0);
+    for (int sw = 0; sw < chunk; ++sw)
+        for (int c = 0; c < 2; ++c)
+            k_srv_half<<<grid, 256, 0, ctx->stream>>>(s->d_jobs, s->d_tiles, (int)tiles.size(), s->d_tables, c, sw);
+    count_launch(ctx, 2 * (uint64_t)chunk);
+    MCX_CUDA(cudaGetLastError());
     MCX_CUDA(cudaStreamSynchronize(ctx->stream));
     s->iterations += 1;
-    for (size_t i = 0; i < muca.size(); ++i) {
-        SrvJob* j = muca[i];
-        const FHWalker& w = walkers[i];
-        j->P = w.P;
-        j->M = w.M;
-        j->Q = w.Q;
-        j->steps += w.steps;
-        j->accepted += w.accepted;
-        if (w.status) {
-            j->status = MCX_ERR_OUT_OF_RANGE;
-            j->done = j->spec.nsweeps;  // stops here, like the reference's BoundsError
-        }
-        long long st[3] = {j->P, j->M, j->Q};
-        MCX_CUDA(cudaMemcpyAsync(j->lat->d_state, st, 24, cudaMemcpyHostToDevice, ctx->stream));
-    }
-    // 3. progress and retirement
+    // 4. progress and retirement of the canonical jobs
     std::vector<SrvJob*> still;
     for (SrvJob* j : s->active) {
-        if (j->status == MCX_OK) j->done += std::min<int64_t>(s->chunk, j->spec.nsweeps - j->done);
-        if (j->done >= j->spec.nsweeps) {
-            MCX_CHECK(finish(s, j));
-        } else {
-            still.push_back(j);
+        if (j->spec.kind == MCX_JOB_CANONICAL) {
+            j->done += std::min<int64_t>(s->chunk, j->spec.nsweeps - j->done);
+            if (j->done >= j->spec.nsweeps) {
+                MCX_CHECK(finish(s, j));
+                continue;
+            }
         }
+        still.push_back(j);
     }
     s->active.swap(still);
     return MCX_OK;
@@ -476,6 +545,8 @@ MCX_API mcx_status mcx_server_create(mcx_ctx* ctx, uint64_t hbm_budget, int32_t 
 MCX_API mcx_status mcx_server_destroy(mcx_server* s) {
     if (!s) return MCX_OK;
     cudaStreamSynchronize(s->ctx->stream);
+    if (s->mstream) cudaStreamSynchronize(s->mstream);
+    s->minflight = false;
     for (auto& kv : s->jobs) {
         if (kv.second->lat || kv.second->fh) release(s, kv.second);
         delete kv.second;
@@ -484,6 +555,8 @@ MCX_API mcx_status mcx_server_destroy(mcx_server* s) {
     dev_free(s->ctx, s->d_tiles, s->cap_tiles * sizeof(SrvTile));
     dev_free(s->ctx, s->d_tables, s->cap_tables * 8);
     dev_free(s->ctx, s->d_walkers, s->cap_walkers * sizeof(FHWalker));
+    if (s->mdone) cudaEventDestroy(s->mdone);
+    if (s->mstream) cudaStreamDestroy(s->mstream);
     delete s;
     return MCX_OK;
 }
@@ -546,9 +619,14 @@ MCX_API mcx_status mcx_server_cancel(mcx_server* s, uint64_t job_id) {
     if (j->state == JOB_PENDING) {
         s->pending.erase(std::find(s->pending.begin(), s->pending.end(), j));
     } else if (j->state == JOB_ACTIVE) {
+        if (j->inflight) {  // its walker launch is running: cancelled when it completes
+            j->cancel_req = true;
+            return MCX_OK;
+        }
         MCX_CUDA(cudaStreamSynchronize(s->ctx->stream));
         s->active.erase(std::find(s->active.begin(), s->active.end(), j));
-        release(s, j);
+        if (s->minflight) s->deferred.push_back(j);
+        else release(s, j);
     } else {
         return MCX_OK;
     }
