@@ -232,46 +232,81 @@ inline bool ising_table_fits32(const uint64_t* thr, int n, int Z, bool hb) {
     return true;
 }
 
-// Blume-Capel decision for the four sites of one word (bytes 0xFF, 0x00, 0x01).
-// Neighbour sums per byte S = c + Z from (v + 1) per neighbour word.  Metropolis /
-// Glauber: proposal bit from the top bit of the proposal word (the reference's
-// rand(rng, Bool)), table entry (s_old+1)*2*NC + bit*NC + S.  Heat bath: cumulative
-// thresholds (T1, T12) at 2S, 2S+1.  Returns the new word.
+// Byte-lane counters of a chunk of Blume-Capel words (at most four words: every lane
+// stays below 256): plus1 of the new and old spins, their squares, and plus1 times the
+// neighbour count cnt = S + Z.
+struct BcLanes {
+    uint32_t pn = 0, po = 0, qn = 0, qo = 0, cn = 0, co = 0;
+};
+
+// Blume-Capel decision for the four sites of one word without per-site branches.
+// Metropolis / Glauber: proposal bits from the top bits of the proposal words (the
+// reference's rand(rng, Bool)), table entry (s_old+1)*2*NC + bit*NC + S formed
+// byte-parallel, one 64-bit threshold compare per site, the proposed spins and the
+// accepted bytes merged with byte masks.  Heat bath: sn = -1 + [u >= T1] + [u >= T12]
+// per site from the cumulative thresholds at 2S, 2S+1.  Returns the new word; counts
+// changed sites into nacc and the observable deltas into the byte lanes.
 template <int Z, bool HB>
-__device__ __forceinline__ uint32_t bc_word(const uint32_t (&nbw)[Z], uint32_t word, uint4 ra, uint4 rp,
-                                            const unsigned long long* s_thr, int& nacc, int& dP, int& dM,
-                                            int& dQ) {
+__device__ __forceinline__ uint32_t bc_word_swar(const uint32_t (&nbw)[Z], uint32_t own, uint4 ra, uint4 rp,
+                                                 const unsigned long long* s_thr, int& nacc, BcLanes& ln) {
     constexpr int NC = 2 * Z + 1;
     uint32_t cnt = 0;
 #pragma unroll
     for (int d = 0; d < Z; ++d) cnt += plus1(nbw[d]);
+    const uint32_t po = plus1(own);
     const uint32_t ua[4] = {ra.x, ra.y, ra.z, ra.w};
-    const uint32_t up[4] = {rp.x, rp.y, rp.z, rp.w};
+    const char* tb = reinterpret_cast<const char*>(s_thr);  // 16-byte aligned
+    uint32_t nw;
+    if (HB) {
+        nw = 0;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const int S = (cnt >> (8 * b)) & 0xFF;
-        const int so = (int)(int8_t)(word >> (8 * b));
-        const uint32_t u = ua[b];
-        int sn;
-        bool acc;
-        if (HB) {
-            sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
-            acc = sn != so;
-        } else {
-            const int bit = (int)(up[b] >> 31);
-            acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
-            sn = bc_propose(so, bit);
+        for (int b = 0; b < 4; ++b) {
+            const uint32_t S = __byte_perm(cnt, 0u, 0x4440u + b);
+            const ulonglong2 t = *reinterpret_cast<const ulonglong2*>(tb + 16u * S);  // (T1, T12) at 2S
+            const uint32_t c = (uint32_t)((unsigned long long)ua[b] >= t.x) + (uint32_t)((unsigned long long)ua[b] >= t.y);
+            nw |= ((c + 0xFFu) & 0xFFu) << (8 * b);
         }
-        if (acc) {
-            const int ds = sn - so;
-            word = (word & ~(0xFFu << (8 * b))) | ((uint32_t)(uint8_t)(int8_t)sn << (8 * b));
-            ++nacc;
-            dP += ds * (S - Z);
-            dM += ds;
-            dQ += sn * sn - so * so;
+    } else {
+        // proposal bits (top bit of each proposal word) as bytes 0/1, and as 0x00/0xFF masks
+        const uint32_t txy = __byte_perm(rp.x, rp.y, 0x0073u);  // bytes 0, 1: top bytes of x, y
+        const uint32_t tzw = __byte_perm(rp.z, rp.w, 0x0073u);
+        const uint32_t bits = (__byte_perm(txy, tzw, 0x5410u) >> 7) & 0x01010101u;
+        const uint32_t bm = bits * 0xFFu;
+        const uint32_t idx = po * (uint32_t)(2 * NC) + bits * (uint32_t)NC + cnt;  // bytes <= 77
+        uint32_t f = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const uint32_t e = __byte_perm(idx, 0u, 0x4440u + b);
+            if ((unsigned long long)ua[b] < s_thr[e]) f |= 1u << (8 * b);
         }
+        const uint32_t am = f * 0xFFu;
+        // proposals: bit 0 -> +1 unless the spin is +1 (then 0); bit 1 -> -1 unless it is -1 (then 0)
+        const uint32_t is1 = (po >> 1) & 0x01010101u;            // s_old = +1
+        const uint32_t ism1 = ~(po | (po >> 1)) & 0x01010101u;  // s_old = -1
+        const uint32_t sn0 = 0x01010101u - is1;                  // bytes 0x01 or 0x00
+        const uint32_t sn1 = (ism1 ^ 0x01010101u) * 0xFFu;       // bytes 0xFF or 0x00
+        const uint32_t sn = (sn1 & bm) | (sn0 & ~bm);
+        nw = (sn & am) | (own & ~am);
     }
-    return word;
+    const uint32_t x = nw ^ own;  // changed bytes
+    nacc += __popc((((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u);
+    const uint32_t pn = plus1(nw);
+    ln.pn += pn;
+    ln.po += po;
+    ln.qn += nw & 0x01010101u;
+    ln.qo += own & 0x01010101u;
+    ln.cn += (cnt & ((pn & 0x01010101u) * 0xFFu)) + ((cnt & (((pn >> 1) & 0x01010101u) * 0xFFu)) << 1);
+    ln.co += (cnt & ((po & 0x01010101u) * 0xFFu)) + ((cnt & (((po >> 1) & 0x01010101u) * 0xFFu)) << 1);
+    return nw;
+}
+
+// Folds a chunk's Blume-Capel byte lanes into (pair, spin, spin2) deltas.
+template <int Z>
+__device__ __forceinline__ void bc_lanes_fold(const BcLanes& ln, int& dP, int& dM, int& dQ) {
+    const int m = hsum8(ln.pn) - hsum8(ln.po);
+    dM += m;
+    dQ += hsum8(ln.qn) - hsum8(ln.qo);
+    dP += (hsum16(ln.cn) - hsum16(ln.co)) - Z * m;
 }
 
 // (pair, spin) deltas of a block of Ising flips from the word accumulators

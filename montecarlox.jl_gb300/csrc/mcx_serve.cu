@@ -62,6 +62,7 @@ __device__ __forceinline__ void srv_tile(const SrvJobDev& J, const SrvTile& tl, 
         Chunk<2, V> ch;
         ch.load(cur, oth, J.W, r, q * V, ri);
         const uint32_t c0 = (uint32_t)(((unsigned long long)r * J.W + q * V) >> 2);
+        BcLanes ln;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
             uint32_t nbw[Z];
@@ -74,13 +75,10 @@ __device__ __forceinline__ void srv_tile(const SrvJobDev& J, const SrvTile& tl, 
             } else {
                 uint4 rp = make_uint4(0, 0, 0, 0);
                 if (!HB) rp = philox10(make_uint4(c0 + w, (uint32_t)t, w2p, J.stream), J.k0, J.k1);
-                int dP = 0, dM = 0, dQ = 0;
-                ch.own[w] = bc_word<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, dP, dM, dQ);
-                a1 += dP;
-                a2 += dM;
-                a3 += dQ;
+                ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, ln);
             }
         }
+        if (MODEL != 0) bc_lanes_fold<Z>(ln, a1, a2, a3);
         store_row<V>(cur + (long long)r * J.W + q * V, ch.own);
     }
 }
@@ -89,7 +87,7 @@ __device__ __forceinline__ void srv_tile(const SrvJobDev& J, const SrvTile& tl, 
 // canonical job (tiles of jobs with fewer than s+1 sweeps left are skipped).
 __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const SrvTile* tiles, int ntiles,
                                                   const unsigned long long* tables, int colour, int s) {
-    __shared__ unsigned long long s_thr[kMaxTable];
+    __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
         const SrvTile tl = tiles[ti];
         const SrvJobDev J = jobs[tl.job];

@@ -114,12 +114,12 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
 
 // ------------------------------------------------------------ Blume-Capel --
 template <int DIM, int V, bool HB>
-__global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
+__global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int NC = 2 * Z + 1;
     constexpr int NT = HB ? 2 * NC : 6 * NC;
     constexpr int NW = V / 4;
-    __shared__ unsigned long long s_thr[NT];
+    __shared__ __align__(16) unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
     const SweepKey key = sweep_key(a);
@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
         const unsigned long long j0 = (unsigned long long)r * a.W + k0;
+        BcLanes ln;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
             uint32_t nbw[Z];
@@ -146,9 +147,9 @@ __global__ void __launch_bounds__(256, 3) k_bc_cb(const SweepArgs a) {
             const uint4 ra = philox10(make_uint4(c0, (uint32_t)sweep, w2a, key.stream), key.k0, key.k1);
             uint4 rp = make_uint4(0, 0, 0, 0);
             if (!HB) rp = philox10(make_uint4(c0, (uint32_t)sweep, w2p, key.stream), key.k0, key.k1);
-            const uint32_t word = bc_word<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, dP, dM, dQ);
-            ch.own[w] = word;
+            ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, ln);
         }
+        bc_lanes_fold<Z>(ln, dP, dM, dQ);
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
     long long v[4] = {dP, dM, dQ, nacc};
