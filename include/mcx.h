@@ -94,6 +94,7 @@ typedef struct mcx_lattice mcx_lattice;
 typedef struct mcx_flathist mcx_flathist;
 typedef struct mcx_pt mcx_pt;
 typedef struct mcx_server mcx_server;
+typedef struct mcx_graph mcx_graph;
 
 /* ---------------------------------------------------------------- errors -- */
 MCX_API const char* mcx_status_string(mcx_status status);
@@ -324,6 +325,64 @@ MCX_API mcx_status mcx_server_step(mcx_server* server, int32_t* active, int32_t*
 MCX_API mcx_status mcx_server_poll(mcx_server* server, uint64_t job_id, mcx_job_result* result);
 MCX_API mcx_status mcx_server_cancel(mcx_server* server, uint64_t job_id);
 MCX_API mcx_status mcx_server_get_stats(mcx_server* server, mcx_server_stats* stats);
+
+/* ------------------------------------------------------- general graphs -- */
+/* Ising models on an arbitrary neighbour list: IsingGraph (one coupling J over a graph,
+ * SpinSystems/src/ising.jl:86-139) and IsingMatrix (a symmetric sparse coupling
+ * matrix J_ij, ising.jl:221-292, also what Ising(graph, Jvec) builds, :391-411), each
+ * with no field, a uniform field h or a field per site (h::Vector).
+ *   n:        number of sites (vertices), 0-based.
+ *   rowptr:   int64[n+1], col: int32[rowptr[n]] -- row v lists the neighbours of v in
+ *             strictly increasing order (the order of Graphs.neighbors and of the
+ *             rowval of a SparseMatrixCSC); diagonal entries are skipped, like the
+ *             j != i test of ising.jl:294-304.  Every off-diagonal (v, u) needs its
+ *             (u, v) with the same coupling, else MCX_ERR_INVALID_ARG (the reference's
+ *             AssertionError, ising.jl:252-263).
+ *   coupling: float64[rowptr[n]] per entry (IsingMatrix), or NULL: every edge has J
+ *             (IsingGraph).
+ *   field:    float64[n] per site, or NULL: the uniform field h (0 = no field).
+ * All spins start at +1.  Sites are updated in colour classes of a first-fit colouring
+ * (in vertex order, each site the smallest colour its lower-numbered neighbours leave
+ * free); one sweep visits every site once, class by class. */
+MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr,
+                                    const int32_t* col, const double* coupling, double J,
+                                    const double* field, double h, mcx_graph** out);
+MCX_API mcx_status mcx_graph_destroy(mcx_graph* g);
+/* n sites, colour classes, stored neighbour entries (padding included), device bytes;
+ * any pointer may be NULL. */
+MCX_API mcx_status mcx_graph_info(const mcx_graph* g, int64_t* nsites, int32_t* colours,
+                                  int64_t* entries, int64_t* device_bytes);
+/* The colour of every site (int32[n]). */
+MCX_API mcx_status mcx_graph_colours(const mcx_graph* g, int32_t* colour, size_t n);
+/* The `spins` field (copy in / copy out, vertex order); values must be +1 or -1. */
+MCX_API mcx_status mcx_graph_set_spins(mcx_graph* g, const int8_t* host, size_t n);
+MCX_API mcx_status mcx_graph_get_spins(mcx_graph* g, int8_t* host, size_t n);
+/* init!(sys, :random; rng) (ising.jl:60-78), fed by Philox; init!(sys, :up / :down). */
+MCX_API mcx_status mcx_graph_init_random(mcx_graph* g, uint64_t seed, uint32_t stream);
+MCX_API mcx_status mcx_graph_init_uniform(mcx_graph* g, int8_t value);
+/* energy(sys; full) and magnetization(sys; full) (ising.jl:17-18): the cached values,
+ * or with full != 0 a recompute from the spins (_full_energy, ising.jl:185, :349) that
+ * also resets the cache (_recompute_cached!).  Waits for the stream. */
+MCX_API mcx_status mcx_graph_energy(mcx_graph* g, int full, double* energy,
+                                    int64_t* magnetization);
+/* delta_energy(sys, i) (ising.jl:20-23, :198, :362) for 0-based site i; waits. */
+MCX_API mcx_status mcx_graph_delta_energy(mcx_graph* g, int64_t i, double* delta_energy);
+/* modify!(sys, i, Δpair, Δspin) with the flip_changes of site i (ising.jl:200-218,
+ * :364-377): flips spin i and updates the cached energy and magnetization. */
+MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i);
+/* `nsweeps` sweeps of n spin_flip!(sys, alg) each (ising.jl:25-58 with accept!,
+ * src/algorithms/metropolis.jl:14-17, :121-127, importance_sampling.jl:80-85): the
+ * reference's FP64 decisions -- Metropolis lr = -beta*ΔE, accept if lr > 0 or
+ * u < exp(lr); Glauber u < logistic(lr); HeatBath s = u < logistic(beta*s*ΔE) ? +1 : -1
+ * -- with u a 53-bit uniform from Philox block (q, sweep lo, sweep hi16 | 7<<24, stream)
+ * for the q-th site the sweep visits, and exp the library's own (bit-identical on host
+ * and device).
+ *   E_series: host float64[nsweeps] of the cached energy after each sweep, or NULL.
+ *   M_series: host int64[nsweeps] of the magnetization after each sweep, or NULL.
+ *   counters: accumulated (HeatBath: accepted = spins that changed), or NULL. */
+MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng,
+                                   int64_t nsweeps, double* E_series, int64_t* M_series,
+                                   mcx_counters* counters);
 
 /* ----------------------------------------------------------- no allocation -- */
 /* mcx_sweep_noalloc has no counterpart in the reference.  It runs the same sweeps as

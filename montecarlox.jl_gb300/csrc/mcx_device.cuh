@@ -3,6 +3,7 @@
 // FP64 expression is evaluated exactly as written.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -104,6 +105,47 @@ __host__ __device__ __forceinline__ double mcx_log(double x) {
     const double ln2_hi = 6.93147180369123816490e-01;
     const double ln2_lo = 1.90821492927058770002e-10;
     return kd * ln2_hi + (lm + kd * ln2_lo);
+}
+
+// exp(x): Cody & Waite argument reduction x = k ln2 + r, |r| <= ln2/2, with ln2 split
+// into a 32-bit head (k * head is exact) and a tail; exp(r) from its Taylor series up to
+// r^13/13! in Horner form; then 2^k is put in with one or two exact scalings.  Plain
+// multiplies and adds in a fixed order, so host and device agree bit for bit.
+__host__ __device__ __forceinline__ double mcx_pow2(int k) {  // 2^k, -1022 <= k <= 1023
+    return bits_to_double((long long)(k + 1023) << 52);
+}
+
+__host__ __device__ __forceinline__ double mcx_exp(double x) {
+    if (x != x) return x;
+    if (x > 709.782712893384) return bits_to_double(0x7FF0000000000000ll);
+    if (x < -745.2) return 0.0;
+    const double kd = floor(x * 0x1.71547652b82fep+0 + 0.5);
+    const double r = (x - kd * 0x1.62e42fee00000p-1) - kd * 0x1.a39ef35793c76p-33;
+    double p = 0x1.6124613a86d09p-33;
+    p = p * r + 0x1.1eed8eff8d898p-29;
+    p = p * r + 0x1.ae64567f544e4p-26;
+    p = p * r + 0x1.27e4fb7789f5cp-22;
+    p = p * r + 0x1.71de3a556c734p-19;
+    p = p * r + 0x1.a01a01a01a01ap-16;
+    p = p * r + 0x1.a01a01a01a01ap-13;
+    p = p * r + 0x1.6c16c16c16c17p-10;
+    p = p * r + 0x1.1111111111111p-7;
+    p = p * r + 0x1.5555555555555p-5;
+    p = p * r + 0x1.5555555555555p-3;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    const int k = (int)kd;
+    if (k > 1023) return (p * mcx_pow2(k - 1)) * 2.0;
+    if (k < -1021) return (p * mcx_pow2(k + 64)) * 0x1p-64;
+    return p * mcx_pow2(k);
+}
+
+// logistic(x), src/infrastructure/utils.jl:82-88, on mcx_exp
+__host__ __device__ __forceinline__ double mcx_logistic(double x) {
+    if (x >= 0) return 1.0 / (1.0 + mcx_exp(-x));
+    const double ex = mcx_exp(x);
+    return ex / (1.0 + ex);
 }
 
 // Block-wide sum of up to 4 int64 values, one atomicAdd per value per block.

@@ -1,0 +1,865 @@
+// mcx_graph.cu -- Ising models on general neighbour lists: IsingGraph (one coupling over a
+// graph, SpinSystems/src/ising.jl:86-218) and IsingMatrix (symmetric sparse J_ij,
+// ising.jl:221-377), with no field, a uniform field or a field per site.
+//
+// Layout in HBM.  Sites are renumbered by colour class (first-fit colouring in vertex
+// order; inside a class in vertex order) and every class is padded to a multiple of 32
+// with dummy sites of spin 0 and no neighbours.  The neighbour lists are stored
+// sliced-ELL: 32 consecutive positions form a slice whose entries are stored column-major
+// -- entry k of lane l at soff[s] + 32k + l, padded with -1 to the longest list of the
+// slice -- so that a warp reads one slice per step and every load of a neighbour position
+// (and of a per-entry coupling) is a single coalesced transaction.  The spins of the other
+// classes are gathered through the L2 (one byte per site; a 16M-site graph is 16 MB).
+//
+// Decisions are the reference's FP64 rules.  With one coupling and no per-site field,
+// ΔE depends only on (s_i, Σ_j s_i s_j), so the host tabulates, per (s_i, lpi), the
+// 53-bit integer threshold T = ceil(p 2^53) with u < p  <=>  k < T for u = k 2^-53: the
+// device decision is then one 64-bit integer compare, identical to the FP64 one.
+// Otherwise every site evaluates ΔE, exp and logistic in FP64 with the library's own
+// mcx_exp (bit-identical on host and device).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mcx_device.cuh"
+#include "mcx_internal.h"
+
+using namespace mcx;
+
+namespace {
+
+constexpr int kGraphBlock = 256;
+constexpr int kSlicesPerBlock = kGraphBlock / 32;
+constexpr int kMaxTableDegree = 4096;
+constexpr unsigned long long kAlways53 = (1ull << 53) + 1;
+
+enum GField { F_NONE = 0, F_UNIFORM = 1, F_VECTOR = 2 };
+
+struct GraphDev {
+    int8_t* spins;                  // padded positions, renumbered order
+    const int32_t* nbr;             // sliced-ELL neighbour positions (-1 = padding)
+    const double* J64;              // per entry (IsingMatrix), or nullptr
+    const long long* soff;          // nslices + 1 entry offsets
+    const double* h;                // per position (vector field), or nullptr
+    double J, hu;                   // uniform coupling, uniform field
+    const unsigned long long* tab;  // thresholds by (s > 0, lpi + dmax)
+    const double* tabdE;            // ΔE by (s > 0, lpi + dmax)
+    int dmax;
+    double beta;
+    unsigned long long* acc;        // accepted moves
+    long long* M;                   // cached magnetization
+    double* E;                      // cached energy
+    double* part;                   // per-block partial sums of ΔE
+};
+
+struct GClass {
+    long long p0;       // first padded position of the class
+    long long count;    // sites of the class
+    long long q0;       // visits before this class in a sweep
+    long long slice0;   // first slice
+    long long nslices;
+    int part0;          // first partial-sum slot
+};
+
+// Deterministic block sum of one FP64 value (fixed shuffle tree, then warps in order);
+// the result is valid in thread 0.
+__device__ __forceinline__ double block_sum_f64(double v) {
+    __shared__ double red[kGraphBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+__device__ __forceinline__ long long warp_sum_i64(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// ΔE of the site at padded position p (lane of its slice), the reference's
+// flip_changes + delta_energy: -Δpair - h Δspin with Δpair = -2 acc (IsingMatrix) or
+// -2 J lpi (IsingGraph), Δspin = -2 s.
+template <bool EDGEJ, int FIELD>
+__device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long p, int si, double acc, int lpi) {
+    const double dpair = EDGEJ ? -2.0 * acc : (-2.0 * g.J) * (double)lpi;
+    const double dspin = (double)(-2 * si);
+    if (FIELD == F_VECTOR) return -dpair - g.h[p] * dspin;
+    if (FIELD == F_UNIFORM) return -dpair - g.hu * dspin;
+    return -dpair;
+}
+
+// One colour class of one sweep.  A warp takes one 32-site slice per step.
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(kGraphBlock) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
+                                                             uint32_t stream, unsigned long long sweep) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t w2 = ctr_word2(sweep, 0, P_GRAPH);
+    double dEsum = 0.0;
+    long long dM = 0;
+    long long nacc = 0;
+    for (long long sl = (long long)blockIdx.x * kSlicesPerBlock + warp; sl < c.nslices;
+         sl += (long long)gridDim.x * kSlicesPerBlock) {
+        const long long s = c.slice0 + sl;
+        const long long p = s * 32 + lane;
+        const long long local = p - c.p0;
+        const long long off = g.soff[s];
+        const int w = (int)((g.soff[s + 1] - off) >> 5);
+        const int si = g.spins[p];
+        int lpi = 0;
+        double acc = 0.0;
+        for (int k = 0; k < w; ++k) {
+            const long long e = off + 32ll * k + lane;
+            const int nb = g.nbr[e];
+            if (nb >= 0) {
+                const int sj = g.spins[nb];
+                if (EDGEJ) {
+                    const double Jk = g.J64[e];
+                    acc += (si * sj > 0) ? Jk : -Jk;  // (s_i J) s_j, exact sign flips
+                } else {
+                    lpi += si * sj;
+                }
+            }
+        }
+        if (local < c.count) {
+            const uint4 r = philox10(make_uint4((uint32_t)(c.q0 + local), (uint32_t)sweep, w2, stream), k0, k1);
+            const unsigned long long ku = ((unsigned long long)r.x << 21) | (unsigned long long)(r.y >> 11);
+            bool flip;
+            double dE;
+            if (TABLE) {
+                const int idx = (si > 0 ? 2 * g.dmax + 1 : 0) + lpi + g.dmax;
+                const bool below = ku < g.tab[idx];
+                flip = ALG == MCX_HEATBATH ? (below != (si == 1)) : below;
+                dE = g.tabdE[idx];
+            } else {
+                dE = site_delta_energy<EDGEJ, FIELD>(g, p, si, acc, lpi);
+                const double u = (double)ku * 0x1p-53;
+                if (ALG == MCX_METROPOLIS) {
+                    const double lr = -g.beta * dE;
+                    flip = (lr > 0) || (u < mcx_exp(lr));
+                } else if (ALG == MCX_GLAUBER) {
+                    flip = u < mcx_logistic(-g.beta * dE);
+                } else {
+                    const bool up = u < mcx_logistic((g.beta * (double)si) * dE);
+                    flip = up != (si == 1);
+                }
+            }
+            if (flip) {
+                g.spins[p] = (int8_t)(-si);
+                dEsum += dE;
+                dM += -2 * si;
+                ++nacc;
+            }
+        }
+    }
+    const double t = block_sum_f64(dEsum);
+    if (threadIdx.x == 0) g.part[c.part0 + blockIdx.x] = t;
+    dM = warp_sum_i64(dM);
+    nacc = warp_sum_i64(nacc);
+    if (lane == 0) {
+        if (dM) atomicAdd(reinterpret_cast<unsigned long long*>(g.M), (unsigned long long)dM);
+        if (nacc) atomicAdd(g.acc, (unsigned long long)nacc);
+    }
+}
+
+// E += Σ partials (fixed order); record the series entry of sweep t.
+__global__ void __launch_bounds__(kGraphBlock) k_graph_finish(double* part, int nparts, double* E, const long long* M,
+                                                              double* Eser, long long* Mser, long long t) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += part[i];
+    const double s = block_sum_f64(v);
+    if (threadIdx.x == 0) {
+        const double e = *E + s;
+        *E = e;
+        if (Eser) Eser[t] = e;
+        if (Mser) Mser[t] = *M;
+    }
+}
+
+// _full_energy / sum(spins): per block the FP64 pair and field sums, one int64 atomic for
+// the integer pair sum and for M.
+template <bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(kGraphBlock) k_graph_recompute(GraphDev g, long long nslices, double* part2,
+                                                                 long long* ilpi) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double pacc = 0.0, facc = 0.0;
+    long long lsum = 0, msum = 0;
+    for (long long s = (long long)blockIdx.x * kSlicesPerBlock + warp; s < nslices;
+         s += (long long)gridDim.x * kSlicesPerBlock) {
+        const long long p = s * 32 + lane;
+        const long long off = g.soff[s];
+        const int w = (int)((g.soff[s + 1] - off) >> 5);
+        const int si = g.spins[p];
+        double acc = 0.0;
+        int lpi = 0;
+        for (int k = 0; k < w; ++k) {
+            const long long e = off + 32ll * k + lane;
+            const int nb = g.nbr[e];
+            if (nb >= 0) {
+                const int sj = g.spins[nb];
+                if (EDGEJ) {
+                    const double Jk = g.J64[e];
+                    acc += (si * sj > 0) ? Jk : -Jk;
+                } else {
+                    lpi += si * sj;
+                }
+            }
+        }
+        pacc += acc;
+        lsum += lpi;
+        msum += si;
+        if (FIELD == F_VECTOR && si != 0) facc += g.h[p] * (double)si;
+    }
+    const double pt = block_sum_f64(pacc);
+    const double ft = block_sum_f64(facc);
+    if (threadIdx.x == 0) {
+        part2[2 * blockIdx.x] = pt;
+        part2[2 * blockIdx.x + 1] = ft;
+    }
+    lsum = warp_sum_i64(lsum);
+    msum = warp_sum_i64(msum);
+    if (lane == 0) {
+        if (lsum) atomicAdd(reinterpret_cast<unsigned long long*>(ilpi), (unsigned long long)lsum);
+        if (msum) atomicAdd(reinterpret_cast<unsigned long long*>(g.M), (unsigned long long)msum);
+    }
+}
+
+// pair = Σ lpi / 2 (FP64 for IsingMatrix, J (Σ lpi / 2) for IsingGraph); E = -pair - field.
+__global__ void __launch_bounds__(kGraphBlock) k_graph_recompute_finish(const double* part2, int nparts,
+                                                                        const long long* ilpi, int edgej, int field,
+                                                                        double J, double hu, const long long* M,
+                                                                        double* E) {
+    double p = 0.0, f = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        p += part2[2 * i];
+        f += part2[2 * i + 1];
+    }
+    const double ps = block_sum_f64(p);
+    const double fs = block_sum_f64(f);
+    if (threadIdx.x == 0) {
+        const double pair = edgej ? ps / 2 : J * (double)(*ilpi / 2);
+        const double fld = field == F_VECTOR ? fs : field == F_UNIFORM ? hu * (double)(*M) : 0.0;
+        *E = field == F_NONE ? -pair : -pair - fld;
+    }
+}
+
+// delta_energy(sys, i) (op 0) or modify! with flip_changes (op 1) at one position.
+template <bool EDGEJ, int FIELD>
+__global__ void k_graph_site(GraphDev g, long long p, int op, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long s = p >> 5;
+    const int lane = (int)(p & 31);
+    const long long off = g.soff[s];
+    const int w = (int)((g.soff[s + 1] - off) >> 5);
+    const int si = g.spins[p];
+    double acc = 0.0;
+    int lpi = 0;
+    for (int k = 0; k < w; ++k) {
+        const long long e = off + 32ll * k + lane;
+        const int nb = g.nbr[e];
+        if (nb >= 0) {
+            const int sj = g.spins[nb];
+            if (EDGEJ) {
+                const double Jk = g.J64[e];
+                acc += (si * sj > 0) ? Jk : -Jk;
+            } else {
+                lpi += si * sj;
+            }
+        }
+    }
+    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, si, acc, lpi);
+    *out = dE;
+    if (op == 1) {
+        g.spins[p] = (int8_t)(-si);
+        *g.E = *g.E + dE;
+        *g.M = *g.M - 2 * si;
+    }
+}
+
+__global__ void k_graph_validate(const int8_t* lin, long long n, unsigned long long* bad) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const int8_t x = lin[v];
+        if (x != 1 && x != -1) atomicAdd(bad, 1ull);
+    }
+}
+
+__global__ void k_graph_scatter(const int8_t* lin, const int32_t* perm, long long n, int8_t* spins) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+        spins[perm[v]] = lin[v];
+}
+
+__global__ void k_graph_gather(int8_t* lin, const int32_t* perm, long long n, const int8_t* spins) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+        lin[v] = spins[perm[v]];
+}
+
+// init!(sys, :random): site v takes the top bit of word v&3 of Philox block
+// (v>>2, 0, P_GRAPH_INIT<<24, stream).
+__global__ void k_graph_init_random(const int32_t* perm, long long n, int8_t* spins, uint32_t k0, uint32_t k1,
+                                    uint32_t stream) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const uint4 r = philox10(make_uint4((uint32_t)(v >> 2), 0u, (uint32_t)P_GRAPH_INIT << 24, stream), k0, k1);
+        spins[perm[v]] = (pick4(r, (int)(v & 3)) & 0x80000000u) ? 1 : -1;
+    }
+}
+
+__global__ void k_graph_init_uniform(const int32_t* perm, long long n, int8_t* spins, int8_t value) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+        spins[perm[v]] = value;
+}
+
+using ClassFn = void (*)(GraphDev, GClass, uint32_t, uint32_t, uint32_t, unsigned long long);
+
+template <int ALG, bool TABLE>
+ClassFn class_fn_t(bool edgej, int field) {
+    if (TABLE) return field == F_UNIFORM ? k_graph_class<ALG, true, false, F_UNIFORM> : k_graph_class<ALG, true, false, F_NONE>;
+    if (edgej)
+        return field == F_VECTOR    ? k_graph_class<ALG, false, true, F_VECTOR>
+               : field == F_UNIFORM ? k_graph_class<ALG, false, true, F_UNIFORM>
+                                    : k_graph_class<ALG, false, true, F_NONE>;
+    return field == F_VECTOR    ? k_graph_class<ALG, false, false, F_VECTOR>
+           : field == F_UNIFORM ? k_graph_class<ALG, false, false, F_UNIFORM>
+                                : k_graph_class<ALG, false, false, F_NONE>;
+}
+
+ClassFn class_fn(mcx_algorithm alg, bool table, bool edgej, int field) {
+    switch (alg) {
+        case MCX_METROPOLIS: return table ? class_fn_t<MCX_METROPOLIS, true>(edgej, field)
+                                          : class_fn_t<MCX_METROPOLIS, false>(edgej, field);
+        case MCX_GLAUBER: return table ? class_fn_t<MCX_GLAUBER, true>(edgej, field)
+                                       : class_fn_t<MCX_GLAUBER, false>(edgej, field);
+        default: return table ? class_fn_t<MCX_HEATBATH, true>(edgej, field)
+                              : class_fn_t<MCX_HEATBATH, false>(edgej, field);
+    }
+}
+
+template <bool EDGEJ>
+void recompute_launch(int field, int grid, cudaStream_t st, const GraphDev& g, long long nslices, double* part2,
+                      long long* ilpi) {
+    if (field == F_VECTOR) k_graph_recompute<EDGEJ, F_VECTOR><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
+    else if (field == F_UNIFORM) k_graph_recompute<EDGEJ, F_UNIFORM><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
+    else k_graph_recompute<EDGEJ, F_NONE><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
+}
+
+template <bool EDGEJ>
+void site_launch(int field, cudaStream_t st, const GraphDev& g, long long p, int op, double* out) {
+    if (field == F_VECTOR) k_graph_site<EDGEJ, F_VECTOR><<<1, 32, 0, st>>>(g, p, op, out);
+    else if (field == F_UNIFORM) k_graph_site<EDGEJ, F_UNIFORM><<<1, 32, 0, st>>>(g, p, op, out);
+    else k_graph_site<EDGEJ, F_NONE><<<1, 32, 0, st>>>(g, p, op, out);
+}
+
+// 53-bit threshold of "u < p" for u = k 2^-53: k < ceil(p 2^53).
+unsigned long long threshold53(double p) {
+    if (!(p > 0.0)) return 0;
+    if (p >= 1.0) return 1ull << 53;
+    return (unsigned long long)std::ceil(p * 9007199254740992.0);
+}
+
+}  // namespace
+
+struct mcx_graph {
+    mcx_ctx* ctx = nullptr;
+    mcx::CtxHold hold;
+    int64_t n = 0, npad = 0, nslices = 0, entries = 0;
+    int ncol = 0;
+    int dmax = 0;
+    bool edgej = false;
+    int field = F_NONE;
+    double J = 1.0, h = 0.0;
+    std::vector<int32_t> colour;    // per vertex
+    std::vector<GClass> classes;
+    int nparts = 0;                 // partial-sum slots over all classes
+    int8_t* d_spins = nullptr;
+    int32_t* d_nbr = nullptr;
+    double* d_J64 = nullptr;
+    long long* d_soff = nullptr;
+    double* d_h = nullptr;
+    int32_t* d_perm = nullptr;      // vertex -> padded position
+    int8_t* d_lin = nullptr;        // staging, vertex order
+    unsigned long long* d_tab = nullptr;
+    double* d_tabdE = nullptr;
+    int tab_alg = -1;
+    double tab_beta = 0.0;
+    double* d_E = nullptr;
+    long long* d_M = nullptr;
+    unsigned long long* d_acc = nullptr;
+    long long* d_ilpi = nullptr;
+    double* d_part = nullptr;
+    int part_cap = 0;               // doubles
+    double* d_Eser = nullptr;
+    long long* d_Mser = nullptr;
+    int64_t ser_cap = 0;
+    double* d_site = nullptr;       // delta_energy result
+    int64_t device_bytes = 0;
+    std::vector<std::pair<void*, size_t>> allocs;
+
+    bool table_mode() const { return !edgej && field != F_VECTOR && dmax <= kMaxTableDegree; }
+    GraphDev dev(double beta) const {
+        GraphDev g;
+        g.spins = d_spins;
+        g.nbr = d_nbr;
+        g.J64 = d_J64;
+        g.soff = d_soff;
+        g.h = d_h;
+        g.J = J;
+        g.hu = h;
+        g.tab = d_tab;
+        g.tabdE = d_tabdE;
+        g.dmax = dmax;
+        g.beta = beta;
+        g.acc = d_acc;
+        g.M = d_M;
+        g.E = d_E;
+        g.part = d_part;
+        return g;
+    }
+};
+
+namespace {
+
+template <typename T>
+mcx_status galloc(mcx_graph* g, T** p, size_t count) {
+    void* q = nullptr;
+    MCX_CHECK(dev_alloc(g->ctx, &q, count * sizeof(T)));
+    g->allocs.push_back({q, count * sizeof(T)});
+    g->device_bytes += (int64_t)(count * sizeof(T));
+    *p = static_cast<T*>(q);
+    return MCX_OK;
+}
+
+void gfree(mcx_graph* g, void* p) {
+    for (size_t i = 0; i < g->allocs.size(); ++i)
+        if (g->allocs[i].first == p) {
+            dev_free(g->ctx, p, g->allocs[i].second);
+            g->device_bytes -= (int64_t)g->allocs[i].second;
+            g->allocs.erase(g->allocs.begin() + (long)i);
+            return;
+        }
+}
+
+int grid_of(const mcx_graph* g, long long slices, int per_sm = 8) {
+    long long b = (slices + kSlicesPerBlock - 1) / kSlicesPerBlock;
+    long long cap = (long long)g->ctx->num_sms * per_sm;
+    return (int)std::max(1ll, std::min(b, cap));
+}
+
+mcx_status graph_recompute(mcx_graph* g) {
+    cudaStream_t st = g->ctx->stream;
+    const int grid = grid_of(g, g->nslices);
+    if (2 * grid > g->part_cap) return fail(MCX_ERR_INVALID_ARG, "partial-sum buffer too small");
+    MCX_CUDA(cudaMemsetAsync(g->d_M, 0, sizeof(long long), st));
+    MCX_CUDA(cudaMemsetAsync(g->d_ilpi, 0, sizeof(long long), st));
+    const GraphDev d = g->dev(0.0);
+    if (g->edgej) recompute_launch<true>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi);
+    else recompute_launch<false>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi);
+    k_graph_recompute_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, grid, g->d_ilpi, g->edgej ? 1 : 0, g->field, g->J,
+                                                        g->h, g->d_M, g->d_E);
+    count_launch(g->ctx, 2);
+    MCX_CUDA(cudaGetLastError());
+    return MCX_OK;
+}
+
+mcx_status graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
+    if (g->tab_alg == (int)alg && g->tab_beta == beta) return MCX_OK;
+    const int D = g->dmax, width = 2 * D + 1;
+    std::vector<unsigned long long> thr(2 * (size_t)width);
+    std::vector<double> dE(2 * (size_t)width);
+    for (int sp = 0; sp < 2; ++sp) {
+        const int s = sp ? 1 : -1;
+        for (int lpi = -D; lpi <= D; ++lpi) {
+            const double dpair = (-2.0 * g->J) * (double)lpi;
+            const double dspin = (double)(-2 * s);
+            const double de = g->field == F_UNIFORM ? -dpair - g->h * dspin : -dpair;
+            unsigned long long t;
+            if (alg == MCX_METROPOLIS) {
+                const double lr = -beta * de;
+                t = lr > 0 ? kAlways53 : threshold53(mcx_exp(lr));
+            } else if (alg == MCX_GLAUBER) {
+                t = threshold53(mcx_logistic(-beta * de));
+            } else {
+                t = threshold53(mcx_logistic((beta * (double)s) * de));
+            }
+            thr[(size_t)sp * width + (lpi + D)] = t;
+            dE[(size_t)sp * width + (lpi + D)] = de;
+        }
+    }
+    MCX_CUDA(cudaMemcpyAsync(g->d_tab, thr.data(), thr.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                             g->ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(g->d_tabdE, dE.data(), dE.size() * sizeof(double), cudaMemcpyHostToDevice,
+                             g->ctx->stream));
+    // the host vectors go out of scope: wait for the copies
+    MCX_CUDA(cudaStreamSynchronize(g->ctx->stream));
+    g->tab_alg = (int)alg;
+    g->tab_beta = beta;
+    return MCX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr, const int32_t* col,
+                                    const double* coupling, double J, const double* field, double h,
+                                    mcx_graph** out) {
+    if (!ctx || !rowptr || !out || (!col && n > 0)) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (n < 1 || n > (1ll << 30)) return fail(MCX_ERR_INVALID_ARG, "n = %lld sites (1 .. 2^30)", (long long)n);
+    if (rowptr[0] != 0) return fail(MCX_ERR_INVALID_ARG, "rowptr[0] must be 0");
+    for (int64_t v = 0; v < n; ++v)
+        if (rowptr[v + 1] < rowptr[v]) return fail(MCX_ERR_INVALID_ARG, "rowptr decreases at %lld", (long long)v);
+    if (!std::isfinite(J) || !std::isfinite(h)) return fail(MCX_ERR_INVALID_ARG, "J and h must be finite");
+    // neighbour lists: in range, strictly increasing; symmetric with equal couplings
+    std::vector<int32_t> deg(n, 0);
+    for (int64_t v = 0; v < n; ++v) {
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+            const int32_t u = col[e];
+            if (u < 0 || u >= n) return fail(MCX_ERR_INVALID_ARG, "neighbour %d of site %lld out of range", u, (long long)v);
+            if (e > rowptr[v] && col[e - 1] >= u)
+                return fail(MCX_ERR_INVALID_ARG, "neighbours of site %lld are not strictly increasing", (long long)v);
+            if (coupling && !std::isfinite(coupling[e])) return fail(MCX_ERR_INVALID_ARG, "coupling not finite");
+            if (u == v) continue;
+            ++deg[v];
+            const int32_t* b = col + rowptr[u];
+            const int32_t* en = col + rowptr[u + 1];
+            const int32_t* f = std::lower_bound(b, en, (int32_t)v);
+            if (f == en || *f != v) return fail(MCX_ERR_INVALID_ARG, "J must be symmetric: (%lld, %d) has no (%d, %lld)",
+                                                (long long)v, u, u, (long long)v);
+            if (coupling && coupling[e] != coupling[rowptr[u] + (f - b)])
+                return fail(MCX_ERR_INVALID_ARG, "J must be symmetric: J[%lld,%d] != J[%d,%lld]", (long long)v, u, u,
+                            (long long)v);
+        }
+    }
+    if (field)
+        for (int64_t v = 0; v < n; ++v)
+            if (!std::isfinite(field[v])) return fail(MCX_ERR_INVALID_ARG, "field not finite");
+    auto g = new mcx_graph();
+    g->ctx = ctx;
+    g->hold.set(ctx);
+    g->n = n;
+    g->edgej = coupling != nullptr;
+    g->field = field ? F_VECTOR : (h != 0.0 ? F_UNIFORM : F_NONE);
+    g->J = J;
+    g->h = h;
+    int dmax = 0;
+    for (int64_t v = 0; v < n; ++v) dmax = std::max(dmax, deg[v]);
+    g->dmax = dmax;
+    // first-fit colouring in vertex order
+    g->colour.assign(n, 0);
+    std::vector<int64_t> seen((size_t)dmax + 2, -1);
+    int ncol = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+            if (col[e] < v) seen[g->colour[col[e]]] = v;
+        int c = 0;
+        while (seen[c] == v) ++c;
+        g->colour[v] = c;
+        ncol = std::max(ncol, c + 1);
+    }
+    g->ncol = ncol;
+    // renumbering: classes in turn, vertex order inside, each class padded to 32
+    std::vector<int64_t> count(ncol, 0);
+    for (int64_t v = 0; v < n; ++v) ++count[g->colour[v]];
+    std::vector<int64_t> start(ncol + 1, 0);
+    for (int c = 0; c < ncol; ++c) start[c + 1] = start[c] + (count[c] + 31) / 32 * 32;
+    g->npad = start[ncol];
+    g->nslices = g->npad / 32;
+    if (g->npad >= (1ll << 31)) {
+        delete g;
+        return fail(MCX_ERR_INVALID_ARG, "graph too large");
+    }
+    std::vector<int32_t> perm(n);
+    std::vector<int64_t> vert(g->npad, -1);  // position -> vertex
+    {
+        std::vector<int64_t> fill(start.begin(), start.end() - 1);
+        for (int64_t v = 0; v < n; ++v) {
+            const int64_t p = fill[g->colour[v]]++;
+            perm[v] = (int32_t)p;
+            vert[p] = v;
+        }
+    }
+    int64_t q0 = 0;
+    int part0 = 0;
+    const long long cap_blocks = (long long)ctx->num_sms * 8;
+    for (int c = 0; c < ncol; ++c) {
+        GClass k;
+        k.p0 = start[c];
+        k.count = count[c];
+        k.q0 = q0;
+        k.slice0 = start[c] / 32;
+        k.nslices = (start[c + 1] - start[c]) / 32;
+        k.part0 = part0;
+        q0 += count[c];
+        part0 += (int)std::min((k.nslices + kSlicesPerBlock - 1) / kSlicesPerBlock, cap_blocks);
+        g->classes.push_back(k);
+    }
+    g->nparts = part0;
+    // sliced-ELL entries
+    std::vector<long long> soff(g->nslices + 1, 0);
+    for (int64_t s = 0; s < g->nslices; ++s) {
+        int w = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int64_t v = vert[s * 32 + l];
+            if (v >= 0) w = std::max(w, deg[v]);
+        }
+        soff[s + 1] = soff[s] + 32ll * w;
+    }
+    g->entries = soff[g->nslices];
+    std::vector<int32_t> nbr(g->entries, -1);
+    std::vector<double> jv(g->edgej ? g->entries : 0, 0.0);
+    for (int64_t s = 0; s < g->nslices; ++s)
+        for (int l = 0; l < 32; ++l) {
+            const int64_t v = vert[s * 32 + l];
+            if (v < 0) continue;
+            int k = 0;
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+                if (col[e] == v) continue;
+                const int64_t idx = soff[s] + 32ll * k + l;
+                nbr[idx] = perm[col[e]];
+                if (g->edgej) jv[idx] = coupling[e];
+                ++k;
+            }
+        }
+    std::vector<double> hv;
+    if (field) {
+        hv.assign(g->npad, 0.0);
+        for (int64_t v = 0; v < n; ++v) hv[perm[v]] = field[v];
+    }
+    // device arrays
+    mcx_status st = MCX_OK;
+    const size_t tabn = 2 * (size_t)(2 * dmax + 1);
+    g->part_cap = std::max(g->nparts, 2 * (int)cap_blocks);
+    do {
+        if ((st = galloc(g, &g->d_spins, (size_t)g->npad))) break;
+        if ((st = galloc(g, &g->d_nbr, (size_t)std::max<int64_t>(g->entries, 1)))) break;
+        if (g->edgej && (st = galloc(g, &g->d_J64, (size_t)std::max<int64_t>(g->entries, 1)))) break;
+        if ((st = galloc(g, &g->d_soff, (size_t)g->nslices + 1))) break;
+        if (field && (st = galloc(g, &g->d_h, (size_t)g->npad))) break;
+        if ((st = galloc(g, &g->d_perm, (size_t)n))) break;
+        if ((st = galloc(g, &g->d_lin, (size_t)n))) break;
+        if (g->table_mode() && (st = galloc(g, &g->d_tab, tabn))) break;
+        if (g->table_mode() && (st = galloc(g, &g->d_tabdE, tabn))) break;
+        if ((st = galloc(g, &g->d_E, 1))) break;
+        if ((st = galloc(g, &g->d_M, 1))) break;
+        if ((st = galloc(g, &g->d_acc, 1))) break;
+        if ((st = galloc(g, &g->d_ilpi, 1))) break;
+        if ((st = galloc(g, &g->d_site, 1))) break;
+        if ((st = galloc(g, &g->d_part, (size_t)g->part_cap))) break;
+    } while (false);
+    if (st != MCX_OK) {
+        mcx_graph_destroy(g);
+        return st;
+    }
+    cudaStream_t s0 = ctx->stream;
+    // every host vector outlives the copies: synchronize before returning
+    std::vector<int8_t> spins(g->npad, 0);
+    for (int64_t v = 0; v < n; ++v) spins[perm[v]] = 1;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s0);
+    };
+    up(g->d_spins, spins.data(), spins.size());
+    up(g->d_nbr, nbr.data(), nbr.size() * sizeof(int32_t));
+    if (g->edgej) up(g->d_J64, jv.data(), jv.size() * sizeof(double));
+    up(g->d_soff, soff.data(), soff.size() * sizeof(long long));
+    if (field) up(g->d_h, hv.data(), hv.size() * sizeof(double));
+    up(g->d_perm, perm.data(), perm.size() * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), s0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) {
+        mcx_graph_destroy(g);
+        return cuda_fail(e, "graph upload");
+    }
+    if ((st = graph_recompute(g)) != MCX_OK) {
+        mcx_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_destroy(mcx_graph* g) {
+    if (!g) return MCX_OK;
+    if (g->ctx) cudaStreamSynchronize(g->ctx->stream);
+    while (!g->allocs.empty()) gfree(g, g->allocs.back().first);
+    delete g;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_info(const mcx_graph* g, int64_t* nsites, int32_t* colours, int64_t* entries,
+                                  int64_t* device_bytes) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (nsites) *nsites = g->n;
+    if (colours) *colours = g->ncol;
+    if (entries) *entries = g->entries;
+    if (device_bytes) *device_bytes = g->device_bytes;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_colours(const mcx_graph* g, int32_t* colour, size_t n) {
+    if (!g || !colour) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if ((int64_t)n != g->n) return fail(MCX_ERR_INVALID_ARG, "expected %lld sites, got %zu", (long long)g->n, n);
+    std::copy(g->colour.begin(), g->colour.end(), colour);
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_set_spins(mcx_graph* g, const int8_t* host, size_t n) {
+    if (!g || !host) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if ((int64_t)n != g->n) return fail(MCX_ERR_INVALID_ARG, "expected %lld spins, got %zu", (long long)g->n, n);
+    cudaStream_t st = g->ctx->stream;
+    MCX_CUDA(cudaMemcpyAsync(g->d_lin, host, n, cudaMemcpyHostToDevice, st));
+    MCX_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), st));
+    // values are checked on the device before any is stored (the counter word is free here)
+    unsigned long long bad = 0;
+    const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
+    k_graph_validate<<<grid, 256, 0, st>>>(g->d_lin, g->n, g->d_acc);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    MCX_CUDA(cudaMemcpyAsync(&bad, g->d_acc, sizeof(bad), cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    if (bad) return fail(MCX_ERR_INVALID_ARG, "%llu values are not +1 or -1", bad);
+    k_graph_scatter<<<grid, 256, 0, st>>>(g->d_lin, g->d_perm, g->n, g->d_spins);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    return graph_recompute(g);
+}
+
+MCX_API mcx_status mcx_graph_get_spins(mcx_graph* g, int8_t* host, size_t n) {
+    if (!g || !host) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if ((int64_t)n != g->n) return fail(MCX_ERR_INVALID_ARG, "expected %lld spins, got %zu", (long long)g->n, n);
+    cudaStream_t st = g->ctx->stream;
+    const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
+    k_graph_gather<<<grid, 256, 0, st>>>(g->d_lin, g->d_perm, g->n, g->d_spins);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    MCX_CUDA(cudaMemcpyAsync(host, g->d_lin, n, cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_init_random(mcx_graph* g, uint64_t seed, uint32_t stream) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
+    k_graph_init_random<<<grid, 256, 0, g->ctx->stream>>>(g->d_perm, g->n, g->d_spins, (uint32_t)seed,
+                                                          (uint32_t)(seed >> 32), stream);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    return graph_recompute(g);
+}
+
+MCX_API mcx_status mcx_graph_init_uniform(mcx_graph* g, int8_t value) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (value != 1 && value != -1) return fail(MCX_ERR_INVALID_ARG, "value %d is not an Ising state", (int)value);
+    const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
+    k_graph_init_uniform<<<grid, 256, 0, g->ctx->stream>>>(g->d_perm, g->n, g->d_spins, value);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    return graph_recompute(g);
+}
+
+MCX_API mcx_status mcx_graph_energy(mcx_graph* g, int full, double* energy, int64_t* magnetization) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (full) MCX_CHECK(graph_recompute(g));
+    double E = 0.0;
+    long long M = 0;
+    cudaStream_t st = g->ctx->stream;
+    MCX_CUDA(cudaMemcpyAsync(&E, g->d_E, sizeof(E), cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaMemcpyAsync(&M, g->d_M, sizeof(M), cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    if (energy) *energy = E;
+    if (magnetization) *magnetization = M;
+    return MCX_OK;
+}
+
+static mcx_status graph_site(mcx_graph* g, int64_t i, int op, double* out) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (i < 0 || i >= g->n) return fail(MCX_ERR_OUT_OF_RANGE, "site %lld outside 0..%lld", (long long)i,
+                                        (long long)g->n - 1);
+    int32_t p = 0;
+    cudaStream_t st = g->ctx->stream;
+    MCX_CUDA(cudaMemcpyAsync(&p, g->d_perm + i, sizeof(p), cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    const GraphDev d = g->dev(0.0);
+    if (g->edgej) site_launch<true>(g->field, st, d, p, op, g->d_site);
+    else site_launch<false>(g->field, st, d, p, op, g->d_site);
+    count_launch(g->ctx);
+    MCX_CUDA(cudaGetLastError());
+    double v = 0.0;
+    MCX_CUDA(cudaMemcpyAsync(&v, g->d_site, sizeof(v), cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    if (out) *out = v;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_delta_energy(mcx_graph* g, int64_t i, double* delta_energy) {
+    return graph_site(g, i, 0, delta_energy);
+}
+
+MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i) { return graph_site(g, i, 1, nullptr); }
+
+MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng, int64_t nsweeps,
+                                   double* E_series, int64_t* M_series, mcx_counters* counters) {
+    if (!g || !rng) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (alg < MCX_METROPOLIS || alg > MCX_HEATBATH) return fail(MCX_ERR_INVALID_ARG, "unknown algorithm %d", (int)alg);
+    if (nsweeps < 0) return fail(MCX_ERR_INVALID_ARG, "nsweeps < 0");
+    if (!std::isfinite(beta)) return fail(MCX_ERR_INVALID_ARG, "beta must be finite");
+    if (nsweeps == 0) return MCX_OK;
+    mcx_ctx* ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    const bool table = g->table_mode();
+    if (table) MCX_CHECK(graph_table(g, alg, beta));
+    const bool rec = E_series || M_series;
+    if (rec && nsweeps > g->ser_cap) {
+        if (g->d_Eser) gfree(g, g->d_Eser);
+        if (g->d_Mser) gfree(g, g->d_Mser);
+        g->d_Eser = nullptr;
+        g->d_Mser = nullptr;
+        g->ser_cap = 0;
+        MCX_CHECK(galloc(g, &g->d_Eser, (size_t)nsweeps));
+        MCX_CHECK(galloc(g, &g->d_Mser, (size_t)nsweeps));
+        g->ser_cap = nsweeps;
+    }
+    const ClassFn fn = class_fn(alg, table, g->edgej, g->field);
+    int bps = 0;
+    MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kGraphBlock, 0));
+    bps = std::max(1, std::min(bps, 8));
+    MCX_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), st));
+    MCX_CUDA(cudaMemsetAsync(g->d_part, 0, sizeof(double) * (size_t)g->nparts, st));
+    const GraphDev d = g->dev(beta);
+    const uint32_t k0 = (uint32_t)rng->seed, k1 = (uint32_t)(rng->seed >> 32);
+    for (int64_t t = 0; t < nsweeps; ++t) {
+        const unsigned long long sweep = rng->counter + (unsigned long long)t;
+        for (const GClass& c : g->classes) {
+            const int grid = (int)std::min<long long>((c.nslices + kSlicesPerBlock - 1) / kSlicesPerBlock,
+                                                      (long long)ctx->num_sms * bps);
+            fn<<<std::max(grid, 1), kGraphBlock, 0, st>>>(d, c, k0, k1, rng->stream, sweep);
+        }
+        k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, rec ? g->d_Eser : nullptr,
+                                                  rec ? g->d_Mser : nullptr, t);
+        count_launch(ctx, (uint64_t)g->classes.size() + 1);
+    }
+    MCX_CUDA(cudaGetLastError());
+    rng->counter += (uint64_t)nsweeps;
+    if (counters || rec) {
+        unsigned long long acc1 = 0;
+        MCX_CUDA(cudaMemcpyAsync(&acc1, g->d_acc, sizeof(acc1), cudaMemcpyDeviceToHost, st));
+        if (E_series)
+            MCX_CUDA(cudaMemcpyAsync(E_series, g->d_Eser, sizeof(double) * (size_t)nsweeps, cudaMemcpyDeviceToHost, st));
+        if (M_series)
+            MCX_CUDA(cudaMemcpyAsync(M_series, g->d_Mser, sizeof(long long) * (size_t)nsweeps, cudaMemcpyDeviceToHost,
+                                     st));
+        MCX_CUDA(cudaStreamSynchronize(st));
+        if (counters) {
+            counters->attempts += (uint64_t)g->n * (uint64_t)nsweeps;
+            counters->accepted += acc1;
+        }
+    }
+    return MCX_OK;
+}
+
+}  // extern "C"

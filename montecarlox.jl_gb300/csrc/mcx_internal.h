@@ -19,7 +19,9 @@ enum Purpose : uint32_t {
     P_PROPOSE = 1,  // Blume-Capel proposal bit (top bit of the word)
     P_LOW = 2,      // low word of a 53-bit uniform (flat-histogram decisions)
     P_INIT = 3,     // init!(sys, :random)
-    P_EXCHANGE = 4  // replica-exchange uniform
+    P_EXCHANGE = 4,  // replica-exchange uniform
+    P_GRAPH = 7,     // 53-bit uniform of a site of a general graph (words 0 and 1)
+    P_GRAPH_INIT = 8  // init!(sys, :random) of a general graph
 };
 
 void set_error(const char* fmt, ...);

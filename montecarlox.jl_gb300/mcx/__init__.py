@@ -10,6 +10,7 @@ Reference API mirrored here (paths inside MonteCarloX.jl):
   HeatBath                    src/algorithms/heat_bath.jl:11-17
   acceptance_rate / reset!    src/algorithms/importance_sampling.jl:95-110
   Ising / IsingLatticeOptim   SpinSystems/src/ising.jl:523-571
+  IsingGraph / IsingMatrix    SpinSystems/src/ising.jl:86-428 (mcx.graph)
   BlumeCapel                  SpinSystems/src/blume_capel.jl:500-511
   init! / energy / magnetization  ising.jl:127-188, blume_capel.jl:18-109
 """
@@ -325,9 +326,40 @@ class BlumeCapelDevice(DeviceLattice):
     STATES = (-1, 0, 1)
 
 
-def Ising(dims, *, J=1, periodic=True, h=0, layout="int8", ctx=None):
-    """Ising(dims; J=1, periodic=true, h=0): all spins up (SpinSystems/src/ising.jl:523-534)."""
-    return IsingDevice(dims, J=J, h=h, periodic=periodic, layout=layout, ctx=ctx)
+def _lattice_ok(dims):
+    return len(dims) in (2, 3) and all(isinstance(d, (int, np.integer)) and d >= 4 and d % 2 == 0 for d in dims)
+
+
+def Ising(dims, J=None, *, periodic=True, h=0, layout="int8", ctx=None):
+    """The reference's Ising constructors (SpinSystems/src/ising.jl:383-428), all spins up.
+
+    * ``Ising(dims; J=1, periodic=true, h=0)`` with a scalar J and h on an even periodic
+      2-D / 3-D grid (every side >= 4): the colour-split device lattice.
+    * Other grids (open boundaries, odd or short sides, 1-D or >3-D), a field vector
+      ``h``, or a coupling vector ``J`` over the grid's edges: the general-graph system
+      on ``grid(dims; periodic)``.
+    * ``Ising(graph::SimpleGraph, J::Real; h)``: IsingGraph; ``Ising(graph, Jvec; h)``:
+      IsingMatrix with Jvec on edges(graph); ``Ising(J::sparse; h)``: IsingMatrix."""
+    from . import graph as G
+    if isinstance(dims, G.SimpleGraph):
+        if J is None or np.isscalar(J):
+            return G.IsingGraph(dims, 1 if J is None else J, h=h, ctx=ctx)
+        return G.IsingMatrix(G.matrix_from_edges(dims, J), h=h, ctx=ctx)
+    if J is None and not isinstance(dims, (list, tuple, np.ndarray)):
+        return G.IsingMatrix(dims, h=h, ctx=ctx)  # Ising(J::SparseMatrixCSC; h)
+    J = 1 if J is None else J
+    dims = [int(d) for d in dims]
+    if np.isscalar(J) and np.isscalar(h) and periodic and _lattice_ok(dims):
+        return IsingDevice(dims, J=J, h=h, periodic=periodic, layout=layout, ctx=ctx)
+    if layout != "int8":
+        raise ArgumentError("layout %r needs an even periodic 2-D / 3-D grid with a scalar J and h" % layout)
+    g = G.grid(dims, periodic=periodic)
+    if np.isscalar(J):
+        return G.IsingGraph(g, J, h=h, ctx=ctx)
+    import scipy.sparse as sp
+    if sp.issparse(J):
+        return G.IsingMatrix(J, h=h, ctx=ctx)
+    return G.IsingMatrix(G.matrix_from_edges(g, J), h=h, ctx=ctx)
 
 
 def IsingLatticeOptim(Lx, Ly, *, layout="int8", ctx=None):
@@ -340,7 +372,15 @@ def BlumeCapel(dims, *, J=1, D=0, periodic=True, h=0, ctx=None):
     return BlumeCapelDevice(dims, J=J, D=D, h=h, periodic=periodic, ctx=ctx)
 
 
+def _is_graph(sys):
+    from .graph import IsingGraphDevice
+    return isinstance(sys, IsingGraphDevice)
+
+
 def set_spins_(sys, values):
+    if _is_graph(sys):
+        sys.spins = values
+        return
     arr = np.ascontiguousarray(values, dtype=np.int8).reshape(-1)
     if arr.size != sys.N:
         raise ArgumentError("expected %d spins, got %d" % (sys.N, arr.size))
@@ -350,6 +390,14 @@ def set_spins_(sys, values):
 def init_(sys, type, rng=None):
     """init!(sys, :up | :down | :zero | :random; rng)."""
     t = type.lstrip(":") if isinstance(type, str) else type
+    if _is_graph(sys):
+        from . import graph as G
+        if t == "random" and rng is None:
+            raise ArgumentError("Random initialization requires rng")
+        if t not in ("random", "up", "down"):
+            raise ArgumentError("Unknown initialization type: %s" % type)
+        G.init(sys, t, rng)
+        return sys
     if t == "random":
         if rng is None:
             raise ArgumentError("Random initialization requires rng")
@@ -374,7 +422,11 @@ def observables(sys, full=False):
 
 
 def energy(sys, full=False):
-    """energy(sys; full): -J*pair - h*M (+ D*sum s^2 for Blume-Capel)."""
+    """energy(sys; full): -J*pair - h*M (+ D*sum s^2 for Blume-Capel); -pair - field on a
+    general graph."""
+    if _is_graph(sys):
+        from . import graph as G
+        return G.energy(sys, full)[0]
     P, M, Q = observables(sys, full)
     E = (-(sys.J * P)) - (sys.h * M)
     if isinstance(sys, BlumeCapelDevice):
@@ -383,6 +435,9 @@ def energy(sys, full=False):
 
 
 def magnetization(sys, full=False):
+    if _is_graph(sys):
+        from . import graph as G
+        return G.energy(sys, full)[1]
     return observables(sys, full)[1]
 
 
@@ -391,7 +446,11 @@ def sweep_(sys, alg, nsweeps=1, record=False):
 
     Updates ``alg.steps`` / ``alg.accepted`` (HeatBath: ``steps``, ``flips``) and the
     rng counter.  With ``record=True`` returns the per-sweep (pair, spin, spin2) series
-    as an int64 array of shape (nsweeps, 3)."""
+    as an int64 array of shape (nsweeps, 3); on a general graph, colour-class sweeps
+    returning (E float64[nsweeps], M int64[nsweeps])."""
+    if _is_graph(sys):
+        from . import graph as G
+        return G.sweep(sys, alg, nsweeps, record)
     beta = alg.beta
     rng = alg.rng._c()
     cnt = L.mcx_counters(0, 0)

@@ -110,6 +110,19 @@ SIGNATURES = {
     "mcx_flathist_get_visited": (C.c_int, [_P, _P, C.c_int64]),
     "mcx_flathist_set_visited": (C.c_int, [_P, _P, C.c_int64]),
     "mcx_wait_flag_test": (C.c_int, [_P, C.c_int64]),
+    "mcx_graph_create": (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, _P, C.c_double, C.POINTER(_P)]),
+    "mcx_graph_destroy": (C.c_int, [_P]),
+    "mcx_graph_info": (C.c_int, [_P, _i64p, _i32p, _i64p, _i64p]),
+    "mcx_graph_colours": (C.c_int, [_P, _P, C.c_size_t]),
+    "mcx_graph_set_spins": (C.c_int, [_P, _P, C.c_size_t]),
+    "mcx_graph_get_spins": (C.c_int, [_P, _P, C.c_size_t]),
+    "mcx_graph_init_random": (C.c_int, [_P, C.c_uint64, C.c_uint32]),
+    "mcx_graph_init_uniform": (C.c_int, [_P, C.c_int8]),
+    "mcx_graph_energy": (C.c_int, [_P, C.c_int, _f64p, _i64p]),
+    "mcx_graph_delta_energy": (C.c_int, [_P, C.c_int64, _f64p]),
+    "mcx_graph_flip": (C.c_int, [_P, C.c_int64]),
+    "mcx_graph_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P, _P,
+                                  C.POINTER(mcx_counters)]),
 }
 
 PT_PERSISTENT, PT_PLAIN = 0, 1

@@ -60,6 +60,23 @@ def lib():
                                       C.c_uint32, C.c_uint64, u64p, u64p]
         L.orc_bench_seq.argtypes = [C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_uint64, C.c_int, C.c_int64, C.POINTER(C.c_double)]
+        vp = C.c_void_p
+        L.orc_exp.argtypes = [C.c_double]
+        L.orc_exp.restype = C.c_double
+        L.orc_logistic.argtypes = [C.c_double]
+        L.orc_logistic.restype = C.c_double
+        L.orc_graph_colour.argtypes = [C.c_int64, i64p, i32p, i32p]
+        L.orc_graph_init_random.argtypes = [i8p, C.c_int64, C.c_uint64, C.c_uint32]
+        L.orc_graph_init_random.restype = None
+        L.orc_graph_delta_energy.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, vp, C.c_double]
+        L.orc_graph_delta_energy.restype = C.c_double
+        L.orc_graph_observables.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, vp, C.c_double,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        L.orc_graph_observables.restype = None
+        L.orc_graph_sweep.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, vp, C.c_double, C.c_int,
+                                      C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_int64), vp, vp,
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
 
@@ -167,6 +184,73 @@ def pt_exchange(betas, pos, stage, x, seed, ladder, t, steps, accepted):
                                np.ascontiguousarray(x, np.float64), seed, ladder, t, steps, accepted)
     assert rc == OK
     return st.value
+
+
+def exp(x):
+    return float(lib().orc_exp(float(x)))
+
+
+def logistic(x):
+    return float(lib().orc_logistic(float(x)))
+
+
+class Graph:
+    """A neighbour list in CSR form for the graph oracle: ``rowptr`` (int64, n+1),
+    ``col`` (int32), optional per-entry couplings ``Jv`` (float64, the IsingMatrix
+    values) and per-site fields ``hv`` (float64)."""
+
+    def __init__(self, rowptr, col, Jv=None, J=1.0, hv=None, h=0.0):
+        self.rowptr = np.ascontiguousarray(rowptr, np.int64)
+        self.col = np.ascontiguousarray(col, np.int32)
+        self.n = len(self.rowptr) - 1
+        self.Jv = None if Jv is None else np.ascontiguousarray(Jv, np.float64)
+        self.hv = None if hv is None else np.ascontiguousarray(hv, np.float64)
+        self.J, self.h = float(J), float(h)
+
+    def _ptrs(self):
+        return (None if self.Jv is None else self.Jv.ctypes.data, None if self.hv is None else self.hv.ctypes.data)
+
+
+def graph_colour(g):
+    c = np.zeros(g.n, np.int32)
+    ncol = lib().orc_graph_colour(g.n, g.rowptr, g.col, c)
+    return c, ncol
+
+
+def graph_init_random(n, seed, stream=0):
+    s = np.zeros(n, np.int8)
+    lib().orc_graph_init_random(s, n, seed, stream)
+    return s
+
+
+def graph_delta_energy(g, s, v):
+    jv, hv = g._ptrs()
+    return float(lib().orc_graph_delta_energy(np.ascontiguousarray(s, np.int8), v, g.rowptr, g.col, jv, g.J, hv,
+                                              g.h))
+
+
+def graph_observables(g, s):
+    jv, hv = g._ptrs()
+    E, M = C.c_double(), C.c_int64()
+    lib().orc_graph_observables(np.ascontiguousarray(s, np.int8), g.n, g.rowptr, g.col, jv, g.J, hv, g.h,
+                                C.byref(E), C.byref(M))
+    return E.value, M.value
+
+
+def graph_sweep(g, s, alg, beta, seed, stream=0, sweep0=0, nsweeps=1):
+    """Colour-class sweeps in place on ``s``; returns (E[nsweeps], M[nsweeps], attempts, accepts)
+    with E and M the cached observables tracked from a full recompute before the first sweep."""
+    jv, hv = g._ptrs()
+    E0, M0 = graph_observables(g, s)
+    E, M = C.c_double(E0), C.c_int64(M0)
+    Es = np.zeros(nsweeps, np.float64)
+    Ms = np.zeros(nsweeps, np.int64)
+    att, acc = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_graph_sweep(s, g.n, g.rowptr, g.col, jv, g.J, hv, g.h, alg, beta, seed, stream, sweep0, nsweeps,
+                               C.byref(E), C.byref(M), Es.ctypes.data, Ms.ctypes.data, C.byref(att), C.byref(acc))
+    if rc != OK:
+        raise ValueError("oracle graph_sweep failed: %d" % rc)
+    return Es, Ms, att.value, acc.value
 
 
 def bench_seq(model, L, alg, beta, seed, nthreads, attempts_per_thread, J=1.0, D=0.0, h=0.0):

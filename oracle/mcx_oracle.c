@@ -626,3 +626,207 @@ int orc_bench_seq(int model, int dim, const int32_t* L, int alg, double beta, do
     free(th);
     return rc;
 }
+
+/* ---------------------------------------------------------------------------
+ * General graphs and couplings: IsingGraph (one J over a neighbour list,
+ * SpinSystems/src/ising.jl:86-139) and IsingMatrix (symmetric sparse J_ij,
+ * ising.jl:221-292), each with no field, a uniform field or a field per site.
+ * ------------------------------------------------------------------------- */
+
+/* exp(x): Cody & Waite argument reduction x = k ln2 + r, |r| <= ln2/2, with ln2 split
+ * into a 32-bit head (k * head exact) and a tail; exp(r) from its Taylor series up to
+ * r^13/13! in Horner form; then the exponent of 2^k is put in with one or two exact
+ * scalings.  Plain multiplies and adds only, so every machine gives the same bits. */
+double orc_exp(double x) {
+    if (x != x) return x;
+    if (x > 709.782712893384) return INFINITY;
+    if (x < -745.2) return 0.0;
+    double kd = floor(x * 0x1.71547652b82fep+0 + 0.5);
+    double r = (x - kd * 0x1.62e42fee00000p-1) - kd * 0x1.a39ef35793c76p-33;
+    double p = 0x1.6124613a86d09p-33;
+    p = p * r + 0x1.1eed8eff8d898p-29;
+    p = p * r + 0x1.ae64567f544e4p-26;
+    p = p * r + 0x1.27e4fb7789f5cp-22;
+    p = p * r + 0x1.71de3a556c734p-19;
+    p = p * r + 0x1.a01a01a01a01ap-16;
+    p = p * r + 0x1.a01a01a01a01ap-13;
+    p = p * r + 0x1.6c16c16c16c17p-10;
+    p = p * r + 0x1.1111111111111p-7;
+    p = p * r + 0x1.5555555555555p-5;
+    p = p * r + 0x1.5555555555555p-3;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    int k = (int)kd;
+    if (k > 1023) return (p * ldexp(1.0, k - 1)) * 2.0;
+    if (k < -1021) return (p * ldexp(1.0, k + 64)) * 0x1p-64;
+    return p * ldexp(1.0, k);
+}
+
+/* logistic(x), src/infrastructure/utils.jl:82-88, on orc_exp */
+double orc_logistic(double x) {
+    if (x >= 0) return 1.0 / (1.0 + orc_exp(-x));
+    double ex = orc_exp(x);
+    return ex / (1.0 + ex);
+}
+
+/* First-fit colouring in vertex order: a vertex takes the smallest colour that none of
+ * its lower-numbered neighbours holds.  Diagonal entries are not neighbours.  Returns
+ * the number of colours. */
+int orc_graph_colour(int64_t n, const int64_t* rowptr, const int32_t* col, int32_t* colour) {
+    int64_t maxdeg = 0;
+    for (int64_t v = 0; v < n; ++v)
+        if (rowptr[v + 1] - rowptr[v] > maxdeg) maxdeg = rowptr[v + 1] - rowptr[v];
+    int64_t* seen = (int64_t*)malloc((size_t)(maxdeg + 2) * sizeof(int64_t));
+    for (int64_t c = 0; c < maxdeg + 2; ++c) seen[c] = -1;
+    int ncol = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+            int64_t u = col[e];
+            if (u < v) seen[colour[u]] = v;
+        }
+        int c = 0;
+        while (seen[c] == v) ++c;
+        colour[v] = c;
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    free(seen);
+    return ncol;
+}
+
+/* init!(sys, :random) for a graph: site v takes the top bit of word v&3 of the Philox
+ * block (v>>2, 0, 8<<24, stream). */
+void orc_graph_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int64_t v = 0; v < n; ++v) {
+        uint32_t ctr[4] = {(uint32_t)(v >> 2), 0u, 8u << 24, stream}, out[4];
+        orc_philox4x32_10(ctr, key, out);
+        s[v] = (out[v & 3] & 0x80000000u) ? 1 : -1;
+    }
+}
+
+/* local_pair_interactions: abstractions.jl:41-48 (integer sum over the neighbour list)
+ * and ising.jl:294-304 (FP64 sum of s_i J_ij s_j over the stored entries, j != i). */
+static double graph_dpair(const int8_t* s, int64_t v, const int64_t* rowptr, const int32_t* col,
+                          const double* Jv, double J) {
+    int si = s[v];
+    if (Jv) {
+        double acc = 0.0;
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+            if (col[e] == v) continue;
+            acc += ((double)si * Jv[e]) * (double)s[col[e]];
+        }
+        return -2.0 * acc;  /* flip_changes, ising.jl:351-356 */
+    }
+    int64_t lpi = 0;
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+        if (col[e] != v) lpi += si * s[col[e]];
+    return (-2.0 * J) * (double)lpi;  /* flip_changes, ising.jl:187-191 */
+}
+
+/* delta_energy, ising.jl:198 and :362: -Δpair - h Δspin */
+static double graph_delta_energy(const int8_t* s, int64_t v, const int64_t* rowptr,
+                                 const int32_t* col, const double* Jv, double J,
+                                 const double* hv, double h) {
+    double dpair = graph_dpair(s, v, rowptr, col, Jv, J);
+    double dspin = (double)(-2 * s[v]);
+    if (hv) return -dpair - hv[v] * dspin;
+    if (h != 0.0) return -dpair - h * dspin;
+    return -dpair;
+}
+
+double orc_graph_delta_energy(const int8_t* s, int64_t v, const int64_t* rowptr,
+                              const int32_t* col, const double* Jv, double J, const double* hv,
+                              double h) {
+    return graph_delta_energy(s, v, rowptr, col, Jv, J, hv, h);
+}
+
+/* _full_energy and magnetization, ising.jl:161-185 and :306-322: -pair - field */
+void orc_graph_observables(const int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                           const double* Jv, double J, const double* hv, double h, double* E,
+                           int64_t* M) {
+    double pair;
+    if (Jv) {
+        double acc = 0.0;
+        for (int64_t v = 0; v < n; ++v) acc += -0.5 * graph_dpair(s, v, rowptr, col, Jv, J);
+        pair = acc / 2;
+    } else {
+        int64_t acc = 0;
+        for (int64_t v = 0; v < n; ++v)
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+                if (col[e] != v) acc += s[v] * s[col[e]];
+        pair = J * (double)(acc / 2);
+    }
+    int64_t m = 0;
+    double field = 0.0;
+    for (int64_t v = 0; v < n; ++v) {
+        m += s[v];
+        if (hv) field += hv[v] * (double)s[v];
+    }
+    if (!hv) field = h * (double)m;
+    *E = -pair - field;
+    *M = m;
+}
+
+/* Colour-class sweeps.  Sweep t visits colour 0, 1, ... in turn and, inside a colour, the
+ * sites in increasing order; q counts the visits of the sweep, and site q takes the 53-bit
+ * uniform from words 0 and 1 of the Philox block (q, t lo, t hi16 | 7<<24, stream).  Sites
+ * of one colour share no edge, so any order inside a colour gives the same result.
+ *   Metropolis: accept!(alg, ΔE), metropolis.jl:14-17 with _accept!,
+ *               importance_sampling.jl:80-85: lr = -β ΔE; lr > 0 or u < exp(lr).
+ *   Glauber:    metropolis.jl:121-127: u < logistic(lr).
+ *   HeatBath:   spin_flip!(::AbstractIsing, ::AbstractHeatBath), ising.jl:43-58:
+ *               p_plus = logistic(β s_old ΔE); s_new = u < p_plus ? +1 : -1.
+ * E and M are the cached observables, updated by modify! (ising.jl:200-218, :364-377).
+ * E_series / M_series (may be NULL) get the values after each sweep. */
+int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                    const double* Jv, double J, const double* hv, double h, int alg, double beta,
+                    uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps, double* E,
+                    int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
+                    uint64_t* accepts) {
+    if (alg < ORC_METROPOLIS || alg > ORC_HEATBATH || n < 1) return ORC_ERR_INVALID;
+    int32_t* colour = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    int ncol = orc_graph_colour(n, rowptr, col, colour);
+    int64_t* order = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    int64_t q = 0;
+    for (int c = 0; c < ncol; ++c)
+        for (int64_t v = 0; v < n; ++v)
+            if (colour[v] == c) order[q++] = v;
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint64_t acc_n = 0;
+    for (int64_t t = 0; t < nsweeps; ++t) {
+        uint64_t sw = sweep0 + (uint64_t)t;
+        for (q = 0; q < n; ++q) {
+            int64_t v = order[q];
+            uint32_t ctr[4] = {(uint32_t)q, (uint32_t)sw,
+                               ((uint32_t)(sw >> 32) & 0xFFFFu) | (7u << 24), stream}, out[4];
+            orc_philox4x32_10(ctr, key, out);
+            double u = u53(out[0], out[1]);
+            int so = s[v];
+            double dE = graph_delta_energy(s, v, rowptr, col, Jv, J, hv, h);
+            int flip;
+            if (alg == ORC_METROPOLIS) {
+                double lr = -beta * dE;
+                flip = (lr > 0) || (u < orc_exp(lr));
+            } else if (alg == ORC_GLAUBER) {
+                flip = u < orc_logistic(-beta * dE);
+            } else {
+                int up = u < orc_logistic((beta * (double)so) * dE);
+                flip = up != (so == 1);
+            }
+            if (flip) {
+                s[v] = (int8_t)(-so);
+                *E += dE;
+                *M += -2 * so;
+                ++acc_n;
+            }
+        }
+        if (E_series) E_series[t] = *E;
+        if (M_series) M_series[t] = *M;
+    }
+    *attempts += (uint64_t)n * (uint64_t)nsweeps;
+    *accepts += acc_n;
+    free(order);
+    free(colour);
+    return ORC_OK;
+}

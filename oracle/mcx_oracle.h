@@ -69,6 +69,23 @@ int orc_pt_exchange(int n, const double* betas, int32_t* pos, int32_t* stage,
                     const double* x, uint64_t seed, uint32_t ladder, uint64_t t,
                     uint64_t* steps, uint64_t* accepted);
 
+/* general graphs and couplings (IsingGraph / IsingMatrix); Jv / hv may be NULL */
+double orc_exp(double x);
+double orc_logistic(double x);
+int orc_graph_colour(int64_t n, const int64_t* rowptr, const int32_t* col, int32_t* colour);
+void orc_graph_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream);
+double orc_graph_delta_energy(const int8_t* s, int64_t v, const int64_t* rowptr,
+                              const int32_t* col, const double* Jv, double J, const double* hv,
+                              double h);
+void orc_graph_observables(const int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                           const double* Jv, double J, const double* hv, double h, double* E,
+                           int64_t* M);
+int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                    const double* Jv, double J, const double* hv, double h, int alg, double beta,
+                    uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps, double* E,
+                    int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
+                    uint64_t* accepts);
+
 /* CPU baseline: nthreads independent chains in sequential random-site order */
 int orc_bench_seq(int model, int dim, const int32_t* L, int alg, double beta, double J,
                   double D, double h, uint64_t seed, int nthreads, int64_t attempts_per_thread,

@@ -187,10 +187,13 @@ def test_known_answers_through_the_abi(gpu):
 
 
 def test_argument_errors(gpu):
+    # the colour-split lattice needs even sides >= 4 (other grids run as general graphs)
     with pytest.raises(gpu.ArgumentError):
-        gpu.Ising([5, 8])
+        gpu.IsingLatticeOptim(5, 8)
     with pytest.raises(gpu.ArgumentError):
-        gpu.Ising([2, 8])
+        gpu.IsingDevice([2, 8])
+    with pytest.raises(gpu.ArgumentError):
+        gpu.Ising([5, 8], layout="msc64")
     with pytest.raises(gpu.ArgumentError):
         gpu.Ising([64, 64], layout="msc64")  # Lx must be a multiple of 128
     sys_ = gpu.Ising([8, 8])
