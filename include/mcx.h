@@ -374,9 +374,10 @@ MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i);
  * src/algorithms/metropolis.jl:14-17, :121-127, importance_sampling.jl:80-85): the
  * reference's FP64 decisions -- Metropolis lr = -beta*ΔE, accept if lr > 0 or
  * u < exp(lr); Glauber u < logistic(lr); HeatBath s = u < logistic(beta*s*ΔE) ? +1 : -1
- * -- with u a 53-bit uniform from Philox block (q, sweep lo, sweep hi16 | 7<<24, stream)
- * for the q-th site the sweep visits, and exp the library's own (bit-identical on host
- * and device).
+ * -- with exp the library's own (bit-identical on host and device) and u a 53-bit
+ * uniform: the l-th site of colour class c takes words 2b, 2b+1 (b = (l>>5)&1) of the
+ * Philox block (B, sweep lo, sweep hi16 | 7<<24, stream), B = B_c + 32 (l>>6) + (l&31),
+ * B_c the sum of 32 ceil(n_c'/64) over the earlier classes.
  *   E_series: host float64[nsweeps] of the cached energy after each sweep, or NULL.
  *   M_series: host int64[nsweeps] of the magnetization after each sweep, or NULL.
  *   counters: accumulated (HeatBath: accepted = spins that changed), or NULL. */

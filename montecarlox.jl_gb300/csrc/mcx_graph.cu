@@ -39,13 +39,17 @@ struct GraphDev {
     int8_t* spins;                  // padded positions, renumbered order
     const int32_t* nbr;             // sliced-ELL neighbour positions (-1 = padding)
     const double* J64;              // per entry (IsingMatrix), or nullptr
+    const float2* J2;               // the same couplings split hi + lo, or nullptr
     const long long* soff;          // nslices + 1 entry offsets
     const double* h;                // per position (vector field), or nullptr
+    const float2* h2;               // the same split hi + lo, or nullptr
     double J, hu;                   // uniform coupling, uniform field
+    float2 J2u, h2u;                // the same split hi + lo
     const unsigned long long* tab;  // thresholds by (s > 0, lpi + dmax)
-    const double* tabdE;            // ΔE by (s > 0, lpi + dmax)
+    const float2* tabdE;            // ΔE (hi + lo) by (s > 0, lpi + dmax)
     int dmax;
     double beta;
+    float beta32;
     unsigned long long* acc;        // accepted moves
     long long* M;                   // cached magnetization
     double* E;                      // cached energy
@@ -55,7 +59,7 @@ struct GraphDev {
 struct GClass {
     long long p0;       // first padded position of the class
     long long count;    // sites of the class
-    long long q0;       // visits before this class in a sweep
+    long long blk0;     // first Philox block of the class
     long long slice0;   // first slice
     long long nslices;
     int part0;          // first partial-sum slot
@@ -83,82 +87,240 @@ __device__ __forceinline__ long long warp_sum_i64(long long v) {
     return v;
 }
 
-// ΔE of the site at padded position p (lane of its slice), the reference's
-// flip_changes + delta_energy: -Δpair - h Δspin with Δpair = -2 acc (IsingMatrix) or
-// -2 J lpi (IsingGraph), Δspin = -2 s.
+// Float-float accumulation (s_hi, s_lo) += (x_hi, x_lo): Knuth's two-sum of the high
+// parts, the low parts added to its error, then a fast renormalisation.
+__device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl) {
+    const float t = sh + xh;
+    const float bb = t - sh;
+    const float e = (sh - (t - bb)) + (xh - bb);
+    const float u = e + (sl + xl);
+    sh = t + u;
+    sl = u - (sh - t);
+}
+
+// ΔE of the site at padded position p in FP64 exactly as the reference: flip_changes +
+// delta_energy, -Δpair - h Δspin with Δpair = -2 acc (IsingMatrix, acc the sequential
+// FP64 sum of s_i J_ij s_j over the row) or -2 J lpi (IsingGraph), Δspin = -2 s.
 template <bool EDGEJ, int FIELD>
-__device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long p, int si, double acc, int lpi) {
-    const double dpair = EDGEJ ? -2.0 * acc : (-2.0 * g.J) * (double)lpi;
+__device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long p, long long off, int w, int lane,
+                                                    int si, int lpi) {
+    double dpair;
+    if (EDGEJ) {
+        double acc = 0.0;
+        for (int k = 0; k < w; ++k) {
+            const long long e = off + 32ll * k + lane;
+            const int nb = g.nbr[e];
+            if (nb >= 0) {
+                const double Jk = g.J64[e];
+                acc += (si * g.spins[nb] > 0) ? Jk : -Jk;  // (s_i J) s_j: exact sign flips
+            }
+        }
+        dpair = -2.0 * acc;
+    } else {
+        dpair = (-2.0 * g.J) * (double)lpi;
+    }
     const double dspin = (double)(-2 * si);
     if (FIELD == F_VECTOR) return -dpair - g.h[p] * dspin;
     if (FIELD == F_UNIFORM) return -dpair - g.hu * dspin;
     return -dpair;
 }
 
-// One colour class of one sweep.  A warp takes one 32-site slice per step.
+// The reference's FP64 decision for one site (the exact path, taken when the FP32 test
+// below cannot decide).  Returns the flip and ΔE.
+template <int ALG, bool EDGEJ, int FIELD>
+__device__ __noinline__ bool exact_site(const GraphDev& g, long long p, long long off, int w, int lane, int si,
+                                        int lpi, unsigned long long ku, double* dE_out) {
+    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, off, w, lane, si, lpi);
+    *dE_out = dE;
+    const double u = (double)ku * 0x1p-53;
+    if (ALG == MCX_METROPOLIS) {
+        const double lr = -g.beta * dE;
+        return (lr > 0) || (u < mcx_exp(lr));
+    }
+    if (ALG == MCX_GLAUBER) return u < mcx_logistic(-g.beta * dE);
+    const bool up = u < mcx_logistic((g.beta * (double)si) * dE);
+    return up != (si == 1);
+}
+
+// Certified FP32 decision of "u < p" where p = exp(x) (Metropolis, x <= 0 or accept) or
+// p = logistic(x), x the FP64 argument of the reference and xf an FP32 estimate with
+// |xf - x| <= errx.  u = w0 2^-32 + (low bits) >= w0 2^-32 and < (w0+1) 2^-32.  With
+// pe the fast estimate of p -- __expf errs by at most 2 + 1.173 |x| ulp (CUDA programming
+// guide), the FP32 addition and division by half an ulp each -- every p compatible with
+// the bounds lies in pe (1 -+ m), m taken with a factor 2 or more on each term.  Returns
+// 1 (u < p for sure), 0 (u >= p for sure) or -1 (undecided).  Outputs of __expf that
+// flush to 0 or overflow leave pe = 0 (p below 2^-120: only w0 = 0 stays undecided) or
+// pe = 1 (p above 1 - 2^-120).
+template <bool LOGISTIC>
+__device__ __forceinline__ int certain_below(float xf, float errx, uint32_t w0) {
+    const float m = errx * 1.01f + fabsf(xf) * 0x1p-22f + 0x1p-19f;
+    if (!(m < 0x1p-8f)) return -1;
+    float pe;
+    if (LOGISTIC) {
+        pe = 1.0f / (1.0f + __expf(-xf));
+    } else {
+        if (xf > errx) return 1;  // x > 0: always accepted
+        pe = __expf(fminf(xf, 0.0f));
+    }
+    const float A = pe * (1.0f - 2.0f * m) * 4294967296.0f;
+    const uint32_t a = A >= 4294967040.0f ? 4294967040u : (uint32_t)A;
+    if (w0 < a) return 1;
+    const float B = pe * (1.0f + 2.0f * m) * 4294967296.0f;
+    if (B >= 4294967040.0f) return -1;
+    const uint32_t b = max((uint32_t)ceilf(B), 1u);
+    return w0 >= b ? 0 : -1;
+}
+
+// Row sums of one site: the integer lpi (IsingGraph) or the float-float sum of
+// s_i J_ij s_j from the split couplings with the bound S = Σ |J_hi| (IsingMatrix).
+struct RowSum {
+    int lpi;
+    float ah, al, S;
+};
+
+// Gathers four entries at a time: every load of a group is issued before any is used.
+template <bool EDGEJ>
+__device__ __forceinline__ void row_sum(const GraphDev& g, long long off, int w, int lane, int si, RowSum& r) {
+    r.lpi = 0;
+    r.ah = r.al = r.S = 0.0f;
+    for (int k = 0; k < w; k += 4) {
+        int nb[4];
+        float2 Jk[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long e = off + 32ll * (k + j) + lane;
+            nb[j] = k + j < w ? __ldg(g.nbr + e) : -1;
+            if (EDGEJ) Jk[j] = k + j < w ? __ldg(g.J2 + e) : make_float2(0.0f, 0.0f);
+        }
+        int sj[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sj[j] = nb[j] >= 0 ? (int)__ldg(g.spins + nb[j]) : 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (EDGEJ) {
+                if (nb[j] >= 0) {
+                    const bool pos = si * sj[j] > 0;
+                    const float xh = pos ? Jk[j].x : -Jk[j].x;
+                    const float xl = pos ? Jk[j].y : -Jk[j].y;
+                    const float t = r.ah + xh;
+                    const float bb = t - r.ah;
+                    r.al += ((r.ah - (t - bb)) + (xh - bb)) + xl;
+                    r.ah = t;
+                    r.S += fabsf(Jk[j].x);
+                }
+            } else {
+                r.lpi += si * sj[j];
+            }
+        }
+    }
+}
+
+// One site: ΔE in float-float, the certified FP32 decision, the exact FP64 one when that
+// cannot decide.  Returns the flip; (eh, el) accumulates ΔE of flipped sites.
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__device__ __forceinline__ bool decide_site(const GraphDev& g, long long p, long long off, int w, int lane, int si,
+                                            const RowSum& r, uint32_t whi, uint32_t wlo, float& eh, float& el) {
+    const unsigned long long ku = ((unsigned long long)whi << 21) | (unsigned long long)(wlo >> 11);
+    if (TABLE) {
+        const int idx = (si > 0 ? 2 * g.dmax + 1 : 0) + r.lpi + g.dmax;
+        const bool below = ku < g.tab[idx];
+        const bool flip = ALG == MCX_HEATBATH ? (below != (si == 1)) : below;
+        if (flip) {
+            const float2 d = g.tabdE[idx];
+            ff_add(eh, el, d.x, d.y);
+        }
+        return flip;
+    }
+    // ΔE = 2 acc + 2 s h (acc = Σ s_i J_ij s_j or J lpi) as float-float
+    float dh, dl, S;
+    if (EDGEJ) {
+        dh = 2.0f * r.ah;
+        dl = 2.0f * r.al;
+        S = r.S;
+    } else {
+        const float lf = (float)r.lpi, j2 = 2.0f * g.J2u.x;
+        dh = lf * j2;
+        dl = __fmaf_rn(lf, j2, -dh) + lf * (2.0f * g.J2u.y);
+        S = fabsf(dh);
+    }
+    float hm = 0.0f;
+    if (FIELD != F_NONE) {
+        const float2 hv = FIELD == F_VECTOR ? g.h2[p] : g.h2u;
+        const float sg = (float)(2 * si);
+        ff_add(dh, dl, sg * hv.x, sg * hv.y);
+        hm = fabsf(hv.x);
+    }
+    // |df - ΔE_FP64| <= errd: df rounds the float-float value (2^-24 |df|); the float-float
+    // row sum is within 2 (w+1)^2 2^-48 S of the exact one (the low word collects up to w
+    // two-sum errors of at most 2^-24 S each, each addition rounding it by 2^-24); the FP64
+    // reference sum is within w 2^-52 (2S + 2|h|) of the exact one.
+    const float df = dh + dl;
+    const float wf = (float)(w + 1);
+    const float errd = (2.0f * S + 2.0f * hm + fabsf(df)) * 0x1p-20f + wf * wf * S * 0x1p-46f;
+    float xf;
+    if (ALG == MCX_HEATBATH) xf = (g.beta32 * (float)si) * df;
+    else xf = -g.beta32 * df;
+    const float errx = fabsf(g.beta32) * errd * 1.01f + fabsf(xf) * 0x1p-21f + 0x1p-126f;
+    const int c = certain_below<ALG != MCX_METROPOLIS>(xf, errx, whi);
+    bool flip;
+    if (c >= 0) {
+        flip = ALG == MCX_HEATBATH ? ((c == 1) != (si == 1)) : c == 1;
+        if (flip) ff_add(eh, el, dh, dl);
+    } else {
+        double dE;
+        flip = exact_site<ALG, EDGEJ, FIELD>(g, p, off, w, lane, si, r.lpi, ku, &dE);
+        if (flip) {
+            const float h = __double2float_rn(dE);
+            ff_add(eh, el, h, __double2float_rn(dE - (double)h));
+        }
+    }
+    return flip;
+}
+
+// One colour class of one sweep.  A warp takes two 32-site slices (2j, 2j+1) per step;
+// lane l draws one Philox block, blk0 + 32 j + l, whose words 0-1 feed its site in slice
+// 2j and words 2-3 its site in slice 2j+1.
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
 __global__ void __launch_bounds__(kGraphBlock) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
                                                              uint32_t stream, unsigned long long sweep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t w2 = ctr_word2(sweep, 0, P_GRAPH);
-    double dEsum = 0.0;
+    const long long npairs = (c.nslices + 1) >> 1;
+    float eh = 0.0f, el = 0.0f;
     long long dM = 0;
     long long nacc = 0;
-    for (long long sl = (long long)blockIdx.x * kSlicesPerBlock + warp; sl < c.nslices;
-         sl += (long long)gridDim.x * kSlicesPerBlock) {
-        const long long s = c.slice0 + sl;
-        const long long p = s * 32 + lane;
-        const long long local = p - c.p0;
-        const long long off = g.soff[s];
-        const int w = (int)((g.soff[s + 1] - off) >> 5);
-        const int si = g.spins[p];
-        int lpi = 0;
-        double acc = 0.0;
-        for (int k = 0; k < w; ++k) {
-            const long long e = off + 32ll * k + lane;
-            const int nb = g.nbr[e];
-            if (nb >= 0) {
-                const int sj = g.spins[nb];
-                if (EDGEJ) {
-                    const double Jk = g.J64[e];
-                    acc += (si * sj > 0) ? Jk : -Jk;  // (s_i J) s_j, exact sign flips
-                } else {
-                    lpi += si * sj;
-                }
+    for (long long j = (long long)blockIdx.x * kSlicesPerBlock + warp; j < npairs;
+         j += (long long)gridDim.x * kSlicesPerBlock) {
+        const long long sA = c.slice0 + 2 * j;
+        const bool hasB = 2 * j + 1 < c.nslices;
+        const long long pA = sA * 32 + lane, pB = pA + 32;
+        const long long lA = 64 * j + lane, lB = lA + 32;  // class-local indices
+        // slice sA + 1 exists (it is slice B or the first of the next class or the end mark)
+        const long long offA = g.soff[sA], offB = g.soff[sA + 1];
+        const int wA = (int)((offB - offA) >> 5);
+        const int wB = hasB ? (int)((g.soff[sA + 2] - offB) >> 5) : 0;
+        const int siA = g.spins[pA];
+        const int siB = hasB ? (int)g.spins[pB] : 0;
+        RowSum rA, rB;
+        row_sum<EDGEJ>(g, offA, wA, lane, siA, rA);
+        row_sum<EDGEJ>(g, offB, wB, lane, siB, rB);
+        const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
+        if (lA < c.count) {
+            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, pA, offA, wA, lane, siA, rA, r.x, r.y, eh, el)) {
+                g.spins[pA] = (int8_t)(-siA);
+                dM += -2 * siA;
+                ++nacc;
             }
         }
-        if (local < c.count) {
-            const uint4 r = philox10(make_uint4((uint32_t)(c.q0 + local), (uint32_t)sweep, w2, stream), k0, k1);
-            const unsigned long long ku = ((unsigned long long)r.x << 21) | (unsigned long long)(r.y >> 11);
-            bool flip;
-            double dE;
-            if (TABLE) {
-                const int idx = (si > 0 ? 2 * g.dmax + 1 : 0) + lpi + g.dmax;
-                const bool below = ku < g.tab[idx];
-                flip = ALG == MCX_HEATBATH ? (below != (si == 1)) : below;
-                dE = g.tabdE[idx];
-            } else {
-                dE = site_delta_energy<EDGEJ, FIELD>(g, p, si, acc, lpi);
-                const double u = (double)ku * 0x1p-53;
-                if (ALG == MCX_METROPOLIS) {
-                    const double lr = -g.beta * dE;
-                    flip = (lr > 0) || (u < mcx_exp(lr));
-                } else if (ALG == MCX_GLAUBER) {
-                    flip = u < mcx_logistic(-g.beta * dE);
-                } else {
-                    const bool up = u < mcx_logistic((g.beta * (double)si) * dE);
-                    flip = up != (si == 1);
-                }
-            }
-            if (flip) {
-                g.spins[p] = (int8_t)(-si);
-                dEsum += dE;
-                dM += -2 * si;
+        if (lB < c.count) {
+            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, pB, offB, wB, lane, siB, rB, r.z, r.w, eh, el)) {
+                g.spins[pB] = (int8_t)(-siB);
+                dM += -2 * siB;
                 ++nacc;
             }
         }
     }
-    const double t = block_sum_f64(dEsum);
+    const double t = block_sum_f64((double)eh + (double)el);
     if (threadIdx.x == 0) g.part[c.part0 + blockIdx.x] = t;
     dM = warp_sum_i64(dM);
     nacc = warp_sum_i64(nacc);
@@ -258,22 +420,13 @@ __global__ void k_graph_site(GraphDev g, long long p, int op, double* out) {
     const long long off = g.soff[s];
     const int w = (int)((g.soff[s + 1] - off) >> 5);
     const int si = g.spins[p];
-    double acc = 0.0;
     int lpi = 0;
-    for (int k = 0; k < w; ++k) {
-        const long long e = off + 32ll * k + lane;
-        const int nb = g.nbr[e];
-        if (nb >= 0) {
-            const int sj = g.spins[nb];
-            if (EDGEJ) {
-                const double Jk = g.J64[e];
-                acc += (si * sj > 0) ? Jk : -Jk;
-            } else {
-                lpi += si * sj;
-            }
+    if (!EDGEJ)
+        for (int k = 0; k < w; ++k) {
+            const int nb = g.nbr[off + 32ll * k + lane];
+            if (nb >= 0) lpi += si * g.spins[nb];
         }
-    }
-    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, si, acc, lpi);
+    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, off, w, lane, si, lpi);
     *out = dE;
     if (op == 1) {
         g.spins[p] = (int8_t)(-si);
@@ -355,6 +508,12 @@ void site_launch(int field, cudaStream_t st, const GraphDev& g, long long p, int
 }
 
 // 53-bit threshold of "u < p" for u = k 2^-53: k < ceil(p 2^53).
+// x = hi + lo with hi = fl32(x), lo = fl32(x - hi)
+float2 split2(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
 unsigned long long threshold53(double p) {
     if (!(p > 0.0)) return 0;
     if (p >= 1.0) return 1ull << 53;
@@ -378,12 +537,14 @@ struct mcx_graph {
     int8_t* d_spins = nullptr;
     int32_t* d_nbr = nullptr;
     double* d_J64 = nullptr;
+    float2* d_J2 = nullptr;
+    float2* d_h2 = nullptr;
     long long* d_soff = nullptr;
     double* d_h = nullptr;
     int32_t* d_perm = nullptr;      // vertex -> padded position
     int8_t* d_lin = nullptr;        // staging, vertex order
     unsigned long long* d_tab = nullptr;
-    double* d_tabdE = nullptr;
+    float2* d_tabdE = nullptr;
     int tab_alg = -1;
     double tab_beta = 0.0;
     double* d_E = nullptr;
@@ -405,6 +566,11 @@ struct mcx_graph {
         g.spins = d_spins;
         g.nbr = d_nbr;
         g.J64 = d_J64;
+        g.J2 = d_J2;
+        g.h2 = d_h2;
+        g.J2u = split2(J);
+        g.h2u = split2(h);
+        g.beta32 = (float)beta;
         g.soff = d_soff;
         g.h = d_h;
         g.J = J;
@@ -469,7 +635,7 @@ mcx_status graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
     if (g->tab_alg == (int)alg && g->tab_beta == beta) return MCX_OK;
     const int D = g->dmax, width = 2 * D + 1;
     std::vector<unsigned long long> thr(2 * (size_t)width);
-    std::vector<double> dE(2 * (size_t)width);
+    std::vector<float2> dE(2 * (size_t)width);
     for (int sp = 0; sp < 2; ++sp) {
         const int s = sp ? 1 : -1;
         for (int lpi = -D; lpi <= D; ++lpi) {
@@ -486,12 +652,12 @@ mcx_status graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
                 t = threshold53(mcx_logistic((beta * (double)s) * de));
             }
             thr[(size_t)sp * width + (lpi + D)] = t;
-            dE[(size_t)sp * width + (lpi + D)] = de;
+            dE[(size_t)sp * width + (lpi + D)] = split2(de);
         }
     }
     MCX_CUDA(cudaMemcpyAsync(g->d_tab, thr.data(), thr.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
                              g->ctx->stream));
-    MCX_CUDA(cudaMemcpyAsync(g->d_tabdE, dE.data(), dE.size() * sizeof(double), cudaMemcpyHostToDevice,
+    MCX_CUDA(cudaMemcpyAsync(g->d_tabdE, dE.data(), dE.size() * sizeof(float2), cudaMemcpyHostToDevice,
                              g->ctx->stream));
     // the host vectors go out of scope: wait for the copies
     MCX_CUDA(cudaStreamSynchronize(g->ctx->stream));
@@ -583,18 +749,18 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
             vert[p] = v;
         }
     }
-    int64_t q0 = 0;
+    int64_t blk0 = 0;
     int part0 = 0;
     const long long cap_blocks = (long long)ctx->num_sms * 8;
     for (int c = 0; c < ncol; ++c) {
         GClass k;
         k.p0 = start[c];
         k.count = count[c];
-        k.q0 = q0;
+        k.blk0 = blk0;
         k.slice0 = start[c] / 32;
         k.nslices = (start[c + 1] - start[c]) / 32;
         k.part0 = part0;
-        q0 += count[c];
+        blk0 += 32 * ((k.nslices + 1) / 2);
         part0 += (int)std::min((k.nslices + kSlicesPerBlock - 1) / kSlicesPerBlock, cap_blocks);
         g->classes.push_back(k);
     }
@@ -626,10 +792,15 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
             }
         }
     std::vector<double> hv;
+    std::vector<float2> hv2;
     if (field) {
         hv.assign(g->npad, 0.0);
         for (int64_t v = 0; v < n; ++v) hv[perm[v]] = field[v];
+        hv2.resize(g->npad);
+        for (int64_t p = 0; p < g->npad; ++p) hv2[p] = split2(hv[p]);
     }
+    std::vector<float2> jv2(jv.size());
+    for (size_t k = 0; k < jv.size(); ++k) jv2[k] = split2(jv[k]);
     // device arrays
     mcx_status st = MCX_OK;
     const size_t tabn = 2 * (size_t)(2 * dmax + 1);
@@ -638,8 +809,10 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
         if ((st = galloc(g, &g->d_spins, (size_t)g->npad))) break;
         if ((st = galloc(g, &g->d_nbr, (size_t)std::max<int64_t>(g->entries, 1)))) break;
         if (g->edgej && (st = galloc(g, &g->d_J64, (size_t)std::max<int64_t>(g->entries, 1)))) break;
+        if (g->edgej && (st = galloc(g, &g->d_J2, (size_t)std::max<int64_t>(g->entries, 1)))) break;
         if ((st = galloc(g, &g->d_soff, (size_t)g->nslices + 1))) break;
         if (field && (st = galloc(g, &g->d_h, (size_t)g->npad))) break;
+        if (field && (st = galloc(g, &g->d_h2, (size_t)g->npad))) break;
         if ((st = galloc(g, &g->d_perm, (size_t)n))) break;
         if ((st = galloc(g, &g->d_lin, (size_t)n))) break;
         if (g->table_mode() && (st = galloc(g, &g->d_tab, tabn))) break;
@@ -666,8 +839,10 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
     up(g->d_spins, spins.data(), spins.size());
     up(g->d_nbr, nbr.data(), nbr.size() * sizeof(int32_t));
     if (g->edgej) up(g->d_J64, jv.data(), jv.size() * sizeof(double));
+    if (g->edgej) up(g->d_J2, jv2.data(), jv2.size() * sizeof(float2));
     up(g->d_soff, soff.data(), soff.size() * sizeof(long long));
     if (field) up(g->d_h, hv.data(), hv.size() * sizeof(double));
+    if (field) up(g->d_h2, hv2.data(), hv2.size() * sizeof(float2));
     up(g->d_perm, perm.data(), perm.size() * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);

@@ -769,9 +769,11 @@ void orc_graph_observables(const int8_t* s, int64_t n, const int64_t* rowptr, co
 }
 
 /* Colour-class sweeps.  Sweep t visits colour 0, 1, ... in turn and, inside a colour, the
- * sites in increasing order; q counts the visits of the sweep, and site q takes the 53-bit
- * uniform from words 0 and 1 of the Philox block (q, t lo, t hi16 | 7<<24, stream).  Sites
- * of one colour share no edge, so any order inside a colour gives the same result.
+ * sites in increasing order.  The l-th site of class c takes its 53-bit uniform from words
+ * 2b and 2b+1, b = (l>>5)&1, of the Philox block (B, t lo, t hi16 | 7<<24, stream) with
+ * B = B_c + 32 (l>>6) + (l&31), where B_c = sum over earlier classes of 32 ceil(n_c'/64):
+ * one block serves the sites l and l+32 of a 64-site group.  Sites of one colour share no
+ * edge, so any order inside a colour gives the same result.
  *   Metropolis: accept!(alg, ΔE), metropolis.jl:14-17 with _accept!,
  *               importance_sampling.jl:80-85: lr = -β ΔE; lr > 0 or u < exp(lr).
  *   Glauber:    metropolis.jl:121-127: u < logistic(lr).
@@ -788,20 +790,32 @@ int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* 
     int32_t* colour = (int32_t*)malloc((size_t)n * sizeof(int32_t));
     int ncol = orc_graph_colour(n, rowptr, col, colour);
     int64_t* order = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    uint64_t* block = (uint64_t*)malloc((size_t)n * sizeof(uint64_t));
+    int* word = (int*)malloc((size_t)n * sizeof(int));
     int64_t q = 0;
-    for (int c = 0; c < ncol; ++c)
+    uint64_t B_c = 0;
+    for (int c = 0; c < ncol; ++c) {
+        int64_t l = 0;
         for (int64_t v = 0; v < n; ++v)
-            if (colour[v] == c) order[q++] = v;
+            if (colour[v] == c) {
+                order[q] = v;
+                block[q] = B_c + 32 * (uint64_t)(l >> 6) + (uint64_t)(l & 31);
+                word[q] = 2 * (int)((l >> 5) & 1);
+                ++q;
+                ++l;
+            }
+        B_c += 32 * (uint64_t)((l + 63) / 64);
+    }
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     uint64_t acc_n = 0;
     for (int64_t t = 0; t < nsweeps; ++t) {
         uint64_t sw = sweep0 + (uint64_t)t;
         for (q = 0; q < n; ++q) {
             int64_t v = order[q];
-            uint32_t ctr[4] = {(uint32_t)q, (uint32_t)sw,
+            uint32_t ctr[4] = {(uint32_t)block[q], (uint32_t)sw,
                                ((uint32_t)(sw >> 32) & 0xFFFFu) | (7u << 24), stream}, out[4];
             orc_philox4x32_10(ctr, key, out);
-            double u = u53(out[0], out[1]);
+            double u = u53(out[word[q]], out[word[q] + 1]);
             int so = s[v];
             double dE = graph_delta_energy(s, v, rowptr, col, Jv, J, hv, h);
             int flip;
@@ -826,6 +840,8 @@ int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* 
     }
     *attempts += (uint64_t)n * (uint64_t)nsweeps;
     *accepts += acc_n;
+    free(word);
+    free(block);
     free(order);
     free(colour);
     return ORC_OK;

@@ -97,20 +97,24 @@ def test_cached_equals_full_after_sweeps(name, g, alg):
 
 
 def test_sweep_order_is_colour_classes():
-    """Colour-class order: site q of the sweep uses Philox block q; swapping the order of
-    two sites inside a class changes nothing, so recomputing sweep 0 by hand agrees."""
-    n, es = grid_edges([6, 4], True)
+    """Colour-class order: the l-th site of class c uses words 2b, 2b+1 (b = (l>>5)&1) of
+    Philox block B_c + 32 (l>>6) + (l&31); recomputing one sweep by hand agrees."""
+    n, es = grid_edges([16, 12], True)
     rp, col, _ = from_edges(n, es)
     g = O.Graph(rp, col, J=1.0, h=0.2)
     s0 = O.graph_init_random(n, 3)
     s = s0.copy()
     O.graph_sweep(g, s, O.METROPOLIS, 0.5, 21, stream=2, sweep0=5, nsweeps=1)
     c, ncol = O.graph_colour(g)
-    order = [v for k in range(ncol) for v in range(n) if c[v] == k]
     t = s0.copy()
-    for q, v in enumerate(order):
-        w = O.philox([q, 5, 7 << 24, 2], [21, 0])
-        u = ((int(w[0]) << 21) | (int(w[1]) >> 11)) * 2.0 ** -53
+    visits, Bc = [], 0
+    for k in range(ncol):
+        members = [v for v in range(n) if c[v] == k]
+        visits += [(v, Bc + 32 * (l >> 6) + (l & 31), 2 * ((l >> 5) & 1)) for l, v in enumerate(members)]
+        Bc += 32 * ((len(members) + 63) // 64)
+    for v, blk, b in visits:
+        w = O.philox([blk, 5, 7 << 24, 2], [21, 0])
+        u = ((int(w[b]) << 21) | (int(w[b + 1]) >> 11)) * 2.0 ** -53
         dE = O.graph_delta_energy(g, t, v)
         lr = -0.5 * dE
         if lr > 0 or u < O.exp(lr):
