@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
-    ap.add_argument("--profile", choices=["pt", "flathist", "serve"], default=None,
+    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph"], default=None,
                     help="run one short workload for a profiler capture and exit (no JSON line)")
     return ap.parse_args()
 
@@ -314,6 +314,99 @@ def bench_serve(mcx, ctx, njobs=40):
     return r
 
 
+def torus_csr(L, seed, per_entry):
+    """CSR of the L x L periodic grid (first coordinate fastest, sorted rows) and, when
+    per_entry, symmetric Gaussian couplings: the 2-D Edwards-Anderson spin glass."""
+    import numpy as np
+    n = L * L
+    v = np.arange(n, dtype=np.int64)
+    x, y = v % L, v // L
+    right, left = y * L + (x + 1) % L, y * L + (x - 1) % L
+    down, up = ((y + 1) % L) * L + x, ((y - 1) % L) * L + x
+    nb = np.stack([right, left, down, up], 1)
+    o = np.argsort(nb, axis=1)
+    nb = np.take_along_axis(nb, o, 1)
+    rowptr = np.arange(n + 1, dtype=np.int64) * 4
+    J = None
+    if per_entry:
+        rng = np.random.default_rng(seed)
+        jh, jv = rng.normal(size=n), rng.normal(size=n)  # edges (v, right(v)), (v, down(v))
+        J = np.take_along_axis(np.stack([jh, jh[left], jv, jv[up]], 1), o, 1).reshape(-1)
+    return rowptr, nb.reshape(-1).astype(np.int32), J
+
+
+GRAPH_L = 4096
+GRAPH_SWEEPS = 50
+
+
+def bench_graph(torch, mcx, ctx, flush, steps, warmup, cpu_seconds, with_cpu):
+    """General-graph sweeps on the 4096^2 torus: the Edwards-Anderson spin glass as an
+    IsingMatrix (Gaussian J_ij, Metropolis at beta 1.0) and the ferromagnet as an
+    IsingGraph (J = 1, beta 0.4407).  Device-timed, L2 flushed between steps; algorithmic
+    bytes per site and sweep = 4 neighbours x (4 B index + 8 B coupling) + 4 neighbour
+    spin reads + own spin read and write (IsingGraph: no couplings)."""
+    from mcx.graph import IsingGraphDevice
+    N = GRAPH_L * GRAPH_L
+    out = {}
+    for name, per_entry, beta, bps in (("ea2d_L4096_matrix_metropolis", True, 1.0, 4 * 12 + 4 + 2),
+                                       ("ferro2d_L4096_graph_metropolis", False, BETA, 4 * 4 + 4 + 2)):
+        rowptr, col, J = torus_csr(GRAPH_L, SEED, per_entry)
+        sysd = IsingGraphDevice(rowptr, col, J, J=1.0, ctx=ctx)
+        mcx.init_(sysd, "random", rng=mcx.Philox(SEED))
+        alg = mcx.Metropolis(mcx.Philox(SEED), beta=beta)
+        lib = mcx._lib.load()
+
+        def step():
+            rng = alg.rng._c()
+            mcx._check(lib.mcx_graph_sweep(sysd.handle, alg.ALG, beta, mcx.C.byref(rng), GRAPH_SWEEPS, None, None,
+                                           None))
+            alg.rng.counter = rng.counter
+
+        for _ in range(warmup):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        info = sysd.info()
+        E_c, E_f = mcx.energy(sysd), mcx.energy(sysd, full=True)
+        sysd.close()
+        sweep_s = tot * 1e-3 / (steps * GRAPH_SWEEPS)
+        peak, peak_kind = measured_peaks()
+        achieved = bps * N / sweep_s / 1e9
+        res = {"attempts_per_ns": N / sweep_s / 1e9, "ms_per_sweep": sweep_s * 1e3, "sweeps_per_step": GRAPH_SWEEPS,
+               "colours": info["colours"], "kernel": "k_graph_class<0,%s>" % ("false,true,0" if per_entry else
+                                                                             "true,false,0"),
+               "alg_bytes_per_site": bps, "achieved_gbs": achieved, "peak_gbs": peak, "frac": achieved / peak,
+               "peak_kind": peak_kind, "cached_minus_full_energy": E_c - E_f}
+        if with_cpu and per_entry:
+            import numpy as np
+
+            import oracle as O
+            Ls = 512
+            rp, cl, Jv = torus_csr(Ls, SEED, True)
+            g = O.Graph(rp, cl, Jv=Jv)
+            sp = O.graph_init_random(Ls * Ls, SEED)
+            ns, t, t0 = 0, 0.0, time.perf_counter()
+            while t < cpu_seconds:
+                O.graph_sweep(g, sp, O.METROPOLIS, beta, SEED, sweep0=ns, nsweeps=4)
+                ns += 4
+                t = time.perf_counter() - t0
+            res["cpu_baseline"] = {"value": Ls * Ls * ns / t / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": "oracle colour-class sweeps (FP64 reference decisions) of a %dx%d "
+                                             "Edwards-Anderson torus, %d sweeps, %.1f s, one thread" % (Ls, Ls, ns, t)}
+        out[name] = res
+    return out
+
+
 def run_mcx(args):
     import numpy as np
     import torch
@@ -410,12 +503,14 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = None
     if not args.no_extras:
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
         msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
+        graph_res = bench_graph(torch, mcx, ctx, flush, max(3, args.steps // 4), 3, min(args.cpu_seconds, 5.0),
+                                rank == 0 and not args.no_cpu_baseline)
     if rank != 0:
         return
     cpu = None
@@ -446,6 +541,7 @@ def run_mcx(args):
         "serving": srv_res,
         "flat_histogram": fh_res,
         "msc64": msc_res,
+        "general_graphs": graph_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -481,6 +577,14 @@ def run_profile_target(args):
         alg = F.Multicanonical(mcx.Philox(SEED), ens)
         F.sweep_walkers_(walkers, alg, 1)
         F.sweep_walkers_(walkers, alg, 2)
+    elif args.profile == "graph":
+        from mcx.graph import IsingGraphDevice
+        rowptr, col, J = torus_csr(2048, SEED, True)  # 4.2M sites, 0.25 GB of neighbour data
+        sysd = IsingGraphDevice(rowptr, col, J, ctx=ctx)
+        mcx.init_(sysd, "random", rng=mcx.Philox(SEED))
+        alg = mcx.Metropolis(mcx.Philox(SEED), beta=1.0)
+        mcx.sweep_(sysd, alg, 2)
+        mcx.sweep_(sysd, alg, 2)
     torch.cuda.synchronize()
 
 

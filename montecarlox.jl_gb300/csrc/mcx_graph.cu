@@ -178,43 +178,6 @@ struct RowSum {
     float ah, al, S;
 };
 
-// Gathers four entries at a time: every load of a group is issued before any is used.
-template <bool EDGEJ>
-__device__ __forceinline__ void row_sum(const GraphDev& g, long long off, int w, int lane, int si, RowSum& r) {
-    r.lpi = 0;
-    r.ah = r.al = r.S = 0.0f;
-    for (int k = 0; k < w; k += 4) {
-        int nb[4];
-        float2 Jk[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const long long e = off + 32ll * (k + j) + lane;
-            nb[j] = k + j < w ? __ldg(g.nbr + e) : -1;
-            if (EDGEJ) Jk[j] = k + j < w ? __ldg(g.J2 + e) : make_float2(0.0f, 0.0f);
-        }
-        int sj[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) sj[j] = nb[j] >= 0 ? (int)__ldg(g.spins + nb[j]) : 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (EDGEJ) {
-                if (nb[j] >= 0) {
-                    const bool pos = si * sj[j] > 0;
-                    const float xh = pos ? Jk[j].x : -Jk[j].x;
-                    const float xl = pos ? Jk[j].y : -Jk[j].y;
-                    const float t = r.ah + xh;
-                    const float bb = t - r.ah;
-                    r.al += ((r.ah - (t - bb)) + (xh - bb)) + xl;
-                    r.ah = t;
-                    r.S += fabsf(Jk[j].x);
-                }
-            } else {
-                r.lpi += si * sj[j];
-            }
-        }
-    }
-}
-
 // One site: ΔE in float-float, the certified FP32 decision, the exact FP64 one when that
 // cannot decide.  Returns the flip; (eh, el) accumulates ΔE of flipped sites.
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
@@ -277,11 +240,69 @@ __device__ __forceinline__ bool decide_site(const GraphDev& g, long long p, long
     return flip;
 }
 
+// Both rows of a slice pair, four entries of each at a time: all index and coupling
+// loads of a group are issued before any spin is gathered, and all gathers before any is
+// used (each row keeps its own order).
+template <bool EDGEJ>
+__device__ __forceinline__ void row_sum2(const GraphDev& g, long long offA, int wA, long long offB, int wB, int lane,
+                                         int siA, int siB, RowSum& rA, RowSum& rB) {
+    rA.lpi = rB.lpi = 0;
+    rA.ah = rA.al = rA.S = rB.ah = rB.al = rB.S = 0.0f;
+    const int wm = max(wA, wB);
+    for (int k = 0; k < wm; k += 4) {
+        int na[4], nb[4];
+        float2 Ja[4], Jb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long ea = offA + 32ll * (k + j) + lane, eb = offB + 32ll * (k + j) + lane;
+            na[j] = k + j < wA ? __ldg(g.nbr + ea) : -1;
+            nb[j] = k + j < wB ? __ldg(g.nbr + eb) : -1;
+            if (EDGEJ) {
+                Ja[j] = k + j < wA ? __ldg(g.J2 + ea) : make_float2(0.0f, 0.0f);
+                Jb[j] = k + j < wB ? __ldg(g.J2 + eb) : make_float2(0.0f, 0.0f);
+            }
+        }
+        int sa[4], sb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            sa[j] = na[j] >= 0 ? (int)__ldg(g.spins + na[j]) : 0;
+            sb[j] = nb[j] >= 0 ? (int)__ldg(g.spins + nb[j]) : 0;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            RowSum& r = h ? rB : rA;
+            const int si = h ? siB : siA;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int nj = h ? nb[j] : na[j];
+                const int sj = h ? sb[j] : sa[j];
+                if (EDGEJ) {
+                    if (nj >= 0) {
+                        const float2 Jk = h ? Jb[j] : Ja[j];
+                        const bool pos = si * sj > 0;
+                        const float xh = pos ? Jk.x : -Jk.x;
+                        const float xl = pos ? Jk.y : -Jk.y;
+                        const float t = r.ah + xh;
+                        const float bb = t - r.ah;
+                        r.al += ((r.ah - (t - bb)) + (xh - bb)) + xl;
+                        r.ah = t;
+                        r.S += fabsf(Jk.x);
+                    }
+                } else {
+                    r.lpi += si * sj;
+                }
+            }
+        }
+    }
+}
+
 // One colour class of one sweep.  A warp takes two 32-site slices (2j, 2j+1) per step;
 // lane l draws one Philox block, blk0 + 32 j + l, whose words 0-1 feed its site in slice
-// 2j and words 2-3 its site in slice 2j+1.
+// 2j and words 2-3 its site in slice 2j+1.  The kernel waits on gathers: the FP32 path
+// is held to 64 registers (4 blocks of 256 per SM), which measured faster than fewer,
+// fatter warps; the table path needs 48.
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
-__global__ void __launch_bounds__(kGraphBlock) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
+__global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
                                                              uint32_t stream, unsigned long long sweep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t w2 = ctr_word2(sweep, 0, P_GRAPH);
@@ -302,8 +323,7 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_class(GraphDev g, GClass 
         const int siA = g.spins[pA];
         const int siB = hasB ? (int)g.spins[pB] : 0;
         RowSum rA, rB;
-        row_sum<EDGEJ>(g, offA, wA, lane, siA, rA);
-        row_sum<EDGEJ>(g, offB, wB, lane, siB, rB);
+        row_sum2<EDGEJ>(g, offA, wA, offB, wB, lane, siA, siB, rA, rB);
         const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
         if (lA < c.count) {
             if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, pA, offA, wA, lane, siA, rA, r.x, r.y, eh, el)) {

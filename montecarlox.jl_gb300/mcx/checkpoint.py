@@ -31,6 +31,10 @@ def export_state(obj):
         return {"kind": "lattice", "model": "bc" if isinstance(obj, BlumeCapelDevice) else "ising",
                 "dims": list(obj.dims), "J": obj.J, "D": obj.D, "h": obj.h, "layout": obj.layout,
                 "spins": obj.spins}
+    from .graph import IsingGraphDevice
+    if isinstance(obj, IsingGraphDevice):
+        return {"kind": "graph", "rowptr": obj.rowptr, "col": obj.col, "coupling": obj.coupling, "J": obj.J,
+                "field": obj.field, "h": obj.h, "spins": obj.spins}
     if isinstance(obj, Philox):
         return {"kind": "rng", "seed": obj.seed, "stream": obj.stream, "counter": obj.counter}
     if isinstance(obj, (Metropolis, Glauber)):
@@ -82,6 +86,12 @@ def import_state(d, ctx=None):
             s = BlumeCapel(d["dims"], J=d["J"], D=d["D"], h=d["h"], ctx=ctx)
         else:
             s = Ising(d["dims"], J=d["J"], h=d["h"], layout=d["layout"], ctx=ctx)
+        s.spins = d["spins"]
+        return s
+    if k == "graph":
+        from .graph import IsingGraphDevice
+        s = IsingGraphDevice(d["rowptr"], d["col"], d["coupling"], J=1.0 if d["J"] is None else d["J"],
+                             h=d["field"] if d["field"] is not None else d["h"], ctx=ctx)
         s.spins = d["spins"]
         return s
     if k in ("Metropolis", "Glauber"):

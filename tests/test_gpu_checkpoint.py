@@ -62,3 +62,25 @@ def test_wang_landau_resume(gpu, tmp_path):
     assert np.array_equal(alg.ensemble.histogram, r.alg.ensemble.histogram)
     assert F.flatness(alg.ensemble) == F.flatness(r.alg.ensemble)
     assert (alg.steps, alg.accepted) == (r.alg.steps, r.alg.accepted)
+
+
+def test_graph_resume(gpu, tmp_path):
+    """An IsingMatrix spin glass with a field per site: the restored run repeats the spins
+    and counters bit for bit; energies agree to FP64 summation order."""
+    from mcx import checkpoint as K
+    from mcx.graph import IsingGraphDevice
+    from graph_cases import from_edges, random_edges
+    es = random_edges(500, 1200, 12)
+    rp, col, val = from_edges(500, es, np.random.default_rng(13).normal(size=len(es)))
+    s = IsingGraphDevice(rp, col, val, h=np.random.default_rng(14).normal(size=500) * 0.2)
+    gpu.init_(s, "random", rng=gpu.Philox(4))
+    alg = gpu.Glauber(gpu.Philox(4), beta=0.9)
+    gpu.sweep_(s, alg, 5)
+    f = str(tmp_path / "graph.ckpt")
+    K.init_checkpoint(f, s=s, alg=alg)
+    Ea, Ma = gpu.sweep_(s, alg, 8, record=True)
+    r = K.restore_checkpoint(f)
+    Eb, Mb = gpu.sweep_(r.s, r.alg, 8, record=True)
+    assert np.array_equal(s.spins, r.s.spins) and np.array_equal(Ma, Mb)
+    assert np.allclose(Ea, Eb, rtol=0, atol=1e-9)
+    assert (alg.steps, alg.accepted) == (r.alg.steps, r.alg.accepted)
