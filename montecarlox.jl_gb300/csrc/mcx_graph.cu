@@ -30,6 +30,8 @@ namespace {
 
 constexpr int kGraphBlock = 256;
 constexpr int kSlicesPerBlock = kGraphBlock / 32;
+constexpr int small_block(bool table) { return table ? 1024 : 512; }
+constexpr long long kSmallGraph = 8192;  // padded positions run by the one-block kernel
 constexpr int kMaxTableDegree = 4096;
 constexpr unsigned long long kAlways53 = (1ull << 53) + 1;
 
@@ -68,7 +70,7 @@ struct GClass {
 // Deterministic block sum of one FP64 value (fixed shuffle tree, then warps in order);
 // the result is valid in thread 0.
 __device__ __forceinline__ double block_sum_f64(double v) {
-    __shared__ double red[kGraphBlock / 32];
+    __shared__ double red[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
@@ -102,8 +104,8 @@ __device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl)
 // delta_energy, -Δpair - h Δspin with Δpair = -2 acc (IsingMatrix, acc the sequential
 // FP64 sum of s_i J_ij s_j over the row) or -2 J lpi (IsingGraph), Δspin = -2 s.
 template <bool EDGEJ, int FIELD>
-__device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long p, long long off, int w, int lane,
-                                                    int si, int lpi) {
+__device__ __forceinline__ double site_delta_energy(const GraphDev& g, const int8_t* sp, long long p, long long off,
+                                                    int w, int lane, int si, int lpi) {
     double dpair;
     if (EDGEJ) {
         double acc = 0.0;
@@ -112,7 +114,7 @@ __device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long
             const int nb = g.nbr[e];
             if (nb >= 0) {
                 const double Jk = g.J64[e];
-                acc += (si * g.spins[nb] > 0) ? Jk : -Jk;  // (s_i J) s_j: exact sign flips
+                acc += (si * sp[nb] > 0) ? Jk : -Jk;  // (s_i J) s_j: exact sign flips
             }
         }
         dpair = -2.0 * acc;
@@ -128,9 +130,9 @@ __device__ __forceinline__ double site_delta_energy(const GraphDev& g, long long
 // The reference's FP64 decision for one site (the exact path, taken when the FP32 test
 // below cannot decide).  Returns the flip and ΔE.
 template <int ALG, bool EDGEJ, int FIELD>
-__device__ __noinline__ bool exact_site(const GraphDev& g, long long p, long long off, int w, int lane, int si,
-                                        int lpi, unsigned long long ku, double* dE_out) {
-    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, off, w, lane, si, lpi);
+__device__ __noinline__ bool exact_site(const GraphDev& g, const int8_t* sp, long long p, long long off, int w,
+                                        int lane, int si, int lpi, unsigned long long ku, double* dE_out) {
+    const double dE = site_delta_energy<EDGEJ, FIELD>(g, sp, p, off, w, lane, si, lpi);
     *dE_out = dE;
     const double u = (double)ku * 0x1p-53;
     if (ALG == MCX_METROPOLIS) {
@@ -181,8 +183,9 @@ struct RowSum {
 // One site: ΔE in float-float, the certified FP32 decision, the exact FP64 one when that
 // cannot decide.  Returns the flip; (eh, el) accumulates ΔE of flipped sites.
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
-__device__ __forceinline__ bool decide_site(const GraphDev& g, long long p, long long off, int w, int lane, int si,
-                                            const RowSum& r, uint32_t whi, uint32_t wlo, float& eh, float& el) {
+__device__ __forceinline__ bool decide_site(const GraphDev& g, const int8_t* sp, long long p, long long off, int w,
+                                            int lane, int si, const RowSum& r, uint32_t whi, uint32_t wlo, float& eh,
+                                            float& el) {
     const unsigned long long ku = ((unsigned long long)whi << 21) | (unsigned long long)(wlo >> 11);
     if (TABLE) {
         const int idx = (si > 0 ? 2 * g.dmax + 1 : 0) + r.lpi + g.dmax;
@@ -231,7 +234,7 @@ __device__ __forceinline__ bool decide_site(const GraphDev& g, long long p, long
         if (flip) ff_add(eh, el, dh, dl);
     } else {
         double dE;
-        flip = exact_site<ALG, EDGEJ, FIELD>(g, p, off, w, lane, si, r.lpi, ku, &dE);
+        flip = exact_site<ALG, EDGEJ, FIELD>(g, sp, p, off, w, lane, si, r.lpi, ku, &dE);
         if (flip) {
             const float h = __double2float_rn(dE);
             ff_add(eh, el, h, __double2float_rn(dE - (double)h));
@@ -242,10 +245,11 @@ __device__ __forceinline__ bool decide_site(const GraphDev& g, long long p, long
 
 // Both rows of a slice pair, four entries of each at a time: all index and coupling
 // loads of a group are issued before any spin is gathered, and all gathers before any is
-// used (each row keeps its own order).
-template <bool EDGEJ>
-__device__ __forceinline__ void row_sum2(const GraphDev& g, long long offA, int wA, long long offB, int wB, int lane,
-                                         int siA, int siB, RowSum& rA, RowSum& rB) {
+// used (each row keeps its own order).  NC: gather the spins through the read-only path,
+// valid when no spin of another class changes during the launch.
+template <bool EDGEJ, bool NC>
+__device__ __forceinline__ void row_sum2(const GraphDev& g, const int8_t* sp, long long offA, int wA, long long offB,
+                                         int wB, int lane, int siA, int siB, RowSum& rA, RowSum& rB) {
     rA.lpi = rB.lpi = 0;
     rA.ah = rA.al = rA.S = rB.ah = rB.al = rB.S = 0.0f;
     const int wm = max(wA, wB);
@@ -265,8 +269,8 @@ __device__ __forceinline__ void row_sum2(const GraphDev& g, long long offA, int 
         int sa[4], sb[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            sa[j] = na[j] >= 0 ? (int)__ldg(g.spins + na[j]) : 0;
-            sb[j] = nb[j] >= 0 ? (int)__ldg(g.spins + nb[j]) : 0;
+            sa[j] = na[j] >= 0 ? (int)(NC ? __ldg(sp + na[j]) : sp[na[j]]) : 0;
+            sb[j] = nb[j] >= 0 ? (int)(NC ? __ldg(sp + nb[j]) : sp[nb[j]]) : 0;
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -296,22 +300,18 @@ __device__ __forceinline__ void row_sum2(const GraphDev& g, long long offA, int 
     }
 }
 
-// One colour class of one sweep.  A warp takes two 32-site slices (2j, 2j+1) per step;
-// lane l draws one Philox block, blk0 + 32 j + l, whose words 0-1 feed its site in slice
-// 2j and words 2-3 its site in slice 2j+1.  The kernel waits on gathers: the FP32 path
-// is held to 64 registers (4 blocks of 256 per SM), which measured faster than fewer,
-// fatter warps; the table path needs 48.
-template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
-__global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
-                                                             uint32_t stream, unsigned long long sweep) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// The slice pairs j = first, first + stride, ... of one colour class.  Pair j holds slices
+// 2j and 2j+1 of the class; lane l draws one Philox block, blk0 + 32 j + l, whose words 0-1
+// feed its site in slice 2j and words 2-3 its site in slice 2j+1.
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD, bool NC>
+__device__ __forceinline__ void class_pairs(const GraphDev& g, int8_t* sp, const GClass& c, long long first,
+                                            long long stride,
+                                            int lane, uint32_t k0, uint32_t k1, uint32_t stream,
+                                            unsigned long long sweep, float& eh, float& el, long long& dM,
+                                            long long& nacc) {
     const uint32_t w2 = ctr_word2(sweep, 0, P_GRAPH);
     const long long npairs = (c.nslices + 1) >> 1;
-    float eh = 0.0f, el = 0.0f;
-    long long dM = 0;
-    long long nacc = 0;
-    for (long long j = (long long)blockIdx.x * kSlicesPerBlock + warp; j < npairs;
-         j += (long long)gridDim.x * kSlicesPerBlock) {
+    for (long long j = first; j < npairs; j += stride) {
         const long long sA = c.slice0 + 2 * j;
         const bool hasB = 2 * j + 1 < c.nslices;
         const long long pA = sA * 32 + lane, pB = pA + 32;
@@ -320,26 +320,41 @@ __global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(Grap
         const long long offA = g.soff[sA], offB = g.soff[sA + 1];
         const int wA = (int)((offB - offA) >> 5);
         const int wB = hasB ? (int)((g.soff[sA + 2] - offB) >> 5) : 0;
-        const int siA = g.spins[pA];
-        const int siB = hasB ? (int)g.spins[pB] : 0;
+        const int siA = sp[pA];
+        const int siB = hasB ? (int)sp[pB] : 0;
         RowSum rA, rB;
-        row_sum2<EDGEJ>(g, offA, wA, offB, wB, lane, siA, siB, rA, rB);
+        row_sum2<EDGEJ, NC>(g, sp, offA, wA, offB, wB, lane, siA, siB, rA, rB);
         const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
         if (lA < c.count) {
-            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, pA, offA, wA, lane, siA, rA, r.x, r.y, eh, el)) {
-                g.spins[pA] = (int8_t)(-siA);
+            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, sp, pA, offA, wA, lane, siA, rA, r.x, r.y, eh, el)) {
+                sp[pA] = (int8_t)(-siA);
                 dM += -2 * siA;
                 ++nacc;
             }
         }
         if (lB < c.count) {
-            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, pB, offB, wB, lane, siB, rB, r.z, r.w, eh, el)) {
-                g.spins[pB] = (int8_t)(-siB);
+            if (decide_site<ALG, TABLE, EDGEJ, FIELD>(g, sp, pB, offB, wB, lane, siB, rB, r.z, r.w, eh, el)) {
+                sp[pB] = (int8_t)(-siB);
                 dM += -2 * siB;
                 ++nacc;
             }
         }
     }
+}
+
+// One colour class of one sweep over the whole grid.  The kernel waits on gathers: the
+// FP32 path is held to 64 registers (4 blocks of 256 per SM), which measured faster than
+// fewer, fatter warps; the table path needs 48.
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
+                                                             uint32_t stream, unsigned long long sweep) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float eh = 0.0f, el = 0.0f;
+    long long dM = 0;
+    long long nacc = 0;
+    class_pairs<ALG, TABLE, EDGEJ, FIELD, true>(g, g.spins, c, (long long)blockIdx.x * kSlicesPerBlock + warp,
+                                                 (long long)gridDim.x * kSlicesPerBlock, lane, k0, k1, stream, sweep,
+                                                 eh, el, dM, nacc);
     const double t = block_sum_f64((double)eh + (double)el);
     if (threadIdx.x == 0) g.part[c.part0 + blockIdx.x] = t;
     dM = warp_sum_i64(dM);
@@ -347,6 +362,81 @@ __global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(Grap
     if (lane == 0) {
         if (dM) atomicAdd(reinterpret_cast<unsigned long long*>(g.M), (unsigned long long)dM);
         if (nacc) atomicAdd(g.acc, (unsigned long long)nacc);
+    }
+}
+
+__device__ __forceinline__ void warp_ff_sum(float& h, float& l) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_down_sync(0xFFFFFFFFu, h, o), ol = __shfl_down_sync(0xFFFFFFFFu, l, o);
+        ff_add(h, l, oh, ol);
+    }
+}
+
+// Small graphs (up to kSmallGraph padded sites): every sweep of the call in one block
+// (1024 threads for the table form; 512 for the FP32 form, whose sites need more than 64
+// registers).  The spins live in shared memory for the whole call (a class reads what
+// the previous one wrote, with a __syncthreads between classes); E, M and the accepted
+// count stay in thread 0's registers; the per-sweep ΔE is reduced in float-float by
+// shuffles (fixed order) and added to the FP64 energy once per sweep.  One launch per
+// call instead of (classes + 1) per sweep.
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(small_block(TABLE), 1) k_graph_small(GraphDev g, const GClass* __restrict__ classes,
+                                                                int ncls, uint32_t k0, uint32_t k1, uint32_t stream,
+                                                                unsigned long long sweep0, long long nsweeps,
+                                                                double* Eser, long long* Mser, int npad) {
+    extern __shared__ int8_t s_spins[];
+    __shared__ float red_f[2][32];
+    __shared__ long long red_i[2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (int)(blockDim.x >> 5);
+    for (int p = threadIdx.x; p < npad; p += blockDim.x) s_spins[p] = g.spins[p];
+    double E = 0.0;
+    long long M = 0, acc = 0;
+    if (threadIdx.x == 0) {
+        E = *g.E;
+        M = *g.M;
+    }
+    __syncthreads();
+    for (long long t = 0; t < nsweeps; ++t) {
+        float eh = 0.0f, el = 0.0f;
+        long long dM = 0, nacc = 0;
+        for (int k = 0; k < ncls; ++k) {
+            class_pairs<ALG, TABLE, EDGEJ, FIELD, false>(g, s_spins, classes[k], warp, nw, lane, k0, k1, stream,
+                                                          sweep0 + (unsigned long long)t, eh, el, dM, nacc);
+            __syncthreads();
+        }
+        warp_ff_sum(eh, el);
+        dM = warp_sum_i64(dM);
+        nacc = warp_sum_i64(nacc);
+        if (lane == 0) {
+            red_f[0][warp] = eh;
+            red_f[1][warp] = el;
+            red_i[0][warp] = dM;
+            red_i[1][warp] = nacc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float h = lane < nw ? red_f[0][lane] : 0.0f, l = lane < nw ? red_f[1][lane] : 0.0f;
+            long long m = lane < nw ? red_i[0][lane] : 0, a = lane < nw ? red_i[1][lane] : 0;
+            warp_ff_sum(h, l);
+            m = warp_sum_i64(m);
+            a = warp_sum_i64(a);
+            if (lane == 0) {
+                E = E + ((double)h + (double)l);
+                M += m;
+                acc += a;
+                if (Eser) Eser[t] = E;
+                if (Mser) Mser[t] = M;
+            }
+        }
+        __syncthreads();  // red_* are reused by the next sweep
+    }
+    for (int p = threadIdx.x; p < npad; p += blockDim.x) g.spins[p] = s_spins[p];
+    if (threadIdx.x == 0) {
+        *g.E = E;
+        *g.M = M;
+        *g.acc = *g.acc + (unsigned long long)acc;
     }
 }
 
@@ -446,7 +536,7 @@ __global__ void k_graph_site(GraphDev g, long long p, int op, double* out) {
             const int nb = g.nbr[off + 32ll * k + lane];
             if (nb >= 0) lpi += si * g.spins[nb];
         }
-    const double dE = site_delta_energy<EDGEJ, FIELD>(g, p, off, w, lane, si, lpi);
+    const double dE = site_delta_energy<EDGEJ, FIELD>(g, g.spins, p, off, w, lane, si, lpi);
     *out = dE;
     if (op == 1) {
         g.spins[p] = (int8_t)(-si);
@@ -488,27 +578,40 @@ __global__ void k_graph_init_uniform(const int32_t* perm, long long n, int8_t* s
 }
 
 using ClassFn = void (*)(GraphDev, GClass, uint32_t, uint32_t, uint32_t, unsigned long long);
+using SmallFn = void (*)(GraphDev, const GClass*, int, uint32_t, uint32_t, uint32_t, unsigned long long, long long,
+                         double*, long long*, int);
 
-template <int ALG, bool TABLE>
-ClassFn class_fn_t(bool edgej, int field) {
-    if (TABLE) return field == F_UNIFORM ? k_graph_class<ALG, true, false, F_UNIFORM> : k_graph_class<ALG, true, false, F_NONE>;
-    if (edgej)
-        return field == F_VECTOR    ? k_graph_class<ALG, false, true, F_VECTOR>
-               : field == F_UNIFORM ? k_graph_class<ALG, false, true, F_UNIFORM>
-                                    : k_graph_class<ALG, false, true, F_NONE>;
-    return field == F_VECTOR    ? k_graph_class<ALG, false, false, F_VECTOR>
-           : field == F_UNIFORM ? k_graph_class<ALG, false, false, F_UNIFORM>
-                                : k_graph_class<ALG, false, false, F_NONE>;
+struct SweepFns {
+    ClassFn cls;        // one class per launch
+    SmallFn small;      // all sweeps in one block
+    int small_threads;  // its block size
+};
+
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+SweepFns fns_of() {
+    return {k_graph_class<ALG, TABLE, EDGEJ, FIELD>, k_graph_small<ALG, TABLE, EDGEJ, FIELD>, small_block(TABLE)};
 }
 
-ClassFn class_fn(mcx_algorithm alg, bool table, bool edgej, int field) {
+template <int ALG, bool TABLE>
+SweepFns sweep_fns_t(bool edgej, int field) {
+    if (TABLE) return field == F_UNIFORM ? fns_of<ALG, true, false, F_UNIFORM>() : fns_of<ALG, true, false, F_NONE>();
+    if (edgej)
+        return field == F_VECTOR    ? fns_of<ALG, false, true, F_VECTOR>()
+               : field == F_UNIFORM ? fns_of<ALG, false, true, F_UNIFORM>()
+                                    : fns_of<ALG, false, true, F_NONE>();
+    return field == F_VECTOR    ? fns_of<ALG, false, false, F_VECTOR>()
+           : field == F_UNIFORM ? fns_of<ALG, false, false, F_UNIFORM>()
+                                : fns_of<ALG, false, false, F_NONE>();
+}
+
+SweepFns sweep_fns(mcx_algorithm alg, bool table, bool edgej, int field) {
     switch (alg) {
-        case MCX_METROPOLIS: return table ? class_fn_t<MCX_METROPOLIS, true>(edgej, field)
-                                          : class_fn_t<MCX_METROPOLIS, false>(edgej, field);
-        case MCX_GLAUBER: return table ? class_fn_t<MCX_GLAUBER, true>(edgej, field)
-                                       : class_fn_t<MCX_GLAUBER, false>(edgej, field);
-        default: return table ? class_fn_t<MCX_HEATBATH, true>(edgej, field)
-                              : class_fn_t<MCX_HEATBATH, false>(edgej, field);
+        case MCX_METROPOLIS: return table ? sweep_fns_t<MCX_METROPOLIS, true>(edgej, field)
+                                          : sweep_fns_t<MCX_METROPOLIS, false>(edgej, field);
+        case MCX_GLAUBER: return table ? sweep_fns_t<MCX_GLAUBER, true>(edgej, field)
+                                       : sweep_fns_t<MCX_GLAUBER, false>(edgej, field);
+        default: return table ? sweep_fns_t<MCX_HEATBATH, true>(edgej, field)
+                              : sweep_fns_t<MCX_HEATBATH, false>(edgej, field);
     }
 }
 
@@ -577,6 +680,7 @@ struct mcx_graph {
     long long* d_Mser = nullptr;
     int64_t ser_cap = 0;
     double* d_site = nullptr;       // delta_energy result
+    GClass* d_classes = nullptr;    // the class descriptors (one-block kernel)
     int64_t device_bytes = 0;
     std::vector<std::pair<void*, size_t>> allocs;
 
@@ -842,6 +946,7 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
         if ((st = galloc(g, &g->d_acc, 1))) break;
         if ((st = galloc(g, &g->d_ilpi, 1))) break;
         if ((st = galloc(g, &g->d_site, 1))) break;
+        if ((st = galloc(g, &g->d_classes, (size_t)ncol))) break;
         if ((st = galloc(g, &g->d_part, (size_t)g->part_cap))) break;
     } while (false);
     if (st != MCX_OK) {
@@ -864,6 +969,7 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
     if (field) up(g->d_h, hv.data(), hv.size() * sizeof(double));
     if (field) up(g->d_h2, hv2.data(), hv2.size() * sizeof(float2));
     up(g->d_perm, perm.data(), perm.size() * sizeof(int32_t));
+    up(g->d_classes, g->classes.data(), g->classes.size() * sizeof(GClass));
     if (e == cudaSuccess) e = cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) {
@@ -1019,24 +1125,31 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
         MCX_CHECK(galloc(g, &g->d_Mser, (size_t)nsweeps));
         g->ser_cap = nsweeps;
     }
-    const ClassFn fn = class_fn(alg, table, g->edgej, g->field);
-    int bps = 0;
-    MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kGraphBlock, 0));
-    bps = std::max(1, std::min(bps, 8));
+    const SweepFns fns = sweep_fns(alg, table, g->edgej, g->field);
     MCX_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), st));
-    MCX_CUDA(cudaMemsetAsync(g->d_part, 0, sizeof(double) * (size_t)g->nparts, st));
     const GraphDev d = g->dev(beta);
     const uint32_t k0 = (uint32_t)rng->seed, k1 = (uint32_t)(rng->seed >> 32);
-    for (int64_t t = 0; t < nsweeps; ++t) {
-        const unsigned long long sweep = rng->counter + (unsigned long long)t;
-        for (const GClass& c : g->classes) {
-            const int grid = (int)std::min<long long>((c.nslices + kSlicesPerBlock - 1) / kSlicesPerBlock,
-                                                      (long long)ctx->num_sms * bps);
-            fn<<<std::max(grid, 1), kGraphBlock, 0, st>>>(d, c, k0, k1, rng->stream, sweep);
+    if (g->npad <= kSmallGraph) {
+        fns.small<<<1, fns.small_threads, (size_t)g->npad, st>>>(d, g->d_classes, g->ncol, k0, k1, rng->stream,
+                                                            rng->counter, nsweeps, rec ? g->d_Eser : nullptr,
+                                                            rec ? g->d_Mser : nullptr, (int)g->npad);
+        count_launch(ctx);
+    } else {
+        int bps = 0;
+        MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fns.cls, kGraphBlock, 0));
+        bps = std::max(1, std::min(bps, 8));
+        MCX_CUDA(cudaMemsetAsync(g->d_part, 0, sizeof(double) * (size_t)g->nparts, st));
+        for (int64_t t = 0; t < nsweeps; ++t) {
+            const unsigned long long sweep = rng->counter + (unsigned long long)t;
+            for (const GClass& c : g->classes) {
+                const int grid = (int)std::min<long long>((c.nslices + 2 * kSlicesPerBlock - 1) / (2 * kSlicesPerBlock),
+                                                          (long long)ctx->num_sms * bps);
+                fns.cls<<<std::max(grid, 1), kGraphBlock, 0, st>>>(d, c, k0, k1, rng->stream, sweep);
+            }
+            k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, rec ? g->d_Eser : nullptr,
+                                                      rec ? g->d_Mser : nullptr, t);
+            count_launch(ctx, (uint64_t)g->classes.size() + 1);
         }
-        k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, rec ? g->d_Eser : nullptr,
-                                                  rec ? g->d_Mser : nullptr, t);
-        count_launch(ctx, (uint64_t)g->classes.size() + 1);
     }
     MCX_CUDA(cudaGetLastError());
     rng->counter += (uint64_t)nsweeps;

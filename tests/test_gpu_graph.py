@@ -1,7 +1,8 @@
 """General graphs and couplings on the device against the oracle (GPU): spins, accepted
 counts and magnetizations bit for bit; FP64 energies within a tolerance written below
 (the device sums per-block partials in a different order than the oracle's sequential
-sum)."""
+sum).  Graphs up to 8192 padded sites run in the one-block kernel, larger ones one launch
+per colour class; the cases cover both."""
 import numpy as np
 import pytest
 
@@ -54,6 +55,13 @@ def _case(name):
     if name == "hub_graph":
         es = hub_edges(1000, 200, 9)
         return O.Graph(*from_edges(1000, es)[:2], J=1.0)
+    if name == "random_big_vector_h":  # above the one-block limit: one launch per class
+        es = random_edges(20000, 50000, 11)
+        rp, col, val = from_edges(20000, es, np.random.default_rng(12).normal(size=len(es)))
+        return O.Graph(rp, col, Jv=val, hv=np.random.default_rng(13).normal(size=20000) * 0.5)
+    if name == "grid_big_uniform_h":
+        n, es = grid_edges([128, 96], True)
+        return O.Graph(*from_edges(n, es)[:2], J=1.0, h=0.1)
     if name == "ea_256":
         n, es = grid_edges([256, 256], True)
         rp, col, val = from_edges(n, es, np.random.default_rng(10).normal(size=len(es)))
@@ -71,7 +79,9 @@ CASES = [("grid8_graph", "metropolis", 0.44), ("grid8_graph", "heatbath", 0.6),
          ("open7x5_uniform_h", "glauber", 0.5), ("cube6_vector_h", "heatbath", 0.3),
          ("cube6_vector_h", "metropolis", 0.25), ("random_gauss", "metropolis", 1.2),
          ("random_gauss", "glauber", 0.8), ("random_gauss_h", "heatbath", 1.0),
-         ("hub_pm_vector_h", "metropolis", 0.9), ("hub_graph", "glauber", 0.4), ("hub_graph", "heatbath", 2.0)]
+         ("hub_pm_vector_h", "metropolis", 0.9), ("hub_graph", "glauber", 0.4), ("hub_graph", "heatbath", 2.0),
+         ("random_big_vector_h", "heatbath", 1.1), ("random_big_vector_h", "metropolis", 0.7),
+         ("grid_big_uniform_h", "glauber", 0.44)]
 
 
 @pytest.mark.parametrize("name,alg,beta", CASES)
