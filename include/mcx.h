@@ -255,6 +255,17 @@ MCX_API mcx_status mcx_pt_set_exchange_counters(mcx_pt* pt, const uint64_t* step
                                                 const uint64_t* accepted);
 /* Cached (pair_sum, spin_sum) of every replica. */
 MCX_API mcx_status mcx_pt_observables(mcx_pt* pt, int64_t* pair_sum, int64_t* spin_sum);
+/* Series kept by mcx_pt_run on the device: 0 (default) only when the caller asks for it,
+ * one column per replica; 1 always, per replica; 2 always, one column per global ladder
+ * position (the energy trace at each fixed beta, as optimize_exchange_interval! groups
+ * samples by ladder index, src/algorithms/parallel_tempering.jl:83-135).  With 2 the
+ * `series` output of mcx_pt_run is in position order too. */
+MCX_API mcx_status mcx_pt_set_record(mcx_pt* pt, int32_t record);
+/* integrated_autocorrelation_times of the columns of the last run's device series:
+ * quantity 0 energy (-J pair - h spin), 1 magnetization; per column under the batch
+ * rules below (taus[nreplicas], NaN for skipped columns). */
+MCX_API mcx_status mcx_pt_tau_int(mcx_pt* pt, int quantity, int64_t min_points, int64_t max_lag,
+                                  double c, double* taus);
 /* Accepted spin flips of every replica during the last mcx_pt_run. */
 MCX_API mcx_status mcx_pt_replica_accepted(mcx_pt* pt, uint64_t* accepted);
 /* Poll limit of the grid barrier waits (default 2^24 polls of ~100 ns). */
@@ -384,6 +395,27 @@ MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i);
 MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng,
                                    int64_t nsweeps, double* E_series, int64_t* M_series,
                                    mcx_counters* counters);
+
+/* ---------------------------------------------------------- measurements -- */
+/* integrated_autocorrelation_times(traces; min_points, max_lag, c)
+ * (src/measurements/autocorrelations.jl:28-110) on the device, for traces in host
+ * memory: trace k is values[offsets[k] .. offsets[k+1]) (float64).  tau = 1/2 + sum of
+ * the normalised autocovariances C(t), t = 1, 2, ..., stopping at the first C(t) <= 0
+ * or when t > c * tau; at least 0.5 (0.5 for a constant trace).  Lag window
+ * min(max_lag, floor(n/2)) (max_lag <= 0: floor(n/2)); traces with fewer than
+ * min_points samples or an empty window give NaN.  c <= 0 or min_points < 2:
+ * MCX_ERR_INVALID_ARG.  Waits for the stream. */
+MCX_API mcx_status mcx_tau_int(mcx_ctx* ctx, const double* values, const int64_t* offsets,
+                               int32_t ntraces, int64_t min_points, int64_t max_lag, double c,
+                               double* taus);
+/* tau_int of the per-sweep series of the last mcx_sweep (lattice) or mcx_graph_sweep
+ * (graph) call, read where it lies on the device: quantity 0 energy, 1 magnetization.
+ * The single-trace rules: at least 2 sweeps, max_lag <= floor(n/2) (<= 0: floor(n/2)),
+ * else MCX_ERR_INVALID_ARG. */
+MCX_API mcx_status mcx_lattice_tau_int(mcx_lattice* lat, int quantity, int64_t max_lag, double c,
+                                       double* tau);
+MCX_API mcx_status mcx_graph_tau_int(mcx_graph* g, int quantity, int64_t max_lag, double c,
+                                     double* tau);
 
 /* ----------------------------------------------------------- no allocation -- */
 /* mcx_sweep_noalloc has no counterpart in the reference.  It runs the same sweeps as

@@ -679,6 +679,7 @@ struct mcx_graph {
     double* d_Eser = nullptr;
     long long* d_Mser = nullptr;
     int64_t ser_cap = 0;
+    int64_t ser_len = 0;            // sweeps recorded by the last sweep call
     double* d_site = nullptr;       // delta_energy result
     GClass* d_classes = nullptr;    // the class descriptors (one-block kernel)
     int64_t device_bytes = 0;
@@ -1114,8 +1115,8 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
     cudaStream_t st = ctx->stream;
     const bool table = g->table_mode();
     if (table) MCX_CHECK(graph_table(g, alg, beta));
-    const bool rec = E_series || M_series;
-    if (rec && nsweeps > g->ser_cap) {
+    // the series always stays on the device (autocorrelation times read it in place)
+    if (nsweeps > g->ser_cap) {
         if (g->d_Eser) gfree(g, g->d_Eser);
         if (g->d_Mser) gfree(g, g->d_Mser);
         g->d_Eser = nullptr;
@@ -1131,8 +1132,8 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
     const uint32_t k0 = (uint32_t)rng->seed, k1 = (uint32_t)(rng->seed >> 32);
     if (g->npad <= kSmallGraph) {
         fns.small<<<1, fns.small_threads, (size_t)g->npad, st>>>(d, g->d_classes, g->ncol, k0, k1, rng->stream,
-                                                            rng->counter, nsweeps, rec ? g->d_Eser : nullptr,
-                                                            rec ? g->d_Mser : nullptr, (int)g->npad);
+                                                            rng->counter, nsweeps, g->d_Eser,
+                                                            g->d_Mser, (int)g->npad);
         count_launch(ctx);
     } else {
         int bps = 0;
@@ -1146,14 +1147,15 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
                                                           (long long)ctx->num_sms * bps);
                 fns.cls<<<std::max(grid, 1), kGraphBlock, 0, st>>>(d, c, k0, k1, rng->stream, sweep);
             }
-            k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, rec ? g->d_Eser : nullptr,
-                                                      rec ? g->d_Mser : nullptr, t);
+            k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, g->d_Eser,
+                                                      g->d_Mser, t);
             count_launch(ctx, (uint64_t)g->classes.size() + 1);
         }
     }
     MCX_CUDA(cudaGetLastError());
     rng->counter += (uint64_t)nsweeps;
-    if (counters || rec) {
+    g->ser_len = nsweeps;
+    if (counters || E_series || M_series) {
         unsigned long long acc1 = 0;
         MCX_CUDA(cudaMemcpyAsync(&acc1, g->d_acc, sizeof(acc1), cudaMemcpyDeviceToHost, st));
         if (E_series)
@@ -1168,6 +1170,30 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
         }
     }
     return MCX_OK;
+}
+
+MCX_API mcx_status mcx_graph_tau_int(mcx_graph* g, int quantity, int64_t max_lag, double c, double* tau) {
+    if (!g || !tau) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (quantity != 0 && quantity != 1) return fail(MCX_ERR_INVALID_ARG, "quantity must be 0 (energy) or 1 (magnetization)");
+    if (!(c > 0)) return fail(MCX_ERR_INVALID_ARG, "c must be positive");
+    const long long n = g->ser_len;
+    if (n < 2) return fail(MCX_ERR_INVALID_ARG, "the last sweep call recorded %lld sweeps (at least 2 needed)", n);
+    if (max_lag > n / 2) return fail(MCX_ERR_INVALID_ARG, "max_lag must satisfy 1 <= max_lag <= floor(n/2)");
+    std::vector<TraceSrc> srcs(1);
+    TraceSrc& s = srcs[0];
+    s = TraceSrc{};
+    s.stride = 1;
+    if (quantity == 0) {
+        s.base = g->d_Eser;
+        s.type = TRACE_F64;
+    } else {
+        s.base = g->d_Mser;
+        s.type = TRACE_I64;
+        s.ncols = 1;
+        s.coef[0] = 1.0;
+    }
+    tau_window(s, n, 2, max_lag);
+    return launch_tau_int(g->ctx, srcs, nullptr, 0, c, tau);
 }
 
 }  // extern "C"

@@ -132,6 +132,24 @@ struct mcx_lattice {
 };
 
 namespace mcx {
+// A per-sweep series read in place by the autocorrelation kernel: sample t is
+// base[t * stride] (float64) or sum_k coef[k] * base[t * stride + k] (int64 columns).
+enum TraceType { TRACE_F64 = 0, TRACE_I64 = 1 };
+struct TraceSrc {
+    const void* base;       // device address of sample 0; nullptr: host values at host_offset
+    long long n, stride;
+    long long cap;          // lag window
+    long long host_offset;
+    int type, ncols, skip, pad;
+    double coef[3];
+};
+// integrated autocorrelation times of the traces (NaN for skipped ones); waits.
+mcx_status launch_tau_int(mcx_ctx* ctx, const std::vector<TraceSrc>& srcs, const double* host_values,
+                          size_t host_count, double c, double* taus);
+// the batch lag-window rules: cap = min(max_lag, n/2) (max_lag <= 0: n/2); skip when
+// n < min_points or cap < 1
+void tau_window(TraceSrc& s, long long n, long long min_points, long long max_lag);
+
 mcx_status dev_alloc(mcx_ctx* ctx, void** p, size_t bytes);
 void dev_free(mcx_ctx* ctx, void* p, size_t bytes);
 // launch accounting helper

@@ -74,6 +74,7 @@ struct PTArgs {
     long long nsweeps;
     int every;
     long long spin_limit;
+    int series_by_pos;                 // series columns: 0 replicas, 1 global ladder positions
 };
 
 // n / d for small n, d: m = ceil(2^32 / d) (exact while n < 2^32 / d); m = 0 encodes d = 1
@@ -380,8 +381,9 @@ __global__ void __launch_bounds__(256, 2) k_pt_persistent(const PTArgs a) {
         __syncthreads();
         if (a.series && blockIdx.x == 0)
             for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) {
-                a.series[((size_t)s * a.nrep + r) * 2] = s_P[r];
-                a.series[((size_t)s * a.nrep + r) * 2 + 1] = s_M[r];
+                const int col = a.series_by_pos ? a.reps[r].gpos0 + s_pos[r] : r;
+                a.series[((size_t)s * a.nrep + col) * 2] = s_P[r];
+                a.series[((size_t)s * a.nrep + col) * 2 + 1] = s_M[r];
             }
         if (exch) {
             pt_exchange(a, s_pos, s_rep, s_P, s_M, stage, t, blockIdx.x == 0, logu);
@@ -430,8 +432,9 @@ __global__ void __launch_bounds__(256) k_pt_plain_exchange(const PTArgs a, long 
         a.state[2 * r + 1] = s_M[r];
         s_pos[r] = a.pos[r];
         if (a.series) {
-            a.series[((size_t)s * a.nrep + r) * 2] = s_P[r];
-            a.series[((size_t)s * a.nrep + r) * 2 + 1] = s_M[r];
+            const int col = a.series_by_pos ? a.reps[r].gpos0 + s_pos[r] : r;
+            a.series[((size_t)s * a.nrep + col) * 2] = s_P[r];
+            a.series[((size_t)s * a.nrep + col) * 2 + 1] = s_M[r];
         }
     }
     __syncthreads();
@@ -494,6 +497,10 @@ struct mcx_pt {
     unsigned long long* d_ex_acc = nullptr;
     long long* d_series = nullptr;
     int64_t series_cap = 0;
+    int record = 0;                // 0: series on request, by replica; 1: always, by replica;
+                                   // 2: always, by ladder position
+    int64_t series_len = 0;        // sweeps the device series holds (last run)
+    int series_by_pos = 0;
     unsigned int* d_bar = nullptr;
     unsigned long long* d_repbar = nullptr;  // [nrep] per-replica arrival counters (persistent form)
     double* d_logu = nullptr;
@@ -625,6 +632,7 @@ static void pt_args(const mcx_pt* pt, PTArgs* a, mcx_algorithm alg) {
     a->logu = pt->d_logu;
     a->J = pt->J;
     a->h = pt->h;
+    a->series_by_pos = 0;
     a->spin_limit = pt->spin_limit;
 }
 
@@ -946,7 +954,8 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
     if (rng->counter + (uint64_t)nsweeps >= (1ull << 48)) return fail(MCX_ERR_INVALID_ARG, "sweep counter beyond 2^48");
     if (nsweeps == 0) return MCX_OK;
     mcx_ctx* ctx = pt->ctx;
-    if (series) {
+    const bool rec = series != nullptr || pt->record != 0;
+    if (rec) {
         if (nsweeps > pt->series_cap) {
             void* p = nullptr;
             MCX_CHECK(dev_alloc(ctx, &p, (size_t)nsweeps * pt->nrep * 2 * sizeof(long long)));
@@ -963,7 +972,8 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
     }
     PTArgs a;
     pt_args(pt, &a, alg);
-    a.series = series ? pt->d_series : nullptr;
+    a.series = rec ? pt->d_series : nullptr;
+    a.series_by_pos = pt->record == 2 ? 1 : 0;
     a.k0 = (uint32_t)rng->seed;
     a.k1 = (uint32_t)(rng->seed >> 32);
     a.sweep0 = rng->counter;
@@ -1002,6 +1012,8 @@ MCX_API mcx_status mcx_pt_run(mcx_pt* pt, mcx_algorithm alg, mcx_rng* rng, int64
         MCX_CUDA(cudaGetLastError());
     }
     rng->counter += (uint64_t)nsweeps;
+    pt->series_len = rec ? nsweeps : 0;
+    pt->series_by_pos = a.series_by_pos;
     if (series) {
         MCX_CUDA(cudaMemcpyAsync(series, pt->d_series, (size_t)nsweeps * pt->nrep * 2 * sizeof(long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
@@ -1109,6 +1121,39 @@ MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls) {
     dev_free(ctx, p, 2 * sizeof(unsigned int));
     if (e != cudaSuccess) return cuda_fail(e, "wait-flag test");
     return res == 1 ? fail(MCX_ERR_TIMEOUT, "flag wait exceeded %lld polls", (long long)polls) : MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_set_record(mcx_pt* pt, int32_t record) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (record < 0 || record > 2) return fail(MCX_ERR_INVALID_ARG, "record must be 0, 1 or 2");
+    pt->record = record;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_tau_int(mcx_pt* pt, int quantity, int64_t min_points, int64_t max_lag, double c,
+                                  double* taus) {
+    if (!pt || !taus) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (quantity != 0 && quantity != 1) return fail(MCX_ERR_INVALID_ARG, "quantity must be 0 (energy) or 1 (magnetization)");
+    if (!(c > 0)) return fail(MCX_ERR_INVALID_ARG, "c must be positive");
+    if (min_points < 2) return fail(MCX_ERR_INVALID_ARG, "min_points must be >= 2");
+    if (pt->series_len == 0) return fail(MCX_ERR_INVALID_ARG, "the last run recorded no series");
+    std::vector<TraceSrc> srcs(pt->nrep);
+    for (int k = 0; k < pt->nrep; ++k) {
+        TraceSrc& s = srcs[k];
+        s = TraceSrc{};
+        s.base = pt->d_series + 2 * (size_t)k;
+        s.type = TRACE_I64;
+        s.stride = 2 * (long long)pt->nrep;
+        s.ncols = 2;
+        if (quantity == 0) {  // -J pair - h spin
+            s.coef[0] = -pt->J;
+            s.coef[1] = -pt->h;
+        } else {
+            s.coef[1] = 1.0;
+        }
+        tau_window(s, pt->series_len, min_points, max_lag);
+    }
+    return launch_tau_int(pt->ctx, srcs, nullptr, 0, c, taus);
 }
 
 }  // extern "C"

@@ -123,6 +123,11 @@ SIGNATURES = {
     "mcx_graph_flip": (C.c_int, [_P, C.c_int64]),
     "mcx_graph_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P, _P,
                                   C.POINTER(mcx_counters)]),
+    "mcx_tau_int": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_double, _P]),
+    "mcx_lattice_tau_int": (C.c_int, [_P, C.c_int, C.c_int64, C.c_double, _f64p]),
+    "mcx_graph_tau_int": (C.c_int, [_P, C.c_int, C.c_int64, C.c_double, _f64p]),
+    "mcx_pt_set_record": (C.c_int, [_P, C.c_int32]),
+    "mcx_pt_tau_int": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int64, C.c_double, _P]),
 }
 
 PT_PERSISTENT, PT_PLAIN = 0, 1

@@ -67,8 +67,32 @@ class ParallelTempering:
                                       betas.ctypes.data_as(C.POINTER(C.c_double)), float(J), float(h), C.byref(h_)))
         self.handle = h_
         self.nrep = int(sum(self.sizes))
+        self.npos = self.nrep  # one replica per ladder position
         self.rng = Philox(seed)
         self.replica_ladder = [l for l, n in enumerate(self.sizes) for _ in range(n)]
+        self._record = "request"
+
+    # -- series and autocorrelation times -------------------------------------
+    def record_(self, mode):
+        """Which series sweep_ keeps on the device: "request" (only with record=True, per
+        replica), "replica" (always, per replica) or "position" (always, one column per
+        global ladder position: the trace at each fixed beta)."""
+        code = {"request": 0, "replica": 1, "position": 2}[mode]
+        _check(L.load().mcx_pt_set_record(self.handle, code))
+        self._record = mode
+        return self
+
+    def tau_int(self, quantity="energy", *, min_points=2, max_lag=None, c=5.0, by=None):
+        """integrated_autocorrelation_times of the columns of the last run's device series
+        (src/measurements/autocorrelations.jl:69-102); ``by`` ("replica" / "position")
+        checks which columns the series holds."""
+        if by is not None and (by == "position") != (self._record == "position"):
+            raise ArgumentError("the device series is kept by %s; call record_(%r) before the run"
+                                % ("position" if self._record == "position" else "replica", by))
+        taus = np.empty(self.nrep, np.float64)
+        _check(L.load().mcx_pt_tau_int(self.handle, {"energy": 0, "magnetization": 1}[quantity], int(min_points),
+                                       0 if max_lag is None else int(max_lag), float(c), taus.ctypes.data))
+        return taus
 
     # -- state ---------------------------------------------------------------
     def init_(self, seed):
@@ -139,7 +163,8 @@ class ParallelTempering:
     def sweep_(self, nsweeps, alg="metropolis", exchange_every=1, mode="persistent", record=False):
         """`nsweeps` sweeps of every replica with an exchange step after every
         `exchange_every`-th sweep.  Returns the (nsweeps, nrep, 2) series of
-        (pair_sum, spin_sum) if `record`."""
+        (pair_sum, spin_sum) if `record` (columns by replica, or by global ladder position
+        after record_("position"))."""
         rng = self.rng._c()
         out = np.empty((nsweeps, self.nrep, 2), np.int64) if record else None
         m = {"persistent": L.PT_PERSISTENT, "plain": L.PT_PLAIN}[mode]

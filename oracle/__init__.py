@@ -77,6 +77,8 @@ def lib():
                                       C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
                                       C.POINTER(C.c_double), C.POINTER(C.c_int64), vp, vp,
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_tau_int.argtypes = [f64p, C.c_int64, C.c_int64, C.c_double]
+        L.orc_tau_int.restype = C.c_double
         _lib = L
     return _lib
 
@@ -251,6 +253,16 @@ def graph_sweep(g, s, alg, beta, seed, stream=0, sweep0=0, nsweeps=1):
     if rc != OK:
         raise ValueError("oracle graph_sweep failed: %d" % rc)
     return Es, Ms, att.value, acc.value
+
+
+def tau_int(x, max_lag=None, c=5.0):
+    """integrated_autocorrelation_time (src/measurements/autocorrelations.jl:28-67);
+    raises ValueError where the reference raises ArgumentError."""
+    x = np.ascontiguousarray(x, np.float64)
+    v = lib().orc_tau_int(x, x.size, 0 if max_lag is None else int(max_lag), float(c))
+    if v < 0:
+        raise ValueError("invalid arguments")
+    return float(v)
 
 
 def bench_seq(model, L, alg, beta, seed, nthreads, attempts_per_thread, J=1.0, D=0.0, h=0.0):

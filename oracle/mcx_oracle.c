@@ -846,3 +846,44 @@ int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* 
     free(colour);
     return ORC_OK;
 }
+
+/* ---------------------------------------------------------------------------
+ * integrated_autocorrelation_time(samples; max_lag, c), src/measurements/
+ * autocorrelations.jl:28-67: tau = 1/2 + sum_t C(t) with C(t) the normalised
+ * autocovariance at lag t (cov over the n - t overlapping pairs), truncated at the
+ * first non-positive C(t) or when t > c * tau.  max_lag <= 0 means floor(n/2).
+ * Returns -1 for invalid arguments (the reference's ArgumentError).
+ * ------------------------------------------------------------------------- */
+double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c) {
+    if (n < 2 || !(c > 0)) return -1.0;
+    int64_t cap = n / 2;
+    if (max_lag > 0) {
+        if (max_lag > cap) return -1.0;
+        cap = max_lag;
+    }
+    double mu = 0.0;
+    for (int64_t i = 0; i < n; ++i) mu += x[i];
+    mu = mu / (double)n;
+    double* ce = (double*)malloc((size_t)n * sizeof(double));
+    double c0 = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        ce[i] = x[i] - mu;
+        c0 += ce[i] * ce[i];
+    }
+    c0 = c0 / (double)n;
+    double tau = 0.5;
+    if (c0 > 0) {
+        for (int64_t lag = 1; lag <= cap; ++lag) {
+            double cov = 0.0;
+            for (int64_t i = 0; i < n - lag; ++i) cov += ce[i] * ce[i + lag];
+            cov = cov / (double)(n - lag);
+            double C = cov / c0;
+            if (C <= 0) break;
+            double next = tau + C;
+            if ((double)lag > c * next) break;
+            tau = next;
+        }
+    }
+    free(ce);
+    return tau > 0.5 ? tau : 0.5;
+}

@@ -86,6 +86,9 @@ int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* 
                     int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
                     uint64_t* accepts);
 
+/* integrated autocorrelation time (-1 on invalid arguments) */
+double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c);
+
 /* CPU baseline: nthreads independent chains in sequential random-site order */
 int orc_bench_seq(int model, int dim, const int32_t* L, int alg, double beta, double J,
                   double D, double h, uint64_t seed, int nthreads, int64_t attempts_per_thread,
