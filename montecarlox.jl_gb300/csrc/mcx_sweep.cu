@@ -21,27 +21,34 @@
 
 namespace mcx {
 
-template <int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
+// The kernel bodies below take the work items first, first + stride, ... of one
+// half-sweep (a.cur / a.oth may point to global or shared memory) and leave the thread's
+// deltas (pair, spin, spin2, accepted) in v.  The grid kernels run one half-sweep per
+// launch; k_lattice_small runs every sweep of a call in one block on a shared-memory copy.
+
+template <int DIM, bool HB, bool T32>
+__device__ __forceinline__ void ising_tables(const SweepArgs& a, unsigned long long* s_thr, uint32_t* s_t32) {
     constexpr int Z = 2 * DIM;
     constexpr int NT = 2 * (Z + 1);
-    constexpr int NW = V / 4;
-    __shared__ unsigned long long s_thr[NT];
-    __shared__ uint32_t s_t32[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) {
         const unsigned long long e = ising_tab_entry(a.thr[t], t, Z, HB);
         if (T32) s_t32[t] = (uint32_t)(e - 1);
         else s_thr[t] = e;
     }
-    __syncthreads();
+}
+
+template <int DIM, int V, bool HB, bool T32>
+__device__ __forceinline__ void ising_cb_body(const SweepArgs& a, const unsigned long long* s_thr,
+                                              const uint32_t* s_t32, long long first, long long stride,
+                                              long long (&v)[4]) {
+    constexpr int Z = 2 * DIM;
+    constexpr int NW = V / 4;
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
     const int cpr = a.W / V;
     const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, isum = 0, nup = 0;
-    for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
-                      a.Ly, a.Lz);
-         it.valid(); it.next()) {
+    for (ChunkIter it(first, stride, cpr, a.Ly, a.Lz); it.valid(); it.next()) {
         const int r = it.row();
         const int k0 = it.q * V;
         const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
@@ -69,26 +76,38 @@ __global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
     }
     long long dP, dM;
     ising_deltas<Z>(nacc, nup, isum, dP, dM);
-    long long v[3] = {dP, dM, (long long)nacc};
-    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
-    block_add_atomic<3>(v, dst);
+    v[0] += dP;
+    v[1] += dM;
+    v[3] += nacc;
+}
+
+template <int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
+    constexpr int NT = 2 * (2 * DIM + 1);
+    __shared__ unsigned long long s_thr[NT];
+    __shared__ uint32_t s_t32[NT];
+    ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
+    __syncthreads();
+    long long v[4] = {0, 0, 0, 0};
+    ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                                   (long long)gridDim.x * blockDim.x, v);
+    long long w[3] = {v[0], v[1], v[3]};
+    const unsigned long long sh = series_shift(a);
+    unsigned long long* const dst[3] = {a.dst[0] + sh, a.dst[1] + sh, a.acc};
+    block_add_atomic<3>(w, dst);
 }
 
 // One site per thread, for rows whose length is not a multiple of 4.
 template <int DIM, bool HB>
-__global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
+__device__ __forceinline__ void ising_site_body(const SweepArgs& a, const unsigned long long* s_thr, long long first,
+                                                long long stride, long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
-    constexpr int NT = 2 * (Z + 1);
-    __shared__ unsigned long long s_thr[NT];
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
-    __syncthreads();
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
     const long long n = (long long)a.W * a.rows;
     const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, asum = 0, nup = 0;
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
-         j += (long long)gridDim.x * blockDim.x) {
+    for (long long j = first; j < n; j += stride) {
         const int r = (int)(j / a.W), k = (int)(j - (long long)r * a.W);
         const RowInfo ri = row_info(r, a.Ly, a.Lz, a.colour, DIM);
         const int s = a.cur[j];
@@ -107,30 +126,39 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
             nup += up;
         }
     }
-    long long v[3] = {2ll * Z * nacc - 4ll * asum, 2ll * nacc - 4ll * nup, (long long)nacc};
-    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
-    block_add_atomic<3>(v, dst);
+    v[0] += 2ll * Z * nacc - 4ll * asum;
+    v[1] += 2ll * nacc - 4ll * nup;
+    v[3] += nacc;
+}
+
+template <int DIM, bool HB>
+__global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
+    constexpr int NT = 2 * (2 * DIM + 1);
+    __shared__ unsigned long long s_thr[NT];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
+    __syncthreads();
+    long long v[4] = {0, 0, 0, 0};
+    ising_site_body<DIM, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                             (long long)gridDim.x * blockDim.x, v);
+    long long w[3] = {v[0], v[1], v[3]};
+    const unsigned long long sh = series_shift(a);
+    unsigned long long* const dst[3] = {a.dst[0] + sh, a.dst[1] + sh, a.acc};
+    block_add_atomic<3>(w, dst);
 }
 
 // ------------------------------------------------------------ Blume-Capel --
 template <int DIM, int V, bool HB>
-__global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
+__device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned long long* s_thr, long long first,
+                                           long long stride, long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
-    constexpr int NC = 2 * Z + 1;
-    constexpr int NT = HB ? 2 * NC : 6 * NC;
     constexpr int NW = V / 4;
-    __shared__ __align__(16) unsigned long long s_thr[NT];
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
-    __syncthreads();
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
     const int cpr = a.W / V;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
-    for (ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, cpr,
-                      a.Ly, a.Lz);
-         it.valid(); it.next()) {
+    for (ChunkIter it(first, stride, cpr, a.Ly, a.Lz); it.valid(); it.next()) {
         const int r = it.row();
         const int k0 = it.q * V;
         const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
@@ -152,27 +180,41 @@ __global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
         bc_lanes_fold<Z>(ln, dP, dM, dQ);
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
-    long long v[4] = {dP, dM, dQ, nacc};
-    unsigned long long* const dst[4] = {a.dst[0], a.dst[1], a.dst[2], a.acc};
+    v[0] += dP;
+    v[1] += dM;
+    v[2] += dQ;
+    v[3] += nacc;
+}
+
+template <int DIM, bool HB>
+__host__ __device__ constexpr int bc_table_size() { return HB ? 2 * (4 * DIM + 1) : 6 * (4 * DIM + 1); }
+
+template <int DIM, int V, bool HB>
+__global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
+    constexpr int NT = bc_table_size<DIM, HB>();
+    __shared__ __align__(16) unsigned long long s_thr[NT];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
+    __syncthreads();
+    long long v[4] = {0, 0, 0, 0};
+    bc_cb_body<DIM, V, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                           (long long)gridDim.x * blockDim.x, v);
+    const unsigned long long sh = series_shift(a);
+    unsigned long long* const dst[4] = {a.dst[0] + sh, a.dst[1] + sh, a.dst[2] + sh, a.acc};
     block_add_atomic<4>(v, dst);
 }
 
 template <int DIM, bool HB>
-__global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
+__device__ __forceinline__ void bc_site_body(const SweepArgs& a, const unsigned long long* s_thr, long long first,
+                                             long long stride, long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
     constexpr int NC = 2 * Z + 1;
-    constexpr int NT = HB ? 2 * NC : 6 * NC;
-    __shared__ unsigned long long s_thr[NT];
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
-    __syncthreads();
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
     const long long n = (long long)a.W * a.rows;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
-         j += (long long)gridDim.x * blockDim.x) {
+    for (long long j = first; j < n; j += stride) {
         const int r = (int)(j / a.W), k = (int)(j - (long long)r * a.W);
         const RowInfo ri = row_info(r, a.Ly, a.Lz, a.colour, DIM);
         const int so = a.cur[j];
@@ -201,9 +243,95 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
             dQ += sn * sn - so * so;
         }
     }
-    long long v[4] = {dP, dM, dQ, nacc};
-    unsigned long long* const dst[4] = {a.dst[0], a.dst[1], a.dst[2], a.acc};
+    v[0] += dP;
+    v[1] += dM;
+    v[2] += dQ;
+    v[3] += nacc;
+}
+
+template <int DIM, bool HB>
+__global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
+    constexpr int NT = bc_table_size<DIM, HB>();
+    __shared__ unsigned long long s_thr[NT];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
+    __syncthreads();
+    long long v[4] = {0, 0, 0, 0};
+    bc_site_body<DIM, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                          (long long)gridDim.x * blockDim.x, v);
+    const unsigned long long sh = series_shift(a);
+    unsigned long long* const dst[4] = {a.dst[0] + sh, a.dst[1] + sh, a.dst[2] + sh, a.acc};
     block_add_atomic<4>(v, dst);
+}
+
+// ------------------------------------------------------ small lattices --
+// Every sweep of one call in one block of 512 threads: both colour arrays are copied
+// to shared memory, each half-sweep runs the body above on them (the neighbours of a
+// colour are the other colour's array, finished by the previous half-sweep; a
+// __syncthreads separates them), and each sweep's deltas go to its series slot with one
+// atomic per value.  One launch per call: no per-half-sweep launch and no graph capture.
+// One SM issues about 2.4e11 thread-instructions per second and a site costs about 30, so
+// this pays up to about 16K sites; the rows are taken four sites at a time (the shortest
+// dependent chain per thread: latency, not issue, bounds a half-sweep this small).
+// KIND: 0 Ising words, 1 Ising per site, 2 Blume-Capel words, 3 Blume-Capel per site.
+template <int KIND, int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(512, 1) k_lattice_small(SweepArgs a, int8_t* g0, int8_t* g1, long long half,
+                                                           long long nsweeps, long long* series) {
+    extern __shared__ __align__(16) int8_t s_lat[];
+    __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
+    __shared__ uint32_t s_t32[kMaxTable];
+    const long long off1 = (half + 15) & ~15ll;
+    int8_t* s0 = s_lat;
+    int8_t* s1 = s_lat + off1;
+    {
+        const uint4* src0 = reinterpret_cast<const uint4*>(g0);
+        const uint4* src1 = reinterpret_cast<const uint4*>(g1);
+        if (half % 16 == 0) {
+            for (long long i = threadIdx.x; i < half / 16; i += blockDim.x) {
+                reinterpret_cast<uint4*>(s0)[i] = src0[i];
+                reinterpret_cast<uint4*>(s1)[i] = src1[i];
+            }
+        } else {
+            for (long long i = threadIdx.x; i < half; i += blockDim.x) {
+                s0[i] = g0[i];
+                s1[i] = g1[i];
+            }
+        }
+    }
+    if constexpr (KIND == 0) {
+        ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
+    } else {
+        for (int t = threadIdx.x; t < kMaxTable; t += blockDim.x) s_thr[t] = a.thr[t];
+    }
+    __syncthreads();
+    const unsigned long long sweep0 = a.sweep;
+    for (long long t = 0; t < nsweeps; ++t) {
+        long long v[4] = {0, 0, 0, 0};
+        for (int c = 0; c < 2; ++c) {
+            a.colour = c;
+            a.cur = c ? s1 : s0;
+            a.oth = c ? s0 : s1;
+            a.sweep = sweep0 + (unsigned long long)t;
+            if constexpr (KIND == 0) ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, threadIdx.x, blockDim.x, v);
+            else if constexpr (KIND == 1) ising_site_body<DIM, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
+            else if constexpr (KIND == 2) bc_cb_body<DIM, V, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
+            else bc_site_body<DIM, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
+            __syncthreads();
+        }
+        unsigned long long* const dst[4] = {(unsigned long long*)(series + 3 * t), (unsigned long long*)(series + 3 * t + 1),
+                                            (unsigned long long*)(series + 3 * t + 2), a.acc};
+        block_add_atomic<4>(v, dst);
+    }
+    if (half % 16 == 0) {
+        for (long long i = threadIdx.x; i < half / 16; i += blockDim.x) {
+            reinterpret_cast<uint4*>(g0)[i] = reinterpret_cast<const uint4*>(s0)[i];
+            reinterpret_cast<uint4*>(g1)[i] = reinterpret_cast<const uint4*>(s1)[i];
+        }
+    } else {
+        for (long long i = threadIdx.x; i < half; i += blockDim.x) {
+            g0[i] = s0[i];
+            g1[i] = s1[i];
+        }
+    }
 }
 
 // ----------------------------------------------------------- dispatching --
@@ -231,6 +359,25 @@ static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, co
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t) {
     return dim == 2 ? pick_kernel_dim<2>(model, alg, V, t) : pick_kernel_dim<3>(model, alg, V, t);
+}
+
+using SmallLatticeFn = void (*)(SweepArgs, int8_t*, int8_t*, long long, long long, long long*);
+
+template <int DIM, bool HB>
+static SmallLatticeFn pick_small_v(int kind, bool t32) {
+    if (kind == 0) return t32 ? k_lattice_small<0, DIM, 4, HB, true> : k_lattice_small<0, DIM, 4, HB, false>;
+    if (kind == 1) return k_lattice_small<1, DIM, 1, HB, false>;
+    if (kind == 2) return k_lattice_small<2, DIM, 4, HB, false>;
+    return k_lattice_small<3, DIM, 1, HB, false>;
+}
+
+static SmallLatticeFn pick_small(int dim, mcx_model model, mcx_algorithm alg, int64_t W, const Table& t) {
+    const bool hb = alg == MCX_HEATBATH;
+    const bool words = W % 4 == 0;
+    const int kind = model == MCX_ISING ? (words ? 0 : 1) : (words ? 2 : 3);
+    const bool t32 = kind == 0 && ising_table_fits32(t.thr, t.n, 2 * dim, hb);
+    if (dim == 2) return hb ? pick_small_v<2, true>(kind, t32) : pick_small_v<2, false>(kind, t32);
+    return hb ? pick_small_v<3, true>(kind, t32) : pick_small_v<3, false>(kind, t32);
 }
 
 int vec_width(int64_t W) { return W % 16 == 0 ? 16 : (W % 8 == 0 ? 8 : (W % 4 == 0 ? 4 : 1)); }
@@ -291,17 +438,25 @@ __global__ void k_set_key(unsigned long long* p, unsigned long long sweep, unsig
     p[0] = sweep;
     p[1] = seed;
     p[2] = stream;
+    p[3] = 0;
 }
 
-// The whole sweep sequence of one call (zero the series and counter, 2*nsweeps
-// half-sweeps, prefix sum) captured once into a CUDA graph on a private stream; the
-// kernels read the first sweep index and the Philox key from lat->d_sweep_base, so the
-// instantiated graph is replayed for every later call with the same algorithm, beta and
-// length, whatever the random stream.
+// last node of a captured chunk: the next replay continues where this one stopped
+__global__ void k_advance_key(unsigned long long* p, unsigned long long n) {
+    p[0] += n;
+    p[3] += n;
+}
+
+// kGraphChunk sweeps (2 * kGraphChunk half-sweeps, then k_advance_key) captured once
+// into a CUDA graph on a private stream.  The kernels read the first sweep, the Philox key
+// and the series offset from lat->d_sweep_base, so the instantiated graph serves every
+// call with the same algorithm and beta, whatever its length or random stream: a call
+// replays it back to back and launches the remainder directly.  (Capturing the whole
+// sequence of a call cost about 10 us per sweep for every new length.)
 static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, const Table& t, int V,
-                              int64_t nsweeps, cudaGraphExec_t* out) {
+                              cudaGraphExec_t* out) {
     for (auto& g : lat->graphs)
-        if (g.alg == (int)alg && g.beta == beta && g.nsweeps == nsweeps && g.V == V && g.series == lat->d_series) {
+        if (g.alg == (int)alg && g.beta == beta && g.V == V && g.series == lat->d_series) {
             *out = g.exec;
             return MCX_OK;
         }
@@ -316,9 +471,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
     const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
     const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
     MCX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), cs);
-    if (e == cudaSuccess) e = cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), cs);
-    for (int64_t s = 0; s < nsweeps && e == cudaSuccess; ++s) {
+    for (int64_t s = 0; s < kGraphChunk; ++s) {
         a.sweep = (uint64_t)s;
         for (int c = 0; c < 2; ++c) {
             a.colour = c;
@@ -328,13 +481,9 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
             fn<<<grid, 256, 0, cs>>>(a);
         }
     }
-    if (e == cudaSuccess) {
-        const mcx_status ps = launch_prefix(lat, nsweeps, cs);
-        if (ps != MCX_OK) e = cudaErrorUnknown;
-    }
+    k_advance_key<<<1, 1, 0, cs>>>(lat->d_sweep_base, (unsigned long long)kGraphChunk);
     cudaGraph_t graph = nullptr;
-    const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
-    if (e == cudaSuccess) e = e2;
+    cudaError_t e = cudaStreamEndCapture(cs, &graph);
     if (e == cudaSuccess) e = cudaGetLastError();
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -344,7 +493,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
         cudaGraphExecDestroy(lat->graphs.front().exec);
         lat->graphs.erase(lat->graphs.begin());
     }
-    lat->graphs.push_back({(int)alg, beta, nsweeps, V, lat->d_series, exec});
+    lat->graphs.push_back({(int)alg, beta, kGraphChunk, V, lat->d_series, exec});
     *out = exec;
     return MCX_OK;
 }
@@ -366,25 +515,59 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     Table t;
     MCX_CHECK(build_table(lat, alg, beta, &t));
     MCX_CHECK(ensure_series(lat, nsweeps > 0 ? nsweeps : 1));
-    // sequences of two or more sweeps replay a captured CUDA graph (which zeroes the
-    // series and counter and ends with the prefix sum itself)
-    const bool graph = lat->layout == MCX_LAYOUT_INT8 && nsweeps >= 2;
-    if (!graph) {
-        MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
-        MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
-    }
+    // small int8 lattices run every sweep of the call in one block (one launch); larger
+    // ones replay a captured chunk of kGraphChunk sweeps as often as it fits and launch
+    // the rest directly
+    const bool small = lat->layout == MCX_LAYOUT_INT8 && lat->N <= kSmallLattice && nsweeps >= 1;
+    const bool graph = !small && lat->layout == MCX_LAYOUT_INT8 && nsweeps >= kGraphChunk;
+    MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
+    MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
     if (lat->layout == MCX_LAYOUT_MSC64) {
         MCX_CHECK(msc_sweep(lat, alg, t, rng, nsweeps));
+    } else if (small) {
+        SweepArgs a;
+        fill_sweep_args(&a, lat, t, rng);
+        a.acc = lat->d_acc;
+        a.sweep = rng->counter;
+        const SmallLatticeFn fn = pick_small(lat->dim, lat->model, alg, lat->W, t);
+        const long long half = lat->N / 2;
+        const size_t smem = (size_t)(((half + 15) & ~15ll) + half);
+        if (smem > 48 * 1024)
+            MCX_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fn<<<1, 512, smem, ctx->stream>>>(a, lat->d_col[0], lat->d_col[1], half, nsweeps,
+                                           reinterpret_cast<long long*>(lat->d_series));
+        count_launch(ctx);
+        MCX_CUDA(cudaGetLastError());
     } else if (graph) {
         const int V = lattice_width(lat);
         cudaGraphExec_t exec = nullptr;
-        MCX_CHECK(sweep_graph(lat, alg, beta, t, V, nsweeps, &exec));
+        MCX_CHECK(sweep_graph(lat, alg, beta, t, V, &exec));
         k_set_key<<<1, 1, 0, ctx->stream>>>(lat->d_sweep_base, (unsigned long long)rng->counter,
                                             (unsigned long long)rng->seed, (unsigned long long)rng->stream);
         MCX_CUDA(cudaGetLastError());
-        MCX_CUDA(cudaGraphLaunch(exec, ctx->stream));
-        count_launch(ctx, 2 * (uint64_t)nsweeps + 2);
-        lat->series_len = nsweeps;
+        const int64_t q = nsweeps / kGraphChunk, rem = nsweeps - q * kGraphChunk;
+        for (int64_t i = 0; i < q; ++i) MCX_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        count_launch(ctx, 1 + (uint64_t)q * (2 * kGraphChunk + 1));
+        if (rem > 0) {  // relative to the advanced key: sweeps q*C .. of the call, slots likewise
+            SweepArgs a;
+            fill_sweep_args(&a, lat, t, rng);
+            a.sweep_base = lat->d_sweep_base;
+            a.acc = lat->d_acc;
+            const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+            const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
+            for (int64_t s = 0; s < rem; ++s) {
+                a.sweep = (uint64_t)s;
+                for (int c = 0; c < 2; ++c) {
+                    a.colour = c;
+                    a.cur = lat->d_col[c];
+                    a.oth = lat->d_col[1 - c];
+                    for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
+                    fn<<<grid, 256, 0, ctx->stream>>>(a);
+                }
+            }
+            count_launch(ctx, 2 * (uint64_t)rem);
+            MCX_CUDA(cudaGetLastError());
+        }
     } else {
         SweepArgs a;
         fill_sweep_args(&a, lat, t, rng);
@@ -405,7 +588,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         count_launch(ctx, 2 * (uint64_t)nsweeps);
         MCX_CUDA(cudaGetLastError());
     }
-    if (!graph) MCX_CHECK(finish_series(lat, nsweeps));
+    MCX_CHECK(finish_series(lat, nsweeps));
     rng->counter += (uint64_t)nsweeps;
     if (obs && nsweeps > 0)
         MCX_CUDA(cudaMemcpyAsync(obs, lat->d_series, (size_t)nsweeps * 3 * sizeof(int64_t),

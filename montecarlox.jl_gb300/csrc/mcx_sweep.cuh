@@ -13,8 +13,9 @@ struct SweepArgs {
     int W, Ly, Lz, rows, colour;
     uint32_t k0, k1, stream;
     unsigned long long sweep;    // sweep index (added to sweep_base[0] when that is set)
-    // device-resident {first sweep index, seed, stream} that replace (0, k0|k1<<32,
-    // stream) when set (captured CUDA graphs), or null
+    // device-resident {first sweep index, seed, stream, series offset} that replace
+    // (0, k0|k1<<32, stream, 0) when set (captured CUDA graphs), or null; the kernels add
+    // the series offset (in sweeps) to their dst slots
     const unsigned long long* sweep_base;
     unsigned long long* dst[3];  // this sweep's (pair, spin, spin2) delta slots
     unsigned long long* acc;     // accepted-move counter
@@ -32,9 +33,21 @@ __device__ __forceinline__ SweepKey sweep_key(const SweepArgs& a) {
     const unsigned long long seed = a.sweep_base[1];
     return SweepKey{a.sweep_base[0] + a.sweep, (uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)a.sweep_base[2]};
 }
+
+// offset of this sweep's series slots (in int64 entries)
+__device__ __forceinline__ unsigned long long series_shift(const SweepArgs& a) {
+    return a.sweep_base ? 3ull * a.sweep_base[3] : 0ull;
+}
 #endif
 
+// captured multi-sweep graphs hold this many sweeps and are replayed back to back
+constexpr int64_t kGraphChunk = 64;
+
 using HalfSweepFn = void (*)(const SweepArgs);
+
+// int8 lattices of at most this many sites run all sweeps of a call in one block with
+// both colour arrays in shared memory
+constexpr long long kSmallLattice = 16384;
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);

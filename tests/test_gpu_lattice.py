@@ -135,19 +135,42 @@ def test_sweeps_compose_and_replay(gpu):
 def test_replayed_sequence_follows_each_calls_stream(gpu):
     """Multi-sweep calls replay one captured sequence per (algorithm, beta, length):
     every replay must still use its own call's seed, stream and counter."""
-    L = [32, 32]
+    L = [128, 160]  # above the one-block limit
     s0 = O.init_random(O.ISING, L, 1, 0)
     sys_ = gpu.Ising(L)
     for seed, stream, counter in ((11, 0, 0), (12, 3, 0), (11, 0, 40), (99, 7, 5)):
         sys_.spins = s0
         a = gpu.Metropolis(gpu.Philox(seed, stream, counter), beta=0.45)
-        obs = gpu.sweep_(sys_, a, 4, record=True)
+        obs = gpu.sweep_(sys_, a, 66, record=True)
         s = s0.copy()
-        oobs, att, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.45, seed, stream=stream, nsweeps=4,
+        oobs, att, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.45, seed, stream=stream, nsweeps=66,
                                     sweep0=counter)
         assert np.array_equal(obs, oobs), (seed, stream, counter)
         assert np.array_equal(sys_.spins, s)
         assert a.accepted == acc
+
+
+@pytest.mark.parametrize("model,L,alg,nsweeps", [(O.ISING, [256, 128], "metropolis", 71),
+                                                  (O.BC, [256, 128], "heatbath", 130),
+                                                  (O.ISING, [32, 32, 32], "glauber", 65)])
+def test_chunked_graph_replay(gpu, model, L, alg, nsweeps):
+    """Lattices above the one-block limit replay a captured 64-sweep chunk back to back and
+    launch the remainder directly; every call (any length, seed, stream, counter) matches
+    the oracle, series included."""
+    D = 1.0 if model == O.BC else 0.0
+    s0 = O.init_random(model, L, 3, 0)
+    sys_ = gpu.Ising(L) if model == O.ISING else gpu.BlumeCapel(L, D=D)
+    for seed, stream, counter, n in ((5, 0, 0, nsweeps), (6, 2, 17, nsweeps), (5, 1, 3, nsweeps + 64)):
+        sys_.spins = s0
+        a = _alg(gpu, alg, seed, 0.4 if len(L) == 2 else 0.22, stream)
+        a.rng.counter = counter
+        obs = gpu.sweep_(sys_, a, n, record=True)
+        s = s0.copy()
+        oobs, att, acc = O.cb_sweep(s, model, L, ALG[alg], 0.4 if len(L) == 2 else 0.22, seed, stream=stream,
+                                    sweep0=counter, nsweeps=n, D=D)
+        assert np.array_equal(obs, oobs), (seed, stream, counter, n)
+        assert np.array_equal(sys_.spins, s)
+        assert (a.flips if alg == "heatbath" else a.accepted) == acc
 
 
 def test_context_outlives_its_objects(gpu):
