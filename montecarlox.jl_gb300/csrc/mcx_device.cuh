@@ -148,6 +148,53 @@ __host__ __device__ __forceinline__ double mcx_logistic(double x) {
     return ex / (1.0 + ex);
 }
 
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch with a bounded wait: bar[0] arrivals,
+// bar[1] generation, bar[2] error flag.  A wait that exceeds `limit` polls sets the error
+// flag; every block then leaves at its next barrier and the host reports MCX_ERR_TIMEOUT.
+// The gpu-scope acquire of the generation orders the block's later loads after every
+// other block's writes before the barrier.
+__device__ __forceinline__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long long limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned g = gen;
+        if (atomicAdd(&bar[0], 1u) == nblocks - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            st_release(&bar[1], g + 1);
+        } else {
+            long long n = 0;
+            while (ld_acquire(&bar[1]) == g) {
+                if (ld_acquire(&bar[2]) != 0u) { ok = 0; break; }
+                if (++n > limit) { atomicExch(&bar[2], 1u); ok = 0; break; }
+                __nanosleep(100);
+            }
+        }
+        gen = g + 1;
+        s_ok = ok && ld_acquire(&bar[2]) == 0u;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 // Block-wide sum of up to 4 int64 values, one atomicAdd per value per block.
 template <int NV>
 __device__ __forceinline__ void block_add_atomic(long long (&v)[NV], unsigned long long* const (&dst)[NV]) {

@@ -253,51 +253,6 @@ __device__ void pt_exchange(const PTArgs& a, int* s_pos, int* s_rep, const long 
     __syncthreads();
 }
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Grid-wide barrier with a bounded wait: bar[0] arrivals, bar[1] generation,
-// bar[2] error flag.  A wait that exceeds `limit` polls sets the error flag; every
-// block then leaves at its next barrier and the host reports MCX_ERR_TIMEOUT.
-__device__ bool grid_sync(unsigned* bar, unsigned nblocks, unsigned& gen, long long limit) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        __threadfence();
-        const unsigned g = gen;
-        if (atomicAdd(&bar[0], 1u) == nblocks - 1) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            st_release(&bar[1], g + 1);
-        } else {
-            long long n = 0;
-            while (ld_acquire(&bar[1]) == g) {
-                if (ld_acquire(&bar[2]) != 0u) { ok = 0; break; }
-                if (++n > limit) { atomicExch(&bar[2], 1u); ok = 0; break; }
-                __nanosleep(100);
-            }
-        }
-        gen = g + 1;
-        s_ok = ok && ld_acquire(&bar[2]) == 0u;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
 template <int DIM, bool HB, bool T32>
 __global__ void __launch_bounds__(256, 2) k_pt_persistent(const PTArgs a) {
     extern __shared__ long long smem[];
