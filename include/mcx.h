@@ -358,6 +358,15 @@ MCX_API mcx_status mcx_server_get_stats(mcx_server* server, mcx_server_stats* st
 MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr,
                                     const int32_t* col, const double* coupling, double J,
                                     const double* field, double h, mcx_graph** out);
+/* BlumeCapelGraph(graph, J, D; h) / BlumeCapelMatrix(J, D; h) (SpinSystems/src/
+ * blume_capel.jl:154-190, :328-360, factory :467-511): the same neighbour lists, spins in
+ * {-1, 0, 1} (all +1 at start), E = -pair - field + D sum s^2.  Sweeps: Metropolis /
+ * Glauber propose one of the two other states (_propose_state, :21-30) from bit 0 of the
+ * low word of the site's uniform; the heat bath draws from the three Boltzmann weights
+ * with r = u z (:59-85). */
+MCX_API mcx_status mcx_bcgraph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr,
+                                      const int32_t* col, const double* coupling, double J,
+                                      double D, const double* field, double h, mcx_graph** out);
 MCX_API mcx_status mcx_graph_destroy(mcx_graph* g);
 /* n sites, colour classes, stored neighbour entries (padding included), device bytes;
  * any pointer may be NULL. */
@@ -381,6 +390,12 @@ MCX_API mcx_status mcx_graph_delta_energy(mcx_graph* g, int64_t i, double* delta
 /* modify!(sys, i, Δpair, Δspin) with the flip_changes of site i (ising.jl:200-218,
  * :364-377): flips spin i and updates the cached energy and magnetization. */
 MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i);
+/* delta_energy(sys, i, s_new) (blume_capel.jl:32-35; for an Ising graph s_new = -s_i is
+ * the flip and s_new = s_i gives 0) and modify! to s_new with propose_changes
+ * (:262-276, :441-466). */
+MCX_API mcx_status mcx_graph_delta_energy_to(mcx_graph* g, int64_t i, int8_t s_new,
+                                             double* delta_energy);
+MCX_API mcx_status mcx_graph_set_site(mcx_graph* g, int64_t i, int8_t s_new);
 /* `nsweeps` sweeps of n spin_flip!(sys, alg) each (ising.jl:25-58 with accept!,
  * src/algorithms/metropolis.jl:14-17, :121-127, importance_sampling.jl:80-85): the
  * reference's FP64 decisions -- Metropolis lr = -beta*ΔE, accept if lr > 0 or

@@ -52,6 +52,7 @@ struct GraphDev {
     int dmax;
     double beta;
     float beta32;
+    double D;                       // crystal field (Blume-Capel)
     unsigned long long* acc;        // accepted moves
     long long* M;                   // cached magnetization
     double* E;                      // cached energy
@@ -440,6 +441,252 @@ __global__ void __launch_bounds__(small_block(TABLE), 1) k_graph_small(GraphDev 
     }
 }
 
+// ------------------------------------------------------------ Blume-Capel --
+// BlumeCapelGraph / BlumeCapelMatrix (SpinSystems/src/blume_capel.jl:117-466): spins in
+// {-1, 0, 1}, the same colour classes, slice pairs and Philox blocks as the Ising graphs.
+// Metropolis / Glauber propose one of the two other states from bit 0 of the low word of
+// the site's uniform (a bit the 53-bit uniform does not use); the heat bath draws from the
+// three Boltzmann weights.  With one J and no per-site field the host tabulates exact
+// 53-bit thresholds (for the heat bath the smallest k with fl(fl(k 2^-53) z) >= w, found
+// by bisection on the reference's own FP64 expression r = u z < w); otherwise every site
+// is evaluated in FP64 as the reference does.
+
+// _propose_state, blume_capel.jl:21-30
+__host__ __device__ __forceinline__ int bc_propose_state(int so, int b) {
+    return so == -1 ? (b ? 0 : 1) : (so == 0 ? (b ? -1 : 1) : (b ? -1 : 0));
+}
+
+// propose_changes + delta_energy (:245-251, :259-260): -Δspin c - h Δspin + D Δspin2
+__host__ __device__ __forceinline__ double bc_delta(double c, int so, int sn, double hf, bool field, double D) {
+    const int ds = sn - so, ds2 = sn * sn - so * so;
+    const double dpair = (double)ds * c;
+    const double dfield = field ? hf * (double)ds : 0.0;
+    return (-dpair - dfield) + D * (double)ds2;
+}
+
+// local_coupling (:241-243, :368-377): the integer neighbour sum and, for per-entry
+// couplings, the FP64 sum of J_ij s_j in row order; four entries at a time.
+template <bool EDGEJ>
+__device__ __forceinline__ void bc_row(const GraphDev& g, const int8_t* sp, long long off, int w, int lane, int& isum,
+                                       double& c) {
+    isum = 0;
+    c = 0.0;
+    for (int k = 0; k < w; k += 4) {
+        int nb[4];
+        double Jk[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long e = off + 32ll * (k + j) + lane;
+            nb[j] = k + j < w ? __ldg(g.nbr + e) : -1;
+            if (EDGEJ) Jk[j] = k + j < w ? __ldg(g.J64 + e) : 0.0;
+        }
+        int sj[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sj[j] = nb[j] >= 0 ? (int)sp[nb[j]] : 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (nb[j] >= 0) {
+                isum += sj[j];
+                if (EDGEJ) c += Jk[j] * (double)sj[j];
+            }
+    }
+}
+
+// One Blume-Capel site: returns the new state (the old one when nothing changes) and adds
+// the ΔE of a change to (eh, el).
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__device__ __forceinline__ int bc_decide(const GraphDev& g, long long p, int so, int isum, double cacc, uint32_t hi,
+                                         uint32_t lo, float& eh, float& el) {
+    const unsigned long long ku = ((unsigned long long)hi << 21) | (unsigned long long)(lo >> 11);
+    if (TABLE) {
+        const int width = 2 * g.dmax + 1, idx = isum + g.dmax;
+        int sn;
+        if (ALG == MCX_HEATBATH) {
+            sn = ku < g.tab[2 * idx] ? -1 : (ku < g.tab[2 * idx + 1] ? 0 : 1);
+            if (sn != so) {
+                const float2 d = g.tabdE[((so + 1) * 3 + sn + 1) * width + idx];
+                ff_add(eh, el, d.x, d.y);
+            }
+        } else {
+            const int b = (int)(lo & 1u);
+            const int e = ((so + 1) * 2 + b) * width + idx;
+            sn = ku < g.tab[e] ? bc_propose_state(so, b) : so;
+            if (sn != so) {
+                const float2 d = g.tabdE[e];
+                ff_add(eh, el, d.x, d.y);
+            }
+        }
+        return sn;
+    }
+    const double c = EDGEJ ? cacc : g.J * (double)isum;
+    const double hf = FIELD == F_VECTOR ? g.h[p] : (FIELD == F_UNIFORM ? g.hu : 0.0);
+    const double u = (double)ku * 0x1p-53;
+    int sn;
+    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :59-85
+        const double e1 = (c - hf * (-1.0)) + g.D;
+        const double e3 = (-c - hf) + g.D;
+        const double w1 = mcx_exp(-g.beta * e1), w2 = mcx_exp(-g.beta * 0.0), w3 = mcx_exp(-g.beta * e3);
+        const double z = (w1 + w2) + w3;
+        const double r = u * z;
+        sn = r < w1 ? -1 : (r < w1 + w2 ? 0 : 1);
+    } else {
+        const int prop = bc_propose_state(so, (int)(lo & 1u));
+        const double lr = -g.beta * bc_delta(c, so, prop, hf, FIELD != F_NONE, g.D);
+        const bool acc = ALG == MCX_METROPOLIS ? ((lr > 0) || (u < mcx_exp(lr))) : (u < mcx_logistic(lr));
+        sn = acc ? prop : so;
+    }
+    if (sn != so) {
+        const double dE = bc_delta(c, so, sn, hf, FIELD != F_NONE, g.D);
+        const float h = __double2float_rn(dE);
+        ff_add(eh, el, h, __double2float_rn(dE - (double)h));
+    }
+    return sn;
+}
+
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__device__ __forceinline__ void bc_class_pairs(const GraphDev& g, int8_t* sp, const GClass& c, long long first,
+                                               long long stride, int lane, uint32_t k0, uint32_t k1, uint32_t stream,
+                                               unsigned long long sweep, float& eh, float& el, long long& dM,
+                                               long long& nacc) {
+    const uint32_t w2 = ctr_word2(sweep, 0, P_GRAPH);
+    const long long npairs = (c.nslices + 1) >> 1;
+    for (long long j = first; j < npairs; j += stride) {
+        const long long sA = c.slice0 + 2 * j;
+        const bool hasB = 2 * j + 1 < c.nslices;
+        const long long pA = sA * 32 + lane, pB = pA + 32;
+        const long long lA = 64 * j + lane, lB = lA + 32;
+        const long long offA = g.soff[sA], offB = g.soff[sA + 1];
+        const int wA = (int)((offB - offA) >> 5);
+        const int wB = hasB ? (int)((g.soff[sA + 2] - offB) >> 5) : 0;
+        const int soA = sp[pA];
+        const int soB = hasB ? (int)sp[pB] : 0;
+        int iA, iB;
+        double cA, cB;
+        bc_row<EDGEJ>(g, sp, offA, wA, lane, iA, cA);
+        bc_row<EDGEJ>(g, sp, offB, wB, lane, iB, cB);
+        const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
+        if (lA < c.count) {
+            const int sn = bc_decide<ALG, TABLE, EDGEJ, FIELD>(g, pA, soA, iA, cA, r.x, r.y, eh, el);
+            if (sn != soA) {
+                sp[pA] = (int8_t)sn;
+                dM += sn - soA;
+                ++nacc;
+            }
+        }
+        if (lB < c.count) {
+            const int sn = bc_decide<ALG, TABLE, EDGEJ, FIELD>(g, pB, soB, iB, cB, r.z, r.w, eh, el);
+            if (sn != soB) {
+                sp[pB] = (int8_t)sn;
+                dM += sn - soB;
+                ++nacc;
+            }
+        }
+    }
+}
+
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(kGraphBlock) k_bcg_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
+                                                           uint32_t stream, unsigned long long sweep) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float eh = 0.0f, el = 0.0f;
+    long long dM = 0, nacc = 0;
+    bc_class_pairs<ALG, TABLE, EDGEJ, FIELD>(g, g.spins, c, (long long)blockIdx.x * kSlicesPerBlock + warp,
+                                             (long long)gridDim.x * kSlicesPerBlock, lane, k0, k1, stream, sweep, eh,
+                                             el, dM, nacc);
+    const double t = block_sum_f64((double)eh + (double)el);
+    if (threadIdx.x == 0) g.part[c.part0 + blockIdx.x] = t;
+    dM = warp_sum_i64(dM);
+    nacc = warp_sum_i64(nacc);
+    if (lane == 0) {
+        if (dM) atomicAdd(reinterpret_cast<unsigned long long*>(g.M), (unsigned long long)dM);
+        if (nacc) atomicAdd(g.acc, (unsigned long long)nacc);
+    }
+}
+
+// every sweep of a call on a small Blume-Capel graph in one block (as k_graph_small)
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+__global__ void __launch_bounds__(512, 1) k_bcg_small(GraphDev g, const GClass* __restrict__ classes, int ncls,
+                                                      uint32_t k0, uint32_t k1, uint32_t stream,
+                                                      unsigned long long sweep0, long long nsweeps, double* Eser,
+                                                      long long* Mser, int npad) {
+    extern __shared__ int8_t s_spins[];
+    __shared__ float red_f[2][32];
+    __shared__ long long red_i[2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (int)(blockDim.x >> 5);
+    for (int p = threadIdx.x; p < npad; p += blockDim.x) s_spins[p] = g.spins[p];
+    double E = 0.0;
+    long long M = 0, acc = 0;
+    if (threadIdx.x == 0) {
+        E = *g.E;
+        M = *g.M;
+    }
+    __syncthreads();
+    for (long long t = 0; t < nsweeps; ++t) {
+        float eh = 0.0f, el = 0.0f;
+        long long dM = 0, nacc = 0;
+        for (int k = 0; k < ncls; ++k) {
+            bc_class_pairs<ALG, TABLE, EDGEJ, FIELD>(g, s_spins, classes[k], warp, nw, lane, k0, k1, stream,
+                                                     sweep0 + (unsigned long long)t, eh, el, dM, nacc);
+            __syncthreads();
+        }
+        warp_ff_sum(eh, el);
+        dM = warp_sum_i64(dM);
+        nacc = warp_sum_i64(nacc);
+        if (lane == 0) {
+            red_f[0][warp] = eh;
+            red_f[1][warp] = el;
+            red_i[0][warp] = dM;
+            red_i[1][warp] = nacc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float h = lane < nw ? red_f[0][lane] : 0.0f, l = lane < nw ? red_f[1][lane] : 0.0f;
+            long long m = lane < nw ? red_i[0][lane] : 0, a = lane < nw ? red_i[1][lane] : 0;
+            warp_ff_sum(h, l);
+            m = warp_sum_i64(m);
+            a = warp_sum_i64(a);
+            if (lane == 0) {
+                E = E + ((double)h + (double)l);
+                M += m;
+                acc += a;
+                if (Eser) Eser[t] = E;
+                if (Mser) Mser[t] = M;
+            }
+        }
+        __syncthreads();
+    }
+    for (int p = threadIdx.x; p < npad; p += blockDim.x) g.spins[p] = s_spins[p];
+    if (threadIdx.x == 0) {
+        *g.E = E;
+        *g.M = M;
+        *g.acc = *g.acc + (unsigned long long)acc;
+    }
+}
+
+// delta_energy(sys, i, s_new) (op 0) or modify! to s_new (op 1) at one position.
+template <bool EDGEJ, int FIELD>
+__global__ void k_bcg_site(GraphDev g, long long p, int sn, int op, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long s = p >> 5;
+    const int lane = (int)(p & 31);
+    const long long off = g.soff[s];
+    const int w = (int)((g.soff[s + 1] - off) >> 5);
+    const int so = g.spins[p];
+    int isum;
+    double c;
+    bc_row<EDGEJ>(g, g.spins, off, w, lane, isum, c);
+    if (!EDGEJ) c = g.J * (double)isum;
+    const double hf = FIELD == F_VECTOR ? g.h[p] : (FIELD == F_UNIFORM ? g.hu : 0.0);
+    const double dE = bc_delta(c, so, sn, hf, FIELD != F_NONE, g.D);
+    *out = dE;
+    if (op == 1 && sn != so) {
+        g.spins[p] = (int8_t)sn;
+        *g.E = *g.E + dE;
+        *g.M = *g.M + (sn - so);
+    }
+}
+
 // E += Σ partials (fixed order); record the series entry of sweep t.
 __global__ void __launch_bounds__(kGraphBlock) k_graph_finish(double* part, int nparts, double* E, const long long* M,
                                                               double* Eser, long long* Mser, long long t) {
@@ -458,10 +705,10 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_finish(double* part, int 
 // the integer pair sum and for M.
 template <bool EDGEJ, int FIELD>
 __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute(GraphDev g, long long nslices, double* part2,
-                                                                 long long* ilpi) {
+                                                                 long long* ilpi, long long* qsum) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double pacc = 0.0, facc = 0.0;
-    long long lsum = 0, msum = 0;
+    long long lsum = 0, msum = 0, q = 0;
     for (long long s = (long long)blockIdx.x * kSlicesPerBlock + warp; s < nslices;
          s += (long long)gridDim.x * kSlicesPerBlock) {
         const long long p = s * 32 + lane;
@@ -477,7 +724,8 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute(GraphDev g, lon
                 const int sj = g.spins[nb];
                 if (EDGEJ) {
                     const double Jk = g.J64[e];
-                    acc += (si * sj > 0) ? Jk : -Jk;
+                    const int pr = si * sj;
+                    if (pr != 0) acc += pr > 0 ? Jk : -Jk;  // (s_i J) s_j; products with 0 add nothing
                 } else {
                     lpi += si * sj;
                 }
@@ -486,6 +734,7 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute(GraphDev g, lon
         pacc += acc;
         lsum += lpi;
         msum += si;
+        q += si * si;
         if (FIELD == F_VECTOR && si != 0) facc += g.h[p] * (double)si;
     }
     const double pt = block_sum_f64(pacc);
@@ -496,16 +745,20 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute(GraphDev g, lon
     }
     lsum = warp_sum_i64(lsum);
     msum = warp_sum_i64(msum);
+    q = warp_sum_i64(q);
     if (lane == 0) {
+        if (q) atomicAdd(reinterpret_cast<unsigned long long*>(qsum), (unsigned long long)q);
         if (lsum) atomicAdd(reinterpret_cast<unsigned long long*>(ilpi), (unsigned long long)lsum);
         if (msum) atomicAdd(reinterpret_cast<unsigned long long*>(g.M), (unsigned long long)msum);
     }
 }
 
-// pair = Σ lpi / 2 (FP64 for IsingMatrix, J (Σ lpi / 2) for IsingGraph); E = -pair - field.
+// pair = Σ lpi / 2 (FP64 for the per-entry couplings, J (Σ lpi / 2) for one J);
+// E = -pair - field (+ D Σ s² for Blume-Capel).
 __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute_finish(const double* part2, int nparts,
-                                                                        const long long* ilpi, int edgej, int field,
-                                                                        double J, double hu, const long long* M,
+                                                                        const long long* ilpi, const long long* qsum,
+                                                                        int edgej, int field, int bc, double J,
+                                                                        double hu, double D, const long long* M,
                                                                         double* E) {
     double p = 0.0, f = 0.0;
     for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
@@ -517,19 +770,25 @@ __global__ void __launch_bounds__(kGraphBlock) k_graph_recompute_finish(const do
     if (threadIdx.x == 0) {
         const double pair = edgej ? ps / 2 : J * (double)(*ilpi / 2);
         const double fld = field == F_VECTOR ? fs : field == F_UNIFORM ? hu * (double)(*M) : 0.0;
-        *E = field == F_NONE ? -pair : -pair - fld;
+        const double e = field == F_NONE ? -pair : -pair - fld;
+        *E = bc ? (-pair - fld) + D * (double)(*qsum) : e;
     }
 }
 
-// delta_energy(sys, i) (op 0) or modify! with flip_changes (op 1) at one position.
+// delta_energy(sys, i) (op 0) or modify! with flip_changes (op 1) at one position;
+// target -1 / +1 is a state to move to (no change when it is the current one), 2 a flip.
 template <bool EDGEJ, int FIELD>
-__global__ void k_graph_site(GraphDev g, long long p, int op, double* out) {
+__global__ void k_graph_site(GraphDev g, long long p, int target, int op, double* out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const long long s = p >> 5;
     const int lane = (int)(p & 31);
     const long long off = g.soff[s];
     const int w = (int)((g.soff[s + 1] - off) >> 5);
     const int si = g.spins[p];
+    if (target != 2 && target == si) {
+        *out = 0.0;
+        return;
+    }
     int lpi = 0;
     if (!EDGEJ)
         for (int k = 0; k < w; ++k) {
@@ -545,10 +804,10 @@ __global__ void k_graph_site(GraphDev g, long long p, int op, double* out) {
     }
 }
 
-__global__ void k_graph_validate(const int8_t* lin, long long n, unsigned long long* bad) {
+__global__ void k_graph_validate(const int8_t* lin, long long n, int bc, unsigned long long* bad) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         const int8_t x = lin[v];
-        if (x != 1 && x != -1) atomicAdd(bad, 1ull);
+        if (x != 1 && x != -1 && !(bc && x == 0)) atomicAdd(bad, 1ull);
     }
 }
 
@@ -562,13 +821,14 @@ __global__ void k_graph_gather(int8_t* lin, const int32_t* perm, long long n, co
         lin[v] = spins[perm[v]];
 }
 
-// init!(sys, :random): site v takes the top bit of word v&3 of Philox block
-// (v>>2, 0, P_GRAPH_INIT<<24, stream).
+// init!(sys, :random): site v takes word v&3 of Philox block (v>>2, 0, P_GRAPH_INIT<<24,
+// stream): its top bit (Ising, +1 / -1) or floor(3 w / 2^32) - 1 (Blume-Capel).
 __global__ void k_graph_init_random(const int32_t* perm, long long n, int8_t* spins, uint32_t k0, uint32_t k1,
-                                    uint32_t stream) {
+                                    uint32_t stream, int bc) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         const uint4 r = philox10(make_uint4((uint32_t)(v >> 2), 0u, (uint32_t)P_GRAPH_INIT << 24, stream), k0, k1);
-        spins[perm[v]] = (pick4(r, (int)(v & 3)) & 0x80000000u) ? 1 : -1;
+        const uint32_t wv = pick4(r, (int)(v & 3));
+        spins[perm[v]] = bc ? (int8_t)((int)(((unsigned long long)wv * 3ull) >> 32) - 1) : ((wv & 0x80000000u) ? 1 : -1);
     }
 }
 
@@ -604,6 +864,34 @@ SweepFns sweep_fns_t(bool edgej, int field) {
                                 : fns_of<ALG, false, false, F_NONE>();
 }
 
+template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
+SweepFns bc_fns_of() {
+    return {k_bcg_class<ALG, TABLE, EDGEJ, FIELD>, k_bcg_small<ALG, TABLE, EDGEJ, FIELD>, 512};
+}
+
+template <int ALG, bool TABLE>
+SweepFns bc_sweep_fns_t(bool edgej, int field) {
+    if (TABLE) return field == F_UNIFORM ? bc_fns_of<ALG, true, false, F_UNIFORM>() : bc_fns_of<ALG, true, false, F_NONE>();
+    if (edgej)
+        return field == F_VECTOR    ? bc_fns_of<ALG, false, true, F_VECTOR>()
+               : field == F_UNIFORM ? bc_fns_of<ALG, false, true, F_UNIFORM>()
+                                    : bc_fns_of<ALG, false, true, F_NONE>();
+    return field == F_VECTOR    ? bc_fns_of<ALG, false, false, F_VECTOR>()
+           : field == F_UNIFORM ? bc_fns_of<ALG, false, false, F_UNIFORM>()
+                                : bc_fns_of<ALG, false, false, F_NONE>();
+}
+
+SweepFns bc_sweep_fns(mcx_algorithm alg, bool table, bool edgej, int field) {
+    switch (alg) {
+        case MCX_METROPOLIS: return table ? bc_sweep_fns_t<MCX_METROPOLIS, true>(edgej, field)
+                                          : bc_sweep_fns_t<MCX_METROPOLIS, false>(edgej, field);
+        case MCX_GLAUBER: return table ? bc_sweep_fns_t<MCX_GLAUBER, true>(edgej, field)
+                                       : bc_sweep_fns_t<MCX_GLAUBER, false>(edgej, field);
+        default: return table ? bc_sweep_fns_t<MCX_HEATBATH, true>(edgej, field)
+                              : bc_sweep_fns_t<MCX_HEATBATH, false>(edgej, field);
+    }
+}
+
 SweepFns sweep_fns(mcx_algorithm alg, bool table, bool edgej, int field) {
     switch (alg) {
         case MCX_METROPOLIS: return table ? sweep_fns_t<MCX_METROPOLIS, true>(edgej, field)
@@ -617,17 +905,26 @@ SweepFns sweep_fns(mcx_algorithm alg, bool table, bool edgej, int field) {
 
 template <bool EDGEJ>
 void recompute_launch(int field, int grid, cudaStream_t st, const GraphDev& g, long long nslices, double* part2,
-                      long long* ilpi) {
-    if (field == F_VECTOR) k_graph_recompute<EDGEJ, F_VECTOR><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
-    else if (field == F_UNIFORM) k_graph_recompute<EDGEJ, F_UNIFORM><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
-    else k_graph_recompute<EDGEJ, F_NONE><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi);
+                      long long* ilpi, long long* qsum) {
+    if (field == F_VECTOR)
+        k_graph_recompute<EDGEJ, F_VECTOR><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi, qsum);
+    else if (field == F_UNIFORM)
+        k_graph_recompute<EDGEJ, F_UNIFORM><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi, qsum);
+    else k_graph_recompute<EDGEJ, F_NONE><<<grid, kGraphBlock, 0, st>>>(g, nslices, part2, ilpi, qsum);
 }
 
 template <bool EDGEJ>
-void site_launch(int field, cudaStream_t st, const GraphDev& g, long long p, int op, double* out) {
-    if (field == F_VECTOR) k_graph_site<EDGEJ, F_VECTOR><<<1, 32, 0, st>>>(g, p, op, out);
-    else if (field == F_UNIFORM) k_graph_site<EDGEJ, F_UNIFORM><<<1, 32, 0, st>>>(g, p, op, out);
-    else k_graph_site<EDGEJ, F_NONE><<<1, 32, 0, st>>>(g, p, op, out);
+void site_launch(bool bc, int field, cudaStream_t st, const GraphDev& g, long long p, int target, int op,
+                 double* out) {
+    if (bc) {
+        if (field == F_VECTOR) k_bcg_site<EDGEJ, F_VECTOR><<<1, 32, 0, st>>>(g, p, target, op, out);
+        else if (field == F_UNIFORM) k_bcg_site<EDGEJ, F_UNIFORM><<<1, 32, 0, st>>>(g, p, target, op, out);
+        else k_bcg_site<EDGEJ, F_NONE><<<1, 32, 0, st>>>(g, p, target, op, out);
+        return;
+    }
+    if (field == F_VECTOR) k_graph_site<EDGEJ, F_VECTOR><<<1, 32, 0, st>>>(g, p, target, op, out);
+    else if (field == F_UNIFORM) k_graph_site<EDGEJ, F_UNIFORM><<<1, 32, 0, st>>>(g, p, target, op, out);
+    else k_graph_site<EDGEJ, F_NONE><<<1, 32, 0, st>>>(g, p, target, op, out);
 }
 
 // 53-bit threshold of "u < p" for u = k 2^-53: k < ceil(p 2^53).
@@ -653,7 +950,8 @@ struct mcx_graph {
     int dmax = 0;
     bool edgej = false;
     int field = F_NONE;
-    double J = 1.0, h = 0.0;
+    bool bc = false;                // Blume-Capel (spins in {-1, 0, 1})
+    double J = 1.0, h = 0.0, D = 0.0;
     std::vector<int32_t> colour;    // per vertex
     std::vector<GClass> classes;
     int nparts = 0;                 // partial-sum slots over all classes
@@ -674,6 +972,7 @@ struct mcx_graph {
     long long* d_M = nullptr;
     unsigned long long* d_acc = nullptr;
     long long* d_ilpi = nullptr;
+    long long* d_qsum = nullptr;
     double* d_part = nullptr;
     int part_cap = 0;               // doubles
     double* d_Eser = nullptr;
@@ -696,6 +995,7 @@ struct mcx_graph {
         g.J2u = split2(J);
         g.h2u = split2(h);
         g.beta32 = (float)beta;
+        g.D = D;
         g.soff = d_soff;
         g.h = d_h;
         g.J = J;
@@ -746,18 +1046,76 @@ mcx_status graph_recompute(mcx_graph* g) {
     if (2 * grid > g->part_cap) return fail(MCX_ERR_INVALID_ARG, "partial-sum buffer too small");
     MCX_CUDA(cudaMemsetAsync(g->d_M, 0, sizeof(long long), st));
     MCX_CUDA(cudaMemsetAsync(g->d_ilpi, 0, sizeof(long long), st));
+    MCX_CUDA(cudaMemsetAsync(g->d_qsum, 0, sizeof(long long), st));
     const GraphDev d = g->dev(0.0);
-    if (g->edgej) recompute_launch<true>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi);
-    else recompute_launch<false>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi);
-    k_graph_recompute_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, grid, g->d_ilpi, g->edgej ? 1 : 0, g->field, g->J,
-                                                        g->h, g->d_M, g->d_E);
+    if (g->edgej) recompute_launch<true>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi, g->d_qsum);
+    else recompute_launch<false>(g->field, grid, st, d, g->nslices, g->d_part, g->d_ilpi, g->d_qsum);
+    k_graph_recompute_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, grid, g->d_ilpi, g->d_qsum, g->edgej ? 1 : 0,
+                                                        g->field, g->bc ? 1 : 0, g->J, g->h, g->D, g->d_M, g->d_E);
     count_launch(g->ctx, 2);
     MCX_CUDA(cudaGetLastError());
     return MCX_OK;
 }
 
+// smallest k in [0, 2^53] with fl(fl(k 2^-53) z) >= w: "r = u z < w" holds exactly for k below
+// it (fl(u z) does not decrease as u grows)
+unsigned long long bisect53(double z, double w) {
+    unsigned long long lo = 0, hi = 1ull << 53;
+    while (lo < hi) {
+        const unsigned long long mid = lo + (hi - lo) / 2;
+        if (((double)mid * 0x1p-53) * z < w) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Blume-Capel tables by the neighbour sum: Metropolis / Glauber [(s_old+1)*2 + b][sum]
+// thresholds and ΔE; heat bath [sum] (T1, T2) and ΔE by [(s_old+1)*3 + s_new+1][sum].
+mcx_status bc_graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
+    const int D_ = g->dmax, width = 2 * D_ + 1;
+    const bool fld = g->field != F_NONE;
+    const double hf = fld ? g->h : 0.0;
+    std::vector<unsigned long long> thr(6 * (size_t)width, 0);
+    std::vector<float2> dE(9 * (size_t)width, make_float2(0.0f, 0.0f));
+    for (int sum = -D_; sum <= D_; ++sum) {
+        const int idx = sum + D_;
+        const double c = g->J * (double)sum;
+        if (alg == MCX_HEATBATH) {
+            const double e1 = (c - hf * (-1.0)) + g->D;
+            const double e3 = (-c - hf) + g->D;
+            const double w1 = mcx_exp(-beta * e1), w2 = mcx_exp(-beta * 0.0), w3 = mcx_exp(-beta * e3);
+            const double z = (w1 + w2) + w3;
+            thr[2 * (size_t)idx] = bisect53(z, w1);
+            thr[2 * (size_t)idx + 1] = bisect53(z, w1 + w2);
+            for (int so = -1; so <= 1; ++so)
+                for (int sn = -1; sn <= 1; ++sn)
+                    dE[(size_t)((so + 1) * 3 + sn + 1) * width + idx] = split2(bc_delta(c, so, sn, hf, fld, g->D));
+        } else {
+            for (int so = -1; so <= 1; ++so)
+                for (int b = 0; b < 2; ++b) {
+                    const int sn = bc_propose_state(so, b);
+                    const double de = bc_delta(c, so, sn, hf, fld, g->D);
+                    const double lr = -beta * de;
+                    const size_t e = (size_t)((so + 1) * 2 + b) * width + idx;
+                    thr[e] = alg == MCX_METROPOLIS ? (lr > 0 ? kAlways53 : threshold53(mcx_exp(lr)))
+                                                   : threshold53(mcx_logistic(lr));
+                    dE[e] = split2(de);
+                }
+        }
+    }
+    MCX_CUDA(cudaMemcpyAsync(g->d_tab, thr.data(), thr.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                             g->ctx->stream));
+    MCX_CUDA(cudaMemcpyAsync(g->d_tabdE, dE.data(), dE.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                             g->ctx->stream));
+    MCX_CUDA(cudaStreamSynchronize(g->ctx->stream));
+    g->tab_alg = (int)alg;
+    g->tab_beta = beta;
+    return MCX_OK;
+}
+
 mcx_status graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
     if (g->tab_alg == (int)alg && g->tab_beta == beta) return MCX_OK;
+    if (g->bc) return bc_graph_table(g, alg, beta);
     const int D = g->dmax, width = 2 * D + 1;
     std::vector<unsigned long long> thr(2 * (size_t)width);
     std::vector<float2> dE(2 * (size_t)width);
@@ -795,16 +1153,17 @@ mcx_status graph_table(mcx_graph* g, mcx_algorithm alg, double beta) {
 
 extern "C" {
 
-MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr, const int32_t* col,
-                                    const double* coupling, double J, const double* field, double h,
-                                    mcx_graph** out) {
+static mcx_status graph_create(mcx_ctx* ctx, bool bc, int64_t n, const int64_t* rowptr, const int32_t* col,
+                               const double* coupling, double J, double D, const double* field, double h,
+                               mcx_graph** out) {
     if (!ctx || !rowptr || !out || (!col && n > 0)) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
     *out = nullptr;
     if (n < 1 || n > (1ll << 30)) return fail(MCX_ERR_INVALID_ARG, "n = %lld sites (1 .. 2^30)", (long long)n);
     if (rowptr[0] != 0) return fail(MCX_ERR_INVALID_ARG, "rowptr[0] must be 0");
     for (int64_t v = 0; v < n; ++v)
         if (rowptr[v + 1] < rowptr[v]) return fail(MCX_ERR_INVALID_ARG, "rowptr decreases at %lld", (long long)v);
-    if (!std::isfinite(J) || !std::isfinite(h)) return fail(MCX_ERR_INVALID_ARG, "J and h must be finite");
+    if (!std::isfinite(J) || !std::isfinite(h) || !std::isfinite(D))
+        return fail(MCX_ERR_INVALID_ARG, "J, D and h must be finite");
     // neighbour lists: in range, strictly increasing; symmetric with equal couplings
     std::vector<int32_t> deg(n, 0);
     for (int64_t v = 0; v < n; ++v) {
@@ -837,6 +1196,8 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
     g->field = field ? F_VECTOR : (h != 0.0 ? F_UNIFORM : F_NONE);
     g->J = J;
     g->h = h;
+    g->bc = bc;
+    g->D = D;
     int dmax = 0;
     for (int64_t v = 0; v < n; ++v) dmax = std::max(dmax, deg[v]);
     g->dmax = dmax;
@@ -928,7 +1289,7 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
     for (size_t k = 0; k < jv.size(); ++k) jv2[k] = split2(jv[k]);
     // device arrays
     mcx_status st = MCX_OK;
-    const size_t tabn = 2 * (size_t)(2 * dmax + 1);
+    const size_t tabn = (bc ? 6 : 2) * (size_t)(2 * dmax + 1), tabdn = (bc ? 9 : 2) * (size_t)(2 * dmax + 1);
     g->part_cap = std::max(g->nparts, 2 * (int)cap_blocks);
     do {
         if ((st = galloc(g, &g->d_spins, (size_t)g->npad))) break;
@@ -941,11 +1302,12 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
         if ((st = galloc(g, &g->d_perm, (size_t)n))) break;
         if ((st = galloc(g, &g->d_lin, (size_t)n))) break;
         if (g->table_mode() && (st = galloc(g, &g->d_tab, tabn))) break;
-        if (g->table_mode() && (st = galloc(g, &g->d_tabdE, tabn))) break;
+        if (g->table_mode() && (st = galloc(g, &g->d_tabdE, tabdn))) break;
         if ((st = galloc(g, &g->d_E, 1))) break;
         if ((st = galloc(g, &g->d_M, 1))) break;
         if ((st = galloc(g, &g->d_acc, 1))) break;
         if ((st = galloc(g, &g->d_ilpi, 1))) break;
+        if ((st = galloc(g, &g->d_qsum, 1))) break;
         if ((st = galloc(g, &g->d_site, 1))) break;
         if ((st = galloc(g, &g->d_classes, (size_t)ncol))) break;
         if ((st = galloc(g, &g->d_part, (size_t)g->part_cap))) break;
@@ -985,6 +1347,18 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
     return MCX_OK;
 }
 
+MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr, const int32_t* col,
+                                    const double* coupling, double J, const double* field, double h,
+                                    mcx_graph** out) {
+    return graph_create(ctx, false, n, rowptr, col, coupling, J, 0.0, field, h, out);
+}
+
+MCX_API mcx_status mcx_bcgraph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr, const int32_t* col,
+                                      const double* coupling, double J, double D, const double* field, double h,
+                                      mcx_graph** out) {
+    return graph_create(ctx, true, n, rowptr, col, coupling, J, D, field, h, out);
+}
+
 MCX_API mcx_status mcx_graph_destroy(mcx_graph* g) {
     if (!g) return MCX_OK;
     if (g->ctx) cudaStreamSynchronize(g->ctx->stream);
@@ -1019,12 +1393,12 @@ MCX_API mcx_status mcx_graph_set_spins(mcx_graph* g, const int8_t* host, size_t 
     // values are checked on the device before any is stored (the counter word is free here)
     unsigned long long bad = 0;
     const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
-    k_graph_validate<<<grid, 256, 0, st>>>(g->d_lin, g->n, g->d_acc);
+    k_graph_validate<<<grid, 256, 0, st>>>(g->d_lin, g->n, g->bc ? 1 : 0, g->d_acc);
     count_launch(g->ctx);
     MCX_CUDA(cudaGetLastError());
     MCX_CUDA(cudaMemcpyAsync(&bad, g->d_acc, sizeof(bad), cudaMemcpyDeviceToHost, st));
     MCX_CUDA(cudaStreamSynchronize(st));
-    if (bad) return fail(MCX_ERR_INVALID_ARG, "%llu values are not +1 or -1", bad);
+    if (bad) return fail(MCX_ERR_INVALID_ARG, "%llu values are not spin states of this model", bad);
     k_graph_scatter<<<grid, 256, 0, st>>>(g->d_lin, g->d_perm, g->n, g->d_spins);
     count_launch(g->ctx);
     MCX_CUDA(cudaGetLastError());
@@ -1048,7 +1422,7 @@ MCX_API mcx_status mcx_graph_init_random(mcx_graph* g, uint64_t seed, uint32_t s
     if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
     const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
     k_graph_init_random<<<grid, 256, 0, g->ctx->stream>>>(g->d_perm, g->n, g->d_spins, (uint32_t)seed,
-                                                          (uint32_t)(seed >> 32), stream);
+                                                          (uint32_t)(seed >> 32), stream, g->bc ? 1 : 0);
     count_launch(g->ctx);
     MCX_CUDA(cudaGetLastError());
     return graph_recompute(g);
@@ -1056,7 +1430,8 @@ MCX_API mcx_status mcx_graph_init_random(mcx_graph* g, uint64_t seed, uint32_t s
 
 MCX_API mcx_status mcx_graph_init_uniform(mcx_graph* g, int8_t value) {
     if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
-    if (value != 1 && value != -1) return fail(MCX_ERR_INVALID_ARG, "value %d is not an Ising state", (int)value);
+    if (value != 1 && value != -1 && !(g->bc && value == 0))
+        return fail(MCX_ERR_INVALID_ARG, "value %d is not a spin state of this model", (int)value);
     const int grid = (int)std::min<long long>((g->n + 255) / 256, (long long)g->ctx->num_sms * 8);
     k_graph_init_uniform<<<grid, 256, 0, g->ctx->stream>>>(g->d_perm, g->n, g->d_spins, value);
     count_launch(g->ctx);
@@ -1078,7 +1453,7 @@ MCX_API mcx_status mcx_graph_energy(mcx_graph* g, int full, double* energy, int6
     return MCX_OK;
 }
 
-static mcx_status graph_site(mcx_graph* g, int64_t i, int op, double* out) {
+static mcx_status graph_site(mcx_graph* g, int64_t i, int target, int op, double* out) {
     if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
     if (i < 0 || i >= g->n) return fail(MCX_ERR_OUT_OF_RANGE, "site %lld outside 0..%lld", (long long)i,
                                         (long long)g->n - 1);
@@ -1087,8 +1462,8 @@ static mcx_status graph_site(mcx_graph* g, int64_t i, int op, double* out) {
     MCX_CUDA(cudaMemcpyAsync(&p, g->d_perm + i, sizeof(p), cudaMemcpyDeviceToHost, st));
     MCX_CUDA(cudaStreamSynchronize(st));
     const GraphDev d = g->dev(0.0);
-    if (g->edgej) site_launch<true>(g->field, st, d, p, op, g->d_site);
-    else site_launch<false>(g->field, st, d, p, op, g->d_site);
+    if (g->edgej) site_launch<true>(g->bc, g->field, st, d, p, target, op, g->d_site);
+    else site_launch<false>(g->bc, g->field, st, d, p, target, op, g->d_site);
     count_launch(g->ctx);
     MCX_CUDA(cudaGetLastError());
     double v = 0.0;
@@ -1099,10 +1474,28 @@ static mcx_status graph_site(mcx_graph* g, int64_t i, int op, double* out) {
 }
 
 MCX_API mcx_status mcx_graph_delta_energy(mcx_graph* g, int64_t i, double* delta_energy) {
-    return graph_site(g, i, 0, delta_energy);
+    if (g && g->bc) return fail(MCX_ERR_INVALID_ARG, "a Blume-Capel site needs the new state: mcx_graph_delta_energy_to");
+    return graph_site(g, i, 2, 0, delta_energy);
 }
 
-MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i) { return graph_site(g, i, 1, nullptr); }
+MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i) {
+    if (g && g->bc) return fail(MCX_ERR_INVALID_ARG, "a Blume-Capel site needs the new state: mcx_graph_set_site");
+    return graph_site(g, i, 2, 1, nullptr);
+}
+
+MCX_API mcx_status mcx_graph_delta_energy_to(mcx_graph* g, int64_t i, int8_t s_new, double* delta_energy) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (s_new < -1 || s_new > 1 || (!g->bc && s_new == 0))
+        return fail(MCX_ERR_INVALID_ARG, "%d is not a spin state of this model", (int)s_new);
+    return graph_site(g, i, s_new, 0, delta_energy);
+}
+
+MCX_API mcx_status mcx_graph_set_site(mcx_graph* g, int64_t i, int8_t s_new) {
+    if (!g) return fail(MCX_ERR_INVALID_ARG, "graph is NULL");
+    if (s_new < -1 || s_new > 1 || (!g->bc && s_new == 0))
+        return fail(MCX_ERR_INVALID_ARG, "%d is not a spin state of this model", (int)s_new);
+    return graph_site(g, i, s_new, 1, nullptr);
+}
 
 MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng, int64_t nsweeps,
                                    double* E_series, int64_t* M_series, mcx_counters* counters) {
@@ -1126,7 +1519,7 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
         MCX_CHECK(galloc(g, &g->d_Mser, (size_t)nsweeps));
         g->ser_cap = nsweeps;
     }
-    const SweepFns fns = sweep_fns(alg, table, g->edgej, g->field);
+    const SweepFns fns = g->bc ? bc_sweep_fns(alg, table, g->edgej, g->field) : sweep_fns(alg, table, g->edgej, g->field);
     MCX_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(unsigned long long), st));
     const GraphDev d = g->dev(beta);
     const uint32_t k0 = (uint32_t)rng->seed, k1 = (uint32_t)(rng->seed >> 32);

@@ -367,14 +367,35 @@ def IsingLatticeOptim(Lx, Ly, *, layout="int8", ctx=None):
     return IsingDevice([Lx, Ly], J=1, h=0, layout=layout, ctx=ctx)
 
 
-def BlumeCapel(dims, *, J=1, D=0, periodic=True, h=0, ctx=None):
-    """BlumeCapel(dims; J=1, D=0, periodic=true, h=0) (SpinSystems/src/blume_capel.jl:500-511)."""
-    return BlumeCapelDevice(dims, J=J, D=D, h=h, periodic=periodic, ctx=ctx)
+def BlumeCapel(dims, J=None, D=0, *, periodic=True, h=0, ctx=None):
+    """The reference's BlumeCapel constructors (SpinSystems/src/blume_capel.jl:467-511), all
+    spins up: ``BlumeCapel(dims; J=1, D=0, periodic=true, h=0)`` on the colour-split lattice
+    for a scalar J and h on an even periodic 2-D / 3-D grid (every side >= 4), otherwise on
+    the general-graph path; ``BlumeCapel(graph, J, D; h)``, ``BlumeCapel(graph, Jvec, D; h)``
+    and ``BlumeCapel(J::sparse, D; h)``."""
+    from . import graph as G
+    if isinstance(dims, G.SimpleGraph):
+        if J is None or np.isscalar(J):
+            return G.BlumeCapelGraph(dims, 1 if J is None else J, D, h=h, ctx=ctx)
+        return G.BlumeCapelMatrix(G.matrix_from_edges(dims, J), D, h=h, ctx=ctx)
+    if not isinstance(dims, (list, tuple, np.ndarray)):
+        return G.BlumeCapelMatrix(dims, 0 if J is None else J, h=h, ctx=ctx)  # BlumeCapel(J::sparse, D; h)
+    J = 1 if J is None else J
+    dims = [int(d) for d in dims]
+    if np.isscalar(J) and np.isscalar(h) and periodic and _lattice_ok(dims):
+        return BlumeCapelDevice(dims, J=J, D=D, h=h, periodic=periodic, ctx=ctx)
+    g = G.grid(dims, periodic=periodic)
+    if np.isscalar(J):
+        return G.BlumeCapelGraph(g, J, D, h=h, ctx=ctx)
+    import scipy.sparse as sp
+    if sp.issparse(J):
+        return G.BlumeCapelMatrix(J, D, h=h, ctx=ctx)
+    return G.BlumeCapelMatrix(G.matrix_from_edges(g, J), D, h=h, ctx=ctx)
 
 
 def _is_graph(sys):
-    from .graph import IsingGraphDevice
-    return isinstance(sys, IsingGraphDevice)
+    from .graph import GraphDevice
+    return isinstance(sys, GraphDevice)
 
 
 def set_spins_(sys, values):
@@ -394,7 +415,7 @@ def init_(sys, type, rng=None):
         from . import graph as G
         if t == "random" and rng is None:
             raise ArgumentError("Random initialization requires rng")
-        if t not in ("random", "up", "down"):
+        if t not in ("random", "up", "down", "zero") or (t == "zero" and 0 not in sys.STATES):
             raise ArgumentError("Unknown initialization type: %s" % type)
         G.init(sys, t, rng)
         return sys

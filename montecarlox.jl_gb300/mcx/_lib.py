@@ -112,6 +112,10 @@ SIGNATURES = {
     "mcx_wait_flag_test": (C.c_int, [_P, C.c_int64]),
     "mcx_graph_create": (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, _P, C.c_double, C.POINTER(_P)]),
     "mcx_graph_destroy": (C.c_int, [_P]),
+    "mcx_bcgraph_create": (C.c_int, [_P, C.c_int64, _P, _P, _P, C.c_double, C.c_double, _P, C.c_double,
+                                     C.POINTER(_P)]),
+    "mcx_graph_delta_energy_to": (C.c_int, [_P, C.c_int64, C.c_int8, _f64p]),
+    "mcx_graph_set_site": (C.c_int, [_P, C.c_int64, C.c_int8]),
     "mcx_graph_info": (C.c_int, [_P, _i64p, _i32p, _i64p, _i64p]),
     "mcx_graph_colours": (C.c_int, [_P, _P, C.c_size_t]),
     "mcx_graph_set_spins": (C.c_int, [_P, _P, C.c_size_t]),

@@ -31,10 +31,10 @@ def export_state(obj):
         return {"kind": "lattice", "model": "bc" if isinstance(obj, BlumeCapelDevice) else "ising",
                 "dims": list(obj.dims), "J": obj.J, "D": obj.D, "h": obj.h, "layout": obj.layout,
                 "spins": obj.spins}
-    from .graph import IsingGraphDevice
-    if isinstance(obj, IsingGraphDevice):
-        return {"kind": "graph", "rowptr": obj.rowptr, "col": obj.col, "coupling": obj.coupling, "J": obj.J,
-                "field": obj.field, "h": obj.h, "spins": obj.spins}
+    from .graph import GraphDevice
+    if isinstance(obj, GraphDevice):
+        return {"kind": "graph", "model": obj.MODEL, "rowptr": obj.rowptr, "col": obj.col, "coupling": obj.coupling,
+                "J": obj.J, "D": obj.D, "field": obj.field, "h": obj.h, "spins": obj.spins}
     if isinstance(obj, Philox):
         return {"kind": "rng", "seed": obj.seed, "stream": obj.stream, "counter": obj.counter}
     if isinstance(obj, (Metropolis, Glauber)):
@@ -89,9 +89,13 @@ def import_state(d, ctx=None):
         s.spins = d["spins"]
         return s
     if k == "graph":
-        from .graph import IsingGraphDevice
-        s = IsingGraphDevice(d["rowptr"], d["col"], d["coupling"], J=1.0 if d["J"] is None else d["J"],
-                             h=d["field"] if d["field"] is not None else d["h"], ctx=ctx)
+        from .graph import IsingGraphDevice, BlumeCapelGraphDevice
+        J = 1.0 if d["J"] is None else d["J"]
+        h = d["field"] if d["field"] is not None else d["h"]
+        if d.get("model", "Ising") == "BlumeCapel":
+            s = BlumeCapelGraphDevice(d["rowptr"], d["col"], d["coupling"], J=J, D=d["D"], h=h, ctx=ctx)
+        else:
+            s = IsingGraphDevice(d["rowptr"], d["col"], d["coupling"], J=J, h=h, ctx=ctx)
         s.spins = d["spins"]
         return s
     if k in ("Metropolis", "Glauber"):

@@ -1,10 +1,12 @@
-"""Ising models on general graphs and sparse couplings over the C ABI.
+"""Ising and Blume-Capel models on general graphs and sparse couplings over the C ABI.
 
 Reference (paths inside MonteCarloX.jl):
   IsingGraph  (one J over a graph; no / uniform / per-site field)  SpinSystems/src/ising.jl:86-218
   IsingMatrix (symmetric sparse J_ij; same fields)                ising.jl:221-377
   Ising(graph, J; h), Ising(J::SparseMatrixCSC; h),
   Ising(graph, Jvec; h), Ising(dims; J, periodic, h)              ising.jl:383-428
+  BlumeCapelGraph / BlumeCapelMatrix (crystal field D)           SpinSystems/src/blume_capel.jl:117-466
+  BlumeCapel(graph, J, D; h), BlumeCapel(J, D; h), ...           blume_capel.jl:467-511
 
 The reference takes its graphs from Graphs.jl (compat "1", not vendored); the parts it
 uses are restated here from that package's published behaviour: a SimpleGraph is an
@@ -22,7 +24,8 @@ from . import _lib as L
 from . import (AbstractSpinSystem, ArgumentError, HeatBath, Philox, _check, default_context)
 
 __all__ = ["SimpleGraph", "nv", "ne", "neighbors", "edges", "add_edge_", "grid", "IsingGraph", "IsingMatrix",
-           "IsingGraphDevice", "delta_energy", "modify_", "graph_csr"]
+           "BlumeCapelGraph", "BlumeCapelMatrix", "GraphDevice", "IsingGraphDevice", "BlumeCapelGraphDevice",
+           "delta_energy", "modify_", "graph_csr"]
 
 
 class SimpleGraph:
@@ -105,10 +108,19 @@ def _field(h, n):
     return hv, 0.0
 
 
-class IsingGraphDevice(AbstractSpinSystem):
-    """An Ising system on a neighbour list held on the device (IsingGraph when
-    ``coupling`` is None, IsingMatrix otherwise).  All spins start at +1."""
+class GraphDevice(AbstractSpinSystem):
+    """A spin system on a neighbour list held on the device (one coupling J when
+    ``coupling`` is None, per-entry couplings otherwise).  All spins start at +1."""
     STATES = (-1, 1)
+    MODEL = "Ising"
+    D = 0.0
+
+    def _create(self, hdl):
+        _check(L.load().mcx_graph_create(
+            self.ctx.handle, self.N, self.rowptr.ctypes.data, self.col.ctypes.data,
+            None if self.coupling is None else self.coupling.ctypes.data,
+            float(self.J) if self.coupling is None else 0.0,
+            None if self.field is None else self.field.ctypes.data, self.h, C.byref(hdl)))
 
     def __init__(self, rowptr, col, coupling=None, J=1.0, h=0.0, ctx=None):
         self.ctx = ctx or default_context()
@@ -121,15 +133,12 @@ class IsingGraphDevice(AbstractSpinSystem):
         self.field, self.h = _field(h, self.N)
         self.J = float(J) if self.coupling is None else None
         hdl = C.c_void_p()
-        _check(L.load().mcx_graph_create(
-            self.ctx.handle, self.N, self.rowptr.ctypes.data, self.col.ctypes.data,
-            None if self.coupling is None else self.coupling.ctypes.data, float(J) if self.coupling is None else 0.0,
-            None if self.field is None else self.field.ctypes.data, self.h, C.byref(hdl)))
+        self._create(hdl)
         self.handle = hdl
 
     @property
     def kind(self):
-        return "IsingGraph" if self.coupling is None else "IsingMatrix"
+        return self.MODEL + ("Graph" if self.coupling is None else "Matrix")
 
     def __len__(self):
         return self.N
@@ -171,6 +180,27 @@ class IsingGraphDevice(AbstractSpinSystem):
             pass
 
 
+class IsingGraphDevice(GraphDevice):
+    """IsingGraph / IsingMatrix on the device."""
+
+
+class BlumeCapelGraphDevice(GraphDevice):
+    """BlumeCapelGraph / BlumeCapelMatrix on the device (spins in {-1, 0, 1})."""
+    STATES = (-1, 0, 1)
+    MODEL = "BlumeCapel"
+
+    def __init__(self, rowptr, col, coupling=None, J=1.0, D=0.0, h=0.0, ctx=None):
+        self.D = float(D)
+        super().__init__(rowptr, col, coupling, J=J, h=h, ctx=ctx)
+
+    def _create(self, hdl):
+        _check(L.load().mcx_bcgraph_create(
+            self.ctx.handle, self.N, self.rowptr.ctypes.data, self.col.ctypes.data,
+            None if self.coupling is None else self.coupling.ctypes.data,
+            float(self.J) if self.coupling is None else 0.0, self.D,
+            None if self.field is None else self.field.ctypes.data, self.h, C.byref(hdl)))
+
+
 def IsingGraph(graph, J=1, *, h=0, ctx=None):
     """IsingGraph(graph, J; h) (ising.jl:117-139); self-loops are not supported."""
     if any(v in graph._adj[v] for v in range(nv(graph))):
@@ -179,9 +209,7 @@ def IsingGraph(graph, J=1, *, h=0, ctx=None):
     return IsingGraphDevice(rowptr, col, None, J=J, h=h, ctx=ctx)
 
 
-def IsingMatrix(J, *, h=0, ctx=None):
-    """IsingMatrix(J::SparseMatrixCSC; h) (ising.jl:265-292): a square symmetric scipy
-    sparse matrix or a dense 2-D array; diagonal entries are ignored."""
+def _csr(J):
     import scipy.sparse as sp
     A = J if sp.issparse(J) else sp.csr_matrix(np.asarray(J, np.float64))
     if A.shape[0] != A.shape[1]:
@@ -189,7 +217,28 @@ def IsingMatrix(J, *, h=0, ctx=None):
     A = sp.csr_matrix(A, dtype=np.float64)
     A.sum_duplicates()
     A.sort_indices()
-    return IsingGraphDevice(A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data, h=h, ctx=ctx)
+    return A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data
+
+
+def IsingMatrix(J, *, h=0, ctx=None):
+    """IsingMatrix(J::SparseMatrixCSC; h) (ising.jl:265-292): a square symmetric scipy
+    sparse matrix or a dense 2-D array; diagonal entries are ignored."""
+    rp, col, val = _csr(J)
+    return IsingGraphDevice(rp, col, val, h=h, ctx=ctx)
+
+
+def BlumeCapelGraph(graph, J=1, D=0, *, h=0, ctx=None):
+    """BlumeCapelGraph(graph, J, D; h) (blume_capel.jl:154-190)."""
+    if any(v in graph._adj[v] for v in range(nv(graph))):
+        raise ArgumentError("self-loops are not supported")
+    rowptr, col = graph_csr(graph)
+    return BlumeCapelGraphDevice(rowptr, col, None, J=J, D=D, h=h, ctx=ctx)
+
+
+def BlumeCapelMatrix(J, D=0, *, h=0, ctx=None):
+    """BlumeCapelMatrix(J::SparseMatrixCSC, D; h) (blume_capel.jl:328-360)."""
+    rp, col, val = _csr(J)
+    return BlumeCapelGraphDevice(rp, col, val, D=D, h=h, ctx=ctx)
 
 
 def matrix_from_edges(graph, Jvec):
@@ -207,16 +256,23 @@ def matrix_from_edges(graph, Jvec):
     return sp.csr_matrix((np.concatenate([Jvec, Jvec]), (u, v)), shape=(nv(graph), nv(graph)))
 
 
-def delta_energy(sys, i):
-    """delta_energy(sys, i) (ising.jl:20-23), 0-based site."""
+def delta_energy(sys, i, s_new=None):
+    """delta_energy(sys, i) of a flip (Ising, ising.jl:20-23) or delta_energy(sys, i, s_new)
+    (blume_capel.jl:32-35); 0-based site."""
     out = C.c_double()
-    _check(L.load().mcx_graph_delta_energy(sys.handle, int(i), C.byref(out)))
+    if s_new is None:
+        _check(L.load().mcx_graph_delta_energy(sys.handle, int(i), C.byref(out)))
+    else:
+        _check(L.load().mcx_graph_delta_energy_to(sys.handle, int(i), int(s_new), C.byref(out)))
     return out.value
 
 
-def modify_(sys, i):
-    """modify!(sys, i, flip_changes(sys, i)...): flip site i and update the cache."""
-    _check(L.load().mcx_graph_flip(sys.handle, int(i)))
+def modify_(sys, i, s_new=None):
+    """modify!(sys, i, ...): flip site i (Ising) or set it to s_new, updating the cache."""
+    if s_new is None:
+        _check(L.load().mcx_graph_flip(sys.handle, int(i)))
+    else:
+        _check(L.load().mcx_graph_set_site(sys.handle, int(i), int(s_new)))
     return sys
 
 
@@ -249,4 +305,4 @@ def init(sys, t, rng=None):
         r = rng if isinstance(rng, Philox) else Philox(rng)
         _check(L.load().mcx_graph_init_random(sys.handle, r.seed, r.stream))
     else:
-        _check(L.load().mcx_graph_init_uniform(sys.handle, {"up": 1, "down": -1}[t]))
+        _check(L.load().mcx_graph_init_uniform(sys.handle, {"up": 1, "down": -1, "zero": 0}[t]))

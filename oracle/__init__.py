@@ -77,6 +77,18 @@ def lib():
                                       C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
                                       C.POINTER(C.c_double), C.POINTER(C.c_int64), vp, vp,
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_bcg_delta_energy.argtypes = [i8p, C.c_int64, C.c_int, i64p, i32p, vp, C.c_double, C.c_double, vp,
+                                           C.c_double]
+        L.orc_bcg_delta_energy.restype = C.c_double
+        L.orc_bcg_observables.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, C.c_double, vp, C.c_double,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        L.orc_bcg_observables.restype = None
+        L.orc_bcg_init_random.argtypes = [i8p, C.c_int64, C.c_uint64, C.c_uint32]
+        L.orc_bcg_init_random.restype = None
+        L.orc_bcg_sweep.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, C.c_double, vp, C.c_double, C.c_int,
+                                    C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_int64), vp, vp, C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_uint64)]
         L.orc_tau_int.argtypes = [f64p, C.c_int64, C.c_int64, C.c_double]
         L.orc_tau_int.restype = C.c_double
         _lib = L
@@ -211,6 +223,49 @@ class Graph:
 
     def _ptrs(self):
         return (None if self.Jv is None else self.Jv.ctypes.data, None if self.hv is None else self.hv.ctypes.data)
+
+
+class BCGraph(Graph):
+    """A Blume-Capel neighbour list for the oracle: Graph plus the crystal field D."""
+
+    def __init__(self, rowptr, col, Jv=None, J=1.0, D=0.0, hv=None, h=0.0):
+        super().__init__(rowptr, col, Jv=Jv, J=J, hv=hv, h=h)
+        self.D = float(D)
+
+
+def bcg_init_random(n, seed, stream=0):
+    s = np.zeros(n, np.int8)
+    lib().orc_bcg_init_random(s, n, seed, stream)
+    return s
+
+
+def bcg_delta_energy(g, s, v, s_new):
+    jv, hv = g._ptrs()
+    return float(lib().orc_bcg_delta_energy(np.ascontiguousarray(s, np.int8), v, int(s_new), g.rowptr, g.col, jv,
+                                            g.J, g.D, hv, g.h))
+
+
+def bcg_observables(g, s):
+    jv, hv = g._ptrs()
+    E, M = C.c_double(), C.c_int64()
+    lib().orc_bcg_observables(np.ascontiguousarray(s, np.int8), g.n, g.rowptr, g.col, jv, g.J, g.D, hv, g.h,
+                              C.byref(E), C.byref(M))
+    return E.value, M.value
+
+
+def bcg_sweep(g, s, alg, beta, seed, stream=0, sweep0=0, nsweeps=1):
+    """Blume-Capel colour-class sweeps in place; returns (E[nsweeps], M[nsweeps], attempts, accepts)."""
+    jv, hv = g._ptrs()
+    E0, M0 = bcg_observables(g, s)
+    E, M = C.c_double(E0), C.c_int64(M0)
+    Es = np.zeros(nsweeps, np.float64)
+    Ms = np.zeros(nsweeps, np.int64)
+    att, acc = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_bcg_sweep(s, g.n, g.rowptr, g.col, jv, g.J, g.D, hv, g.h, alg, beta, seed, stream, sweep0, nsweeps,
+                             C.byref(E), C.byref(M), Es.ctypes.data, Ms.ctypes.data, C.byref(att), C.byref(acc))
+    if rc != OK:
+        raise ValueError("oracle bcg_sweep failed: %d" % rc)
+    return Es, Ms, att.value, acc.value
 
 
 def graph_colour(g):

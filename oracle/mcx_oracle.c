@@ -887,3 +887,164 @@ double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c) {
     free(ce);
     return tau > 0.5 ? tau : 0.5;
 }
+
+/* ---------------------------------------------------------------------------
+ * Blume-Capel on general graphs: BlumeCapelGraph (one J, blume_capel.jl:117-276) and
+ * BlumeCapelMatrix (symmetric sparse J_ij, :278-466), no / uniform / per-site field.
+ * Spins in {-1, 0, 1}; Jv NULL means one coupling J.
+ * ------------------------------------------------------------------------- */
+
+/* local_coupling: J * sum_j s_j (:241-243) or the FP64 sum of J_ij s_j over the row,
+ * diagonal skipped (:368-377) */
+static double bcg_coupling(const int8_t* s, int64_t v, const int64_t* rowptr, const int32_t* col,
+                           const double* Jv, double J) {
+    if (Jv) {
+        double acc = 0.0;
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+            if (col[e] != v) acc += Jv[e] * (double)s[col[e]];
+        return acc;
+    }
+    int64_t sum = 0;
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+        if (col[e] != v) sum += s[col[e]];
+    return J * (double)sum;
+}
+
+static double bcg_field(int64_t v, const double* hv, double h) { return hv ? hv[v] : h; }
+
+/* delta_energy(sys, i, s_new), :32-35 with propose_changes :245-251 and :259-260:
+ * -Δspin*c - h Δspin + D Δspin2 */
+double orc_bcg_delta_energy(const int8_t* s, int64_t v, int s_new, const int64_t* rowptr,
+                            const int32_t* col, const double* Jv, double J, double D,
+                            const double* hv, double h) {
+    int so = s[v];
+    int ds = s_new - so, ds2 = s_new * s_new - so * so;
+    double dpair = (double)ds * bcg_coupling(s, v, rowptr, col, Jv, J);
+    double dfield = (hv || h != 0.0) ? bcg_field(v, hv, h) * (double)ds : 0.0;
+    return (-dpair - dfield) + D * (double)ds2;
+}
+
+/* _full_energy (:213-214, :396-423) and sum(spins) */
+void orc_bcg_observables(const int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                         const double* Jv, double J, double D, const double* hv, double h,
+                         double* E, int64_t* M) {
+    double pair;
+    if (Jv) {
+        double acc = 0.0;
+        for (int64_t v = 0; v < n; ++v) {
+            double a = 0.0;
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+                if (col[e] != v) a += ((double)s[v] * Jv[e]) * (double)s[col[e]];
+            acc += a;
+        }
+        pair = acc / 2;
+    } else {
+        double pu = 0.0;
+        for (int64_t v = 0; v < n; ++v) {
+            int64_t a = 0;
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+                if (col[e] != v) a += s[v] * s[col[e]];
+            pu += (double)a;
+        }
+        pair = J * (pu / 2);
+    }
+    int64_t m = 0, q = 0;
+    double field = 0.0;
+    for (int64_t v = 0; v < n; ++v) {
+        m += s[v];
+        q += s[v] * s[v];
+        if (hv) field += hv[v] * (double)s[v];
+    }
+    if (!hv) field = h * (double)m;
+    *E = (-pair - field) + D * (double)q;
+    *M = m;
+}
+
+/* init!(sys, :random) of a graph: state floor(3 w / 2^32) - 1 from word v&3 of block
+ * (v>>2, 0, 8<<24, stream) */
+void orc_bcg_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int64_t v = 0; v < n; ++v) {
+        uint32_t ctr[4] = {(uint32_t)(v >> 2), 0u, 8u << 24, stream}, out[4];
+        orc_philox4x32_10(ctr, key, out);
+        s[v] = (int8_t)((int)(((uint64_t)out[v & 3] * 3u) >> 32) - 1);
+    }
+}
+
+/* Colour-class sweeps (the order and uniforms of orc_graph_sweep); the proposal of
+ * Metropolis / Glauber is bit 0 of the low word of the site's uniform (a bit the 53-bit
+ * uniform does not use), standing in for rand(rng, Bool) of _propose_state (:21-30).
+ *   Metropolis / Glauber: spin_flip! :50-57 (accept!(alg, ΔE)).
+ *   HeatBath: :59-85 -- three Boltzmann weights, r = u z, cumulative choice. */
+int orc_bcg_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                  const double* Jv, double J, double D, const double* hv, double h, int alg,
+                  double beta, uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps,
+                  double* E, int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
+                  uint64_t* accepts) {
+    if (alg < ORC_METROPOLIS || alg > ORC_HEATBATH || n < 1) return ORC_ERR_INVALID;
+    int32_t* colour = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    int ncol = orc_graph_colour(n, rowptr, col, colour);
+    int64_t* order = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    uint64_t* block = (uint64_t*)malloc((size_t)n * sizeof(uint64_t));
+    int* word = (int*)malloc((size_t)n * sizeof(int));
+    int64_t q = 0;
+    uint64_t B_c = 0;
+    for (int c = 0; c < ncol; ++c) {
+        int64_t l = 0;
+        for (int64_t v = 0; v < n; ++v)
+            if (colour[v] == c) {
+                order[q] = v;
+                block[q] = B_c + 32 * (uint64_t)(l >> 6) + (uint64_t)(l & 31);
+                word[q] = 2 * (int)((l >> 5) & 1);
+                ++q;
+                ++l;
+            }
+        B_c += 32 * (uint64_t)((l + 63) / 64);
+    }
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint64_t acc_n = 0;
+    for (int64_t t = 0; t < nsweeps; ++t) {
+        uint64_t sw = sweep0 + (uint64_t)t;
+        for (q = 0; q < n; ++q) {
+            int64_t v = order[q];
+            uint32_t ctr[4] = {(uint32_t)block[q], (uint32_t)sw,
+                               ((uint32_t)(sw >> 32) & 0xFFFFu) | (7u << 24), stream}, out[4];
+            orc_philox4x32_10(ctr, key, out);
+            uint32_t hi = out[word[q]], lo = out[word[q] + 1];
+            double u = u53(hi, lo);
+            int so = s[v], sn;
+            if (alg == ORC_HEATBATH) {
+                double c = bcg_coupling(s, v, rowptr, col, Jv, J);
+                double hi_ = (hv || h != 0.0) ? bcg_field(v, hv, h) : 0.0;
+                double e1 = (c - hi_ * (-1.0)) + D;
+                double e3 = (-c - hi_) + D;
+                double w1 = orc_exp(-beta * e1), w2 = orc_exp(-beta * 0.0), w3 = orc_exp(-beta * e3);
+                double z = (w1 + w2) + w3;
+                double r = u * z;
+                sn = r < w1 ? -1 : (r < w1 + w2 ? 0 : 1);
+            } else {
+                sn = bc_propose(so, (int)(lo & 1u));
+                double dE = orc_bcg_delta_energy(s, v, sn, rowptr, col, Jv, J, D, hv, h);
+                double lr = -beta * dE;
+                int acc = alg == ORC_METROPOLIS ? ((lr > 0) || (u < orc_exp(lr))) : (u < orc_logistic(lr));
+                if (!acc) sn = so;
+            }
+            if (sn != so) {
+                double dE = orc_bcg_delta_energy(s, v, sn, rowptr, col, Jv, J, D, hv, h);
+                s[v] = (int8_t)sn;
+                *E += dE;
+                *M += sn - so;
+                ++acc_n;
+            }
+        }
+        if (E_series) E_series[t] = *E;
+        if (M_series) M_series[t] = *M;
+    }
+    *attempts += (uint64_t)n * (uint64_t)nsweeps;
+    *accepts += acc_n;
+    free(word);
+    free(block);
+    free(order);
+    free(colour);
+    return ORC_OK;
+}

@@ -86,6 +86,20 @@ int orc_graph_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* 
                     int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
                     uint64_t* accepts);
 
+/* Blume-Capel on general graphs (BlumeCapelGraph / BlumeCapelMatrix); Jv / hv may be NULL */
+double orc_bcg_delta_energy(const int8_t* s, int64_t v, int s_new, const int64_t* rowptr,
+                            const int32_t* col, const double* Jv, double J, double D,
+                            const double* hv, double h);
+void orc_bcg_observables(const int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                         const double* Jv, double J, double D, const double* hv, double h,
+                         double* E, int64_t* M);
+void orc_bcg_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream);
+int orc_bcg_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                  const double* Jv, double J, double D, const double* hv, double h, int alg,
+                  double beta, uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps,
+                  double* E, int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
+                  uint64_t* accepts);
+
 /* integrated autocorrelation time (-1 on invalid arguments) */
 double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c);
 

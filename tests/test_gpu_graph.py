@@ -198,3 +198,85 @@ def test_graph_errors(gpu):
         __import__("mcx.graph", fromlist=["x"]).delta_energy(d, 4)
     with pytest.raises(gpu.ArgumentError):
         gpu.init_(d, "zero")
+
+
+# ---------------------------------------------------------------- Blume-Capel --
+def _bc_case(name):
+    if name == "bc_grid8":
+        n, es = grid_edges([8, 8], True)
+        return O.BCGraph(*from_edges(n, es)[:2], J=1.0, D=0.5)
+    if name == "bc_open7x5_uniform_h":
+        n, es = grid_edges([7, 5], False)
+        return O.BCGraph(*from_edges(n, es)[:2], J=1.0, D=1.0, h=0.2)
+    if name == "bc_random_gauss_vector_h":
+        es = random_edges(2500, 6000, 31)
+        rp, col, val = from_edges(2500, es, np.random.default_rng(32).normal(size=len(es)))
+        return O.BCGraph(rp, col, Jv=val, D=0.3, hv=np.random.default_rng(33).normal(size=2500) * 0.5)
+    if name == "bc_hub":
+        es = hub_edges(1000, 150, 34)
+        return O.BCGraph(*from_edges(1000, es)[:2], J=0.5, D=0.2)
+    if name == "bc_cube_vector_h":  # one J, a field per site: FP64 path
+        n, es = grid_edges([6, 6, 6], True)
+        return O.BCGraph(*from_edges(n, es)[:2], J=1.0, D=0.6, hv=np.random.default_rng(35).normal(size=n))
+    if name == "bc_big_table":  # above the one-block limit
+        n, es = grid_edges([120, 100], False)
+        return O.BCGraph(*from_edges(n, es)[:2], J=1.0, D=1.0, h=0.05)
+    if name == "bc_big_gauss":
+        es = random_edges(12000, 30000, 36)
+        rp, col, val = from_edges(12000, es, np.random.default_rng(37).normal(size=len(es)))
+        return O.BCGraph(rp, col, Jv=val, D=0.5)
+    raise KeyError(name)
+
+
+BC_CASES = [("bc_grid8", "metropolis", 0.6), ("bc_grid8", "heatbath", 0.6), ("bc_open7x5_uniform_h", "glauber", 0.5),
+            ("bc_random_gauss_vector_h", "metropolis", 1.0), ("bc_random_gauss_vector_h", "heatbath", 1.0),
+            ("bc_hub", "glauber", 0.7), ("bc_hub", "heatbath", 1.5), ("bc_cube_vector_h", "heatbath", 0.4),
+            ("bc_big_table", "metropolis", 0.6), ("bc_big_table", "heatbath", 0.6), ("bc_big_gauss", "glauber", 1.2)]
+
+
+@pytest.mark.parametrize("name,alg,beta", BC_CASES)
+def test_blume_capel_graph_parity(gpu, name, alg, beta):
+    from mcx.graph import BlumeCapelGraphDevice
+    g = _bc_case(name)
+    sysd = BlumeCapelGraphDevice(g.rowptr, g.col, g.Jv, J=g.J, D=g.D, h=g.hv if g.hv is not None else g.h)
+    gpu.init_(sysd, "random", rng=gpu.Philox(41, 1))
+    s = O.bcg_init_random(g.n, 41, 1)
+    assert np.array_equal(sysd.spins, s)
+    a = _alg(gpu, alg, 43, beta, stream=2, counter=7)
+    Es, Ms = gpu.sweep_(sysd, a, 6, record=True)
+    oE, oM, att, acc = O.bcg_sweep(g, s, ALG[alg], beta, 43, stream=2, sweep0=7, nsweeps=6)
+    assert np.array_equal(sysd.spins, s)
+    assert np.array_equal(Ms, oM)
+    scale = _scale(g) + abs(g.D) * g.n
+    assert np.allclose(Es, oE, rtol=0, atol=E_RTOL * scale)
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    assert abs(gpu.energy(sysd, full=True) - O.bcg_observables(g, s)[0]) <= E_RTOL * scale
+
+
+def test_blume_capel_graph_known_answers(gpu):
+    # SpinSystems/test/test_blume_capel.jl:8-31 on graphs; constructors blume_capel.jl:467-511
+    import scipy.sparse as sp
+    from mcx import graph as G
+    d = gpu.BlumeCapel([5, 5], D=0.5)  # odd sides: a BlumeCapelGraph on the torus
+    assert d.kind == "BlumeCapelGraph"
+    n, es = grid_edges([5, 5], True)
+    assert gpu.energy(d) == -len(es) + 0.5 * n and gpu.magnetization(d) == n
+    g = O.BCGraph(*from_edges(n, es)[:2], J=1.0, D=0.5)
+    s = np.ones(n, np.int8)
+    assert G.delta_energy(d, 0, 0) == O.bcg_delta_energy(g, s, 0, 0)
+    G.modify_(d, 0, 0)
+    s[0] = 0
+    assert gpu.energy(d) == O.bcg_observables(g, s)[0] == gpu.energy(d, full=True)
+    assert gpu.magnetization(d) == n - 1
+    gpu.init_(d, "zero")
+    assert gpu.energy(d) == 0.0 and gpu.magnetization(d) == 0
+    grid = G.grid([3, 4], periodic=False)
+    assert gpu.BlumeCapel(grid, 1.0, 0.5).kind == "BlumeCapelGraph"
+    Jvec = np.arange(1.0, G.ne(grid) + 1)
+    assert gpu.BlumeCapel(grid, Jvec, 0.5).kind == "BlumeCapelMatrix"
+    assert gpu.BlumeCapel(sp.csr_matrix(G.matrix_from_edges(grid, Jvec)), 0.5).kind == "BlumeCapelMatrix"
+    assert gpu.BlumeCapel([6, 6], periodic=False, D=1.0).kind == "BlumeCapelGraph"
+    with pytest.raises(gpu.ArgumentError):
+        G.delta_energy(d, 0)  # a Blume-Capel site needs the new state
+    with pytest.raises(gpu.ArgumentError):
+        d.spins = np.full(n, 2, np.int8)

@@ -157,3 +157,42 @@ def test_grid_graph_restatement(mcxlib):
     assert (A != A.T).nnz == 0 and A.nnz == 2 * G.ne(g)
     with pytest.raises(mcxlib.ArgumentError):
         G.matrix_from_edges(g, Jvec[:-1])
+
+
+def test_blume_capel_graph_known_answers():
+    # SpinSystems/test/test_blume_capel.jl:8-31 on the 4x4 torus as a graph
+    n, es = grid_edges([4, 4], True)
+    rp, col, _ = from_edges(n, es)
+    g = O.BCGraph(rp, col, J=1.0, D=0.5)
+    s = np.ones(16, np.int8)
+    assert O.bcg_observables(g, s) == (-24.0, 16)
+    assert O.bcg_delta_energy(g, s, 0, 0) == 3.5
+    s[0] = 0
+    assert O.bcg_observables(g, s) == (-24.0 + 3.5, 15)
+    assert O.bcg_observables(g, np.zeros(16, np.int8)) == (0.0, 0)
+
+
+@pytest.mark.parametrize("alg", [O.METROPOLIS, O.GLAUBER, O.HEATBATH])
+def test_blume_capel_graph_cached_equals_full(alg):
+    es = random_edges(300, 700, 21)
+    rp, col, val = from_edges(300, es, np.random.default_rng(22).normal(size=len(es)))
+    for g in (O.BCGraph(rp, col, Jv=val, D=0.3, hv=np.random.default_rng(23).normal(size=300) * 0.2),
+              O.BCGraph(rp, col, J=1.0, D=0.7, h=0.1)):
+        s = O.bcg_init_random(g.n, 4)
+        assert set(np.unique(s)) <= {-1, 0, 1} and len(np.unique(s)) == 3
+        Es, Ms, att, acc = O.bcg_sweep(g, s, alg, 0.8, 4, nsweeps=5)
+        E, M = O.bcg_observables(g, s)
+        assert abs(Es[-1] - E) < 1e-9 and Ms[-1] == M and 0 < acc < att
+
+
+def test_blume_capel_graph_heat_bath_distribution():
+    """The three-state heat bath on a graph with no edges samples each site from
+    exp(-beta (D s^2 - h s)) / Z (blume_capel.jl:59-85)."""
+    n = 4000
+    g = O.BCGraph(np.zeros(n + 1, np.int64), np.zeros(0, np.int32), J=1.0, D=0.4, h=0.3)
+    s = O.bcg_init_random(n, 8)
+    O.bcg_sweep(g, s, O.HEATBATH, 1.0, 8, nsweeps=3)
+    w = np.array([math.exp(-1.0 * (0.4 * v * v - 0.3 * v)) for v in (-1, 0, 1)])
+    p = w / w.sum()
+    counts = np.array([(s == v).sum() for v in (-1, 0, 1)])
+    assert np.all(np.abs(counts / n - p) < 4 * np.sqrt(p * (1 - p) / n)), (counts / n, p)
