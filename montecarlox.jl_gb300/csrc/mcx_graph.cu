@@ -46,7 +46,7 @@ struct GraphDev {
     const double* h;                // per position (vector field), or nullptr
     const float2* h2;               // the same split hi + lo, or nullptr
     double J, hu;                   // uniform coupling, uniform field
-    float2 J2u, h2u;                // the same split hi + lo
+    float2 J2u, h2u, D2u;           // the same split hi + lo (and the crystal field)
     const unsigned long long* tab;  // thresholds by (s > 0, lpi + dmax)
     const float2* tabdE;            // ΔE (hi + lo) by (s > 0, lpi + dmax)
     int dmax;
@@ -492,6 +492,178 @@ __device__ __forceinline__ void bc_row(const GraphDev& g, const int8_t* sp, long
     }
 }
 
+// Float-float form of the coupling sum for the FP32 test: (ch, cl) = Σ J_ij s_j (or
+// J Σ s_j) and S = Σ |J_ij| over the neighbours that are not 0 (|c| <= S).
+struct BcRowFF {
+    int isum;
+    float ch, cl, S;
+};
+
+template <bool EDGEJ>
+__device__ __forceinline__ void bc_row_ff(const GraphDev& g, const int8_t* sp, long long off, int w, int lane,
+                                          BcRowFF& r) {
+    r.isum = 0;
+    r.ch = r.cl = r.S = 0.0f;
+    for (int k = 0; k < w; k += 4) {
+        int nb[4];
+        float2 Jk[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long e = off + 32ll * (k + j) + lane;
+            nb[j] = k + j < w ? __ldg(g.nbr + e) : -1;
+            if (EDGEJ) Jk[j] = k + j < w ? __ldg(g.J2 + e) : make_float2(0.0f, 0.0f);
+        }
+        int sj[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sj[j] = nb[j] >= 0 ? (int)sp[nb[j]] : 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            r.isum += sj[j];
+            if (EDGEJ && sj[j] != 0) {
+                const float xh = sj[j] > 0 ? Jk[j].x : -Jk[j].x, xl = sj[j] > 0 ? Jk[j].y : -Jk[j].y;
+                const float t = r.ch + xh;
+                const float bb = t - r.ch;
+                r.cl += ((r.ch - (t - bb)) + (xh - bb)) + xl;
+                r.ch = t;
+                r.S += fabsf(Jk[j].x);
+            }
+        }
+    }
+    if (!EDGEJ) {
+        const float lf = (float)r.isum;
+        r.ch = lf * g.J2u.x;
+        r.cl = __fmaf_rn(lf, g.J2u.x, -r.ch) + lf * g.J2u.y;
+        r.S = fabsf(r.ch);
+    }
+}
+
+// "u < p" from an FP32 estimate pe of p with every p compatible with the bounds in
+// pe (1 -+ m): 1 sure, 0 surely not, -1 undecided (as certain_below).
+__device__ __forceinline__ int certain_u(float pe, float m, uint32_t w0) {
+    const float A = pe * (1.0f - 2.0f * m) * 4294967296.0f;
+    const uint32_t a = A >= 4294967040.0f ? 4294967040u : (uint32_t)A;
+    if (w0 < a) return 1;
+    const float B = pe * (1.0f + 2.0f * m) * 4294967296.0f;
+    if (B >= 4294967040.0f) return -1;
+    const uint32_t b = max((uint32_t)ceilf(B), 1u);
+    return w0 >= b ? 0 : -1;
+}
+
+// (dh, dl) = -ds c - ds h + ds2 D in float-float (|ds| <= 2, ds2 in {-1, 0, 1}: the
+// products are exact)
+template <int FIELD>
+__device__ __forceinline__ void bc_delta_ff(const BcRowFF& r, float2 hv, float2 Dv, int ds, int ds2, float& dh,
+                                            float& dl) {
+    const float m = (float)(-ds);
+    dh = m * r.ch;
+    dl = m * r.cl;
+    if (FIELD != F_NONE) ff_add(dh, dl, m * hv.x, m * hv.y);
+    if (ds2 != 0) ff_add(dh, dl, (float)ds2 * Dv.x, (float)ds2 * Dv.y);
+}
+
+// The reference's FP64 rule for one Blume-Capel site (taken when the FP32 test cannot decide).
+template <int ALG, bool EDGEJ, int FIELD>
+__device__ __noinline__ int bc_exact_site(const GraphDev& g, const int8_t* sp, long long p, long long off, int w,
+                                          int lane, int so, int isum, unsigned long long ku, uint32_t lo,
+                                          double* dE_out) {
+    double c = g.J * (double)isum;
+    if (EDGEJ) {
+        c = 0.0;
+        for (int k = 0; k < w; ++k) {
+            const long long e = off + 32ll * k + lane;
+            const int nb = g.nbr[e];
+            if (nb >= 0) c += g.J64[e] * (double)sp[nb];
+        }
+    }
+    const double hf = FIELD == F_VECTOR ? g.h[p] : (FIELD == F_UNIFORM ? g.hu : 0.0);
+    const double u = (double)ku * 0x1p-53;
+    int sn;
+    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :59-85
+        const double e1 = (c - hf * (-1.0)) + g.D;
+        const double e3 = (-c - hf) + g.D;
+        const double w1 = mcx_exp(-g.beta * e1), w2 = mcx_exp(-g.beta * 0.0), w3 = mcx_exp(-g.beta * e3);
+        const double z = (w1 + w2) + w3;
+        const double r = u * z;
+        sn = r < w1 ? -1 : (r < w1 + w2 ? 0 : 1);
+    } else {
+        const int prop = bc_propose_state(so, (int)(lo & 1u));
+        const double lr = -g.beta * bc_delta(c, so, prop, hf, FIELD != F_NONE, g.D);
+        const bool acc = ALG == MCX_METROPOLIS ? ((lr > 0) || (u < mcx_exp(lr))) : (u < mcx_logistic(lr));
+        sn = acc ? prop : so;
+    }
+    *dE_out = sn != so ? bc_delta(c, so, sn, hf, FIELD != F_NONE, g.D) : 0.0;
+    return sn;
+}
+
+// One Blume-Capel site on the FP32 path: ΔE and the Boltzmann weights from the
+// float-float coupling sum with proven error bounds (as for the Ising graphs), the
+// decision certified against the FP64 rule, the exact evaluation when it cannot be.
+template <int ALG, bool EDGEJ, int FIELD>
+__device__ __forceinline__ int bc_decide_fast(const GraphDev& g, const int8_t* sp, long long p, long long off, int w,
+                                              int lane, int so, const BcRowFF& r, uint32_t hi, uint32_t lo, float& eh,
+                                              float& el) {
+    const float2 hv = FIELD == F_VECTOR ? g.h2[p] : (FIELD == F_UNIFORM ? g.h2u : make_float2(0.0f, 0.0f));
+    const float hm = fabsf(hv.x), Dm = fabsf(g.D2u.x);
+    const float wf = (float)(w + 1);
+    const float errc = wf * wf * r.S * 0x1p-45f;  // float-float coupling sum vs exact, doubled
+    int sn = -2;
+    if (ALG == MCX_HEATBATH) {
+        float e1h = r.ch, e1l = r.cl, e3h = -r.ch, e3l = -r.cl;
+        if (FIELD != F_NONE) {
+            ff_add(e1h, e1l, hv.x, hv.y);
+            ff_add(e3h, e3l, -hv.x, -hv.y);
+        }
+        ff_add(e1h, e1l, g.D2u.x, g.D2u.y);
+        ff_add(e3h, e3l, g.D2u.x, g.D2u.y);
+        const float e1 = e1h + e1l, e3 = e3h + e3l;
+        const float x1 = -g.beta32 * e1, x3 = -g.beta32 * e3;
+        const float b = fabsf(g.beta32) * 1.01f;
+        const float ex1 = b * ((2.0f * r.S + 2.0f * hm + Dm + fabsf(e1)) * 0x1p-20f + errc) + fabsf(x1) * 0x1p-21f;
+        const float ex3 = b * ((2.0f * r.S + 2.0f * hm + Dm + fabsf(e3)) * 0x1p-20f + errc) + fabsf(x3) * 0x1p-21f;
+        const float m = 1.01f * (ex1 + ex3) + (fabsf(x1) + fabsf(x3)) * 0x1p-21f + 0x1p-19f;
+        if (m < 0x1p-8f) {
+            const float M = fmaxf(x1, fmaxf(0.0f, x3));
+            const float q1 = __expf(x1 - M), q2 = __expf(-M), q3 = __expf(x3 - M);
+            const float z = (q1 + q2) + q3;
+            const int c1 = certain_u(q1 / z, m, hi);
+            if (c1 == 1) {
+                sn = -1;
+            } else if (c1 == 0) {
+                const int c2 = certain_u((q1 + q2) / z, m, hi);
+                sn = c2 == 1 ? 0 : (c2 == 0 ? 1 : -2);
+            }
+        }
+    } else {
+        const int prop = bc_propose_state(so, (int)(lo & 1u));
+        const int ds = prop - so, ds2 = prop * prop - so * so;
+        float dh, dl;
+        bc_delta_ff<FIELD>(r, hv, g.D2u, ds, ds2, dh, dl);
+        const float df = dh + dl;
+        const float ad = fabsf((float)ds);
+        const float errd = (ad * (2.0f * r.S + hm) + Dm + fabsf(df)) * 0x1p-20f + ad * errc;
+        const float xf = -g.beta32 * df;
+        const float errx = fabsf(g.beta32) * errd * 1.01f + fabsf(xf) * 0x1p-21f + 0x1p-126f;
+        const int c = certain_below<ALG != MCX_METROPOLIS>(xf, errx, hi);
+        if (c >= 0) sn = c == 1 ? prop : so;
+    }
+    if (sn != -2) {
+        if (sn != so) {
+            float dh, dl;
+            bc_delta_ff<FIELD>(r, hv, g.D2u, sn - so, sn * sn - so * so, dh, dl);
+            ff_add(eh, el, dh, dl);
+        }
+        return sn;
+    }
+    const unsigned long long ku = ((unsigned long long)hi << 21) | (unsigned long long)(lo >> 11);
+    double dE;
+    sn = bc_exact_site<ALG, EDGEJ, FIELD>(g, sp, p, off, w, lane, so, r.isum, ku, lo, &dE);
+    if (sn != so) {
+        const float h = __double2float_rn(dE);
+        ff_add(eh, el, h, __double2float_rn(dE - (double)h));
+    }
+    return sn;
+}
+
 // One Blume-Capel site: returns the new state (the old one when nothing changes) and adds
 // the ΔE of a change to (eh, el).
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
@@ -560,32 +732,40 @@ __device__ __forceinline__ void bc_class_pairs(const GraphDev& g, int8_t* sp, co
         const int wB = hasB ? (int)((g.soff[sA + 2] - offB) >> 5) : 0;
         const int soA = sp[pA];
         const int soB = hasB ? (int)sp[pB] : 0;
-        int iA, iB;
-        double cA, cB;
-        bc_row<EDGEJ>(g, sp, offA, wA, lane, iA, cA);
-        bc_row<EDGEJ>(g, sp, offB, wB, lane, iB, cB);
-        const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
-        if (lA < c.count) {
-            const int sn = bc_decide<ALG, TABLE, EDGEJ, FIELD>(g, pA, soA, iA, cA, r.x, r.y, eh, el);
-            if (sn != soA) {
-                sp[pA] = (int8_t)sn;
-                dM += sn - soA;
-                ++nacc;
-            }
+        int snA = soA, snB = soB;
+        if (TABLE) {
+            int iA, iB;
+            double cA, cB;
+            bc_row<false>(g, sp, offA, wA, lane, iA, cA);
+            bc_row<false>(g, sp, offB, wB, lane, iB, cB);
+            const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
+            if (lA < c.count) snA = bc_decide<ALG, true, false, FIELD>(g, pA, soA, iA, cA, r.x, r.y, eh, el);
+            if (lB < c.count) snB = bc_decide<ALG, true, false, FIELD>(g, pB, soB, iB, cB, r.z, r.w, eh, el);
+        } else {
+            BcRowFF rA, rB;
+            bc_row_ff<EDGEJ>(g, sp, offA, wA, lane, rA);
+            bc_row_ff<EDGEJ>(g, sp, offB, wB, lane, rB);
+            const uint4 r = philox10(make_uint4((uint32_t)(c.blk0 + 32 * j + lane), (uint32_t)sweep, w2, stream), k0, k1);
+            if (lA < c.count)
+                snA = bc_decide_fast<ALG, EDGEJ, FIELD>(g, sp, pA, offA, wA, lane, soA, rA, r.x, r.y, eh, el);
+            if (lB < c.count)
+                snB = bc_decide_fast<ALG, EDGEJ, FIELD>(g, sp, pB, offB, wB, lane, soB, rB, r.z, r.w, eh, el);
         }
-        if (lB < c.count) {
-            const int sn = bc_decide<ALG, TABLE, EDGEJ, FIELD>(g, pB, soB, iB, cB, r.z, r.w, eh, el);
-            if (sn != soB) {
-                sp[pB] = (int8_t)sn;
-                dM += sn - soB;
-                ++nacc;
-            }
+        if (snA != soA) {
+            sp[pA] = (int8_t)snA;
+            dM += snA - soA;
+            ++nacc;
+        }
+        if (snB != soB) {
+            sp[pB] = (int8_t)snB;
+            dM += snB - soB;
+            ++nacc;
         }
     }
 }
 
 template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
-__global__ void __launch_bounds__(kGraphBlock) k_bcg_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
+__global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_bcg_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
                                                            uint32_t stream, unsigned long long sweep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float eh = 0.0f, el = 0.0f;
@@ -994,6 +1174,7 @@ struct mcx_graph {
         g.h2 = d_h2;
         g.J2u = split2(J);
         g.h2u = split2(h);
+        g.D2u = split2(D);
         g.beta32 = (float)beta;
         g.D = D;
         g.soff = d_soff;
