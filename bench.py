@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
-    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph"], default=None,
+    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph", "graph_table"], default=None,
                     help="run one short workload for a profiler capture and exit (no JSON line)")
     return ap.parse_args()
 
@@ -577,12 +577,13 @@ def run_profile_target(args):
         alg = F.Multicanonical(mcx.Philox(SEED), ens)
         F.sweep_walkers_(walkers, alg, 1)
         F.sweep_walkers_(walkers, alg, 2)
-    elif args.profile == "graph":
+    elif args.profile in ("graph", "graph_table"):
         from mcx.graph import IsingGraphDevice
-        rowptr, col, J = torus_csr(2048, SEED, True)  # 4.2M sites, 0.25 GB of neighbour data
+        # 4.2M sites; Gaussian couplings (0.25 GB of neighbour data) or one J (the table form)
+        rowptr, col, J = torus_csr(2048, SEED, args.profile == "graph")
         sysd = IsingGraphDevice(rowptr, col, J, ctx=ctx)
         mcx.init_(sysd, "random", rng=mcx.Philox(SEED))
-        alg = mcx.Metropolis(mcx.Philox(SEED), beta=1.0)
+        alg = mcx.Metropolis(mcx.Philox(SEED), beta=1.0 if args.profile == "graph" else BETA)
         mcx.sweep_(sysd, alg, 2)
         mcx.sweep_(sysd, alg, 2)
     torch.cuda.synchronize()

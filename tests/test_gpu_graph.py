@@ -280,3 +280,33 @@ def test_blume_capel_graph_known_answers(gpu):
         G.delta_energy(d, 0)  # a Blume-Capel site needs the new state
     with pytest.raises(gpu.ArgumentError):
         d.spins = np.full(n, 2, np.int8)
+
+
+@pytest.mark.parametrize("bc", [False, True])
+def test_graph_edge_cases(gpu, bc):
+    """One site, no edges, J = 0, beta = 0: the paths still agree with the oracle."""
+    from mcx.graph import IsingGraphDevice, BlumeCapelGraphDevice
+    cases = [(np.array([0, 0], np.int64), np.zeros(0, np.int32), None, 1.0, 0.0),     # one site
+             (np.zeros(101, np.int64), np.zeros(0, np.int32), None, 1.0, 0.3),       # 100 isolated sites, field
+             (*from_edges(50, random_edges(50, 80, 51))[:2], None, 0.0, 0.0),        # J = 0
+             (*from_edges(60, random_edges(60, 90, 52), np.zeros(90)), 1.0, 0.2)]    # per-entry zeros
+    for rp, col, jv, J, h in cases:
+        n = len(rp) - 1
+        for alg, beta in (("metropolis", 0.0), ("heatbath", 0.7), ("glauber", 1.3)):
+            if bc:
+                g = O.BCGraph(rp, col, Jv=jv, J=J, D=0.4, h=h)
+                d = BlumeCapelGraphDevice(rp, col, jv, J=J, D=0.4, h=h)
+                s = O.bcg_init_random(n, 9)
+                gpu.init_(d, "random", rng=gpu.Philox(9))
+            else:
+                g = O.Graph(rp, col, Jv=jv, J=J, h=h)
+                d = IsingGraphDevice(rp, col, jv, J=J, h=h)
+                s = O.graph_init_random(n, 9)
+                gpu.init_(d, "random", rng=gpu.Philox(9))
+            a = _alg(gpu, alg, 3, beta)
+            Es, Ms = gpu.sweep_(d, a, 4, record=True)
+            sweep = O.bcg_sweep if bc else O.graph_sweep
+            oE, oM, att, acc = sweep(g, s, ALG[alg], beta, 3, nsweeps=4)
+            assert np.array_equal(d.spins, s) and np.array_equal(Ms, oM), (n, alg, beta)
+            assert np.allclose(Es, oE, rtol=0, atol=1e-9)
+            d.close()
