@@ -51,7 +51,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
-    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph", "graph_table"], default=None,
+    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph", "graph_table", "lattice_small"],
+                    default=None,
                     help="run one short workload for a profiler capture and exit (no JSON line)")
     return ap.parse_args()
 
@@ -314,6 +315,44 @@ def bench_serve(mcx, ctx, njobs=40):
     return r
 
 
+def bench_small(torch, mcx, ctx, with_cpu, cpu_seconds):
+    """The reference's own CPU-run configuration: 2-D Ising L=64, Metropolis at beta 0.4407,
+    seed 42, 10^3 thermalisation sweeps then 10^4 sweeps with E and M recorded every sweep,
+    each one library call (the second is timed with CUDA events on the context's stream,
+    the per-sweep series copied back to the host inside the timed region)."""
+    import numpy as np
+    L = 64
+    N = L * L
+    lat = mcx.Ising([L, L], ctx=ctx)
+    mcx.init_(lat, "random", rng=mcx.Philox(42))
+    alg = mcx.Metropolis(mcx.Philox(42), beta=BETA)
+    mcx.sweep_(lat, alg, 1000)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    obs = mcx.sweep_(lat, alg, 10000, record=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    lat.close()
+    res = {"workload": "ising2d_L64_metropolis_1e3_therm_1e4_sweeps_record", "attempts_per_ns": N * 1e4 / (ms * 1e6),
+           "us_per_sweep": ms * 1e3 / 1e4, "kernel": "k_lattice_small<0,2,4,false,true>", "launches_per_call": 2,
+           "series_rows": int(obs.shape[0])}
+    if with_cpu:
+        import oracle as O
+        s = O.init_random(O.ISING, [L, L], 42)
+        done, t, t0 = 0, 0.0, time.perf_counter()
+        while t < cpu_seconds:
+            O.seq_attempts(s, O.ISING, [L, L], O.METROPOLIS, BETA, 42, attempt0=done, nattempts=N * 100)
+            done += N * 100
+            t = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": done / t / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "one chain of the sequential random-site order (spin_flip! with FP64 exp), "
+                                         "L=64, %d attempts, %.1f s" % (done, t)}
+    return res
+
+
 def torus_csr(L, seed, per_entry):
     """CSR of the L x L periodic grid (first coordinate fastest, sorted rows) and, when
     per_entry, symmetric Gaussian couplings: the 2-D Edwards-Anderson spin glass."""
@@ -503,8 +542,9 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = graph_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = None
     if not args.no_extras:
+        small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
@@ -542,6 +582,7 @@ def run_mcx(args):
         "flat_histogram": fh_res,
         "msc64": msc_res,
         "general_graphs": graph_res,
+        "small_lattice": small_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -577,6 +618,12 @@ def run_profile_target(args):
         alg = F.Multicanonical(mcx.Philox(SEED), ens)
         F.sweep_walkers_(walkers, alg, 1)
         F.sweep_walkers_(walkers, alg, 2)
+    elif args.profile == "lattice_small":
+        lat = mcx.Ising([64, 64], ctx=ctx)
+        mcx.init_(lat, "random", rng=mcx.Philox(42))
+        alg = mcx.Metropolis(mcx.Philox(42), beta=BETA)
+        mcx.sweep_(lat, alg, 1000)
+        mcx.sweep_(lat, alg, 10000, record=True)
     elif args.profile in ("graph", "graph_table"):
         from mcx.graph import IsingGraphDevice
         # 4.2M sites; Gaussian couplings (0.25 GB of neighbour data) or one J (the table form)
