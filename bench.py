@@ -315,11 +315,16 @@ def bench_serve(mcx, ctx, njobs=40):
     return r
 
 
+def ctx_sms(torch):
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def bench_small(torch, mcx, ctx, with_cpu, cpu_seconds):
     """The reference's own CPU-run configuration: 2-D Ising L=64, Metropolis at beta 0.4407,
     seed 42, 10^3 thermalisation sweeps then 10^4 sweeps with E and M recorded every sweep,
     each one library call (the second is timed with CUDA events on the context's stream,
-    the per-sweep series copied back to the host inside the timed region)."""
+    the per-sweep series copied back to the host inside the timed region); then one such
+    chain per SM as independent chains in one batched call (mcx_sweep_batch)."""
     import numpy as np
     L = 64
     N = L * L
@@ -336,7 +341,25 @@ def bench_small(torch, mcx, ctx, with_cpu, cpu_seconds):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     lat.close()
+    # the same chain replicated as independent chains (ParallelChains), one per SM, one call
+    nch = ctx_sms(torch)
+    chains = [mcx.Ising([L, L], ctx=ctx) for _ in range(nch)]
+    for i, c in enumerate(chains):
+        mcx.init_(c, "random", rng=mcx.Philox(42, i))
+    calgs = [mcx.Metropolis(mcx.Philox(42, i), beta=BETA) for i in range(nch)]
+    mcx.sweep_batch_(chains, calgs, 1000)
+    torch.cuda.synchronize()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    mcx.sweep_batch_(chains, calgs, 10000, record=True)
+    e3.record()
+    torch.cuda.synchronize()
+    bms = e2.elapsed_time(e3)
+    for c in chains:
+        c.close()
     res = {"workload": "ising2d_L64_metropolis_1e3_therm_1e4_sweeps_record", "attempts_per_ns": N * 1e4 / (ms * 1e6),
+           "batched_chains": nch, "batched_attempts_per_ns": nch * N * 1e4 / (bms * 1e6),
            "us_per_sweep": ms * 1e3 / 1e4, "kernel": "k_lattice_small<0,2,4,false,true>", "launches_per_call": 2,
            "series_rows": int(obs.shape[0])}
     if with_cpu:

@@ -163,6 +163,17 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
  * NULL. */
 MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, double beta,
                                 int32_t* chosen, double* ns_per_site);
+/* The sweeps of many independent lattices in one call (the chains of a ParallelChains
+ * with a threads backend, src/infrastructure/parallel_chains.jl:99-105): lattice i runs
+ * `nsweeps` sweeps at betas[i] on its own stream rngs[i] (advanced), with the results of
+ * mcx_sweep(lats[i], alg, betas[i], &rngs[i], ...) bit for bit.  All lattices on one
+ * context, one model and dimension.  int8 lattices of at most 16384 sites run in one
+ * launch, one block per lattice; any other batch runs as one mcx_sweep per lattice.
+ *   obs_series: n host pointers to int64[nsweeps*3] (or NULL entries), or NULL.
+ *   counters:   n accumulated counters, or NULL. */
+MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx_algorithm alg,
+                                   const double* betas, mcx_rng* rngs, int64_t nsweeps,
+                                   int64_t** obs_series, mcx_counters* counters);
 /* Copy the per-sweep series of the last mcx_sweep call (first n sweeps). */
 MCX_API mcx_status mcx_read_series(mcx_lattice* lat, int64_t* obs_series, int64_t n);
 

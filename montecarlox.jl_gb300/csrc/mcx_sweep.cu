@@ -274,36 +274,42 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
 // dependent chain per thread: latency, not issue, bounds a half-sweep this small).
 // KIND: 0 Ising words, 1 Ising per site, 2 Blume-Capel words, 3 Blume-Capel per site.
 template <int KIND, int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(512, 1) k_lattice_small(SweepArgs a, int8_t* g0, int8_t* g1, long long half,
-                                                           long long nsweeps, long long* series) {
+__device__ __forceinline__ void lattice_small_run(const SweepArgs& a0, int8_t* g0, int8_t* g1, long long half,
+                                                  long long nsweeps, long long* series) {
     extern __shared__ __align__(16) int8_t s_lat[];
     __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
     __shared__ uint32_t s_t32[kMaxTable];
     const long long off1 = (half + 15) & ~15ll;
     int8_t* s0 = s_lat;
     int8_t* s1 = s_lat + off1;
-    {
-        const uint4* src0 = reinterpret_cast<const uint4*>(g0);
-        const uint4* src1 = reinterpret_cast<const uint4*>(g1);
-        if (half % 16 == 0) {
-            for (long long i = threadIdx.x; i < half / 16; i += blockDim.x) {
-                reinterpret_cast<uint4*>(s0)[i] = src0[i];
-                reinterpret_cast<uint4*>(s1)[i] = src1[i];
-            }
-        } else {
-            for (long long i = threadIdx.x; i < half; i += blockDim.x) {
-                s0[i] = g0[i];
-                s1[i] = g1[i];
-            }
+    if (half % 16 == 0) {
+        for (long long i = threadIdx.x; i < half / 16; i += blockDim.x) {
+            reinterpret_cast<uint4*>(s0)[i] = reinterpret_cast<const uint4*>(g0)[i];
+            reinterpret_cast<uint4*>(s1)[i] = reinterpret_cast<const uint4*>(g1)[i];
+        }
+    } else {
+        for (long long i = threadIdx.x; i < half; i += blockDim.x) {
+            s0[i] = g0[i];
+            s1[i] = g1[i];
         }
     }
     if constexpr (KIND == 0) {
-        ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
+        ising_tables<DIM, HB, T32>(a0, s_thr, s_t32);
     } else {
-        for (int t = threadIdx.x; t < kMaxTable; t += blockDim.x) s_thr[t] = a.thr[t];
+        for (int t = threadIdx.x; t < kMaxTable; t += blockDim.x) s_thr[t] = a0.thr[t];
     }
     __syncthreads();
-    const unsigned long long sweep0 = a.sweep;
+    SweepArgs a;  // the fields the bodies read (the table is in shared memory)
+    a.W = a0.W;
+    a.Ly = a0.Ly;
+    a.Lz = a0.Lz;
+    a.rows = a0.rows;
+    a.k0 = a0.k0;
+    a.k1 = a0.k1;
+    a.stream = a0.stream;
+    a.sweep_base = nullptr;
+    a.acc = a0.acc;
+    const unsigned long long sweep0 = a0.sweep;
     for (long long t = 0; t < nsweeps; ++t) {
         long long v[4] = {0, 0, 0, 0};
         for (int c = 0; c < 2; ++c) {
@@ -332,6 +338,47 @@ __global__ void __launch_bounds__(512, 1) k_lattice_small(SweepArgs a, int8_t* g
             g1[i] = s1[i];
         }
     }
+}
+
+template <int KIND, int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(512, 1) k_lattice_small(SweepArgs a, int8_t* g0, int8_t* g1, long long half,
+                                                          long long nsweeps, long long* series) {
+    lattice_small_run<KIND, DIM, V, HB, T32>(a, g0, g1, half, nsweeps, series);
+}
+
+// Many independent small lattices (the chains of a ParallelChains with a threads backend,
+// src/infrastructure/parallel_chains.jl:99-105) in one launch: block b runs every sweep of
+// lattice b as k_lattice_small does, after zeroing that lattice's series slots and counter.
+struct SmallBatchDesc {
+    SweepArgs a;  // the lattice's geometry, key, table (its beta) and counter
+    int8_t* col0;
+    int8_t* col1;
+    long long half;
+    long long* series;
+    long long* state;
+};
+
+template <int KIND, int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(512, 1) k_lattice_small_batch(const SmallBatchDesc* __restrict__ descs,
+                                                                long long nsweeps) {
+    const SmallBatchDesc& d = descs[blockIdx.x];
+    for (long long i = threadIdx.x; i < 3 * nsweeps; i += blockDim.x) d.series[i] = 0;
+    if (threadIdx.x == 0) *d.a.acc = 0ull;
+    __syncthreads();
+    lattice_small_run<KIND, DIM, V, HB, T32>(d.a, d.col0, d.col1, d.half, nsweeps, d.series);
+}
+
+// the prefix sum of k_prefix_series for every lattice of a batch (block b: lattice b)
+__global__ void k_prefix_series_batch(const SmallBatchDesc* __restrict__ descs, long long n) {
+    const SmallBatchDesc& d = descs[blockIdx.x];
+    const int j = threadIdx.x;
+    if (j >= 3) return;
+    long long acc = d.state[j];
+    for (long long s = 0; s < n; ++s) {
+        acc += d.series[3 * s + j];
+        d.series[3 * s + j] = acc;
+    }
+    d.state[j] = acc;
 }
 
 // ----------------------------------------------------------- dispatching --
@@ -369,6 +416,16 @@ static SmallLatticeFn pick_small_v(int kind, bool t32) {
     if (kind == 1) return k_lattice_small<1, DIM, 1, HB, false>;
     if (kind == 2) return k_lattice_small<2, DIM, 4, HB, false>;
     return k_lattice_small<3, DIM, 1, HB, false>;
+}
+
+using SmallBatchFn = void (*)(const SmallBatchDesc*, long long);
+
+template <int DIM, bool HB>
+static SmallBatchFn pick_batch_v(int kind, bool t32) {
+    if (kind == 0) return t32 ? k_lattice_small_batch<0, DIM, 4, HB, true> : k_lattice_small_batch<0, DIM, 4, HB, false>;
+    if (kind == 1) return k_lattice_small_batch<1, DIM, 1, HB, false>;
+    if (kind == 2) return k_lattice_small_batch<2, DIM, 4, HB, false>;
+    return k_lattice_small_batch<3, DIM, 1, HB, false>;
 }
 
 static SmallLatticeFn pick_small(int dim, mcx_model model, mcx_algorithm alg, int64_t W, const Table& t) {
@@ -678,5 +735,88 @@ extern "C" MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, 
     lat->tuned_V = best;
     if (chosen) *chosen = best;
     if (ns_per_site) *ns_per_site = (double)best_ms * 1e6 / (8.0 * (double)half);
+    return MCX_OK;
+}
+
+extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx_algorithm alg, const double* betas,
+                                              mcx_rng* rngs, int64_t nsweeps, int64_t** obs_series,
+                                              mcx_counters* counters) {
+    if (!lats || !betas || !rngs || n < 1) return fail(MCX_ERR_INVALID_ARG, "NULL argument or no lattice");
+    if (nsweeps < 0) return fail(MCX_ERR_INVALID_ARG, "nsweeps < 0");
+    if (alg != MCX_METROPOLIS && alg != MCX_GLAUBER && alg != MCX_HEATBATH)
+        return fail(MCX_ERR_INVALID_ARG, "unknown algorithm %d", (int)alg);
+    mcx_ctx* ctx = lats[0] ? lats[0]->ctx : nullptr;
+    bool small = true, words = true, fits32 = true;
+    std::vector<Table> tabs(n);
+    for (int i = 0; i < n; ++i) {
+        const mcx_lattice* L = lats[i];
+        if (!L) return fail(MCX_ERR_INVALID_ARG, "lattice %d is NULL", i);
+        if (L->ctx != ctx) return fail(MCX_ERR_INVALID_ARG, "lattice %d is on another context", i);
+        if (L->model != lats[0]->model || L->dim != lats[0]->dim)
+            return fail(MCX_ERR_INVALID_ARG, "lattice %d: a batch holds one model and dimension", i);
+        if (!std::isfinite(betas[i])) return fail(MCX_ERR_INVALID_ARG, "beta %d must be finite", i);
+        if (rngs[i].counter + (uint64_t)nsweeps >= (1ull << 48))
+            return fail(MCX_ERR_INVALID_ARG, "sweep counter beyond 2^48");
+        MCX_CHECK(build_table(L, alg, betas[i], &tabs[i]));
+        small = small && L->layout == MCX_LAYOUT_INT8 && L->N <= kSmallLattice;
+        words = words && L->W % 4 == 0;
+        fits32 = fits32 && ising_table_fits32(tabs[i].thr, tabs[i].n, 2 * L->dim, alg == MCX_HEATBATH);
+    }
+    if (nsweeps == 0) return MCX_OK;
+    if (!small) {  // one call per lattice (identical results)
+        for (int i = 0; i < n; ++i)
+            MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
+                                counters ? &counters[i] : nullptr));
+        return MCX_OK;
+    }
+    std::vector<SmallBatchDesc> descs(n);
+    long long maxhalf = 0;
+    for (int i = 0; i < n; ++i) {
+        mcx_lattice* L = lats[i];
+        MCX_CHECK(ensure_series(L, nsweeps));
+        SmallBatchDesc& d = descs[i];
+        fill_sweep_args(&d.a, L, tabs[i], &rngs[i]);
+        d.a.acc = L->d_acc;
+        d.a.sweep = rngs[i].counter;
+        d.col0 = L->d_col[0];
+        d.col1 = L->d_col[1];
+        d.half = L->N / 2;
+        d.series = reinterpret_cast<long long*>(L->d_series);
+        d.state = reinterpret_cast<long long*>(L->d_state);
+        maxhalf = std::max(maxhalf, d.half);
+    }
+    void* scratch = nullptr;
+    MCX_CHECK(ctx_scratch(ctx, sizeof(SmallBatchDesc) * (size_t)n, &scratch));
+    SmallBatchDesc* d_descs = static_cast<SmallBatchDesc*>(scratch);
+    cudaStream_t st = ctx->stream;
+    MCX_CUDA(cudaMemcpyAsync(d_descs, descs.data(), sizeof(SmallBatchDesc) * (size_t)n, cudaMemcpyHostToDevice, st));
+    const int kind = lats[0]->model == MCX_ISING ? (words ? 0 : 1) : (words ? 2 : 3);
+    const bool hb = alg == MCX_HEATBATH;
+    const bool t32 = kind == 0 && fits32;
+    const SmallBatchFn fn = lats[0]->dim == 2 ? (hb ? pick_batch_v<2, true>(kind, t32) : pick_batch_v<2, false>(kind, t32))
+                                              : (hb ? pick_batch_v<3, true>(kind, t32) : pick_batch_v<3, false>(kind, t32));
+    const size_t smem = (size_t)(((maxhalf + 15) & ~15ll) + maxhalf);
+    if (smem > 48 * 1024)
+        MCX_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fn<<<n, 512, smem, st>>>(d_descs, nsweeps);
+    k_prefix_series_batch<<<n, 32, 0, st>>>(d_descs, nsweeps);
+    count_launch(ctx, 2);
+    MCX_CUDA(cudaGetLastError());
+    std::vector<unsigned long long> acc(counters ? n : 0);
+    for (int i = 0; i < n; ++i) {
+        lats[i]->series_len = nsweeps;
+        rngs[i].counter += (uint64_t)nsweeps;
+        if (obs_series && obs_series[i])
+            MCX_CUDA(cudaMemcpyAsync(obs_series[i], lats[i]->d_series, (size_t)nsweeps * 3 * sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, st));
+        if (counters)
+            MCX_CUDA(cudaMemcpyAsync(&acc[i], lats[i]->d_acc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    }
+    MCX_CUDA(cudaStreamSynchronize(st));  // the descriptors and acc outlive the copies
+    if (counters)
+        for (int i = 0; i < n; ++i) {
+            counters[i].attempts += (uint64_t)lats[i]->N * (uint64_t)nsweeps;
+            counters[i].accepted += acc[i];
+        }
     return MCX_OK;
 }

@@ -487,6 +487,36 @@ def sweep_(sys, alg, nsweeps=1, record=False):
     return obs
 
 
+def sweep_batch_(systems, algs, nsweeps=1, record=False):
+    """``nsweeps`` sweeps of every lattice systems[i] with algs[i] (one algorithm kind,
+    each with its own beta and rng), as one device call: the independent chains of the
+    reference's ParallelChains (src/infrastructure/parallel_chains.jl).  Results are those
+    of sweep_(systems[i], algs[i], nsweeps) bit for bit; returns the per-sweep series of
+    every lattice when ``record``."""
+    n = len(systems)
+    if n != len(algs) or n == 0:
+        raise ArgumentError("one algorithm per system, at least one")
+    kinds = {a.ALG for a in algs}
+    if len(kinds) != 1:
+        raise ArgumentError("a batch runs one algorithm kind")
+    handles = (C.c_void_p * n)(*[s.handle.value if isinstance(s.handle, C.c_void_p) else s.handle for s in systems])
+    betas = np.array([float(a.beta) for a in algs], np.float64)
+    rngs = (L.mcx_rng * n)(*[a.rng._c() for a in algs])
+    cnts = (L.mcx_counters * n)()
+    obs = [np.zeros((nsweeps, 3), np.int64) for _ in range(n)] if record else None
+    ptrs = (C.c_void_p * n)(*[o.ctypes.data for o in obs]) if record else None
+    _check(L.load().mcx_sweep_batch(handles, n, algs[0].ALG, betas.ctypes.data_as(C.POINTER(C.c_double)), rngs,
+                                    int(nsweeps), ptrs, cnts))
+    for i, a in enumerate(algs):
+        a.rng.counter = rngs[i].counter
+        a.steps += cnts[i].attempts
+        if isinstance(a, HeatBath):
+            a.flips += cnts[i].accepted
+        else:
+            a.accepted += cnts[i].accepted
+    return obs
+
+
 def autotune_(sys, alg):
     """Pick the fastest kernel shape for this lattice and algorithm (results unchanged).
     Returns (sites per thread, ns per site per half-sweep)."""

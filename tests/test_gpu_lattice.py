@@ -250,3 +250,44 @@ def test_autotune_keeps_results(gpu, L, alg):
     s = O.init_random(O.ISING, L, 4)
     oobs, _, acc = O.cb_sweep(s, O.ISING, L, ALG[alg], 0.3 if len(L) == 2 else 0.22, 4, nsweeps=3)
     assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s)
+
+
+@pytest.mark.parametrize("model,dims,alg", [
+    (O.ISING, [[64, 64], [32, 48], [8, 8], [128, 128], [6, 10]], "metropolis"),
+    (O.ISING, [[16, 16, 16], [8, 8, 12]], "heatbath"),
+    (O.BC, [[64, 64], [16, 24], [40, 8]], "heatbath"),
+    (O.BC, [[32, 32], [8, 8]], "metropolis"),
+    (O.ISING, [[64, 64], [256, 128]], "glauber"),   # a lattice above the one-block size: one call each
+])
+def test_sweep_batch_matches_each_chain(gpu, model, dims, alg):
+    """Independent chains in one call (ParallelChains): each lattice's series, spins and
+    counters equal its own oracle run."""
+    systems, algs, refs = [], [], []
+    for i, L in enumerate(dims):
+        beta = (0.3 + 0.05 * i) if len(L) == 2 else 0.2 + 0.01 * i
+        D = 0.5 + 0.1 * i if model == O.BC else 0.0
+        sysd = gpu.Ising(L) if model == O.ISING else gpu.BlumeCapel(L, D=D)
+        gpu.init_(sysd, "random", rng=gpu.Philox(10 + i, i))
+        a = _alg(gpu, alg, 20 + i, beta, stream=i)
+        a.rng.counter = 3 * i
+        s = O.init_random(model, L, 10 + i, i)
+        refs.append((s, L, beta, D, a.rng.counter))
+        systems.append(sysd)
+        algs.append(a)
+    obs = gpu.sweep_batch_(systems, algs, 25, record=True)
+    for i, (s, L, beta, D, c0) in enumerate(refs):
+        oobs, att, acc = O.cb_sweep(s, model, L, ALG[alg], beta, 20 + i, stream=i, sweep0=c0, nsweeps=25, D=D)
+        assert np.array_equal(obs[i], oobs), (i, L)
+        assert np.array_equal(systems[i].spins, s)
+        assert algs[i].steps == att and (algs[i].flips if alg == "heatbath" else algs[i].accepted) == acc
+        assert algs[i].rng.counter == c0 + 25
+        assert gpu.observables(systems[i]) == gpu.observables(systems[i], full=True)
+
+
+def test_sweep_batch_argument_errors(gpu):
+    a = gpu.Ising([8, 8])
+    b = gpu.BlumeCapel([8, 8], D=1.0)
+    with pytest.raises(gpu.ArgumentError):
+        gpu.sweep_batch_([a, b], [gpu.Metropolis(gpu.Philox(1), beta=0.3), gpu.Metropolis(gpu.Philox(2), beta=0.3)], 2)
+    with pytest.raises(gpu.ArgumentError):
+        gpu.sweep_batch_([a, a], [gpu.Metropolis(gpu.Philox(1), beta=0.3), gpu.HeatBath(gpu.Philox(2), beta=0.3)], 2)
