@@ -358,8 +358,10 @@ struct SmallBatchDesc {
     long long* state;
 };
 
+// 256 threads and up to two lattices per SM: with more chains than SMs this hides more
+// latency than one 512-thread block per SM (608 chains of 64^2: +28 %)
 template <int KIND, int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(512, 1) k_lattice_small_batch(const SmallBatchDesc* __restrict__ descs,
+__global__ void __launch_bounds__(256, 2) k_lattice_small_batch(const SmallBatchDesc* __restrict__ descs,
                                                                 long long nsweeps) {
     const SmallBatchDesc& d = descs[blockIdx.x];
     for (long long i = threadIdx.x; i < 3 * nsweeps; i += blockDim.x) d.series[i] = 0;
@@ -798,7 +800,7 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
     const size_t smem = (size_t)(((maxhalf + 15) & ~15ll) + maxhalf);
     if (smem > 48 * 1024)
         MCX_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    fn<<<n, 512, smem, st>>>(d_descs, nsweeps);
+    fn<<<n, 256, smem, st>>>(d_descs, nsweeps);
     k_prefix_series_batch<<<n, 32, 0, st>>>(d_descs, nsweeps);
     count_launch(ctx, 2);
     MCX_CUDA(cudaGetLastError());
