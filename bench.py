@@ -261,12 +261,15 @@ def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
             "alg_bytes_per_launch": 1.5 * N / 8}
 
 
-def bench_flathist(torch, mcx, ctx, dev, nwalkers=512, L=1024):
+def bench_flathist(torch, mcx, ctx, dev, nwalkers=None, L=1024):
     """Multicanonical production on 2-D Blume-Capel L=1024, J=1, D=1 (integer energies,
     4,194,305 bins of FP64 ln g and int64 H shared by the walkers): one sweep of
-    `nwalkers` independent walkers (one warp each).  The walker itself is serial, so the
-    throughput comes from the number of walkers."""
+    `nwalkers` independent walkers (one block of a producer and a consumer warp each).  The
+    walker itself is serial, so the throughput comes from the number of walkers: by default
+    one full wave, four walkers per SM (the resident limit of the walker kernel)."""
     from mcx import flathist as F
+    if nwalkers is None:
+        nwalkers = 4 * torch.cuda.get_device_properties(dev).multi_processor_count
 
     N = L * L
     walkers = []
