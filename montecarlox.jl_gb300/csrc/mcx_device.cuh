@@ -221,4 +221,19 @@ __device__ __forceinline__ void block_add_atomic(long long (&v)[NV], unsigned lo
     __syncthreads();
 }
 
+// Warp-wide sum of up to 4 values, one atomicAdd per nonzero value per warp, no barrier.
+// The caller guarantees that every per-warp sum fits in int32 (the small-lattice bodies:
+// at most 64 sites per thread and sweep, each changing a count by at most 12).
+template <int NV>
+__device__ __forceinline__ void warp_add_atomic(const long long (&v)[NV], unsigned long long* const (&dst)[NV]) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        int x = (int)v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+        if ((threadIdx.x & 31) == 0 && x != 0 && dst[j] != nullptr)
+            atomicAdd(dst[j], (unsigned long long)(long long)x);
+    }
+}
+
 }  // namespace mcx

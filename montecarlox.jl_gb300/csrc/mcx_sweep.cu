@@ -22,8 +22,9 @@
 namespace mcx {
 
 // The kernel bodies below take the work items first, first + stride, ... of one
-// half-sweep (a.cur / a.oth may point to global or shared memory) and leave the thread's
-// deltas (pair, spin, spin2, accepted) in v.  The grid kernels run one half-sweep per
+// half-sweep (the word bodies as a ChunkIter already decomposed into row and chunk;
+// a.cur / a.oth may point to global or shared memory) and leave the thread's deltas
+// (pair, spin, spin2, accepted) in v.  The grid kernels run one half-sweep per
 // launch; k_lattice_small runs every sweep of a call in one block on a shared-memory copy.
 
 template <int DIM, bool HB, bool T32>
@@ -39,16 +40,14 @@ __device__ __forceinline__ void ising_tables(const SweepArgs& a, unsigned long l
 
 template <int DIM, int V, bool HB, bool T32>
 __device__ __forceinline__ void ising_cb_body(const SweepArgs& a, const unsigned long long* s_thr,
-                                              const uint32_t* s_t32, long long first, long long stride,
-                                              long long (&v)[4]) {
+                                              const uint32_t* s_t32, ChunkIter it, long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
-    const int cpr = a.W / V;
     const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
     int nacc = 0, isum = 0, nup = 0;
-    for (ChunkIter it(first, stride, cpr, a.Ly, a.Lz); it.valid(); it.next()) {
+    for (; it.valid(); it.next()) {
         const int r = it.row();
         const int k0 = it.q * V;
         const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
@@ -89,8 +88,9 @@ __global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
     ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
     __syncthreads();
     long long v[4] = {0, 0, 0, 0};
-    ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, blockIdx.x * (long long)blockDim.x + threadIdx.x,
-                                   (long long)gridDim.x * blockDim.x, v);
+    const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
+                       a.Ly, a.Lz);
+    ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, it, v);
     long long w[3] = {v[0], v[1], v[3]};
     const unsigned long long sh = series_shift(a);
     unsigned long long* const dst[3] = {a.dst[0] + sh, a.dst[1] + sh, a.acc};
@@ -148,17 +148,16 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
 
 // ------------------------------------------------------------ Blume-Capel --
 template <int DIM, int V, bool HB>
-__device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned long long* s_thr, long long first,
-                                           long long stride, long long (&v)[4]) {
+__device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned long long* s_thr, ChunkIter it,
+                                           long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
     const SweepKey key = sweep_key(a);
     const unsigned long long sweep = key.sweep;
-    const int cpr = a.W / V;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
     const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
-    for (ChunkIter it(first, stride, cpr, a.Ly, a.Lz); it.valid(); it.next()) {
+    for (; it.valid(); it.next()) {
         const int r = it.row();
         const int k0 = it.q * V;
         const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
@@ -196,8 +195,9 @@ __global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
     long long v[4] = {0, 0, 0, 0};
-    bc_cb_body<DIM, V, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
-                           (long long)gridDim.x * blockDim.x, v);
+    const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
+                       a.Ly, a.Lz);
+    bc_cb_body<DIM, V, HB>(a, s_thr, it, v);
     const unsigned long long sh = series_shift(a);
     unsigned long long* const dst[4] = {a.dst[0] + sh, a.dst[1] + sh, a.dst[2] + sh, a.acc};
     block_add_atomic<4>(v, dst);
@@ -310,6 +310,8 @@ __device__ __forceinline__ void lattice_small_run(const SweepArgs& a0, int8_t* g
     a.sweep_base = nullptr;
     a.acc = a0.acc;
     const unsigned long long sweep0 = a0.sweep;
+    // this thread's chunks are the same in every half-sweep: decompose them once
+    const ChunkIter it0(threadIdx.x, blockDim.x, a0.W / V, a0.Ly, a0.Lz);
     for (long long t = 0; t < nsweeps; ++t) {
         long long v[4] = {0, 0, 0, 0};
         for (int c = 0; c < 2; ++c) {
@@ -317,15 +319,15 @@ __device__ __forceinline__ void lattice_small_run(const SweepArgs& a0, int8_t* g
             a.cur = c ? s1 : s0;
             a.oth = c ? s0 : s1;
             a.sweep = sweep0 + (unsigned long long)t;
-            if constexpr (KIND == 0) ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, threadIdx.x, blockDim.x, v);
+            if constexpr (KIND == 0) ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, it0, v);
             else if constexpr (KIND == 1) ising_site_body<DIM, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
-            else if constexpr (KIND == 2) bc_cb_body<DIM, V, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
+            else if constexpr (KIND == 2) bc_cb_body<DIM, V, HB>(a, s_thr, it0, v);
             else bc_site_body<DIM, HB>(a, s_thr, threadIdx.x, blockDim.x, v);
             __syncthreads();
         }
         unsigned long long* const dst[4] = {(unsigned long long*)(series + 3 * t), (unsigned long long*)(series + 3 * t + 1),
                                             (unsigned long long*)(series + 3 * t + 2), a.acc};
-        block_add_atomic<4>(v, dst);
+        warp_add_atomic<4>(v, dst);  // half <= 8192: per-warp sums fit in int32
     }
     if (half % 16 == 0) {
         for (long long i = threadIdx.x; i < half / 16; i += blockDim.x) {
