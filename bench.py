@@ -363,7 +363,7 @@ def bench_small(torch, mcx, ctx, with_cpu, cpu_seconds):
         c.close()
     res = {"workload": "ising2d_L64_metropolis_1e3_therm_1e4_sweeps_record", "attempts_per_ns": N * 1e4 / (ms * 1e6),
            "batched_chains": nch, "batched_attempts_per_ns": nch * N * 1e4 / (bms * 1e6),
-           "us_per_sweep": ms * 1e3 / 1e4, "kernel": "k_lattice_small<0,2,4,false,true>", "launches_per_call": 2,
+           "us_per_sweep": ms * 1e3 / 1e4, "kernel": "k_lattice_small<0,2,8,false,true> (256 threads)", "launches_per_call": 2,
            "series_rows": int(obs.shape[0])}
     if with_cpu:
         import oracle as O

@@ -40,6 +40,10 @@ ISING_CASES = [
     ([32, 32], "metropolis", 0.4407, 0.0),  # W=16: 128-bit rows
     ([64, 64], "glauber", 0.4407, 0.0),
     ([64, 48], "heatbath", 0.3, -0.2),
+    # one-block kernel chunk widths: 64^2 takes 8-site chunks, these 16-site chunks
+    ([128, 64], "metropolis", 0.4407, 0.0),
+    ([128, 128], "heatbath", 0.4407, 0.1),
+    ([32, 16, 16], "glauber", 0.22, 0.0),
     ([4, 4, 4], "metropolis", 0.22, 0.0),
     ([24, 24, 24], "metropolis", 0.2216, 0.0),
     ([32, 8, 6], "heatbath", 0.25, 0.1),
@@ -66,6 +70,7 @@ BC_CASES = [
     ([32, 32], "metropolis", 0.6, 1.0, 0.0),
     ([64, 64], "heatbath", 0.6, 1.0, 0.0),
     ([64, 40], "glauber", 0.45, 0.5, 0.2),
+    ([128, 96], "metropolis", 0.6, 1.0, 0.0),  # 16-site chunks in the one-block kernel
     ([8, 8, 8], "metropolis", 0.3, 1.0, 0.0),
     ([32, 16, 8], "heatbath", 0.35, 0.7, 0.0),
 ]
@@ -258,6 +263,10 @@ def test_autotune_keeps_results(gpu, L, alg):
     (O.BC, [[64, 64], [16, 24], [40, 8]], "heatbath"),
     (O.BC, [[32, 32], [8, 8]], "metropolis"),
     (O.ISING, [[64, 64], [256, 128]], "glauber"),   # a lattice above the one-block size: one call each
+    (O.ISING, [[128, 128], [128, 64]], "metropolis"),  # 16-site chunks
+    (O.ISING, [[64, 64], [128, 128]], "heatbath"),     # 8-site chunks (the narrower lattice's width)
+    (O.BC, [[128, 128], [64, 128]], "metropolis"),
+    (O.BC, [[64, 64]], "glauber"),                    # 8-site chunks
 ])
 def test_sweep_batch_matches_each_chain(gpu, model, dims, alg):
     """Independent chains in one call (ParallelChains): each lattice's series, spins and
