@@ -119,6 +119,7 @@ struct mcx_lattice {
     int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
+    int cluster_size = 0;          // CTAs of the last cluster-form call (0: not tried, -1: none fits)
     unsigned long long* d_sweep_base = nullptr;  // {first sweep, seed, stream, series offset} read by captured graphs
     struct Graph {
         int alg;

@@ -19,6 +19,7 @@
 #include "mcx_internal.h"
 #include "mcx_sweep.cuh"
 #include "mcx_cb.cuh"
+#include "mcx_body.cuh"
 
 namespace mcx {
 
@@ -28,25 +29,12 @@ namespace mcx {
 // (pair, spin, spin2, accepted) in v.  The grid kernels run one half-sweep per
 // launch; k_lattice_small runs every sweep of a call in one block on a shared-memory copy.
 
-template <int DIM, bool HB, bool T32>
-__device__ __forceinline__ void ising_tables(const SweepArgs& a, unsigned long long* s_thr, uint32_t* s_t32) {
-    constexpr int Z = 2 * DIM;
-    constexpr int NT = 2 * (Z + 1);
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-        const unsigned long long e = ising_tab_entry(a.thr[t], t, Z, HB);
-        if (T32) s_t32[t] = (uint32_t)(e - 1);
-        else s_thr[t] = e;
-    }
-}
-
 template <int DIM, int V, bool HB, bool T32>
 __device__ __forceinline__ void ising_cb_body(const SweepArgs& a, const unsigned long long* s_thr,
                                               const uint32_t* s_t32, ChunkIter it, long long (&v)[4]) {
     constexpr int Z = 2 * DIM;
-    constexpr int NW = V / 4;
     const SweepKey key = sweep_key(a);
-    const unsigned long long sweep = key.sweep;
-    const uint32_t w2 = ctr_word2(sweep, a.colour, P_ACCEPT);
+    const uint32_t w2 = ctr_word2(key.sweep, a.colour, P_ACCEPT);
     int nacc = 0, isum = 0, nup = 0;
     for (; it.valid(); it.next()) {
         const int r = it.row();
@@ -55,23 +43,7 @@ __device__ __forceinline__ void ising_cb_body(const SweepArgs& a, const unsigned
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
         const uint32_t c0 = (uint32_t)(((unsigned long long)r * a.W + k0) >> 2);
-        uint32_t af = 0, au = 0, ai = 0;
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            uint32_t nbw[Z];
-#pragma unroll
-            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
-            const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)sweep, w2, key.stream), key.k0, key.k1);
-            uint32_t fb;
-            if (T32) fb = ising_word32<Z, HB>(nbw, ch.own[w], rnd, s_t32, af, au, ai);
-            else fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);
-            ch.own[w] ^= fb * 0xFEu;
-        }
-        if (T32) {
-            nacc += hsum8(af);
-            nup += hsum8(au);
-            isum += hsum16(ai);
-        }
+        ising_chunk<DIM, V, HB, T32>(ch, c0, key, w2, s_thr, s_t32, nacc, nup, isum);
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
     long long dP, dM;
@@ -151,12 +123,9 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
 template <int DIM, int V, bool HB>
 __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned long long* s_thr, ChunkIter it,
                                            long long (&v)[4]) {
-    constexpr int Z = 2 * DIM;
-    constexpr int NW = V / 4;
     const SweepKey key = sweep_key(a);
-    const unsigned long long sweep = key.sweep;
-    const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
-    const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
+    const uint32_t w2a = ctr_word2(key.sweep, a.colour, P_ACCEPT);
+    const uint32_t w2p = ctr_word2(key.sweep, a.colour, P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
     for (; it.valid(); it.next()) {
         const int r = it.row();
@@ -164,20 +133,8 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
         const RowInfo ri = row_info_yz(it.y, it.z, a.Ly, a.Lz, a.colour, DIM);
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
-        const unsigned long long j0 = (unsigned long long)r * a.W + k0;
-        BcLanes ln;
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            uint32_t nbw[Z];
-#pragma unroll
-            for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
-            const uint32_t c0 = (uint32_t)(j0 >> 2) + w;
-            const uint4 ra = philox10(make_uint4(c0, (uint32_t)sweep, w2a, key.stream), key.k0, key.k1);
-            uint4 rp = make_uint4(0, 0, 0, 0);
-            if (!HB) rp = philox10(make_uint4(c0, (uint32_t)sweep, w2p, key.stream), key.k0, key.k1);
-            ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, ln);
-        }
-        bc_lanes_fold<Z>(ln, dP, dM, dQ);
+        const uint32_t c0 = (uint32_t)(((unsigned long long)r * a.W + k0) >> 2);
+        bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, s_thr, nacc, dP, dM, dQ);
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
     v[0] += dP;
@@ -185,9 +142,6 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
     v[2] += dQ;
     v[3] += nacc;
 }
-
-template <int DIM, bool HB>
-__host__ __device__ constexpr int bc_table_size() { return HB ? 2 * (4 * DIM + 1) : 6 * (4 * DIM + 1); }
 
 template <int DIM, int V, bool HB>
 __global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
@@ -415,14 +369,15 @@ HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, 
 
 using SmallLatticeFn = void (*)(SweepArgs, int8_t*, int8_t*, long long, long long, long long*);
 
-// The chunk width of the small-lattice kernels: the widest V in {16, 8} that divides the
-// row and still leaves at least 256 chunks of one colour, else 4.  Wider chunks share the
+// The chunk width of the one-block and cluster kernels: the widest V in {16, 8} that
+// divides the row and still leaves at least 256 chunks of the sites of a colour one block
+// holds, else 4.  Wider chunks share the
 // per-chunk row and address work over more sites; 256 chunks keep enough warps busy on
 // the one SM (64^2: V = 8 on 256 threads, 9 % faster than V = 4; 128^2: V = 16 on 512
 // threads, 25 % faster; identical results, the stream does not depend on V).
-static int small_width(int64_t W, long long half) {
+int small_width(int64_t W, long long sites) {
     for (int V : {16, 8})
-        if (W % V == 0 && half / V >= 256) return V;
+        if (W % V == 0 && sites / V >= 256) return V;
     return 4;
 }
 
@@ -599,14 +554,20 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     Table t;
     MCX_CHECK(build_table(lat, alg, beta, &t));
     MCX_CHECK(ensure_series(lat, nsweeps > 0 ? nsweeps : 1));
-    // small int8 lattices run every sweep of the call in one block (one launch); larger
-    // ones replay a captured chunk of kGraphChunk sweeps as often as it fits and launch
-    // the rest directly
-    const bool small = lat->layout == MCX_LAYOUT_INT8 && lat->N <= kSmallLattice && nsweeps >= 1;
-    const bool graph = !small && lat->layout == MCX_LAYOUT_INT8 && nsweeps >= kGraphChunk;
+    // medium int8 lattices run every sweep of the call in one thread-block cluster, small
+    // ones (and those the cluster form does not take, up to kSmallLattice sites) in one
+    // block; larger ones replay a captured chunk of kGraphChunk sweeps as often as it fits
+    // and launch the rest directly
+    const bool int8 = lat->layout == MCX_LAYOUT_INT8;
     MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
     MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
-    if (lat->layout == MCX_LAYOUT_MSC64) {
+    bool clustered = false;
+    if (int8 && lat->N > kClusterMin) MCX_CHECK(cluster_sweep(lat, alg, t, rng, nsweeps, &clustered));
+    const bool small = !clustered && int8 && lat->N <= kSmallLattice && nsweeps >= 1;
+    const bool graph = !small && !clustered && int8 && nsweeps >= kGraphChunk;
+    if (clustered) {
+        // launched by cluster_sweep
+    } else if (lat->layout == MCX_LAYOUT_MSC64) {
         MCX_CHECK(msc_sweep(lat, alg, t, rng, nsweeps));
     } else if (small) {
         SweepArgs a;

@@ -48,6 +48,20 @@ using HalfSweepFn = void (*)(const SweepArgs);
 // int8 lattices of at most this many sites run all sweeps of a call in one block with
 // both colour arrays in shared memory
 constexpr long long kSmallLattice = 16384;
+// int8 lattices above kClusterMin and up to kClusterLattice sites run all sweeps of a call
+// in one thread-block cluster (rows or z-planes spread over its CTAs' shared memory) when
+// their rows are a multiple of 4 sites of a colour; per sweep on a GB300: Ising 96^2 2.56 us
+// in one block against 1.53 in a cluster, 128^2 3.28 against 1.53; 64^2 1.46 against 1.51;
+// 640^2 6.23 with a graph node per half-sweep against 5.58
+constexpr long long kClusterMin = 4096;
+constexpr long long kClusterLattice = 524288;
+
+// chunk width of the one-block and cluster kernels for rows of W sites of a colour and
+// `sites` sites of a colour per block
+int small_width(int64_t W, long long sites);
+// the cluster form; *done = false when it does not apply or no cluster fits the device
+mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
+                         bool* done);
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);

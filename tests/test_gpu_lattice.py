@@ -40,7 +40,7 @@ ISING_CASES = [
     ([32, 32], "metropolis", 0.4407, 0.0),  # W=16: 128-bit rows
     ([64, 64], "glauber", 0.4407, 0.0),
     ([64, 48], "heatbath", 0.3, -0.2),
-    # one-block kernel chunk widths: 64^2 takes 8-site chunks, these 16-site chunks
+    # 64^2 takes 8-site chunks in the one-block kernel; these run as thread-block clusters
     ([128, 64], "metropolis", 0.4407, 0.0),
     ([128, 128], "heatbath", 0.4407, 0.1),
     ([32, 16, 16], "glauber", 0.22, 0.0),
@@ -70,7 +70,7 @@ BC_CASES = [
     ([32, 32], "metropolis", 0.6, 1.0, 0.0),
     ([64, 64], "heatbath", 0.6, 1.0, 0.0),
     ([64, 40], "glauber", 0.45, 0.5, 0.2),
-    ([128, 96], "metropolis", 0.6, 1.0, 0.0),  # 16-site chunks in the one-block kernel
+    ([128, 96], "metropolis", 0.6, 1.0, 0.0),  # a thread-block cluster
     ([8, 8, 8], "metropolis", 0.3, 1.0, 0.0),
     ([32, 16, 8], "heatbath", 0.35, 0.7, 0.0),
 ]
@@ -140,7 +140,7 @@ def test_sweeps_compose_and_replay(gpu):
 def test_replayed_sequence_follows_each_calls_stream(gpu):
     """Multi-sweep calls replay one captured sequence per (algorithm, beta, length):
     every replay must still use its own call's seed, stream and counter."""
-    L = [128, 160]  # above the one-block limit
+    L = [1088, 512]  # above the one-cluster limit: captured graph replay
     s0 = O.init_random(O.ISING, L, 1, 0)
     sys_ = gpu.Ising(L)
     for seed, stream, counter in ((11, 0, 0), (12, 3, 0), (11, 0, 40), (99, 7, 5)):
@@ -155,11 +155,13 @@ def test_replayed_sequence_follows_each_calls_stream(gpu):
         assert a.accepted == acc
 
 
-@pytest.mark.parametrize("model,L,alg,nsweeps", [(O.ISING, [256, 128], "metropolis", 71),
-                                                  (O.BC, [256, 128], "heatbath", 130),
-                                                  (O.ISING, [32, 32, 32], "glauber", 65)])
+@pytest.mark.parametrize("model,L,alg,nsweeps", [(O.ISING, [1024, 544], "metropolis", 71),
+                                                  (O.BC, [736, 736], "heatbath", 66),
+                                                  (O.ISING, [64, 64, 136], "glauber", 65),
+                                                  (O.ISING, [130, 256], "metropolis", 65)])  # rows of 65: site kernel
 def test_chunked_graph_replay(gpu, model, L, alg, nsweeps):
-    """Lattices above the one-block limit replay a captured 64-sweep chunk back to back and
+    """Lattices above the one-cluster limit (and medium ones whose rows are not a multiple
+    of four) replay a captured 64-sweep chunk back to back and
     launch the remainder directly; every call (any length, seed, stream, counter) matches
     the oracle, series included."""
     D = 1.0 if model == O.BC else 0.0
@@ -176,6 +178,52 @@ def test_chunked_graph_replay(gpu, model, L, alg, nsweeps):
         assert np.array_equal(obs, oobs), (seed, stream, counter, n)
         assert np.array_equal(sys_.spins, s)
         assert (a.flips if alg == "heatbath" else a.accepted) == acc
+
+
+CLUSTER_CASES = [
+    # model, dims, algorithm, beta, D, h: medium lattices (4,096 < N <= 524,288 sites), every
+    # sweep of a call in one thread-block cluster; uneven cuts, 4/8/16-site chunks, 3-D planes
+    (O.ISING, [256, 256], "metropolis", 0.4407, 0.0, 0.0),
+    (O.ISING, [512, 512], "heatbath", 0.44, 0.0, 0.1),
+    (O.ISING, [200, 200], "glauber", 0.4, 0.0, 0.0),
+    (O.ISING, [4096, 8], "metropolis", 3.0, 0.0, 0.0),  # 8 rows: 8 CTAs; thresholds of 0
+    (O.ISING, [64, 64, 16], "metropolis", 0.2216, 0.0, 0.0),
+    (O.ISING, [40, 40, 40], "heatbath", 0.22, 0.0, 0.0),
+    (O.ISING, [128, 64, 8], "glauber", 0.25, 0.0, -0.2),
+    (O.BC, [256, 256], "metropolis", 0.6, 1.0, 0.0),
+    (O.BC, [200, 160], "heatbath", 0.5, 0.5, 0.1),
+    (O.BC, [32, 32, 32], "metropolis", 0.35, 1.0, 0.0),
+    (O.BC, [64, 64, 64], "heatbath", 0.3, 0.7, 0.0),
+]
+
+
+@pytest.mark.parametrize("model,L,alg,beta,D,h", CLUSTER_CASES)
+def test_cluster_parity(gpu, model, L, alg, beta, D, h):
+    """The cluster form (rows or planes spread over the CTAs' shared memory, halos through
+    distributed shared memory) equals the oracle bit for bit: series, spins, counters."""
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, model, L, alg, beta, D=D, h=h)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.steps == att
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    assert gpu.observables(sys_) == gpu.observables(sys_, full=True)
+
+
+def test_cluster_calls_compose(gpu):
+    """Cluster form: 1 + 3 + 70 sweeps equal one call of 74, and the oracle."""
+    L = [256, 192]
+    s0 = O.init_random(O.ISING, L, 2, 0)
+    runs = []
+    for parts in ((1, 3, 70), (74,)):
+        sys_ = gpu.Ising(L)
+        sys_.spins = s0
+        a = gpu.Metropolis(gpu.Philox(8, 1), beta=0.42)
+        obs = np.concatenate([gpu.sweep_(sys_, a, n, record=True) for n in parts])
+        runs.append((obs, sys_.spins.copy(), a.accepted))
+    s = s0.copy()
+    oobs, att, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.42, 8, stream=1, nsweeps=74)
+    for obs, spins, accepted in runs:
+        assert np.array_equal(obs, oobs) and np.array_equal(spins, s) and accepted == acc
 
 
 def test_context_outlives_its_objects(gpu):
