@@ -51,7 +51,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
-    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph", "graph_table", "lattice_small"],
+    ap.add_argument("--profile", choices=["pt", "flathist", "serve", "graph", "graph_table", "lattice_small",
+                                          "lattice_cluster"],
                     default=None,
                     help="run one short workload for a profiler capture and exit (no JSON line)")
     return ap.parse_args()
@@ -379,6 +380,32 @@ def bench_small(torch, mcx, ctx, with_cpu, cpu_seconds):
     return res
 
 
+def bench_medium(torch, mcx, ctx):
+    """Medium lattices, one call of 1000 sweeps with E and M every sweep (CUDA events on the
+    context's stream): every sweep of the call runs in one thread-block cluster."""
+    import numpy as np
+    res = []
+    for dims, model, beta in (([256, 256], "ising", BETA), ([128, 128], "ising", BETA), ([32, 32, 32], "ising", 0.2216),
+                              ([256, 256], "blume_capel", 0.6)):
+        lat = mcx.Ising(dims, ctx=ctx) if model == "ising" else mcx.BlumeCapel(dims, D=1.0, ctx=ctx)
+        mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+        alg = mcx.Metropolis(mcx.Philox(SEED), beta=beta)
+        mcx.sweep_(lat, alg, 100)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mcx.sweep_(lat, alg, 1000, record=True)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        N = int(np.prod(dims))
+        res.append({"workload": "%s_%s_metropolis_1000_sweeps_record" % (model, "x".join(map(str, dims))),
+                    "us_per_sweep": ms, "attempts_per_ns": N * 1000 / (ms * 1e6)})
+        lat.close()
+    return {"kernel": "k_lattice_cluster (one cluster of up to 16 CTAs, one launch per call)", "lines": res}
+
+
 def torus_csr(L, seed, per_entry):
     """CSR of the L x L periodic grid (first coordinate fastest, sorted rows) and, when
     per_entry, symmetric Gaussian couplings: the 2-D Edwards-Anderson spin glass."""
@@ -568,9 +595,10 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = None
     if not args.no_extras:
         small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
+        med_res = bench_medium(torch, mcx, ctx)
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
@@ -609,6 +637,7 @@ def run_mcx(args):
         "msc64": msc_res,
         "general_graphs": graph_res,
         "small_lattice": small_res,
+        "medium_lattice": med_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -650,6 +679,12 @@ def run_profile_target(args):
         alg = mcx.Metropolis(mcx.Philox(42), beta=BETA)
         mcx.sweep_(lat, alg, 1000)
         mcx.sweep_(lat, alg, 10000, record=True)
+    elif args.profile == "lattice_cluster":
+        lat = mcx.Ising([256, 256], ctx=ctx)
+        mcx.init_(lat, "random", rng=mcx.Philox(42))
+        alg = mcx.Metropolis(mcx.Philox(42), beta=BETA)
+        mcx.sweep_(lat, alg, 100)
+        mcx.sweep_(lat, alg, 1000, record=True)
     elif args.profile in ("graph", "graph_table"):
         from mcx.graph import IsingGraphDevice
         # 4.2M sites; Gaussian couplings (0.25 GB of neighbour data) or one J (the table form)
