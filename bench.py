@@ -403,7 +403,27 @@ def bench_medium(torch, mcx, ctx):
         res.append({"workload": "%s_%s_metropolis_1000_sweeps_record" % (model, "x".join(map(str, dims))),
                     "us_per_sweep": ms, "attempts_per_ns": N * 1000 / (ms * 1e6)})
         lat.close()
-    return {"kernel": "k_lattice_cluster (one cluster of up to 16 CTAs, one launch per call)", "lines": res}
+    # independent 256^2 chains (ParallelChains): one cluster each in one mcx_sweep_batch launch;
+    # eight clusters of 16 CTAs run at once on a GB300 (nine took 1.5x as long as eight)
+    nch = 8
+    chains = [mcx.Ising([256, 256], ctx=ctx) for _ in range(nch)]
+    for i, c in enumerate(chains):
+        mcx.init_(c, "random", rng=mcx.Philox(SEED, i))
+    calgs = [mcx.Metropolis(mcx.Philox(SEED, i), beta=BETA) for i in range(nch)]
+    mcx.sweep_batch_(chains, calgs, 100)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    mcx.sweep_batch_(chains, calgs, 1000, record=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    res.append({"workload": "ising_256x256_metropolis_1000_sweeps_record_x%d_chains_one_call" % nch,
+                "us_per_sweep": ms, "attempts_per_ns": nch * 65536 * 1000 / (ms * 1e6)})
+    for c in chains:
+        c.close()
+    return {"kernel": "k_lattice_cluster (one cluster of up to 16 CTAs per lattice, one launch per call)", "lines": res}
 
 
 def torus_csr(L, seed, per_entry):

@@ -32,14 +32,16 @@ struct ClusterArgs {
     SweepArgs a;      // geometry, key, table and counter (cur, oth and dst are not used)
     int8_t* g[2];     // the colour arrays in global memory
     long long* series;
+    long long* state;  // running (pair, spin, spin2), for the batched prefix
     long long nsweeps;
     int units, U;     // units of the cut and rows per unit
+    int zero;         // zero the series slots and the counter first (batched form)
 };
 
 __device__ __forceinline__ int first_unit(int units, int C, int b) { return (int)((long long)units * b / C); }
 
 template <int KIND, int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(512, 1) k_lattice_cluster(const ClusterArgs ca) {
+__device__ __forceinline__ void cluster_run(const ClusterArgs& ca) {
     extern __shared__ __align__(16) int8_t s_lat[];
     __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
     __shared__ uint32_t s_t32[kMaxTable];
@@ -70,7 +72,12 @@ __global__ void __launch_bounds__(512, 1) k_lattice_cluster(const ClusterArgs ca
     } else {
         for (int t = threadIdx.x; t < kMaxTable; t += blockDim.x) s_thr[t] = a0.thr[t];
     }
-    cl.sync();  // every halo is loaded before a neighbour stores into it
+    if (ca.zero) {
+        for (long long i = (long long)k * blockDim.x + threadIdx.x; i < 3 * ca.nsweeps; i += (long long)C * blockDim.x)
+            ca.series[i] = 0;
+        if (k == 0 && threadIdx.x == 0) *a0.acc = 0ull;
+    }
+    cl.sync();  // every halo is loaded (and the slots zeroed) before a neighbour stores into it
     // where this CTA's first unit lives in the previous CTA (its bottom halo) and its last
     // unit in the next CTA (its top halo)
     int8_t* const up0 = cl.map_shared_rank(s[0], kp) + (nu_p + 1) * unitB;
@@ -151,22 +158,116 @@ __global__ void __launch_bounds__(512, 1) k_lattice_cluster(const ClusterArgs ca
     }
 }
 
-using ClusterFn = void (*)(const ClusterArgs);
-
-template <int KIND, int DIM, bool HB, bool T32>
-ClusterFn pick_cluster_v(int V) {
-    if (V == 16) return k_lattice_cluster<KIND, DIM, 16, HB, T32>;
-    if (V == 8) return k_lattice_cluster<KIND, DIM, 8, HB, T32>;
-    return k_lattice_cluster<KIND, DIM, 4, HB, T32>;
+template <int KIND, int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(512, 1) k_lattice_cluster(const ClusterArgs ca) {
+    cluster_run<KIND, DIM, V, HB, T32>(ca);
 }
 
-template <int DIM>
-ClusterFn pick_cluster_dim(bool ising, bool hb, bool t32, int V) {
-    if (ising) {
-        if (hb) return t32 ? pick_cluster_v<0, DIM, true, true>(V) : pick_cluster_v<0, DIM, true, false>(V);
-        return t32 ? pick_cluster_v<0, DIM, false, true>(V) : pick_cluster_v<0, DIM, false, false>(V);
+// Independent lattices (a ParallelChains batch), one cluster each; clusters never wait on
+// one another, so the device may run them in any order and number at a time.
+template <int KIND, int DIM, int V, bool HB, bool T32>
+__global__ void __launch_bounds__(512, 1) k_lattice_cluster_batch(const ClusterArgs* __restrict__ d) {
+    cluster_run<KIND, DIM, V, HB, T32>(d[blockIdx.x / cg::this_cluster().num_blocks()]);
+}
+
+// the running series of every lattice of a batch (block b: lattice b), as k_prefix_series
+__global__ void k_prefix_series_cluster(const ClusterArgs* __restrict__ d, long long n) {
+    const ClusterArgs& c = d[blockIdx.x];
+    const int j = threadIdx.x;
+    if (j >= 3) return;
+    long long acc = c.state[j];
+    for (long long s = 0; s < n; ++s) {
+        acc += c.series[3 * s + j];
+        c.series[3 * s + j] = acc;
     }
-    return hb ? pick_cluster_v<2, DIM, true, false>(V) : pick_cluster_v<2, DIM, false, false>(V);
+    c.state[j] = acc;
+}
+
+using ClusterFn = void (*)(const ClusterArgs);
+using ClusterBatchFn = void (*)(const ClusterArgs*);
+
+template <int KIND, int DIM, int V, bool HB, bool T32>
+struct SingleC {
+    using Fn = ClusterFn;
+    static constexpr Fn fn = k_lattice_cluster<KIND, DIM, V, HB, T32>;
+};
+template <int KIND, int DIM, int V, bool HB, bool T32>
+struct BatchC {
+    using Fn = ClusterBatchFn;
+    static constexpr Fn fn = k_lattice_cluster_batch<KIND, DIM, V, HB, T32>;
+};
+
+template <template <int, int, int, bool, bool> class K, int KIND, int DIM, bool HB, bool T32>
+typename K<0, 2, 4, false, false>::Fn pick_cluster_v(int V) {
+    if (V == 16) return K<KIND, DIM, 16, HB, T32>::fn;
+    if (V == 8) return K<KIND, DIM, 8, HB, T32>::fn;
+    return K<KIND, DIM, 4, HB, T32>::fn;
+}
+
+template <template <int, int, int, bool, bool> class K, int DIM>
+typename K<0, 2, 4, false, false>::Fn pick_cluster_dim(bool ising, bool hb, bool t32, int V) {
+    if (ising) {
+        if (hb) return t32 ? pick_cluster_v<K, 0, DIM, true, true>(V) : pick_cluster_v<K, 0, DIM, true, false>(V);
+        return t32 ? pick_cluster_v<K, 0, DIM, false, true>(V) : pick_cluster_v<K, 0, DIM, false, false>(V);
+    }
+    return hb ? pick_cluster_v<K, 2, DIM, true, false>(V) : pick_cluster_v<K, 2, DIM, false, false>(V);
+}
+
+template <template <int, int, int, bool, bool> class K>
+typename K<0, 2, 4, false, false>::Fn pick_cluster(int dim, bool ising, bool hb, bool t32, int V) {
+    return dim == 2 ? pick_cluster_dim<K, 2>(ising, hb, t32, V) : pick_cluster_dim<K, 3>(ising, hb, t32, V);
+}
+
+// The cut of a lattice: units (rows in 2-D, z-planes in 3-D) and rows per unit.
+int cut_units(const mcx_lattice* lat) { return (int)(lat->dim == 2 ? lat->L[1] : lat->L[2]); }
+int cut_rows(const mcx_lattice* lat) { return (int)(lat->dim == 2 ? 1 : lat->L[1]); }
+
+// own sites of a colour of the largest CTA when the lattice is cut over C CTAs
+long long cut_sites(const mcx_lattice* lat, int C) {
+    const int units = cut_units(lat);
+    return (long long)((units + C - 1) / C) * cut_rows(lat) * lat->W;
+}
+
+bool cluster_eligible(const mcx_lattice* lat) {
+    return lat->layout == MCX_LAYOUT_INT8 && lat->W % 4 == 0 && lat->N <= kClusterLattice && cut_units(lat) >= 2;
+}
+
+void fill_cluster_args(ClusterArgs* ca, mcx_lattice* lat, const Table& t, const mcx_rng* rng, int64_t nsweeps,
+                       int zero) {
+    fill_sweep_args(&ca->a, lat, t, rng);
+    ca->a.acc = lat->d_acc;
+    ca->a.sweep = rng->counter;
+    ca->g[0] = lat->d_col[0];
+    ca->g[1] = lat->d_col[1];
+    ca->series = reinterpret_cast<long long*>(lat->d_series);
+    ca->state = reinterpret_cast<long long*>(lat->d_state);
+    ca->nsweeps = nsweeps;
+    ca->units = cut_units(lat);
+    ca->U = cut_rows(lat);
+    ca->zero = zero;
+}
+
+// Launch configuration of `nclusters` clusters of C CTAs; false when the device cannot
+// place one such cluster.
+mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int nclusters, cudaStream_t st,
+                          cudaLaunchConfig_t* cfg, cudaLaunchAttribute* attr, bool* ok) {
+    if (C > 8) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    if (smem > 48 * 1024) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    *cfg = cudaLaunchConfig_t{};
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg->gridDim = dim3((unsigned)(C * nclusters));
+    cfg->blockDim = dim3((unsigned)threads);
+    cfg->dynamicSmemBytes = smem;
+    cfg->stream = st;
+    cfg->attrs = attr;
+    cfg->numAttrs = 1;
+    int active = 0;
+    *ok = cudaOccupancyMaxActiveClusters(&active, fn, cfg) == cudaSuccess && active >= 1;
+    if (!*ok) (void)cudaGetLastError();
+    return MCX_OK;
 }
 
 }  // namespace
@@ -174,61 +275,84 @@ ClusterFn pick_cluster_dim(bool ising, bool hb, bool t32, int V) {
 mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
                          bool* done) {
     *done = false;
-    if (lat->layout != MCX_LAYOUT_INT8 || lat->W % 4 != 0 || lat->N > kClusterLattice || nsweeps < 1 ||
-        lat->cluster_size < 0)
-        return MCX_OK;
-    mcx_ctx* ctx = lat->ctx;
-    const int units = (int)(lat->dim == 2 ? lat->L[1] : lat->L[2]);
-    const int U = (int)(lat->dim == 2 ? 1 : lat->L[1]);
-    const long long unitB = (long long)U * lat->W;
+    if (!cluster_eligible(lat) || nsweeps < 1 || lat->cluster_size < 0) return MCX_OK;
     const bool hb = alg == MCX_HEATBATH, ising = lat->model == MCX_ISING;
     const bool t32 = ising && ising_table_fits32(t.thr, t.n, 2 * lat->dim, hb);
+    const long long unitB = (long long)cut_rows(lat) * lat->W;
     ClusterArgs ca;
-    fill_sweep_args(&ca.a, lat, t, rng);
-    ca.a.acc = lat->d_acc;
-    ca.a.sweep = rng->counter;
-    ca.g[0] = lat->d_col[0];
-    ca.g[1] = lat->d_col[1];
-    ca.series = reinterpret_cast<long long*>(lat->d_series);
-    ca.nsweeps = nsweeps;
-    ca.units = units;
-    ca.U = U;
+    fill_cluster_args(&ca, lat, t, rng, nsweeps, 0);
     // the largest cluster (<= 16 CTAs, one unit each at least) whose CTAs hold at most
     // 16384 sites of a colour and that the device can place
-    for (int C = std::min(16, units); C >= 2; --C) {
-        const long long per = (long long)((units + C - 1) / C) * unitB;  // own sites of one colour
+    for (int C = std::min(16, cut_units(lat)); C >= 2; --C) {
+        const long long per = cut_sites(lat, C);
         if (per > kSmallLattice) break;
         const int V = small_width(lat->W, per);
-        const ClusterFn fn = lat->dim == 2 ? pick_cluster_dim<2>(ising, hb, t32, V) : pick_cluster_dim<3>(ising, hb, t32, V);
+        const ClusterFn fn = pick_cluster<SingleC>(lat->dim, ising, hb, t32, V);
         const int threads = (int)std::min<long long>(512, std::max<long long>(32, (per / V + 31) & ~31ll));
         const size_t smem = 2 * (size_t)((per + 2 * unitB + 15) & ~15ll);
-        if (C > 8) MCX_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        if (smem > 48 * 1024)
-            MCX_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        cudaLaunchConfig_t cfg = {};
+        cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = (unsigned)C;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.gridDim = dim3((unsigned)C);
-        cfg.blockDim = dim3((unsigned)threads);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = ctx->stream;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)fn, &cfg) != cudaSuccess || nclusters < 1) {
-            (void)cudaGetLastError();
-            continue;
-        }
+        bool ok = false;
+        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, 1, lat->ctx->stream, &cfg, attr, &ok));
+        if (!ok) continue;
         MCX_CUDA(cudaLaunchKernelEx(&cfg, fn, ca));
-        count_launch(ctx);
+        count_launch(lat->ctx);
         lat->cluster_size = C;
         *done = true;
         return MCX_OK;
     }
     lat->cluster_size = -1;  // no cluster fits: the per-half-sweep forms
+    return MCX_OK;
+}
+
+mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, const Table* tabs, const mcx_rng* rngs,
+                               int64_t nsweeps, bool fits32, bool* done) {
+    *done = false;
+    if (n < 1 || nsweeps < 1) return MCX_OK;
+    int cmax = 16;
+    for (int i = 0; i < n; ++i) {
+        if (!cluster_eligible(lats[i])) return MCX_OK;
+        cmax = std::min(cmax, cut_units(lats[i]));
+    }
+    mcx_lattice* L0 = lats[0];
+    mcx_ctx* ctx = L0->ctx;
+    const bool hb = alg == MCX_HEATBATH, ising = L0->model == MCX_ISING;
+    const bool t32 = ising && fits32;
+    // one cluster size for the batch: the largest every lattice takes
+    for (int C = cmax; C >= 2; --C) {
+        bool fit = true;
+        int V = 16;
+        long long maxchunks = 0;
+        size_t smem = 0;
+        for (int i = 0; i < n && fit; ++i) {
+            const long long per = cut_sites(lats[i], C);
+            fit = per <= kSmallLattice;
+            V = std::min(V, small_width(lats[i]->W, per));  // divides every row (powers of two)
+            smem = std::max(smem, 2 * (size_t)((per + 2LL * cut_rows(lats[i]) * lats[i]->W + 15) & ~15ll));
+        }
+        if (!fit) break;
+        for (int i = 0; i < n; ++i) maxchunks = std::max(maxchunks, cut_sites(lats[i], C) / V);
+        const int threads = (int)std::min<long long>(512, std::max<long long>(32, (maxchunks + 31) & ~31ll));
+        const ClusterBatchFn fn = pick_cluster<BatchC>(L0->dim, ising, hb, t32, V);
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr[1];
+        bool ok = false;
+        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, n, ctx->stream, &cfg, attr, &ok));
+        if (!ok) continue;
+        std::vector<ClusterArgs> descs(n);
+        for (int i = 0; i < n; ++i) fill_cluster_args(&descs[i], lats[i], tabs[i], &rngs[i], nsweeps, 1);
+        void* scratch = nullptr;
+        MCX_CHECK(ctx_scratch(ctx, sizeof(ClusterArgs) * (size_t)n, &scratch));
+        ClusterArgs* d = static_cast<ClusterArgs*>(scratch);
+        MCX_CUDA(cudaMemcpyAsync(d, descs.data(), sizeof(ClusterArgs) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        MCX_CUDA(cudaLaunchKernelEx(&cfg, fn, (const ClusterArgs*)d));
+        k_prefix_series_cluster<<<n, 32, 0, ctx->stream>>>(d, nsweeps);
+        count_launch(ctx, 2);
+        MCX_CUDA(cudaGetLastError());
+        MCX_CUDA(cudaStreamSynchronize(ctx->stream));  // the descriptors outlive the copy
+        *done = true;
+        return MCX_OK;
+    }
     return MCX_OK;
 }
 

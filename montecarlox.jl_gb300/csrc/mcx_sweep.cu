@@ -732,6 +732,29 @@ extern "C" MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, 
     return MCX_OK;
 }
 
+// after a batched launch: series lengths, counters, the caller's series and counts
+static mcx_status batch_tail(mcx_lattice** lats, int n, mcx_rng* rngs, int64_t nsweeps, int64_t** obs_series,
+                             mcx_counters* counters) {
+    cudaStream_t st = lats[0]->ctx->stream;
+    std::vector<unsigned long long> acc(counters ? n : 0);
+    for (int i = 0; i < n; ++i) {
+        lats[i]->series_len = nsweeps;
+        rngs[i].counter += (uint64_t)nsweeps;
+        if (obs_series && obs_series[i])
+            MCX_CUDA(cudaMemcpyAsync(obs_series[i], lats[i]->d_series, (size_t)nsweeps * 3 * sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, st));
+        if (counters)
+            MCX_CUDA(cudaMemcpyAsync(&acc[i], lats[i]->d_acc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    }
+    MCX_CUDA(cudaStreamSynchronize(st));  // acc outlives the copies
+    if (counters)
+        for (int i = 0; i < n; ++i) {
+            counters[i].attempts += (uint64_t)lats[i]->N * (uint64_t)nsweeps;
+            counters[i].accepted += acc[i];
+        }
+    return MCX_OK;
+}
+
 extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx_algorithm alg, const double* betas,
                                               mcx_rng* rngs, int64_t nsweeps, int64_t** obs_series,
                                               mcx_counters* counters) {
@@ -757,11 +780,21 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
         fits32 = fits32 && ising_table_fits32(tabs[i].thr, tabs[i].n, 2 * L->dim, alg == MCX_HEATBATH);
     }
     if (nsweeps == 0) return MCX_OK;
-    if (!small) {  // one call per lattice (identical results)
-        for (int i = 0; i < n; ++i)
-            MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
-                                counters ? &counters[i] : nullptr));
-        return MCX_OK;
+    if (!small) {
+        // medium lattices: one cluster each in one launch; otherwise one call per lattice
+        // (identical results)
+        bool clustered = false;
+        if (n > 1) {
+            for (int i = 0; i < n; ++i) MCX_CHECK(ensure_series(lats[i], nsweeps));
+            MCX_CHECK(cluster_sweep_batch(lats, n, alg, tabs.data(), rngs, nsweeps, fits32, &clustered));
+        }
+        if (!clustered) {
+            for (int i = 0; i < n; ++i)
+                MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
+                                    counters ? &counters[i] : nullptr));
+            return MCX_OK;
+        }
+        return batch_tail(lats, n, rngs, nsweeps, obs_series, counters);
     }
     std::vector<SmallBatchDesc> descs(n);
     long long maxhalf = 0;
@@ -800,21 +833,6 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
     k_prefix_series_batch<<<n, 32, 0, st>>>(d_descs, nsweeps);
     count_launch(ctx, 2);
     MCX_CUDA(cudaGetLastError());
-    std::vector<unsigned long long> acc(counters ? n : 0);
-    for (int i = 0; i < n; ++i) {
-        lats[i]->series_len = nsweeps;
-        rngs[i].counter += (uint64_t)nsweeps;
-        if (obs_series && obs_series[i])
-            MCX_CUDA(cudaMemcpyAsync(obs_series[i], lats[i]->d_series, (size_t)nsweeps * 3 * sizeof(int64_t),
-                                     cudaMemcpyDeviceToHost, st));
-        if (counters)
-            MCX_CUDA(cudaMemcpyAsync(&acc[i], lats[i]->d_acc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    }
-    MCX_CUDA(cudaStreamSynchronize(st));  // the descriptors and acc outlive the copies
-    if (counters)
-        for (int i = 0; i < n; ++i) {
-            counters[i].attempts += (uint64_t)lats[i]->N * (uint64_t)nsweeps;
-            counters[i].accepted += acc[i];
-        }
-    return MCX_OK;
+    MCX_CUDA(cudaStreamSynchronize(st));  // the descriptors outlive the copy
+    return batch_tail(lats, n, rngs, nsweeps, obs_series, counters);
 }

@@ -62,6 +62,10 @@ int small_width(int64_t W, long long sites);
 // the cluster form; *done = false when it does not apply or no cluster fits the device
 mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
                          bool* done);
+// independent lattices, one cluster each, in one launch (series zeroed and prefixed on the
+// device); fits32: every table has the 32-bit form
+mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, const Table* tabs, const mcx_rng* rngs,
+                               int64_t nsweeps, bool fits32, bool* done);
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);

@@ -310,7 +310,11 @@ def test_autotune_keeps_results(gpu, L, alg):
     (O.ISING, [[16, 16, 16], [8, 8, 12]], "heatbath"),
     (O.BC, [[64, 64], [16, 24], [40, 8]], "heatbath"),
     (O.BC, [[32, 32], [8, 8]], "metropolis"),
-    (O.ISING, [[64, 64], [256, 128]], "glauber"),   # a lattice above the one-block size: one call each
+    (O.ISING, [[64, 64], [256, 128]], "glauber"),   # above the one-block size: one cluster per lattice
+    (O.ISING, [[256, 256], [128, 128], [192, 160]], "metropolis"),
+    (O.BC, [[256, 256], [256, 256]], "heatbath"),
+    (O.ISING, [[32, 32, 32], [64, 64, 16]], "heatbath"),
+    (O.ISING, [[32, 32], [1024, 544]], "metropolis"),  # above the one-cluster size: one call each
     (O.ISING, [[128, 128], [128, 64]], "metropolis"),  # 16-site chunks
     (O.ISING, [[64, 64], [128, 128]], "heatbath"),     # 8-site chunks (the narrower lattice's width)
     (O.BC, [[128, 128], [64, 128]], "metropolis"),
