@@ -404,8 +404,9 @@ def bench_medium(torch, mcx, ctx):
                     "us_per_sweep": ms, "attempts_per_ns": N * 1000 / (ms * 1e6)})
         lat.close()
     # independent 256^2 chains (ParallelChains): one cluster each in one mcx_sweep_batch launch;
-    # eight clusters of 16 CTAs run at once on a GB300 (nine took 1.5x as long as eight)
-    nch = 8
+    # seven clusters of 16 CTAs run side by side on a GB300 (measured: 2.38 us per sweep for
+    # seven chains, 2.88 for eight, where an eighth cluster shares SMs)
+    nch = 7
     chains = [mcx.Ising([256, 256], ctx=ctx) for _ in range(nch)]
     for i, c in enumerate(chains):
         mcx.init_(c, "random", rng=mcx.Philox(SEED, i))

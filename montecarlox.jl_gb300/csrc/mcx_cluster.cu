@@ -248,9 +248,9 @@ void fill_cluster_args(ClusterArgs* ca, mcx_lattice* lat, const Table& t, const 
 }
 
 // Launch configuration of `nclusters` clusters of C CTAs; false when the device cannot
-// place one such cluster.
-mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int nclusters, cudaStream_t st,
-                          cudaLaunchConfig_t* cfg, cudaLaunchAttribute* attr, bool* ok) {
+// place one such cluster (or, with all_at_once, all of them at the same time).
+mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int nclusters, bool all_at_once,
+                          cudaStream_t st, cudaLaunchConfig_t* cfg, cudaLaunchAttribute* attr, bool* ok) {
     if (C > 8) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     if (smem > 48 * 1024) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     *cfg = cudaLaunchConfig_t{};
@@ -265,7 +265,7 @@ mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int n
     cfg->attrs = attr;
     cfg->numAttrs = 1;
     int active = 0;
-    *ok = cudaOccupancyMaxActiveClusters(&active, fn, cfg) == cudaSuccess && active >= 1;
+    *ok = cudaOccupancyMaxActiveClusters(&active, fn, cfg) == cudaSuccess && active >= (all_at_once ? nclusters : 1);
     if (!*ok) (void)cudaGetLastError();
     return MCX_OK;
 }
@@ -293,7 +293,7 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
         cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr[1];
         bool ok = false;
-        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, 1, lat->ctx->stream, &cfg, attr, &ok));
+        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, 1, false, lat->ctx->stream, &cfg, attr, &ok));
         if (!ok) continue;
         MCX_CUDA(cudaLaunchKernelEx(&cfg, fn, ca));
         count_launch(lat->ctx);
@@ -306,7 +306,7 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
 }
 
 mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, const Table* tabs, const mcx_rng* rngs,
-                               int64_t nsweeps, bool fits32, bool* done) {
+                               int64_t nsweeps, bool fits32, bool all_at_once, bool* done) {
     *done = false;
     if (n < 1 || nsweeps < 1) return MCX_OK;
     int cmax = 16;
@@ -337,8 +337,11 @@ mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, con
         cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr[1];
         bool ok = false;
-        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, n, ctx->stream, &cfg, attr, &ok));
-        if (!ok) continue;
+        MCX_CHECK(cluster_config((const void*)fn, C, threads, smem, n, all_at_once, ctx->stream, &cfg, attr, &ok));
+        if (!ok) {
+            if (all_at_once) return MCX_OK;  // the one-block batch form instead
+            continue;
+        }
         std::vector<ClusterArgs> descs(n);
         for (int i = 0; i < n; ++i) fill_cluster_args(&descs[i], lats[i], tabs[i], &rngs[i], nsweeps, 1);
         void* scratch = nullptr;

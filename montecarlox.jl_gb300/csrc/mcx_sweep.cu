@@ -780,21 +780,25 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
         fits32 = fits32 && ising_table_fits32(tabs[i].thr, tabs[i].n, 2 * L->dim, alg == MCX_HEATBATH);
     }
     if (nsweeps == 0) return MCX_OK;
-    if (!small) {
-        // medium lattices: one cluster each in one launch; otherwise one call per lattice
-        // (identical results)
+    if (n == 1)  // the single-lattice forms
+        return mcx_sweep(lats[0], alg, betas[0], &rngs[0], nsweeps, obs_series ? obs_series[0] : nullptr, counters);
+    // One cluster per lattice in one launch: medium lattices always; lattices the one-block
+    // form also takes (above kClusterMin sites) when the device runs every cluster at once
+    // (a few 128^2 chains: 1.5 against 3.6 us per sweep; many chains fill more SMs one block
+    // each).  Otherwise one block per lattice, or one call per lattice (identical results).
+    bool few = true;
+    for (int i = 0; i < n; ++i) few = few && lats[i]->N > kClusterMin;
+    if (!small || few) {
+        for (int i = 0; i < n; ++i) MCX_CHECK(ensure_series(lats[i], nsweeps));
         bool clustered = false;
-        if (n > 1) {
-            for (int i = 0; i < n; ++i) MCX_CHECK(ensure_series(lats[i], nsweeps));
-            MCX_CHECK(cluster_sweep_batch(lats, n, alg, tabs.data(), rngs, nsweeps, fits32, &clustered));
-        }
-        if (!clustered) {
-            for (int i = 0; i < n; ++i)
-                MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
-                                    counters ? &counters[i] : nullptr));
-            return MCX_OK;
-        }
-        return batch_tail(lats, n, rngs, nsweeps, obs_series, counters);
+        MCX_CHECK(cluster_sweep_batch(lats, n, alg, tabs.data(), rngs, nsweeps, fits32, small, &clustered));
+        if (clustered) return batch_tail(lats, n, rngs, nsweeps, obs_series, counters);
+    }
+    if (!small) {
+        for (int i = 0; i < n; ++i)
+            MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
+                                counters ? &counters[i] : nullptr));
+        return MCX_OK;
     }
     std::vector<SmallBatchDesc> descs(n);
     long long maxhalf = 0;

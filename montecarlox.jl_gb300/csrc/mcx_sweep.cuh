@@ -63,9 +63,10 @@ int small_width(int64_t W, long long sites);
 mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
                          bool* done);
 // independent lattices, one cluster each, in one launch (series zeroed and prefixed on the
-// device); fits32: every table has the 32-bit form
+// device); fits32: every table has the 32-bit form; all_at_once: only when the device holds
+// every cluster of the batch at the same time
 mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, const Table* tabs, const mcx_rng* rngs,
-                               int64_t nsweeps, bool fits32, bool* done);
+                               int64_t nsweeps, bool fits32, bool all_at_once, bool* done);
 
 HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);

@@ -315,7 +315,9 @@ def test_autotune_keeps_results(gpu, L, alg):
     (O.BC, [[256, 256], [256, 256]], "heatbath"),
     (O.ISING, [[32, 32, 32], [64, 64, 16]], "heatbath"),
     (O.ISING, [[32, 32], [1024, 544]], "metropolis"),  # above the one-cluster size: one call each
-    (O.ISING, [[128, 128], [128, 64]], "metropolis"),  # 16-site chunks
+    (O.ISING, [[128, 128], [128, 64]], "metropolis"),  # a few chains above 4,096 sites: one cluster each
+    (O.ISING, [[128, 64]] * 20, "metropolis"),         # more chains than clusters at once: 16-site chunks
+    (O.BC, [[96, 96], [128, 128]], "metropolis"),
     (O.ISING, [[64, 64], [128, 128]], "heatbath"),     # 8-site chunks (the narrower lattice's width)
     (O.BC, [[128, 128], [64, 128]], "metropolis"),
     (O.BC, [[64, 64]], "glauber"),                    # 8-site chunks
