@@ -221,6 +221,14 @@ __device__ __forceinline__ void block_add_atomic(long long (&v)[NV], unsigned lo
     __syncthreads();
 }
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later).  pdl_wait blocks
+// until the grid this launch depends on has completed and its memory operations are
+// visible (it returns at once for a launch made without that dependency); pdl_trigger lets
+// the dependent launch be scheduled before this grid ends.  A kernel reads nothing another
+// kernel writes before pdl_wait.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Warp-wide sum of up to 4 values, one atomicAdd per nonzero value per warp, no barrier.
 // The caller guarantees that every per-warp sum fits in int32 (the small-lattice bodies:
 // at most 64 sites per thread and sweep, each changing a count by at most 12).

@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
     __shared__ uint32_t s_t32[NT];
     ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
     __syncthreads();
+    pdl_trigger();
+    pdl_wait();  // the previous half-sweep's colour array is complete
     long long v[4] = {0, 0, 0, 0};
     const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
                        a.Ly, a.Lz);
@@ -110,6 +112,8 @@ __global__ void __launch_bounds__(256) k_ising_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    pdl_trigger();
+    pdl_wait();
     long long v[4] = {0, 0, 0, 0};
     ising_site_body<DIM, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
                              (long long)gridDim.x * blockDim.x, v);
@@ -149,6 +153,8 @@ __global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
     __shared__ __align__(16) unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    pdl_trigger();
+    pdl_wait();
     long long v[4] = {0, 0, 0, 0};
     const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
                        a.Ly, a.Lz);
@@ -210,6 +216,8 @@ __global__ void __launch_bounds__(256) k_bc_cb_site(const SweepArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    pdl_trigger();
+    pdl_wait();
     long long v[4] = {0, 0, 0, 0};
     bc_site_body<DIM, HB>(a, s_thr, blockIdx.x * (long long)blockDim.x + threadIdx.x,
                           (long long)gridDim.x * blockDim.x, v);
@@ -509,7 +517,19 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
     a.acc = lat->d_acc;
     const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
     const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
+    // Each half-sweep node after the first depends programmatically on the one before: its
+    // blocks may be scheduled, and build their tables, while the previous half-sweep drains;
+    // they read the lattice only after pdl_wait.  The key-advancing node depends fully.
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = cs;
+    cfg.attrs = pdl;
     MCX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
     for (int64_t s = 0; s < kGraphChunk; ++s) {
         a.sweep = (uint64_t)s;
         for (int c = 0; c < 2; ++c) {
@@ -517,12 +537,14 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
             a.cur = lat->d_col[c];
             a.oth = lat->d_col[1 - c];
             for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
-            fn<<<grid, 256, 0, cs>>>(a);
+            cfg.numAttrs = (s == 0 && c == 0) ? 0 : 1;
+            if (le == cudaSuccess) le = cudaLaunchKernelEx(&cfg, fn, a);
         }
     }
     k_advance_key<<<1, 1, 0, cs>>>(lat->d_sweep_base, (unsigned long long)kGraphChunk);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = le;
     if (e == cudaSuccess) e = cudaGetLastError();
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
