@@ -85,6 +85,8 @@ __global__ void __launch_bounds__(256) k_msc_cb(const MscArgs a) {
     __shared__ unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
     __syncthreads();
+    pdl_trigger();
+    pdl_wait();  // the previous half-sweep's words are complete
     const long long nwords = (long long)a.nw * a.rows;
     const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
     int nacc = 0, asum = 0, nup = 0;
@@ -159,6 +161,8 @@ __global__ void __launch_bounds__(256, 2) k_msc_metro(const MscArgs a) {
     uint32_t tk[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) tk[k] = (uint32_t)a.thr[Z / 2 + 1 + k];  // < 2^32 for these classes
+    pdl_trigger();
+    pdl_wait();  // the previous half-sweep's words are complete
     const int nwords = a.nw * a.rows;  // < 2^28 words (N <= 2^34 sites)
     const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
     unsigned long long nacc = 0, asum = 0, nup = 0;
@@ -301,6 +305,16 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const 
         fn = lat->dim == 2 ? k_msc_metro<2> : k_msc_metro<3>;
         grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 256, 0);  // one wave
     }
+    // every launch after the first depends programmatically on the one before (the
+    // kernels read the lattice after pdl_wait)
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = ctx->stream;
+    cfg.attrs = pdl;
     for (int64_t s = 0; s < nsweeps; ++s) {
         a.sweep = rng->counter + (uint64_t)s;
         for (int c = 0; c < 2; ++c) {
@@ -309,7 +323,8 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const 
             a.oth = lat->d_msc[1 - c];
             a.dst[0] = (unsigned long long*)(lat->d_series + 3 * s);
             a.dst[1] = (unsigned long long*)(lat->d_series + 3 * s + 1);
-            fn<<<grid, 256, 0, ctx->stream>>>(a);
+            cfg.numAttrs = (s == 0 && c == 0) ? 0 : 1;
+            MCX_CUDA(cudaLaunchKernelEx(&cfg, fn, a));
         }
     }
     count_launch(ctx, 2 * (uint64_t)nsweeps);

@@ -500,6 +500,21 @@ __global__ void k_advance_key(unsigned long long* p, unsigned long long n) {
 // call with the same algorithm and beta, whatever its length or random stream: a call
 // replays it back to back and launches the remainder directly.  (Capturing the whole
 // sequence of a call cost about 10 us per sweep for every new length.)
+// One half-sweep launch; `dependent`: programmatic dependency on the launch before it in
+// the stream (the kernels read the lattice only after pdl_wait).
+static cudaError_t launch_half(HalfSweepFn fn, int grid, cudaStream_t st, const SweepArgs& a, bool dependent) {
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = dependent ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, fn, a);
+}
+
 static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, const Table& t, int V,
                               cudaGraphExec_t* out) {
     for (auto& g : lat->graphs)
@@ -520,14 +535,6 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
     // Each half-sweep node after the first depends programmatically on the one before: its
     // blocks may be scheduled, and build their tables, while the previous half-sweep drains;
     // they read the lattice only after pdl_wait.  The key-advancing node depends fully.
-    cudaLaunchAttribute pdl[1];
-    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    pdl[0].val.programmaticStreamSerializationAllowed = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(256);
-    cfg.stream = cs;
-    cfg.attrs = pdl;
     MCX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = cudaSuccess;
     for (int64_t s = 0; s < kGraphChunk; ++s) {
@@ -537,8 +544,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
             a.cur = lat->d_col[c];
             a.oth = lat->d_col[1 - c];
             for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
-            cfg.numAttrs = (s == 0 && c == 0) ? 0 : 1;
-            if (le == cudaSuccess) le = cudaLaunchKernelEx(&cfg, fn, a);
+            if (le == cudaSuccess) le = launch_half(fn, grid, cs, a, s > 0 || c > 0);
         }
     }
     k_advance_key<<<1, 1, 0, cs>>>(lat->d_sweep_base, (unsigned long long)kGraphChunk);
@@ -635,7 +641,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
                     a.cur = lat->d_col[c];
                     a.oth = lat->d_col[1 - c];
                     for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
-                    fn<<<grid, 256, 0, ctx->stream>>>(a);
+                    MCX_CUDA(launch_half(fn, grid, ctx->stream, a, s > 0 || c > 0));
                 }
             }
             count_launch(ctx, 2 * (uint64_t)rem);
@@ -655,7 +661,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
                 a.cur = lat->d_col[c];
                 a.oth = lat->d_col[1 - c];
                 for (int j = 0; j < 3; ++j) a.dst[j] = (unsigned long long*)(lat->d_series + 3 * s + j);
-                fn<<<grid, 256, 0, ctx->stream>>>(a);
+                MCX_CUDA(launch_half(fn, grid, ctx->stream, a, s > 0 || c > 0));
             }
         }
         count_launch(ctx, 2 * (uint64_t)nsweeps);
