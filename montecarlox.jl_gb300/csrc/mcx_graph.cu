@@ -405,6 +405,8 @@ template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
 __global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_graph_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
                                                              uint32_t stream, unsigned long long sweep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_trigger();
+    pdl_wait();  // the previous class (or sweep) is complete
     float eh = 0.0f, el = 0.0f;
     long long dM = 0;
     long long nacc = 0;
@@ -823,6 +825,8 @@ template <int ALG, bool TABLE, bool EDGEJ, int FIELD>
 __global__ void __launch_bounds__(kGraphBlock, TABLE ? 5 : 4) k_bcg_class(GraphDev g, GClass c, uint32_t k0, uint32_t k1,
                                                            uint32_t stream, unsigned long long sweep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_trigger();
+    pdl_wait();  // the previous class (or sweep) is complete
     float eh = 0.0f, el = 0.0f;
     long long dM = 0, nacc = 0;
     bc_class_pairs<ALG, TABLE, EDGEJ, FIELD>(g, g.spins, c, (long long)blockIdx.x * kSlicesPerBlock + warp,
@@ -925,6 +929,8 @@ __global__ void k_bcg_site(GraphDev g, long long p, int sn, int op, double* out)
 // E += Σ partials (fixed order); record the series entry of sweep t.
 __global__ void __launch_bounds__(kGraphBlock) k_graph_finish(double* part, int nparts, double* E, const long long* M,
                                                               double* Eser, long long* Mser, long long t) {
+    pdl_trigger();
+    pdl_wait();  // every class of the sweep is complete
     double v = 0.0;
     for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += part[i];
     const double s = block_sum_f64(v);
@@ -1769,15 +1775,30 @@ MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta,
         MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fns.cls, kGraphBlock, 0));
         bps = std::max(1, std::min(bps, 8));
         MCX_CUDA(cudaMemsetAsync(g->d_part, 0, sizeof(double) * (size_t)g->nparts, st));
+        // every launch after the first depends programmatically on the one before: the
+        // kernels read nothing before pdl_wait, which waits for the previous grid (and so,
+        // one grid at a time, for every earlier one)
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.blockDim = dim3(kGraphBlock);
+        cfg.stream = st;
+        cfg.attrs = pdl;
         for (int64_t t = 0; t < nsweeps; ++t) {
             const unsigned long long sweep = rng->counter + (unsigned long long)t;
-            for (const GClass& c : g->classes) {
+            for (size_t ci = 0; ci < g->classes.size(); ++ci) {
+                const GClass& c = g->classes[ci];
                 const int grid = (int)std::min<long long>((c.nslices + 2 * kSlicesPerBlock - 1) / (2 * kSlicesPerBlock),
                                                           (long long)ctx->num_sms * bps);
-                fns.cls<<<std::max(grid, 1), kGraphBlock, 0, st>>>(d, c, k0, k1, rng->stream, sweep);
+                cfg.gridDim = dim3((unsigned)std::max(grid, 1));
+                cfg.numAttrs = (t == 0 && ci == 0) ? 0 : 1;
+                MCX_CUDA(cudaLaunchKernelEx(&cfg, fns.cls, d, c, k0, k1, rng->stream, sweep));
             }
-            k_graph_finish<<<1, kGraphBlock, 0, st>>>(g->d_part, g->nparts, g->d_E, g->d_M, g->d_Eser,
-                                                      g->d_Mser, t);
+            cfg.gridDim = dim3(1);
+            cfg.numAttrs = 1;
+            MCX_CUDA(cudaLaunchKernelEx(&cfg, k_graph_finish, g->d_part, g->nparts, g->d_E, (const long long*)g->d_M,
+                                        g->d_Eser, g->d_Mser, (long long)t));
             count_launch(ctx, (uint64_t)g->classes.size() + 1);
         }
     }
