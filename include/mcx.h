@@ -284,6 +284,19 @@ MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls);
 /* Failure-detection check: a bounded wait on a device flag that nothing sets;
  * returns MCX_ERR_TIMEOUT after `polls` polls, with the context still usable. */
 MCX_API mcx_status mcx_wait_flag_test(mcx_ctx* ctx, int64_t polls);
+/* One exchange stage of one ladder of n replicas, on the host, for a ladder whose
+ * replicas are swept by several processes (replaces update!(rx, xs) / update!(rx, x),
+ * src/algorithms/replica_exchange.jl:158-178 and :227-243, with attempt_exchange_pair!
+ * :124-136).  betas by ladder position; pair_sum / spin_sum / pos by replica (pos a
+ * permutation of 0..n-1, updated in place); *stage 0 tries pairs (0,1), (2,3), ... and 1
+ * tries (1,2), (3,4), ..., then flips; steps / accepted by lower position of each edge
+ * (n - 1 entries, incremented).  The uniforms are those of the device exchange step for
+ * (seed, ladder, sweep), so the positions equal a single-device mcx_pt_run on the same
+ * ladder.  Needs no GPU. */
+MCX_API mcx_status mcx_ladder_exchange(int32_t n, const double* betas, const int64_t* pair_sum,
+                                       const int64_t* spin_sum, double J, double h, int32_t* pos,
+                                       int32_t* stage, uint64_t seed, int32_t ladder, uint64_t sweep,
+                                       uint64_t* steps, uint64_t* accepted);
 
 /* ----------------------------------------------------------------- serving -- */
 /* Continuous batching of simulation jobs (no counterpart in the reference, whose

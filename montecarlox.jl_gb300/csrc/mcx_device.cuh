@@ -34,8 +34,9 @@ constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
 constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
 constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
 
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
-__device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11); also on the host, where the
+// exchange decisions of a ladder spread over processes are taken.
+__host__ __device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
         if (r) {
@@ -51,7 +52,7 @@ __device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
 }
 
 // word 2 of a checkerboard counter
-__device__ __forceinline__ uint32_t ctr_word2(unsigned long long sweep, int colour,
+__host__ __device__ __forceinline__ uint32_t ctr_word2(unsigned long long sweep, int colour,
                                               uint32_t purpose) {
     return ((uint32_t)(sweep >> 32) & 0xFFFFu) | ((uint32_t)colour << 16) | (purpose << 24);
 }
@@ -60,7 +61,7 @@ __device__ __forceinline__ uint32_t pick4(uint4 w, int lane) {
     return lane == 0 ? w.x : lane == 1 ? w.y : lane == 2 ? w.z : w.w;
 }
 
-__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
+__host__ __device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
     unsigned long long k = ((unsigned long long)hi << 21) | (unsigned long long)(lo >> 11);
     return (double)k * 1.1102230246251565404236316680908203125e-16;  // 2^-53
 }

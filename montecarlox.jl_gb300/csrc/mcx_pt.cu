@@ -1111,4 +1111,49 @@ MCX_API mcx_status mcx_pt_tau_int(mcx_pt* pt, int quantity, int64_t min_points, 
     return launch_tau_int(pt->ctx, srcs, nullptr, 0, c, taus);
 }
 
+// One exchange stage of one ladder on the host, for a ladder whose replicas are swept by
+// several processes (replica_exchange.jl:110-136 pair rule and acceptance, :158-178 stage
+// order; :227-243 is the reference's MPI form, one replica per rank).  The uniforms are the
+// ones the device exchange step draws (Philox counter (position, sweep, sweep>>32 |
+// exchange purpose, ladder) under the ladder's seed), and the arithmetic is the device's
+// in the same order, so every process taking this step with the same inputs reaches the
+// same positions as k_pt_persistent.
+MCX_API mcx_status mcx_ladder_exchange(int32_t n, const double* betas, const int64_t* pair_sum,
+                                       const int64_t* spin_sum, double J, double h, int32_t* pos, int32_t* stage,
+                                       uint64_t seed, int32_t ladder, uint64_t sweep, uint64_t* steps,
+                                       uint64_t* accepted) {
+    if (!betas || !pair_sum || !spin_sum || !pos || !stage || !steps || !accepted)
+        return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (n < 2) return fail(MCX_ERR_INVALID_ARG, "a ladder needs at least 2 replicas");
+    if (ladder < 0) return fail(MCX_ERR_INVALID_ARG, "ladder < 0");
+    std::vector<int> rep(n, -1);
+    for (int r = 0; r < n; ++r) {
+        if (pos[r] < 0 || pos[r] >= n || rep[pos[r]] != -1)
+            return fail(MCX_ERR_INVALID_ARG, "positions are not a permutation of 0..%d", n - 1);
+        rep[pos[r]] = r;
+    }
+    for (int p = 0; p < n; ++p)
+        if (!std::isfinite(betas[p])) return fail(MCX_ERR_INVALID_ARG, "beta %d must be finite", p);
+    const int first = (*stage & 1) ? 1 : 0;
+    for (int p = first; p + 1 < n; p += 2) {
+        const int ri = rep[p], rj = rep[p + 1];
+        const uint4 w = philox10(make_uint4((uint32_t)p, (uint32_t)sweep, ctr_word2(sweep, 0, P_EXCHANGE),
+                                            (uint32_t)ladder),
+                                 (uint32_t)seed, (uint32_t)(seed >> 32));
+        const double lu = mcx_log(u53(w.x, w.y));
+        const double bi = betas[p], bj = betas[p + 1];
+        const double xi = (-(J * (double)pair_sum[ri])) - (h * (double)spin_sum[ri]);
+        const double xj = (-(J * (double)pair_sum[rj])) - (h * (double)spin_sum[rj]);
+        const double lr = (((-bi) * xj) - ((-bi) * xi)) + (((-bj) * xi) - ((-bj) * xj));
+        steps[p] += 1;
+        if ((lr > 0.0) || (lu < lr)) {
+            accepted[p] += 1;
+            pos[ri] = p + 1;
+            pos[rj] = p;
+        }
+    }
+    *stage = (*stage & 1) ^ 1;
+    return MCX_OK;
+}
+
 }  // extern "C"

@@ -134,6 +134,8 @@ SIGNATURES = {
     "mcx_graph_tau_int": (C.c_int, [_P, C.c_int, C.c_int64, C.c_double, _f64p]),
     "mcx_pt_set_record": (C.c_int, [_P, C.c_int32]),
     "mcx_pt_tau_int": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int64, C.c_double, _P]),
+    "mcx_ladder_exchange": (C.c_int, [C.c_int32, _P, _P, _P, C.c_double, C.c_double, _P, _i32p, C.c_uint64,
+                                      C.c_int32, C.c_uint64, _P, _P]),
 }
 
 PT_PERSISTENT, PT_PLAIN = 0, 1

@@ -81,6 +81,32 @@ def test_pt_runs_compose(gpu):
         assert np.array_equal(a.spins(r), b.spins(r))
 
 
+@pytest.mark.parametrize("alg,every", [("metropolis", 1), ("heatbath", 3)])
+def test_distributed_ladder_matches_device_pt(gpu, alg, every):
+    """Ladder 1 of a two-ladder ParallelTempering rerun by DistributedLadder in one process
+    (device lattices swept by sweep_batch_, the exchange stage on the host through
+    mcx_ladder_exchange): series, positions, stage, counters and spins are the kernel's."""
+    from mcx.parallel import DistributedLadder
+    from mcx.pt import ParallelTempering
+    seed, n = 41, 11
+    lad = [(8, [0.3, 0.25]), (16, [0.26, 0.25, 0.24, 0.235, 0.23, 0.22])]
+    pt = ParallelTempering(lad, dim=3, seed=seed)
+    pt.init_(seed)
+    series = pt.sweep_(n, alg=alg, exchange_every=every, record=True)
+    dl = DistributedLadder(16, lad[1][1], dim=3, seed=seed, ladder=1, stream0=2)
+    dl.init_(seed)
+    ds = np.concatenate([dl.sweep_(4, alg=alg, exchange_every=every, record=True),
+                         dl.sweep_(n - 4, alg=alg, exchange_every=every, record=True)])
+    assert np.array_equal(ds, series[:, 2:])
+    assert np.array_equal(dl.positions, pt.positions[2:])
+    assert dl.stage == pt.stage
+    s, a = pt.counters()
+    assert np.array_equal(dl.steps, s[1:]) and np.array_equal(dl.accepted, a[1:])
+    for r in range(6):
+        assert np.array_equal(dl.spins(r), pt.spins(2 + r)), r
+    dl.close()
+
+
 def test_bounded_wait_reports_timeout(gpu):
     """A device wait on a flag nothing sets gives up and reports, context intact."""
     ctx = gpu.default_context()
