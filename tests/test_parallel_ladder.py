@@ -84,7 +84,7 @@ def _run(P, c, backend, out_dir=None):
     s2 = lad.sweep_(c["nsweeps"] - 4, alg=c["alg"], exchange_every=c["every"], record=True)
     res = {"series": np.concatenate([s1, s2]), "pos": lad.positions, "stage": np.array([lad.stage]),
            "steps": lad.steps, "acc": lad.accepted, "obs": lad.observables(),
-           "spins": np.concatenate([lad.spins(r) for r in lad.local_replicas()])}
+           "spins": np.concatenate([lad.spins(r) for r in lad.local_replicas()] + [np.zeros(0, np.int8)])}
     if out_dir is not None:
         for k, v in res.items():
             np.save(os.path.join(out_dir, "%s%d.npy" % (k, rank)), v)
@@ -96,7 +96,7 @@ def _bounds(n, backend):
     return n * rank // size, n * (rank + 1) // size
 
 
-def _rank_main(rank, world, port, out_dir):
+def _rank_main(rank, world, port, out_dir, case=None):
     import sys
     for p in (os.path.dirname(HERE), os.path.join(os.path.dirname(HERE), "montecarlox.jl_gb300")):
         if p not in sys.path:
@@ -104,7 +104,7 @@ def _rank_main(rank, world, port, out_dir):
     import torch.distributed as dist
     dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
     from mcx import parallel as P
-    _run(P, CASE, P.DistributedBackend(), out_dir)
+    _run(P, case or CASE, P.DistributedBackend(), out_dir)
     dist.barrier()
     dist.destroy_process_group()
 
@@ -116,7 +116,7 @@ def _check_against_oracle(res, spins_ref, series, pos, stage, steps, acc, r0=0, 
     assert np.array_equal(res["steps"], steps) and np.array_equal(res["acc"], acc)
     assert np.array_equal(res["obs"], series[-1])
     r1 = len(spins_ref) if r1 is None else r1
-    assert np.array_equal(res["spins"], np.concatenate(spins_ref[r0:r1]))
+    assert np.array_equal(res["spins"], np.concatenate(list(spins_ref[r0:r1]) + [np.zeros(0, np.int8)]))
 
 
 def test_ladder_exchange_matches_oracle_exchange(mcxlib):
@@ -180,3 +180,31 @@ def test_ladder_two_ranks(tmp_path):
         res = {k: np.load(tmp_path / ("%s%d.npy" % (k, rank))) for k in
                ("series", "pos", "stage", "steps", "acc", "obs", "spins")}
         _check_against_oracle(res, *ref, r0=n * rank // 2, r1=n * (rank + 1) // 2)
+
+
+@pytest.mark.parametrize("betas", [[0.30, 0.27, 0.245, 0.22, 0.2], [0.4, 0.2]])
+def test_ladder_three_ranks(tmp_path, betas):
+    """Uneven shares over three ranks (1 + 2 + 2 replicas, and 0 + 1 + 1 for a two-replica
+    ladder): the same result on every rank as the oracle's single-process ladder."""
+    mp = pytest.importorskip("torch.multiprocessing")
+    c = dict(CASE, betas=betas)
+    ref = oracle_ladder(c["L"], c["dim"], c["betas"], c["seed"], c["nsweeps"], c["every"], c["alg"])
+    mp.spawn(_rank_main, args=(3, _free_port(), str(tmp_path), c), nprocs=3, join=True)
+    n = len(betas)
+    for rank in range(3):
+        res = {k: np.load(tmp_path / ("%s%d.npy" % (k, rank))) for k in
+               ("series", "pos", "stage", "steps", "acc", "obs", "spins")}
+        _check_against_oracle(res, *ref, r0=n * rank // 3, r1=n * (rank + 1) // 3)  # rank 0 of 3 may hold none
+
+
+def test_ladder_argument_errors(mcxlib):
+    from mcx import parallel as P
+    with pytest.raises(mcxlib.ArgumentError):
+        P.DistributedLadder(4, [0.3], sweeper=OracleSweeper(4, 3, 0, 1))
+    lad = P.DistributedLadder(4, [0.3, 0.2], sweeper=OracleSweeper(4, 3, 0, 2))
+    with pytest.raises(mcxlib.ArgumentError):
+        lad.sweep_(2, exchange_every=0)
+    with pytest.raises(mcxlib.ArgumentError):
+        lad.sweep_(2, alg="wolff")
+    with pytest.raises(mcxlib.ArgumentError):
+        lad.spins(5)
