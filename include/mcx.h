@@ -194,6 +194,15 @@ MCX_API mcx_status mcx_flathist_set_histogram(mcx_flathist* fh, const int64_t* h
 MCX_API mcx_status mcx_flathist_get_histogram(mcx_flathist* fh, int64_t* host, int64_t n);
 /* reset!(::Multicanonical) histogram part (src/algorithms/multicanonical.jl:27-33): H := 0. */
 MCX_API mcx_status mcx_flathist_reset(mcx_flathist* fh);
+/* Reweighting on the device from the ensemble's log density of states ln g = -logweight
+ * (replaces distribution_from_logdos / log_sum, src/infrastructure/utils.jl:54-105, and the
+ * energy moments of the reweighted distribution): for each betas[k] (nbeta in 1..65535),
+ * over the bins whose w_b = ln g_b - beta E_b is finite (E_b the bin centres),
+ * logz[k] = log sum exp(w_b), mean_e[k] = <E>, mean_e2[k] = <E^2>.  dist (may be NULL;
+ * dist_len = nbins) receives exp(w_b - logz[0]) at betas[0], 0 on bins that are not finite.
+ * FP64 throughout, deterministic; MCX_ERR_INVALID_ARG when no bin is finite. */
+MCX_API mcx_status mcx_flathist_reweight(mcx_flathist* fh, const double* betas, int32_t nbeta, double* logz,
+                                         double* mean_e, double* mean_e2, double* dist, int64_t dist_len);
 /* update!(::MulticanonicalEnsemble; mode=:simple) (multicanonical.jl:32-43):
  * ln g[b] -= log(H[b]) where H[b] > 0. */
 MCX_API mcx_status mcx_flathist_update_muca(mcx_flathist* fh);

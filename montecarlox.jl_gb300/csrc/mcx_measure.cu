@@ -17,6 +17,8 @@
 #include <cmath>
 #include <vector>
 
+#include "mcx_device.cuh"
+#include "mcx_flathist.cuh"
 #include "mcx_internal.h"
 
 using namespace mcx;
@@ -126,6 +128,105 @@ __global__ void __launch_bounds__(kTauBlock) k_tau_int(const TraceSrc* __restric
     if (threadIdx.x == 0) taus[blockIdx.x] = tau > 0.5 ? tau : 0.5;
 }
 
+// ---------------------------------------------------------------- reweighting --
+// Canonical moments from a log density of states (distribution_from_logdos,
+// src/infrastructure/utils.jl:95-105): for each beta, over the bins whose log weight
+// w_b = ln g_b - beta E_b is finite, the log-sum-exp state (m, sum exp(w - m) (1, E, E^2)).
+// A thread folds its bins in order (rescaling the sums when the maximum grows), a block
+// merges its threads in a fixed tree, and one thread per beta merges the blocks in order,
+// so results are deterministic; exp and log are mcx_exp / mcx_log.
+constexpr int kRwBlock = 256;
+
+struct Lse {
+    double m, s0, s1, s2;
+};
+
+__device__ __forceinline__ void lse_add(Lse& a, double w, double E) {
+    if (w > a.m) {
+        const double f = mcx_exp(a.m - w);  // 0 while the state is empty (m = -inf)
+        a.s0 = a.s0 * f;
+        a.s1 = a.s1 * f;
+        a.s2 = a.s2 * f;
+        a.m = w;
+    }
+    const double e = mcx_exp(w - a.m);
+    a.s0 = a.s0 + e;
+    a.s1 = a.s1 + e * E;
+    a.s2 = a.s2 + (e * E) * E;
+}
+
+__device__ __forceinline__ Lse lse_merge(Lse a, Lse b) {
+    if (b.m > a.m) {
+        const Lse t = a;
+        a = b;
+        b = t;
+    }
+    if (b.s0 == 0.0) return a;  // b is empty
+    const double f = mcx_exp(b.m - a.m);
+    a.s0 = a.s0 + b.s0 * f;
+    a.s1 = a.s1 + b.s1 * f;
+    a.s2 = a.s2 + b.s2 * f;
+    return a;
+}
+
+__device__ __forceinline__ Lse lse_shfl(const Lse& a, int o) {
+    return Lse{__shfl_down_sync(0xFFFFFFFFu, a.m, o), __shfl_down_sync(0xFFFFFFFFu, a.s0, o),
+               __shfl_down_sync(0xFFFFFFFFu, a.s1, o), __shfl_down_sync(0xFFFFFFFFu, a.s2, o)};
+}
+
+// grid (blocks over the bins, betas): block x folds bins [x*per, (x+1)*per) at betas[y]
+__global__ void __launch_bounds__(kRwBlock) k_reweight_partial(const double* __restrict__ lnw, long long nbins,
+                                                               long long start, long long step,
+                                                               const double* __restrict__ betas,
+                                                               Lse* __restrict__ part) {
+    __shared__ Lse red[kRwBlock / 32];
+    const double beta = betas[blockIdx.y];
+    const long long per = (nbins + gridDim.x - 1) / gridDim.x;
+    const long long b0 = (long long)blockIdx.x * per;
+    const long long b1 = b0 + per < nbins ? b0 + per : nbins;
+    Lse a{-HUGE_VAL, 0.0, 0.0, 0.0};
+    for (long long b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+        const double E = (double)(start + step * b);
+        const double w = (-lnw[b]) - beta * E;  // ln g = -logweight
+        if (isfinite(w)) lse_add(a, w, E);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = lse_merge(a, lse_shfl(a, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Lse t = red[0];
+        for (int w = 1; w < kRwBlock / 32; ++w) t = lse_merge(t, red[w]);
+        part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// one thread per beta: the blocks in order, then (log Z, <E>, <E^2>); log Z is NaN when
+// no bin was finite
+__global__ void k_reweight_finish(const Lse* __restrict__ part, int nblk, int nbeta, double* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nbeta) return;
+    Lse t = part[(size_t)k * nblk];
+    for (int x = 1; x < nblk; ++x) t = lse_merge(t, part[(size_t)k * nblk + x]);
+    const bool any = t.s0 > 0.0;
+    out[3 * k] = any ? t.m + mcx_log(t.s0) : __longlong_as_double(0x7FF8000000000000ll);
+    out[3 * k + 1] = any ? t.s1 / t.s0 : 0.0;
+    out[3 * k + 2] = any ? t.s2 / t.s0 : 0.0;
+}
+
+// the distribution at one beta: exp(w_b - log Z) on finite bins, 0 elsewhere
+__global__ void k_reweight_dist(const double* __restrict__ lnw, long long nbins, long long start, long long step,
+                                const double* __restrict__ beta, const double* __restrict__ logz,
+                                double* __restrict__ dist) {
+    const double bt = *beta, lz = *logz;
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nbins;
+         b += (long long)gridDim.x * blockDim.x) {
+        const double w = (-lnw[b]) - bt * (double)(start + step * b);
+        dist[b] = isfinite(w) ? mcx_exp(w - lz) : 0.0;
+    }
+}
+
 }  // namespace
 
 namespace mcx {
@@ -228,6 +329,57 @@ MCX_API mcx_status mcx_lattice_tau_int(mcx_lattice* lat, int quantity, int64_t m
     }
     tau_window(s, n, 2, max_lag);
     return launch_tau_int(lat->ctx, srcs, nullptr, 0, c, tau);
+}
+
+MCX_API mcx_status mcx_flathist_reweight(mcx_flathist* fh, const double* betas, int32_t nbeta, double* logz,
+                                         double* mean_e, double* mean_e2, double* dist, int64_t dist_len) {
+    if (!fh || !betas || !logz || !mean_e || !mean_e2) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (nbeta < 1 || nbeta > 65535) return fail(MCX_ERR_INVALID_ARG, "nbeta must be in 1..65535");
+    if (dist && dist_len != fh->nbins)
+        return fail(MCX_ERR_INVALID_ARG, "the distribution needs %lld entries", (long long)fh->nbins);
+    for (int k = 0; k < nbeta; ++k)
+        if (!std::isfinite(betas[k])) return fail(MCX_ERR_INVALID_ARG, "beta %d must be finite", k);
+    mcx_ctx* ctx = fh->ctx;
+    const long long nbins = fh->nbins;
+    // about 8 blocks per SM over all betas, at least 4 * kRwBlock bins per block
+    const long long by_bins = (nbins + 4 * kRwBlock - 1) / (4 * kRwBlock);
+    const long long by_grid = std::max<long long>(1, 8LL * std::max(ctx->num_sms, 1) / nbeta);
+    const int nblk = (int)std::max<long long>(1, std::min(by_bins, by_grid));
+    auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const size_t b_beta = up16(sizeof(double) * nbeta), b_out = up16(sizeof(double) * 3 * nbeta);
+    const size_t b_part = up16(sizeof(Lse) * (size_t)nbeta * nblk);
+    const size_t b_dist = dist ? sizeof(double) * (size_t)nbins : 0;
+    // scratch: betas | (log Z, <E>, <E^2>) per beta | block partials | the distribution
+    void* scratch = nullptr;
+    MCX_CHECK(ctx_scratch(ctx, b_beta + b_out + b_part + b_dist, &scratch));
+    char* base = static_cast<char*>(scratch);
+    double* d_beta = reinterpret_cast<double*>(base);
+    double* d_out = reinterpret_cast<double*>(base + b_beta);
+    Lse* d_part = reinterpret_cast<Lse*>(base + b_beta + b_out);
+    double* d_dist = reinterpret_cast<double*>(base + b_beta + b_out + b_part);
+    cudaStream_t st = ctx->stream;
+    MCX_CUDA(cudaMemcpyAsync(d_beta, betas, sizeof(double) * nbeta, cudaMemcpyHostToDevice, st));
+    k_reweight_partial<<<dim3((unsigned)nblk, (unsigned)nbeta), kRwBlock, 0, st>>>(fh->d_lnw, nbins, fh->start,
+                                                                                  fh->step, d_beta, d_part);
+    k_reweight_finish<<<(nbeta + 127) / 128, 128, 0, st>>>(d_part, nblk, nbeta, d_out);
+    count_launch(ctx, 2);
+    if (dist) {
+        const unsigned grid = (unsigned)std::min<long long>((nbins + 255) / 256, 8LL * std::max(ctx->num_sms, 1));
+        k_reweight_dist<<<grid, 256, 0, st>>>(fh->d_lnw, nbins, fh->start, fh->step, d_beta, d_out, d_dist);
+        count_launch(ctx);
+    }
+    MCX_CUDA(cudaGetLastError());
+    std::vector<double> out(3 * (size_t)nbeta);
+    MCX_CUDA(cudaMemcpyAsync(out.data(), d_out, sizeof(double) * 3 * nbeta, cudaMemcpyDeviceToHost, st));
+    if (dist) MCX_CUDA(cudaMemcpyAsync(dist, d_dist, b_dist, cudaMemcpyDeviceToHost, st));
+    MCX_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < nbeta; ++k) {
+        if (std::isnan(out[3 * k])) return fail(MCX_ERR_INVALID_ARG, "the log density of states has no finite entry");
+        logz[k] = out[3 * k];
+        mean_e[k] = out[3 * k + 1];
+        mean_e2[k] = out[3 * k + 2];
+    }
+    return MCX_OK;
 }
 
 }  // extern "C"

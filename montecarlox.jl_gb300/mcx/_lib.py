@@ -80,6 +80,7 @@ SIGNATURES = {
     "mcx_flathist_set_histogram": (C.c_int, [_P, _P, C.c_int64]),
     "mcx_flathist_get_histogram": (C.c_int, [_P, _P, C.c_int64]),
     "mcx_flathist_reset": (C.c_int, [_P]),
+    "mcx_flathist_reweight": (C.c_int, [_P, _P, C.c_int32, _P, _P, _P, _P, C.c_int64]),
     "mcx_flathist_update_muca": (C.c_int, [_P]),
     "mcx_flathist_flatness": (C.c_int, [_P, C.c_double, C.POINTER(C.c_int), _f64p]),
     "mcx_flathist_merge": (C.c_int, [_P, C.POINTER(_P), C.c_int]),

@@ -85,6 +85,19 @@ class _FlatEnsemble:
     def reset_histogram(self):
         _check(L.load().mcx_flathist_reset(self.handle))
 
+    def reweight(self, betas, distribution=False):
+        """Canonical averages from the log density of states ln g = -logweight, on the
+        device (distribution_from_logdos, src/infrastructure/utils.jl:95-105): returns
+        (log Z, <E>, <E^2>) per beta, and with ``distribution`` also the normalised
+        distribution over the bins at betas[0]."""
+        b = np.ascontiguousarray(np.atleast_1d(betas), np.float64)
+        lz, e1, e2 = (np.empty(b.size, np.float64) for _ in range(3))
+        dist = np.empty(self.bins.nbins, np.float64) if distribution else None
+        _check(L.load().mcx_flathist_reweight(self.handle, b.ctypes.data, b.size, lz.ctypes.data, e1.ctypes.data,
+                                              e2.ctypes.data, dist.ctypes.data if distribution else None,
+                                              self.bins.nbins if distribution else 0))
+        return (lz, e1, e2, dist) if distribution else (lz, e1, e2)
+
     def close(self):
         if getattr(self, "handle", None):
             L.load().mcx_flathist_destroy(self.handle)

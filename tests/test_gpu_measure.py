@@ -110,3 +110,77 @@ def test_exchange_interval_reference_case(gpu):
     Mx.optimize_exchange_interval_(2, samples, sweeps, base_sweeps=10, min_sweeps=2, max_sweeps=50, min_points=2,
                                    max_lag=2)
     assert all(2 <= v <= 50 for v in sweeps) and sweeps[1] >= sweeps[0]
+
+
+# ---- reweighting from a log density of states on the device (utils.jl:54-105) ----
+
+def _reweight_ref(lng, centers, beta):
+    """FP64 numpy: log Z, <E>, <E^2> and the distribution over the finite bins."""
+    w = lng - beta * centers
+    m = np.isfinite(w)
+    lz = np.logaddexp.reduce(w[m])
+    p = np.zeros_like(w)
+    p[m] = np.exp(w[m] - lz)
+    return lz, float((p * centers).sum()), float((p * centers * centers).sum()), p
+
+
+def test_reweight_exact_ising_8x8(gpu):
+    """The exact 8x8 Ising density of states (Beale 1996, the reference's ising2d_exact
+    data) reweighted on the device: log Z, <E>, <E^2> and the distribution at several
+    betas against FP64 numpy, and the distribution against distribution_from_logdos."""
+    import json
+    import os
+    from mcx import analysis as A
+    from mcx import flathist as F
+    d = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ising2d_8x8_logdos.json")))
+    ens = F.MulticanonicalEnsemble((-128, 4, 65))
+    lng = np.full(65, -np.inf)
+    for E, g in d["energy_logdos"]:
+        lng[(E + 128) // 4] = g
+    ens.logweight = -lng  # ln g = -logweight; impossible energies are +inf weights
+    centers = ens.bins.centers().astype(np.float64)
+    betas = [0.1, 0.3, 0.4406868, 0.6, 1.0]
+    lz, e1, e2, dist = ens.reweight(betas, distribution=True)
+    for k, b in enumerate(betas):
+        rlz, re1, re2, rp = _reweight_ref(lng, centers, b)
+        assert abs(lz[k] - rlz) <= 1e-12 * abs(rlz) + 1e-12
+        assert abs(e1[k] - re1) <= 1e-11 * abs(re1)
+        assert abs(e2[k] - re2) <= 1e-11 * abs(re2)
+        if k == 0:
+            np.testing.assert_allclose(dist, rp, rtol=1e-11, atol=1e-300)
+            np.testing.assert_allclose(dist, A.distribution_from_logdos(centers, lng, b), rtol=1e-11, atol=1e-300)
+    assert abs(np.log(np.exp(lng[np.isfinite(lng)]).sum()) - np.log(2.0) * 64) < 1e-9  # sum g = 2^64
+
+
+@pytest.mark.parametrize("nbins,step,nbeta", [(4 * 1024 * 1024 + 1, 1, 3), (100003, 4, 300)])
+def test_reweight_many_bins(gpu, nbins, step, nbeta):
+    """A smooth log density of states over millions of bins (the Blume-Capel L=1024 range)
+    and a scan of many betas: every block and both grid dimensions in use."""
+    from mcx import flathist as F
+    start = -nbins // 2 * step
+    ens = F.MulticanonicalEnsemble((start, step, nbins))
+    x = np.linspace(-1.0, 1.0, nbins)
+    lng = nbins * 0.5 * (1.0 - x * x) + np.sin(37.0 * x)
+    lng[::97] = -np.inf  # some impossible energies
+    ens.logweight = -lng
+    centers = ens.bins.centers().astype(np.float64)
+    betas = np.linspace(-0.5, 0.5, nbeta)
+    lz, e1, e2 = ens.reweight(betas)
+    for k in range(0, nbeta, max(1, nbeta // 7)):
+        rlz, re1, re2, _ = _reweight_ref(lng, centers, betas[k])
+        assert abs(lz[k] - rlz) <= 1e-12 * abs(rlz), k
+        assert abs(e1[k] - re1) <= 1e-10 * np.sqrt(re2), k  # sums of E p cancel: scale by rms E
+        assert abs(e2[k] - re2) <= 1e-9 * abs(re2), k
+
+
+def test_reweight_errors(gpu):
+    from mcx import flathist as F
+    ens = F.MulticanonicalEnsemble((0, 1, 8))
+    ens.logweight = np.full(8, np.inf)  # no finite bin
+    with pytest.raises(gpu.ArgumentError):
+        ens.reweight([0.5])
+    ens.logweight = np.zeros(8)
+    with pytest.raises(gpu.ArgumentError):
+        ens.reweight([np.nan])
+    lz, e1, e2 = ens.reweight([0.0])
+    assert abs(lz[0] - np.log(8.0)) < 1e-14 and abs(e1[0] - 3.5) < 1e-14
