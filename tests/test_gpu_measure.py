@@ -115,13 +115,17 @@ def test_exchange_interval_reference_case(gpu):
 # ---- reweighting from a log density of states on the device (utils.jl:54-105) ----
 
 def _reweight_ref(lng, centers, beta):
-    """FP64 numpy: log Z, <E>, <E^2> and the distribution over the finite bins."""
+    """FP64 numpy: log Z, <E>, <E^2> and the distribution over the finite bins, from
+    weights shifted by their maximum and pairwise sums (a sequential logaddexp over
+    millions of bins drifts by ~1e-8 and would scale every probability by that)."""
     w = lng - beta * centers
     m = np.isfinite(w)
-    lz = np.logaddexp.reduce(w[m])
-    p = np.zeros_like(w)
-    p[m] = np.exp(w[m] - lz)
-    return lz, float((p * centers).sum()), float((p * centers * centers).sum()), p
+    wmax = w[m].max()
+    q = np.zeros_like(w)
+    q[m] = np.exp(w[m] - wmax)
+    z = q.sum()
+    p = q / z
+    return wmax + np.log(z), float((q * centers).sum() / z), float((q * centers * centers).sum() / z), p
 
 
 def test_reweight_exact_ising_8x8(gpu):
