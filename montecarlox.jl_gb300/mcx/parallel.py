@@ -153,6 +153,8 @@ class DistributedLadder:
     ParallelTempering run of the same ladder (ladder index `ladder`, its replicas from global
     replica index `stream0` on, same seed).
 
+    sweep_, observables and energies are collective: every rank of the group calls them.
+
     backend: a DistributedBackend (None: one process holds the whole ladder).
     sweeper: what sweeps this rank's replicas (default: device lattices on the current
     context); it provides init(seed), spins(i), set_spins(i, v), observables() and
