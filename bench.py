@@ -427,6 +427,28 @@ def bench_medium(torch, mcx, ctx):
     return {"kernel": "k_lattice_cluster (one cluster of up to 16 CTAs per lattice, one launch per call)", "lines": res}
 
 
+def bench_reweight(torch, mcx, ctx):
+    """Reweighting from a Multicanonical ln g on the device: the Blume-Capel L=1024 energy
+    range (4N + 1 = 4,194,305 bins of width 1, a smooth synthetic ln g), log Z, <E> and
+    <E^2> at 100 betas in one call (synchronous; wall time around it)."""
+    import numpy as np
+    from mcx import flathist as F
+    N = 1024 * 1024
+    nb = 4 * N + 1
+    ens = F.MulticanonicalEnsemble((-N, 1, nb), ctx=ctx)
+    x = np.linspace(-1.0, 1.0, nb)
+    ens.logweight = -(N * np.log(3.0) * (1.0 - x * x))
+    betas = np.linspace(0.3, 0.7, 100)
+    ens.reweight(betas[:4])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.reweight(betas)
+    dt = time.perf_counter() - t0
+    ens.close()
+    return {"workload": "reweight_bc_L1024_4194305_bins_100_betas", "ms_per_call": dt * 1e3,
+            "bin_betas_per_ns": nb * len(betas) / (dt * 1e9), "kernel": "k_reweight_partial (FP64, mcx_exp)"}
+
+
 def torus_csr(L, seed, per_entry):
     """CSR of the L x L periodic grid (first coordinate fastest, sorted rows) and, when
     per_entry, symmetric Gaussian couplings: the 2-D Edwards-Anderson spin glass."""
@@ -616,10 +638,11 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = None
     if not args.no_extras:
         small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
         med_res = bench_medium(torch, mcx, ctx)
+        rw_res = bench_reweight(torch, mcx, ctx)
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
@@ -659,6 +682,7 @@ def run_mcx(args):
         "general_graphs": graph_res,
         "small_lattice": small_res,
         "medium_lattice": med_res,
+        "reweighting": rw_res,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
