@@ -208,3 +208,22 @@ def test_ladder_argument_errors(mcxlib):
         lad.sweep_(2, alg="wolff")
     with pytest.raises(mcxlib.ArgumentError):
         lad.spins(5)
+
+
+def test_ladder_without_record_matches(mcxlib):
+    """Runs that keep no series (only the last sweep before each exchange is gathered)
+    reach the same state as recorded runs, for several exchange intervals."""
+    from mcx import parallel as P
+    c = CASE
+    for every in (1, 3):
+        ref = oracle_ladder(c["L"], c["dim"], c["betas"], c["seed"], 10, every, "heatbath")
+        lad = P.DistributedLadder(c["L"], c["betas"], dim=c["dim"], seed=c["seed"],
+                                  sweeper=OracleSweeper(c["L"], c["dim"], 0, len(c["betas"])))
+        lad.init_(c["seed"])
+        assert lad.sweep_(7, alg="heatbath", exchange_every=every) is None
+        lad.sweep_(3, alg="heatbath", exchange_every=every)
+        assert np.array_equal(lad.positions, ref[2]) and lad.stage == ref[3]
+        assert np.array_equal(lad.steps, ref[4]) and np.array_equal(lad.accepted, ref[5])
+        assert np.array_equal(lad.observables(), ref[1][-1])
+        for r in range(len(c["betas"])):
+            assert np.array_equal(lad.spins(r), ref[0][r])
