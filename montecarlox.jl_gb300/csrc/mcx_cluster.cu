@@ -247,12 +247,8 @@ void fill_cluster_args(ClusterArgs* ca, mcx_lattice* lat, const Table& t, const 
     ca->zero = zero;
 }
 
-// Launch configuration of `nclusters` clusters of C CTAs; false when the device cannot
-// place one such cluster (or, with all_at_once, all of them at the same time).
-mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int nclusters, bool all_at_once,
-                          cudaStream_t st, cudaLaunchConfig_t* cfg, cudaLaunchAttribute* attr, bool* ok) {
-    if (C > 8) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    if (smem > 48 * 1024) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+void make_cluster_cfg(int C, int threads, size_t smem, int nclusters, cudaStream_t st, cudaLaunchConfig_t* cfg,
+                      cudaLaunchAttribute* attr) {
     *cfg = cudaLaunchConfig_t{};
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)C;
@@ -264,6 +260,15 @@ mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int n
     cfg->stream = st;
     cfg->attrs = attr;
     cfg->numAttrs = 1;
+}
+
+// Launch configuration of `nclusters` clusters of C CTAs; false when the device cannot
+// place one such cluster (or, with all_at_once, all of them at the same time).
+mcx_status cluster_config(const void* fn, int C, int threads, size_t smem, int nclusters, bool all_at_once,
+                          cudaStream_t st, cudaLaunchConfig_t* cfg, cudaLaunchAttribute* attr, bool* ok) {
+    if (C > 8) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    if (smem > 48 * 1024) MCX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    make_cluster_cfg(C, threads, smem, nclusters, st, cfg, attr);
     int active = 0;
     *ok = cudaOccupancyMaxActiveClusters(&active, fn, cfg) == cudaSuccess && active >= (all_at_once ? nclusters : 1);
     if (!*ok) (void)cudaGetLastError();
@@ -281,6 +286,16 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
     const long long unitB = (long long)cut_rows(lat) * lat->W;
     ClusterArgs ca;
     fill_cluster_args(&ca, lat, t, rng, nsweeps, 0);
+    const int key = (hb ? 2 : 0) | (t32 ? 1 : 0);
+    if (lat->cluster_size > 0 && lat->cluster_key == key) {  // the plan of the previous call
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr[1];
+        make_cluster_cfg(lat->cluster_size, lat->cluster_threads, lat->cluster_smem, 1, lat->ctx->stream, &cfg, attr);
+        MCX_CUDA(cudaLaunchKernelEx(&cfg, reinterpret_cast<ClusterFn>(const_cast<void*>(lat->cluster_fn)), ca));
+        count_launch(lat->ctx);
+        *done = true;
+        return MCX_OK;
+    }
     // the largest cluster (<= 16 CTAs, one unit each at least) whose CTAs hold at most
     // 16384 sites of a colour and that the device can place
     for (int C = std::min(16, cut_units(lat)); C >= 2; --C) {
@@ -298,6 +313,10 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
         MCX_CUDA(cudaLaunchKernelEx(&cfg, fn, ca));
         count_launch(lat->ctx);
         lat->cluster_size = C;
+        lat->cluster_key = key;
+        lat->cluster_fn = (const void*)fn;
+        lat->cluster_threads = threads;
+        lat->cluster_smem = smem;
         *done = true;
         return MCX_OK;
     }

@@ -120,6 +120,13 @@ struct mcx_lattice {
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
     int cluster_size = 0;          // CTAs of the last cluster-form call (0: not tried, -1: none fits)
+    // that call's kernel, block size and shared memory, reused while its key (heat bath,
+    // 32-bit table) is the same, so later calls skip the occupancy query (about 1 us of the
+    // ~32 us a one-sweep call through the Python mirror costs on a GB300 host)
+    int cluster_key = -1;
+    const void* cluster_fn = nullptr;
+    int cluster_threads = 0;
+    size_t cluster_smem = 0;
     unsigned long long* d_sweep_base = nullptr;  // {first sweep, seed, stream, series offset} read by captured graphs
     struct Graph {
         int alg;
