@@ -17,6 +17,18 @@ so L2 is flushed (256 MiB write) between timed steps.
   cpu_baseline  the oracle's sequential random-site mode (the reference's
              spin_flip! order, FP64 exp decisions), one chain per host core
 
+Further lines in the same JSON object (skipped with --no-extras), each timed on its own:
+  small_lattice     the L=64 configuration (10^3 + 10^4 sweeps, one block) and one such
+                    chain per SM in one batched call
+  medium_lattice    256^2 / 128^2 / 32^3 / Blume-Capel 256^2 in one thread-block cluster,
+                    and seven 256^2 chains in one batched call
+  reweighting       log Z, <E>, <E^2> at 100 betas from a 4,194,305-bin ln g on the device
+  batched_pt        256 3-D replicas in five ladders: persistent kernel against the plain form
+  serving           40 Poisson jobs through the continuous-batching server (p50 / p99)
+  flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block
+  msc64             the headline workload on the 64-spins-per-word layout
+  general_graphs    4096^2 torus as IsingMatrix (Gaussian couplings) and as IsingGraph
+
 `--impl reference` times that CPU path alone on every host core.
 """
 import argparse
