@@ -3,38 +3,9 @@ import numpy as np
 import pytest
 
 import oracle as O
+from oracle_runs import oracle_pt
 
 pytestmark = pytest.mark.gpu
-
-ALG = {"metropolis": O.METROPOLIS, "glauber": O.GLAUBER, "heatbath": O.HEATBATH}
-
-
-def oracle_pt(ladders, dim, alg, seed, nsweeps, every, J=1.0, h=0.0):
-    reps = [(L, l, k) for l, (L, b) in enumerate(ladders) for k in range(len(b))]
-    spins = [O.init_random(O.ISING, [L] * dim, seed, r) for r, (L, l, k) in enumerate(reps)]
-    pos = [np.arange(len(b), dtype=np.int32) for _, b in ladders]
-    steps = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
-    acc = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
-    stage = 0
-    series = np.zeros((nsweeps, len(reps), 2), np.int64)
-    for t in range(nsweeps):
-        for r, (L, l, k) in enumerate(reps):
-            beta = ladders[l][1][pos[l][k]]
-            O.cb_sweep(spins[r], O.ISING, [L] * dim, ALG[alg], beta, seed, stream=r, sweep0=t, nsweeps=1, J=J, h=h,
-                       record=False)
-            P, M, _ = O.observables(spins[r], [L] * dim)
-            series[t, r] = (P, M)
-        if (t + 1) % every == 0:
-            new_stage = stage
-            first = 0
-            for l, (L, b) in enumerate(ladders):
-                idx = [r for r, rr in enumerate(reps) if rr[1] == l]
-                x = np.array([(-(J * float(series[t, r, 0]))) - (h * float(series[t, r, 1])) for r in idx])
-                new_stage = O.pt_exchange(np.array(b), pos[l], stage, x, seed, l, t, steps[l], acc[l])
-            stage = new_stage
-    positions = np.concatenate(pos)
-    return spins, series, positions, stage, np.concatenate(steps), np.concatenate(acc)
-
 
 CASES = [
     (3, [(8, [0.25, 0.235, 0.22]), (16, [0.25, 0.24, 0.23, 0.2])], "metropolis", 7, 1),
