@@ -174,6 +174,20 @@ MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, double beta
 MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx_algorithm alg,
                                    const double* betas, mcx_rng* rngs, int64_t nsweeps,
                                    int64_t** obs_series, mcx_counters* counters);
+/* `nattempts` x spin_flip!(sys, alg) in the reference's own order: each attempt picks a
+ * uniformly random site (pick_site, SpinSystems/src/abstractions.jl:19) and decides with the
+ * reference's FP64 rule (Ising: SpinSystems/src/ising.jl:25-58; Blume-Capel:
+ * SpinSystems/src/blume_capel.jl:41-85; accept!: src/algorithms/importance_sampling.jl:80-85,
+ * src/algorithms/metropolis.jl:121-127), the probabilities computed on the host with the C
+ * library's exp.  Attempt a = rng->counter + k draws Philox4x32-10(seed, (a lo, a hi, 5<<24,
+ * stream)): site ((w0<<32)|w1) mod N, U = u53(w2, w3); Blume-Capel Metropolis / Glauber
+ * proposals take the top bit of word 0 of (a lo, a hi, 6<<24, stream).  rng->counter advances
+ * by nattempts.  Serial by nature (one thread applies the attempts in order): a single-site
+ * call for code written around spin_flip!, not a substitute for mcx_sweep.  Updates the cached
+ * bookkeeping; counters (accumulated; HeatBath: accepted = spins that changed) may be NULL,
+ * in which case the call only enqueues work. */
+MCX_API mcx_status mcx_spin_flip(mcx_lattice* lat, mcx_algorithm alg, double beta, mcx_rng* rng,
+                                 int64_t nattempts, mcx_counters* counters);
 /* Copy the per-sweep series of the last mcx_sweep call (first n sweeps). */
 MCX_API mcx_status mcx_read_series(mcx_lattice* lat, int64_t* obs_series, int64_t n);
 
@@ -443,6 +457,18 @@ MCX_API mcx_status mcx_graph_set_site(mcx_graph* g, int64_t i, int8_t s_new);
 MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng,
                                    int64_t nsweeps, double* E_series, int64_t* M_series,
                                    mcx_counters* counters);
+
+/* `nattempts` x spin_flip!(sys, alg) in the reference's own order on a general graph: a
+ * uniformly random vertex per attempt (pick_site, SpinSystems/src/abstractions.jl:19) and the
+ * site's FP64 rule of mcx_graph_sweep (Ising: ising.jl:25-58; Blume-Capel:
+ * SpinSystems/src/blume_capel.jl:41-85).  Attempt a = rng->counter + k draws
+ * Philox4x32-10(seed, (a lo, a hi, 5<<24, stream)): vertex ((w0<<32)|w1) mod n, u = u53(w2, w3);
+ * Blume-Capel Metropolis / Glauber proposals take the top bit of word 0 of (a lo, a hi, 6<<24,
+ * stream).  rng->counter advances by nattempts.  Serial (one thread applies the attempts in
+ * order); the cached energy is the sequential FP64 sum of the accepted changes.  counters may
+ * be NULL (the call then only enqueues work). */
+MCX_API mcx_status mcx_graph_spin_flip(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng,
+                                       int64_t nattempts, mcx_counters* counters);
 
 /* ---------------------------------------------------------- measurements -- */
 /* integrated_autocorrelation_times(traces; min_points, max_lag, c)

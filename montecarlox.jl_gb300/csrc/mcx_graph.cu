@@ -926,6 +926,102 @@ __global__ void k_bcg_site(GraphDev g, long long p, int sn, int op, double* out)
     }
 }
 
+// spin_flip!(sys, alg) at uniformly random sites, one attempt after another (the reference's
+// own order: pick_site, SpinSystems/src/abstractions.jl:19, then the site's FP64 rule, the
+// exact path of the sweeps).  Attempt a draws Philox(seed, (a lo, a hi, 5<<24, stream)):
+// vertex ((w0<<32)|w1) mod n, u = u53(w2, w3); a Blume-Capel Metropolis / Glauber proposal is
+// the top bit of word 0 of (a lo, a hi, 6<<24, stream).  Lanes draw 32 attempts at a time,
+// lane 0 applies them in order and keeps E as a sequential FP64 sum.
+template <bool EDGEJ, int FIELD, bool BC>
+__global__ void k_graph_seq(GraphDev g, const int32_t* __restrict__ perm, long long n, int alg, uint32_t k0,
+                            uint32_t k1, uint32_t stream, unsigned long long a0, long long nat,
+                            unsigned long long* counts) {
+    __shared__ long long s_p[32];
+    __shared__ unsigned long long s_k[32];
+    __shared__ uint32_t s_b[32];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    double E = *g.E;
+    long long M = *g.M;
+    unsigned long long acc = 0;
+    for (long long base = 0; base < nat; base += 32) {
+        const long long m = nat - base < 32 ? nat - base : 32;
+        if (lane < m) {
+            const unsigned long long a = a0 + (unsigned long long)(base + lane);
+            const uint4 w = philox10(make_uint4((uint32_t)a, (uint32_t)(a >> 32), 5u << 24, stream), k0, k1);
+            const long long v = (long long)((((unsigned long long)w.x << 32) | w.y) % (unsigned long long)n);
+            s_p[lane] = perm[v];
+            s_k[lane] = ((unsigned long long)w.z << 21) | (unsigned long long)(w.w >> 11);
+            s_b[lane] = BC && alg != MCX_HEATBATH
+                            ? philox10(make_uint4((uint32_t)a, (uint32_t)(a >> 32), 6u << 24, stream), k0, k1).x >> 31
+                            : 0u;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            for (int j = 0; j < (int)m; ++j) {
+                const long long p = s_p[j];
+                const long long sl = p >> 5;
+                const int ln = (int)(p & 31);
+                const long long off = g.soff[sl];
+                const int w = (int)((g.soff[sl + 1] - off) >> 5);
+                const int so = g.spins[p];
+                int isum = 0;
+                if (!EDGEJ)
+                    for (int k = 0; k < w; ++k) {
+                        const int nb = g.nbr[off + 32ll * k + ln];
+                        if (nb >= 0) isum += g.spins[nb];
+                    }
+                double dE = 0.0;
+                int sn = so;
+                if (BC) {
+                    if (alg == MCX_METROPOLIS)
+                        sn = bc_exact_site<MCX_METROPOLIS, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, isum, s_k[j],
+                                                                         s_b[j], &dE);
+                    else if (alg == MCX_GLAUBER)
+                        sn = bc_exact_site<MCX_GLAUBER, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, isum, s_k[j],
+                                                                      s_b[j], &dE);
+                    else
+                        sn = bc_exact_site<MCX_HEATBATH, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, isum, s_k[j],
+                                                                       s_b[j], &dE);
+                } else {
+                    bool flip;
+                    if (alg == MCX_METROPOLIS)
+                        flip = exact_site<MCX_METROPOLIS, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, so * isum,
+                                                                        s_k[j], &dE);
+                    else if (alg == MCX_GLAUBER)
+                        flip = exact_site<MCX_GLAUBER, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, so * isum, s_k[j],
+                                                                     &dE);
+                    else
+                        flip = exact_site<MCX_HEATBATH, EDGEJ, FIELD>(g, g.spins, p, off, w, ln, so, so * isum,
+                                                                      s_k[j], &dE);
+                    if (flip) sn = -so;
+                }
+                if (sn != so) {
+                    g.spins[p] = (int8_t)sn;
+                    E = E + dE;
+                    M += sn - so;
+                    ++acc;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        *g.E = E;
+        *g.M = M;
+        counts[0] = (unsigned long long)nat;
+        counts[1] = acc;
+    }
+}
+
+template <bool EDGEJ, bool BC>
+cudaError_t seq_launch(int field, cudaStream_t st, void** args) {
+    const void* fn = field == F_VECTOR    ? reinterpret_cast<const void*>(&k_graph_seq<EDGEJ, F_VECTOR, BC>)
+                     : field == F_UNIFORM ? reinterpret_cast<const void*>(&k_graph_seq<EDGEJ, F_UNIFORM, BC>)
+                                          : reinterpret_cast<const void*>(&k_graph_seq<EDGEJ, F_NONE, BC>);
+    return cudaLaunchKernel(fn, dim3(1), dim3(32), args, 0, st);
+}
+
 // E += Σ partials (fixed order); record the series entry of sweep t.
 __global__ void __launch_bounds__(kGraphBlock) k_graph_finish(double* part, int nparts, double* E, const long long* M,
                                                               double* Eser, long long* Mser, long long t) {
@@ -1737,6 +1833,41 @@ MCX_API mcx_status mcx_graph_set_site(mcx_graph* g, int64_t i, int8_t s_new) {
     if (s_new < -1 || s_new > 1 || (!g->bc && s_new == 0))
         return fail(MCX_ERR_INVALID_ARG, "%d is not a spin state of this model", (int)s_new);
     return graph_site(g, i, s_new, 1, nullptr);
+}
+
+MCX_API mcx_status mcx_graph_spin_flip(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng, int64_t nattempts,
+                                       mcx_counters* counters) {
+    if (!g || !rng) return fail(MCX_ERR_INVALID_ARG, "NULL argument");
+    if (alg < MCX_METROPOLIS || alg > MCX_HEATBATH) return fail(MCX_ERR_INVALID_ARG, "unknown algorithm %d", (int)alg);
+    if (nattempts < 0) return fail(MCX_ERR_INVALID_ARG, "nattempts < 0");
+    if (!std::isfinite(beta)) return fail(MCX_ERR_INVALID_ARG, "beta must be finite");
+    if (nattempts == 0) return MCX_OK;
+    mcx_ctx* ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    void* scratch = nullptr;  // (attempts, accepted) of this call
+    MCX_CHECK(ctx_scratch(ctx, 2 * sizeof(unsigned long long), &scratch));
+    GraphDev d = g->dev(beta);
+    const int32_t* perm = g->d_perm;
+    long long n = g->n, nat = nattempts;
+    int ialg = (int)alg;
+    uint32_t k0 = (uint32_t)rng->seed, k1 = (uint32_t)(rng->seed >> 32), sid = rng->stream;
+    unsigned long long a0 = rng->counter;
+    unsigned long long* counts = static_cast<unsigned long long*>(scratch);
+    void* args[] = {&d, &perm, &n, &ialg, &k0, &k1, &sid, &a0, &nat, &counts};
+    cudaError_t e;
+    if (g->edgej) e = g->bc ? seq_launch<true, true>(g->field, st, args) : seq_launch<true, false>(g->field, st, args);
+    else e = g->bc ? seq_launch<false, true>(g->field, st, args) : seq_launch<false, false>(g->field, st, args);
+    count_launch(ctx);
+    MCX_CUDA(e);
+    rng->counter += (uint64_t)nattempts;
+    if (counters) {
+        unsigned long long h[2];
+        MCX_CUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
+        MCX_CUDA(cudaStreamSynchronize(st));
+        counters->attempts += h[0];
+        counters->accepted += h[1];
+    }
+    return MCX_OK;
 }
 
 MCX_API mcx_status mcx_graph_sweep(mcx_graph* g, mcx_algorithm alg, double beta, mcx_rng* rng, int64_t nsweeps,

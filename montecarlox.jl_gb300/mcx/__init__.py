@@ -526,6 +526,21 @@ def autotune_(sys, alg):
     return v.value, ns.value
 
 
-def spin_flip_(sys, alg):
-    """Single random-site updates are not run on the device; use sweep_ (checkerboard)."""
-    raise NotImplementedError("spin_flip_ on a device lattice: use sweep_(sys, alg, n)")
+def spin_flip_(sys, alg, n=1):
+    """spin_flip!(sys, alg) (SpinSystems/src/ising.jl:25-58, blume_capel.jl:41-85), ``n``
+    times: single-site updates at uniformly random sites in the reference's own order and
+    with its FP64 decisions, run on the device one after another.  Advances ``alg.rng`` by
+    ``n`` and the algorithm's counters like ``sweep_``.  A loop written around spin_flip!
+    runs unchanged; ``sweep_`` is the fast path."""
+    if _is_graph(sys):
+        from . import graph as G
+        return G.spin_flip(sys, alg, n)
+    rng = alg.rng._c()
+    cnt = L.mcx_counters(0, 0)
+    _check(L.load().mcx_spin_flip(sys.handle, alg.ALG, float(alg.beta), C.byref(rng), int(n), C.byref(cnt)))
+    alg.rng.counter = rng.counter
+    alg.steps += cnt.attempts
+    if isinstance(alg, HeatBath):
+        alg.flips += cnt.accepted
+    else:
+        alg.accepted += cnt.accepted

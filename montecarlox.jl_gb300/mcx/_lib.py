@@ -70,6 +70,9 @@ SIGNATURES = {
     "mcx_sweep": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P,
                             C.POINTER(mcx_counters)]),
     "mcx_read_series": (C.c_int, [_P, _P, C.c_int64]),
+    "mcx_spin_flip": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, C.POINTER(mcx_counters)]),
+    "mcx_graph_spin_flip": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64,
+                                      C.POINTER(mcx_counters)]),
     "mcx_sweep_batch": (C.c_int, [C.POINTER(_P), C.c_int32, C.c_int, _f64p, C.POINTER(mcx_rng), C.c_int64,
                                   C.POINTER(C.c_void_p), C.POINTER(mcx_counters)]),
     "mcx_autotune": (C.c_int, [_P, C.c_int, C.c_double, _i32p, _f64p]),

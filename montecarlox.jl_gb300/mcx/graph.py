@@ -276,6 +276,20 @@ def modify_(sys, i, s_new=None):
     return sys
 
 
+def spin_flip(sys, alg, n=1):
+    """n x spin_flip!(sys, alg) at uniformly random vertices, in order, with the reference's
+    FP64 rule (mcx_graph_spin_flip); advances alg.rng and the counters like sweep."""
+    rng = alg.rng._c()
+    cnt = L.mcx_counters(0, 0)
+    _check(L.load().mcx_graph_spin_flip(sys.handle, alg.ALG, float(alg.beta), C.byref(rng), int(n), C.byref(cnt)))
+    alg.rng.counter = rng.counter
+    alg.steps += cnt.attempts
+    if isinstance(alg, HeatBath):
+        alg.flips += cnt.accepted
+    else:
+        alg.accepted += cnt.accepted
+
+
 def sweep(sys, alg, nsweeps=1, record=False):
     beta = alg.beta
     rng = alg.rng._c()

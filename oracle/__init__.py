@@ -36,6 +36,8 @@ def lib():
         L.orc_site_word.restype = C.c_uint32
         L.orc_log.argtypes = [C.c_double]
         L.orc_log.restype = C.c_double
+        L.orc_log_array.argtypes = [f64p, f64p, C.c_int64]
+        L.orc_log_array.restype = None
         L.orc_table_ising.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, u64p, u32p]
         L.orc_table_bc.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, u64p]
         L.orc_init_random.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_uint64, C.c_uint32]
@@ -53,6 +55,10 @@ def lib():
                                          C.c_int, f64p, i64p, C.c_int64, C.c_int64, C.c_int64, C.c_double,
                                          C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64, C.c_void_p,
                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_flathist_trace.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_double, C.c_double, C.c_double,
+                                         C.c_int, f64p, i64p, C.c_int64, C.c_int64, C.c_int64, C.c_double,
+                                         C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64, f64p, f64p, C.c_int64,
+                                         C.POINTER(C.c_int64)]
         L.orc_muca_update.argtypes = [f64p, i64p, C.c_int64]
         L.orc_muca_update.restype = None
         L.orc_wl_flat.argtypes = [i64p, u8p, C.c_int64, C.c_double, C.POINTER(C.c_double)]
@@ -89,6 +95,10 @@ def lib():
                                     C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
                                     C.POINTER(C.c_double), C.POINTER(C.c_int64), vp, vp, C.POINTER(C.c_uint64),
                                     C.POINTER(C.c_uint64)]
+        L.orc_graph_seq_attempts.argtypes = [i8p, C.c_int64, i64p, i32p, vp, C.c_double, vp, C.c_double, C.c_int,
+                                             C.c_double, C.c_int, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64,
+                                             C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                             C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.orc_tau_int.argtypes = [f64p, C.c_int64, C.c_int64, C.c_double]
         L.orc_tau_int.restype = C.c_double
         _lib = L
@@ -112,6 +122,14 @@ def site_word(seed, stream, sweep, colour, purpose, site):
 
 def log(x):
     return float(lib().orc_log(float(x)))
+
+
+def log_array(x):
+    """The project log (the one the device uses) of every element."""
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.empty_like(x)
+    lib().orc_log_array(x, y, x.size)
+    return y
 
 
 def table_ising(dim, alg, beta, J=1.0, h=0.0):
@@ -178,6 +196,20 @@ def flathist_sweep(s, model, L, mode, lnw, H, start, step, logf, seed, stream=0,
                                   seed, stream, sweep0, nsweeps, obs.ctypes.data if record else None,
                                   C.byref(st), C.byref(ac))
     return rc, obs, st.value, ac.value
+
+
+def flathist_trace(s, model, L, mode, lnw, H, start, step, logf, seed, stream=0, sweep0=0, nsweeps=1,
+                   J=1.0, D=0.0, h=0.0):
+    """flathist_sweep that also returns the (U, lr) of every decision in order:
+    (rc, U[n], lr[n])."""
+    dim, Lv = _dims(L)
+    cap = int(np.prod(L)) * nsweeps
+    u = np.zeros(cap, np.float64)
+    lr = np.zeros(cap, np.float64)
+    n = C.c_int64(0)
+    rc = lib().orc_flathist_trace(s, model, dim, Lv, J, D, h, mode, lnw, H, start, step, len(lnw), logf, seed,
+                                  stream, sweep0, nsweeps, u, lr, cap, C.byref(n))
+    return rc, u[:n.value], lr[:n.value]
 
 
 def muca_update(lnw, H):
@@ -308,6 +340,23 @@ def graph_sweep(g, s, alg, beta, seed, stream=0, sweep0=0, nsweeps=1):
     if rc != OK:
         raise ValueError("oracle graph_sweep failed: %d" % rc)
     return Es, Ms, att.value, acc.value
+
+
+def graph_seq_attempts(g, s, alg, beta, seed, stream=0, attempt0=0, nattempts=1):
+    """nattempts random-site spin flips in place on ``s`` (Ising or, for a BCGraph,
+    Blume-Capel rules); returns (E, M, attempts, accepts), E and M tracked from a full
+    recompute before the first attempt."""
+    jv, hv = g._ptrs()
+    bc = isinstance(g, BCGraph)
+    E0, M0 = bcg_observables(g, s) if bc else graph_observables(g, s)
+    E, M = C.c_double(E0), C.c_int64(M0)
+    att, acc = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().orc_graph_seq_attempts(s, g.n, g.rowptr, g.col, jv, g.J, hv, g.h, int(bc), g.D if bc else 0.0, alg,
+                                      beta, seed, stream, attempt0, nattempts, C.byref(E), C.byref(M), C.byref(att),
+                                      C.byref(acc))
+    if rc != OK:
+        raise ValueError("oracle graph_seq_attempts failed: %d" % rc)
+    return E.value, M.value, att.value, acc.value
 
 
 def tau_int(x, max_lag=None, c=5.0):

@@ -111,6 +111,10 @@ double orc_log(double x) {
     return kd * ln2_hi + (lm + kd * ln2_lo);
 }
 
+void orc_log_array(const double* x, double* y, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) y[i] = orc_log(x[i]);
+}
+
 /* logistic, src/infrastructure/utils.jl:82-88 */
 static double logistic(double x) {
     if (x >= 0) return 1.0 / (1.0 + exp(-x));
@@ -454,11 +458,12 @@ static int bin_of(int64_t E, int64_t start, int64_t step, int64_t nbins, int64_t
     return 1;
 }
 
-int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
-                       double h, int mode, double* lnw, int64_t* H, int64_t start,
-                       int64_t step, int64_t nbins, double logf, uint64_t seed,
-                       uint32_t stream, uint64_t sweep0, int64_t nsweeps, int64_t* obs,
-                       uint64_t* steps, uint64_t* accepted) {
+static int flathist_run(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
+                        double h, int mode, double* lnw, int64_t* H, int64_t start,
+                        int64_t step, int64_t nbins, double logf, uint64_t seed,
+                        uint32_t stream, uint64_t sweep0, int64_t nsweeps, int64_t* obs,
+                        uint64_t* steps, uint64_t* accepted, double* tr_u, double* tr_lr,
+                        int64_t tr_cap, int64_t* tr_n) {
     geom_t g;
     if (geom_init(&g, dim, L)) return ORC_ERR_INVALID;
     if (step <= 0 || nbins <= 0) return ORC_ERR_INVALID;
@@ -489,6 +494,11 @@ int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J
                 double U = u53(orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i),
                                orc_site_word(seed, stream, t, c, P_LOW, (uint64_t)i));
                 int acc = (lr > 0) || (orc_log(U) < lr);
+                if (tr_n && *tr_n < tr_cap) {
+                    tr_u[*tr_n] = U;
+                    tr_lr[*tr_n] = lr;
+                    ++*tr_n;
+                }
                 ++st;
                 if (acc) {
                     ++ac;
@@ -506,6 +516,27 @@ int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J
     if (steps) *steps += st;
     if (accepted) *accepted += ac;
     return rc;
+}
+
+int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
+                       double h, int mode, double* lnw, int64_t* H, int64_t start,
+                       int64_t step, int64_t nbins, double logf, uint64_t seed,
+                       uint32_t stream, uint64_t sweep0, int64_t nsweeps, int64_t* obs,
+                       uint64_t* steps, uint64_t* accepted) {
+    return flathist_run(s, model, dim, L, J, D, h, mode, lnw, H, start, step, nbins, logf, seed, stream,
+                        sweep0, nsweeps, obs, steps, accepted, NULL, NULL, 0, NULL);
+}
+
+/* The same sweeps, also recording the (U, lr) of every decision, in order (up to tr_cap). */
+int orc_flathist_trace(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
+                       double h, int mode, double* lnw, int64_t* H, int64_t start,
+                       int64_t step, int64_t nbins, double logf, uint64_t seed,
+                       uint32_t stream, uint64_t sweep0, int64_t nsweeps, double* tr_u,
+                       double* tr_lr, int64_t tr_cap, int64_t* tr_n) {
+    uint64_t st = 0, ac = 0;
+    *tr_n = 0;
+    return flathist_run(s, model, dim, L, J, D, h, mode, lnw, H, start, step, nbins, logf, seed, stream,
+                        sweep0, nsweeps, NULL, &st, &ac, tr_u, tr_lr, tr_cap, tr_n);
 }
 
 /* update!(::MulticanonicalEnsemble; mode=:simple), src/ensembles/multicanonical.jl:32-43 */
@@ -1046,5 +1077,72 @@ int orc_bcg_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* co
     free(block);
     free(order);
     free(colour);
+    return ORC_OK;
+}
+
+/* The reference's own order on a general graph: nattempts x spin_flip!(sys, alg) at a
+ * uniformly random vertex (pick_site, SpinSystems/src/abstractions.jl:19) with the site
+ * rules of orc_graph_sweep / orc_bcg_sweep.  Attempt a draws Philox(seed, (a lo, a hi,
+ * P_SEQ<<24, stream)): vertex ((w0<<32)|w1) mod n, u = u53(w2, w3); a Blume-Capel
+ * Metropolis / Glauber proposal is the top bit of word 0 of (a lo, a hi, P_SEQ2<<24,
+ * stream).  bc selects the Blume-Capel rules (crystal field D).  E and M are the cached
+ * observables, updated after each accepted move. */
+int orc_graph_seq_attempts(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                           const double* Jv, double J, const double* hv, double h, int bc, double D,
+                           int alg, double beta, uint64_t seed, uint32_t stream, uint64_t attempt0,
+                           int64_t nattempts, double* E, int64_t* M, uint64_t* attempts,
+                           uint64_t* accepts) {
+    if (alg < ORC_METROPOLIS || alg > ORC_HEATBATH || n < 1) return ORC_ERR_INVALID;
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint64_t acc_n = 0;
+    for (int64_t k = 0; k < nattempts; ++k) {
+        uint64_t a = attempt0 + (uint64_t)k;
+        uint32_t ctr[4] = {(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)P_SEQ << 24, stream}, w[4];
+        orc_philox4x32_10(ctr, key, w);
+        int64_t v = (int64_t)((((uint64_t)w[0] << 32) | w[1]) % (uint64_t)n);
+        double u = u53(w[2], w[3]);
+        int so = s[v], sn = so;
+        double dE = 0.0;
+        if (!bc) {
+            dE = graph_delta_energy(s, v, rowptr, col, Jv, J, hv, h);
+            int flip;
+            if (alg == ORC_METROPOLIS) {
+                double lr = -beta * dE;
+                flip = (lr > 0) || (u < orc_exp(lr));
+            } else if (alg == ORC_GLAUBER) {
+                flip = u < orc_logistic(-beta * dE);
+            } else {
+                int up = u < orc_logistic((beta * (double)so) * dE);
+                flip = up != (so == 1);
+            }
+            if (flip) sn = -so;
+        } else if (alg == ORC_HEATBATH) {
+            double c = bcg_coupling(s, v, rowptr, col, Jv, J);
+            double hf = (hv || h != 0.0) ? bcg_field(v, hv, h) : 0.0;
+            double e1 = (c - hf * (-1.0)) + D;
+            double e3 = (-c - hf) + D;
+            double w1 = orc_exp(-beta * e1), w2 = orc_exp(-beta * 0.0), w3 = orc_exp(-beta * e3);
+            double z = (w1 + w2) + w3;
+            double r = u * z;
+            sn = r < w1 ? -1 : (r < w1 + w2 ? 0 : 1);
+            if (sn != so) dE = orc_bcg_delta_energy(s, v, sn, rowptr, col, Jv, J, D, hv, h);
+        } else {
+            uint32_t c2[4] = {(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)P_SEQ2 << 24, stream}, w2[4];
+            orc_philox4x32_10(c2, key, w2);
+            int prop = bc_propose(so, (int)(w2[0] >> 31));
+            dE = orc_bcg_delta_energy(s, v, prop, rowptr, col, Jv, J, D, hv, h);
+            double lr = -beta * dE;
+            int acc = alg == ORC_METROPOLIS ? ((lr > 0) || (u < orc_exp(lr))) : (u < orc_logistic(lr));
+            if (acc) sn = prop;
+        }
+        if (sn != so) {
+            s[v] = (int8_t)sn;
+            *E += dE;
+            *M += sn - so;
+            ++acc_n;
+        }
+    }
+    *attempts += (uint64_t)nattempts;
+    *accepts += acc_n;
     return ORC_OK;
 }

@@ -34,6 +34,7 @@ uint32_t orc_site_word(uint64_t seed, uint32_t stream, uint64_t sweep, int colou
                        int purpose, uint64_t site);
 /* natural logarithm restated from the atanh series; used for every FP64 decision */
 double orc_log(double x);
+void orc_log_array(const double* x, double* y, int64_t n);
 
 /* acceptance tables (uint32 thresholds widened to u64 so 2^32 means "always") */
 int orc_table_ising(int dim, int alg, double beta, double J, double h,
@@ -61,6 +62,11 @@ int orc_flathist_sweep(int8_t* s, int model, int dim, const int32_t* L, double J
                        int64_t step, int64_t nbins, double logf, uint64_t seed,
                        uint32_t stream, uint64_t sweep0, int64_t nsweeps, int64_t* obs,
                        uint64_t* steps, uint64_t* accepted);
+int orc_flathist_trace(int8_t* s, int model, int dim, const int32_t* L, double J, double D,
+                       double h, int mode, double* lnw, int64_t* H, int64_t start,
+                       int64_t step, int64_t nbins, double logf, uint64_t seed,
+                       uint32_t stream, uint64_t sweep0, int64_t nsweeps, double* tr_u,
+                       double* tr_lr, int64_t tr_cap, int64_t* tr_n);
 void orc_muca_update(double* lnw, const int64_t* H, int64_t nbins);
 int orc_wl_flat(const int64_t* H, const uint8_t* visited, int64_t nbins, double flatness,
                 double* ratio);
@@ -99,6 +105,11 @@ int orc_bcg_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* co
                   double beta, uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps,
                   double* E, int64_t* M, double* E_series, int64_t* M_series, uint64_t* attempts,
                   uint64_t* accepts);
+int orc_graph_seq_attempts(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
+                           const double* Jv, double J, const double* hv, double h, int bc, double D,
+                           int alg, double beta, uint64_t seed, uint32_t stream, uint64_t attempt0,
+                           int64_t nattempts, double* E, int64_t* M, uint64_t* attempts,
+                           uint64_t* accepts);
 
 /* integrated autocorrelation time (-1 on invalid arguments) */
 double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c);

@@ -204,3 +204,88 @@ def test_pt_256_replicas_configured_ladder(gpu, mode):
     for r in range(pt.nrep):
         assert np.array_equal(pt.spins(r), spins[r]), r
     pt.close()
+
+
+# ------------------------------- FP64 decisions against the reference's literal rule --
+def _u53(hi, lo):
+    return float((int(hi) << 21) | (int(lo) >> 11)) * 2.0 ** -53
+
+
+def test_pt_exchange_replay_and_literal_rule(gpu):
+    """400 sweeps of the configured ladder with an exchange after every sweep.  The host
+    replays every exchange decision from the device's recorded energies and the exchange
+    uniforms (Philox(seed, (pair, sweep lo, sweep hi16 | 4<<24, ladder)), words 0-1): the
+    device's rule lr > 0 || log(U) < lr reproduces the final positions, stage and edge
+    counters, and the reference's literal rule lr > 0 || U < exp(lr)
+    (src/algorithms/replica_exchange.jl:110-115) takes the same decision every time."""
+    import math
+    from mcx.pt import ParallelTempering
+    ladders = _pt_ladders()
+    nsw = 400
+    pt = ParallelTempering(ladders, dim=3, seed=PT_SEED)
+    pt.init_(PT_SEED)
+    series = pt.sweep_(nsw, alg="metropolis", exchange_every=1, record=True)
+    key = np.array([PT_SEED & 0xFFFFFFFF, PT_SEED >> 32], np.uint32)
+    first = np.cumsum([0] + [len(b) for _, b in ladders])
+    pos = [np.arange(len(b)) for _, b in ladders]
+    steps = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
+    acc = [np.zeros(len(b) - 1, np.uint64) for _, b in ladders]
+    stage, ndec, disagree = 0, 0, 0
+    for t in range(nsw):
+        for l, (_, b) in enumerate(ladders):
+            n = len(b)
+            rep = np.empty(n, np.int64)
+            rep[pos[l]] = np.arange(n)
+            for p in range(stage % 2, n - 1, 2):
+                ri, rj = rep[p], rep[p + 1]
+                w = O.philox([p, t & 0xFFFFFFFF, ((t >> 32) & 0xFFFF) | (4 << 24), l], key)
+                U = _u53(w[0], w[1])
+                xi = -float(series[t, first[l] + ri, 0])
+                xj = -float(series[t, first[l] + rj, 0])
+                bi, bj = b[p], b[p + 1]
+                lr = (((-bi) * xj) - ((-bi) * xi)) + (((-bj) * xi) - ((-bj) * xj))
+                d_dev = (lr > 0) or (O.log(U) < lr)
+                d_ref = (lr > 0) or (U < math.exp(lr))
+                ndec += 1
+                disagree += d_dev != d_ref
+                steps[l][p] += 1
+                if d_dev:
+                    acc[l][p] += 1
+                    pos[l][ri], pos[l][rj] = p + 1, p
+        stage = 1 - stage
+    assert ndec > 50000
+    assert disagree == 0
+    assert np.array_equal(pt.positions, np.concatenate(pos))
+    assert pt.stage == stage
+    s, a = pt.counters()
+    assert np.array_equal(s, np.concatenate(steps)) and np.array_equal(a, np.concatenate(acc))
+    pt.close()
+
+
+def test_muca_update_configured_bins_against_numpy(gpu):
+    """update!(::MulticanonicalEnsemble) over the 4,194,305 bins: bit for bit with the
+    oracle, and within 1 ulp of log(H) plus the rounding of the subtraction of numpy's
+    lnw - log(H) (src/ensembles/multicanonical.jl:37-41) on every bin."""
+    from mcx import flathist as F
+    rng = np.random.default_rng(17)
+    start, step, nb = BINS
+    E = start + step * np.arange(nb, dtype=np.float64)
+    lnw = -0.35 * E - 1e-7 * E * E
+    H = np.zeros(nb, np.int64)
+    band = slice(NBC // 2, 3 * NBC)  # the visited energies of a production run
+    H[band] = rng.poisson(rng.uniform(0.5, 2e6, size=H[band].size))
+    ens = F.MulticanonicalEnsemble(BINS)
+    ens.logweight = lnw
+    ens.histogram = H
+    F.update_(ens)
+    got = ens.logweight
+    ens.close()
+    orc = lnw.copy()
+    O.muca_update(orc, H)
+    assert np.array_equal(got, orc)
+    m = H > 0
+    logh = np.log(H[m].astype(np.float64))
+    ref = lnw[m] - logh
+    bound = np.spacing(np.abs(logh)) + np.spacing(np.abs(ref))
+    assert np.all(np.abs(got[m] - ref) <= bound)
+    assert np.array_equal(got[~m], lnw[~m])

@@ -196,3 +196,23 @@ def test_blume_capel_graph_heat_bath_distribution():
     p = w / w.sum()
     counts = np.array([(s == v).sum() for v in (-1, 0, 1)])
     assert np.all(np.abs(counts / n - p) < 4 * np.sqrt(p * (1 - p) / n)), (counts / n, p)
+
+
+@pytest.mark.parametrize("model,alg,beta,D,h", [(O.ISING, O.METROPOLIS, 0.44, 0.0, 0.0),
+                                                 (O.ISING, O.HEATBATH, 0.3, 0.0, 0.2),
+                                                 (O.BC, O.METROPOLIS, 0.6, 1.0, 0.0),
+                                                 (O.BC, O.HEATBATH, 0.5, 0.5, 0.1)])
+def test_graph_sequential_mode_equals_lattice_sequential_mode(model, alg, beta, D, h):
+    """On a periodic torus the graph oracle's random-vertex attempts (exp of the library's
+    own) and the lattice oracle's (exp of the C library) pick the same sites and take the
+    same decisions: the two exps differ by at most an ulp, far below 1 in 10^5 attempts."""
+    L = [12, 10]
+    n, es = grid_edges(L, True)
+    rp, col, _ = from_edges(n, es)
+    g = O.BCGraph(rp, col, J=1.0, D=D, h=h) if model == O.BC else O.Graph(rp, col, J=1.0, h=h)
+    s1 = O.init_random(model, L, 3)
+    s2 = s1.copy()
+    st, ac = O.seq_attempts(s1, model, L, alg, beta, 9, stream=2, attempt0=5, nattempts=100000, J=1.0, D=D, h=h)
+    E, M, att, acc = O.graph_seq_attempts(g, s2, alg, beta, 9, stream=2, attempt0=5, nattempts=100000)
+    assert np.array_equal(s1, s2)
+    assert (st, ac) == (att, acc)
