@@ -506,11 +506,15 @@ MCX_API mcx_status mcx_graph_tau_int(mcx_graph* g, int quantity, int64_t max_lag
  *                   (pair_sum, spin_sum, spin2_sum), or NULL.
  *   accepted_dev:   caller-owned device uint64, set to this call's accepted moves, or NULL.
  * The call only enqueues work on the context stream; the lattice's cached bookkeeping
- * (mcx_observables) is updated, mcx_read_series is not.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  Every call shares the array and clears the part it
- * uses; calls whose work overlaps on the GPU (other streams or contexts on the same
- * device) race on it and must be serialized by the caller. */
+ * (mcx_observables) is updated.  The series the library keeps for the lattice is not
+ * written: after this call mcx_read_series and mcx_lattice_tau_int find no recorded
+ * sweeps (MCX_ERR_INVALID_ARG) until the next mcx_sweep.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) and keeps it for the life
+ * of the process; make that first call before any stream capture, and do not use the
+ * library on a device after resetting it (cudaDeviceReset).  Every call shares the
+ * array and clears the part it uses; calls whose work overlaps on the GPU (other
+ * streams or contexts on the same device) race on it and must be serialized by the
+ * caller. */
 #define MCX_NOALLOC_MAX_SWEEPS 4096
 MCX_API mcx_status mcx_sweep_noalloc(mcx_lattice* lat, mcx_algorithm alg, double beta,
                                      mcx_rng* rng, int64_t nsweeps, int64_t* obs_series_dev,

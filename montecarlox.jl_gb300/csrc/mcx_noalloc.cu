@@ -51,7 +51,10 @@ __global__ void k_noalloc_finish(const long long* partial, long long* series_out
 }
 
 // Device address of g_noalloc_scratch on `device`, looked up once per device (with
-// that device current) and cached.
+// that device current) and cached for the life of the process.  A device reset
+// (cudaDeviceReset, or a primary-context reset by another runtime in the process) may
+// reload the module elsewhere; like every other device object of the library, the
+// cached address is then invalid and the library must not be used on that device again.
 static mcx_status noalloc_scratch_ptr(int device, unsigned long long** out) {
     constexpr int kMaxDevices = 64;
     static std::mutex mu;
@@ -121,5 +124,7 @@ extern "C" MCX_API mcx_status mcx_sweep_noalloc(mcx_lattice* lat, mcx_algorithm 
     count_launch(ctx, 2 * (uint64_t)nsweeps + 1);
     MCX_CUDA(cudaGetLastError());
     rng->counter += (uint64_t)nsweeps;
+    // the stored series describes states before these sweeps: report none rather than stale data
+    lat->series_len = 0;
     return MCX_OK;
 }

@@ -55,14 +55,20 @@ def test_noalloc_matches_mcx_sweep(gpu, kind, L, alg, beta, D):
         obs_b = torch.full((nsweeps, 3), -1, dtype=torch.int64, device="cuda")
         acc_b = torch.full((1,), -1, dtype=torch.int64, device="cuda")
         used0 = ctx.memory()[0]
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         mcx._check(fn(b.handle, alg, beta, C.byref(rb), nsweeps, obs_b.data_ptr(), acc_b.data_ptr()))
         ctx.sync()
         assert ctx.memory()[0] == used0  # nothing allocated through the context
+        if nsweeps == 12:  # after the first call has loaded the kernels: no device allocation at all
+            assert torch.cuda.mem_get_info()[0] == free0
         assert rb.counter == ra.counter
         assert np.array_equal(obs_b.cpu().numpy(), obs_a)
         assert int(acc_b.item()) == cnt.accepted
         assert np.array_equal(a.spins, b.spins)
         assert mcx.observables(a) == mcx.observables(b)
+        with pytest.raises(mcx.ArgumentError):  # no stale series after a no-alloc call
+            mcx._check(lib.mcx_read_series(b.handle, np.zeros(3, np.int64).ctypes.data, 1))
     b.close()
     a.close()
 
