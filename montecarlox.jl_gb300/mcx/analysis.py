@@ -11,13 +11,20 @@ cumulant and Onsager's results are restated from the published formulas:
             kind (Onsager, Phys. Rev. 65, 117 (1944));
             spontaneous magnetisation m = (1 - sinh(2b)^-4)^(1/8) for b > b_c
             (Yang, Phys. Rev. 85, 808 (1952)), b_c = ln(1 + sqrt 2) / 2.
+  Kaufman:  the partition function of the finite m x n torus (Kaufman, Phys. Rev. 76,
+            1232 (1949); in the form of Ferdinand & Fisher, Phys. Rev. 185, 832 (1969)):
+            Z = 1/2 (2 sinh 2K)^(mn/2) (Z1 + Z2 + Z3 + Z4), K = beta J,
+            Z1 = prod_r 2 cosh(m g_{2r+1} / 2), Z2 = prod_r 2 sinh(m g_{2r+1} / 2),
+            Z3 = prod_r 2 cosh(m g_{2r} / 2),   Z4 = prod_r 2 sinh(m g_{2r} / 2),
+            r = 0 .. n-1, cosh g_l = cosh 2K coth 2K - cos(pi l / n) for l >= 1 and
+            g_0 = 2K + ln tanh K (negative below the critical coupling).
 """
 import math
 
 import numpy as np
 
 __all__ = ["binning_error", "binned_mean", "binder_cumulant", "jackknife", "onsager_energy_per_site",
-           "onsager_magnetization", "BETA_C", "log_sum", "distribution_from_logdos"]
+           "onsager_magnetization", "BETA_C", "log_sum", "distribution_from_logdos", "kaufman_ising2d"]
 
 BETA_C = 0.5 * math.log(1.0 + math.sqrt(2.0))
 
@@ -80,6 +87,66 @@ def onsager_magnetization(beta, J=1.0):
     if b <= BETA_C:
         return 0.0
     return (1.0 - math.sinh(2 * b) ** -4) ** 0.125
+
+
+def kaufman_ising2d(m, n, beta, J=1.0):
+    """Exact (log Z, <E>) of the 2-D Ising model with coupling J on the periodic m x n
+    lattice at inverse temperature beta, E = -J sum over the 2mn bonds of s_i s_j, from
+    Kaufman's partition function (formula in the module docstring).  <E> = -J d ln Z / dK
+    is evaluated analytically; products are summed as logarithms with their signs, so any
+    size works in FP64.  m, n >= 3, beta J > 0."""
+    m, n = int(m), int(n)
+    if m < 3 or n < 3:
+        raise ValueError("m, n >= 3")
+    K = float(beta) * float(J)
+    if not K > 0:
+        raise ValueError("beta * J must be positive")
+    s2, c2 = math.sinh(2 * K), math.cosh(2 * K)
+    c = c2 * c2 / s2                                   # cosh 2K coth 2K
+    dc = 2.0 * c2 * (s2 * s2 - 1.0) / (s2 * s2)        # d c / dK
+    g = np.empty(2 * n)
+    dg = np.empty(2 * n)
+    g[0] = 2 * K + math.log(math.tanh(K))
+    dg[0] = 2.0 + 2.0 / s2
+    lv = np.arange(1, 2 * n)
+    g[1:] = np.arccosh(c - np.cos(math.pi * lv / n))
+    dg[1:] = dc / np.sinh(g[1:])
+    x = 0.5 * m * g
+    dx = 0.5 * m * dg
+
+    def lcosh(v):  # log(2 cosh v), stable for large |v|
+        a = np.abs(v)
+        return a + np.log1p(np.exp(-2.0 * a))
+
+    def lsinh(v):  # log|2 sinh v| for v != 0
+        a = np.abs(v)
+        return a + np.log1p(-np.exp(-2.0 * a))
+
+    terms = []  # (log|Z_i| or None for an exact zero, sign, numerator of d ln Z contribution as (log, sign))
+    for parity, kind in ((1, "cosh"), (1, "sinh"), (0, "cosh"), (0, "sinh")):
+        xs, ds = x[parity::2], dx[parity::2]
+        if kind == "cosh":
+            lz = float(lcosh(xs).sum())
+            d = float((ds * np.tanh(xs)).sum())
+            terms.append((lz, 1.0, d, None))
+            continue
+        if np.all(xs != 0):
+            lz = float(lsinh(xs).sum())
+            sign = float(np.prod(np.sign(xs)))
+            d = float((ds / np.tanh(xs)).sum())
+            terms.append((lz, sign, d, None))
+        else:  # g_0 = 0 exactly: the term vanishes, its derivative does not
+            k = int(np.flatnonzero(xs == 0)[0])
+            rest = np.delete(np.arange(xs.size), k)
+            lrest = float(lsinh(xs[rest]).sum())
+            terms.append((None, 0.0, 0.0, (lrest + math.log(2.0 * abs(ds[k])), float(np.sign(ds[k])))))
+    top = max(t[0] for t in terms if t[0] is not None)
+    den = sum(sg * math.exp(lz - top) for lz, sg, _, _ in terms if lz is not None)
+    num = sum(sg * math.exp(lz - top) * d for lz, sg, d, _ in terms if lz is not None)
+    num += sum(z[1] * math.exp(z[0] - top) for _, _, _, z in terms if z is not None)
+    logz = math.log(0.5) + 0.5 * m * n * math.log(2.0 * s2) + top + math.log(den)
+    dlogz = m * n * c2 / s2 + num / den
+    return logz, -float(J) * dlogz
 
 
 def log_sum(values):

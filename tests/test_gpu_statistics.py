@@ -98,3 +98,41 @@ def test_exact_dos_distribution_l8(gpu):
     chi2 = (((counts - n * p) ** 2) / (n * p))[mask].sum()
     dof = mask.sum() - 1
     assert chi2 < dof + 5 * math.sqrt(2 * dof), (chi2, dof)
+
+
+def test_kaufman_configured_l64_chain(gpu):
+    """The configured small run: L=64, Philox key 42, Metropolis at beta 0.4407 (next to
+    beta_c), 10^3 thermalisation sweeps then 10^4 recorded: the mean energy per site within
+    3 sigma (binning) of the exact finite-torus value (Kaufman 1949)."""
+    from mcx.analysis import binning_error, kaufman_ising2d
+    L, beta = 64, 0.4407
+    sys_ = gpu.Ising([L, L])
+    gpu.init_(sys_, "random", rng=gpu.Philox(42))
+    a = gpu.Metropolis(gpu.Philox(42), beta=beta)
+    gpu.sweep_(sys_, a, 1000)
+    obs = gpu.sweep_(sys_, a, 10000, record=True)
+    e = -obs[:, 0] / (L * L)
+    exact = kaufman_ising2d(L, L, beta)[1] / (L * L)
+    err = binning_error(e, min_bins=16)
+    assert abs(e.mean() - exact) < 3 * err, (e.mean(), exact, err)
+
+
+@pytest.mark.parametrize("L", [32, 64])
+def test_kaufman_independent_chains(gpu, L):
+    """64 independent chains (one batched call, streams 0..63) of the same workload: the
+    mean energy per site over the chains within 3 standard errors of the chain means of
+    Kaufman's exact value at beta 0.4407."""
+    from mcx.analysis import kaufman_ising2d
+    beta, nch = 0.4407, 64
+    chains = [gpu.Ising([L, L]) for _ in range(nch)]
+    for i, c in enumerate(chains):
+        gpu.init_(c, "random", rng=gpu.Philox(42, i))
+    algs = [gpu.Metropolis(gpu.Philox(42, i), beta=beta) for i in range(nch)]
+    gpu.sweep_batch_(chains, algs, 1000)
+    obs = gpu.sweep_batch_(chains, algs, 10000, record=True)
+    means = np.array([(-o[:, 0] / (L * L)).mean() for o in obs])
+    exact = kaufman_ising2d(L, L, beta)[1] / (L * L)
+    se = means.std(ddof=1) / math.sqrt(nch)
+    assert abs(means.mean() - exact) < 3 * se, (means.mean(), exact, se)
+    for c in chains:
+        c.close()
