@@ -12,8 +12,8 @@
  *     library; host buffers are owned by the caller.
  *   - Spins cross the boundary in the SpinSystems linear order: site
  *     i = x + Lx*(y + Ly*z) (0-based), the Graphs.grid vertex order used by
- *     Ising(dims)/BlumeCapel(dims) (SpinSystems/src/ising.jl:523-534) and by
- *     IsingLatticeOptim (ising.jl:550-571).  Values are int8 in {-1,+1} (Ising)
+ *     Ising(dims)/BlumeCapel(dims) (SpinSystems/src/ising.jl:413-424,
+ *     SpinSystems/src/blume_capel.jl:500-511) and by IsingLatticeOptim (ising.jl:430-461).  Values are int8 in {-1,+1} (Ising)
  *     or {-1,0,+1} (Blume-Capel), as SpinSystems' `spins::Vector{Int8}`.
  *   - A context owns one CUDA stream; calls on one context are ordered on it.
  *     A context is not thread-safe; distinct contexts are independent.
@@ -52,9 +52,9 @@ typedef enum mcx_status {
 
 typedef enum mcx_model { MCX_ISING = 0, MCX_BLUME_CAPEL = 1 } mcx_model;
 
-/* Metropolis: src/algorithms/metropolis.jl:124-127, Glauber: :231-237,
- * HeatBath: src/algorithms/heat_bath.jl + SpinSystems ising.jl:153-168 /
- * blume_capel.jl:61-85. */
+/* Metropolis: src/algorithms/metropolis.jl:14-17, Glauber: :121-127,
+ * HeatBath: src/algorithms/heat_bath.jl:11-17 + SpinSystems/src/ising.jl:43-58 /
+ * SpinSystems/src/blume_capel.jl:61-85. */
 typedef enum mcx_algorithm { MCX_METROPOLIS = 0, MCX_GLAUBER = 1, MCX_HEATBATH = 2 } mcx_algorithm;
 
 /* INT8: one byte per site.  MSC64: 64 same-colour sites per uint64 word
@@ -74,7 +74,7 @@ typedef struct mcx_config {
 /* Counter-based random stream: Philox4x32-10 keyed by `seed`; `counter` is the
  * next sweep index and advances by the number of sweeps run; `stream` separates
  * independent chains with the same seed.  Stands in for the `rng` field of the
- * reference's algorithm objects (src/algorithms/metropolis.jl:173-178). */
+ * reference's algorithm objects (src/algorithms/metropolis.jl:63-68). */
 typedef struct mcx_rng {
     uint64_t seed;
     uint64_t counter;
@@ -114,8 +114,8 @@ MCX_API mcx_status mcx_ctx_memory(mcx_ctx* ctx, uint64_t* used, uint64_t* budget
 MCX_API mcx_status mcx_ctx_launches(mcx_ctx* ctx, uint64_t* launches);
 
 /* --------------------------------------------------------------- lattice -- */
-/* Replaces Ising(dims; J, periodic=true, h) (SpinSystems/src/ising.jl:523-534),
- * IsingLatticeOptim(Lx, Ly) (ising.jl:550-571) and BlumeCapel(dims; J, D, h)
+/* Replaces Ising(dims; J, periodic=true, h) (SpinSystems/src/ising.jl:413-424),
+ * IsingLatticeOptim(Lx, Ly) (ising.jl:430-461) and BlumeCapel(dims; J, D, h)
  * (SpinSystems/src/blume_capel.jl:500-511).  All spins start at +1, like the
  * reference constructors. */
 MCX_API mcx_status mcx_lattice_create(mcx_ctx* ctx, mcx_model model, int dim,
@@ -129,28 +129,28 @@ MCX_API mcx_status mcx_lattice_info(const mcx_lattice* lat, int64_t* nsites,
 MCX_API mcx_status mcx_set_spins(mcx_lattice* lat, const int8_t* host, size_t n);
 MCX_API mcx_status mcx_get_spins(mcx_lattice* lat, int8_t* host, size_t n);
 
-/* init!(sys, :random; rng) (ising.jl:170-188, blume_capel.jl:87-109), fed by Philox. */
+/* init!(sys, :random; rng) (SpinSystems/src/ising.jl:60-78, SpinSystems/src/blume_capel.jl:87-109), fed by Philox. */
 MCX_API mcx_status mcx_init_random(mcx_lattice* lat, uint64_t seed, uint32_t stream);
 /* init!(sys, :up / :down / :zero): every site set to `value`. */
 MCX_API mcx_status mcx_init_uniform(mcx_lattice* lat, int8_t value);
 
 /* Cached bookkeeping of the reference systems (sum_pair_interactions without J,
- * sum_spins, sum_spins2; ising.jl:196-203, blume_capel.jl:117-127).  Waits for
+ * sum_spins, sum_spins2; SpinSystems/src/ising.jl:430-438, SpinSystems/src/blume_capel.jl:117-126).  Waits for
  * the stream. */
 MCX_API mcx_status mcx_observables(mcx_lattice* lat, int64_t* pair_sum, int64_t* spin_sum,
                                    int64_t* spin2_sum);
 /* energy(sys; full=true) / magnetization(sys; full=true): recompute the bookkeeping
- * from the spins (ising.jl:127-128, _recompute_cached! :251-269); waits. */
+ * from the spins (SpinSystems/src/ising.jl:17-18, _recompute_cached! :141-159, :500-504); waits. */
 MCX_API mcx_status mcx_recompute_observables(mcx_lattice* lat, int64_t* pair_sum,
                                              int64_t* spin_sum, int64_t* spin2_sum);
-/* energy(sys), magnetization(sys) (ising.jl:127-128, blume_capel.jl:18-19):
+/* energy(sys), magnetization(sys) (SpinSystems/src/ising.jl:17-18, SpinSystems/src/blume_capel.jl:18-19):
  * E = -J*pair_sum - h*spin_sum + D*spin2_sum. */
 MCX_API mcx_status mcx_energy(mcx_lattice* lat, double* energy, int64_t* magnetization);
 
 /* N x spin_flip!(sys, alg) per sweep in checkerboard order, `nsweeps` sweeps
  * (replaces the user loop `for _ in 1:N; spin_flip!(sys, alg); end`, e.g.
  * docs/src/examples/spin_systems/importance_Ising2D.jl:105-122, over
- * spin_flip! ising.jl:145-168 / blume_capel.jl:52-85).
+ * spin_flip! SpinSystems/src/ising.jl:25-58 / SpinSystems/src/blume_capel.jl:41-85).
  *   obs_series: host int64[nsweeps*3] of (pair_sum, spin_sum, spin2_sum) after each
  *               sweep, or NULL.  counters: accumulated, or NULL.
  * With both NULL the call only enqueues work on the context stream. */
@@ -217,7 +217,7 @@ MCX_API mcx_status mcx_flathist_reset(mcx_flathist* fh);
  * FP64 throughout, deterministic; MCX_ERR_INVALID_ARG when no bin is finite. */
 MCX_API mcx_status mcx_flathist_reweight(mcx_flathist* fh, const double* betas, int32_t nbeta, double* logz,
                                          double* mean_e, double* mean_e2, double* dist, int64_t dist_len);
-/* update!(::MulticanonicalEnsemble; mode=:simple) (multicanonical.jl:32-43):
+/* update!(::MulticanonicalEnsemble; mode=:simple) (src/ensembles/multicanonical.jl:32-43):
  * ln g[b] -= log(H[b]) where H[b] > 0. */
 MCX_API mcx_status mcx_flathist_update_muca(mcx_flathist* fh);
 /* Wang-Landau flatness (the reference has none; Wang & Landau 2001): marks every bin
@@ -233,9 +233,9 @@ MCX_API mcx_status mcx_flathist_merge(mcx_flathist* dst, mcx_flathist* const* sr
 /* distribute_logweight! (parallel_multicanonical.jl:59-68): dst.lnw := src.lnw. */
 MCX_API mcx_status mcx_flathist_copy_logweight(mcx_flathist* dst, const mcx_flathist* src);
 /* `nsweeps` checkerboard sweeps of N importance-sampling spin flips
- * (ising.jl:135-143, blume_capel.jl:41-50) for each of `nwalkers` walkers, with
+ * (SpinSystems/src/ising.jl:25-33, SpinSystems/src/blume_capel.jl:41-50) for each of `nwalkers` walkers, with
  * accept!(alg, E_new, E_old) of a Multicanonical (importance_sampling.jl:69-78) or
- * Wang-Landau (wang_landau.jl:29-37) algorithm; the decision lr > 0 || U < exp(lr)
+ * Wang-Landau (src/algorithms/wang_landau.jl:29-37) algorithm; the decision lr > 0 || U < exp(lr)
  * is evaluated as log(U) < lr.  fhs: one table shared by all walkers (nfh = 1;
  * Multicanonical only: H adds up over walkers like merge_histograms!) or one per
  * walker (nfh = nwalkers).  Walker i draws from rngs[i].  Lattices must be int8, of
@@ -410,7 +410,7 @@ MCX_API mcx_status mcx_graph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowp
  * {-1, 0, 1} (all +1 at start), E = -pair - field + D sum s^2.  Sweeps: Metropolis /
  * Glauber propose one of the two other states (_propose_state, :21-30) from bit 0 of the
  * low word of the site's uniform; the heat bath draws from the three Boltzmann weights
- * with r = u z (:59-85). */
+ * with r = u z (:61-85). */
 MCX_API mcx_status mcx_bcgraph_create(mcx_ctx* ctx, int64_t n, const int64_t* rowptr,
                                       const int32_t* col, const double* coupling, double J,
                                       double D, const double* field, double h, mcx_graph** out);
@@ -434,12 +434,13 @@ MCX_API mcx_status mcx_graph_energy(mcx_graph* g, int full, double* energy,
                                     int64_t* magnetization);
 /* delta_energy(sys, i) (ising.jl:20-23, :198, :362) for 0-based site i; waits. */
 MCX_API mcx_status mcx_graph_delta_energy(mcx_graph* g, int64_t i, double* delta_energy);
-/* modify!(sys, i, Δpair, Δspin) with the flip_changes of site i (ising.jl:200-218,
- * :364-377): flips spin i and updates the cached energy and magnetization. */
+/* modify!(sys, i, Δpair, Δspin) (SpinSystems/src/ising.jl:200-218, :364-377) with the
+ * flip_changes of site i (:187-192, :351-356): flips spin i and updates the cached energy and
+ * magnetization. */
 MCX_API mcx_status mcx_graph_flip(mcx_graph* g, int64_t i);
-/* delta_energy(sys, i, s_new) (blume_capel.jl:32-35; for an Ising graph s_new = -s_i is
+/* delta_energy(sys, i, s_new) (SpinSystems/src/blume_capel.jl:36-39; for an Ising graph s_new = -s_i is
  * the flip and s_new = s_i gives 0) and modify! to s_new with propose_changes
- * (:262-276, :441-466). */
+ * (:235-241, :250-272, :423-429, :438-460). */
 MCX_API mcx_status mcx_graph_delta_energy_to(mcx_graph* g, int64_t i, int8_t s_new,
                                              double* delta_energy);
 MCX_API mcx_status mcx_graph_set_site(mcx_graph* g, int64_t i, int8_t s_new);

@@ -105,14 +105,14 @@ static uint64_t threshold(double p) {
 }
 
 // accept iff lr > 0 || U < exp(lr), lr = -beta*dE
-// (src/algorithms/metropolis.jl:124-127, importance_sampling.jl:80-85, boltzmann.jl:28)
+// (src/algorithms/metropolis.jl:14-17, importance_sampling.jl:80-85, boltzmann.jl:28)
 static uint64_t metropolis(double beta, double dE) {
     double lr = (-beta) * dE;
     if (lr >= 0.0) return 1ull << 32;
     return threshold(std::exp(lr));
 }
 
-// accept iff U < logistic(lr)  (src/algorithms/metropolis.jl:231-237)
+// accept iff U < logistic(lr)  (src/algorithms/metropolis.jl:121-127)
 static uint64_t glauber(double beta, double dE) { return threshold(logistic((-beta) * dE)); }
 
 // Ising: entry a + (2d+1)*up, a = aligned neighbours; flip iff (u ^ m) < thr with
@@ -125,13 +125,13 @@ mcx_status build_ising_table(int dim, mcx_algorithm alg, double beta, double J, 
         for (int a = 0; a <= z; ++a) {
             const double s = up ? 1.0 : -1.0;
             const double lpi = (double)(2 * a - z);
-            const double dpair = ((-2.0) * J) * lpi;     // SpinSystems/src/ising.jl:297-301
-            const double dE = (-dpair) - (h * (-2.0 * s));  // ising.jl:308
+            const double dpair = ((-2.0) * J) * lpi;     // flip_changes, SpinSystems/src/ising.jl:484-489
+            const double dE = (-dpair) - (h * (-2.0 * s));  // delta_energy, ising.jl:198
             uint64_t v;
             if (alg == MCX_METROPOLIS) v = metropolis(beta, dE);
             else if (alg == MCX_GLAUBER) v = glauber(beta, dE);
             else if (alg == MCX_HEATBATH) {
-                // ising.jl:153-168: p_plus = logistic(beta*s_old*dE); s_new = U<p_plus ? +1 : -1
+                // ising.jl:43-58: p_plus = logistic(beta*s_old*dE); s_new = U<p_plus ? +1 : -1
                 const uint64_t tp = threshold(logistic((beta * s) * dE));
                 v = up ? (1ull << 32) - tp : tp;
             } else
@@ -682,7 +682,7 @@ MCX_API mcx_status mcx_recompute_observables(mcx_lattice* lat, int64_t* pair_sum
 MCX_API mcx_status mcx_energy(mcx_lattice* lat, double* energy, int64_t* magnetization) {
     int64_t P, M, Q;
     MCX_CHECK(mcx_observables(lat, &P, &M, &Q));
-    // _cached_energy: -J*pair - h*M (+ D*Q for Blume-Capel), ising.jl:290-293, blume_capel.jl:221-223
+    // _cached_energy: -J*pair - h*M (+ D*Q for Blume-Capel), SpinSystems/src/ising.jl:181-183, :472, SpinSystems/src/blume_capel.jl:221-223
     double E = (-(lat->J * (double)P)) - (lat->h * (double)M);
     if (lat->model == MCX_BLUME_CAPEL) E = E + lat->D * (double)Q;
     if (energy) *energy = E;

@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     }
 }
 
-// lnw[b] -= log(H[b]) for H[b] > 0 (multicanonical.jl:32-43)
+// lnw[b] -= log(H[b]) for H[b] > 0 (src/ensembles/multicanonical.jl:32-43)
 __global__ void k_muca_update(double* lnw, const unsigned long long* H, long long n) {
     for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n;
          b += (long long)gridDim.x * blockDim.x) {

@@ -513,7 +513,7 @@ __host__ __device__ __forceinline__ int bc_propose_state(int so, int b) {
     return so == -1 ? (b ? 0 : 1) : (so == 0 ? (b ? -1 : 1) : (b ? -1 : 0));
 }
 
-// propose_changes + delta_energy (:245-251, :259-260): -Δspin c - h Δspin + D Δspin2
+// propose_changes + delta_energy (:235-241, :247-248): -Δspin c - h Δspin + D Δspin2
 __host__ __device__ __forceinline__ double bc_delta(double c, int so, int sn, double hf, bool field, double D) {
     const int ds = sn - so, ds2 = sn * sn - so * so;
     const double dpair = (double)ds * c;
@@ -521,7 +521,7 @@ __host__ __device__ __forceinline__ double bc_delta(double c, int so, int sn, do
     return (-dpair - dfield) + D * (double)ds2;
 }
 
-// local_coupling (:241-243, :368-377): the integer neighbour sum and, for per-entry
+// local_coupling (:227-229, :368-377): the integer neighbour sum and, for per-entry
 // couplings, the FP64 sum of J_ij s_j in row order; four entries at a time.
 template <bool EDGEJ>
 __device__ __forceinline__ void bc_row(const GraphDev& g, const int8_t* sp, long long off, int w, int lane, int& isum,
@@ -635,7 +635,7 @@ __device__ __noinline__ int bc_exact_site(const GraphDev& g, const int8_t* sp, l
     const double hf = FIELD == F_VECTOR ? g.h[p] : (FIELD == F_UNIFORM ? g.hu : 0.0);
     const double u = (double)ku * 0x1p-53;
     int sn;
-    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :59-85
+    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :61-85
         const double e1 = (c - hf * (-1.0)) + g.D;
         const double e3 = (-c - hf) + g.D;
         const double w1 = mcx_exp(-g.beta * e1), w2 = mcx_exp(-g.beta * 0.0), w3 = mcx_exp(-g.beta * e3);
@@ -751,7 +751,7 @@ __device__ __forceinline__ int bc_decide(const GraphDev& g, long long p, int so,
     const double hf = FIELD == F_VECTOR ? g.h[p] : (FIELD == F_UNIFORM ? g.hu : 0.0);
     const double u = (double)ku * 0x1p-53;
     int sn;
-    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :59-85
+    if (ALG == MCX_HEATBATH) {  // spin_flip!(::AbstractBlumeCapel, ::AbstractHeatBath), :61-85
         const double e1 = (c - hf * (-1.0)) + g.D;
         const double e3 = (-c - hf) + g.D;
         const double w1 = mcx_exp(-g.beta * e1), w2 = mcx_exp(-g.beta * 0.0), w3 = mcx_exp(-g.beta * e3);

@@ -84,7 +84,7 @@ mcx_status build_seq_table(const mcx_lattice* lat, mcx_algorithm alg, double bet
             for (int a = 0; a <= z; ++a) {
                 const double so = up ? 1.0 : -1.0;
                 const double lpi = (double)(2 * a - z);     // s_i * sum of the neighbours
-                const double dpair = ((-2.0) * J) * lpi;    // flip_changes, ising.jl:187-198
+                const double dpair = ((-2.0) * J) * lpi;    // flip_changes, ising.jl:484-489
                 const double dspin = -2.0 * so;
                 const double dE = (-dpair) - (h * dspin);   // delta_energy
                 double p;

@@ -6,13 +6,13 @@ a trailing underscore (``init!`` -> ``init_``, ``spin_flip!`` -> ``spin_flip_``)
 
 Reference API mirrored here (paths inside MonteCarloX.jl):
   BoltzmannEnsemble           src/ensembles/boltzmann.jl:7-30
-  Metropolis / Glauber        src/algorithms/metropolis.jl:173-237
+  Metropolis / Glauber        src/algorithms/metropolis.jl:63-127
   HeatBath                    src/algorithms/heat_bath.jl:11-17
   acceptance_rate / reset!    src/algorithms/importance_sampling.jl:95-110
-  Ising / IsingLatticeOptim   SpinSystems/src/ising.jl:523-571
+  Ising / IsingLatticeOptim   SpinSystems/src/ising.jl:413-461
   IsingGraph / IsingMatrix    SpinSystems/src/ising.jl:86-428 (mcx.graph)
   BlumeCapel                  SpinSystems/src/blume_capel.jl:500-511
-  init! / energy / magnetization  ising.jl:127-188, blume_capel.jl:18-109
+  init! / energy / magnetization  ising.jl:17-18, :60-78, blume_capel.jl:18-19, :87-109
 """
 import ctypes as C
 import math
@@ -363,7 +363,7 @@ def Ising(dims, J=None, *, periodic=True, h=0, layout="int8", ctx=None):
 
 
 def IsingLatticeOptim(Lx, Ly, *, layout="int8", ctx=None):
-    """2-D periodic J=1 Ising (SpinSystems/src/ising.jl:550-571)."""
+    """2-D periodic J=1 Ising (SpinSystems/src/ising.jl:430-461)."""
     return IsingDevice([Lx, Ly], J=1, h=0, layout=layout, ctx=ctx)
 
 

@@ -130,7 +130,7 @@ static uint64_t prob_to_thr(double p) {
     return (uint64_t)v;
 }
 
-/* Metropolis rule, src/algorithms/metropolis.jl:124-127 and
+/* Metropolis rule, src/algorithms/metropolis.jl:14-17 and
  * src/algorithms/importance_sampling.jl:80-85: accept iff lr > 0 || U < exp(lr),
  * with lr = logweight(BoltzmannEnsemble, dE) = -beta*dE (src/ensembles/boltzmann.jl:28). */
 static uint64_t metropolis_thr(double beta, double dE) {
@@ -139,7 +139,7 @@ static uint64_t metropolis_thr(double beta, double dE) {
     return prob_to_thr(exp(lr));
 }
 
-/* Glauber rule, src/algorithms/metropolis.jl:231-237: accept iff U < logistic(lr). */
+/* Glauber rule, src/algorithms/metropolis.jl:121-127: accept iff U < logistic(lr). */
 static uint64_t glauber_thr(double beta, double dE) {
     double lr = (-beta) * dE;
     return prob_to_thr(logistic(lr));
@@ -156,9 +156,9 @@ int orc_table_ising(int dim, int alg, double beta, double J, double h, uint64_t*
             int idx = a + (z + 1) * up;
             double s = up ? 1.0 : -1.0;
             double lpi = (double)(2 * a - z);            /* s_i * sum_j s_j  */
-            double dpair = ((-2.0) * J) * lpi;            /* ising.jl:297-301 */
+            double dpair = ((-2.0) * J) * lpi;            /* flip_changes, SpinSystems/src/ising.jl:484-489 */
             double dspin = -2.0 * s;
-            double dE = (-dpair) - (h * dspin);           /* ising.jl:308     */
+            double dE = (-dpair) - (h * dspin);           /* delta_energy, ising.jl:198, :491 */
             if (alg == ORC_METROPOLIS) {
                 thr[idx] = metropolis_thr(beta, dE);
                 xmask[idx] = 0;
@@ -166,7 +166,7 @@ int orc_table_ising(int dim, int alg, double beta, double J, double h, uint64_t*
                 thr[idx] = glauber_thr(beta, dE);
                 xmask[idx] = 0;
             } else if (alg == ORC_HEATBATH) {
-                /* ising.jl:153-168: p_plus = logistic(beta*s_old*dE), s_new = U<p_plus ? +1:-1 */
+                /* ising.jl:43-58: p_plus = logistic(beta*s_old*dE), s_new = U<p_plus ? +1:-1 */
                 uint64_t tp = prob_to_thr(logistic((beta * s) * dE));
                 if (up) { thr[idx] = (1ull << 32) - tp; xmask[idx] = 0xFFFFFFFFu; }
                 else    { thr[idx] = tp;                xmask[idx] = 0; }
@@ -278,7 +278,7 @@ void orc_observables(const int8_t* s, int dim, const int32_t* L, int64_t* P, int
     *P = p; *M = m; *Q = q;
 }
 
-/* init!(sys, :random), ising.jl:170-188 / blume_capel.jl:87-109, fed by Philox */
+/* init!(sys, :random), SpinSystems/src/ising.jl:60-78 / SpinSystems/src/blume_capel.jl:87-109, fed by Philox */
 void orc_init_random(int8_t* s, int model, int dim, const int32_t* L, uint64_t seed,
                      uint32_t stream) {
     geom_t g;
@@ -295,7 +295,7 @@ void orc_init_random(int8_t* s, int model, int dim, const int32_t* L, uint64_t s
  * colour every site sees only the other colour, so visiting the sites of one colour
  * in any order equals the simultaneous update the device performs.
  *   Ising: spin_flip!(::AbstractIsing, ::AbstractMetropolis / ::AbstractHeatBath),
- *          SpinSystems/src/ising.jl:145-168, modify! :310-315.
+ *          SpinSystems/src/ising.jl:25-58, modify! :493-498.
  *   Blume-Capel: spin_flip! blume_capel.jl:52-85, modify! :250-256.
  * ------------------------------------------------------------------------- */
 int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
@@ -364,9 +364,10 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
 /* ---------------------------------------------------------------------------
  * Mode (ii): the reference's sequential random-site order with FP64 decisions.
  *   pick_site:   SpinSystems/src/abstractions.jl:19 (rand(rng, UInt) % N + 1)
- *   Metropolis:  ising.jl:145-151 -> metropolis.jl:124-127 -> importance_sampling.jl:80-85
- *   Glauber:     metropolis.jl:231-237
- *   HeatBath:    ising.jl:153-168, blume_capel.jl:61-85
+ *   Metropolis:  SpinSystems/src/ising.jl:35-41 -> src/algorithms/metropolis.jl:14-17 ->
+ *                src/algorithms/importance_sampling.jl:80-85
+ *   Glauber:     src/algorithms/metropolis.jl:121-127
+ *   HeatBath:    SpinSystems/src/ising.jl:43-58, SpinSystems/src/blume_capel.jl:61-85
  *   BC proposal: blume_capel.jl:21-30, 52-59
  * Attempt a draws Philox(seed, (a lo, a hi, P_SEQ<<24, stream)) -> site from words
  * 0,1 and U from words 2,3; Blume-Capel proposals take the top bit of word 0 of
@@ -440,7 +441,8 @@ int orc_seq_attempts(int8_t* s, int model, int dim, const int32_t* L, int alg, d
 
 /* ---------------------------------------------------------------------------
  * Flat-histogram sweeps in checkerboard order.
- *   generic importance-sampling spin flip: ising.jl:135-143, blume_capel.jl:41-50
+ *   generic importance-sampling spin flip: SpinSystems/src/ising.jl:25-33,
+ *                                SpinSystems/src/blume_capel.jl:41-50
  *   accept!(alg, x_new, x_old):  src/algorithms/importance_sampling.jl:69-85
  *   MUCA record_visit!:          src/ensembles/multicanonical.jl:25-30 (h[x] += 1)
  *   WangLandau accept!:          src/algorithms/wang_landau.jl:29-37 (lw[x_vis] -= logf)
@@ -736,7 +738,7 @@ void orc_graph_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream)
     }
 }
 
-/* local_pair_interactions: abstractions.jl:41-48 (integer sum over the neighbour list)
+/* local_pair_interactions: SpinSystems/src/abstractions.jl:41-48 (integer sum over the neighbour list)
  * and ising.jl:294-304 (FP64 sum of s_i J_ij s_j over the stored entries, j != i). */
 static double graph_dpair(const int8_t* s, int64_t v, const int64_t* rowptr, const int32_t* col,
                           const double* Jv, double J) {
@@ -925,7 +927,7 @@ double orc_tau_int(const double* x, int64_t n, int64_t max_lag, double c) {
  * Spins in {-1, 0, 1}; Jv NULL means one coupling J.
  * ------------------------------------------------------------------------- */
 
-/* local_coupling: J * sum_j s_j (:241-243) or the FP64 sum of J_ij s_j over the row,
+/* local_coupling: J * sum_j s_j (:227-229) or the FP64 sum of J_ij s_j over the row,
  * diagonal skipped (:368-377) */
 static double bcg_coupling(const int8_t* s, int64_t v, const int64_t* rowptr, const int32_t* col,
                            const double* Jv, double J) {
@@ -943,7 +945,7 @@ static double bcg_coupling(const int8_t* s, int64_t v, const int64_t* rowptr, co
 
 static double bcg_field(int64_t v, const double* hv, double h) { return hv ? hv[v] : h; }
 
-/* delta_energy(sys, i, s_new), :32-35 with propose_changes :245-251 and :259-260:
+/* delta_energy(sys, i, s_new), :36-39 with propose_changes :235-241 / :423-429 and :247-248:
  * -Δspin*c - h Δspin + D Δspin2 */
 double orc_bcg_delta_energy(const int8_t* s, int64_t v, int s_new, const int64_t* rowptr,
                             const int32_t* col, const double* Jv, double J, double D,
@@ -955,7 +957,7 @@ double orc_bcg_delta_energy(const int8_t* s, int64_t v, int s_new, const int64_t
     return (-dpair - dfield) + D * (double)ds2;
 }
 
-/* _full_energy (:213-214, :396-423) and sum(spins) */
+/* _full_energy (:225, :417) and sum(spins) */
 void orc_bcg_observables(const int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
                          const double* Jv, double J, double D, const double* hv, double h,
                          double* E, int64_t* M) {
@@ -1005,8 +1007,8 @@ void orc_bcg_init_random(int8_t* s, int64_t n, uint64_t seed, uint32_t stream) {
 /* Colour-class sweeps (the order and uniforms of orc_graph_sweep); the proposal of
  * Metropolis / Glauber is bit 0 of the low word of the site's uniform (a bit the 53-bit
  * uniform does not use), standing in for rand(rng, Bool) of _propose_state (:21-30).
- *   Metropolis / Glauber: spin_flip! :50-57 (accept!(alg, ΔE)).
- *   HeatBath: :59-85 -- three Boltzmann weights, r = u z, cumulative choice. */
+ *   Metropolis / Glauber: spin_flip! :52-59 (accept!(alg, ΔE)).
+ *   HeatBath: :61-85 -- three Boltzmann weights, r = u z, cumulative choice. */
 int orc_bcg_sweep(int8_t* s, int64_t n, const int64_t* rowptr, const int32_t* col,
                   const double* Jv, double J, double D, const double* hv, double h, int alg,
                   double beta, uint64_t seed, uint32_t stream, uint64_t sweep0, int64_t nsweeps,

@@ -77,7 +77,7 @@ def test_algorithm_objects(mcxlib):
 
 
 def test_set_betas(mcxlib):
-    # test/test_parallel_ensembles.jl:164-170
+    # test/test_parallel_ensembles.jl:152-158
     from mcx.pt import set_betas
     assert set_betas(4, 0.4, 1.0, ":uniform") == [1.0, 0.8, 0.6, 0.4]
     b2 = set_betas(4, 0.5, 1.0, ":geometric")

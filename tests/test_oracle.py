@@ -180,7 +180,7 @@ def test_flathist_invariants_and_bounds():
     rc, obs, st, ac = O.flathist_sweep(s, O.ISING, L, O.MUCA, lnw, H, -32, 4, 0.0, 5, nsweeps=20)
     assert rc == O.OK and st == 20 * 16 and H.sum() == st
     assert ac == st  # flat weights: every move accepted (test_multicanonical.jl:30-34)
-    # Wang-Landau decrements the visited bin by logf each step (wang_landau.jl:29-37)
+    # Wang-Landau decrements the visited bin by logf each step (src/algorithms/wang_landau.jl:29-37)
     lnw = np.zeros(17)
     H = np.zeros(17, np.int64)
     rc, obs, st, ac = O.flathist_sweep(s, O.ISING, L, O.WL, lnw, H, -32, 4, math.log(2), 5, sweep0=20, nsweeps=3)
@@ -194,7 +194,7 @@ def test_flathist_invariants_and_bounds():
 
 
 def test_exchange_known_answers():
-    # test/test_parallel_ensembles.jl:199-214: beta 1.0 / 0.5, x_i = 0, x_j = -5 -> lr = 2.5 > 0 accepted
+    # test/test_parallel_ensembles.jl:189-206: beta 1.0 / 0.5, x_i = 0, x_j = -5 -> lr = 2.5 > 0 accepted
     betas = np.array([1.0, 0.5])
     pos = np.array([0, 1], np.int32)
     steps = np.zeros(1, np.uint64)

@@ -187,7 +187,7 @@ def test_blume_capel_graph_cached_equals_full(alg):
 
 def test_blume_capel_graph_heat_bath_distribution():
     """The three-state heat bath on a graph with no edges samples each site from
-    exp(-beta (D s^2 - h s)) / Z (blume_capel.jl:59-85)."""
+    exp(-beta (D s^2 - h s)) / Z (blume_capel.jl:61-85)."""
     n = 4000
     g = O.BCGraph(np.zeros(n + 1, np.int64), np.zeros(0, np.int32), J=1.0, D=0.4, h=0.3)
     s = O.bcg_init_random(n, 8)
