@@ -7,8 +7,10 @@ sweeps at beta=0.4407, energy and magnetisation recorded every sweep.  One step 
 one mcx_sweep call of --sweeps-per-step sweeps.  The lattice (16 MiB) fits in L2,
 so L2 is flushed (256 MiB write) between timed steps.
 
-  value      attempts/ns with the lattice resident in HBM, CUDA events on the
-             library's stream (torch's current stream is handed to the context)
+  value      attempts/ns, CUDA events on the library's stream (torch's current stream is
+             handed to the context); L2 is flushed before every timed step, so each step
+             starts from HBM, and the 16 MiB lattice stays L2-resident across the sweeps of
+             the step
   e2e        the same metric through the public C ABI with host buffers: every step
              uploads the lattice from pinned host memory (mcx_set_spins) and reads
              the per-sweep (pair, spin, spin2) series back (mcx_sweep obs_series)
@@ -86,15 +88,10 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch():
-    """DRAM bytes per half-sweep launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "ising_cb_traffic.json")
-    try:
-        with open(path) as f:
-            d = json.load(f)
-        return d.get("dram_bytes_per_launch_full_size")
-    except Exception:
-        return None
+# DRAM bytes (read + write) of one k_ising_cb<2,16,false,true> half-sweep launch on the headline
+# lattice, from one ncu capture (profiles/ising_cb_L4096_metropolis.md; ncu replays with flushed
+# caches, so this is a cold launch: both colour arrays read once)
+CB_TRAFFIC_PER_LAUNCH = 16798976
 
 
 class ClockSampler:
@@ -670,7 +667,7 @@ def run_mcx(args):
         cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
                          "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
-    tr = traffic_per_launch()
+    tr = CB_TRAFFIC_PER_LAUNCH
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

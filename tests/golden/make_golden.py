@@ -93,7 +93,9 @@ def traj():
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MCX_REFERENCE_ROOT")
+    if not ref:
+        sys.exit("usage: make_golden.py <MonteCarloX.jl checkout>  (or set MCX_REFERENCE_ROOT)")
     dos(ref)
     kat()
     traj()
