@@ -27,7 +27,8 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
   reweighting       log Z, <E>, <E^2> at 100 betas from a 4,194,305-bin ln g on the device
   batched_pt        256 3-D replicas in five ladders: persistent kernel against the plain form
   serving           40 Poisson jobs through the continuous-batching server (p50 / p99)
-  flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block
+  flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block, and a
+                    fixed-budget Wang-Landau stage 1 (ln f = 1, flatness 0.8, one walker per SM)
   msc64             the headline workload on the 64-spins-per-word layout
   general_graphs    4096^2 torus as IsingMatrix (Gaussian couplings) and as IsingGraph
 
@@ -304,6 +305,56 @@ def bench_flathist(torch, mcx, ctx, dev, nwalkers=None, L=1024):
     return {"workload": "bc2d_L1024_D1_muca_production_%d_walkers_1_sweep" % nwalkers, "walkers": nwalkers,
             "bins": 4 * N + 1, "attempts_per_ns": nwalkers * N / (ms * 1e6),
             "ns_per_attempt_per_walker": ms * 1e6 / N, "ms": ms}
+
+
+def bench_wang_landau(torch, mcx, ctx, dev, nwalkers=None, L=1024, sweeps=24, check_every=6):
+    """Wang-Landau stage 1 of the Blume-Capel configuration: L=1024, J=1, D=1, 4,194,305 bins,
+    ln f = 1, flatness 0.8, one walker per SM, each with its own FP64 ln g and int64 H (the
+    reference's WangLandau keeps one table per walker).  A fixed budget of `sweeps` sweeps,
+    the flatness test on every walker's histogram every `check_every` sweeps.  Reports the
+    sweep throughput, the cost of one flatness test of all walkers, and the flatness ratio
+    min H / mean H over the visited bins reached at the end of the budget (the stage needs
+    ratio >= 0.8 to end; a 1024^2 lattice needs far more sweeps than this budget)."""
+    from mcx import flathist as F
+    if nwalkers is None:
+        nwalkers = torch.cuda.get_device_properties(dev).multi_processor_count
+    N = L * L
+    bins = (-N, 1, 4 * N + 1)
+    walkers, algs = [], []
+    for i in range(nwalkers):
+        s = mcx.BlumeCapel([L, L], D=1.0, ctx=ctx)
+        mcx.init_(s, "random", rng=mcx.Philox(SEED, i))
+        walkers.append(s)
+        algs.append(F.WangLandau(mcx.Philox(SEED, i), F.WangLandauEnsemble(bins, logf=1.0, ctx=ctx)))
+    stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize()
+    sweep_ms = check_ms = 0.0
+    checks = 0
+    ratios = []
+    for k in range(sweeps // check_every):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        F.sweep_walkers_(walkers, algs, check_every)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep_ms += e0.elapsed_time(e1)
+        t0 = time.perf_counter()
+        ratios = [F.flatness(a.ensemble, 0.8)[1] for a in algs]
+        check_ms += (time.perf_counter() - t0) * 1e3
+        checks += 1
+    visited = int((algs[0].ensemble.histogram > 0).sum())
+    for s in walkers:
+        s.close()
+    for a in algs:
+        a.ensemble.close()
+    done = (sweeps // check_every) * check_every
+    return {"workload": "bc2d_L1024_D1_wang_landau_stage1_logf1_%d_walkers_%d_sweeps" % (nwalkers, done),
+            "walkers": nwalkers, "bins": 4 * N + 1, "sweeps": done,
+            "attempts_per_ns": nwalkers * N * done / (sweep_ms * 1e6), "ms_per_sweep": sweep_ms / done,
+            "flatness_check_ms_all_walkers": check_ms / max(checks, 1),
+            "flatness_ratio_mean": float(sum(ratios) / len(ratios)), "flatness_ratio_max": float(max(ratios)),
+            "visited_bins_walker0": visited, "stage_flat": bool(max(ratios) >= 0.8)}
 
 
 def bench_serve(mcx, ctx, njobs=40):
@@ -655,6 +706,7 @@ def run_mcx(args):
         pt_res = bench_pt(torch, mcx, ctx, dev, flush, max(3, args.steps // 2), 2)
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
+        fh_res["wang_landau_stage1"] = bench_wang_landau(torch, mcx, ctx, dev)
         msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
         graph_res = bench_graph(torch, mcx, ctx, flush, max(3, args.steps // 4), 3, min(args.cpu_seconds, 5.0),
                                 rank == 0 and not args.no_cpu_baseline)
