@@ -15,7 +15,9 @@ so L2 is flushed (256 MiB write) between timed steps.
              uploads the lattice from pinned host memory (mcx_set_spins) and reads
              the per-sweep (pair, spin, spin2) series back (mcx_sweep obs_series)
   roofline   the half-sweep kernel: algorithmic bytes 1.5*N per launch (reads both
-             colour arrays, writes its own) over the average launch time
+             colour arrays, writes its own) over the average launch time, against HBM; and
+             int_frac, the fraction of the integer-pipe roof (issue, ALU, FMA) that binds the
+             kernel, from its per-launch instruction counts and the sampled SM clock
   cpu_baseline  the oracle's sequential random-site mode (the reference's
              spin_flip! order, FP64 exp decisions), one chain per host core
 
@@ -93,6 +95,24 @@ def measured_peaks():
 # lattice, from one ncu capture (profiles/ising_cb_L4096_metropolis.md; ncu replays with flushed
 # caches, so this is a cold launch: both colour arrays read once)
 CB_TRAFFIC_PER_LAUNCH = 16798976
+
+# Per-launch integer-pipe work of the two headline kernels from one ncu capture each
+# (profiles/int_pipes_ising_cb_and_pt_persistent.md): warp instructions, ALU-pipe warp
+# instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
+CB_PIPES = {"warp_inst": 7263804, "alu_inst": 3933758, "fma_cycles": 7892832, "per": "launch"}
+PT_PIPES = {"warp_inst": 68099464 / 3, "alu_inst": 35368743 / 3, "fma_cycles": 70799920 / 3, "per": "sweep"}
+
+
+def int_roof(pipes, seconds, sm_mhz, nsm):
+    """Fractions of the integer roofs reached in `seconds` per launch (or sweep): issue
+    (1 warp instruction per cycle per sub-partition), ALU pipe (2 cycles per instruction) and
+    FMA pipe (the counted active cycles); int_frac is the largest, the pipe that binds."""
+    cycles = nsm * 4 * sm_mhz * 1e6 * seconds
+    issue = pipes["warp_inst"] / cycles
+    alu = 2.0 * pipes["alu_inst"] / cycles
+    fma = pipes["fma_cycles"] / cycles
+    return {"int_frac": max(issue, alu, fma), "issue_frac": issue, "alu_frac": alu, "fma_frac": fma,
+            "sm_mhz": sm_mhz, "counts_per": pipes["per"]}
 
 
 class ClockSampler:
@@ -202,6 +222,8 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
     ladders = [(L, set_betas(n, 0.20, 0.25, ":geometric")) for L, n in zip(PT_SIZES, PT_COUNTS)]
     pt = ParallelTempering(ladders, dim=3, seed=SEED, ctx=ctx)
     pt.init_(SEED)
+    default_schedule = pt.schedule[:3]
+    tuned = pt.autotune_("metropolis", exchange_every=1, sweeps=20)  # state restored; results unchanged
     sites = sum(L ** 3 * n for L, n in zip(PT_SIZES, PT_COUNTS))
     stream = torch.cuda.current_stream(dev)
     out = {}
@@ -234,6 +256,9 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "alg_bytes_per_sweep": 3 * sites, "kernel": "k_pt_persistent<3,false,true>"},
         "exchange_acceptance": float(pt.acceptance_rate()),
+        "schedule": {"default": list(default_schedule), "tuned": list(tuned[:3]),
+                     "tuned_ns_per_attempt": tuned[3],
+                     "fields": "blocks_per_sm, widest chunk (sites per thread), warp-split weights"},
     }
 
 
@@ -720,6 +745,10 @@ def run_mcx(args):
                "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
                          "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
     tr = CB_TRAFFIC_PER_LAUNCH
+    nsm = ctx_sms(torch)
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    if pt_res:
+        pt_res["roofline"].update(int_roof(PT_PIPES, pt_res["persistent"]["ms_per_sweep"] * 1e-3, sm_mhz, nsm))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -728,9 +757,10 @@ def run_mcx(args):
                    "layout": "int8 colour-split", "sweeps_per_step": S, "record": "E,M every sweep",
                    "l2": "flushed between timed steps (256 MiB write)", "replicas_per_gpu": 1,
                    "parallelism": "replicas"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                     "kernel": "k_ising_cb<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
+        "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
+                          "kernel": "k_ising_cb<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
+                         **int_roof(CB_PIPES, avg_launch_s, sm_mhz, nsm)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
         "gpu_launches": launches,

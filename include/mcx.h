@@ -302,6 +302,24 @@ MCX_API mcx_status mcx_pt_tau_int(mcx_pt* pt, int quantity, int64_t min_points, 
                                   double c, double* taus);
 /* Accepted spin flips of every replica during the last mcx_pt_run. */
 MCX_API mcx_status mcx_pt_replica_accepted(mcx_pt* pt, uint64_t* accepted);
+/* Schedule of the persistent form (results never depend on it): blocks_per_sm in
+ * 1..max_blocks_per_sm (0 = the maximum, the default), the co-resident blocks per SM of the
+ * cooperative launch; vcap 16, 8 or 4, the widest chunk of same-colour sites a thread sweeps
+ * (a replica takes the widest of 16, 8, 4 that divides its rows and is at most vcap; default
+ * 16); weights 0, 1 or 2, the per-site costs (16-, 8-, 4-site chunks) by which warps are
+ * handed to replicas: (1, 1.15, 1.4) (default), (1, 1, 1), (1, 1.3, 1.8).  No counterpart in
+ * the reference, whose replicas run on threads or MPI ranks. */
+MCX_API mcx_status mcx_pt_set_schedule(mcx_pt* pt, int32_t blocks_per_sm, int32_t vcap, int32_t weights);
+MCX_API mcx_status mcx_pt_get_schedule(const mcx_pt* pt, int32_t* blocks_per_sm, int32_t* vcap, int32_t* weights,
+                                       int32_t* max_blocks_per_sm);
+/* Times every schedule (blocks per SM x vcap 16 / 8 x weights) with `sweeps` persistent sweeps
+ * of the ladder's own state and keeps the fastest; the spins, cached observables, positions,
+ * stage and counters are restored afterwards, the caller's rng is not used, and later runs give
+ * the same results as without tuning.  Outputs may be NULL; ns_per_attempt is the chosen
+ * schedule's host-timed cost per spin-flip attempt. */
+MCX_API mcx_status mcx_pt_autotune(mcx_pt* pt, mcx_algorithm alg, int32_t exchange_every, int32_t sweeps,
+                                   int32_t* blocks_per_sm, int32_t* vcap, int32_t* weights,
+                                   double* ns_per_attempt);
 /* Poll limit of the grid barrier waits (default 2^24 polls of ~100 ns). */
 MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls);
 /* Failure-detection check: a bounded wait on a device flag that nothing sets;

@@ -20,6 +20,7 @@
 // on acceptance the two replicas swap ladder positions (their betas); the stage
 // toggles after every exchange step.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -463,6 +464,11 @@ struct mcx_pt {
     size_t lin_bytes = 0;
     std::vector<std::pair<void*, size_t>> allocs;
     long long spin_limit = 1ll << 24;
+    // schedule of the persistent form (results never depend on it)
+    int bps_max = 1;       // co-resident blocks per SM of the persistent kernel
+    int sched_bps = 1;     // blocks per SM in use
+    int sched_vcap = 16;   // widest chunk (sites per thread) a replica may use
+    int sched_weights = 0; // cost weights of the warp split (0, 1, 2)
 };
 
 namespace mcx {
@@ -482,6 +488,19 @@ static mcx_status pt_upload(mcx_pt* pt, T** dst, const std::vector<T>& v) {
     if (!v.empty()) MCX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     *dst = (T*)p;
     return MCX_OK;
+}
+
+// Replaces the device copy held in *dst (allocated by pt_upload) by a new upload of v.
+template <typename T>
+static mcx_status pt_reupload(mcx_pt* pt, T** dst, const std::vector<T>& v) {
+    for (auto it = pt->allocs.begin(); it != pt->allocs.end(); ++it)
+        if (it->first == (void*)*dst) {
+            dev_free(pt->ctx, it->first, it->second);
+            pt->allocs.erase(it);
+            break;
+        }
+    *dst = nullptr;
+    return pt_upload(pt, dst, v);
 }
 
 using PersistentFn = void (*)(const PTArgs);
@@ -519,7 +538,9 @@ static size_t pt_smem_persistent(const mcx_pt* pt, bool t32) {
 // one replica per phase.  Replica r gets k_r warps, handed out one at a time to the
 // replica whose cost per warp is largest (costs per site: 1.0 for 16-site rows chunks,
 // 1.15 for 8, 1.4 for 4), and its chunks are split evenly among them.
-static mcx_status pt_schedule(mcx_pt* pt, int grid) {
+static mcx_status pt_schedule(mcx_pt* pt, int grid, int weights) {
+    static const double kW[3][3] = {{1.0, 1.15, 1.4}, {1.0, 1.0, 1.0}, {1.0, 1.3, 1.8}};
+    const double* w = kW[weights];
     const int nwarps = grid * 8;
     const int R = pt->nrep;
     if (nwarps < R) return fail(MCX_ERR_INVALID_ARG, "%d replicas need at least as many resident warps", R);
@@ -529,7 +550,7 @@ static mcx_status pt_schedule(mcx_pt* pt, int grid) {
     for (int r = 0; r < R; ++r) {
         const PTReplica& P = pt->reps[r];
         nch[r] = P.cpr * P.rows;
-        cost[r] = (double)nch[r] * P.V * (P.V == 16 ? 1.0 : (P.V == 8 ? 1.15 : 1.4));
+        cost[r] = (double)nch[r] * P.V * (P.V == 16 ? w[0] : (P.V == 8 ? w[1] : w[2]));
         heap.push({cost[r], r});
     }
     for (int left = nwarps - R; left > 0 && !heap.empty();) {
@@ -555,8 +576,50 @@ static mcx_status pt_schedule(mcx_pt* pt, int grid) {
     PTTile idle;
     std::memset(&idle, 0, sizeof(idle));
     spans.resize(nwarps, idle);
-    MCX_CHECK(pt_upload(pt, &pt->d_spans, spans));
+    MCX_CHECK(pt_reupload(pt, &pt->d_spans, spans));
     pt->grid = grid;
+    return MCX_OK;
+}
+
+// Sites per thread of every replica: the widest of 16, 8, 4 that divides its colour rows and is
+// at most vcap (rows of a multiple of 4 sites always admit 4); the plain form's tiles of about
+// 4096 same-colour sites follow.  The random stream does not depend on the width.
+static mcx_status pt_set_widths(mcx_pt* pt, int vcap) {
+    pt->tiles.clear();
+    pt->rep_tile0.clear();
+    pt->rep_ntiles.clear();
+    for (int r = 0; r < pt->nrep; ++r) {
+        PTReplica& R = pt->reps[r];
+        R.V = (R.W % 16 == 0 && vcap >= 16) ? 16 : ((R.W % 8 == 0 && vcap >= 8) ? 8 : 4);
+        R.cpr = R.W / R.V;
+        R.m_cpr = roundup_recip((uint32_t)R.cpr);
+        const int nchunks = R.cpr * R.rows;
+        const int per = 256 * (16 / R.V);
+        pt->rep_tile0.push_back((int)pt->tiles.size());
+        for (int c = 0; c < nchunks; c += per) {
+            PTTile t;
+            std::memset(&t, 0, sizeof(t));
+            t.rep = r;
+            t.c_begin = c;
+            t.c_end = std::min(nchunks, c + per);
+            t.sites = (t.c_end - t.c_begin) * R.V;
+            pt->tiles.push_back(t);
+        }
+        pt->rep_ntiles.push_back((int)pt->tiles.size() - pt->rep_tile0.back());
+    }
+    MCX_CHECK(pt_reupload(pt, &pt->d_reps, pt->reps));
+    MCX_CHECK(pt_reupload(pt, &pt->d_tiles, pt->tiles));
+    return MCX_OK;
+}
+
+// Applies a schedule (validated by the caller).
+static mcx_status pt_apply_schedule(mcx_pt* pt, int bps, int vcap, int weights) {
+    MCX_CUDA(cudaStreamSynchronize(pt->ctx->stream));  // no launch may read the old descriptors
+    if (vcap != pt->sched_vcap) MCX_CHECK(pt_set_widths(pt, vcap));
+    MCX_CHECK(pt_schedule(pt, pt->ctx->num_sms * bps, weights));
+    pt->sched_bps = bps;
+    pt->sched_vcap = vcap;
+    pt->sched_weights = weights;
     return MCX_OK;
 }
 
@@ -831,7 +894,9 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
             bps = std::min(bps, b);
         }
         cudaFuncSetAttribute(k_pt_plain_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pt_smem(pt));
-        run(pt_schedule(pt, ctx->num_sms * bps));
+        pt->bps_max = bps;
+        pt->sched_bps = bps;
+        run(pt_schedule(pt, ctx->num_sms * bps, 0));
     }
     if (st == MCX_OK) {
         // all spins up, like the reference constructors
@@ -1056,6 +1121,100 @@ MCX_API mcx_status mcx_pt_set_exchange_counters(mcx_pt* pt, const uint64_t* step
 MCX_API mcx_status mcx_pt_set_wait_limit(mcx_pt* pt, int64_t polls) {
     if (!pt || polls < 1) return fail(MCX_ERR_INVALID_ARG, "bad argument");
     pt->spin_limit = polls;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_set_schedule(mcx_pt* pt, int32_t blocks_per_sm, int32_t vcap, int32_t weights) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (blocks_per_sm == 0) blocks_per_sm = pt->bps_max;
+    if (blocks_per_sm < 1 || blocks_per_sm > pt->bps_max)
+        return fail(MCX_ERR_INVALID_ARG, "blocks_per_sm must be in 1..%d", pt->bps_max);
+    if (vcap != 16 && vcap != 8 && vcap != 4) return fail(MCX_ERR_INVALID_ARG, "vcap must be 16, 8 or 4");
+    if (weights < 0 || weights > 2) return fail(MCX_ERR_INVALID_ARG, "weights must be 0, 1 or 2");
+    if (pt->ctx->num_sms * blocks_per_sm * 8 < pt->nrep)
+        return fail(MCX_ERR_INVALID_ARG, "%d replicas need at least as many resident warps", pt->nrep);
+    return pt_apply_schedule(pt, blocks_per_sm, vcap, weights);
+}
+
+MCX_API mcx_status mcx_pt_get_schedule(const mcx_pt* pt, int32_t* blocks_per_sm, int32_t* vcap, int32_t* weights,
+                                       int32_t* max_blocks_per_sm) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (blocks_per_sm) *blocks_per_sm = pt->sched_bps;
+    if (vcap) *vcap = pt->sched_vcap;
+    if (weights) *weights = pt->sched_weights;
+    if (max_blocks_per_sm) *max_blocks_per_sm = pt->bps_max;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_pt_autotune(mcx_pt* pt, mcx_algorithm alg, int32_t exchange_every, int32_t sweeps,
+                                   int32_t* blocks_per_sm, int32_t* vcap, int32_t* weights, double* ns_per_attempt) {
+    if (!pt) return fail(MCX_ERR_INVALID_ARG, "pt is NULL");
+    if (alg != MCX_METROPOLIS && alg != MCX_GLAUBER && alg != MCX_HEATBATH)
+        return fail(MCX_ERR_INVALID_ARG, "unknown algorithm");
+    if (exchange_every < 1 || sweeps < 1) return fail(MCX_ERR_INVALID_ARG, "exchange_every and sweeps must be >= 1");
+    mcx_ctx* ctx = pt->ctx;
+    cudaStream_t st = ctx->stream;
+    // snapshot of everything a run changes
+    const size_t sbytes = pt->arena_bytes + (size_t)pt->nrep * (2 * 8 + 4 + 8) + (size_t)pt->npos * 16 + 4;
+    void* snap = nullptr;
+    MCX_CHECK(dev_alloc(ctx, &snap, sbytes));
+    char* sp = (char*)snap;
+    struct Piece { void* dev; size_t n; };
+    const Piece pieces[] = {{pt->d_arena, pt->arena_bytes}, {pt->d_state, (size_t)pt->nrep * 16},
+                            {pt->d_pos, (size_t)pt->nrep * 4}, {pt->d_acc, (size_t)pt->nrep * 8},
+                            {pt->d_ex_steps, (size_t)pt->npos * 8}, {pt->d_ex_acc, (size_t)pt->npos * 8},
+                            {pt->d_stage, 4}};
+    size_t o = 0;
+    for (const Piece& q : pieces) {
+        MCX_CUDA(cudaMemcpyAsync(sp + o, q.dev, q.n, cudaMemcpyDeviceToDevice, st));
+        o += q.n;
+    }
+    const int rec = pt->record;
+    const int64_t slen = pt->series_len;
+    const int sbp = pt->series_by_pos;
+    pt->record = 0;
+    const int b0 = pt->sched_bps, v0 = pt->sched_vcap, w0 = pt->sched_weights;
+    double best = 1e300;
+    int bb = b0, bv = v0, bw = w0;
+    mcx_status stt = MCX_OK;
+    for (int b = 1; b <= pt->bps_max && stt == MCX_OK; ++b) {
+        if (ctx->num_sms * b * 8 < pt->nrep) continue;
+        for (int v : {16, 8})
+            for (int w = 0; w < 3 && stt == MCX_OK; ++w) {
+                stt = pt_apply_schedule(pt, b, v, w);
+                mcx_rng r{0x5eedull, 0, 0, 0};
+                if (stt == MCX_OK) stt = mcx_pt_run(pt, alg, &r, 2, exchange_every, MCX_PT_PERSISTENT, nullptr);
+                double tmin = 1e300;
+                for (int rep = 0; rep < 2 && stt == MCX_OK; ++rep) {
+                    const auto t0 = std::chrono::steady_clock::now();
+                    stt = mcx_pt_run(pt, alg, &r, sweeps, exchange_every, MCX_PT_PERSISTENT, nullptr);
+                    tmin = std::min(tmin, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+                }
+                if (stt == MCX_OK && tmin < best) {
+                    best = tmin;
+                    bb = b;
+                    bv = v;
+                    bw = w;
+                }
+            }
+    }
+    if (stt == MCX_OK) stt = pt_apply_schedule(pt, bb, bv, bw);
+    else pt_apply_schedule(pt, b0, v0, w0);
+    o = 0;
+    for (const Piece& q : pieces) {
+        cudaMemcpyAsync(q.dev, sp + o, q.n, cudaMemcpyDeviceToDevice, st);
+        o += q.n;
+    }
+    cudaStreamSynchronize(st);
+    dev_free(ctx, snap, sbytes);
+    pt->record = rec;
+    pt->series_len = slen;
+    pt->series_by_pos = sbp;
+    MCX_CHECK(stt);
+    if (blocks_per_sm) *blocks_per_sm = bb;
+    if (vcap) *vcap = bv;
+    if (weights) *weights = bw;
+    if (ns_per_attempt) *ns_per_attempt = best * 1e9 / ((double)pt->sites * sweeps);
     return MCX_OK;
 }
 

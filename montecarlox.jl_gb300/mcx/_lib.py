@@ -110,6 +110,9 @@ SIGNATURES = {
     "mcx_pt_exchange_counters": (C.c_int, [_P, _P, _P]),
     "mcx_pt_observables": (C.c_int, [_P, _P, _P]),
     "mcx_pt_replica_accepted": (C.c_int, [_P, _P]),
+    "mcx_pt_set_schedule": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "mcx_pt_get_schedule": (C.c_int, [_P, _i32p, _i32p, _i32p, _i32p]),
+    "mcx_pt_autotune": (C.c_int, [_P, C.c_int, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, _f64p]),
     "mcx_pt_set_wait_limit": (C.c_int, [_P, C.c_int64]),
     "mcx_pt_set_indices": (C.c_int, [_P, _P, C.c_int32]),
     "mcx_pt_set_exchange_counters": (C.c_int, [_P, _P, _P]),

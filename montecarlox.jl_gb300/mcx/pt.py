@@ -173,6 +173,28 @@ class ParallelTempering:
         self.rng.counter = rng.counter
         return out
 
+    # -- schedule of the persistent form (results never depend on it) ------------
+    def set_schedule(self, blocks_per_sm=0, vcap=16, weights=0):
+        """Blocks per SM (0 = the co-resident maximum), the widest chunk of sites per thread
+        (16, 8 or 4) and the warp-split cost weights (0, 1, 2) of the persistent kernel."""
+        _check(L.load().mcx_pt_set_schedule(self.handle, int(blocks_per_sm), int(vcap), int(weights)))
+
+    @property
+    def schedule(self):
+        """(blocks_per_sm, vcap, weights, max_blocks_per_sm)."""
+        v = [C.c_int32() for _ in range(4)]
+        _check(L.load().mcx_pt_get_schedule(self.handle, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def autotune_(self, alg="metropolis", exchange_every=1, sweeps=20):
+        """Time every schedule on the ladder's own state (restored afterwards) and keep the
+        fastest; returns (blocks_per_sm, vcap, weights, ns per attempt)."""
+        b, v, w = C.c_int32(), C.c_int32(), C.c_int32()
+        ns = C.c_double()
+        _check(L.load().mcx_pt_autotune(self.handle, _ALG[alg], int(exchange_every), int(sweeps), C.byref(b),
+                                        C.byref(v), C.byref(w), C.byref(ns)))
+        return b.value, v.value, w.value, ns.value
+
     def set_wait_limit(self, polls):
         _check(L.load().mcx_pt_set_wait_limit(self.handle, int(polls)))
 

@@ -289,3 +289,58 @@ def test_muca_update_configured_bins_against_numpy(gpu):
     bound = np.spacing(np.abs(logh)) + np.spacing(np.abs(ref))
     assert np.all(np.abs(got[m] - ref) <= bound)
     assert np.array_equal(got[~m], lnw[~m])
+
+
+# ------------------------------------------- schedules of the persistent ladder kernel --
+def test_pt_every_schedule_is_bit_exact(gpu):
+    """Every schedule the autotuner may choose (blocks per SM x widest chunk 16 / 8 / 4 x
+    warp-split weights) gives the oracle's run of the configured ladder bit for bit."""
+    from mcx.pt import ParallelTempering
+    ladders = _pt_ladders()
+    spins, oseries, opos, ostage, osteps, oacc = _pt_oracle()
+    probe = ParallelTempering(ladders, dim=3, seed=PT_SEED)
+    bmax = probe.schedule[3]
+    probe.close()
+    for b in range(1, bmax + 1):
+        for v in (16, 8, 4):
+            for w in (0, 1, 2):
+                pt = ParallelTempering(ladders, dim=3, seed=PT_SEED)
+                pt.set_schedule(b, v, w)
+                assert pt.schedule[:3] == (b, v, w)
+                pt.init_(PT_SEED)
+                series = pt.sweep_(PT_SWEEPS, alg="metropolis", exchange_every=1, record=True)
+                assert np.array_equal(series, oseries), (b, v, w)
+                assert np.array_equal(pt.positions, opos) and pt.stage == ostage, (b, v, w)
+                s, a = pt.counters()
+                assert np.array_equal(s, osteps) and np.array_equal(a, oacc), (b, v, w)
+                assert np.array_equal(pt.spins(255), spins[255]), (b, v, w)
+                pt.close()
+
+
+def test_pt_autotune_keeps_the_run(gpu):
+    """Autotuning times the schedules on the ladder's own state and restores it: a ladder
+    tuned between two runs ends exactly where an untuned twin ends."""
+    from mcx.pt import ParallelTempering
+    lad = [(16, [0.25, 0.24, 0.23, 0.22]), (24, [0.23, 0.22, 0.21]), (32, [0.22, 0.21])]
+    a = ParallelTempering(lad, dim=3, seed=9)
+    b = ParallelTempering(lad, dim=3, seed=9)
+    a.init_(9)
+    b.init_(9)
+    a.sweep_(3, alg="heatbath", exchange_every=2)
+    b.sweep_(3, alg="heatbath", exchange_every=2)
+    before = (a.positions.copy(), a.stage, a.counters(), a.observables(), [a.spins(r) for r in range(a.nrep)])
+    bb, vv, ww, ns = a.autotune_(alg="heatbath", exchange_every=2, sweeps=5)
+    assert a.schedule[:3] == (bb, vv, ww) and ns > 0
+    after = (a.positions, a.stage, a.counters(), a.observables(), [a.spins(r) for r in range(a.nrep)])
+    assert np.array_equal(before[0], after[0]) and before[1] == after[1]
+    for x, y in zip(before[2] + before[3], after[2] + after[3]):
+        assert np.array_equal(x, y)
+    for x, y in zip(before[4], after[4]):
+        assert np.array_equal(x, y)
+    sa = a.sweep_(4, alg="heatbath", exchange_every=2, record=True)
+    sb = b.sweep_(4, alg="heatbath", exchange_every=2, record=True)
+    assert np.array_equal(sa, sb) and np.array_equal(a.positions, b.positions)
+    for r in range(a.nrep):
+        assert np.array_equal(a.spins(r), b.spins(r))
+    a.close()
+    b.close()
