@@ -401,6 +401,33 @@ MCX_API mcx_status mcx_server_step(mcx_server* server, int32_t* active, int32_t*
 MCX_API mcx_status mcx_server_poll(mcx_server* server, uint64_t job_id, mcx_job_result* result);
 MCX_API mcx_status mcx_server_cancel(mcx_server* server, uint64_t job_id);
 MCX_API mcx_status mcx_server_get_stats(mcx_server* server, mcx_server_stats* stats);
+/* Switches a new server (before its first job is admitted) to the resident loop: one
+ * persistent kernel on the device runs a sweep of every admitted canonical job per round,
+ * takes newly admitted jobs from a mailbox in pinned host memory between rounds and
+ * publishes finished ones there, so mcx_server_step no longer launches sweeps or waits for
+ * the device: it admits jobs into a device arena of exactly hbm_budget bytes (allocated
+ * here; no device allocation or free happens while the loop runs), arms them, retires the
+ * finished ones, and launches the loop again when it has left for lack of work.
+ * Multicanonical jobs run as walker launches on their own stream beside the loop.  Results
+ * are those of the stepped server bit for bit.  Needs hbm_budget > 0 and max_jobs <= 256.
+ * Every device wait is bounded: a grid barrier gives up after the spin limit (the next step
+ * returns MCX_ERR_TIMEOUT and the affected jobs fail with it), and a round with nothing to
+ * run waits at most the idle limit before the kernel leaves. */
+MCX_API mcx_status mcx_server_start(mcx_server* server);
+/* Asks the resident loop to leave at the end of its round and waits at most timeout_s
+ * seconds (MCX_ERR_TIMEOUT); jobs still armed stay unfinished. */
+MCX_API mcx_status mcx_server_stop(mcx_server* server, double timeout_s);
+/* Bounds of the resident loop's waits: spin_polls per grid barrier (polls of ~0.1 us,
+ * default 2^24) and idle_polls (polls of ~1 us, default 100000) before it leaves when it
+ * has nothing to run; idle_polls * 100 < spin_polls. */
+MCX_API mcx_status mcx_server_set_loop_limits(mcx_server* server, int64_t spin_polls, int64_t idle_polls);
+/* Resident loop state: resident (started), running, status of the last launch (0 running,
+ * 1 stopped, 2 left idle, 3 barrier timeout), launches so far, rounds of the current launch. */
+MCX_API mcx_status mcx_server_loop_info(mcx_server* server, int32_t* resident, int32_t* running, uint32_t* status,
+                                        uint64_t* launches, uint64_t* rounds);
+/* The host side's bounded wait on a word the device (or another thread) writes: MCX_OK once
+ * *flag >= target, MCX_ERR_TIMEOUT after `polls` polls sleeping sleep_ns each.  Needs no GPU. */
+MCX_API mcx_status mcx_poll_flag(const uint32_t* flag, uint32_t target, int64_t polls, int64_t sleep_ns);
 
 /* ------------------------------------------------------- general graphs -- */
 /* Ising models on an arbitrary neighbour list: IsingGraph (one coupling J over a graph,

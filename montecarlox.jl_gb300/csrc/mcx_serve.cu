@@ -16,6 +16,7 @@
 // result does not depend on which other jobs share the device: identical alone and
 // in the mix.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -132,6 +133,237 @@ __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const S
     }
 }
 
+// ------------------------------------------------------------- resident loop --
+// In the resident mode one cooperative kernel keeps running while jobs come and go: every
+// round it runs one sweep (both colours) of every armed canonical job, block 0 then takes the
+// jobs the host has armed in a mailbox in pinned host memory and prepares the next round, and
+// after the round's last barrier it publishes the jobs that finished.  The host only admits,
+// arms and retires jobs; it never waits for the kernel.  Every wait is bounded: the grid
+// barriers by spin_limit polls (then the kernel leaves with kLoopTimeout), and a round with no
+// job to run by idle_limit polls of about 1 us (then the kernel leaves with kLoopIdle and the
+// host launches it again when work arrives).
+constexpr int kSrvSlots = 256;
+static_assert(sizeof(SrvJobDev) % 8 == 0, "SrvJobDev is copied in 8-byte words");
+enum LoopStatus : unsigned { kLoopRunning = 0, kLoopStopped = 1, kLoopIdle = 2, kLoopTimeout = 3 };
+
+struct SrvSlotDesc {
+    SrvJobDev job;  // series: the job's per-sweep rows (sweep t at 3t); todo: its sweeps
+    unsigned long long table[kMaxTable];
+};
+
+// Shared by host and device (pinned, mapped).  The host writes a slot's descriptor, then its
+// generation, then bumps arm_seq; the device reads arm_seq, then the generations and slots.
+struct SrvMailbox {
+    unsigned int arm_seq;                 // host: bumped after arming or cancelling slots
+    unsigned int stop;                    // host: leave the loop at the end of the round
+    unsigned int status;                  // device: LoopStatus of the launch
+    unsigned int pad;
+    unsigned long long rounds;            // device: rounds run by the current launch
+    unsigned int gen[kSrvSlots];          // host: generation of the job armed in the slot (0: none)
+    unsigned int cancel[kSrvSlots];       // host: generation to drop before it ends
+    unsigned int finished[kSrvSlots];     // device: generation whose run ended (done or dropped)
+    unsigned int pad2[kSrvSlots];
+    unsigned long long done[kSrvSlots];   // device: sweeps completed by the slot's job
+    SrvSlotDesc slots[kSrvSlots];
+};
+
+struct SrvRound {
+    int n, exit;
+    int slot[kSrvSlots];
+    int per[kSrvSlots];                   // chunks per tile of the slot's job
+    int tile0[kSrvSlots + 1];             // first tile of each entry; tile0[n] = tiles of the round
+    unsigned long long t[kSrvSlots];      // sweep of each job in this round
+};
+
+struct SrvLoop {
+    SrvJobDev jobs[kSrvSlots];
+    unsigned long long tables[kSrvSlots][kMaxTable];
+    unsigned int gen[kSrvSlots];          // generation taken into each slot
+    int fin[kSrvSlots];                   // slots whose job ended in this round
+    int nfin;
+    unsigned int seen_seq;
+    unsigned int reason;                  // exit reason (LoopStatus)
+    unsigned int bar[4];                  // grid barrier: arrivals, generation, error
+    SrvRound round[2];
+};
+
+// Block 0, after its share of the round: the next round's job list (every job one sweep on,
+// jobs that ended or were cancelled out), newly armed jobs copied in from the mailbox, and,
+// when there is nothing to run, a bounded wait for work.
+__device__ void srv_leader(SrvLoop* L, volatile SrvMailbox* mb, long long r, long long idle_limit) {
+    __shared__ int s_n, s_seq_changed, s_stop;
+    __shared__ unsigned s_seq;
+    const SrvRound* R = &L->round[r & 1];
+    SrvRound* X = &L->round[(r + 1) & 1];
+    if (threadIdx.x == 0) {
+        int n = 0, nf = 0;
+        for (int k = 0; k < R->n; ++k) {
+            const int sl = R->slot[k];
+            const unsigned long long t1 = R->t[k] + 1;
+            if (t1 >= (unsigned long long)L->jobs[sl].todo || mb->cancel[sl] == L->gen[sl]) {
+                L->fin[nf++] = sl;
+                continue;
+            }
+            X->slot[n] = sl;
+            X->t[n] = t1;
+            ++n;
+        }
+        L->nfin = nf;
+        s_n = n;
+    }
+    __syncthreads();
+    for (long long polls = 0;; ++polls) {
+        if (threadIdx.x == 0) {
+            s_seq = mb->arm_seq;
+            s_stop = mb->stop;
+            __threadfence_system();
+            s_seq_changed = s_seq != L->seen_seq;
+        }
+        __syncthreads();
+        if (s_seq_changed) {
+            for (int sl = threadIdx.x; sl < kSrvSlots; sl += blockDim.x) {
+                const unsigned g = mb->gen[sl];
+                if (g == 0u || g == L->gen[sl]) continue;
+                L->gen[sl] = g;
+                if (mb->cancel[sl] == g) {  // cancelled before it started
+                    __threadfence_system();
+                    mb->finished[sl] = g;
+                    continue;
+                }
+                const volatile unsigned long long* src = reinterpret_cast<const volatile unsigned long long*>(&mb->slots[sl]);
+                unsigned long long* dj = reinterpret_cast<unsigned long long*>(&L->jobs[sl]);
+                for (int w = 0; w < (int)(sizeof(SrvJobDev) / 8); ++w) dj[w] = src[w];
+                const volatile unsigned long long* st = src + sizeof(SrvJobDev) / 8;
+                for (int w = 0; w < kMaxTable; ++w) L->tables[sl][w] = st[w];
+                const int k = atomicAdd(&s_n, 1);
+                X->slot[k] = sl;
+                X->t[k] = 0;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) L->seen_seq = s_seq;
+        }
+        __syncthreads();
+        if (s_n > 0 || s_stop || polls >= idle_limit) break;
+        if (threadIdx.x == 0) __nanosleep(1000);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int n = s_n;
+        int acc = 0;
+        for (int k = 0; k < n; ++k) {
+            const SrvJobDev& J = L->jobs[X->slot[k]];
+            const int per = 256 * (16 / J.V);
+            const int nch = J.cpr * J.rows;
+            X->per[k] = per;
+            X->tile0[k] = acc;
+            acc += (nch + per - 1) / per;
+        }
+        X->tile0[n] = acc;
+        X->n = n;
+        X->exit = (s_stop || n == 0) ? 1 : 0;
+        L->reason = s_stop ? kLoopStopped : (n == 0 ? kLoopIdle : kLoopRunning);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mbp, long long spin_limit,
+                                                  long long idle_limit) {
+    volatile SrvMailbox* mb = mbp;
+    __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
+    __shared__ unsigned s_bgen;
+    if (threadIdx.x == 0) s_bgen = ld_acquire(&L->bar[1]);
+    __syncthreads();
+    unsigned gen = s_bgen;
+    for (long long r = 0;; ++r) {
+        const SrvRound* R = &L->round[r & 1];
+        if (R->exit) break;
+        const int n = R->n;
+        const int total = R->tile0[n];
+        for (int colour = 0; colour < 2; ++colour) {
+            int loaded = -1;
+            for (int ti = blockIdx.x; ti < total; ti += gridDim.x) {
+                int lo = 0, hi = n - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (R->tile0[mid] <= ti) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int sl = R->slot[lo];
+                const SrvJobDev J = L->jobs[sl];
+                if (sl != loaded) {
+                    __syncthreads();
+                    for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
+                        const unsigned long long x = L->tables[sl][i];
+                        s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
+                    }
+                    __syncthreads();
+                    loaded = sl;
+                }
+                SrvTile tl;
+                tl.job = sl;
+                tl.c_begin = (ti - R->tile0[lo]) * R->per[lo];
+                tl.c_end = min(J.cpr * J.rows, tl.c_begin + R->per[lo]);
+                tl.pad = 0;
+                const unsigned long long t = R->t[lo];
+                int nacc = 0, a1 = 0, a2 = 0, a3 = 0;
+                const int key = J.V * 4 + J.model * 2 + J.hb;
+                switch (key) {
+                    case 16 * 4 + 0: srv_tile<16, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 16 * 4 + 1: srv_tile<16, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 16 * 4 + 2: srv_tile<16, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 16 * 4 + 3: srv_tile<16, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 8 * 4 + 0: srv_tile<8, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 8 * 4 + 1: srv_tile<8, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 8 * 4 + 2: srv_tile<8, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 8 * 4 + 3: srv_tile<8, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 4 * 4 + 0: srv_tile<4, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 4 * 4 + 1: srv_tile<4, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    case 4 * 4 + 2: srv_tile<4, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    default: srv_tile<4, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                }
+                long long dP, dM, dQ;
+                if (J.model == 0) {
+                    ising_deltas<4>(nacc, a1, a2, dP, dM);
+                    dQ = 0;
+                } else {
+                    dP = a1;
+                    dM = a2;
+                    dQ = a3;
+                }
+                long long v[4] = {dP, dM, dQ, (long long)nacc};
+                unsigned long long* const dst[4] = {(unsigned long long*)&J.series[3 * t],
+                                                    (unsigned long long*)&J.series[3 * t + 1],
+                                                    (unsigned long long*)&J.series[3 * t + 2], J.acc};
+                block_add_atomic<4>(v, dst);
+            }
+            if (colour == 1 && blockIdx.x == 0) srv_leader(L, mb, r, idle_limit);
+            if (!grid_sync(L->bar, gridDim.x, gen, spin_limit)) {
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    __threadfence_system();
+                    mb->status = kLoopTimeout;
+                }
+                return;
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            // the jobs that ended in this round are complete on the device: publish them
+            const SrvRound* X = &L->round[(r + 1) & 1];
+            __threadfence_system();
+            for (int k = 0; k < L->nfin; ++k) {
+                const int sl = L->fin[k];
+                mb->done[sl] = (unsigned long long)L->jobs[sl].todo;
+                mb->finished[sl] = L->gen[sl];
+            }
+            for (int k = 0; k < X->n; ++k) mb->done[X->slot[k]] = X->t[k];
+            mb->rounds = (unsigned long long)r + 1;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        __threadfence_system();
+        mb->status = L->reason;
+    }
+}
+
 }  // namespace mcx
 
 using namespace mcx;
@@ -156,6 +388,12 @@ struct SrvJob {
     Table table{};
     int inflight = 0;       // sweeps of the Multicanonical launch in flight (0: none)
     bool cancel_req = false;
+    // resident mode
+    size_t pool_off = 0, pool_bytes = 0;  // the job's block of the server arena
+    int slot = -1;                        // mailbox slot while armed
+    unsigned gen = 0;                     // generation armed in the slot
+    cudaEvent_t ready = nullptr;          // initialisation done on the admin stream
+    bool armed = false;
 };
 
 double now_s(std::chrono::steady_clock::time_point t0) {
@@ -192,6 +430,24 @@ struct mcx_server {
     std::vector<FHWalker> mwalk;
     std::vector<SrvJob*> mjobs;
     std::vector<SrvJob*> deferred;  // finished jobs whose memory is freed when no walker launch runs
+    // resident mode (mcx_server_start): one persistent kernel sweeps the canonical jobs
+    bool resident = false;
+    mcx_ctx* admin = nullptr;          // its own stream for initialisation and results
+    cudaStream_t lstream = nullptr;    // the loop kernel's stream
+    cudaEvent_t ldone = nullptr;
+    bool lrunning = false;
+    int loop_grid = 0;
+    uint64_t loop_launches = 0;
+    unsigned last_status = 0;
+    long long spin_limit = 1ll << 24, idle_limit = 100000;
+    SrvMailbox* mb = nullptr;          // pinned, mapped
+    SrvMailbox* mb_dev = nullptr;
+    SrvLoop* d_loop = nullptr;
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    std::map<size_t, size_t> free_blocks;  // offset -> bytes, coalesced
+    std::vector<SrvJob*> slot_job;
+    unsigned gen_next = 1;
 };
 
 namespace {
@@ -222,6 +478,91 @@ uint64_t job_bytes(const mcx_job& j) {
     return b;
 }
 
+// Bytes of a job's block in the resident arena: colour arrays, staging, (state, counter),
+// per-sweep rows, and ln g / H for Multicanonical jobs, each piece 256-byte aligned.
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+size_t carve_bytes(const mcx_job& j) {
+    const size_t N = (size_t)j.L[0] * j.L[1];
+    size_t b = 2 * up256(N / 2) + up256(N) + 256 + up256((size_t)j.nsweeps * 24);
+    if (j.kind == MCX_JOB_MULTICANONICAL) b += 2 * up256((size_t)j.nbins * 8);
+    return b;
+}
+
+bool pool_alloc(mcx_server* s, size_t bytes, size_t* off) {
+    for (auto it = s->free_blocks.begin(); it != s->free_blocks.end(); ++it)
+        if (it->second >= bytes) {
+            *off = it->first;
+            const size_t rest = it->second - bytes;
+            const size_t o2 = it->first + bytes;
+            s->free_blocks.erase(it);
+            if (rest) s->free_blocks[o2] = rest;
+            return true;
+        }
+    return false;
+}
+
+void pool_free(mcx_server* s, size_t off, size_t bytes) {
+    auto it = s->free_blocks.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != s->free_blocks.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        s->free_blocks.erase(nx);
+    }
+    if (it != s->free_blocks.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            s->free_blocks.erase(it);
+        }
+    }
+}
+
+// A lattice (and flat-histogram tables) laid out in the job's arena block, on the admin
+// context: the library's lattice routines run on it unchanged and never allocate.
+void carve_job(mcx_server* s, SrvJob* j) {
+    const mcx_job& sp = j->spec;
+    char* b = s->arena + j->pool_off;
+    const size_t N = (size_t)sp.L[0] * sp.L[1];
+    mcx_lattice* L = new mcx_lattice();
+    L->ctx = s->admin;
+    L->model = (mcx_model)sp.model;
+    L->layout = MCX_LAYOUT_INT8;
+    L->dim = 2;
+    L->L[0] = sp.L[0];
+    L->L[1] = sp.L[1];
+    L->L[2] = 1;
+    L->J = sp.J;
+    L->D = sp.D;
+    L->h = sp.h;
+    L->N = (int64_t)N;
+    L->W = sp.L[0] / 2;
+    L->rows = sp.L[1];
+    L->d_col[0] = (int8_t*)b;
+    b += up256(N / 2);
+    L->d_col[1] = (int8_t*)b;
+    b += up256(N / 2);
+    L->d_lin = (int8_t*)b;
+    b += up256(N);
+    L->d_state = (int64_t*)b;
+    L->d_acc = (unsigned long long*)(b + 32);
+    b += 256;
+    L->d_series = (int64_t*)b;
+    L->series_cap = sp.nsweeps;
+    b += up256((size_t)sp.nsweeps * 24);
+    j->lat = L;
+    if (sp.kind == MCX_JOB_MULTICANONICAL) {
+        mcx_flathist* F = new mcx_flathist();
+        F->ctx = s->admin;
+        F->start = sp.bin_start;
+        F->step = sp.bin_step;
+        F->nbins = sp.nbins;
+        F->d_lnw = (double*)b;
+        b += up256((size_t)sp.nbins * 8);
+        F->d_H = (unsigned long long*)b;
+        j->fh = F;
+    }
+}
+
 mcx_status validate(const mcx_job& j) {
     if (j.model != MCX_ISING && j.model != MCX_BLUME_CAPEL) return fail(MCX_ERR_INVALID_ARG, "job: unknown model");
     if (j.dim != 2) return fail(MCX_ERR_INVALID_ARG, "job: the serving loop runs 2-D lattices");
@@ -245,8 +586,17 @@ mcx_status validate(const mcx_job& j) {
 }
 
 void release(mcx_server* s, SrvJob* j) {
-    if (j->lat) mcx_lattice_destroy(j->lat);
-    if (j->fh) mcx_flathist_destroy(j->fh);
+    if (s->resident) {
+        delete j->lat;  // carved from the arena: no device memory of its own
+        delete j->fh;
+        if (j->pool_bytes) pool_free(s, j->pool_off, j->pool_bytes);
+        j->pool_bytes = 0;
+        if (j->ready) cudaEventDestroy(j->ready);
+        j->ready = nullptr;
+    } else {
+        if (j->lat) mcx_lattice_destroy(j->lat);
+        if (j->fh) mcx_flathist_destroy(j->fh);
+    }
     j->lat = nullptr;
     j->fh = nullptr;
     s->used -= j->bytes;
@@ -254,24 +604,37 @@ void release(mcx_server* s, SrvJob* j) {
 
 mcx_status admit(mcx_server* s, SrvJob* j) {
     const mcx_job& sp = j->spec;
-    const int32_t L[3] = {sp.L[0], sp.L[1], 1};
-    MCX_CHECK(mcx_lattice_create(s->ctx, (mcx_model)sp.model, 2, L, MCX_LAYOUT_INT8, sp.J, sp.D, sp.h, &j->lat));
+    if (s->resident) {
+        carve_job(s, j);
+    } else {
+        const int32_t L[3] = {sp.L[0], sp.L[1], 1};
+        MCX_CHECK(mcx_lattice_create(s->ctx, (mcx_model)sp.model, 2, L, MCX_LAYOUT_INT8, sp.J, sp.D, sp.h, &j->lat));
+    }
     s->used += j->bytes;
     s->peak = std::max(s->peak, s->used);
+    cudaStream_t st0 = j->lat->ctx->stream;
     MCX_CHECK(mcx_init_random(j->lat, sp.seed, sp.stream));
     MCX_CHECK(ensure_series(j->lat, sp.nsweeps));
-    MCX_CUDA(cudaMemsetAsync(j->lat->d_series, 0, (size_t)sp.nsweeps * 24, s->ctx->stream));
-    MCX_CUDA(cudaMemsetAsync(j->lat->d_acc, 0, 8, s->ctx->stream));
+    MCX_CUDA(cudaMemsetAsync(j->lat->d_series, 0, (size_t)sp.nsweeps * 24, st0));
+    MCX_CUDA(cudaMemsetAsync(j->lat->d_acc, 0, 8, st0));
     if (sp.kind == MCX_JOB_CANONICAL) {
         MCX_CHECK(build_table(j->lat, (mcx_algorithm)sp.alg, sp.beta, &j->table));
+        if (s->resident) {
+            MCX_CUDA(cudaEventCreateWithFlags(&j->ready, cudaEventDisableTiming));
+            MCX_CUDA(cudaEventRecord(j->ready, st0));
+        }
     } else {
-        MCX_CHECK(mcx_flathist_create(s->ctx, sp.bin_start, sp.bin_step, sp.nbins, &j->fh));
+        if (s->resident) {
+            MCX_CUDA(cudaMemsetAsync(j->fh->d_lnw, 0, (size_t)sp.nbins * 8, st0));
+            MCX_CUDA(cudaMemsetAsync(j->fh->d_H, 0, (size_t)sp.nbins * 8, st0));
+        } else {
+            MCX_CHECK(mcx_flathist_create(s->ctx, sp.bin_start, sp.bin_step, sp.nbins, &j->fh));
+        }
         if (!j->lnw0.empty())
-            MCX_CUDA(cudaMemcpyAsync(j->fh->d_lnw, j->lnw0.data(), j->lnw0.size() * 8, cudaMemcpyHostToDevice,
-                                     s->ctx->stream));
+            MCX_CUDA(cudaMemcpyAsync(j->fh->d_lnw, j->lnw0.data(), j->lnw0.size() * 8, cudaMemcpyHostToDevice, st0));
         long long st[3];
-        MCX_CUDA(cudaMemcpyAsync(st, j->lat->d_state, 24, cudaMemcpyDeviceToHost, s->ctx->stream));
-        MCX_CUDA(cudaStreamSynchronize(s->ctx->stream));
+        MCX_CUDA(cudaMemcpyAsync(st, j->lat->d_state, 24, cudaMemcpyDeviceToHost, st0));
+        MCX_CUDA(cudaStreamSynchronize(st0));
         j->P = st[0];
         j->M = st[1];
         j->Q = st[2];
@@ -283,7 +646,7 @@ mcx_status admit(mcx_server* s, SrvJob* j) {
 
 mcx_status finish(mcx_server* s, SrvJob* j) {
     const mcx_job& sp = j->spec;
-    mcx_ctx* ctx = s->ctx;
+    mcx_ctx* ctx = j->lat->ctx;  // the server's context, or in the resident mode its admin context
     if (sp.kind == MCX_JOB_CANONICAL) {
         MCX_CHECK(finish_series(j->lat, sp.nsweeps));
         unsigned long long acc = 0;
@@ -412,8 +775,8 @@ mcx_status launch_muca(mcx_server* s) {
         MCX_CUDA(cudaStreamCreateWithFlags(&s->mstream, cudaStreamNonBlocking));
         MCX_CUDA(cudaEventCreateWithFlags(&s->mdone, cudaEventDisableTiming));
     }
-    // the walkers' lattices were initialised on the context stream
-    MCX_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    // the walkers' lattices were initialised on the context (or admin) stream
+    MCX_CUDA(cudaStreamSynchronize(s->resident ? s->admin->stream : s->ctx->stream));
     MCX_CHECK(grow(s, &s->d_walkers, &s->cap_walkers, s->mwalk.size()));
     MCX_CUDA(cudaMemcpyAsync(s->d_walkers, s->mwalk.data(), s->mwalk.size() * sizeof(FHWalker), cudaMemcpyHostToDevice,
                              s->mstream));
@@ -423,8 +786,171 @@ mcx_status launch_muca(mcx_server* s) {
     return MCX_OK;
 }
 
+// ---------------------------------------------------------------- resident pump --
+unsigned vload(const unsigned* p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
+void vstore(unsigned* p, unsigned v) { __atomic_store_n(p, v, __ATOMIC_RELEASE); }
+
+// Writes the job's descriptor into a free mailbox slot, then its generation, then bumps the
+// arm sequence the loop kernel watches.
+mcx_status arm(mcx_server* s, SrvJob* j) {
+    int sl = -1;
+    for (int k = 0; k < kSrvSlots; ++k)
+        if (!s->slot_job[k]) {
+            sl = k;
+            break;
+        }
+    if (sl < 0) return MCX_OK;  // every slot busy: armed at a later step
+    const mcx_lattice* L = j->lat;
+    SrvSlotDesc& d = s->mb->slots[sl];
+    std::memset(&d, 0, sizeof(d));
+    d.job.col[0] = L->d_col[0];
+    d.job.col[1] = L->d_col[1];
+    d.job.series = (long long*)L->d_series;
+    d.job.acc = L->d_acc;
+    d.job.W = (int)L->W;
+    d.job.Ly = (int)L->L[1];
+    d.job.rows = (int)L->rows;
+    d.job.V = L->W % 16 == 0 ? 16 : (L->W % 8 == 0 ? 8 : 4);
+    d.job.cpr = d.job.W / d.job.V;
+    d.job.model = L->model == MCX_ISING ? 0 : 1;
+    d.job.hb = j->spec.alg == MCX_HEATBATH;
+    d.job.todo = (int)j->spec.nsweeps;
+    d.job.k0 = (uint32_t)j->spec.seed;
+    d.job.k1 = (uint32_t)(j->spec.seed >> 32);
+    d.job.stream = j->spec.stream;
+    d.job.m_cpr = d.job.cpr <= 1 ? 0u : (uint32_t)(((1ull << 32) + d.job.cpr - 1) / d.job.cpr);
+    d.job.t0 = 0;
+    for (int i = 0; i < kMaxTable; ++i) d.table[i] = i < j->table.n ? j->table.thr[i] : 0ull;
+    j->gen = s->gen_next++;
+    if (s->gen_next == 0) s->gen_next = 1;
+    j->slot = sl;
+    j->armed = true;
+    s->slot_job[sl] = j;
+    vstore(&s->mb->cancel[sl], 0u);
+    vstore(&s->mb->finished[sl], 0u);
+    s->mb->done[sl] = 0;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    vstore(&s->mb->gen[sl], j->gen);
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    vstore(&s->mb->arm_seq, s->mb->arm_seq + 1);
+    return MCX_OK;
+}
+
+mcx_status launch_loop(mcx_server* s) {
+    MCX_CUDA(cudaMemsetAsync(s->d_loop, 0, sizeof(SrvLoop), s->lstream));
+    vstore(&s->mb->stop, 0u);
+    vstore(&s->mb->status, kLoopRunning);
+    SrvLoop* L = s->d_loop;
+    SrvMailbox* mb = s->mb_dev;
+    long long spin = s->spin_limit, idle = s->idle_limit;
+    void* args[] = {&L, &mb, &spin, &idle};
+    MCX_CUDA(cudaLaunchCooperativeKernel((const void*)k_srv_loop, dim3(s->loop_grid), dim3(256), args, 0,
+                                         s->lstream));
+    MCX_CUDA(cudaEventRecord(s->ldone, s->lstream));
+    count_launch(s->ctx);
+    s->loop_launches += 1;
+    s->lrunning = true;
+    return MCX_OK;
+}
+
+mcx_status step_resident(mcx_server* s) {
+    // 1. the loop kernel: has it left (idle, stopped, or a barrier that gave up)?
+    if (s->lrunning) {
+        const cudaError_t q = cudaEventQuery(s->ldone);
+        if (q == cudaSuccess) {
+            s->lrunning = false;
+            s->last_status = vload(&s->mb->status);
+            if (s->last_status == kLoopTimeout) {
+                for (SrvJob* j : s->active)
+                    if (j->armed) j->status = MCX_ERR_TIMEOUT;
+                return fail(MCX_ERR_TIMEOUT, "serving loop: a grid barrier wait exceeded its limit");
+            }
+        } else if (q != cudaErrorNotReady) {
+            return cuda_fail(q, "serving loop");
+        }
+    }
+    // 2. jobs the loop has finished (or dropped after a cancel)
+    std::vector<SrvJob*> still;
+    for (SrvJob* j : s->active) {
+        if (j->armed && vload(&s->mb->finished[j->slot]) == j->gen) {
+            s->slot_job[j->slot] = nullptr;
+            j->armed = false;
+            vstore(&s->mb->gen[j->slot], 0u);
+            if (j->cancel_req) {
+                j->state = JOB_CANCELLED;
+                j->t_finish = now_s(s->t0);
+                release(s, j);
+            } else {
+                j->done = j->spec.nsweeps;
+                MCX_CHECK(finish(s, j));
+            }
+            continue;
+        }
+        still.push_back(j);
+    }
+    s->active.swap(still);
+    // 3. admission in arrival order, by slots, HBM budget and room in the arena
+    while (!s->pending.empty() && (int)s->active.size() < s->max_jobs) {
+        SrvJob* j = s->pending.front();
+        if (s->budget && s->used + j->bytes > s->budget) break;
+        if (!pool_alloc(s, carve_bytes(j->spec), &j->pool_off)) break;
+        j->pool_bytes = carve_bytes(j->spec);
+        s->pending.pop_front();
+        mcx_status st = admit(s, j);
+        if (st != MCX_OK) {
+            j->status = st;
+            j->state = JOB_FAILED;
+            j->t_finish = now_s(s->t0);
+            release(s, j);
+            continue;
+        }
+        s->active.push_back(j);
+    }
+    // 4. initialised canonical jobs are armed for the loop
+    bool waiting = false;
+    for (SrvJob* j : s->active) {
+        if (j->spec.kind != MCX_JOB_CANONICAL || j->armed) continue;
+        const cudaError_t q = cudaEventQuery(j->ready);
+        if (q == cudaSuccess) MCX_CHECK(arm(s, j));
+        else if (q != cudaErrorNotReady) return cuda_fail(q, "job initialisation");
+    }
+    for (SrvJob* j : s->active)
+        if (j->armed) waiting = true;
+    // 5. Multicanonical jobs on the walker stream
+    MCX_CHECK(collect_muca(s));
+    if (!s->minflight) {
+        for (SrvJob* j : s->deferred) release(s, j);
+        s->deferred.clear();
+    }
+    MCX_CHECK(launch_muca(s));
+    // 6. the loop runs while armed jobs wait for it
+    if (waiting && !s->lrunning) MCX_CHECK(launch_loop(s));
+    s->iterations += 1;
+    if (!s->active.empty()) std::this_thread::sleep_for(std::chrono::microseconds(20));  // a pump, not a spin
+    return MCX_OK;
+}
+
+// Bounded host wait for the loop kernel to leave.
+mcx_status wait_loop(mcx_server* s, double seconds) {
+    const auto t0 = std::chrono::steady_clock::now();
+    while (s->lrunning) {
+        const cudaError_t q = cudaEventQuery(s->ldone);
+        if (q == cudaSuccess) {
+            s->lrunning = false;
+            s->last_status = vload(&s->mb->status);
+            break;
+        }
+        if (q != cudaErrorNotReady) return cuda_fail(q, "serving loop");
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > seconds)
+            return fail(MCX_ERR_TIMEOUT, "the serving loop did not stop within %.1f s", seconds);
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+    return MCX_OK;
+}
+
 // one scheduling iteration
 mcx_status step(mcx_server* s) {
+    if (s->resident) return step_resident(s);
     mcx_ctx* ctx = s->ctx;
     // 1. admission in arrival order, by slots and HBM budget
     while (!s->pending.empty() && (int)s->active.size() < s->max_jobs) {
@@ -542,6 +1068,12 @@ MCX_API mcx_status mcx_server_create(mcx_ctx* ctx, uint64_t hbm_budget, int32_t 
 
 MCX_API mcx_status mcx_server_destroy(mcx_server* s) {
     if (!s) return MCX_OK;
+    if (s->resident && s->lrunning) {
+        vstore(&s->mb->stop, 1u);
+        wait_loop(s, 30.0);
+    }
+    if (s->lstream) cudaStreamSynchronize(s->lstream);
+    if (s->admin) cudaStreamSynchronize(s->admin->stream);
     cudaStreamSynchronize(s->ctx->stream);
     if (s->mstream) cudaStreamSynchronize(s->mstream);
     s->minflight = false;
@@ -555,6 +1087,14 @@ MCX_API mcx_status mcx_server_destroy(mcx_server* s) {
     dev_free(s->ctx, s->d_walkers, s->cap_walkers * sizeof(FHWalker));
     if (s->mdone) cudaEventDestroy(s->mdone);
     if (s->mstream) cudaStreamDestroy(s->mstream);
+    if (s->resident) {
+        if (s->d_loop) dev_free(s->ctx, s->d_loop, sizeof(SrvLoop));
+        if (s->arena) dev_free(s->ctx, s->arena, s->arena_bytes);
+        if (s->mb) cudaFreeHost(s->mb);
+        if (s->ldone) cudaEventDestroy(s->ldone);
+        if (s->lstream) cudaStreamDestroy(s->lstream);
+        if (s->admin) mcx_ctx_destroy(s->admin);
+    }
     delete s;
     return MCX_OK;
 }
@@ -604,7 +1144,7 @@ MCX_API mcx_status mcx_server_poll(mcx_server* s, uint64_t job_id, mcx_job_resul
     res->submit_s = j->t_submit;
     res->admit_s = j->t_admit;
     res->finish_s = j->t_finish;
-    res->sweeps_done = j->done;
+    res->sweeps_done = j->armed ? (int64_t)s->mb->done[j->slot] : j->done;
     if (j->state == JOB_PENDING || j->state == JOB_ACTIVE) return MCX_ERR_NOT_READY;
     return MCX_OK;
 }
@@ -621,6 +1161,22 @@ MCX_API mcx_status mcx_server_cancel(mcx_server* s, uint64_t job_id) {
             j->cancel_req = true;
             return MCX_OK;
         }
+        if (j->armed) {  // the loop drops it at the end of a round; retired at a later step
+            j->cancel_req = true;
+            vstore(&s->mb->cancel[j->slot], j->gen);
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            vstore(&s->mb->arm_seq, s->mb->arm_seq + 1);
+            return MCX_OK;
+        }
+        if (s->resident) {  // admitted, not armed yet: its initialisation may still run
+            MCX_CUDA(cudaStreamSynchronize(s->admin->stream));
+            s->active.erase(std::find(s->active.begin(), s->active.end(), j));
+            if (s->minflight) s->deferred.push_back(j);
+            else release(s, j);
+            j->state = JOB_CANCELLED;
+            j->t_finish = now_s(s->t0);
+            return MCX_OK;
+        }
         MCX_CUDA(cudaStreamSynchronize(s->ctx->stream));
         s->active.erase(std::find(s->active.begin(), s->active.end(), j));
         if (s->minflight) s->deferred.push_back(j);
@@ -631,6 +1187,142 @@ MCX_API mcx_status mcx_server_cancel(mcx_server* s, uint64_t job_id) {
     j->state = JOB_CANCELLED;
     j->t_finish = now_s(s->t0);
     return MCX_OK;
+}
+
+MCX_API mcx_status mcx_server_start(mcx_server* s) {
+    if (!s) return fail(MCX_ERR_INVALID_ARG, "server is NULL");
+    if (s->resident) return MCX_OK;
+    if (!s->budget) return fail(MCX_ERR_INVALID_ARG, "the resident loop needs an HBM budget (its job arena)");
+    if (s->max_jobs > kSrvSlots) return fail(MCX_ERR_INVALID_ARG, "the resident loop has %d job slots", kSrvSlots);
+    if (!s->active.empty()) return fail(MCX_ERR_INVALID_ARG, "start the resident loop before admitting jobs");
+    mcx_ctx* ctx = s->ctx;
+    int coop = 0;
+    MCX_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+    if (!coop) return fail(MCX_ERR_CUDA, "the device has no cooperative launch");
+    int bps = 0;
+    MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_srv_loop, 256, 0));
+    if (bps < 1) return fail(MCX_ERR_CUDA, "the serving loop kernel does not fit on an SM");
+    // two blocks per SM at most, on all but a few SMs: room for initialisation and walker kernels
+    const int reserve = std::min(16, ctx->num_sms / 4);
+    s->loop_grid = std::min(bps, 2) * (ctx->num_sms - reserve);
+    void* p = nullptr;
+    MCX_CHECK(dev_alloc(ctx, &p, (size_t)s->budget));
+    s->arena = (char*)p;
+    s->arena_bytes = (size_t)s->budget;
+    s->free_blocks.clear();
+    s->free_blocks[0] = s->arena_bytes;
+    MCX_CHECK(dev_alloc(ctx, &p, sizeof(SrvLoop)));
+    s->d_loop = (SrvLoop*)p;
+    MCX_CUDA(cudaHostAlloc((void**)&s->mb, sizeof(SrvMailbox), cudaHostAllocMapped));
+    std::memset(s->mb, 0, sizeof(SrvMailbox));
+    MCX_CUDA(cudaHostGetDevicePointer((void**)&s->mb_dev, s->mb, 0));
+    mcx_config cfg{ctx->device, nullptr, 0};
+    MCX_CHECK(mcx_ctx_create(&cfg, &s->admin));
+    MCX_CUDA(cudaStreamCreateWithFlags(&s->lstream, cudaStreamNonBlocking));
+    MCX_CUDA(cudaEventCreateWithFlags(&s->ldone, cudaEventDisableTiming));
+    if (!s->mstream) {
+        MCX_CUDA(cudaStreamCreateWithFlags(&s->mstream, cudaStreamNonBlocking));
+        MCX_CUDA(cudaEventCreateWithFlags(&s->mdone, cudaEventDisableTiming));
+    }
+    s->slot_job.assign(kSrvSlots, nullptr);
+    // walker descriptors for every slot now: no device allocation may happen while the loop runs
+    MCX_CHECK(grow(s, &s->d_walkers, &s->cap_walkers, (size_t)kSrvSlots));
+    s->resident = true;
+    // Load every kernel the pump launches while the loop runs (initialisation, series prefix,
+    // both spin gathers, walker) with small jobs run to completion first: a kernel loaded on
+    // first use while the loop kernel holds the device would wait for it.
+    mcx_job w{};
+    w.model = MCX_ISING;
+    w.dim = 2;
+    w.L[0] = w.L[1] = 16;
+    w.L[2] = 1;
+    w.kind = MCX_JOB_CANONICAL;
+    w.alg = MCX_METROPOLIS;
+    w.beta = 0.4;
+    w.J = 1.0;
+    w.nsweeps = 2;
+    std::vector<int8_t> spins(256);
+    std::vector<int64_t> ser(6);
+    w.obs_series = ser.data();
+    w.final_spins = spins.data();
+    uint64_t ids[3] = {0, 0, 0};
+    mcx_job wm = w;  // the Multicanonical jobs run first, with no loop kernel on the device
+    wm.kind = MCX_JOB_MULTICANONICAL;
+    wm.bin_start = -512;
+    wm.bin_step = 4;
+    wm.nbins = 257;
+    std::vector<int64_t> hist(257);
+    wm.histogram = hist.data();
+    mcx_job wm2 = wm;  // rows of 24 sites: the gather without 16-site vectors
+    wm2.L[0] = 24;
+    wm2.L[1] = 8;
+    wm2.bin_start = -384;
+    wm2.nbins = 193;
+    const mcx_job* warm[3] = {&wm, &wm2, &w};
+    const long long idle = s->idle_limit;
+    s->idle_limit = 16;  // the loop leaves as soon as the warm-up job is done
+    mcx_status st = MCX_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int phase = 0; phase < 3 && st == MCX_OK; ++phase) {
+        st = mcx_server_submit(s, warm[phase], &ids[phase]);
+        while (st == MCX_OK) {
+            st = step_resident(s);
+            if (st == MCX_OK && s->active.empty() && s->pending.empty()) {
+                st = wait_loop(s, 10.0);
+                break;
+            }
+            if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > 60.0)
+                st = fail(MCX_ERR_TIMEOUT, "the serving loop's first jobs did not finish");
+        }
+    }
+    s->idle_limit = idle;
+    MCX_CHECK(st);
+    for (uint64_t id : ids) {
+        auto it = s->jobs.find(id);
+        delete it->second;
+        s->jobs.erase(it);
+    }
+    s->jobs_done -= 3;
+    s->attempts_done = 0;
+    s->peak = s->used;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_server_stop(mcx_server* s, double timeout_s) {
+    if (!s) return fail(MCX_ERR_INVALID_ARG, "server is NULL");
+    if (!s->resident || !s->lrunning) return MCX_OK;
+    vstore(&s->mb->stop, 1u);
+    return wait_loop(s, timeout_s);
+}
+
+MCX_API mcx_status mcx_server_set_loop_limits(mcx_server* s, int64_t spin_polls, int64_t idle_polls) {
+    if (!s || spin_polls < 1 || idle_polls < 0) return fail(MCX_ERR_INVALID_ARG, "bad argument");
+    if (idle_polls * 100 >= spin_polls)
+        return fail(MCX_ERR_INVALID_ARG, "the idle wait (polls of ~1 us) must stay well below the barrier limit "
+                                         "(polls of ~0.1 us): idle_polls * 100 < spin_polls");
+    s->spin_limit = spin_polls;
+    s->idle_limit = idle_polls;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_server_loop_info(mcx_server* s, int32_t* resident, int32_t* running, uint32_t* status,
+                                        uint64_t* launches, uint64_t* rounds) {
+    if (!s) return fail(MCX_ERR_INVALID_ARG, "server is NULL");
+    if (resident) *resident = s->resident ? 1 : 0;
+    if (running) *running = s->lrunning ? 1 : 0;
+    if (status) *status = s->resident ? (s->lrunning ? (unsigned)kLoopRunning : s->last_status) : 0u;
+    if (launches) *launches = s->loop_launches;
+    if (rounds) *rounds = s->resident ? s->mb->rounds : 0;
+    return MCX_OK;
+}
+
+MCX_API mcx_status mcx_poll_flag(const uint32_t* flag, uint32_t target, int64_t polls, int64_t sleep_ns) {
+    if (!flag || polls < 0 || sleep_ns < 0) return fail(MCX_ERR_INVALID_ARG, "bad argument");
+    for (int64_t n = 0;; ++n) {
+        if (__atomic_load_n(flag, __ATOMIC_ACQUIRE) >= target) return MCX_OK;
+        if (n >= polls) return fail(MCX_ERR_TIMEOUT, "flag stayed below %u for %lld polls", target, (long long)polls);
+        if (sleep_ns) std::this_thread::sleep_for(std::chrono::nanoseconds(sleep_ns));
+    }
 }
 
 MCX_API mcx_status mcx_server_get_stats(mcx_server* s, mcx_server_stats* st) {

@@ -96,6 +96,12 @@ SIGNATURES = {
     "mcx_server_step": (C.c_int, [_P, _i32p, _i32p]),
     "mcx_server_poll": (C.c_int, [_P, C.c_uint64, _P]),
     "mcx_server_cancel": (C.c_int, [_P, C.c_uint64]),
+    "mcx_server_start": (C.c_int, [_P]),
+    "mcx_server_stop": (C.c_int, [_P, C.c_double]),
+    "mcx_server_set_loop_limits": (C.c_int, [_P, C.c_int64, C.c_int64]),
+    "mcx_server_loop_info": (C.c_int, [_P, _i32p, _i32p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint64)]),
+    "mcx_poll_flag": (C.c_int, [_P, C.c_uint32, C.c_int64, C.c_int64]),
     "mcx_server_get_stats": (C.c_int, [_P, _P]),
     "mcx_sweep_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(mcx_rng), C.c_int64, _P, _P]),
     "mcx_pt_create": (C.c_int, [_P, C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_double, C.c_double,

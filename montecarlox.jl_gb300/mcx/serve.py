@@ -47,12 +47,32 @@ class Job:
 
 
 class Server:
-    def __init__(self, hbm_budget=0, max_jobs=64, chunk=50, ctx=None):
+    """Continuous batching of jobs.  ``resident=True`` runs the sweeps in one persistent
+    device loop fed through a mailbox (mcx_server_start); ``step`` then only admits, arms
+    and retires jobs.  The resident loop needs an HBM budget (its job arena)."""
+
+    def __init__(self, hbm_budget=0, max_jobs=64, chunk=50, ctx=None, resident=False, loop_limits=None):
         self.ctx = ctx or default_context()
         h = C.c_void_p()
         _check(_L.load().mcx_server_create(self.ctx.handle, int(hbm_budget), int(max_jobs), int(chunk), C.byref(h)))
         self.handle = h
         self.jobs = {}
+        if loop_limits is not None:
+            _check(_L.load().mcx_server_set_loop_limits(self.handle, int(loop_limits[0]), int(loop_limits[1])))
+        if resident:
+            _check(_L.load().mcx_server_start(self.handle))
+
+    def loop_info(self):
+        """(resident, running, status, launches, rounds) of the resident loop."""
+        r, run, st = C.c_int32(), C.c_int32(), C.c_uint32()
+        la, ro = C.c_uint64(), C.c_uint64()
+        _check(_L.load().mcx_server_loop_info(self.handle, C.byref(r), C.byref(run), C.byref(st), C.byref(la),
+                                              C.byref(ro)))
+        return {"resident": bool(r.value), "running": bool(run.value), "status": st.value,
+                "launches": la.value, "rounds": ro.value}
+
+    def stop(self, timeout_s=10.0):
+        _check(_L.load().mcx_server_stop(self.handle, float(timeout_s)))
 
     def submit(self, *, model="ising", L=(64, 64), kind="canonical", alg="metropolis", beta=0.44, J=1.0, D=0.0,
                h=0.0, seed=0, stream=0, nsweeps=100, bins=None, logweight=None, record=True, spins=False):

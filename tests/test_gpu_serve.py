@@ -101,3 +101,96 @@ def test_budget_rejects_oversized_job_and_cancel(gpu):
     srv.cancel(small)
     srv.run_until_idle()
     assert srv.poll(small)["state"] == 3
+
+
+# ------------------------------------------------------------------ resident loop --
+def test_resident_loop_same_result_as_stepped_server(gpu):
+    """The resident loop (one persistent kernel fed through the mailbox) gives every job the
+    stepped server's result bit for bit, alone and in a mix that a small arena admits a few
+    jobs at a time, with staggered arrivals."""
+    from mcx.serve import Server
+    alone = []
+    for j in JOBS:
+        srv = Server(chunk=7)
+        job = srv.submit(spins=True, **_spec(j))
+        srv.run_until_idle()
+        srv.poll(job)
+        alone.append(_snapshot(job))
+        srv.close()
+    srv = Server(hbm_budget=4 << 20, max_jobs=3, resident=True)
+    info = srv.loop_info()
+    assert info["resident"]
+    jobs = []
+    for k, j in enumerate(JOBS):
+        jobs.append(srv.submit(spins=True, **_spec(j)))
+        if k % 2 == 1:
+            srv.step()
+    srv.run_until_idle()
+    st = srv.stats()
+    assert st["jobs_done"] == len(JOBS) and st["peak_bytes"] <= 4 << 20
+    for job, ref in zip(jobs, alone):
+        assert srv.poll(job) is not None
+        assert _snapshot(job) == ref
+    assert srv.loop_info()["launches"] >= 1
+    srv.close()
+
+
+def test_resident_loop_leaves_when_idle_and_comes_back(gpu):
+    """With a short idle limit the loop kernel leaves once it has nothing to run (status 2)
+    and the next job launches it again; results are unaffected."""
+    import time
+    from mcx.serve import Server
+    srv = Server(hbm_budget=1 << 20, max_jobs=4, resident=True, loop_limits=(1 << 24, 2000))
+    a = srv.submit(spins=True, **JOBS[0])
+    srv.run_until_idle()
+    t0 = time.time()
+    while srv.loop_info()["running"] and time.time() - t0 < 10:
+        srv.step()
+        time.sleep(0.001)
+    info = srv.loop_info()
+    assert not info["running"] and info["status"] == 2
+    b = srv.submit(spins=True, **JOBS[2])
+    srv.run_until_idle()
+    assert srv.loop_info()["launches"] == info["launches"] + 1
+    ref = Server(chunk=5)
+    ra, rb = ref.submit(spins=True, **JOBS[0]), ref.submit(spins=True, **JOBS[2])
+    ref.run_until_idle()
+    for x, y in ((a, ra), (b, rb)):
+        srv.poll(x)
+        ref.poll(y)
+        assert _snapshot(x) == _snapshot(y)
+    srv.close()
+    ref.close()
+
+
+def test_resident_loop_cancel_and_mixed_sizes(gpu):
+    """A long job cancelled while the loop runs it is dropped at the end of a round; the
+    other jobs (a 512^2 lattice among 16^2 ones) finish with the oracle's results."""
+    from mcx.serve import Server
+    srv = Server(hbm_budget=64 << 20, max_jobs=8, resident=True)
+    long = srv.submit(model="ising", L=(256, 256), nsweeps=200000, seed=3, stream=9)
+    small = [srv.submit(model="ising", L=(16, 16), nsweeps=40 + 7 * k, seed=4, stream=k, beta=0.5, spins=True)
+             for k in range(5)]
+    big = srv.submit(model="bc", L=(512, 512), D=1.0, beta=0.6, nsweeps=30, seed=4, stream=20, spins=True)
+    for _ in range(200):
+        srv.step()
+    srv.cancel(long)
+    srv.run_until_idle()
+    assert srv.poll(long)["state"] == 3
+    for k, job in enumerate(small):
+        assert srv.poll(job)["state"] == 2
+        s = O.init_random(O.ISING, [16, 16], 4, k)
+        obs, att, acc = O.cb_sweep(s, O.ISING, [16, 16], O.METROPOLIS, 0.5, 4, stream=k, nsweeps=40 + 7 * k)
+        assert np.array_equal(job.series, obs) and np.array_equal(job.spins, s)
+        assert (job.result["attempts"], job.result["accepted"]) == (att, acc)
+    assert srv.poll(big)["state"] == 2
+    s = O.init_random(O.BC, [512, 512], 4, 20)
+    obs, att, acc = O.cb_sweep(s, O.BC, [512, 512], O.METROPOLIS, 0.6, 4, stream=20, nsweeps=30, D=1.0)
+    assert np.array_equal(big.series, obs) and np.array_equal(big.spins, s)
+    srv.close()
+
+
+def test_resident_loop_needs_a_budget(gpu):
+    from mcx.serve import Server
+    with pytest.raises(gpu.ArgumentError):
+        Server(resident=True)
