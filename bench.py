@@ -28,7 +28,9 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
                     and seven 256^2 chains in one batched call
   reweighting       log Z, <E>, <E^2> at 100 betas from a 4,194,305-bin ln g on the device
   batched_pt        256 3-D replicas in five ladders: persistent kernel against the plain form
-  serving           40 Poisson jobs through the continuous-batching server (p50 / p99)
+  serving           the serving configuration (Poisson 200 / s, L 32-2048, 1e3-1e5 sweeps) on the
+                    resident loop, and a saturated queue on the resident loop and the stepped
+                    server (p50 / p99 latency, aggregate attempts/ns)
   flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block, and a
                     fixed-budget Wang-Landau stage 1 (ln f = 1, flatness 0.8, one walker per SM)
   msc64             the headline workload on the 64-spins-per-word layout
@@ -382,26 +384,39 @@ def bench_wang_landau(torch, mcx, ctx, dev, nwalkers=None, L=1024, sweeps=24, ch
             "visited_bins_walker0": visited, "stage_flat": bool(max(ratios) >= 0.8)}
 
 
-def bench_serve(mcx, ctx, njobs=40):
-    """Poisson arrivals (200 / s, seed 11) of Metropolis and Multicanonical jobs on 2-D
-    Ising / Blume-Capel, L log-uniform in [32, 512] (Multicanonical jobs, whose walker
-    is serial, capped at 128), sweeps log-uniform in [100, 1000] (the configured
-    [32, 2048] x [1e3, 1e5] stream would hold one GPU for hours), HBM budget 8 GiB,
-    64 slots, 25-sweep chunks."""
+def bench_serve(mcx, ctx, njobs=120, nsat=100):
+    """The serving configuration on the resident loop (one persistent kernel fed through a
+    mailbox, jobs admitted into a 4 GiB arena, 64 slots).
+      poisson:   Poisson arrivals at 200 / s (seed 11) of Metropolis or Multicanonical jobs on
+                 2-D Ising / Blume-Capel, L log-uniform in [32, 2048], beta uniform in
+                 [0.3, 0.6], sweeps log-uniform in [1e3, 1e5]; Multicanonical jobs (a quarter)
+                 run a serial walker each and are capped at L = 64 and 2000 sweeps (a single
+                 walker at L = 2048 and 1e5 sweeps would take hours at ~55 ns per attempt).
+      saturated: `nsat` canonical jobs all queued at t = 0 (L in [32, 2048], sweeps in
+                 [1e3, 1e4]) on the resident loop and on the stepped server, for the aggregate
+                 throughput of continuous batching against the single-lattice rate.
+    Latency = arrival to completion; attempts/ns = all attempts over the wall time."""
     from mcx.serve import Server, poisson_jobs, run_load
-
-    srv = Server(hbm_budget=8 << 30, max_jobs=64, chunk=25, ctx=ctx)
-    # warm the kernels once
-    srv.submit(model="ising", L=(64, 64), nsweeps=30)
-    srv.run_until_idle()
-    stream = poisson_jobs(njobs, rate=200.0, seed=11, L_range=(32, 512), sweeps_range=(100, 1000), muca_L_max=128)
+    out = {}
+    srv = Server(hbm_budget=4 << 30, max_jobs=64, chunk=50, ctx=ctx, resident=True)
+    stream = poisson_jobs(njobs, rate=200.0, seed=11, L_range=(32, 2048), sweeps_range=(1e3, 1e5),
+                          muca_fraction=0.25, muca_L_max=64, muca_sweeps_max=2000)
     r = run_load(srv, stream)
     st = srv.stats()
+    li = srv.loop_info()
     srv.close()
-    r.update({"workload": "poisson200_ising_bc_metropolis_muca_L32-512_muca_L<=128_sweeps100-1000",
-              "rate_per_s": 200.0,
-              "peak_bytes": st["peak_bytes"], "iterations": st["iterations"]})
-    return r
+    r.update({"workload": "poisson200_seed11_ising_bc_L32-2048_sweeps1e3-1e5_muca_quarter_L<=64_sweeps<=2000",
+              "mode": "resident loop", "peak_bytes": st["peak_bytes"], "loop_launches": li["launches"]})
+    out["poisson"] = r
+    sat = poisson_jobs(nsat, rate=1e9, seed=12, L_range=(32, 2048), sweeps_range=(1e3, 1e4), muca_fraction=0.0)
+    for mode in ("resident", "stepped"):
+        srv = Server(hbm_budget=4 << 30, max_jobs=64, chunk=50, ctx=ctx, resident=mode == "resident")
+        r = run_load(srv, sat)
+        srv.close()
+        r.update({"workload": "saturated_%d_canonical_jobs_L32-2048_sweeps1e3-1e4" % nsat,
+                  "mode": "resident loop" if mode == "resident" else "stepped server"})
+        out["saturated_" + mode] = r
+    return out
 
 
 def ctx_sms(torch):

@@ -142,6 +142,24 @@ __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const S
 // barriers by spin_limit polls (then the kernel leaves with kLoopTimeout), and a round with no
 // job to run by idle_limit polls of about 1 us (then the kernel leaves with kLoopIdle and the
 // host launches it again when work arrives).
+// Mailbox words live in pinned host memory: system-scope loads and stores.
+__device__ __forceinline__ unsigned mb_ld(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long mb_ld64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void mb_st(unsigned* p, unsigned v) {
+    asm volatile("st.relaxed.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void mb_st64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 constexpr int kSrvSlots = 256;
 static_assert(sizeof(SrvJobDev) % 8 == 0, "SrvJobDev is copied in 8-byte words");
 enum LoopStatus : unsigned { kLoopRunning = 0, kLoopStopped = 1, kLoopIdle = 2, kLoopTimeout = 3 };
@@ -190,7 +208,7 @@ struct SrvLoop {
 // Block 0, after its share of the round: the next round's job list (every job one sweep on,
 // jobs that ended or were cancelled out), newly armed jobs copied in from the mailbox, and,
 // when there is nothing to run, a bounded wait for work.
-__device__ void srv_leader(SrvLoop* L, volatile SrvMailbox* mb, long long r, long long idle_limit) {
+__device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long idle_limit) {
     __shared__ int s_n, s_seq_changed, s_stop;
     __shared__ unsigned s_seq;
     const SrvRound* R = &L->round[r & 1];
@@ -200,7 +218,7 @@ __device__ void srv_leader(SrvLoop* L, volatile SrvMailbox* mb, long long r, lon
         for (int k = 0; k < R->n; ++k) {
             const int sl = R->slot[k];
             const unsigned long long t1 = R->t[k] + 1;
-            if (t1 >= (unsigned long long)L->jobs[sl].todo || mb->cancel[sl] == L->gen[sl]) {
+            if (t1 >= (unsigned long long)L->jobs[sl].todo || mb_ld(&mb->cancel[sl]) == L->gen[sl]) {
                 L->fin[nf++] = sl;
                 continue;
             }
@@ -214,27 +232,27 @@ __device__ void srv_leader(SrvLoop* L, volatile SrvMailbox* mb, long long r, lon
     __syncthreads();
     for (long long polls = 0;; ++polls) {
         if (threadIdx.x == 0) {
-            s_seq = mb->arm_seq;
-            s_stop = mb->stop;
+            s_seq = mb_ld(&mb->arm_seq);
+            s_stop = mb_ld(&mb->stop);
             __threadfence_system();
             s_seq_changed = s_seq != L->seen_seq;
         }
         __syncthreads();
         if (s_seq_changed) {
             for (int sl = threadIdx.x; sl < kSrvSlots; sl += blockDim.x) {
-                const unsigned g = mb->gen[sl];
+                const unsigned g = mb_ld(&mb->gen[sl]);
                 if (g == 0u || g == L->gen[sl]) continue;
                 L->gen[sl] = g;
-                if (mb->cancel[sl] == g) {  // cancelled before it started
-                    __threadfence_system();
-                    mb->finished[sl] = g;
+                __threadfence_system();  // the descriptor was written before the generation
+                if (mb_ld(&mb->cancel[sl]) == g) {  // cancelled before it started
+                    mb_st(&mb->finished[sl], g);
                     continue;
                 }
-                const volatile unsigned long long* src = reinterpret_cast<const volatile unsigned long long*>(&mb->slots[sl]);
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&mb->slots[sl]);
                 unsigned long long* dj = reinterpret_cast<unsigned long long*>(&L->jobs[sl]);
-                for (int w = 0; w < (int)(sizeof(SrvJobDev) / 8); ++w) dj[w] = src[w];
-                const volatile unsigned long long* st = src + sizeof(SrvJobDev) / 8;
-                for (int w = 0; w < kMaxTable; ++w) L->tables[sl][w] = st[w];
+                for (int w = 0; w < (int)(sizeof(SrvJobDev) / 8); ++w) dj[w] = mb_ld64(src + w);
+                const unsigned long long* st = src + sizeof(SrvJobDev) / 8;
+                for (int w = 0; w < kMaxTable; ++w) L->tables[sl][w] = mb_ld64(st + w);
                 const int k = atomicAdd(&s_n, 1);
                 X->slot[k] = sl;
                 X->t[k] = 0;
@@ -266,9 +284,8 @@ __device__ void srv_leader(SrvLoop* L, volatile SrvMailbox* mb, long long r, lon
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mbp, long long spin_limit,
+__global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mb, long long spin_limit,
                                                   long long idle_limit) {
-    volatile SrvMailbox* mb = mbp;
     __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
     __shared__ unsigned s_bgen;
     if (threadIdx.x == 0) s_bgen = ld_acquire(&L->bar[1]);
@@ -340,7 +357,7 @@ __global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mbp, l
             if (!grid_sync(L->bar, gridDim.x, gen, spin_limit)) {
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
                     __threadfence_system();
-                    mb->status = kLoopTimeout;
+                    mb_st(&mb->status, kLoopTimeout);
                 }
                 return;
             }
@@ -351,16 +368,16 @@ __global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mbp, l
             __threadfence_system();
             for (int k = 0; k < L->nfin; ++k) {
                 const int sl = L->fin[k];
-                mb->done[sl] = (unsigned long long)L->jobs[sl].todo;
-                mb->finished[sl] = L->gen[sl];
+                mb_st64(&mb->done[sl], (unsigned long long)L->jobs[sl].todo);
+                mb_st(&mb->finished[sl], L->gen[sl]);
             }
-            for (int k = 0; k < X->n; ++k) mb->done[X->slot[k]] = X->t[k];
-            mb->rounds = (unsigned long long)r + 1;
+            for (int k = 0; k < X->n; ++k) mb_st64(&mb->done[X->slot[k]], X->t[k]);
+            mb_st64(&mb->rounds, (unsigned long long)r + 1);
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         __threadfence_system();
-        mb->status = L->reason;
+        mb_st(&mb->status, L->reason);
     }
 }
 

@@ -151,11 +151,11 @@ class Server:
 
 
 def poisson_jobs(n, *, rate=200.0, seed=11, L_range=(32, 2048), beta_range=(0.3, 0.6), sweeps_range=(1e3, 1e5),
-                 muca_fraction=0.5, muca_L_max=None, models=("ising", "bc")):
+                 muca_fraction=0.5, muca_L_max=None, muca_sweeps_max=None, models=("ising", "bc")):
     """Synthetic request stream: Poisson arrivals (mean `rate` per s), L log-uniform in
     L_range (rounded to a multiple of 8; Multicanonical jobs capped at muca_L_max),
-    beta uniform, sweeps log-uniform, Metropolis or Multicanonical, Ising or
-    Blume-Capel (D = 1)."""
+    beta uniform, sweeps log-uniform (Multicanonical jobs capped at muca_sweeps_max),
+    Metropolis or Multicanonical, Ising or Blume-Capel (D = 1)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -168,6 +168,8 @@ def poisson_jobs(n, *, rate=200.0, seed=11, L_range=(32, 2048), beta_range=(0.3,
         kind = "multicanonical" if rng.uniform() < muca_fraction else "canonical"
         if kind == "multicanonical" and muca_L_max is not None:
             Lside = min(Lside, int(muca_L_max) // 8 * 8)
+        if kind == "multicanonical" and muca_sweeps_max is not None:
+            sweeps = min(sweeps, int(muca_sweeps_max))
         beta = float(rng.uniform(*beta_range))
         N = Lside * Lside
         spec = dict(model=model, L=(Lside, Lside), kind=kind, alg="metropolis", beta=beta, seed=int(seed),

@@ -167,16 +167,25 @@ def test_resident_loop_cancel_and_mixed_sizes(gpu):
     """A long job cancelled while the loop runs it is dropped at the end of a round; the
     other jobs (a 512^2 lattice among 16^2 ones) finish with the oracle's results."""
     from mcx.serve import Server
-    srv = Server(hbm_budget=64 << 20, max_jobs=8, resident=True)
-    long = srv.submit(model="ising", L=(256, 256), nsweeps=200000, seed=3, stream=9)
+    import time
+    srv = Server(hbm_budget=128 << 20, max_jobs=8, resident=True)
+    long = srv.submit(model="ising", L=(256, 256), nsweeps=2_000_000, seed=3, stream=9, record=False)
     small = [srv.submit(model="ising", L=(16, 16), nsweeps=40 + 7 * k, seed=4, stream=k, beta=0.5, spins=True)
              for k in range(5)]
     big = srv.submit(model="bc", L=(512, 512), D=1.0, beta=0.6, nsweeps=30, seed=4, stream=20, spins=True)
-    for _ in range(200):
+    t0 = time.time()
+    done = 0
+    while time.time() - t0 < 20:
         srv.step()
+        r = _progress(srv, long)
+        if r["sweeps_done"] > 100 and all(srv.poll(j) is not None for j in small + [big]):
+            done = r["sweeps_done"]
+            break
+    info = srv.loop_info()
     srv.cancel(long)
     srv.run_until_idle()
-    assert srv.poll(long)["state"] == 3
+    r = srv.poll(long)
+    assert r["state"] == 3, (done, r["sweeps_done"], info, time.time() - t0)
     for k, job in enumerate(small):
         assert srv.poll(job)["state"] == 2
         s = O.init_random(O.ISING, [16, 16], 4, k)
@@ -188,6 +197,14 @@ def test_resident_loop_cancel_and_mixed_sizes(gpu):
     obs, att, acc = O.cb_sweep(s, O.BC, [512, 512], O.METROPOLIS, 0.6, 4, stream=20, nsweeps=30, D=1.0)
     assert np.array_equal(big.series, obs) and np.array_equal(big.spins, s)
     srv.close()
+
+
+def _progress(srv, job):
+    import ctypes as C
+    from mcx import _lib as L
+    r = L.mcx_job_result()
+    L.load().mcx_server_poll(srv.handle, job.id, C.byref(r))
+    return {f: getattr(r, f) for f, _ in L.mcx_job_result._fields_}
 
 
 def test_resident_loop_needs_a_budget(gpu):
