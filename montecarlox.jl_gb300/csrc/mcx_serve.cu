@@ -207,41 +207,60 @@ struct SrvLoop {
 
 // Block 0, after its share of the round: the next round's job list (every job one sweep on,
 // jobs that ended or were cancelled out), newly armed jobs copied in from the mailbox, and,
-// when there is nothing to run, a bounded wait for work.
+// when there is nothing to run, a bounded wait for work.  The host bumps arm_seq after every
+// change it makes (arm, cancel, stop), so a round in which nothing changed reads one word of
+// host memory; the slots are scanned in parallel only after a change.
 __device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long idle_limit) {
-    __shared__ int s_n, s_seq_changed, s_stop;
+    __shared__ int s_n, s_changed, s_stop;
     __shared__ unsigned s_seq;
+    __shared__ unsigned s_new[kSrvSlots];
+    __shared__ unsigned char s_cancel[kSrvSlots];
     const SrvRound* R = &L->round[r & 1];
     SrvRound* X = &L->round[(r + 1) & 1];
-    if (threadIdx.x == 0) {
-        int n = 0, nf = 0;
-        for (int k = 0; k < R->n; ++k) {
-            const int sl = R->slot[k];
-            const unsigned long long t1 = R->t[k] + 1;
-            if (t1 >= (unsigned long long)L->jobs[sl].todo || mb_ld(&mb->cancel[sl]) == L->gen[sl]) {
-                L->fin[nf++] = sl;
-                continue;
-            }
-            X->slot[n] = sl;
-            X->t[n] = t1;
-            ++n;
-        }
-        L->nfin = nf;
-        s_n = n;
-    }
-    __syncthreads();
+    if (threadIdx.x == 0) s_stop = 0;
     for (long long polls = 0;; ++polls) {
         if (threadIdx.x == 0) {
             s_seq = mb_ld(&mb->arm_seq);
-            s_stop = mb_ld(&mb->stop);
+            s_changed = s_seq != L->seen_seq;
+            if (s_changed) s_stop = (int)mb_ld(&mb->stop);
             __threadfence_system();
-            s_seq_changed = s_seq != L->seen_seq;
         }
         __syncthreads();
-        if (s_seq_changed) {
+        if (s_changed) {
             for (int sl = threadIdx.x; sl < kSrvSlots; sl += blockDim.x) {
                 const unsigned g = mb_ld(&mb->gen[sl]);
-                if (g == 0u || g == L->gen[sl]) continue;
+                const unsigned c = mb_ld(&mb->cancel[sl]);
+                s_cancel[sl] = (c != 0u && c == L->gen[sl]) ? 1 : 0;
+                s_new[sl] = (g != 0u && g != L->gen[sl]) ? g : 0u;
+            }
+        } else if (polls == 0) {
+            for (int sl = threadIdx.x; sl < kSrvSlots; sl += blockDim.x) {
+                s_cancel[sl] = 0;
+                s_new[sl] = 0u;
+            }
+        }
+        __syncthreads();
+        if (polls == 0 && threadIdx.x == 0) {  // the jobs that go on
+            int n = 0, nf = 0;
+            for (int k = 0; k < R->n; ++k) {
+                const int sl = R->slot[k];
+                const unsigned long long t1 = R->t[k] + 1;
+                if (t1 >= (unsigned long long)L->jobs[sl].todo || s_cancel[sl]) {
+                    L->fin[nf++] = sl;
+                    continue;
+                }
+                X->slot[n] = sl;
+                X->t[n] = t1;
+                ++n;
+            }
+            L->nfin = nf;
+            s_n = n;
+        }
+        __syncthreads();
+        if (s_changed) {
+            for (int sl = threadIdx.x; sl < kSrvSlots; sl += blockDim.x) {
+                const unsigned g = s_new[sl];
+                if (!g) continue;
                 L->gen[sl] = g;
                 __threadfence_system();  // the descriptor was written before the generation
                 if (mb_ld(&mb->cancel[sl]) == g) {  // cancelled before it started
@@ -371,8 +390,10 @@ __global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mb, lo
                 mb_st64(&mb->done[sl], (unsigned long long)L->jobs[sl].todo);
                 mb_st(&mb->finished[sl], L->gen[sl]);
             }
-            for (int k = 0; k < X->n; ++k) mb_st64(&mb->done[X->slot[k]], X->t[k]);
-            mb_st64(&mb->rounds, (unsigned long long)r + 1);
+            if ((r & 15) == 0) {  // progress, every 16 rounds
+                for (int k = 0; k < X->n; ++k) mb_st64(&mb->done[X->slot[k]], X->t[k]);
+                mb_st64(&mb->rounds, (unsigned long long)r + 1);
+            }
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -857,6 +878,8 @@ mcx_status launch_loop(mcx_server* s) {
     MCX_CUDA(cudaMemsetAsync(s->d_loop, 0, sizeof(SrvLoop), s->lstream));
     vstore(&s->mb->stop, 0u);
     vstore(&s->mb->status, kLoopRunning);
+    // a new launch starts with seen_seq = 0: make sure it scans the slots once
+    if (s->mb->arm_seq == 0u) vstore(&s->mb->arm_seq, 1u);
     SrvLoop* L = s->d_loop;
     SrvMailbox* mb = s->mb_dev;
     long long spin = s->spin_limit, idle = s->idle_limit;
@@ -1087,6 +1110,8 @@ MCX_API mcx_status mcx_server_destroy(mcx_server* s) {
     if (!s) return MCX_OK;
     if (s->resident && s->lrunning) {
         vstore(&s->mb->stop, 1u);
+        std::atomic_thread_fence(std::memory_order_seq_cst);
+        vstore(&s->mb->arm_seq, s->mb->arm_seq + 1);
         wait_loop(s, 30.0);
     }
     if (s->lstream) cudaStreamSynchronize(s->lstream);
@@ -1309,6 +1334,8 @@ MCX_API mcx_status mcx_server_stop(mcx_server* s, double timeout_s) {
     if (!s) return fail(MCX_ERR_INVALID_ARG, "server is NULL");
     if (!s->resident || !s->lrunning) return MCX_OK;
     vstore(&s->mb->stop, 1u);
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    vstore(&s->mb->arm_seq, s->mb->arm_seq + 1);
     return wait_loop(s, timeout_s);
 }
 
