@@ -824,6 +824,8 @@ def run_profile_target(args):
         alg = F.Multicanonical(mcx.Philox(SEED), ens)
         F.sweep_walkers_(walkers, alg, 1)
         F.sweep_walkers_(walkers, alg, 2)
+    elif args.profile == "serve":
+        print(json.dumps(bench_serve(mcx, ctx)), flush=True)
     elif args.profile == "lattice_small":
         lat = mcx.Ising([64, 64], ctx=ctx)
         mcx.init_(lat, "random", rng=mcx.Philox(42))

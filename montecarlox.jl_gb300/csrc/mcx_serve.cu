@@ -135,9 +135,9 @@ __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const S
 
 // ------------------------------------------------------------- resident loop --
 // In the resident mode one cooperative kernel keeps running while jobs come and go: every
-// round it runs one sweep (both colours) of every armed canonical job, block 0 then takes the
-// jobs the host has armed in a mailbox in pinned host memory and prepares the next round, and
-// after the round's last barrier it publishes the jobs that finished.  The host only admits,
+// round it runs one sweep (both colours) of every armed canonical job on blocks 1..; block 0
+// meanwhile takes the jobs the host has armed in a mailbox in pinned host memory and prepares
+// the next round, and after the round's last barrier it publishes the jobs that finished.  The host only admits,
 // arms and retires jobs; it never waits for the kernel.  Every wait is bounded: the grid
 // barriers by spin_limit polls (then the kernel leaves with kLoopTimeout), and a round with no
 // job to run by idle_limit polls of about 1 us (then the kernel leaves with kLoopIdle and the
@@ -280,7 +280,8 @@ __device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long id
             if (threadIdx.x == 0) L->seen_seq = s_seq;
         }
         __syncthreads();
-        if (s_n > 0 || s_stop || polls >= idle_limit) break;
+        // wait for work only in an empty round: a round that still runs jobs publishes them first
+        if (s_n > 0 || s_stop || R->n > 0 || polls >= idle_limit) break;
         if (threadIdx.x == 0) __nanosleep(1000);
         __syncthreads();
     }
@@ -297,8 +298,8 @@ __device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long id
         }
         X->tile0[n] = acc;
         X->n = n;
-        X->exit = (s_stop || n == 0) ? 1 : 0;
-        L->reason = s_stop ? kLoopStopped : (n == 0 ? kLoopIdle : kLoopRunning);
+        X->exit = (s_stop || (n == 0 && R->n == 0)) ? 1 : 0;
+        L->reason = s_stop ? kLoopStopped : (X->exit ? kLoopIdle : kLoopRunning);
     }
     __syncthreads();
 }
@@ -316,8 +317,10 @@ __global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mb, lo
         const int n = R->n;
         const int total = R->tile0[n];
         for (int colour = 0; colour < 2; ++colour) {
+            // block 0 prepares the next round while the others sweep; it sweeps no tiles
+            if (colour == 0 && blockIdx.x == 0) srv_leader(L, mb, r, idle_limit);
             int loaded = -1;
-            for (int ti = blockIdx.x; ti < total; ti += gridDim.x) {
+            for (int ti = blockIdx.x - 1; blockIdx.x > 0 && ti < total; ti += gridDim.x - 1) {
                 int lo = 0, hi = n - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
@@ -372,7 +375,6 @@ __global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mb, lo
                                                     (unsigned long long*)&J.series[3 * t + 2], J.acc};
                 block_add_atomic<4>(v, dst);
             }
-            if (colour == 1 && blockIdx.x == 0) srv_leader(L, mb, r, idle_limit);
             if (!grid_sync(L->bar, gridDim.x, gen, spin_limit)) {
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
                     __threadfence_system();
