@@ -290,7 +290,7 @@ __device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long id
         int acc = 0;
         for (int k = 0; k < n; ++k) {
             const SrvJobDev& J = L->jobs[X->slot[k]];
-            const int per = 256 * (16 / J.V);
+            const int per = (int)blockDim.x * (16 / J.V);  // one chunk per thread and 16 / V sites
             const int nch = J.cpr * J.rows;
             X->per[k] = per;
             X->tile0[k] = acc;
@@ -304,8 +304,10 @@ __device__ void srv_leader(SrvLoop* L, SrvMailbox* mb, long long r, long long id
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) k_srv_loop(SrvLoop* L, SrvMailbox* mb, long long spin_limit,
-                                                  long long idle_limit) {
+constexpr int kLoopThreads = 512;
+
+__global__ void __launch_bounds__(kLoopThreads, 1) k_srv_loop(SrvLoop* L, SrvMailbox* mb, long long spin_limit,
+                                                              long long idle_limit) {
     __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
     __shared__ unsigned s_bgen;
     if (threadIdx.x == 0) s_bgen = ld_acquire(&L->bar[1]);
@@ -886,7 +888,7 @@ mcx_status launch_loop(mcx_server* s) {
     SrvMailbox* mb = s->mb_dev;
     long long spin = s->spin_limit, idle = s->idle_limit;
     void* args[] = {&L, &mb, &spin, &idle};
-    MCX_CUDA(cudaLaunchCooperativeKernel((const void*)k_srv_loop, dim3(s->loop_grid), dim3(256), args, 0,
+    MCX_CUDA(cudaLaunchCooperativeKernel((const void*)k_srv_loop, dim3(s->loop_grid), dim3(kLoopThreads), args, 0,
                                          s->lstream));
     MCX_CUDA(cudaEventRecord(s->ldone, s->lstream));
     count_launch(s->ctx);
@@ -1244,11 +1246,14 @@ MCX_API mcx_status mcx_server_start(mcx_server* s) {
     MCX_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
     if (!coop) return fail(MCX_ERR_CUDA, "the device has no cooperative launch");
     int bps = 0;
-    MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_srv_loop, 256, 0));
+    MCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_srv_loop, kLoopThreads, 0));
     if (bps < 1) return fail(MCX_ERR_CUDA, "the serving loop kernel does not fit on an SM");
-    // two blocks per SM at most, on all but a few SMs: room for initialisation and walker kernels
+    // One 512-thread block per SM at most on all but `reserve` SMs: each block holds an SM's
+    // whole register file, so at least `reserve` SMs stay empty for the kernels the pump
+    // launches beside the loop (initialisation, series prefix, spin gather, walkers) and for
+    // any kernel that needs a whole SM; with the loop on every SM those would wait for it.
     const int reserve = std::min(16, ctx->num_sms / 4);
-    s->loop_grid = std::min(bps, 2) * (ctx->num_sms - reserve);
+    s->loop_grid = ctx->num_sms - reserve;
     void* p = nullptr;
     MCX_CHECK(dev_alloc(ctx, &p, (size_t)s->budget));
     s->arena = (char*)p;
