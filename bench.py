@@ -398,16 +398,18 @@ def bench_serve(mcx, ctx, njobs=120, nsat=100):
     Latency = arrival to completion; attempts/ns = all attempts over the wall time."""
     from mcx.serve import Server, poisson_jobs, run_load
     out = {}
-    srv = Server(hbm_budget=4 << 30, max_jobs=64, chunk=50, ctx=ctx, resident=True)
     stream = poisson_jobs(njobs, rate=200.0, seed=11, L_range=(32, 2048), sweeps_range=(1e3, 1e5),
                           muca_fraction=0.25, muca_L_max=64, muca_sweeps_max=2000)
-    r = run_load(srv, stream)
-    st = srv.stats()
-    li = srv.loop_info()
-    srv.close()
-    r.update({"workload": "poisson200_seed11_ising_bc_L32-2048_sweeps1e3-1e5_muca_quarter_L<=64_sweeps<=2000",
-              "mode": "resident loop", "peak_bytes": st["peak_bytes"], "loop_launches": li["launches"]})
-    out["poisson"] = r
+    for mode in ("resident", "stepped"):
+        srv = Server(hbm_budget=4 << 30, max_jobs=64, chunk=50, ctx=ctx, resident=mode == "resident")
+        r = run_load(srv, stream)
+        st = srv.stats()
+        li = srv.loop_info()
+        srv.close()
+        r.update({"workload": "poisson200_seed11_ising_bc_L32-2048_sweeps1e3-1e5_muca_quarter_L<=64_sweeps<=2000",
+                  "mode": "resident loop" if mode == "resident" else "stepped server", "peak_bytes": st["peak_bytes"],
+                  "loop_launches": li["launches"]})
+        out["poisson" if mode == "resident" else "poisson_stepped"] = r
     sat = poisson_jobs(nsat, rate=1e9, seed=12, L_range=(32, 2048), sweeps_range=(1e3, 1e4), muca_fraction=0.0)
     for mode in ("resident", "stepped"):
         srv = Server(hbm_budget=4 << 30, max_jobs=64, chunk=50, ctx=ctx, resident=mode == "resident")

@@ -1252,7 +1252,7 @@ MCX_API mcx_status mcx_server_start(mcx_server* s) {
     // whole register file, so at least `reserve` SMs stay empty for the kernels the pump
     // launches beside the loop (initialisation, series prefix, spin gather, walkers) and for
     // any kernel that needs a whole SM; with the loop on every SM those would wait for it.
-    const int reserve = std::min(16, ctx->num_sms / 4);
+    const int reserve = std::min(8, ctx->num_sms / 4);
     s->loop_grid = ctx->num_sms - reserve;
     void* p = nullptr;
     MCX_CHECK(dev_alloc(ctx, &p, (size_t)s->budget));
