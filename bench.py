@@ -93,15 +93,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) of one k_ising_cb<2,16,false,true> half-sweep launch on the headline
-# lattice, from one ncu capture (profiles/ising_cb_L4096_metropolis.md; ncu replays with flushed
-# caches, so this is a cold launch: both colour arrays read once)
-CB_TRAFFIC_PER_LAUNCH = 16798976
+# DRAM bytes (read + write) of one k_ising_strip<2,16,false,true> half-sweep launch on the
+# headline lattice, from one ncu capture (profiles/int_pipes_ising_strip_and_pt_persistent.md;
+# ncu replays with flushed caches, so this is a cold launch: both colour arrays read once)
+CB_TRAFFIC_PER_LAUNCH = 16810240
 
 # Per-launch integer-pipe work of the two headline kernels from one ncu capture each
-# (profiles/int_pipes_ising_cb_and_pt_persistent.md): warp instructions, ALU-pipe warp
+# (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
-CB_PIPES = {"warp_inst": 7263804, "alu_inst": 3933758, "fma_cycles": 7892832, "per": "launch"}
+CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
 PT_PIPES = {"warp_inst": 68099464 / 3, "alu_inst": 35368743 / 3, "fma_cycles": 70799920 / 3, "per": "sweep"}
 
 
@@ -297,6 +297,48 @@ def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
     return {"workload": "ising2d_L4096_metropolis_msc64", "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6),
             "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2>",
             "alg_bytes_per_launch": 1.5 * N / 8}
+
+
+def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_step=100):
+    """Other single-lattice sweeps through the same grid kernels (column-strip half-sweeps),
+    device-timed, L2 flushed between steps: 3-D Ising 256^3, Ising heat bath and Blume-Capel
+    (D = 1) Metropolis / heat bath on the 4096^2 lattice."""
+    lib = mcx._lib.load()
+    cases = [("ising3d_L256_metropolis", lambda: mcx.Ising([256, 256, 256], ctx=ctx), mcx.Metropolis, 0.2216),
+             ("ising2d_L4096_heatbath", lambda: mcx.Ising([L_SIDE, L_SIDE], ctx=ctx), mcx.HeatBath, BETA),
+             ("bc2d_L4096_D1_metropolis", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.Metropolis,
+              0.6),
+             ("bc2d_L4096_D1_heatbath", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.HeatBath, 0.6)]
+    out = {}
+    for name, make, kind, beta in cases:
+        lat = make()
+        mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+        alg = kind(mcx.Philox(SEED), beta=beta)
+        n = int(lat.N)
+
+        def step():
+            rng = alg.rng._c()
+            mcx._check(lib.mcx_sweep(lat.handle, alg.ALG, beta, mcx.C.byref(rng), sweeps_per_step, None, None))
+            alg.rng.counter = rng.counter
+
+        for _ in range(warmup):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        lat.close()
+        out[name] = {"attempts_per_ns": n * sweeps_per_step * steps / (tot * 1e6), "ms_per_step": tot / steps,
+                     "sweeps_per_step": sweeps_per_step}
+    return out
 
 
 def bench_flathist(torch, mcx, ctx, dev, nwalkers=None, L=1024):
@@ -740,7 +782,7 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = other_res = None
     if not args.no_extras:
         small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
         med_res = bench_medium(torch, mcx, ctx)
@@ -750,6 +792,7 @@ def run_mcx(args):
         fh_res = bench_flathist(torch, mcx, ctx, dev)
         fh_res["wang_landau_stage1"] = bench_wang_landau(torch, mcx, ctx, dev)
         msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
+        other_res = bench_other_lattices(torch, mcx, ctx, flush)
         graph_res = bench_graph(torch, mcx, ctx, flush, max(3, args.steps // 4), 3, min(args.cpu_seconds, 5.0),
                                 rank == 0 and not args.no_cpu_baseline)
     if rank != 0:
@@ -776,7 +819,7 @@ def run_mcx(args):
                    "parallelism": "replicas"},
         "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                          "kernel": "k_ising_cb<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
+                          "kernel": "k_ising_strip<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
                          **int_roof(CB_PIPES, avg_launch_s, sm_mhz, nsm)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
@@ -787,6 +830,7 @@ def run_mcx(args):
         "serving": srv_res,
         "flat_histogram": fh_res,
         "msc64": msc_res,
+        "other_lattices": other_res,
         "general_graphs": graph_res,
         "small_lattice": small_res,
         "medium_lattice": med_res,

@@ -53,9 +53,107 @@ __device__ __forceinline__ void ising_cb_body(const SweepArgs& a, const unsigned
     v[3] += nacc;
 }
 
+// Column-strip walk of one half-sweep, shared by the Ising and Blume-Capel grid kernels.
+// Thread (q, j) takes chunk q of a run of consecutive rows [j*rows/tpc, (j+1)*rows/tpc)
+// (tpc = threads per chunk column; adjacent threads on adjacent chunks of a row).  Moving
+// from row y to y+1 of a plane, the other colour's rows y and y+1 are the previous row's
+// y and y+1 neighbours, so a row costs its own words, the other colour's row y+2 (and
+// the two z rows in 3-D) and one edge byte, and the row, edge and counter indices
+// advance by constants.  `body(ch, c0)` decides the chunk (c0 = global site index of its
+// first site / 4) and leaves the new words in ch.own.  The stream does not depend on
+// the walk, so results equal those of the grid-stride walk (ChunkIter).  On a GB300 this
+// form beat the grid-stride walk by 4 % (2-D) and 10 % (3-D); loading the next row one
+// row ahead made it 12 % slower, and the same walk inside the batched replica kernel's
+// warp ranges 15 % slower.
+template <int DIM, int V>
+struct StripRows {
+    static constexpr int NW = V / 4;
+    uint32_t dn[NW], mid[NW], up[NW];
+};
+
+template <int DIM, int V, class Body>
+__device__ __forceinline__ void strip_walk(const SweepArgs& a, long long tid, long long tpc, Body&& body) {
+    constexpr int NW = V / 4;
+    const int cpr = a.W / V;
+    const int q = (int)(tid % cpr);
+    const long long j = tid / cpr;
+    long long r = j * a.rows / tpc;
+    const long long rend = (j + 1) * a.rows / tpc;
+    const int k0 = q * V;
+    const int keL = k0 == 0 ? a.W - 1 : k0 - 1;  // in-row neighbour byte of a p = 0 row
+    const int keR = k0 + V == a.W ? 0 : k0 + V;  // of a p = 1 row
+    const long long W = a.W;
+    int y = 0, p = 0;
+    uint32_t c0 = 0;
+    int8_t* cp = nullptr;        // own chunk of row r
+    const int8_t* op = nullptr;  // the other colour's row r
+    long long dzp = 0, dzm = 0;  // 3-D: offsets of the z + 1 and z - 1 rows from row r
+    StripRows<DIM, V> R;
+    bool fresh = true;
+    for (; r < rend; ++r) {
+        if (fresh || y == 0) {  // the first row of the run or of a plane
+            const int z = (int)(r / a.Ly);
+            y = (int)(r - (long long)z * a.Ly);
+            p = (y + z + a.colour) & 1;
+            c0 = (uint32_t)(((unsigned long long)r * W + k0) >> 2);
+            cp = a.cur + r * W + k0;
+            op = a.oth + r * W;
+            if constexpr (DIM == 3) {
+                dzp = (long long)((z + 1 == a.Lz ? 0 : z + 1) - z) * a.Ly * W;
+                dzm = (long long)((z == 0 ? a.Lz - 1 : z - 1) - z) * a.Ly * W;
+            }
+            load_row<V>((y == 0 ? op + (long long)(a.Ly - 1) * W : op - W) + k0, R.dn);
+            load_row<V>(op + k0, R.mid);
+            fresh = false;
+        } else {
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                R.dn[w] = R.mid[w];
+                R.mid[w] = R.up[w];
+            }
+        }
+        load_row<V>((y + 1 == a.Ly ? op - (long long)y * W : op + W) + k0, R.up);
+        Chunk<DIM, V> ch;
+        load_row<V>(cp, ch.own);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {  // the neighbour order of Chunk::load
+            ch.nb[0][w] = R.mid[w];
+            ch.nb[1][w] = R.up[w];
+            ch.nb[2][w] = R.dn[w];
+        }
+        if constexpr (DIM == 3) {
+            load_row<V>(op + dzp + k0, ch.nb[4]);
+            load_row<V>(op + dzm + k0, ch.nb[5]);
+        }
+        const uint32_t edge = (uint32_t)(uint8_t)op[p == 0 ? keL : keR];
+        if (p == 0) {
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                ch.nb[3][w] = __funnelshift_l(w == 0 ? (edge << 24) : R.mid[w - 1], R.mid[w], 8);
+        } else {
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                ch.nb[3][w] = __funnelshift_r(R.mid[w], w == NW - 1 ? edge : R.mid[w + 1], 8);
+        }
+        body(ch, c0);
+        store_row<V>(cp, ch.own);
+        cp += W;
+        op += W;
+        c0 += (uint32_t)(W >> 2);
+        p ^= 1;
+        if (++y == a.Ly) y = 0;
+    }
+}
+
+// threads per chunk column of a launch; 0 when a row has more chunks than the grid threads
+__device__ __forceinline__ long long strip_tpc(const SweepArgs& a, int V) {
+    return (long long)gridDim.x * blockDim.x / (a.W / V);
+}
+
 template <int DIM, int V, bool HB, bool T32>
-__global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
-    constexpr int NT = 2 * (2 * DIM + 1);
+__global__ void __launch_bounds__(256, 2) k_ising_strip(const SweepArgs a) {
+    constexpr int Z = 2 * DIM;
+    constexpr int NT = 2 * (Z + 1);
     __shared__ unsigned long long s_thr[NT];
     __shared__ uint32_t s_t32[NT];
     ising_tables<DIM, HB, T32>(a, s_thr, s_t32);
@@ -63,9 +161,24 @@ __global__ void __launch_bounds__(256, 2) k_ising_cb(const SweepArgs a) {
     pdl_trigger();
     pdl_wait();  // the previous half-sweep's colour array is complete
     long long v[4] = {0, 0, 0, 0};
-    const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
-                       a.Ly, a.Lz);
-    ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, it, v);
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long tpc = strip_tpc(a, V);
+    if (tpc == 0) {  // the grid-stride walk
+        const ChunkIter it(tid, (long long)gridDim.x * blockDim.x, a.W / V, a.Ly, a.Lz);
+        ising_cb_body<DIM, V, HB, T32>(a, s_thr, s_t32, it, v);
+    } else if (tid < tpc * (a.W / V)) {
+        const SweepKey key = sweep_key(a);
+        const uint32_t w2 = ctr_word2(key.sweep, a.colour, P_ACCEPT);
+        int nacc = 0, isum = 0, nup = 0;
+        strip_walk<DIM, V>(a, tid, tpc, [&](Chunk<DIM, V>& ch, uint32_t c0) {
+            ising_chunk<DIM, V, HB, T32>(ch, c0, key, w2, s_thr, s_t32, nacc, nup, isum);
+        });
+        long long dP, dM;
+        ising_deltas<Z>(nacc, nup, isum, dP, dM);
+        v[0] += dP;
+        v[1] += dM;
+        v[3] += nacc;
+    }
     long long w[3] = {v[0], v[1], v[3]};
     const unsigned long long sh = series_shift(a);
     unsigned long long* const dst[3] = {a.dst[0] + sh, a.dst[1] + sh, a.acc};
@@ -148,7 +261,7 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
 }
 
 template <int DIM, int V, bool HB>
-__global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
+__global__ void __launch_bounds__(256, 2) k_bc_strip(const SweepArgs a) {
     constexpr int NT = bc_table_size<DIM, HB>();
     __shared__ __align__(16) unsigned long long s_thr[NT];
     for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
@@ -156,9 +269,24 @@ __global__ void __launch_bounds__(256, 2) k_bc_cb(const SweepArgs a) {
     pdl_trigger();
     pdl_wait();
     long long v[4] = {0, 0, 0, 0};
-    const ChunkIter it(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, a.W / V,
-                       a.Ly, a.Lz);
-    bc_cb_body<DIM, V, HB>(a, s_thr, it, v);
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long tpc = strip_tpc(a, V);
+    if (tpc == 0) {  // the grid-stride walk
+        const ChunkIter it(tid, (long long)gridDim.x * blockDim.x, a.W / V, a.Ly, a.Lz);
+        bc_cb_body<DIM, V, HB>(a, s_thr, it, v);
+    } else if (tid < tpc * (a.W / V)) {
+        const SweepKey key = sweep_key(a);
+        const uint32_t w2a = ctr_word2(key.sweep, a.colour, P_ACCEPT);
+        const uint32_t w2p = ctr_word2(key.sweep, a.colour, P_PROPOSE);
+        int nacc = 0, dP = 0, dM = 0, dQ = 0;
+        strip_walk<DIM, V>(a, tid, tpc, [&](Chunk<DIM, V>& ch, uint32_t c0) {
+            bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, s_thr, nacc, dP, dM, dQ);
+        });
+        v[0] += dP;
+        v[1] += dM;
+        v[2] += dQ;
+        v[3] += nacc;
+    }
     const unsigned long long sh = series_shift(a);
     unsigned long long* const dst[4] = {a.dst[0] + sh, a.dst[1] + sh, a.dst[2] + sh, a.acc};
     block_add_atomic<4>(v, dst);
@@ -351,9 +479,9 @@ __global__ void k_prefix_series_batch(const SmallBatchDesc* __restrict__ descs, 
 // ----------------------------------------------------------- dispatching --
 template <int DIM, bool T32>
 static HalfSweepFn pick_ising_word(bool hb, int V) {
-    if (V == 16) return hb ? k_ising_cb<DIM, 16, true, T32> : k_ising_cb<DIM, 16, false, T32>;
-    if (V == 8) return hb ? k_ising_cb<DIM, 8, true, T32> : k_ising_cb<DIM, 8, false, T32>;
-    return hb ? k_ising_cb<DIM, 4, true, T32> : k_ising_cb<DIM, 4, false, T32>;
+    if (V == 16) return hb ? k_ising_strip<DIM, 16, true, T32> : k_ising_strip<DIM, 16, false, T32>;
+    if (V == 8) return hb ? k_ising_strip<DIM, 8, true, T32> : k_ising_strip<DIM, 8, false, T32>;
+    return hb ? k_ising_strip<DIM, 4, true, T32> : k_ising_strip<DIM, 4, false, T32>;
 }
 
 template <int DIM>
@@ -365,9 +493,9 @@ static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, co
                                                                : pick_ising_word<DIM, false>(hb, V);
         return hb ? k_ising_cb_site<DIM, true> : k_ising_cb_site<DIM, false>;
     }
-    if (V == 16) return hb ? k_bc_cb<DIM, 16, true> : k_bc_cb<DIM, 16, false>;
-    if (V == 8) return hb ? k_bc_cb<DIM, 8, true> : k_bc_cb<DIM, 8, false>;
-    if (V == 4) return hb ? k_bc_cb<DIM, 4, true> : k_bc_cb<DIM, 4, false>;
+    if (V == 16) return hb ? k_bc_strip<DIM, 16, true> : k_bc_strip<DIM, 16, false>;
+    if (V == 8) return hb ? k_bc_strip<DIM, 8, true> : k_bc_strip<DIM, 8, false>;
+    if (V == 4) return hb ? k_bc_strip<DIM, 4, true> : k_bc_strip<DIM, 4, false>;
     return hb ? k_bc_cb_site<DIM, true> : k_bc_cb_site<DIM, false>;
 }
 

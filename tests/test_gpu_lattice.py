@@ -120,6 +120,33 @@ def test_l4096_two_sweeps_bit_exact(gpu):
         sys_.close()
 
 
+STRIP_CASES = [
+    # model, dims, algorithm, beta, D, h: lattices above the one-cluster limit with more rows
+    # than threads per chunk column, so each thread carries its neighbour rows over runs of
+    # two or more rows; 3-D runs cross planes; 16-, 8- and 4-site chunks; thresholds of 0
+    (O.ISING, [64, 24, 3600], "metropolis", 0.2216, 0.0, 0.0),  # 2 chunks per row, Ly = 24
+    (O.ISING, [32, 48, 4000], "heatbath", 0.22, 0.0, 0.1),      # 1 chunk per row
+    (O.ISING, [64, 6, 12000], "glauber", 0.25, 0.0, 0.0),       # Ly = 6: runs cross a plane every few rows
+    (O.ISING, [2048, 2048], "metropolis", 3.0, 0.0, 0.0),       # 64-bit thresholds
+    (O.ISING, [1008, 2000], "glauber", 0.4407, 0.0, -0.1),      # W = 504: 8-site chunks
+    (O.ISING, [1000, 1200], "heatbath", 0.5, 0.0, 0.0),         # W = 500: 4-site chunks
+    (O.BC, [2048, 2048], "metropolis", 0.6, 1.0, 0.0),
+    (O.BC, [32, 24, 8000], "heatbath", 0.35, 0.7, 0.1),
+    (O.BC, [2000, 2048], "glauber", 0.5, 0.5, 0.0),             # W = 1000: 8-site chunks
+]
+
+
+@pytest.mark.parametrize("model,L,alg,beta,D,h", STRIP_CASES)
+def test_strip_walk_parity(gpu, model, L, alg, beta, D, h):
+    """The column-strip half-sweep (runs of consecutive rows per thread) against the oracle:
+    spins, per-sweep series and counters over three sweeps, bit for bit."""
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, model, L, alg, beta, D=D, h=h, seed=13, stream=1, nsweeps=3)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    sys_.close()
+
+
 def test_sweeps_compose_and_replay(gpu):
     """Counter-based stream: 3+5 sweeps equal 8 sweeps; a replay from the same
     counter reproduces the run."""
