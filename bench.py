@@ -5,7 +5,9 @@ Workload (the 2-D configuration the headline metric is quoted on): Ising, L=4096
 periodic, J=1, h=0, int8 spins, +/-1 start from seed 7, Metropolis checkerboard
 sweeps at beta=0.4407, energy and magnetisation recorded every sweep.  One step is
 one mcx_sweep call of --sweeps-per-step sweeps.  The lattice (16 MiB) fits in L2,
-so L2 is flushed (256 MiB write) between timed steps.
+so L2 is flushed (256 MiB write) between timed steps.  The int8 lattice runs each call
+on a transient 64-sites-per-word copy (packed at the start of the call, unpacked at its
+end, k_msc_metro half-sweeps; results bit-identical to the int8 kernels).
 
   value      attempts/ns, CUDA events on the library's stream (torch's current stream is
              handed to the context); L2 is flushed before every timed step, so each step
@@ -14,8 +16,9 @@ so L2 is flushed (256 MiB write) between timed steps.
   e2e        the same metric through the public C ABI with host buffers: every step
              uploads the lattice from pinned host memory (mcx_set_spins) and reads
              the per-sweep (pair, spin, spin2) series back (mcx_sweep obs_series)
-  roofline   the half-sweep kernel: algorithmic bytes 1.5*N per launch (reads both
-             colour arrays, writes its own) over the average launch time, against HBM; and
+  roofline   the half-sweep kernel: algorithmic bytes 1.5*N/8 per launch (reads both
+             packed colour arrays, writes its own) over the average launch time (packing
+             included), against HBM; and
              int_frac, the fraction of the integer-pipe roof (issue, ALU, FMA) that binds the
              kernel, from its per-launch instruction counts and the sampled SM clock
   cpu_baseline  the oracle's sequential random-site mode (the reference's
@@ -34,6 +37,9 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
   flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block, and a
                     fixed-budget Wang-Landau stage 1 (ln f = 1, flatness 0.8, one walker per SM)
   msc64             the headline workload on the 64-spins-per-word layout
+  other_lattices    3-D Ising 256^3, Ising heat bath and Blume-Capel Metropolis / heat bath on
+                    4096^2, and the headline workload with packing off (the int8 words,
+                    k_ising_strip, with its own roofline)
   general_graphs    4096^2 torus as IsingMatrix (Gaussian couplings) and as IsingGraph
 
 `--impl reference` times that CPU path alone on every host core.
@@ -98,10 +104,15 @@ def measured_peaks():
 # ncu replays with flushed caches, so this is a cold launch: both colour arrays read once)
 CB_TRAFFIC_PER_LAUNCH = 16810240
 
+# The same for one k_msc_metro<2> launch (the headline workload's kernel: int8 lattices run
+# multi-sweep calls on a transient 64-sites-per-word copy), profiles/msc_metro_L4096.md.
+MSC_TRAFFIC_PER_LAUNCH = 2124800
+
 # Per-launch integer-pipe work of the two headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
+MSC_PIPES = {"warp_inst": 4564682, "alu_inst": 2259824, "fma_cycles": 6523808, "per": "launch"}
 PT_PIPES = {"warp_inst": 68099464 / 3, "alu_inst": 35368743 / 3, "fma_cycles": 70799920 / 3, "per": "sweep"}
 
 
@@ -297,6 +308,44 @@ def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
     return {"workload": "ising2d_L4096_metropolis_msc64", "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6),
             "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2>",
             "alg_bytes_per_launch": 1.5 * N / 8}
+
+
+def bench_int8_words(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, nsm, sm_mhz):
+    """The headline workload with packing off (mcx_lattice_set_packing): every half-sweep on
+    the int8 words (k_ising_strip, captured 64-sweep graphs), device-timed, L2 flushed."""
+    L = [L_SIDE, L_SIDE]
+    N = L_SIDE * L_SIDE
+    lat = mcx.Ising(L, ctx=ctx)
+    lat.set_packing(False)
+    mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+    alg = mcx.Metropolis(mcx.Philox(SEED), beta=BETA)
+    lib = mcx._lib.load()
+
+    def step():
+        rng = alg.rng._c()
+        mcx._check(lib.mcx_sweep(lat.handle, alg.ALG, BETA, mcx.C.byref(rng), sweeps_per_step, None, None))
+        alg.rng.counter = rng.counter
+
+    for _ in range(warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    lat.close()
+    launch_s = tot * 1e-3 / (2 * sweeps_per_step * steps)
+    return {"workload": "ising2d_L4096_metropolis_int8_words", "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6),
+            "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_ising_strip<2,16,false,true>",
+            "roofline": dict({"alg_bytes_per_launch": 1.5 * N, "achieved_gbs": 1.5 * N / launch_s / 1e9,
+                              "traffic": CB_TRAFFIC_PER_LAUNCH}, **int_roof(CB_PIPES, launch_s, sm_mhz, nsm))}
 
 
 def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_step=100):
@@ -748,9 +797,10 @@ def run_mcx(args):
     attempts = N * S * args.steps * ws
     value = attempts / (total_ms * 1e6)
 
-    # roofline of the half-sweep kernel (2 launches per sweep)
+    # roofline of the half-sweep kernel (2 launches per sweep; the call's packing and
+    # unpacking of the transient 64-sites-per-word copy are inside the average)
     avg_launch_s = total_ms * 1e-3 / (2 * S * args.steps)
-    alg_bytes = 1.5 * N
+    alg_bytes = 1.5 * N / 8
     achieved = alg_bytes / avg_launch_s / 1e9
     peak, peak_kind = measured_peaks()
 
@@ -793,6 +843,8 @@ def run_mcx(args):
         fh_res["wang_landau_stage1"] = bench_wang_landau(torch, mcx, ctx, dev)
         msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
         other_res = bench_other_lattices(torch, mcx, ctx, flush)
+        other_res["ising2d_L4096_metropolis_int8_words"] = bench_int8_words(
+            torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S, ctx_sms(torch), (clk or {}).get("sm_mhz") or 2070.0)
         graph_res = bench_graph(torch, mcx, ctx, flush, max(3, args.steps // 4), 3, min(args.cpu_seconds, 5.0),
                                 rank == 0 and not args.no_cpu_baseline)
     if rank != 0:
@@ -804,7 +856,7 @@ def run_mcx(args):
         cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
                          "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
-    tr = CB_TRAFFIC_PER_LAUNCH
+    tr = MSC_TRAFFIC_PER_LAUNCH
     nsm = ctx_sms(torch)
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
     if pt_res:
@@ -814,13 +866,15 @@ def run_mcx(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
         "config": {"workload": "ising2d_L4096_metropolis_int8", "L": L_SIDE, "beta": BETA, "seed": SEED,
-                   "layout": "int8 colour-split", "sweeps_per_step": S, "record": "E,M every sweep",
+                   "layout": "int8 colour-split storage; each call sweeps a transient 64-sites-per-word copy "
+                             "(packed at its start, unpacked at its end; mcx_lattice_set_packing)",
+                   "sweeps_per_step": S, "record": "E,M every sweep",
                    "l2": "flushed between timed steps (256 MiB write)", "replicas_per_gpu": 1,
                    "parallelism": "replicas"},
         "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                          "kernel": "k_ising_strip<2,16,false,true>", "alg_bytes_per_launch": alg_bytes},
-                         **int_roof(CB_PIPES, avg_launch_s, sm_mhz, nsm)),
+                          "kernel": "k_msc_metro<2>", "alg_bytes_per_launch": alg_bytes},
+                         **int_roof(MSC_PIPES, avg_launch_s, sm_mhz, nsm)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
         "gpu_launches": launches,

@@ -157,6 +157,12 @@ MCX_API mcx_status mcx_energy(mcx_lattice* lat, double* energy, int64_t* magneti
 MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
                              mcx_rng* rng, int64_t nsweeps, int64_t* obs_series,
                              mcx_counters* counters);
+/* Whether mcx_sweep may run calls of 16 sweeps or more of this int8 Ising lattice on a
+ * transient 64-sites-per-word copy (Metropolis without a field, Lx a multiple of 128,
+ * above 524,288 sites): packed at the start of the call, unpacked at its end, N/8 bytes
+ * of device memory on first use within the HBM budget.  Results are bit-identical either
+ * way; the copy is faster.  Default on; off keeps every call on the int8 kernels. */
+MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow);
 /* Times the admissible kernel shapes (sites per thread: 16, 8, 4) for this lattice
  * and algorithm on a scratch copy of the spins and keeps the fastest for later
  * mcx_sweep calls; results never depend on the choice.  chosen / ns_per_site may be

@@ -36,12 +36,13 @@ __device__ __forceinline__ void ising_chunk(Chunk<DIM, V>& ch, uint32_t c0, cons
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
     uint32_t af = 0, au = 0, ai = 0;
+    const PhiloxPre pre = philox_pre((uint32_t)key.sweep, w2, key.k0);  // invariant: hoisted out of loops
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
         uint32_t nbw[Z];
 #pragma unroll
         for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
-        const uint4 rnd = philox10(make_uint4(c0 + w, (uint32_t)key.sweep, w2, key.stream), key.k0, key.k1);
+        const uint4 rnd = philox10_pre(c0 + w, key.stream, pre, key.k0, key.k1);
         uint32_t fb;
         if (T32) fb = ising_word32<Z, HB>(nbw, ch.own[w], rnd, s_t32, af, au, ai);
         else fb = ising_word<Z, HB>(nbw, ch.own[w], rnd, s_thr, nacc, nup, isum);

@@ -51,6 +51,45 @@ __host__ __device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_
     return c;
 }
 
+// philox10 for counters (x, y, z, w) of which only x and w vary between calls: the
+// round-0 product of z and the round-1 product of the resulting first word do not depend
+// on x or w, so they are formed once (philox_pre) and each call does 18 products, not 20.
+// philox10_pre(x, w, philox_pre(y, z, k0), k0, k1) == philox10({x, y, z, w}, k0, k1).
+struct PhiloxPre {
+    uint32_t x1, y1;      // round-0 words 0 and 1
+    uint32_t hi1, lo1;    // round-1 product of word 0
+};
+
+__host__ __device__ __forceinline__ PhiloxPre philox_pre(uint32_t y, uint32_t z, uint32_t k0) {
+    const unsigned long long p1 = (unsigned long long)kPhiloxM1 * z;
+    PhiloxPre P;
+    P.x1 = (uint32_t)(p1 >> 32) ^ y ^ k0;
+    P.y1 = (uint32_t)p1;
+    const unsigned long long p0 = (unsigned long long)kPhiloxM0 * P.x1;
+    P.hi1 = (uint32_t)(p0 >> 32);
+    P.lo1 = (uint32_t)p0;
+    return P;
+}
+
+__host__ __device__ __forceinline__ uint4 philox10_pre(uint32_t x, uint32_t w, const PhiloxPre& P, uint32_t k0,
+                                                       uint32_t k1) {
+    const unsigned long long q0 = (unsigned long long)kPhiloxM0 * x;  // round 0
+    const uint32_t z1 = (uint32_t)(q0 >> 32) ^ w ^ k1, w1 = (uint32_t)q0;
+    k0 += kPhiloxW0;  // round 1
+    k1 += kPhiloxW1;
+    const unsigned long long q1 = (unsigned long long)kPhiloxM1 * z1;
+    uint4 c = make_uint4((uint32_t)(q1 >> 32) ^ P.y1 ^ k0, (uint32_t)q1, P.hi1 ^ w1 ^ k1, P.lo1);
+#pragma unroll
+    for (int r = 2; r < 10; ++r) {
+        k0 += kPhiloxW0;
+        k1 += kPhiloxW1;
+        unsigned long long p0 = (unsigned long long)kPhiloxM0 * c.x;
+        unsigned long long p1 = (unsigned long long)kPhiloxM1 * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0);
+    }
+    return c;
+}
+
 // word 2 of a checkerboard counter
 __host__ __device__ __forceinline__ uint32_t ctr_word2(unsigned long long sweep, int colour,
                                               uint32_t purpose) {

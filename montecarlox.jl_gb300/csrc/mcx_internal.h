@@ -119,6 +119,7 @@ struct mcx_lattice {
     int64_t series_len = 0;        // sweeps recorded by the last mcx_sweep
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
+    int allow_packing = 1;         // int8: multi-sweep calls may use a transient MSC64 copy
     int cluster_size = 0;          // CTAs of the last cluster-form call (0: not tried, -1: none fits)
     // that call's kernel, block size and shared memory, reused while its key (heat bath,
     // 32-bit table) is the same, so later calls skip the occupancy query (about 1 us of the

@@ -42,6 +42,8 @@ __device__ __forceinline__ unsigned long long series_shift(const SweepArgs& a) {
 
 // captured multi-sweep graphs hold this many sweeps and are replayed back to back
 constexpr int64_t kGraphChunk = 64;
+// int8 sweep calls of at least this many sweeps may run on a transient MSC64 copy
+constexpr int64_t kMscMinSweeps = 16;
 
 using HalfSweepFn = void (*)(const SweepArgs);
 

@@ -293,6 +293,11 @@ class DeviceLattice(AbstractSpinSystem):
     def __len__(self):
         return self.N
 
+    def set_packing(self, allow=True):
+        """Whether multi-sweep calls may run on a transient 64-sites-per-word copy of this
+        int8 Ising lattice (mcx_lattice_set_packing; results are identical either way)."""
+        _check(L.load().mcx_lattice_set_packing(self.handle, 1 if allow else 0))
+
     @property
     def spins(self):
         """Copy of the spins in SpinSystems linear order (int8)."""

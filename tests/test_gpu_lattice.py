@@ -147,6 +147,74 @@ def test_strip_walk_parity(gpu, model, L, alg, beta, D, h):
     sys_.close()
 
 
+@pytest.mark.parametrize("L,beta,nsweeps", [([2048, 1024], 0.4407, 20), ([128, 64, 80], 0.2216, 16),
+                                             ([1024, 544], 3.0, 17)])
+def test_int8_calls_on_transient_msc64(gpu, L, beta, nsweeps):
+    """Large int8 Ising lattices under Metropolis without a field run calls of 16 sweeps or
+    more on a packed 64-sites-per-word copy: spins, series and counters still equal the
+    oracle's, and a following heat-bath call (int8 kernels) continues from the unpacked
+    state."""
+    sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.ISING, L, "metropolis", beta, seed=21, stream=2,
+                                                nsweeps=nsweeps)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.accepted == acc
+    hb = _alg(gpu, "heatbath", 22, beta, 0)
+    obs2 = gpu.sweep_(sys_, hb, 3, record=True)
+    oobs2, _, acc2 = O.cb_sweep(s, O.ISING, L, O.HEATBATH, beta, 22, stream=0, nsweeps=3)
+    assert np.array_equal(obs2, oobs2)
+    assert np.array_equal(sys_.spins, s)
+    assert hb.flips == acc2
+    sys_.close()
+
+
+def test_packing_switch(gpu):
+    """mcx_lattice_set_packing(lat, 0) keeps calls on the int8 kernels: no copy is
+    allocated and the results are the same; switching it back on gives the packed path."""
+    L = [2048, 1024]
+    ctx = gpu.Context()
+    sys_ = gpu.Ising(L, ctx=ctx)
+    gpu.init_(sys_, "random", rng=gpu.Philox(8))
+    sys_.set_packing(False)
+    before = ctx.memory()[0]
+    a = gpu.Metropolis(gpu.Philox(8), beta=0.4407)
+    obs = gpu.sweep_(sys_, a, 16, record=True)
+    assert ctx.memory()[0] == before
+    s = O.init_random(O.ISING, L, 8)
+    oobs, _, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.4407, 8, nsweeps=16)
+    assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s) and a.accepted == acc
+    sys_.set_packing(True)
+    obs = gpu.sweep_(sys_, a, 16, record=True)
+    assert ctx.memory()[0] == before + L[0] * L[1] // 8
+    oobs, _, _ = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.4407, 8, sweep0=16, nsweeps=16)
+    assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s)
+    sys_.close()
+
+
+def test_transient_msc64_respects_the_budget(gpu):
+    """With no room in the HBM budget for the packed copy the call stays on the int8
+    kernels, with the same results and no memory taken."""
+    L = [4096, 2048]
+    probe = gpu.Context()
+    lat = gpu.Ising(L, ctx=probe)
+    used = probe.memory()[0]
+    lat.close()
+    probe.close()
+    ctx = gpu.Context(hbm_budget=used + (64 << 10))
+    sys_ = gpu.Ising(L, ctx=ctx)
+    gpu.init_(sys_, "random", rng=gpu.Philox(4))
+    before = ctx.memory()[0]
+    a = gpu.Metropolis(gpu.Philox(4), beta=0.4407)
+    obs = gpu.sweep_(sys_, a, 16, record=True)
+    assert ctx.memory()[0] == before
+    s = O.init_random(O.ISING, L, 4)
+    oobs, _, acc = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.4407, 4, nsweeps=16)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.accepted == acc
+    sys_.close()
+
+
 def test_sweeps_compose_and_replay(gpu):
     """Counter-based stream: 3+5 sweeps equal 8 sweeps; a replay from the same
     counter reproduces the run."""
