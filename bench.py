@@ -105,14 +105,15 @@ def measured_peaks():
 CB_TRAFFIC_PER_LAUNCH = 16810240
 
 # The same for one k_msc_metro<2> launch (the headline workload's kernel: int8 lattices run
-# multi-sweep calls on a transient 64-sites-per-word copy), profiles/msc_metro_L4096.md.
-MSC_TRAFFIC_PER_LAUNCH = 2124800
+# multi-sweep calls on a transient 64-sites-per-word copy), profiles/msc_metro_L4096.md and
+# profiles/int_pipes_ising_strip_and_pt_persistent.md.
+MSC_TRAFFIC_PER_LAUNCH = 2126848
 
 # Per-launch integer-pipe work of the two headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
-MSC_PIPES = {"warp_inst": 4564682, "alu_inst": 2259824, "fma_cycles": 6523808, "per": "launch"}
+MSC_PIPES = {"warp_inst": 4982506, "alu_inst": 2372112, "fma_cycles": 6765216, "per": "launch"}
 PT_PIPES = {"warp_inst": 68099464 / 3, "alu_inst": 35368743 / 3, "fma_cycles": 70799920 / 3, "per": "sweep"}
 
 
