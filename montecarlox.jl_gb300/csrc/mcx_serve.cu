@@ -321,61 +321,77 @@ __global__ void __launch_bounds__(kLoopThreads, 1) k_srv_loop(SrvLoop* L, SrvMai
         for (int colour = 0; colour < 2; ++colour) {
             // block 0 prepares the next round while the others sweep; it sweeps no tiles
             if (colour == 0 && blockIdx.x == 0) srv_leader(L, mb, r, idle_limit);
-            int loaded = -1;
-            for (int ti = blockIdx.x - 1; blockIdx.x > 0 && ti < total; ti += gridDim.x - 1) {
-                int lo = 0, hi = n - 1;
+            // every sweeping block takes an equal contiguous range of the round's tiles, so
+            // consecutive tiles mostly belong to one job: its table is loaded and its counts
+            // are flushed (one block reduction, four atomics) once per job, not per tile
+            if (blockIdx.x > 0) {
+                const int nb = gridDim.x - 1;
+                const int t_lo = (int)((long long)(blockIdx.x - 1) * total / nb);
+                const int t_hi = (int)((long long)blockIdx.x * total / nb);
+                int lo = 0, hi = n - 1;  // the job of tile t_lo
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (R->tile0[mid] <= ti) lo = mid;
+                    if (R->tile0[mid] <= t_lo) lo = mid;
                     else hi = mid - 1;
                 }
-                const int sl = R->slot[lo];
-                const SrvJobDev J = L->jobs[sl];
-                if (sl != loaded) {
-                    __syncthreads();
-                    for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
-                        const unsigned long long x = L->tables[sl][i];
-                        s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
-                    }
-                    __syncthreads();
-                    loaded = sl;
-                }
-                SrvTile tl;
-                tl.job = sl;
-                tl.c_begin = (ti - R->tile0[lo]) * R->per[lo];
-                tl.c_end = min(J.cpr * J.rows, tl.c_begin + R->per[lo]);
-                tl.pad = 0;
-                const unsigned long long t = R->t[lo];
+                int cur = -1;  // job index whose table is loaded and whose counts accumulate
                 int nacc = 0, a1 = 0, a2 = 0, a3 = 0;
-                const int key = J.V * 4 + J.model * 2 + J.hb;
-                switch (key) {
-                    case 16 * 4 + 0: srv_tile<16, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 16 * 4 + 1: srv_tile<16, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 16 * 4 + 2: srv_tile<16, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 16 * 4 + 3: srv_tile<16, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 8 * 4 + 0: srv_tile<8, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 8 * 4 + 1: srv_tile<8, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 8 * 4 + 2: srv_tile<8, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 8 * 4 + 3: srv_tile<8, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 4 * 4 + 0: srv_tile<4, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 4 * 4 + 1: srv_tile<4, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    case 4 * 4 + 2: srv_tile<4, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
-                    default: srv_tile<4, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                for (int ti = t_lo; ti <= t_hi; ++ti) {
+                    while (ti < t_hi && R->tile0[lo + 1] <= ti) ++lo;
+                    if (cur >= 0 && (ti == t_hi || lo != cur)) {  // flush the previous job's counts
+                        const SrvJobDev& P = L->jobs[R->slot[cur]];
+                        const unsigned long long tp = R->t[cur];
+                        long long dP, dM, dQ;
+                        if (P.model == 0) {
+                            ising_deltas<4>(nacc, a1, a2, dP, dM);
+                            dQ = 0;
+                        } else {
+                            dP = a1;
+                            dM = a2;
+                            dQ = a3;
+                        }
+                        long long v[4] = {dP, dM, dQ, (long long)nacc};
+                        unsigned long long* const dst[4] = {(unsigned long long*)&P.series[3 * tp],
+                                                            (unsigned long long*)&P.series[3 * tp + 1],
+                                                            (unsigned long long*)&P.series[3 * tp + 2], P.acc};
+                        block_add_atomic<4>(v, dst);
+                        nacc = a1 = a2 = a3 = 0;
+                        cur = -1;
+                    }
+                    if (ti == t_hi) break;
+                    const int sl = R->slot[lo];
+                    const SrvJobDev J = L->jobs[sl];
+                    if (cur != lo) {
+                        __syncthreads();
+                        for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
+                            const unsigned long long x = L->tables[sl][i];
+                            s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
+                        }
+                        __syncthreads();
+                        cur = lo;
+                    }
+                    SrvTile tl;
+                    tl.job = sl;
+                    tl.c_begin = (ti - R->tile0[lo]) * R->per[lo];
+                    tl.c_end = min(J.cpr * J.rows, tl.c_begin + R->per[lo]);
+                    tl.pad = 0;
+                    const unsigned long long t = R->t[lo];
+                    const int key = J.V * 4 + J.model * 2 + J.hb;
+                    switch (key) {
+                        case 16 * 4 + 0: srv_tile<16, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 16 * 4 + 1: srv_tile<16, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 16 * 4 + 2: srv_tile<16, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 16 * 4 + 3: srv_tile<16, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 8 * 4 + 0: srv_tile<8, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 8 * 4 + 1: srv_tile<8, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 8 * 4 + 2: srv_tile<8, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 8 * 4 + 3: srv_tile<8, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 4 * 4 + 0: srv_tile<4, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 4 * 4 + 1: srv_tile<4, 0, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        case 4 * 4 + 2: srv_tile<4, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                        default: srv_tile<4, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
+                    }
                 }
-                long long dP, dM, dQ;
-                if (J.model == 0) {
-                    ising_deltas<4>(nacc, a1, a2, dP, dM);
-                    dQ = 0;
-                } else {
-                    dP = a1;
-                    dM = a2;
-                    dQ = a3;
-                }
-                long long v[4] = {dP, dM, dQ, (long long)nacc};
-                unsigned long long* const dst[4] = {(unsigned long long*)&J.series[3 * t],
-                                                    (unsigned long long*)&J.series[3 * t + 1],
-                                                    (unsigned long long*)&J.series[3 * t + 2], J.acc};
-                block_add_atomic<4>(v, dst);
             }
             if (!grid_sync(L->bar, gridDim.x, gen, spin_limit)) {
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
