@@ -2,7 +2,11 @@
 // uint64 word (bit b of word w of a colour row <-> entry k = 64w + b of the int8
 // colour-split layout; bit set = spin up).  Neighbour counts are formed for 64
 // sites at once with bit-sliced adders; every site still draws its own Philox word,
-// so results are bit-identical to the int8 kernels.
+// so results are bit-identical to the int8 kernels.  Only rules in the rank form of
+// k_msc_metro (Metropolis without a field) are swept on the words: the other rules
+// (heat bath, Glauber, a field) need a per-site table lookup, which on a GB300 ran
+// at 451-479 attempts/ns against 749-759 on the int8 words, so MSC64 lattices sweep
+// those on their int8 arrays (mcx_sweep unpacks before and packs after the call).
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
 #include "mcx_sweep.cuh"
@@ -76,75 +80,6 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
         b1 ^= c0;
         b2 ^= c1;  // n <= 6 never overflows three bits
     }
-}
-
-template <int DIM, bool HB>
-__global__ void __launch_bounds__(256) k_msc_cb(const MscArgs a) {
-    constexpr int Z = 2 * DIM;
-    constexpr int NT = 2 * (Z + 1);
-    __shared__ unsigned long long s_thr[NT];
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) s_thr[t] = a.thr[t];
-    __syncthreads();
-    pdl_trigger();
-    pdl_wait();  // the previous half-sweep's words are complete
-    const long long nwords = (long long)a.nw * a.rows;
-    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
-    int nacc = 0, asum = 0, nup = 0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nwords;
-         g += (long long)gridDim.x * blockDim.x) {
-        const int r = (int)(g / a.nw);
-        const int w = (int)(g - (long long)r * a.nw);
-        const int y = r % a.Ly, z = r / a.Ly;
-        const int p = (y + z + a.colour) & 1;
-        const long long ryp = (y + 1 == a.Ly ? 0 : y + 1) + (long long)a.Ly * z;
-        const long long rym = (y == 0 ? a.Ly - 1 : y - 1) + (long long)a.Ly * z;
-        unsigned long long nb[Z];
-        const unsigned long long mid = a.oth[g];
-        nb[0] = mid;
-        nb[1] = a.oth[ryp * a.nw + w];
-        nb[2] = a.oth[rym * a.nw + w];
-        if (p == 0) {
-            const unsigned long long prev = a.oth[(long long)r * a.nw + (w == 0 ? a.nw - 1 : w - 1)];
-            nb[3] = (mid << 1) | (prev >> 63);
-        } else {
-            const unsigned long long next = a.oth[(long long)r * a.nw + (w == a.nw - 1 ? 0 : w + 1)];
-            nb[3] = (mid >> 1) | (next << 63);
-        }
-        if constexpr (DIM == 3) {
-            const long long rzp = y + (long long)a.Ly * (z + 1 == a.Lz ? 0 : z + 1);
-            const long long rzm = y + (long long)a.Ly * (z == 0 ? a.Lz - 1 : z - 1);
-            nb[4] = a.oth[rzp * a.nw + w];
-            nb[5] = a.oth[rzm * a.nw + w];
-        }
-        unsigned long long b0, b1, b2;
-        count_bits<Z>(nb, b0, b1, b2);
-        const unsigned long long own = a.cur[g];
-        unsigned long long fm = 0;
-        const uint32_t cbase = (uint32_t)(((unsigned long long)r * a.W + 64ull * w) >> 2);
-#pragma unroll 4
-        for (int q = 0; q < 16; ++q) {
-            const uint4 rnd = philox10(make_uint4(cbase + q, (uint32_t)a.sweep, w2, a.stream), a.k0, a.k1);
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int bit = 4 * q + b;
-                const int n = (int)((b0 >> bit) & 1) + 2 * (int)((b1 >> bit) & 1) + 4 * (int)((b2 >> bit) & 1);
-                const int up = (int)((own >> bit) & 1);
-                const int al = up ? n : Z - n;
-                uint32_t u = b == 0 ? rnd.x : b == 1 ? rnd.y : b == 2 ? rnd.z : rnd.w;
-                if (HB && up) u = ~u;
-                if ((unsigned long long)u < s_thr[al + (Z + 1) * up]) {
-                    fm |= 1ull << bit;
-                    ++nacc;
-                    asum += al;
-                    nup += up;
-                }
-            }
-        }
-        a.cur[g] = own ^ fm;
-    }
-    long long v[3] = {2ll * Z * nacc - 4ll * asum, 2ll * nacc - 4ll * nup, (long long)nacc};
-    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
-    block_add_atomic<3>(v, dst);
 }
 
 // Metropolis-type rule in rank form (no field): every class with at most Z/2 aligned
@@ -261,15 +196,19 @@ static bool msc_rank_form(const Table& t, int Z) {
     return true;
 }
 
+// Whether `alg` with table `t` is swept on the packed words (k_msc_metro's rank form).
+bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
+    return lat->model == MCX_ISING && alg != MCX_HEATBATH && msc_rank_form(t, 2 * lat->dim);
+}
+
 // Whether a multi-sweep call on an int8 Ising lattice may run on a transient MSC64 copy
 // (packed at the start of the call, unpacked at its end): Metropolis-type rule in the rank
 // form of k_msc_metro, rows of a multiple of 64 same-colour sites.  Same stream, same
 // results; the copy is allocated on first use (within the HBM budget, else the call
 // stays on the int8 kernels).
 bool msc_transient_ok(mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
-    if (lat->layout != MCX_LAYOUT_INT8 || lat->model != MCX_ISING || alg == MCX_HEATBATH || !lat->allow_packing)
+    if (lat->layout != MCX_LAYOUT_INT8 || !lat->allow_packing || lat->L[0] % 128 != 0 || !msc_rank_ok(lat, alg, t))
         return false;
-    if (lat->L[0] % 128 != 0 || !msc_rank_form(t, 2 * lat->dim)) return false;
     if (lat->d_msc[0]) return true;
     mcx_ctx* ctx = lat->ctx;
     const size_t bytes = (size_t)(lat->N / 2) / 8;
@@ -315,8 +254,8 @@ mcx_status msc_unpack(mcx_lattice* lat) {
     return MCX_OK;
 }
 
-mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
-                     int64_t nsweeps) {
+// `nsweeps` sweeps of the packed words with k_msc_metro (the caller checked msc_rank_ok).
+mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_rng* rng, int64_t nsweeps) {
     mcx_ctx* ctx = lat->ctx;
     MscArgs a;
     a.nw = (int)(lat->W / 64);
@@ -329,14 +268,8 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const 
     a.stream = rng->stream;
     a.acc = lat->d_acc;
     for (int i = 0; i < t.n && i < 14; ++i) a.thr[i] = t.thr[i];
-    const bool hb = alg == MCX_HEATBATH;
-    void (*fn)(const MscArgs) = lat->dim == 2 ? (hb ? k_msc_cb<2, true> : k_msc_cb<2, false>)
-                                              : (hb ? k_msc_cb<3, true> : k_msc_cb<3, false>);
-    int grid = grid_cap(ctx, (long long)a.nw * a.rows);
-    if (!hb && msc_rank_form(t, 2 * lat->dim)) {
-        fn = lat->dim == 2 ? k_msc_metro<2> : k_msc_metro<3>;
-        grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 256, 0);  // one wave
-    }
+    void (*fn)(const MscArgs) = lat->dim == 2 ? k_msc_metro<2> : k_msc_metro<3>;
+    const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 256, 0);  // one wave
     // every launch after the first depends programmatically on the one before (the
     // kernels read the lattice after pdl_wait)
     cudaLaunchAttribute pdl[1];

@@ -608,6 +608,7 @@ void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const
 mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
                      int64_t nsweeps);  // mcx_msc.cu
 bool msc_transient_ok(mcx_lattice* lat, mcx_algorithm alg, const Table& t);  // mcx_msc.cu
+bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t);  // mcx_msc.cu
 mcx_status msc_pack(mcx_lattice* lat);                                       // mcx_msc.cu
 mcx_status msc_unpack(mcx_lattice* lat);                                     // mcx_msc.cu
 
@@ -717,7 +718,13 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // ones (and those the cluster form does not take, up to kSmallLattice sites) in one
     // block; larger ones replay a captured chunk of kGraphChunk sweeps as often as it fits
     // and launch the rest directly
-    const bool int8 = lat->layout == MCX_LAYOUT_INT8;
+    // MSC64 lattices sweep the packed words only under k_msc_metro's rank form; other rules
+    // run on their int8 arrays (unpacked before, packed after the call), which is faster
+    // than a per-site table lookup on the words
+    const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && msc_rank_ok(lat, alg, t);
+    const bool via_int8 = lat->layout == MCX_LAYOUT_MSC64 && !msc_words;
+    const bool int8 = lat->layout == MCX_LAYOUT_INT8 || via_int8;
+    if (via_int8) MCX_CHECK(msc_unpack(lat));
     MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
     MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
     // large int8 Ising lattices under a rank-form Metropolis rule run calls of kMscMinSweeps
@@ -735,7 +742,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         MCX_CHECK(msc_pack(lat));
         MCX_CHECK(msc_sweep(lat, alg, t, rng, nsweeps));
         MCX_CHECK(msc_unpack(lat));
-    } else if (lat->layout == MCX_LAYOUT_MSC64) {
+    } else if (msc_words) {
         MCX_CHECK(msc_sweep(lat, alg, t, rng, nsweeps));
     } else if (small) {
         SweepArgs a;
@@ -807,6 +814,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         count_launch(ctx, 2 * (uint64_t)nsweeps);
         MCX_CUDA(cudaGetLastError());
     }
+    if (via_int8) MCX_CHECK(msc_pack(lat));
     MCX_CHECK(finish_series(lat, nsweeps));
     rng->counter += (uint64_t)nsweeps;
     if (obs && nsweeps > 0)
