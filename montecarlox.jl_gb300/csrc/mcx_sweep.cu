@@ -1,11 +1,12 @@
 // mcx_sweep.cu -- checkerboard half-sweep kernels on the colour-split int8 layout.
 //
-// One launch updates every site of one colour.  A thread owns V consecutive sites
-// of one row (V = 16: one 128-bit load/store per array row; V = 4 when the row is
-// not a multiple of 16; V = 1 for rows that are not a multiple of 4).  Neighbour
-// sums are formed four sites at a time inside 32-bit words; each Philox4x32-10 call
-// feeds the four sites of one word, which is exactly the counter mapping of the
-// stream (site i takes word (i>>1)&3 of the call with counter (i>>3, ...)).
+// One launch updates every site of one colour.  A thread owns chunks of V consecutive
+// sites of a row (V = 16: one 128-bit load/store per array row; V = 8 or 4 when the row
+// is not a multiple of 16; V = 1 for rows that are not a multiple of 4), one chunk column
+// over a run of consecutive rows in the grid kernels (strip_walk).  Neighbour sums are
+// formed four sites at a time inside 32-bit words; each Philox4x32-10 call feeds the
+// four sites of one word, which is exactly the counter mapping of the stream (site i
+// takes word (i>>1)&3 of the call with counter (i>>3, ...)).
 //
 // Per-sweep energy / magnetisation deltas are reduced per block (warp shuffles)
 // and added with one 64-bit atomic per block into the sweep's slot of the series.
