@@ -37,6 +37,8 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
   flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block, and a
                     fixed-budget Wang-Landau stage 1 (ln f = 1, flatness 0.8, one walker per SM)
   msc64             the headline workload on the 64-spins-per-word layout
+  c2_matrix         the configured 2-D runs: Metropolis and Glauber at beta 0.30 / 0.4407 / 0.60
+                    on int8 and MSC64, 10^4 sweeps each with the series, then U4 and binning errors
   other_lattices    3-D Ising 256^3, Ising heat bath and Blume-Capel Metropolis / heat bath on
                     4096^2, and the headline workload with packing off (the int8 words,
                     k_ising_strip, with its own roofline)
@@ -347,6 +349,43 @@ def bench_int8_words(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, nsm
             "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_ising_strip<2,16,false,true>",
             "roofline": dict({"alg_bytes_per_launch": 1.5 * N, "achieved_gbs": 1.5 * N / launch_s / 1e9,
                               "traffic": CB_TRAFFIC_PER_LAUNCH}, **int_roof(CB_PIPES, launch_s, sm_mhz, nsm))}
+
+
+def bench_c2_matrix(torch, mcx, ctx, sweeps=10000):
+    """The 2-D L=4096 configuration as configured: Metropolis and Glauber at beta 0.30, 0.4407
+    and 0.60, on the int8 and the MSC64 layout, seed 7, `sweeps` sweeps in one call with
+    (pair, spin) recorded every sweep (CUDA events around the call, series copied back
+    inside), then the Binder cumulant U4 (jackknife) and the binning error of the energy per
+    site from the series, after the first tenth as thermalisation."""
+    import numpy as np
+    from mcx import analysis as A
+    N = L_SIDE * L_SIDE
+    out = {}
+    for alg_name, kind in (("metropolis", mcx.Metropolis), ("glauber", mcx.Glauber)):
+        for beta in (0.30, 0.4407, 0.60):
+            for layout in ("int8", "msc64"):
+                lat = mcx.Ising([L_SIDE, L_SIDE], layout=layout, ctx=ctx)
+                mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+                alg = kind(mcx.Philox(SEED), beta=beta)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                obs = mcx.sweep_(lat, alg, sweeps, record=True)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                lat.close()
+                th = sweeps // 10
+                e = -np.asarray(obs[th:, 0], np.float64) / N  # J = 1, h = 0: E = -(pair sum)
+                m = np.asarray(obs[th:, 1], np.float64) / N
+                u4, u4_err = A.binder_cumulant(m)
+                out["%s_beta%.4g_%s" % (alg_name, beta, layout)] = {
+                    "attempts_per_ns": N * sweeps / (ms * 1e6), "ms": ms,
+                    "e_per_site": float(e.mean()), "e_err_binning": A.binning_error(e),
+                    "abs_m": float(np.abs(m).mean()), "u4": u4, "u4_err": u4_err,
+                    "acceptance": alg.accepted / float(N * sweeps) if alg_name == "metropolis" else None}
+    return {"workload": "ising2d_L4096_seed7_%d_sweeps_record" % sweeps, "runs": out}
 
 
 def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_step=100):
@@ -833,7 +872,7 @@ def run_mcx(args):
     e2e_value = N * S * args.steps * ws / (e2e_s * 1e9)
     barrier()
 
-    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = other_res = None
+    pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = other_res = c2_res = None
     if not args.no_extras:
         small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
         med_res = bench_medium(torch, mcx, ctx)
@@ -844,6 +883,7 @@ def run_mcx(args):
         fh_res["wang_landau_stage1"] = bench_wang_landau(torch, mcx, ctx, dev)
         msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
         other_res = bench_other_lattices(torch, mcx, ctx, flush)
+        c2_res = bench_c2_matrix(torch, mcx, ctx)
         other_res["ising2d_L4096_metropolis_int8_words"] = bench_int8_words(
             torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S, ctx_sms(torch), (clk or {}).get("sm_mhz") or 2070.0)
         graph_res = bench_graph(torch, mcx, ctx, flush, max(3, args.steps // 4), 3, min(args.cpu_seconds, 5.0),
@@ -886,6 +926,7 @@ def run_mcx(args):
         "flat_histogram": fh_res,
         "msc64": msc_res,
         "other_lattices": other_res,
+        "c2_matrix": c2_res,
         "general_graphs": graph_res,
         "small_lattice": small_res,
         "medium_lattice": med_res,

@@ -27,6 +27,7 @@
 #include <queue>
 #include <vector>
 
+#include "mcx_body.cuh"
 #include "mcx_cb.cuh"
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
@@ -44,6 +45,9 @@ struct PTReplica {
 struct PTTile {
     int rep, c_begin, c_end, sites;
     int nw;  // persistent spans: warps sharing this replica
+    // 3-D plane walk (ze > zb): lane l takes chunk c_begin + l of every plane (while it is
+    // below c_end, the plane's chunk count) for the planes zb .. ze-1
+    int zb, ze;
 };
 
 struct PTArgs {
@@ -176,14 +180,89 @@ __device__ __forceinline__ void pt_span(const PTArgs& a, const PTReplica& R, int
     }
 }
 
+// 3-D plane walk of one warp: lane l takes chunk pc = c_plane + l of a plane (row y = pc /
+// cpr, chunk q) in every plane zb .. ze-1, in order; the other colour's planes z and z+1 of
+// that row are carried to the next plane as its z-1 and z neighbours, so a plane costs the
+// own words, the other colour's rows y+1 and y-1 and plane z+1, and one edge byte.  The 32
+// lanes read 32 consecutive chunks of a plane (one coalesced range).  Same stream, same
+// results as pt_span.
+template <int V, bool HB, bool T32>
+__device__ __forceinline__ void pt_zwalk(const PTArgs& a, const PTReplica& R, int rep, int c_plane, int c_lim, int zb,
+                                         int ze, int colour, unsigned long long sweep, const void* tab, int lane,
+                                         int& nacc, int& nup, int& isum) {
+    constexpr int NW = V / 4;
+    const int pc = c_plane + lane;
+    if (pc >= c_lim) return;
+    const int y = (int)fdiv((uint32_t)pc, R.m_cpr);
+    const int q = pc - y * R.cpr;
+    const int k0 = q * V;
+    const long long W = R.W;
+    const long long PS = (long long)R.Ly * W;  // bytes of one plane of a colour array
+    const long long dyp = (y + 1 == R.Ly ? -(long long)y : 1ll) * W;
+    const long long dym = (y == 0 ? (long long)(R.Ly - 1) : -1ll) * W;
+    const int keL = k0 == 0 ? R.W - 1 : k0 - 1;
+    const int keR = k0 + V == R.W ? 0 : k0 + V;
+    int8_t* cp = a.arena + R.off[colour] + (long long)zb * PS + (long long)y * W + k0;
+    const int8_t* op = a.arena + R.off[1 - colour] + (long long)zb * PS + (long long)y * W;  // row y of plane z
+    uint32_t c0 = (uint32_t)((((unsigned long long)zb * R.Ly + y) * (unsigned long long)R.W + k0) >> 2);
+    int p = (y + zb + colour) & 1;
+    const SweepKey key{sweep, a.k0, a.k1, (uint32_t)rep};
+    const uint32_t w2 = ctr_word2(sweep, colour, P_ACCEPT);
+    uint32_t zm[NW], mid[NW], zp[NW];
+    load_row<V>(op + (zb == 0 ? (long long)(R.Lz - 1) * PS : -PS) + k0, zm);
+    load_row<V>(op + k0, mid);
+    for (int z = zb; z < ze; ++z) {
+        load_row<V>(op + (z + 1 == R.Lz ? -(long long)z * PS : PS) + k0, zp);
+        Chunk<3, V> ch;
+        load_row<V>(cp, ch.own);
+        load_row<V>(op + dyp + k0, ch.nb[1]);
+        load_row<V>(op + dym + k0, ch.nb[2]);
+        const uint32_t edge = (uint32_t)(uint8_t)op[p == 0 ? keL : keR];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            ch.nb[0][w] = mid[w];
+            ch.nb[4][w] = zp[w];
+            ch.nb[5][w] = zm[w];
+        }
+        if (p == 0) {
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                ch.nb[3][w] = __funnelshift_l(w == 0 ? (edge << 24) : mid[w - 1], mid[w], 8);
+        } else {
+#pragma unroll
+            for (int w = 0; w < NW; ++w) ch.nb[3][w] = __funnelshift_r(mid[w], w == NW - 1 ? edge : mid[w + 1], 8);
+        }
+        ising_chunk<3, V, HB, T32>(ch, c0, key, w2, (const unsigned long long*)tab, (const uint32_t*)tab, nacc, nup,
+                                   isum);
+        store_row<V>(cp, ch.own);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            zm[w] = mid[w];
+            mid[w] = zp[w];
+        }
+        cp += PS;
+        op += PS;
+        c0 += (uint32_t)(PS >> 2);
+        p ^= 1;
+    }
+}
+
 template <int DIM, bool HB, bool T32>
 __device__ __forceinline__ void pt_run_span(const PTArgs& a, const PTTile& sp, int colour, unsigned long long sweep,
                                             long long* dcur, const void* thr, int lane) {
     const PTReplica R = a.reps[sp.rep];
     int nacc = 0, nup = 0, isum = 0;
-    if (R.V == 16) pt_span<DIM, 16, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
-    else if (R.V == 8) pt_span<DIM, 8, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
-    else pt_span<DIM, 4, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    if (DIM == 3 && sp.ze > sp.zb) {
+        if (R.V == 16) pt_zwalk<16, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, sp.zb, sp.ze, colour, sweep, thr, lane, nacc, nup, isum);
+        else if (R.V == 8) pt_zwalk<8, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, sp.zb, sp.ze, colour, sweep, thr, lane, nacc, nup, isum);
+        else pt_zwalk<4, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, sp.zb, sp.ze, colour, sweep, thr, lane, nacc, nup, isum);
+    } else if (R.V == 16) {
+        pt_span<DIM, 16, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    } else if (R.V == 8) {
+        pt_span<DIM, 8, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    } else {
+        pt_span<DIM, 4, HB, T32>(a, R, sp.rep, sp.c_begin, sp.c_end, colour, sweep, thr, lane, nacc, nup, isum);
+    }
     constexpr int Z = 2 * DIM;
     long long dP, dM;
     ising_deltas<Z>(nacc, nup, isum, dP, dM);
@@ -538,11 +617,73 @@ static size_t pt_smem_persistent(const mcx_pt* pt, bool t32) {
 // one replica per phase.  Replica r gets k_r warps, handed out one at a time to the
 // replica whose cost per warp is largest (costs per site: 1.0 for 16-site rows chunks,
 // 1.15 for 8, 1.4 for 4), and its chunks are split evenly among them.
+// 3-D ladders: the units are (replica, plane column): chunks [32j, 32j + 32) of every plane
+// (fewer in a plane's last column), each walked through the planes by its warps (pt_zwalk).
+// A warp's time per plane does not depend on how many of its lanes have a chunk, so a unit
+// costs Lz planes at the per-chunk weight of its width; unit u gets k_u warps (the next warp
+// to the largest cost per warp, at most one plane each), which split its planes evenly.
+// Returns false (nothing changed) when there are more units than warps.
+static bool pt_schedule_planes(mcx_pt* pt, int nwarps, const double* w, std::vector<PTTile>& spans) {
+    struct Unit {
+        int r, c0, c1;
+        double cost;
+    };
+    std::vector<Unit> units;
+    for (int r = 0; r < pt->nrep; ++r) {
+        const PTReplica& P = pt->reps[r];
+        const int pc = P.cpr * P.Ly;
+        const double c = (double)P.Lz * P.V * (P.V == 16 ? w[0] : (P.V == 8 ? w[1] : w[2]));
+        for (int c0 = 0; c0 < pc; c0 += 32) units.push_back(Unit{r, c0, std::min(pc, c0 + 32), c});
+    }
+    const int U = (int)units.size();
+    if (U > nwarps) return false;
+    std::vector<int> k(U, 1), kr(pt->nrep, 0);
+    std::priority_queue<std::pair<double, int>> heap;
+    for (int u = 0; u < U; ++u) heap.push({units[u].cost, u});
+    for (int left = nwarps - U; left > 0 && !heap.empty();) {
+        const int u = heap.top().second;
+        heap.pop();
+        if (k[u] >= pt->reps[units[u].r].Lz) continue;  // one plane per warp at most
+        ++k[u];
+        --left;
+        heap.push({units[u].cost / k[u], u});
+    }
+    for (int u = 0; u < U; ++u) kr[units[u].r] += k[u];
+    spans.clear();
+    for (int u = 0; u < U; ++u) {
+        const PTReplica& P = pt->reps[units[u].r];
+        for (int j = 0; j < k[u]; ++j) {
+            PTTile t;
+            std::memset(&t, 0, sizeof(t));
+            t.rep = units[u].r;
+            t.c_begin = units[u].c0;
+            t.c_end = units[u].c1;
+            t.zb = (int)((long long)j * P.Lz / k[u]);
+            t.ze = (int)((long long)(j + 1) * P.Lz / k[u]);
+            t.sites = (t.c_end - t.c_begin) * P.V * (t.ze - t.zb);
+            t.nw = kr[units[u].r];
+            spans.push_back(t);
+        }
+    }
+    return true;
+}
+
 static mcx_status pt_schedule(mcx_pt* pt, int grid, int weights) {
     static const double kW[3][3] = {{1.0, 1.15, 1.4}, {1.0, 1.0, 1.0}, {1.0, 1.3, 1.8}};
     const double* w = kW[weights];
     const int nwarps = grid * 8;
     const int R = pt->nrep;
+    if (pt->dim == 3) {
+        std::vector<PTTile> spans;
+        if (pt_schedule_planes(pt, nwarps, w, spans)) {
+            PTTile idle;
+            std::memset(&idle, 0, sizeof(idle));
+            spans.resize(nwarps, idle);
+            MCX_CHECK(pt_reupload(pt, &pt->d_spans, spans));
+            pt->grid = grid;
+            return MCX_OK;
+        }
+    }
     if (nwarps < R) return fail(MCX_ERR_INVALID_ARG, "%d replicas need at least as many resident warps", R);
     std::vector<double> cost(R);
     std::vector<int> nch(R), k(R, 1);
@@ -566,6 +707,7 @@ static mcx_status pt_schedule(mcx_pt* pt, int grid, int weights) {
     for (int r = 0; r < R; ++r)
         for (int j = 0; j < k[r]; ++j) {
             PTTile t;
+            std::memset(&t, 0, sizeof(t));  // zb = ze = 0: a chunk range
             t.rep = r;
             t.c_begin = (int)((long long)j * nch[r] / k[r]);
             t.c_end = (int)((long long)(j + 1) * nch[r] / k[r]);
@@ -821,8 +963,8 @@ MCX_API mcx_status mcx_pt_create(mcx_ctx* ctx, int dim, int nladders, const int3
         pt->rep_tile0.push_back((int)pt->tiles.size());
         for (int c = 0; c < nchunks; c += per) {
             PTTile t;
+            std::memset(&t, 0, sizeof(t));
             t.rep = r;
-            t.nw = 0;
             t.c_begin = c;
             t.c_end = std::min(nchunks, c + per);
             t.sites = (t.c_end - t.c_begin) * R.V;
