@@ -185,15 +185,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(seconds, nthreads):
-    """Oracle sequential random-site mode on `nthreads` chains, sized to ~`seconds`."""
+def cpu_sample(seconds, nthreads, per_thread=None):
+    """Oracle sequential random-site mode on `nthreads` chains, sized to ~`seconds` by a pilot
+    run unless `per_thread` (attempts per chain) is given."""
     import oracle as O
 
     L = [L_SIDE, L_SIDE]
-    pilot = 200_000
-    t = O.bench_seq(O.ISING, L, O.METROPOLIS, BETA, SEED, nthreads, pilot)
-    rate = nthreads * pilot / max(t, 1e-6)
-    per_thread = max(pilot, int(rate * seconds / nthreads))
+    if per_thread is None:
+        pilot = 200_000
+        t = O.bench_seq(O.ISING, L, O.METROPOLIS, BETA, SEED, nthreads, pilot)
+        rate = nthreads * pilot / max(t, 1e-6)
+        per_thread = max(pilot, int(rate * seconds / nthreads))
     t = O.bench_seq(O.ISING, L, O.METROPOLIS, BETA, SEED, nthreads, per_thread)
     return nthreads * per_thread / (t * 1e9), t, per_thread
 
@@ -204,9 +206,9 @@ def run_reference(args):
         return
     ncores = os.cpu_count() or 1
     secs = max(1.0, min(5.0, 120.0 / max(1, args.steps + args.warmup)))
-    vals, times, per = [], [], 0
+    vals, times, per = [], [], None
     for k in range(args.warmup + args.steps):
-        v, t, per = cpu_sample(secs, ncores)
+        v, t, per = cpu_sample(secs, ncores, per)  # sized by a pilot on the first step
         if k >= args.warmup:
             vals.append(v)
             times.append(t)

@@ -620,6 +620,12 @@ typedef struct {
     int rc;
 } bench_arg_t;
 
+static void* bench_init_thread(void* p) {
+    bench_arg_t* a = (bench_arg_t*)p;
+    orc_init_random(a->s, a->model, a->dim, a->L, a->seed, a->stream);
+    return NULL;
+}
+
 static void* bench_thread(void* p) {
     bench_arg_t* a = (bench_arg_t*)p;
     uint64_t st = 0, ac = 0;
@@ -642,8 +648,10 @@ int orc_bench_seq(int model, int dim, const int32_t* L, int alg, double beta, do
         a->beta = beta; a->J = J; a->D = D; a->h = h;
         a->seed = seed; a->stream = (uint32_t)k; a->attempts = attempts_per_thread;
         a->s = (int8_t*)malloc((size_t)g.N);
-        orc_init_random(a->s, model, dim, L, seed, (uint32_t)k);
     }
+    /* every chain's start from its own stream, one thread each, before the clock starts */
+    for (int k = 0; k < nthreads; ++k) pthread_create(&th[k], NULL, bench_init_thread, &args[k]);
+    for (int k = 0; k < nthreads; ++k) pthread_join(th[k], NULL);
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     for (int k = 0; k < nthreads; ++k) pthread_create(&th[k], NULL, bench_thread, &args[k]);
