@@ -116,7 +116,7 @@ MSC_TRAFFIC_PER_LAUNCH = 2126848
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
 MSC_PIPES = {"warp_inst": 4982506, "alu_inst": 2372112, "fma_cycles": 6765216, "per": "launch"}
-PT_PIPES = {"warp_inst": 68099464 / 3, "alu_inst": 35368743 / 3, "fma_cycles": 70799920 / 3, "per": "sweep"}
+PT_PIPES = {"warp_inst": 64528754 / 3, "alu_inst": 32555444 / 3, "fma_cycles": 67545556 / 3, "per": "sweep"}
 
 
 def int_roof(pipes, seconds, sm_mhz, nsm):
