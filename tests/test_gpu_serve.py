@@ -199,6 +199,31 @@ def test_resident_loop_cancel_and_mixed_sizes(gpu):
     srv.close()
 
 
+def test_resident_loop_runs_small_jobs_many_sweeps_per_round(gpu):
+    """Small jobs (a colour within one pass of a block) run several sweeps per round on blocks
+    of their own: 16^2 Ising and 64^2 Blume-Capel jobs with thousands of sweeps, first beside a
+    512^2 job (one sweep per round each) and then alone, finish in far fewer rounds than sweeps
+    with the oracle's spins, series and counters."""
+    from mcx.serve import Server
+    srv = Server(hbm_budget=64 << 20, max_jobs=8, resident=True)
+    specs = [dict(model="ising", L=(16, 16), nsweeps=3001 + 17 * k, seed=5, stream=k, beta=0.44) for k in range(3)]
+    specs.append(dict(model="bc", L=(64, 64), D=1.0, nsweeps=777, seed=5, stream=9, beta=0.6))
+    specs.append(dict(model="ising", L=(512, 512), nsweeps=40, seed=5, stream=11, beta=0.44))
+    jobs = [srv.submit(spins=True, **sp) for sp in specs]
+    srv.run_until_idle()
+    assert srv.loop_info()["rounds"] < 1000
+    for job, sp in zip(jobs, specs):
+        assert srv.poll(job)["state"] == 2
+        model = O.ISING if sp["model"] == "ising" else O.BC
+        D = sp.get("D", 0.0)
+        s = O.init_random(model, list(sp["L"]), 5, sp["stream"])
+        obs, att, acc = O.cb_sweep(s, model, list(sp["L"]), O.METROPOLIS, sp["beta"], 5, stream=sp["stream"],
+                                   nsweeps=sp["nsweeps"], D=D)
+        assert np.array_equal(job.series, obs) and np.array_equal(job.spins, s), sp
+        assert (job.result["attempts"], job.result["accepted"]) == (att, acc)
+    srv.close()
+
+
 def _progress(srv, job):
     import ctypes as C
     from mcx import _lib as L
