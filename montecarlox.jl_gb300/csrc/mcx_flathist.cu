@@ -114,9 +114,22 @@ __device__ __forceinline__ float fh_margin(float B) {
     return B <= 3.0e38f ? (B + 64.0f) * 9.5367431640625e-07f : __int_as_float(0x7FC00000);
 }
 
-// Loads the window at wb (all lanes of the consumer); returns the margin.
-__device__ __forceinline__ float fh_window_load(FHShared& sh, const double* lnw, long long wb, long long nbins,
-                                                long long centre, int lane, double& c) {
+// x * 2^e as an integer when that is exact and below 2^52 in magnitude (the range in which
+// FP64 sums of such values are exact), else false.
+__device__ __forceinline__ bool fh_units(double x, int e, long long& n) {
+    const double y = ldexp(x, e);
+    if (!(fabs(y) < 4503599627370496.0)) return false;  // 2^52; false for NaN
+    n = (long long)y;
+    return (double)n == y;
+}
+
+// Loads the window at wb (all lanes of the consumer); returns the margin.  With g.wl_exact
+// and every value (and the centre) a multiple of logf = 2^-wl_exp in range, the window is
+// held as integers in units of logf (`exact`, icw = the centre in those units); the single-
+// precision copy is the same either way.
+__device__ __forceinline__ float fh_window_load(FHShared& sh, const FHGeom& g, const double* lnw, long long wb,
+                                                long long centre, int lane, double& c, int& exact, long long& icw) {
+    const long long nbins = g.nbins;
     const double v = lnw[centre];
     c = (v - v == 0.0) ? v : 0.0;  // v finite ? v : 0
     unsigned int m = 0;
@@ -128,17 +141,29 @@ __device__ __forceinline__ float fh_window_load(FHShared& sh, const double* lnw,
         const unsigned int a = __float_as_uint(f) & 0x7FFFFFFFu;  // |f|; NaN / inf above every finite
         m = a > m ? a : m;
     }
+    exact = 0;
+    if (g.wl_exact) {  // Wang-Landau: the integer form when every value allows it
+        bool ok = fh_units(c, g.wl_exp, icw);
+        long long n = 0;
+        for (int i = lane; i < kFHWin; i += 32) ok = ok && fh_units(sh.win[i], g.wl_exp, n);
+        exact = __all_sync(0xFFFFFFFFu, ok) ? 1 : 0;
+        if (exact) {
+            long long* iw = reinterpret_cast<long long*>(sh.win);
+            for (int i = lane; i < kFHWin; i += 32) iw[i] = (long long)ldexp(sh.win[i], g.wl_exp);
+        }
+    }
     m = __reduce_max_sync(0xFFFFFFFFu, m);
     __syncwarp();
     return fh_margin(__uint_as_float(m));
 }
 
 
-__device__ __forceinline__ void fh_window_store(const FHShared& sh, double* lnw, long long wb, long long nbins,
-                                                int lane) {
+__device__ __forceinline__ void fh_window_store(const FHShared& sh, const FHGeom& g, double* lnw, long long wb,
+                                                int lane, int exact) {
     __syncwarp();
+    const long long* iw = reinterpret_cast<const long long*>(sh.win);
     for (int i = lane; i < kFHWin; i += 32)
-        if (wb + i < nbins) lnw[wb + i] = sh.win[i];
+        if (wb + i < g.nbins) lnw[wb + i] = exact ? ldexp((double)iw[i], -g.wl_exp) : sh.win[i];
     __syncwarp();
 }
 
@@ -234,6 +259,8 @@ struct FHScan {
     float flwo;    // fwin[bi]
     float ew;      // decision margin of the window
     double cw;     // centre of the single-precision window copy
+    int exact;     // the window holds ln g in integer units of logf (Wang-Landau)
+    long long icw; // cw in those units
     unsigned long long steps;
 };
 
@@ -287,7 +314,8 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, FHSlot& sl, const FHGeom& 
         if (d > __int_as_float(cd.z) + st.ew) acc = true;
         else if (d <= __int_as_float(cd.y) - st.ew) acc = false;
         else {
-            const double lr = sh.win[bn] - sh.win[st.bi];
+            const long long* iw = reinterpret_cast<const long long*>(sh.win);
+            const double lr = st.exact ? ldexp((double)(iw[bn] - iw[st.bi]), -g.wl_exp) : sh.win[bn] - sh.win[st.bi];
             acc = (lr > 0.0) || (mcx_log((double)sl.k53[i] * 1.1102230246251565404236316680908203125e-16) < lr);
         }
         if (acc) {
@@ -298,9 +326,18 @@ __device__ __forceinline__ void fh_scan(FHShared& sh, FHSlot& sl, const FHGeom& 
             st.flwo = fa;
         }
         if (wl) {
-            const double v = sh.win[st.bi] - g.logf;
-            sh.win[st.bi] = v;
-            const float f = (float)(v - st.cw);
+            float f;
+            if (st.exact) {  // ln g -= logf is a decrement in units of logf, exact like the FP64 one
+                long long* iw = reinterpret_cast<long long*>(sh.win);
+                const long long n = iw[st.bi] - 1;
+                iw[st.bi] = n;
+                // = (float)(v - cw): rounding n - icw, then scaling by 2^-wl_exp, which is exact
+                f = __ll2float_rn(n - st.icw) * __int_as_float((127 - g.wl_exp) << 23);
+            } else {
+                const double v = sh.win[st.bi] - g.logf;
+                sh.win[st.bi] = v;
+                f = (float)(v - st.cw);
+            }
             fwin(sh)[st.bi] = f;
             st.flwo = f;
             // keep the margin valid for the changed value (NaN stays NaN)
@@ -575,7 +612,9 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
     if (!fh_bin(st.E, g, bo)) status = 2;
     const bool fast = g.shift >= 0 && g.shift <= 20;
     long long wb = fh_window_base(status ? 0 : bo, g.nbins);
-    st.ew = fh_window_load(sh, lnw, wb, g.nbins, status ? 0 : bo, lane, st.cw);
+    int exact = 0;  // the window's integer form (all lanes)
+    st.ew = fh_window_load(sh, g, lnw, wb, status ? 0 : bo, lane, st.cw, exact, st.icw);
+    st.exact = exact;
     st.Ewb = g.start + wb * g.step;
     st.er = (int)(st.E - st.Ewb);
     st.bi = status ? 0 : (int)(bo - wb);
@@ -628,15 +667,18 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
                         // move the window around the proposed bin (the current bin stays
                         // inside: one move changes the bin by far less than half the window);
                         // the bins recorded so far in this batch are rebased on the new window
-                        if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
+                        if (g.mode == 1) fh_window_store(sh, g, lnw, wb, lane, exact);
                         const long long bo_all = __shfl_sync(0xFFFFFFFFu, wb + st.bi, 0);
                         const long long wb_new = fh_window_base(need, g.nbins);
                         __syncwarp();
                         if (lane < i) sl.bin[lane] += (int)(wb - wb_new);
                         __syncwarp();
-                        const float ew = fh_window_load(sh, lnw, wb_new, g.nbins, need, lane, st.cw);
+                        long long icw = 0;
+                        const float ew = fh_window_load(sh, g, lnw, wb_new, need, lane, st.cw, exact, icw);
                         if (lane == 0) {
                             st.ew = ew;
+                            st.exact = exact;
+                            st.icw = icw;
                             st.er += (int)((wb - wb_new) * g.step);  // FAST only (wb moves < 2^11 bins)
                             st.Ewb = g.start + wb_new * g.step;
                             st.bi = (int)(bo_all - wb_new);
@@ -664,7 +706,7 @@ __global__ void __launch_bounds__(64, 1) k_flathist(const FHArgs a) {
             fh_bar_arrive(kFHBarCol);
         }
     }
-    if (g.mode == 1) fh_window_store(sh, lnw, wb, g.nbins, lane);
+    if (g.mode == 1) fh_window_store(sh, g, lnw, wb, lane, exact);
     if (lane == 0) {
         w.steps = st.steps;
         w.accepted = accepted;
@@ -958,6 +1000,14 @@ MCX_API mcx_status mcx_flathist_sweep(mcx_lattice* const* lats, int nwalkers, mc
     g.shift = fh_shift(F0->step);
     g.mode = mode == MCX_MUCA ? 0 : 1;
     g.logf = logf;
+    {
+        int ex = 0;
+        const double mant = std::frexp(logf, &ex);  // logf = mant * 2^ex
+        if (g.mode == 1 && mant == 0.5 && 1 - ex >= 0 && 1 - ex <= 40) {
+            g.wl_exact = 1;
+            g.wl_exp = 1 - ex;  // logf = 2^-wl_exp
+        }
+    }
     g.nsweeps = nsweeps;
     for (auto& w : hw) w.g = g;
     cudaError_t e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(FHWalker), cudaMemcpyHostToDevice, ctx->stream);

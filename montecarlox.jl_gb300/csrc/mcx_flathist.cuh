@@ -28,6 +28,12 @@ struct FHGeom {
     int mode;   // 0 MUCA, 1 Wang-Landau
     double logf;
     long long nsweeps;
+    // Wang-Landau with logf = 2^-wl_exp (0 <= wl_exp <= 40): windows whose ln g values are all
+    // multiples of 2^-wl_exp below 2^(52 - wl_exp) in magnitude are held as integers in units
+    // of logf, so the update ln g -= logf is an integer decrement (the FP64 subtraction of the
+    // reference is exact on such values, so the results are the same bits).  0: off.
+    int wl_exact;
+    int wl_exp;
 };
 
 struct FHWalker {

@@ -35,6 +35,12 @@ CASES = [
     # more bins than the 512-bin shared-memory window: the energy drifts and the window moves
     (O.BC, [32, 32], 1.0, (-1024, 1, 4097), "muca", 4, True, 0.0, 20, "beta"),
     (O.ISING, [32, 32], 0.0, (-2048, 1, 4097), "wl", 2, False, 0.05, 10, "beta"),
+    # Wang-Landau with ln f a power of two holds windows of multiples of ln f as integers: with
+    # moving windows (Ising and Blume-Capel), and weights that are not such multiples (the
+    # FP64 form is kept)
+    (O.ISING, [32, 32], 0.0, (-2048, 1, 4097), "wl", 2, False, 2.0 ** -10, 10, "flat"),
+    (O.BC, [32, 32], 1.0, (-1024, 1, 4097), "wl", 2, False, 0.5, 15, "flat"),
+    (O.BC, [32, 32], 1.0, (-1024, 1, 4097), "wl", 2, False, 1.0, 10, "beta"),
     (O.ISING, [8, 8, 8], 0.0, (-1536, 2, 1537), "muca", 3, True, 0.0, 6, "beta"),
     # bin width not a power of two: the general 64-bit binning path
     (O.ISING, [16, 16], 0.0, (-512, 12, 86), "muca", 2, True, 0.0, 10, "beta"),
