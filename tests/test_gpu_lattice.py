@@ -95,8 +95,9 @@ def test_msc64_matches_int8_and_oracle(gpu, L, alg):
 
 @pytest.mark.parametrize("L,beta,h", [([128, 16, 8], 0.22, 0.0), ([256, 32], 0.5, 0.25), ([128, 64], 3.0, 0.0)])
 def test_msc64_metropolis_forms(gpu, L, beta, h):
-    """MSC64 Metropolis: the rank-form kernel (no field; also with thresholds of 0 at large
-    beta) and the general kernel (field) against the oracle."""
+    """MSC64 Metropolis: the rank-form kernel on the packed words (no field; also with
+    thresholds of 0 at large beta) and, with a field, the int8 arrays of the lattice
+    (unpacked before and packed after the call) against the oracle."""
     sys_, a, obs, s, oobs, att, acc = _run_pair(gpu, O.ISING, L, "metropolis", beta, h=h, layout="msc64")
     assert np.array_equal(obs, oobs)
     assert np.array_equal(sys_.spins, s)
@@ -374,6 +375,29 @@ def test_argument_errors(gpu):
         gpu.init_(sys_, "zero")
     with pytest.raises(gpu.ArgumentError):
         gpu.init_(sys_, "random")
+
+
+@pytest.mark.parametrize("L,layout", [([8, 8], "int8"), ([2048, 1024], "int8"), ([128, 64], "msc64")])
+def test_sweep_call_edges(gpu, L, layout):
+    """Zero sweeps change nothing and return an empty series (on the one-block, packed-copy
+    and MSC64 paths); a negative count, a non-finite beta and a sweep counter beyond 2^48 are
+    argument errors that leave the lattice and the rng as they were."""
+    sys_ = gpu.Ising(L, layout=layout)
+    gpu.init_(sys_, "random", rng=gpu.Philox(3))
+    s0 = sys_.spins
+    e0 = gpu.observables(sys_)
+    a = gpu.Metropolis(gpu.Philox(3), beta=0.44)
+    obs = gpu.sweep_(sys_, a, 0, record=True)
+    assert obs.shape == (0, 3) and a.steps == 0 and a.rng.counter == 0
+    assert np.array_equal(sys_.spins, s0) and gpu.observables(sys_) == e0
+    with pytest.raises(gpu.ArgumentError):
+        gpu.sweep_(sys_, a, -1)
+    with pytest.raises(gpu.ArgumentError):
+        gpu.sweep_(sys_, gpu.Metropolis(gpu.Philox(3), beta=float("nan")), 1)
+    with pytest.raises(gpu.ArgumentError):
+        gpu.sweep_(sys_, gpu.Metropolis(gpu.Philox(3, 0, (1 << 48) - 4), beta=0.44), 20)
+    assert np.array_equal(sys_.spins, s0) and a.rng.counter == 0
+    sys_.close()
 
 
 def test_hbm_budget(gpu):
