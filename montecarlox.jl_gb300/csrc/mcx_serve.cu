@@ -85,22 +85,50 @@ __device__ __forceinline__ void srv_tile(const SrvJobDev& J, const SrvTile& tl, 
 }
 
 // One colour of sweep s of the current chunk, for the tiles of every active
-// canonical job (tiles of jobs with fewer than s+1 sweeps left are skipped).
+// canonical job (tiles of jobs with fewer than s+1 sweeps left are skipped).  Every block
+// takes an equal contiguous range of the tiles (laid out job by job), so it loads a job's
+// table and flushes its counts once per job rather than once per tile.
 __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const SrvTile* tiles, int ntiles,
                                                   const unsigned long long* tables, int colour, int s) {
     __shared__ __align__(16) unsigned long long s_thr[kMaxTable];
-    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-        const SrvTile tl = tiles[ti];
+    const int t_lo = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+    const int t_hi = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+    int cur = -1;  // job whose table is loaded and whose counts accumulate
+    int nacc = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int ti = t_lo; ti <= t_hi; ++ti) {
+        const SrvTile tl = ti < t_hi ? tiles[ti] : SrvTile{-1, 0, 0, 0};
+        if (cur >= 0 && tl.job != cur) {  // flush the previous job's counts
+            const SrvJobDev& P = jobs[cur];
+            long long dP, dM, dQ;
+            if (P.model == 0) {
+                ising_deltas<4>(nacc, a1, a2, dP, dM);
+                dQ = 0;
+            } else {
+                dP = a1;
+                dM = a2;
+                dQ = a3;
+            }
+            long long v[4] = {dP, dM, dQ, (long long)nacc};
+            unsigned long long* const dst[4] = {(unsigned long long*)&P.series[3 * s],
+                                                (unsigned long long*)&P.series[3 * s + 1],
+                                                (unsigned long long*)&P.series[3 * s + 2], P.acc};
+            block_add_atomic<4>(v, dst);
+            nacc = a1 = a2 = a3 = 0;
+            cur = -1;
+        }
+        if (ti == t_hi) break;
         const SrvJobDev J = jobs[tl.job];
         if (s >= J.todo) continue;  // uniform over the block
-        __syncthreads();
-        for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
-            const unsigned long long x = tables[(size_t)tl.job * kMaxTable + i];
-            s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
+        if (cur != tl.job) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < kMaxTable; i += blockDim.x) {
+                const unsigned long long x = tables[(size_t)tl.job * kMaxTable + i];
+                s_thr[i] = J.model == 0 ? ising_tab_entry(x, i, 4, J.hb != 0) : x;
+            }
+            __syncthreads();
+            cur = tl.job;
         }
-        __syncthreads();
         const unsigned long long t = J.t0 + (unsigned long long)s;
-        int nacc = 0, a1 = 0, a2 = 0, a3 = 0;
         const int key = J.V * 4 + J.model * 2 + J.hb;
         switch (key) {
             case 16 * 4 + 0: srv_tile<16, 0, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
@@ -116,20 +144,6 @@ __global__ void __launch_bounds__(256) k_srv_half(const SrvJobDev* jobs, const S
             case 4 * 4 + 2: srv_tile<4, 1, false>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
             default: srv_tile<4, 1, true>(J, tl, colour, t, s_thr, nacc, a1, a2, a3); break;
         }
-        long long dP, dM, dQ;
-        if (J.model == 0) {
-            ising_deltas<4>(nacc, a1, a2, dP, dM);
-            dQ = 0;
-        } else {
-            dP = a1;
-            dM = a2;
-            dQ = a3;
-        }
-        long long v[4] = {dP, dM, dQ, (long long)nacc};
-        unsigned long long* const dst[4] = {(unsigned long long*)&J.series[3 * s],
-                                            (unsigned long long*)&J.series[3 * s + 1],
-                                            (unsigned long long*)&J.series[3 * s + 2], J.acc};
-        block_add_atomic<4>(v, dst);
     }
 }
 
