@@ -61,6 +61,20 @@ typedef enum mcx_algorithm { MCX_METROPOLIS = 0, MCX_GLAUBER = 1, MCX_HEATBATH =
  * (Ising only; needs Lx a multiple of 128). */
 typedef enum mcx_layout { MCX_LAYOUT_INT8 = 0, MCX_LAYOUT_MSC64 = 1 } mcx_layout;
 
+/* How checkerboard sweeps of a lattice draw the 32-bit uniform u that a site's
+ * Metropolis decision u < threshold compares (both forms give every site an independent
+ * uniform on [0, 2^32)).
+ *   SITE (default): u is word e & 3 of one Philox4x32-10 block at counter e >> 2, e the
+ *         site's index among the sites of its colour (one block per four sites).
+ *   PLANES: the top 8 bits of u are bit planes: four Philox blocks per 64 same-colour
+ *         sites give planes 0..7 (block j holds planes 2j and 2j+1 as two 64-bit words,
+ *         bit b of a plane for site b of the 64), compared with the thresholds bit by bit
+ *         for 64 sites at once; the low 24 bits come from a per-site block (like SITE,
+ *         another counter purpose) and are drawn only for the sites whose top 8 bits equal
+ *         their threshold's.  Applies to Ising Metropolis without a field (the rules
+ *         swept on 64-sites-per-word words); every other rule draws the SITE form. */
+typedef enum mcx_uniforms { MCX_UNIFORMS_SITE = 0, MCX_UNIFORMS_PLANES = 1 } mcx_uniforms;
+
 /* Flat-histogram mode: Multicanonical (src/algorithms/multicanonical.jl) or
  * Wang-Landau (src/algorithms/wang_landau.jl). */
 typedef enum mcx_flathist_mode { MCX_MUCA = 0, MCX_WANG_LANDAU = 1 } mcx_flathist_mode;
@@ -163,6 +177,14 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
  * of device memory on first use within the HBM budget.  Results are bit-identical either
  * way; the copy is faster.  Default on; off keeps every call on the int8 kernels. */
 MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow);
+/* Selects the uniforms of later sweeps (mcx_uniforms; default SITE).  PLANES needs an
+ * Ising lattice with Lx a multiple of 128 (MCX_ERR_INVALID_ARG otherwise); on the int8
+ * layout its Metropolis calls run on the transient 64-sites-per-word copy whatever their
+ * length, so mcx_sweep returns MCX_ERR_INVALID_ARG with packing off and MCX_ERR_BUDGET /
+ * MCX_ERR_OOM when the N/8-byte copy does not fit.  mcx_sweep_noalloc (int8 kernels
+ * only) refuses such calls; mcx_sweep_batch runs them one mcx_sweep per lattice.  The two
+ * forms give different chains with the same distribution. */
+MCX_API mcx_status mcx_lattice_set_uniforms(mcx_lattice* lat, int32_t form);
 /* Times the admissible kernel shapes (sites per thread: 16, 8, 4) for this lattice
  * and algorithm on a scratch copy of the spins and keeps the fastest for later
  * mcx_sweep calls; results never depend on the choice.  chosen / ns_per_site may be

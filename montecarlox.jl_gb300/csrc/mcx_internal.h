@@ -21,7 +21,9 @@ enum Purpose : uint32_t {
     P_INIT = 3,     // init!(sys, :random)
     P_EXCHANGE = 4,  // replica-exchange uniform
     P_GRAPH = 7,     // 53-bit uniform of a site of a general graph (words 0 and 1)
-    P_GRAPH_INIT = 8  // init!(sys, :random) of a general graph
+    P_GRAPH_INIT = 8,  // init!(sys, :random) of a general graph
+    P_PLANES = 9,      // bit planes 0..7 of the MCX_UNIFORMS_PLANES uniforms (four blocks per 64 sites)
+    P_TAIL = 10        // low 24 bits of a MCX_UNIFORMS_PLANES uniform (word e & 3 of block e >> 2)
 };
 
 void set_error(const char* fmt, ...);
@@ -120,6 +122,7 @@ struct mcx_lattice {
     int64_t device_bytes = 0;
     int tuned_V = 0;               // row width chosen by mcx_autotune (0 = default)
     int allow_packing = 1;         // int8: multi-sweep calls may use a transient MSC64 copy
+    int uniforms = 0;              // mcx_uniforms of rank-form Metropolis sweeps
     int cluster_size = 0;          // CTAs of the last cluster-form call (0: not tried, -1: none fits)
     // that call's kernel, block size and shared memory, reused while its key (heat bath,
     // 32-bit table) is the same, so later calls skip the occupancy query (about 1 us of the

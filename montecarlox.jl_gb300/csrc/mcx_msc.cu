@@ -18,6 +18,8 @@ struct MscArgs {
     const unsigned long long* oth;
     int nw;  // words per row
     int W, Ly, Lz, rows, colour;
+    int nw_shift, ly_shift;  // log2 of nw / Ly when they are powers of two, else -1
+    uint32_t pmask[8][3];    // bit-plane uniforms: all ones where bit 31-p of class k's threshold is set
     uint32_t k0, k1, stream;
     unsigned long long sweep;
     unsigned long long* dst[2];
@@ -88,9 +90,14 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
 // neighbours are counted bit-sliced (c0, c1, c2) for 64 sites at once; each site's
 // uniform is compared with the K = Z/2 thresholds into bit masks A_k (u < t_k), and the
 // flips are the always-class sites plus, per class k, the sites whose A_k bit is set.
-// Same Philox word per site as every other kernel, so results are bit-identical.
-template <int DIM>
-__global__ void __launch_bounds__(256, 3) k_msc_metro(const MscArgs a) {
+// PL = false: the per-site Philox word of every other kernel, so results are bit-identical
+// to theirs.  PL = true: the bit-plane uniforms (mcx_uniforms PLANES): four Philox blocks
+// give planes 0..7 of the 64 sites (bits 31..24 of u), compared with the thresholds bit by
+// bit, most significant first, for all 64 sites at once; a site is decided at the first
+// plane where its bit and its threshold's differ, and only the sites tied after 8 planes
+// (probability 2^-8 each) draw the low 24 bits from a per-site block.
+template <int DIM, bool PL>
+__global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
     constexpr int Z = 2 * DIM;
     constexpr int K = Z / 2;
     uint32_t tk[K];
@@ -99,17 +106,20 @@ __global__ void __launch_bounds__(256, 3) k_msc_metro(const MscArgs a) {
     pdl_trigger();
     pdl_wait();  // the previous half-sweep's words are complete
     const int nwords = a.nw * a.rows;  // < 2^28 words (N <= 2^34 sites)
-    const uint32_t w2 = ctr_word2(a.sweep, a.colour, P_ACCEPT);
-    const PhiloxPre pre = philox_pre((uint32_t)a.sweep, w2, a.k0);
-    unsigned long long nacc = 0, asum = 0, nup = 0;
+    const PhiloxPre pre = philox_pre((uint32_t)a.sweep, ctr_word2(a.sweep, a.colour, PL ? P_PLANES : P_ACCEPT), a.k0);
+    const PhiloxPre pre_tail = philox_pre((uint32_t)a.sweep, ctr_word2(a.sweep, a.colour, P_TAIL), a.k0);
+    // a thread's counts fit 32 bits: at most 64 * 6 per word, ceil(2^27 / 131,328) words
+    uint32_t nacc = 0, asum = 0, nup = 0;
     // every block takes an equal contiguous range of words (with 3 blocks per SM 2 % faster
-    // on a GB300 than the grid-stride walk; 2 or 4 blocks per SM were slower either way)
+    // on a GB300 than the grid-stride walk; 2 or 4 blocks per SM were slower either way);
+    // 288 threads per block give the 131,072 words of a 4096^2 or 256^3 colour one word per
+    // thread (256 left 31 threads of each block a second word: 3-8 % slower)
     const int gb = (int)((long long)blockIdx.x * nwords / gridDim.x);
     const int ge = (int)((long long)(blockIdx.x + 1) * nwords / gridDim.x);
     for (int g = gb + threadIdx.x; g < ge; g += blockDim.x) {
-        const int r = g / a.nw;
+        const int r = a.nw_shift >= 0 ? g >> a.nw_shift : g / a.nw;
         const int w = g - r * a.nw;
-        const int z = DIM == 3 ? r / a.Ly : 0;
+        const int z = DIM == 3 ? (a.ly_shift >= 0 ? r >> a.ly_shift : r / a.Ly) : 0;
         const int y = r - z * a.Ly;
         const int p = (y + z + a.colour) & 1;
         const long long ryp = (y + 1 == a.Ly ? 0 : y + 1) + (long long)a.Ly * z;
@@ -149,35 +159,89 @@ __global__ void __launch_bounds__(256, 3) k_msc_metro(const MscArgs a) {
         }
         unsigned long long flip = ~c2;
         if constexpr (DIM == 2) flip = ~(m[0] | m[1]);
-        // u < t_k for the 64 sites of the word (16 Philox blocks of four words)
-        uint32_t A[K][2];
-#pragma unroll
-        for (int k = 0; k < K; ++k) A[k][0] = A[k][1] = 0u;
         const uint32_t cbase = (uint32_t)(((unsigned long long)r * a.W + 64ull * w) >> 2);
+        if constexpr (PL) {
+            unsigned long long tied = 0, lt = 0;  // sites still tied with their threshold / u < t
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const uint4 rnd = philox10_pre(cbase + q, a.stream, pre, a.k0, a.k1);
-            const uint32_t us[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+            for (int k = 0; k < K; ++k) tied |= m[k];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int j = 4 * q + b;
+            for (int j = 0; j < 4; ++j) {
+                const uint4 rnd = philox10_pre(cbase + j, a.stream, pre, a.k0, a.k1);
+                const unsigned long long R[2] = {((unsigned long long)rnd.y << 32) | rnd.x,
+                                                 ((unsigned long long)rnd.w << 32) | rnd.z};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    unsigned long long T = 0;  // the threshold's bit of every site
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const uint32_t pm = a.pmask[2 * j + h][k];
+                        T |= m[k] & (((unsigned long long)pm << 32) | pm);
+                    }
+                    lt |= tied & T & ~R[h];
+                    tied &= ~(T ^ R[h]);
+                }
+            }
+            while (tied) {  // top 8 bits equal: compare the low 24
+                const int b = __ffsll((long long)tied) - 1;
+                tied &= tied - 1;
+                const uint4 rr = philox10_pre(cbase + (uint32_t)(b >> 2), a.stream, pre_tail, a.k0, a.k1);
+                uint32_t t24 = 0;
 #pragma unroll
                 for (int k = 0; k < K; ++k)
-                    if (us[b] < tk[k]) A[k][j >> 5] |= 1u << (j & 31);
+                    if ((m[k] >> b) & 1ull) t24 = tk[k] & 0xFFFFFFu;
+                if ((pick4(rr, b & 3) & 0xFFFFFFu) < t24) lt |= 1ull << b;
             }
-        }
+            flip |= lt;
+        } else {
+            // u < t_k for the 64 sites of the word (16 Philox blocks of four words)
+            uint32_t A[K][2];
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            flip |= m[k] & (((unsigned long long)A[k][1] << 32) | A[k][0]);
+            for (int k = 0; k < K; ++k) A[k][0] = A[k][1] = 0u;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const uint4 rnd = philox10_pre(cbase + q, a.stream, pre, a.k0, a.k1);
+                const uint32_t us[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int j = 4 * q + b;
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (us[b] < tk[k]) A[k][j >> 5] |= 1u << (j & 31);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                flip |= m[k] & (((unsigned long long)A[k][1] << 32) | A[k][0]);
+        }
         a.cur[g] = own ^ flip;
         nacc += __popcll(flip);
         nup += __popcll(flip & own);
-        asum += __popcll(flip & c0) + 2ull * __popcll(flip & c1) + 4ull * __popcll(flip & c2);
+        asum += __popcll(flip & c0) + 2u * __popcll(flip & c1) + 4u * __popcll(flip & c2);
     }
-    long long v[3] = {2ll * Z * (long long)nacc - 4ll * (long long)asum, 2ll * (long long)nacc - 4ll * (long long)nup,
-                      (long long)nacc};
-    unsigned long long* const dst[3] = {a.dst[0], a.dst[1], a.acc};
-    block_add_atomic<3>(v, dst);
+    // warp sums by redux (below 2^24), block sums likewise (below 2^29), then one atomic
+    // per series entry per block
+    __shared__ uint32_t red[3][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t w0 = __reduce_add_sync(0xFFFFFFFFu, nacc), w1 = __reduce_add_sync(0xFFFFFFFFu, asum),
+                   w2 = __reduce_add_sync(0xFFFFFFFFu, nup);
+    if (lane == 0) {
+        red[0][warp] = w0;
+        red[1][warp] = w1;
+        red[2][warp] = w2;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const bool in = lane < (int)(blockDim.x >> 5);
+        const uint32_t n = __reduce_add_sync(0xFFFFFFFFu, in ? red[0][lane] : 0u);
+        const uint32_t as = __reduce_add_sync(0xFFFFFFFFu, in ? red[1][lane] : 0u);
+        const uint32_t up = __reduce_add_sync(0xFFFFFFFFu, in ? red[2][lane] : 0u);
+        if (lane == 0 && n != 0) {
+            const long long dP = 2ll * Z * n - 4ll * as, dM = 2ll * n - 4ll * up;
+            if (dP != 0) atomicAdd(a.dst[0], (unsigned long long)dP);
+            if (dM != 0) atomicAdd(a.dst[1], (unsigned long long)dM);
+            atomicAdd(a.acc, (unsigned long long)n);
+        }
+    }
 }
 
 // Whether a table has the rank form of k_msc_metro: always for <= Z/2 aligned
@@ -206,25 +270,41 @@ bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
 // form of k_msc_metro, rows of a multiple of 64 same-colour sites.  Same stream, same
 // results; the copy is allocated on first use (within the HBM budget, else the call
 // stays on the int8 kernels).
-bool msc_transient_ok(mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
-    if (lat->layout != MCX_LAYOUT_INT8 || !lat->allow_packing || lat->L[0] % 128 != 0 || !msc_rank_ok(lat, alg, t))
-        return false;
-    if (lat->d_msc[0]) return true;
+// Allocates the transient copy once (MCX_OK, MCX_ERR_BUDGET or MCX_ERR_OOM; sets no error).
+static mcx_status msc_copy_alloc(mcx_lattice* lat) {
+    if (lat->d_msc[0]) return MCX_OK;
     mcx_ctx* ctx = lat->ctx;
     const size_t bytes = (size_t)(lat->N / 2) / 8;
-    if (ctx->budget && ctx->used + 2 * bytes > ctx->budget) return false;
+    if (ctx->budget && ctx->used + 2 * bytes > ctx->budget) return MCX_ERR_BUDGET;
     void* p0 = nullptr;
     void* p1 = nullptr;
     if (cudaMalloc(&p0, bytes) != cudaSuccess || cudaMalloc(&p1, bytes) != cudaSuccess) {
-        cudaGetLastError();  // a failed allocation leaves no sticky error; the int8 kernels run
+        cudaGetLastError();  // a failed allocation leaves no sticky error
         if (p0) cudaFree(p0);
-        return false;
+        return MCX_ERR_OOM;
     }
     ctx->used += 2 * bytes;
     lat->device_bytes += (int64_t)(2 * bytes);
     lat->d_msc[0] = (unsigned long long*)p0;
     lat->d_msc[1] = (unsigned long long*)p1;
-    return true;
+    return MCX_OK;
+}
+
+bool msc_transient_ok(mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
+    if (lat->layout != MCX_LAYOUT_INT8 || !lat->allow_packing || lat->L[0] % 128 != 0 || !msc_rank_ok(lat, alg, t))
+        return false;
+    return msc_copy_alloc(lat) == MCX_OK;  // else the call stays on the int8 kernels
+}
+
+// The transient copy that a rank-form call with bit-plane uniforms of an int8 lattice
+// must run on (the int8 kernels draw per-site words only).
+mcx_status msc_planes_copy(mcx_lattice* lat) {
+    if (!lat->allow_packing)
+        return fail(MCX_ERR_INVALID_ARG, "bit-plane uniforms sweep the packed copy, and packing is off");
+    const mcx_status st = msc_copy_alloc(lat);
+    if (st != MCX_OK)
+        return fail(st, "bit-plane uniforms: no room for the packed copy (%lld bytes)", (long long)(lat->N / 8));
+    return MCX_OK;
 }
 
 static int grid_cap(const mcx_ctx* ctx, long long work) {
@@ -268,8 +348,17 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_
     a.stream = rng->stream;
     a.acc = lat->d_acc;
     for (int i = 0; i < t.n && i < 14; ++i) a.thr[i] = t.thr[i];
-    void (*fn)(const MscArgs) = lat->dim == 2 ? k_msc_metro<2> : k_msc_metro<3>;
-    const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 256, 0);  // one wave
+    auto log2_or = [](long long v) { return v > 0 && (v & (v - 1)) == 0 ? __builtin_ctzll((unsigned long long)v) : -1; };
+    a.nw_shift = log2_or(a.nw);
+    a.ly_shift = log2_or(a.Ly);
+    const int Z = 2 * lat->dim;
+    for (int p = 0; p < 8; ++p)
+        for (int k = 0; k < 3; ++k)
+            a.pmask[p][k] = k < Z / 2 && ((t.thr[Z / 2 + 1 + k] >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
+    const bool pl = lat->uniforms == MCX_UNIFORMS_PLANES;
+    void (*fn)(const MscArgs) = lat->dim == 2 ? (pl ? k_msc_metro<2, true> : k_msc_metro<2, false>)
+                                              : (pl ? k_msc_metro<3, true> : k_msc_metro<3, false>);
+    const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 288, 0);  // one wave
     // every launch after the first depends programmatically on the one before (the
     // kernels read the lattice after pdl_wait)
     cudaLaunchAttribute pdl[1];
@@ -277,7 +366,7 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_
     pdl[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(288);
     cfg.stream = ctx->stream;
     cfg.attrs = pdl;
     for (int64_t s = 0; s < nsweeps; ++s) {
@@ -302,5 +391,15 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_
 extern "C" MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow) {
     if (!lat) return mcx::fail(MCX_ERR_INVALID_ARG, "lattice is NULL");
     lat->allow_packing = allow ? 1 : 0;
+    return MCX_OK;
+}
+
+extern "C" MCX_API mcx_status mcx_lattice_set_uniforms(mcx_lattice* lat, int32_t form) {
+    if (!lat) return mcx::fail(MCX_ERR_INVALID_ARG, "lattice is NULL");
+    if (form != MCX_UNIFORMS_SITE && form != MCX_UNIFORMS_PLANES)
+        return mcx::fail(MCX_ERR_INVALID_ARG, "unknown uniforms form %d", (int)form);
+    if (form == MCX_UNIFORMS_PLANES && (lat->model != MCX_ISING || lat->L[0] % 128 != 0))
+        return mcx::fail(MCX_ERR_INVALID_ARG, "bit-plane uniforms need an Ising lattice with Lx a multiple of 128");
+    lat->uniforms = form;
     return MCX_OK;
 }

@@ -609,9 +609,9 @@ void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const
 mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
                      int64_t nsweeps);  // mcx_msc.cu
 bool msc_transient_ok(mcx_lattice* lat, mcx_algorithm alg, const Table& t);  // mcx_msc.cu
-bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t);  // mcx_msc.cu
 mcx_status msc_pack(mcx_lattice* lat);                                       // mcx_msc.cu
 mcx_status msc_unpack(mcx_lattice* lat);                                     // mcx_msc.cu
+mcx_status msc_planes_copy(mcx_lattice* lat);                                // mcx_msc.cu
 
 __global__ void k_set_key(unsigned long long* p, unsigned long long sweep, unsigned long long seed,
                           unsigned long long stream) {
@@ -722,17 +722,22 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // MSC64 lattices sweep the packed words only under k_msc_metro's rank form; other rules
     // run on their int8 arrays (unpacked before, packed after the call), which is faster
     // than a per-site table lookup on the words
+    // A rank-form call with bit-plane uniforms always runs on the words: an int8 lattice's
+    // on its transient copy, whatever the call's length (the int8 kernels draw per-site words).
     const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && msc_rank_ok(lat, alg, t);
     const bool via_int8 = lat->layout == MCX_LAYOUT_MSC64 && !msc_words;
     const bool int8 = lat->layout == MCX_LAYOUT_INT8 || via_int8;
+    const bool planes = lat->layout == MCX_LAYOUT_INT8 && lat->uniforms == MCX_UNIFORMS_PLANES && nsweeps > 0 &&
+                        msc_rank_ok(lat, alg, t);
+    if (planes) MCX_CHECK(msc_planes_copy(lat));
     if (via_int8) MCX_CHECK(msc_unpack(lat));
     MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
     MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
     // large int8 Ising lattices under a rank-form Metropolis rule run calls of kMscMinSweeps
     // sweeps or more on a transient 64-sites-per-word copy (k_msc_metro: 25 % faster than the
     // int8 words; packing and unpacking cost about two sweeps' worth of one-pass copies)
-    const bool transient = int8 && lat->N > kClusterLattice && nsweeps >= kMscMinSweeps &&
-                           msc_transient_ok(lat, alg, t);
+    const bool transient = planes || (int8 && lat->N > kClusterLattice && nsweeps >= kMscMinSweeps &&
+                                      msc_transient_ok(lat, alg, t));
     bool clustered = false;
     if (!transient && int8 && lat->N > kClusterMin) MCX_CHECK(cluster_sweep(lat, alg, t, rng, nsweeps, &clustered));
     const bool small = !transient && !clustered && int8 && lat->N <= kSmallLattice && nsweeps >= 1;
@@ -959,6 +964,15 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
     if (nsweeps == 0) return MCX_OK;
     if (n == 1)  // the single-lattice forms
         return mcx_sweep(lats[0], alg, betas[0], &rngs[0], nsweeps, obs_series ? obs_series[0] : nullptr, counters);
+    bool planes = false;  // bit-plane uniforms run on the words, one mcx_sweep per lattice
+    for (int i = 0; i < n; ++i)
+        planes = planes || (lats[i]->uniforms == MCX_UNIFORMS_PLANES && msc_rank_ok(lats[i], alg, tabs[i]));
+    if (planes) {
+        for (int i = 0; i < n; ++i)
+            MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
+                                counters ? &counters[i] : nullptr));
+        return MCX_OK;
+    }
     // One cluster per lattice in one launch: medium lattices always; lattices the one-block
     // form also takes (above kClusterMin sites) when the device runs every cluster at once
     // (a few 128^2 chains: 1.5 against 3.6 us per sweep; many chains fill more SMs one block

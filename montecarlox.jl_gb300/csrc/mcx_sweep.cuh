@@ -61,6 +61,8 @@ constexpr long long kClusterLattice = 524288;
 // chunk width of the one-block and cluster kernels for rows of W sites of a colour and
 // `sites` sites of a colour per block
 int small_width(int64_t W, long long sites);
+// whether `alg` with table `t` has the rank form swept on 64-sites-per-word words (mcx_msc.cu)
+bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t);
 // the cluster form; *done = false when it does not apply or no cluster fits the device
 mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
                          bool* done);

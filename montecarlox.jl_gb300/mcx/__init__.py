@@ -289,9 +289,18 @@ class DeviceLattice(AbstractSpinSystem):
                                            float(D), float(h), C.byref(hdl)))
         self.handle = hdl
         self.N = int(np.prod(self.dims))
+        self.uniforms = "site"
 
     def __len__(self):
         return self.N
+
+    def set_uniforms(self, form="planes"):
+        """How Metropolis sweeps without a field draw their uniforms (mcx_lattice_set_uniforms):
+        "site" (one Philox word per site, the default) or "planes" (bit planes for the top 8
+        bits, compared for 64 sites at once; Ising, Lx a multiple of 128).  Same distribution,
+        different chain."""
+        _check(L.load().mcx_lattice_set_uniforms(self.handle, {"site": 0, "planes": 1}[form]))
+        self.uniforms = form
 
     def set_packing(self, allow=True):
         """Whether multi-sweep calls may run on a transient 64-sites-per-word copy of this

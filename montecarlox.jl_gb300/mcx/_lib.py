@@ -77,6 +77,7 @@ SIGNATURES = {
                                   C.POINTER(C.c_void_p), C.POINTER(mcx_counters)]),
     "mcx_autotune": (C.c_int, [_P, C.c_int, C.c_double, _i32p, _f64p]),
     "mcx_lattice_set_packing": (C.c_int, [_P, C.c_int32]),
+    "mcx_lattice_set_uniforms": (C.c_int, [_P, C.c_int32]),
     "mcx_flathist_create": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "mcx_flathist_destroy": (C.c_int, [_P]),
     "mcx_flathist_set_logweight": (C.c_int, [_P, _P, C.c_int64]),

@@ -30,7 +30,7 @@ def export_state(obj):
     if isinstance(obj, (IsingDevice, BlumeCapelDevice)):
         return {"kind": "lattice", "model": "bc" if isinstance(obj, BlumeCapelDevice) else "ising",
                 "dims": list(obj.dims), "J": obj.J, "D": obj.D, "h": obj.h, "layout": obj.layout,
-                "spins": obj.spins}
+                "uniforms": obj.uniforms, "spins": obj.spins}
     from .graph import GraphDevice
     if isinstance(obj, GraphDevice):
         return {"kind": "graph", "model": obj.MODEL, "rowptr": obj.rowptr, "col": obj.col, "coupling": obj.coupling,
@@ -86,6 +86,8 @@ def import_state(d, ctx=None):
             s = BlumeCapel(d["dims"], J=d["J"], D=d["D"], h=d["h"], ctx=ctx)
         else:
             s = Ising(d["dims"], J=d["J"], h=d["h"], layout=d["layout"], ctx=ctx)
+            if d.get("uniforms", "site") != "site":
+                s.set_uniforms(d["uniforms"])
         s.spins = d["spins"]
         return s
     if k == "graph":

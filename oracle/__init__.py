@@ -48,6 +48,9 @@ def lib():
         L.orc_cb_sweep.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64, C.c_void_p,
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_cb_sweep_u.argtypes = L.orc_cb_sweep.argtypes + [C.c_int]
+        L.orc_plane_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_uint64]
+        L.orc_plane_uniform.restype = C.c_uint32
         L.orc_seq_attempts.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -164,16 +167,23 @@ def observables(s, L):
 
 
 def cb_sweep(s, model, L, alg, beta, seed, stream=0, sweep0=0, nsweeps=1, J=1.0, D=0.0, h=0.0,
-             record=True):
-    """Checkerboard sweeps in place on ``s``; returns (obs[nsweeps,3] or None, attempts, accepts)."""
+             record=True, uniforms=0):
+    """Checkerboard sweeps in place on ``s``; returns (obs[nsweeps,3] or None, attempts, accepts).
+    ``uniforms``: 0 per-site Philox words, 1 bit-plane uniforms for the rank-form rules."""
     dim, Lv = _dims(L)
     obs = np.zeros((nsweeps, 3), np.int64) if record else None
     att, acc = C.c_uint64(0), C.c_uint64(0)
-    rc = lib().orc_cb_sweep(s, model, dim, Lv, alg, beta, J, D, h, seed, stream, sweep0, nsweeps,
-                            obs.ctypes.data if record else None, C.byref(att), C.byref(acc))
+    args = (s, model, dim, Lv, alg, beta, J, D, h, seed, stream, sweep0, nsweeps,
+            obs.ctypes.data if record else None, C.byref(att), C.byref(acc))
+    rc = lib().orc_cb_sweep_u(*args, int(uniforms)) if uniforms else lib().orc_cb_sweep(*args)
     if rc != OK:
         raise ValueError("oracle cb_sweep failed: %d" % rc)
     return obs, att.value, acc.value
+
+
+def plane_uniform(seed, stream, sweep, colour, e):
+    """The bit-plane uniform of colour-class site ``e`` (linear index >> 1)."""
+    return lib().orc_plane_uniform(seed, stream, sweep, colour, e)
 
 
 def seq_attempts(s, model, L, alg, beta, seed, stream=0, attempt0=0, nattempts=1, J=1.0, D=0.0, h=0.0):

@@ -17,7 +17,8 @@
 #include <time.h>
 
 /* Philox purposes (counter word 2, bits 24..31) */
-enum { P_ACCEPT = 0, P_PROPOSE = 1, P_LOW = 2, P_INIT = 3, P_EXCHANGE = 4, P_SEQ = 5, P_SEQ2 = 6 };
+enum { P_ACCEPT = 0, P_PROPOSE = 1, P_LOW = 2, P_INIT = 3, P_EXCHANGE = 4, P_SEQ = 5, P_SEQ2 = 6,
+       P_PLANES = 9, P_TAIL = 10 };
 
 /* ---------------------------------------------------------------------------
  * Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
@@ -57,6 +58,37 @@ uint32_t orc_site_word(uint64_t seed, uint32_t stream, uint64_t sweep, int colou
     uint32_t out[4];
     orc_philox4x32_10(ctr, key, out);
     return out[(site >> 1) & 3];
+}
+
+/* The Philox block of the checkerboard stream at counter word 0 = x. */
+static void orc_cb_block(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, int purpose, uint32_t x,
+                         uint32_t out[4]) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t ctr[4] = {x, (uint32_t)sweep,
+                       ((uint32_t)(sweep >> 32) & 0xFFFFu) | ((uint32_t)colour << 16) | ((uint32_t)purpose << 24),
+                       stream};
+    orc_philox4x32_10(ctr, key, out);
+}
+
+/* The bit-plane uniform (the library's MCX_UNIFORMS_PLANES form) of the site with index e
+ * among the sites of its colour (e = linear index >> 1; Lx a multiple of 128, so every
+ * 64 consecutive e share one row): bits 31..24 are bit e & 63 of planes 0..7, where
+ * plane 2j is words 0 | 1 << 32 and plane 2j+1 words 2 | 3 << 32 of the block at counter
+ * (e >> 6) * 16 + j, purpose P_PLANES; bits 23..0 are the low 24 bits of word e & 3 of
+ * the block at counter e >> 2, purpose P_TAIL.  Every bit is an independent Philox bit,
+ * so u is uniform on [0, 2^32) like the per-site word. */
+uint32_t orc_plane_uniform(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, uint64_t e) {
+    const int b = (int)(e & 63);
+    uint32_t u = 0, out[4];
+    for (int j = 0; j < 4; ++j) {
+        orc_cb_block(seed, stream, sweep, colour, P_PLANES, (uint32_t)((e >> 6) * 16 + (uint64_t)j), out);
+        const uint64_t p0 = (uint64_t)out[0] | ((uint64_t)out[1] << 32);
+        const uint64_t p1 = (uint64_t)out[2] | ((uint64_t)out[3] << 32);
+        u |= (uint32_t)((p0 >> b) & 1u) << (31 - 2 * j);
+        u |= (uint32_t)((p1 >> b) & 1u) << (30 - 2 * j);
+    }
+    orc_cb_block(seed, stream, sweep, colour, P_TAIL, (uint32_t)(e >> 2), out);
+    return u | (out[e & 3] & 0xFFFFFFu);
 }
 
 static double u53(uint32_t hi, uint32_t lo) {
@@ -298,10 +330,27 @@ void orc_init_random(int8_t* s, int model, int dim, const int32_t* L, uint64_t s
  *          SpinSystems/src/ising.jl:25-58, modify! :493-498.
  *   Blume-Capel: spin_flip! blume_capel.jl:52-85, modify! :250-256.
  * ------------------------------------------------------------------------- */
-int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
-                 double J, double D, double h, uint64_t seed, uint32_t stream,
-                 uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
-                 uint64_t* accepts) {
+/* Whether an Ising table has the rank form that the bit-plane uniforms apply to: always
+ * accepted with at most z/2 aligned neighbours, the same threshold for both spin states
+ * above, non-increasing in the aligned count (Metropolis without a field). */
+static int rank_form(const uint64_t* thr, int z) {
+    const uint64_t always = 1ull << 32;
+    for (int a = 0; a <= z; ++a) {
+        const uint64_t dn = thr[a], up = thr[a + z + 1];
+        if (a <= z / 2) {
+            if (dn != always || up != always) return 0;
+        } else {
+            if (dn != up || dn >= always) return 0;
+            if (a > z / 2 + 1 && dn > thr[a - 1]) return 0;
+        }
+    }
+    return 1;
+}
+
+static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                    double J, double D, double h, uint64_t seed, uint32_t stream,
+                    uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
+                    uint64_t* accepts, int uniforms) {
     geom_t g;
     if (geom_init(&g, dim, L)) return ORC_ERR_INVALID;
     int z = 2 * dim, nc = 2 * z + 1;
@@ -310,6 +359,8 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
     int rc = model == ORC_ISING ? orc_table_ising(dim, alg, beta, J, h, thr, xm)
                                 : orc_table_bc(dim, alg, beta, J, D, h, thr);
     if (rc) return rc;
+    if (uniforms && (model != ORC_ISING || L[0] % 128 != 0)) return ORC_ERR_INVALID;
+    const int planes = uniforms && alg != ORC_HEATBATH && rank_form(thr, z);
     int64_t P, M, Q;
     orc_observables(s, dim, L, &P, &M, &Q);
     uint64_t att = 0, acc = 0;
@@ -325,7 +376,9 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
                     int sigma = so * S;
                     int a = (sigma + z) / 2;
                     int idx = a + (z + 1) * (so > 0);
-                    uint32_t u = orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i);
+                    /* an always-accepted class flips whatever u is */
+                    uint32_t u = !planes ? orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i)
+                                 : thr[idx] >> 32 ? 0u : orc_plane_uniform(seed, stream, t, c, (uint64_t)i >> 1);
                     if ((uint64_t)(u ^ xm[idx]) < thr[idx]) {
                         s[i] = (int8_t)(-so);
                         P += -2 * sigma;
@@ -359,6 +412,23 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
     if (attempts) *attempts += att;
     if (accepts) *accepts += acc;
     return ORC_OK;
+}
+
+int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                 double J, double D, double h, uint64_t seed, uint32_t stream,
+                 uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
+                 uint64_t* accepts) {
+    return cb_sweep(s, model, dim, L, alg, beta, J, D, h, seed, stream, sweep0, nsweeps, obs, attempts, accepts, 0);
+}
+
+/* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes for
+ * the rank-form rules; bit planes need an Ising lattice with Lx a multiple of 128). */
+int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                   double J, double D, double h, uint64_t seed, uint32_t stream,
+                   uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
+                   uint64_t* accepts, int uniforms) {
+    return cb_sweep(s, model, dim, L, alg, beta, J, D, h, seed, stream, sweep0, nsweeps, obs, attempts, accepts,
+                    uniforms);
 }
 
 /* ---------------------------------------------------------------------------

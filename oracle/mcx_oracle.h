@@ -52,6 +52,14 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
                  uint64_t sweep0, int64_t nsweeps, int64_t* obs /* nsweeps*3 or NULL */,
                  uint64_t* attempts, uint64_t* accepts);
 
+/* orc_cb_sweep with the uniforms form (0 per-site words, 1 bit planes) */
+int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
+                   double J, double D, double h, uint64_t seed, uint32_t stream,
+                   uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
+                   uint64_t* accepts, int uniforms);
+/* the bit-plane uniform of colour-class site e (e = linear index >> 1) */
+uint32_t orc_plane_uniform(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, uint64_t e);
+
 int orc_seq_attempts(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                      double J, double D, double h, uint64_t seed, uint32_t stream,
                      uint64_t attempt0, int64_t nattempts, uint64_t* steps,

@@ -1,0 +1,98 @@
+"""The oracle's bit-plane uniforms (CPU): the definition against raw Philox blocks, the
+rules it applies to, and the same equilibrium as the per-site words."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+P_PLANES, P_TAIL = 9, 10
+
+
+def _block(seed, stream, sweep, colour, purpose, x):
+    w2 = ((sweep >> 32) & 0xFFFF) | (colour << 16) | (purpose << 24)
+    return [int(v) for v in O.philox([x & 0xFFFFFFFF, sweep & 0xFFFFFFFF, w2, stream],
+                                     [seed & 0xFFFFFFFF, seed >> 32])]
+
+
+def _plane_uniform(seed, stream, sweep, colour, e):
+    b, u = e & 63, 0
+    for j in range(4):
+        o = _block(seed, stream, sweep, colour, P_PLANES, (e >> 6) * 16 + j)
+        p0, p1 = o[0] | (o[1] << 32), o[2] | (o[3] << 32)
+        u |= ((p0 >> b) & 1) << (31 - 2 * j)
+        u |= ((p1 >> b) & 1) << (30 - 2 * j)
+    return u | (_block(seed, stream, sweep, colour, P_TAIL, e >> 2)[e & 3] & 0xFFFFFF)
+
+
+def test_plane_uniform_definition():
+    for seed, stream, sweep in ((7, 0, 0), (2 ** 40 + 3, 5, 2 ** 33 + 9), (123, 1, 77)):
+        for colour in (0, 1):
+            for e in (0, 1, 3, 4, 63, 64, 65, 127, 1000, 2 ** 20 + 17):
+                assert O.plane_uniform(seed, stream, sweep, colour, e) == _plane_uniform(seed, stream, sweep,
+                                                                                          colour, e)
+
+
+def test_plane_uniform_bits_are_balanced():
+    us = np.array([O.plane_uniform(11, 0, 3, 1, e) for e in range(1 << 14)], np.uint64)
+    for bit in (31, 28, 24, 23, 12, 0):  # plane bits and tail bits
+        frac = float(((us >> np.uint64(bit)) & np.uint64(1)).mean())
+        assert abs(frac - 0.5) < 4 * 0.5 / np.sqrt(us.size), (bit, frac)
+    # the top byte (the planes) is uniform over its 256 values
+    counts = np.bincount((us >> np.uint64(24)).astype(np.int64), minlength=256)
+    exp = us.size / 256
+    assert ((counts - exp) ** 2 / exp).sum() < 255 + 6 * np.sqrt(2 * 255)
+
+
+@pytest.mark.parametrize("alg,h", [(O.GLAUBER, 0.0), (O.HEATBATH, 0.0), (O.METROPOLIS, 0.2)])
+def test_planes_leave_other_rules_on_the_site_words(alg, h):
+    L = [128, 4]
+    a = O.init_random(O.ISING, L, 5)
+    b = a.copy()
+    oa = O.cb_sweep(a, O.ISING, L, alg, 0.44, 5, nsweeps=3, h=h)
+    ob = O.cb_sweep(b, O.ISING, L, alg, 0.44, 5, nsweeps=3, h=h, uniforms=1)
+    assert np.array_equal(a, b) and np.array_equal(oa[0], ob[0]) and oa[1:] == ob[1:]
+
+
+def test_planes_change_the_metropolis_chain():
+    L = [128, 8]
+    a = O.init_random(O.ISING, L, 5)
+    b = a.copy()
+    O.cb_sweep(a, O.ISING, L, O.METROPOLIS, 0.44, 5, nsweeps=2)
+    O.cb_sweep(b, O.ISING, L, O.METROPOLIS, 0.44, 5, nsweeps=2, uniforms=1)
+    assert not np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("model,L", [(O.ISING, [64, 64]), (O.ISING, [96, 8]), (O.BC, [128, 4])])
+def test_planes_need_an_ising_lattice_with_lx_multiple_of_128(model, L):
+    s = O.init_random(model, L, 1)
+    with pytest.raises(ValueError):
+        O.cb_sweep(s, model, L, O.METROPOLIS, 0.4, 1, nsweeps=1, D=0.5, uniforms=1)
+
+
+def _energy_series(uniforms, beta, L, nsweeps, burn, seed):
+    s = O.init_random(O.ISING, L, seed)
+    O.cb_sweep(s, O.ISING, L, O.METROPOLIS, beta, seed, nsweeps=burn, record=False, uniforms=uniforms)
+    obs, _, _ = O.cb_sweep(s, O.ISING, L, O.METROPOLIS, beta, seed, sweep0=burn, nsweeps=nsweeps,
+                           uniforms=uniforms)
+    return -obs[:, 0].astype(float) / s.size
+
+
+@pytest.mark.parametrize("beta", [0.3, 0.6])
+def test_planes_sample_the_same_equilibrium(beta):
+    """<E>/N of the two forms (128 x 128, 600 sweeps after 100) agree within 4 combined
+    sigma of 20-sweep bins; at beta = 0.6 both sit on Onsager's infinite-lattice energy
+    (finite-size corrections are exponentially small there)."""
+    L = [128, 128]
+    means, errs = [], []
+    for u in (0, 1):
+        e = _energy_series(u, beta, L, 600, 100, 21 + u)
+        bins = e.reshape(30, 20).mean(axis=1)
+        means.append(bins.mean())
+        errs.append(bins.std(ddof=1) / np.sqrt(bins.size))
+    assert abs(means[0] - means[1]) < 4 * np.hypot(*errs), (means, errs)
+    if beta == 0.6:
+        from scipy.special import ellipk
+        k = 2 * np.sinh(2 * beta) / np.cosh(2 * beta) ** 2
+        exact = -1 / np.tanh(2 * beta) * (1 + 2 / np.pi * (2 * np.tanh(2 * beta) ** 2 - 1) * ellipk(k * k))
+        for m, s in zip(means, errs):
+            assert abs(m - exact) < 4 * s + 1e-4, (m, exact, s)
