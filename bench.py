@@ -7,7 +7,12 @@ sweeps at beta=0.4407, energy and magnetisation recorded every sweep.  One step 
 one mcx_sweep call of --sweeps-per-step sweeps.  The lattice (16 MiB) fits in L2,
 so L2 is flushed (256 MiB write) between timed steps.  The int8 lattice runs each call
 on a transient 64-sites-per-word copy (packed at the start of the call, unpacked at its
-end, k_msc_metro half-sweeps; results bit-identical to the int8 kernels).
+end, k_msc_metro half-sweeps).  --uniforms (default planes) selects how the sweeps draw
+each site's 32-bit Metropolis uniform (mcx_lattice_set_uniforms): "planes" takes its top 8
+bits from bit planes shared by 64 sites and the low 24 only where they decide, "site" one
+Philox word per site (the stream of every other kernel); both forms are bit-exact against
+their oracle restatement and sample the same distribution, and the line reports the other
+form's rate beside the headline (site_uniforms / plane_uniforms).
 
   value      attempts/ns, CUDA events on the library's stream (torch's current stream is
              handed to the context); L2 is flushed before every timed step, so each step
@@ -36,10 +41,12 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
                     server (p50 / p99 latency, aggregate attempts/ns)
   flat_histogram    Blume-Capel L=1024 Multicanonical walkers, one per resident block, and a
                     fixed-budget Wang-Landau stage 1 (ln f = 1, flatness 0.8, one walker per SM)
-  msc64             the headline workload on the 64-spins-per-word layout
+  site_uniforms     the headline workload with the other uniforms form (per-site words when the
+                    headline draws bit planes), with its kernel's integer-pipe fractions
+  msc64             the headline workload on the 64-spins-per-word layout (the headline's uniforms)
   c2_matrix         the configured 2-D runs: Metropolis and Glauber at beta 0.30 / 0.4407 / 0.60
                     on int8 and MSC64, 10^4 sweeps each with the series, then U4 and binning errors
-  other_lattices    3-D Ising 256^3, Ising heat bath and Blume-Capel Metropolis / heat bath on
+  other_lattices    3-D Ising 256^3 (both uniforms forms), Ising heat bath and Blume-Capel Metropolis / heat bath on
                     4096^2, and the headline workload with packing off (the int8 words,
                     k_ising_strip, with its own roofline)
   general_graphs    4096^2 torus as IsingMatrix (Gaussian couplings) and as IsingGraph
@@ -75,6 +82,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mcx", "reference"], default="mcx")
     ap.add_argument("--sweeps-per-step", type=int, default=200)
+    ap.add_argument("--uniforms", choices=["planes", "site"], default="planes",
+                    help="how the headline sweeps draw their Metropolis uniforms (mcx_lattice_set_uniforms)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
@@ -106,16 +115,17 @@ def measured_peaks():
 # ncu replays with flushed caches, so this is a cold launch: both colour arrays read once)
 CB_TRAFFIC_PER_LAUNCH = 16810240
 
-# The same for one k_msc_metro<2> launch (the headline workload's kernel: int8 lattices run
-# multi-sweep calls on a transient 64-sites-per-word copy), profiles/msc_metro_L4096.md and
-# profiles/int_pipes_ising_strip_and_pt_persistent.md.
-MSC_TRAFFIC_PER_LAUNCH = 2126848
+# The same for one k_msc_metro<2,*> launch (the headline workload's kernel: int8 lattices run
+# multi-sweep calls on a transient 64-sites-per-word copy), per uniforms form,
+# profiles/msc_metro_L4096.md and profiles/int_pipes_ising_strip_and_pt_persistent.md.
+MSC_TRAFFIC_PER_LAUNCH = {"site": 2121472, "planes": 2112512}
 
-# Per-launch integer-pipe work of the two headline kernels from one ncu capture each
+# Per-launch integer-pipe work of the headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
-MSC_PIPES = {"warp_inst": 4982506, "alu_inst": 2372112, "fma_cycles": 6765216, "per": "launch"}
+MSC_PIPES = {"site": {"warp_inst": 4616780, "alu_inst": 2176942, "fma_cycles": 6611072, "per": "launch"},
+             "planes": {"warp_inst": 2555192, "alu_inst": 1280710, "fma_cycles": 2556880, "per": "launch"}}
 PT_PIPES = {"warp_inst": 64528754 / 3, "alu_inst": 32555444 / 3, "fma_cycles": 67545556 / 3, "per": "sweep"}
 
 
@@ -280,12 +290,14 @@ def bench_pt(torch, mcx, ctx, dev, flush, steps, warmup, sweeps_per_step=100, pl
     }
 
 
-def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
-    """The headline workload on the 64-spins-per-word layout (same Philox stream, results
-    bit-identical to int8): device-timed, L2 flushed between steps."""
+def bench_headline_form(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, layout, uniforms, nsm, sm_mhz):
+    """The headline workload on `layout` with `uniforms` (the int8 layout on its transient
+    packed copy, or the 64-spins-per-word layout itself): device-timed, L2 flushed between
+    steps, with the half-sweep kernel's integer-pipe fractions."""
     L = [L_SIDE, L_SIDE]
     N = L_SIDE * L_SIDE
-    lat = mcx.Ising(L, layout="msc64", ctx=ctx)
+    lat = mcx.Ising(L, layout=layout, ctx=ctx)
+    lat.set_uniforms(uniforms)
     mcx.init_(lat, "random", rng=mcx.Philox(SEED))
     alg = mcx.Metropolis(mcx.Philox(SEED), beta=BETA)
     lib = mcx._lib.load()
@@ -310,9 +322,11 @@ def bench_msc64(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step):
         torch.cuda.synchronize()
         tot += e0.elapsed_time(e1)
     lat.close()
-    return {"workload": "ising2d_L4096_metropolis_msc64", "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6),
-            "ms_per_step": tot / steps, "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2>",
-            "alg_bytes_per_launch": 1.5 * N / 8}
+    launch_s = tot * 1e-3 / (2 * sweeps_per_step * steps)
+    return {"workload": "ising2d_L4096_metropolis_%s_%s_uniforms" % (layout, uniforms),
+            "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6), "ms_per_step": tot / steps,
+            "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2,%s>" % ("true" if uniforms == "planes" else "false"),
+            "roofline": int_roof(MSC_PIPES[uniforms], launch_s, sm_mhz, nsm)}
 
 
 def bench_int8_words(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, nsm, sm_mhz):
@@ -391,11 +405,17 @@ def bench_c2_matrix(torch, mcx, ctx, sweeps=10000):
 
 
 def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_step=100):
-    """Other single-lattice sweeps through the same grid kernels (column-strip half-sweeps),
-    device-timed, L2 flushed between steps: 3-D Ising 256^3, Ising heat bath and Blume-Capel
-    (D = 1) Metropolis / heat bath on the 4096^2 lattice."""
+    """Other single-lattice sweeps, device-timed, L2 flushed between steps: 3-D Ising 256^3
+    (transient packed copy; per-site and bit-plane uniforms), Ising heat bath and Blume-Capel
+    (D = 1) Metropolis / heat bath on the 4096^2 lattice (column-strip half-sweeps)."""
     lib = mcx._lib.load()
+    def planes(lat):
+        lat.set_uniforms("planes")
+        return lat
+
     cases = [("ising3d_L256_metropolis", lambda: mcx.Ising([256, 256, 256], ctx=ctx), mcx.Metropolis, 0.2216),
+             ("ising3d_L256_metropolis_plane_uniforms", lambda: planes(mcx.Ising([256, 256, 256], ctx=ctx)),
+              mcx.Metropolis, 0.2216),
              ("ising2d_L4096_heatbath", lambda: mcx.Ising([L_SIDE, L_SIDE], ctx=ctx), mcx.HeatBath, BETA),
              ("bc2d_L4096_D1_metropolis", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.Metropolis,
               0.6),
@@ -799,6 +819,7 @@ def run_mcx(args):
     L = [L_SIDE, L_SIDE]
     N = L_SIDE * L_SIDE
     lat = mcx.Ising(L, ctx=ctx)
+    lat.set_uniforms(args.uniforms)
     mcx.init_(lat, "random", rng=mcx.Philox(SEED, rank))
     alg = mcx.Metropolis(mcx.Philox(SEED, rank), beta=BETA)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -875,7 +896,11 @@ def run_mcx(args):
     barrier()
 
     pt_res = srv_res = fh_res = msc_res = graph_res = small_res = med_res = rw_res = other_res = c2_res = None
+    other_form = None
+    nsm = ctx_sms(torch)
     if not args.no_extras:
+        other_form = bench_headline_form(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S, "int8",
+                                         "site" if args.uniforms == "planes" else "planes", nsm, 2070.0)
         small_res = bench_small(torch, mcx, ctx, rank == 0 and not args.no_cpu_baseline, min(args.cpu_seconds, 3.0))
         med_res = bench_medium(torch, mcx, ctx)
         rw_res = bench_reweight(torch, mcx, ctx)
@@ -883,7 +908,8 @@ def run_mcx(args):
         srv_res = bench_serve(mcx, ctx)
         fh_res = bench_flathist(torch, mcx, ctx, dev)
         fh_res["wang_landau_stage1"] = bench_wang_landau(torch, mcx, ctx, dev)
-        msc_res = bench_msc64(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S)
+        msc_res = bench_headline_form(torch, mcx, ctx, flush, max(3, args.steps // 2), 3, S, "msc64", args.uniforms,
+                                      nsm, 2070.0)
         other_res = bench_other_lattices(torch, mcx, ctx, flush)
         c2_res = bench_c2_matrix(torch, mcx, ctx)
         other_res["ising2d_L4096_metropolis_int8_words"] = bench_int8_words(
@@ -899,11 +925,14 @@ def run_mcx(args):
         cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
                          "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
-    tr = MSC_TRAFFIC_PER_LAUNCH
-    nsm = ctx_sms(torch)
+    tr = MSC_TRAFFIC_PER_LAUNCH[args.uniforms]
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
     if pt_res:
         pt_res["roofline"].update(int_roof(PT_PIPES, pt_res["persistent"]["ms_per_sweep"] * 1e-3, sm_mhz, nsm))
+    for r in (other_form, msc_res):  # the legs' fractions at the clock sampled in the timed region
+        if r:
+            r["roofline"] = int_roof(MSC_PIPES[r["workload"].split("_")[-2]], r["ms_per_step"] * 1e-3 / (2 * S),
+                                     sm_mhz, nsm)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -911,13 +940,18 @@ def run_mcx(args):
         "config": {"workload": "ising2d_L4096_metropolis_int8", "L": L_SIDE, "beta": BETA, "seed": SEED,
                    "layout": "int8 colour-split storage; each call sweeps a transient 64-sites-per-word copy "
                              "(packed at its start, unpacked at its end; mcx_lattice_set_packing)",
+                   "uniforms": args.uniforms + (" (top 8 bits of each site's 32-bit uniform from bit planes "
+                                                "shared by 64 sites, low 24 bits drawn where they decide; "
+                                                "mcx_lattice_set_uniforms)" if args.uniforms == "planes" else
+                                                " (one Philox word per site)"),
                    "sweeps_per_step": S, "record": "E,M every sweep",
                    "l2": "flushed between timed steps (256 MiB write)", "replicas_per_gpu": 1,
                    "parallelism": "replicas"},
         "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                          "kernel": "k_msc_metro<2>", "alg_bytes_per_launch": alg_bytes},
-                         **int_roof(MSC_PIPES, avg_launch_s, sm_mhz, nsm)),
+                          "kernel": "k_msc_metro<2,%s>" % ("true" if args.uniforms == "planes" else "false"),
+                          "alg_bytes_per_launch": alg_bytes},
+                         **int_roof(MSC_PIPES[args.uniforms], avg_launch_s, sm_mhz, nsm)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
         "gpu_launches": launches,
@@ -926,6 +960,7 @@ def run_mcx(args):
         "batched_pt": pt_res,
         "serving": srv_res,
         "flat_histogram": fh_res,
+        ("site_uniforms" if args.uniforms == "planes" else "plane_uniforms"): other_form,
         "msc64": msc_res,
         "other_lattices": other_res,
         "c2_matrix": c2_res,
