@@ -118,14 +118,14 @@ CB_TRAFFIC_PER_LAUNCH = 16810240
 # The same for one k_msc_metro<2,*> launch (the headline workload's kernel: int8 lattices run
 # multi-sweep calls on a transient 64-sites-per-word copy), per uniforms form,
 # profiles/msc_metro_L4096.md and profiles/int_pipes_ising_strip_and_pt_persistent.md.
-MSC_TRAFFIC_PER_LAUNCH = {"site": 2121472, "planes": 2112512}
+MSC_TRAFFIC_PER_LAUNCH = {"site": 2136576, "planes": 2118656}
 
 # Per-launch integer-pipe work of the headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
-MSC_PIPES = {"site": {"warp_inst": 4616780, "alu_inst": 2176942, "fma_cycles": 6611072, "per": "launch"},
-             "planes": {"warp_inst": 2555192, "alu_inst": 1280710, "fma_cycles": 2556880, "per": "launch"}}
+MSC_PIPES = {"site": {"warp_inst": 4710668, "alu_inst": 2143878, "fma_cycles": 6717168, "per": "launch"},
+             "planes": {"warp_inst": 2699982, "alu_inst": 1276356, "fma_cycles": 2403736, "per": "launch"}}
 PT_PIPES = {"warp_inst": 64528754 / 3, "alu_inst": 32555444 / 3, "fma_cycles": 67545556 / 3, "per": "sweep"}
 
 
