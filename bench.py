@@ -45,7 +45,8 @@ Further lines in the same JSON object (skipped with --no-extras), each timed on 
                     headline draws bit planes), with its kernel's integer-pipe fractions
   msc64             the headline workload on the 64-spins-per-word layout (the headline's uniforms)
   c2_matrix         the configured 2-D runs: Metropolis and Glauber at beta 0.30 / 0.4407 / 0.60
-                    on int8 and MSC64, 10^4 sweeps each with the series, then U4 and binning errors
+                    on int8 and MSC64, 10^4 sweeps each with the series, then U4 and binning errors,
+                    with per-site and with bit-plane uniforms
   other_lattices    3-D Ising 256^3 (both uniforms forms), Ising heat bath and Blume-Capel Metropolis / heat bath on
                     4096^2, and the headline workload with packing off (the int8 words,
                     k_ising_strip, with its own roofline)
@@ -372,35 +373,37 @@ def bench_c2_matrix(torch, mcx, ctx, sweeps=10000):
     and 0.60, on the int8 and the MSC64 layout, seed 7, `sweeps` sweeps in one call with
     (pair, spin) recorded every sweep (CUDA events around the call, series copied back
     inside), then the Binder cumulant U4 (jackknife) and the binning error of the energy per
-    site from the series, after the first tenth as thermalisation."""
+    site from the series, after the first tenth as thermalisation.  Every run with per-site
+    uniforms, and again with bit-plane uniforms (keys ending in _planes)."""
     import numpy as np
     from mcx import analysis as A
     N = L_SIDE * L_SIDE
     out = {}
     for alg_name, kind in (("metropolis", mcx.Metropolis), ("glauber", mcx.Glauber)):
-        for beta in (0.30, 0.4407, 0.60):
-            for layout in ("int8", "msc64"):
-                lat = mcx.Ising([L_SIDE, L_SIDE], layout=layout, ctx=ctx)
-                mcx.init_(lat, "random", rng=mcx.Philox(SEED))
-                alg = kind(mcx.Philox(SEED), beta=beta)
-                torch.cuda.synchronize()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record()
-                obs = mcx.sweep_(lat, alg, sweeps, record=True)
-                e1.record()
-                torch.cuda.synchronize()
-                ms = e0.elapsed_time(e1)
-                lat.close()
-                th = sweeps // 10
-                e = -np.asarray(obs[th:, 0], np.float64) / N  # J = 1, h = 0: E = -(pair sum)
-                m = np.asarray(obs[th:, 1], np.float64) / N
-                u4, u4_err = A.binder_cumulant(m)
-                out["%s_beta%.4g_%s" % (alg_name, beta, layout)] = {
-                    "attempts_per_ns": N * sweeps / (ms * 1e6), "ms": ms,
-                    "e_per_site": float(e.mean()), "e_err_binning": A.binning_error(e),
-                    "abs_m": float(np.abs(m).mean()), "u4": u4, "u4_err": u4_err,
-                    "acceptance": alg.accepted / float(N * sweeps) if alg_name == "metropolis" else None}
+        for beta, layout, uniforms in [(b, l, u) for u in ("site", "planes") for b in (0.30, 0.4407, 0.60)
+                                       for l in ("int8", "msc64")]:
+            lat = mcx.Ising([L_SIDE, L_SIDE], layout=layout, ctx=ctx)
+            lat.set_uniforms(uniforms)
+            mcx.init_(lat, "random", rng=mcx.Philox(SEED))
+            alg = kind(mcx.Philox(SEED), beta=beta)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            obs = mcx.sweep_(lat, alg, sweeps, record=True)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            lat.close()
+            th = sweeps // 10
+            e = -np.asarray(obs[th:, 0], np.float64) / N  # J = 1, h = 0: E = -(pair sum)
+            m = np.asarray(obs[th:, 1], np.float64) / N
+            u4, u4_err = A.binder_cumulant(m)
+            out["%s_beta%.4g_%s%s" % (alg_name, beta, layout, "_planes" if uniforms == "planes" else "")] = {
+                "attempts_per_ns": N * sweeps / (ms * 1e6), "ms": ms,
+                "e_per_site": float(e.mean()), "e_err_binning": A.binning_error(e),
+                "abs_m": float(np.abs(m).mean()), "u4": u4, "u4_err": u4_err,
+                "acceptance": alg.accepted / float(N * sweeps) if alg_name == "metropolis" else None}
     return {"workload": "ising2d_L4096_seed7_%d_sweeps_record" % sweeps, "runs": out}
 
 

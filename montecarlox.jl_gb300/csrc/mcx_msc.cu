@@ -19,7 +19,7 @@ struct MscArgs {
     int nw;  // words per row
     int W, Ly, Lz, rows, colour;
     int nw_shift, ly_shift;  // log2 of nw / Ly when they are powers of two, else -1
-    uint32_t pmask[8][3];    // bit-plane uniforms: all ones where bit 31-p of class k's threshold is set
+    uint32_t pmask[8][7];    // bit-plane uniforms: all ones where bit 31-p of class k's threshold is set
     uint32_t k0, k1, stream;
     unsigned long long sweep;
     unsigned long long* dst[2];
@@ -96,13 +96,19 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
 // bit, most significant first, for all 64 sites at once; a site is decided at the first
 // plane where its bit and its threshold's differ, and only the sites tied after 8 planes
 // (probability 2^-8 each) draw the low 24 bits from a per-site block.
-template <int DIM, bool PL>
+//
+// ALL = true (bit planes only): the class form, a threshold below 2^32 for every aligned
+// count, the same for both spin states (Glauber without a field); K = Z + 1 classes, none
+// always accepted.
+template <int DIM, bool PL, bool ALL>
 __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
+    static_assert(PL || !ALL, "the class form is swept with bit-plane uniforms only");
     constexpr int Z = 2 * DIM;
-    constexpr int K = Z / 2;
+    constexpr int K = ALL ? Z + 1 : Z / 2;
+    constexpr int A0 = ALL ? 0 : Z / 2 + 1;  // aligned count of class 0
     uint32_t tk[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) tk[k] = (uint32_t)a.thr[Z / 2 + 1 + k];  // < 2^32 for these classes
+    for (int k = 0; k < K; ++k) tk[k] = (uint32_t)a.thr[A0 + k];  // < 2^32 for these classes
     pdl_trigger();
     const int nwords = a.nw * a.rows;  // < 2^28 words (N <= 2^34 sites)
     const PhiloxPre pre = philox_pre((uint32_t)a.sweep, ctr_word2(a.sweep, a.colour, PL ? P_PLANES : P_ACCEPT), a.k0);
@@ -201,18 +207,22 @@ __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
         for (int d = 0; d < Z; ++d) al[d] = ~(al[d] ^ own);
         unsigned long long c0, c1, c2;
         count_bits<Z>(al, c0, c1, c2);
-        // class masks of Z/2 + k aligned neighbours, k = 1..K (the rest always flips)
+        // class masks of A0 + k aligned neighbours (in the rank form the rest always flips)
         unsigned long long m[K];
-        if constexpr (DIM == 2) {
+        unsigned long long flip = 0;
+        if constexpr (ALL) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) m[k] = (k & 1 ? c0 : ~c0) & (k & 2 ? c1 : ~c1) & (k & 4 ? c2 : ~c2);
+        } else if constexpr (DIM == 2) {
             m[0] = c0 & c1;  // 3 = 011
             m[1] = c2;       // 4 = 100
+            flip = ~(m[0] | m[1]);
         } else {
             m[0] = c2 & ~c1 & ~c0;  // 4 = 100
             m[1] = c2 & c0;         // 5 = 101
             m[2] = c2 & c1;         // 6 = 110
+            flip = ~c2;
         }
-        unsigned long long flip = ~c2;
-        if constexpr (DIM == 2) flip = ~(m[0] | m[1]);
 #pragma unroll
         for (int k = 0; k < K; ++k) flip |= m[k] & lt[k];
         if constexpr (PL) {
@@ -281,6 +291,20 @@ static bool msc_rank_form(const Table& t, int Z) {
 // Whether `alg` with table `t` is swept on the packed words (k_msc_metro's rank form).
 bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
     return lat->model == MCX_ISING && alg != MCX_HEATBATH && msc_rank_form(t, 2 * lat->dim);
+}
+
+// The class form: one threshold below 2^32 per aligned count, equal for both spin states.
+static bool msc_class_form(const Table& t, int Z) {
+    for (int al = 0; al <= Z; ++al)
+        if (t.thr[al] != t.thr[al + Z + 1] || t.thr[al] >= (1ull << 32)) return false;
+    return true;
+}
+
+// Whether a call of `alg` on `lat` draws bit-plane uniforms (and so runs on the packed words):
+// the lattice asks for them and the rule has the rank or the class form.
+bool msc_planes_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
+    return lat->uniforms == MCX_UNIFORMS_PLANES && lat->model == MCX_ISING && alg != MCX_HEATBATH &&
+           (msc_rank_form(t, 2 * lat->dim) || msc_class_form(t, 2 * lat->dim));
 }
 
 // Whether a multi-sweep call on an int8 Ising lattice may run on a transient MSC64 copy
@@ -370,12 +394,15 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_
     a.nw_shift = log2_or(a.nw);
     a.ly_shift = log2_or(a.Ly);
     const int Z = 2 * lat->dim;
-    for (int p = 0; p < 8; ++p)
-        for (int k = 0; k < 3; ++k)
-            a.pmask[p][k] = k < Z / 2 && ((t.thr[Z / 2 + 1 + k] >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
     const bool pl = lat->uniforms == MCX_UNIFORMS_PLANES;
-    void (*fn)(const MscArgs) = lat->dim == 2 ? (pl ? k_msc_metro<2, true> : k_msc_metro<2, false>)
-                                              : (pl ? k_msc_metro<3, true> : k_msc_metro<3, false>);
+    const bool all = !msc_rank_form(t, Z);  // then the caller checked the class form (bit planes)
+    const int K = all ? Z + 1 : Z / 2, A0 = all ? 0 : Z / 2 + 1;
+    for (int p = 0; p < 8; ++p)
+        for (int k = 0; k < 7; ++k)
+            a.pmask[p][k] = k < K && ((t.thr[A0 + k] >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
+    void (*fn)(const MscArgs) =
+        lat->dim == 2 ? (all ? k_msc_metro<2, true, true> : pl ? k_msc_metro<2, true, false> : k_msc_metro<2, false, false>)
+                      : (all ? k_msc_metro<3, true, true> : pl ? k_msc_metro<3, true, false> : k_msc_metro<3, false, false>);
     const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 288, 0);  // one wave
     // every launch after the first depends programmatically on the one before (the
     // kernels read the lattice after pdl_wait)

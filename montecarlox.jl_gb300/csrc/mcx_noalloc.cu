@@ -99,7 +99,7 @@ extern "C" MCX_API mcx_status mcx_sweep_noalloc(mcx_lattice* lat, mcx_algorithm 
     unsigned long long* counter = scratch + (size_t)kNoallocMaxSweeps * 3;
     Table t;
     MCX_CHECK(build_table(lat, alg, beta, &t));
-    if (lat->uniforms == MCX_UNIFORMS_PLANES && msc_rank_ok(lat, alg, t))
+    if (msc_planes_ok(lat, alg, t))
         return fail(MCX_ERR_INVALID_ARG, "mcx_sweep_noalloc draws per-site words: bit-plane uniforms need mcx_sweep");
     // the partial sums of this call's sweeps and the counter start at zero
     MCX_CUDA(cudaMemsetAsync(scratch, 0, (size_t)nsweeps * 3 * sizeof(unsigned long long), ctx->stream));

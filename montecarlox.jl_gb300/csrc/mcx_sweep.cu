@@ -724,11 +724,11 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // than a per-site table lookup on the words
     // A rank-form call with bit-plane uniforms always runs on the words: an int8 lattice's
     // on its transient copy, whatever the call's length (the int8 kernels draw per-site words).
-    const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && msc_rank_ok(lat, alg, t);
+    const bool pl_rule = msc_planes_ok(lat, alg, t);
+    const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && (pl_rule || msc_rank_ok(lat, alg, t));
     const bool via_int8 = lat->layout == MCX_LAYOUT_MSC64 && !msc_words;
     const bool int8 = lat->layout == MCX_LAYOUT_INT8 || via_int8;
-    const bool planes = lat->layout == MCX_LAYOUT_INT8 && lat->uniforms == MCX_UNIFORMS_PLANES && nsweeps > 0 &&
-                        msc_rank_ok(lat, alg, t);
+    const bool planes = lat->layout == MCX_LAYOUT_INT8 && pl_rule && nsweeps > 0;
     if (planes) MCX_CHECK(msc_planes_copy(lat));
     if (via_int8) MCX_CHECK(msc_unpack(lat));
     MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
@@ -966,7 +966,7 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
         return mcx_sweep(lats[0], alg, betas[0], &rngs[0], nsweeps, obs_series ? obs_series[0] : nullptr, counters);
     bool planes = false;  // bit-plane uniforms run on the words, one mcx_sweep per lattice
     for (int i = 0; i < n; ++i)
-        planes = planes || (lats[i]->uniforms == MCX_UNIFORMS_PLANES && msc_rank_ok(lats[i], alg, tabs[i]));
+        planes = planes || msc_planes_ok(lats[i], alg, tabs[i]);
     if (planes) {
         for (int i = 0; i < n; ++i)
             MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,

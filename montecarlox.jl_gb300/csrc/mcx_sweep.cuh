@@ -63,6 +63,8 @@ constexpr long long kClusterLattice = 524288;
 int small_width(int64_t W, long long sites);
 // whether `alg` with table `t` has the rank form swept on 64-sites-per-word words (mcx_msc.cu)
 bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t);
+// whether a call draws bit-plane uniforms (the lattice asks for them, rank or class form; mcx_msc.cu)
+bool msc_planes_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t);
 // the cluster form; *done = false when it does not apply or no cluster fits the device
 mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps,
                          bool* done);

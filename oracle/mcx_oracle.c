@@ -347,6 +347,14 @@ static int rank_form(const uint64_t* thr, int z) {
     return 1;
 }
 
+/* Whether an Ising table has the class form: one threshold below 2^32 per aligned count,
+ * the same for both spin states, no xor mask (Glauber without a field). */
+static int class_form(const uint64_t* thr, const uint32_t* xm, int z) {
+    for (int a = 0; a <= z; ++a)
+        if (thr[a] != thr[a + z + 1] || thr[a] >= (1ull << 32) || xm[a] || xm[a + z + 1]) return 0;
+    return 1;
+}
+
 static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                     double J, double D, double h, uint64_t seed, uint32_t stream,
                     uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
@@ -360,7 +368,7 @@ static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, do
                                 : orc_table_bc(dim, alg, beta, J, D, h, thr);
     if (rc) return rc;
     if (uniforms && (model != ORC_ISING || L[0] % 128 != 0)) return ORC_ERR_INVALID;
-    const int planes = uniforms && alg != ORC_HEATBATH && rank_form(thr, z);
+    const int planes = uniforms && alg != ORC_HEATBATH && (rank_form(thr, z) || class_form(thr, xm, z));
     int64_t P, M, Q;
     orc_observables(s, dim, L, &P, &M, &Q);
     uint64_t att = 0, acc = 0;
@@ -422,7 +430,8 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
 }
 
 /* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes for
- * the rank-form rules; bit planes need an Ising lattice with Lx a multiple of 128). */
+ * the rules of the rank or the class form; bit planes need an Ising lattice with Lx a
+ * multiple of 128). */
 int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                    double J, double D, double h, uint64_t seed, uint32_t stream,
                    uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,

@@ -47,6 +47,23 @@ def test_planes_parity(gpu, L, beta, layout):
     sys_.close()
 
 
+GLAUBER_CASES = [([128, 128], 0.4407), ([256, 64], 0.3), ([1024, 96], 0.6), ([128, 64], 0.0),
+                 ([128, 16, 8], 0.2216), ([256, 12, 10], 3.0)]
+
+
+@pytest.mark.parametrize("layout", ["int8", "msc64"])
+@pytest.mark.parametrize("L,beta", GLAUBER_CASES)
+def test_planes_glauber_parity(gpu, L, beta, layout):
+    """Glauber without a field (the class form: a threshold for every aligned count) with
+    bit-plane uniforms on the packed words, against the oracle; beta 0 (every threshold 2^31)
+    and beta 3 (thresholds near 0 and near 2^32)."""
+    sys_, a, obs, s, oobs, att, acc = _pair(gpu, L, beta, seed=9, stream=2, layout=layout, alg="glauber")
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert a.accepted == acc and a.steps == att
+    sys_.close()
+
+
 def test_planes_l4096_bit_exact(gpu):
     """2-D L=4096, seed 7, Metropolis at beta 0.4407: two sweeps of the plane form against
     the oracle, both layouts."""
@@ -63,9 +80,19 @@ def test_planes_l4096_bit_exact(gpu):
         assert a.accepted == acc
         assert np.array_equal(sys_.spins, s)
         sys_.close()
+    # Glauber at the configured beta 0.30, int8 storage
+    s = O.init_random(O.ISING, L, 7)
+    oobs, _, acc = O.cb_sweep(s, O.ISING, L, O.GLAUBER, 0.3, 7, nsweeps=2, uniforms=1)
+    sys_ = gpu.Ising(L)
+    sys_.set_uniforms("planes")
+    gpu.init_(sys_, "random", rng=gpu.Philox(7))
+    a = gpu.Glauber(gpu.Philox(7), beta=0.3)
+    obs = gpu.sweep_(sys_, a, 2, record=True)
+    assert np.array_equal(obs, oobs) and a.accepted == acc and np.array_equal(sys_.spins, s)
+    sys_.close()
 
 
-@pytest.mark.parametrize("alg,h", [("glauber", 0.0), ("heatbath", 0.0), ("metropolis", 0.3)])
+@pytest.mark.parametrize("alg,h", [("glauber", 0.2), ("heatbath", 0.0), ("metropolis", 0.3)])
 def test_other_rules_keep_the_site_words(gpu, alg, h):
     """Rules without the rank form draw per-site words on a plane lattice too."""
     sys_, a, obs, s, oobs, att, acc = _pair(gpu, [256, 64], 0.44, alg=alg, h=h, nsweeps=3)
