@@ -210,9 +210,10 @@ def test_planes_refused_by_noalloc(gpu):
     s.close()
 
 
-def test_planes_kaufman_l128(gpu):
-    """16 independent 128^2 chains with plane uniforms (Metropolis, beta 0.4407, 10^3
-    thermalisation + 5000 recorded sweeps): the mean energy per site within 3 standard
+@pytest.mark.parametrize("alg", ["metropolis", "glauber"])
+def test_planes_kaufman_l128(gpu, alg):
+    """16 independent 128^2 chains with plane uniforms (Metropolis or Glauber, beta 0.4407,
+    10^3 thermalisation + 5000 recorded sweeps): the mean energy per site within 3 standard
     errors of the chain means of Kaufman's exact finite-torus value."""
     from mcx.analysis import kaufman_ising2d
     L, beta, nch = 128, 0.4407, 16
@@ -221,7 +222,7 @@ def test_planes_kaufman_l128(gpu):
         c = gpu.Ising([L, L])
         c.set_uniforms("planes")
         gpu.init_(c, "random", rng=gpu.Philox(42, i))
-        a = gpu.Metropolis(gpu.Philox(42, i), beta=beta)
+        a = (gpu.Metropolis if alg == "metropolis" else gpu.Glauber)(gpu.Philox(42, i), beta=beta)
         gpu.sweep_(c, a, 1000)
         obs = gpu.sweep_(c, a, 5000, record=True)
         means.append((-obs[:, 0] / (L * L)).mean())
