@@ -71,9 +71,8 @@ typedef enum mcx_layout { MCX_LAYOUT_INT8 = 0, MCX_LAYOUT_MSC64 = 1 } mcx_layout
  *         bit b of a plane for site b of the 64), compared with the thresholds bit by bit
  *         for 64 sites at once; the low 24 bits come from a per-site block (like SITE,
  *         another counter purpose) and are drawn only for the sites whose top 8 bits equal
- *         their threshold's.  Applies to Ising Metropolis and Glauber without a field
- *         (the rules whose threshold depends on the aligned-neighbour count alone, swept on
- *         64-sites-per-word words); every other rule draws the SITE form. */
+ *         their threshold's.  Applies to every Ising rule (Metropolis, Glauber, heat
+ *         bath, with or without a field; all swept on 64-sites-per-word words). */
 typedef enum mcx_uniforms { MCX_UNIFORMS_SITE = 0, MCX_UNIFORMS_PLANES = 1 } mcx_uniforms;
 
 /* Flat-histogram mode: Multicanonical (src/algorithms/multicanonical.jl) or
@@ -180,7 +179,7 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
 MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow);
 /* Selects the uniforms of later sweeps (mcx_uniforms; default SITE).  PLANES needs an
  * Ising lattice with Lx a multiple of 128 (MCX_ERR_INVALID_ARG otherwise); on the int8
- * layout its Metropolis and Glauber calls run on the transient 64-sites-per-word copy whatever their
+ * layout its calls run on the transient 64-sites-per-word copy whatever their
  * length, so mcx_sweep returns MCX_ERR_INVALID_ARG with packing off and MCX_ERR_BUDGET /
  * MCX_ERR_OOM when the N/8-byte copy does not fit.  mcx_sweep_noalloc (int8 kernels
  * only) refuses such calls; mcx_sweep_batch runs them one mcx_sweep per lattice.  The two

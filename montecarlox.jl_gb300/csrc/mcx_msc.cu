@@ -20,6 +20,10 @@ struct MscArgs {
     int W, Ly, Lz, rows, colour;
     int nw_shift, ly_shift;  // log2 of nw / Ly when they are powers of two, else -1
     uint32_t pmask[8][7];    // bit-plane uniforms: all ones where bit 31-p of class k's threshold is set
+    // the general form: per class c = aligned count + (Z+1) * (spin up), all ones where bit
+    // 31-p of its threshold is set / where it always flips; the low 24 bits of its threshold
+    uint32_t gmask[8][14], galways[14], gt24[14];
+    int hb;  // heat bath: up spins compare the complement of u
     uint32_t k0, k1, stream;
     unsigned long long sweep;
     unsigned long long* dst[2];
@@ -97,14 +101,18 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
 // plane where its bit and its threshold's differ, and only the sites tied after 8 planes
 // (probability 2^-8 each) draw the low 24 bits from a per-site block.
 //
-// ALL = true (bit planes only): the class form, a threshold below 2^32 for every aligned
-// count, the same for both spin states (Glauber without a field); K = Z + 1 classes, none
-// always accepted.
-template <int DIM, bool PL, bool ALL>
+// FORM 1 (bit planes only): the class form, a threshold below 2^32 for every aligned count,
+// the same for both spin states (Glauber without a field); K = Z + 1 classes, none always
+// accepted.  FORM 2 (bit planes only): any Ising rule (heat bath, a field): a site flips iff
+// (u ^ x) < t_c for its class c = (aligned count, spin), x all ones for up spins under heat
+// bath; the word keeps its eight planes from before the wait, and each plane's per-site
+// threshold bit is selected from the class leaves by the bit-sliced count and the spin.
+template <int DIM, bool PL, int FORM>
 __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
-    static_assert(PL || !ALL, "the class form is swept with bit-plane uniforms only");
+    static_assert(PL || FORM == 0, "the class and general forms are swept with bit-plane uniforms only");
+    constexpr bool ALL = FORM == 1, GEN = FORM == 2;
     constexpr int Z = 2 * DIM;
-    constexpr int K = ALL ? Z + 1 : Z / 2;
+    constexpr int K = GEN ? 1 : ALL ? Z + 1 : Z / 2;
     constexpr int A0 = ALL ? 0 : Z / 2 + 1;  // aligned count of class 0
     uint32_t tk[K];
 #pragma unroll
@@ -130,11 +138,19 @@ __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
     // the class masks are known, ran slower: 2015 against 2040 attempts/ns in 2-D, 1642
     // against 1778 in 3-D.)
     unsigned long long lt[K], eq[K];
+    unsigned long long R[GEN ? 8 : 1];  // the general form: planes 0..7 of the word
     int ix_up = 0, ix_dn = 0, ix_side = 0, ix_zp = 0, ix_zm = 0;
     bool shift_left = false;
     auto draw = [&](int g) {
         const uint32_t cbase = 16u * (uint32_t)g;
-        if constexpr (PL) {
+        if constexpr (GEN) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint4 rnd = philox10_pre(cbase + j, a.stream, pre, a.k0, a.k1);
+                R[2 * j] = ((unsigned long long)rnd.y << 32) | rnd.x;
+                R[2 * j + 1] = ((unsigned long long)rnd.w << 32) | rnd.z;
+            }
+        } else if constexpr (PL) {
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 lt[k] = 0;
@@ -210,7 +226,40 @@ __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
         // class masks of A0 + k aligned neighbours (in the rank form the rest always flips)
         unsigned long long m[K];
         unsigned long long flip = 0;
-        if constexpr (ALL) {
+        if constexpr (GEN) {
+            // per-site value of a class leaf set: select on the count bits, then on the spin
+            auto bc = [](uint32_t x) { return ((unsigned long long)x << 32) | x; };
+            auto sel = [](unsigned long long s, unsigned long long x, unsigned long long y) { return (s & x) | (~s & y); };
+            auto leaf = [&](const uint32_t* l) {
+                auto cnt = [&](const uint32_t* q) {
+                    const unsigned long long lo = sel(c1, sel(c0, bc(q[3]), bc(q[2])), sel(c0, bc(q[1]), bc(q[0])));
+                    if constexpr (DIM == 2) return sel(c2, bc(q[4]), lo);
+                    const unsigned long long hi = sel(c1, bc(q[6]), sel(c0, bc(q[5]), bc(q[4])));
+                    return sel(c2, hi, lo);
+                };
+                return sel(own, cnt(l + Z + 1), cnt(l));
+            };
+            const unsigned long long X = a.hb ? own : 0ull;  // heat bath: up spins compare ~u
+            const unsigned long long always = leaf(a.galways);
+            unsigned long long less = 0, tied = ~always;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const unsigned long long T = leaf(a.gmask[q]), Re = R[q] ^ X;
+                less |= tied & T & ~Re;
+                tied &= ~(T ^ Re);
+            }
+            flip = always | less;
+            while (tied) {  // top 8 bits equal to the class threshold's: compare the low 24
+                const int b = __ffsll((long long)tied) - 1;
+                tied &= tied - 1;
+                const uint4 rr = philox10_pre(16u * (uint32_t)g + (uint32_t)(b >> 2), a.stream, pre_tail, a.k0, a.k1);
+                const int up = (int)((own >> b) & 1ull);
+                const int cls = (int)((c0 >> b) & 1ull) + 2 * (int)((c1 >> b) & 1ull) + 4 * (int)((c2 >> b) & 1ull) +
+                                (Z + 1) * up;
+                const uint32_t lo = (pick4(rr, b & 3) & 0xFFFFFFu) ^ ((a.hb && up) ? 0xFFFFFFu : 0u);
+                if (lo < a.gt24[cls]) flip |= 1ull << b;
+            }
+        } else if constexpr (ALL) {
 #pragma unroll
             for (int k = 0; k < K; ++k) m[k] = (k & 1 ? c0 : ~c0) & (k & 2 ? c1 : ~c1) & (k & 4 ? c2 : ~c2);
         } else if constexpr (DIM == 2) {
@@ -223,9 +272,11 @@ __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
             m[2] = c2 & c1;         // 6 = 110
             flip = ~c2;
         }
+        if constexpr (!GEN) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) flip |= m[k] & lt[k];
-        if constexpr (PL) {
+            for (int k = 0; k < K; ++k) flip |= m[k] & lt[k];
+        }
+        if constexpr (PL && !GEN) {
             unsigned long long tied = 0;  // top 8 bits equal to the class threshold's
 #pragma unroll
             for (int k = 0; k < K; ++k) tied |= m[k] & eq[k];
@@ -301,10 +352,9 @@ static bool msc_class_form(const Table& t, int Z) {
 }
 
 // Whether a call of `alg` on `lat` draws bit-plane uniforms (and so runs on the packed words):
-// the lattice asks for them and the rule has the rank or the class form.
-bool msc_planes_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
-    return lat->uniforms == MCX_UNIFORMS_PLANES && lat->model == MCX_ISING && alg != MCX_HEATBATH &&
-           (msc_rank_form(t, 2 * lat->dim) || msc_class_form(t, 2 * lat->dim));
+// every Ising rule does once the lattice asks for them (rank, class or general form).
+bool msc_planes_ok(const mcx_lattice* lat, mcx_algorithm, const Table&) {
+    return lat->uniforms == MCX_UNIFORMS_PLANES && lat->model == MCX_ISING;
 }
 
 // Whether a multi-sweep call on an int8 Ising lattice may run on a transient MSC64 copy
@@ -377,7 +427,7 @@ mcx_status msc_unpack(mcx_lattice* lat) {
 }
 
 // `nsweeps` sweeps of the packed words with k_msc_metro (the caller checked msc_rank_ok).
-mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_rng* rng, int64_t nsweeps) {
+mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng, int64_t nsweeps) {
     mcx_ctx* ctx = lat->ctx;
     MscArgs a;
     a.nw = (int)(lat->W / 64);
@@ -395,14 +445,23 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm, const Table& t, const mcx_
     a.ly_shift = log2_or(a.Ly);
     const int Z = 2 * lat->dim;
     const bool pl = lat->uniforms == MCX_UNIFORMS_PLANES;
-    const bool all = !msc_rank_form(t, Z);  // then the caller checked the class form (bit planes)
-    const int K = all ? Z + 1 : Z / 2, A0 = all ? 0 : Z / 2 + 1;
+    // rank form (any uniforms), else with bit planes the class or the general form
+    const int form = msc_rank_form(t, Z) ? 0 : msc_class_form(t, Z) ? 1 : 2;
+    const int K = form == 1 ? Z + 1 : Z / 2, A0 = form == 1 ? 0 : Z / 2 + 1;
     for (int p = 0; p < 8; ++p)
         for (int k = 0; k < 7; ++k)
-            a.pmask[p][k] = k < K && ((t.thr[A0 + k] >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
-    void (*fn)(const MscArgs) =
-        lat->dim == 2 ? (all ? k_msc_metro<2, true, true> : pl ? k_msc_metro<2, true, false> : k_msc_metro<2, false, false>)
-                      : (all ? k_msc_metro<3, true, true> : pl ? k_msc_metro<3, true, false> : k_msc_metro<3, false, false>);
+            a.pmask[p][k] = form < 2 && k < K && ((t.thr[A0 + k] >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
+    for (int c = 0; c < 14; ++c) {
+        const unsigned long long v = c < 2 * (Z + 1) ? t.thr[c] : 0;
+        for (int p = 0; p < 8; ++p) a.gmask[p][c] = v < (1ull << 32) && ((v >> (31 - p)) & 1ull) ? 0xFFFFFFFFu : 0u;
+        a.galways[c] = v >= (1ull << 32) ? 0xFFFFFFFFu : 0u;
+        a.gt24[c] = (uint32_t)(v & 0xFFFFFFu);
+    }
+    a.hb = alg == MCX_HEATBATH;
+    using Fn = void (*)(const MscArgs);
+    const Fn fns[2][4] = {{k_msc_metro<2, false, 0>, k_msc_metro<2, true, 0>, k_msc_metro<2, true, 1>, k_msc_metro<2, true, 2>},
+                          {k_msc_metro<3, false, 0>, k_msc_metro<3, true, 0>, k_msc_metro<3, true, 1>, k_msc_metro<3, true, 2>}};
+    const Fn fn = fns[lat->dim == 3][pl ? 1 + form : 0];
     const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 288, 0);  // one wave
     // every launch after the first depends programmatically on the one before (the
     // kernels read the lattice after pdl_wait)

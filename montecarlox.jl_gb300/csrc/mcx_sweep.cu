@@ -724,7 +724,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // than a per-site table lookup on the words
     // A rank-form call with bit-plane uniforms always runs on the words: an int8 lattice's
     // on its transient copy, whatever the call's length (the int8 kernels draw per-site words).
-    const bool pl_rule = msc_planes_ok(lat, alg, t);
+    const bool pl_rule = msc_planes_ok(lat, alg, t);  // every Ising rule under bit-plane uniforms
     const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && (pl_rule || msc_rank_ok(lat, alg, t));
     const bool via_int8 = lat->layout == MCX_LAYOUT_MSC64 && !msc_words;
     const bool int8 = lat->layout == MCX_LAYOUT_INT8 || via_int8;

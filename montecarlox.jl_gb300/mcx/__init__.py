@@ -295,7 +295,7 @@ class DeviceLattice(AbstractSpinSystem):
         return self.N
 
     def set_uniforms(self, form="planes"):
-        """How Metropolis and Glauber sweeps without a field draw their uniforms (mcx_lattice_set_uniforms):
+        """How the sweeps of this Ising lattice draw their uniforms (mcx_lattice_set_uniforms):
         "site" (one Philox word per site, the default) or "planes" (bit planes for the top 8
         bits, compared for 64 sites at once; Ising, Lx a multiple of 128).  Same distribution,
         different chain."""

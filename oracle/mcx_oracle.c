@@ -330,31 +330,6 @@ void orc_init_random(int8_t* s, int model, int dim, const int32_t* L, uint64_t s
  *          SpinSystems/src/ising.jl:25-58, modify! :493-498.
  *   Blume-Capel: spin_flip! blume_capel.jl:52-85, modify! :250-256.
  * ------------------------------------------------------------------------- */
-/* Whether an Ising table has the rank form that the bit-plane uniforms apply to: always
- * accepted with at most z/2 aligned neighbours, the same threshold for both spin states
- * above, non-increasing in the aligned count (Metropolis without a field). */
-static int rank_form(const uint64_t* thr, int z) {
-    const uint64_t always = 1ull << 32;
-    for (int a = 0; a <= z; ++a) {
-        const uint64_t dn = thr[a], up = thr[a + z + 1];
-        if (a <= z / 2) {
-            if (dn != always || up != always) return 0;
-        } else {
-            if (dn != up || dn >= always) return 0;
-            if (a > z / 2 + 1 && dn > thr[a - 1]) return 0;
-        }
-    }
-    return 1;
-}
-
-/* Whether an Ising table has the class form: one threshold below 2^32 per aligned count,
- * the same for both spin states, no xor mask (Glauber without a field). */
-static int class_form(const uint64_t* thr, const uint32_t* xm, int z) {
-    for (int a = 0; a <= z; ++a)
-        if (thr[a] != thr[a + z + 1] || thr[a] >= (1ull << 32) || xm[a] || xm[a + z + 1]) return 0;
-    return 1;
-}
-
 static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                     double J, double D, double h, uint64_t seed, uint32_t stream,
                     uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
@@ -368,7 +343,7 @@ static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, do
                                 : orc_table_bc(dim, alg, beta, J, D, h, thr);
     if (rc) return rc;
     if (uniforms && (model != ORC_ISING || L[0] % 128 != 0)) return ORC_ERR_INVALID;
-    const int planes = uniforms && alg != ORC_HEATBATH && (rank_form(thr, z) || class_form(thr, xm, z));
+    const int planes = uniforms;  /* every Ising rule: flip iff (u ^ xm) < thr with the plane uniform */
     int64_t P, M, Q;
     orc_observables(s, dim, L, &P, &M, &Q);
     uint64_t att = 0, acc = 0;
@@ -429,9 +404,8 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
     return cb_sweep(s, model, dim, L, alg, beta, J, D, h, seed, stream, sweep0, nsweeps, obs, attempts, accepts, 0);
 }
 
-/* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes for
- * the rules of the rank or the class form; bit planes need an Ising lattice with Lx a
- * multiple of 128). */
+/* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes; bit
+ * planes need an Ising lattice with Lx a multiple of 128 and apply to every Ising rule). */
 int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                    double J, double D, double h, uint64_t seed, uint32_t stream,
                    uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,

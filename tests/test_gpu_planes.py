@@ -92,21 +92,28 @@ def test_planes_l4096_bit_exact(gpu):
     sys_.close()
 
 
-@pytest.mark.parametrize("alg,h", [("glauber", 0.2), ("heatbath", 0.0), ("metropolis", 0.3)])
-def test_other_rules_keep_the_site_words(gpu, alg, h):
-    """Rules without the rank form draw per-site words on a plane lattice too."""
-    sys_, a, obs, s, oobs, att, acc = _pair(gpu, [256, 64], 0.44, alg=alg, h=h, nsweeps=3)
-    assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s)
-    s2 = O.init_random(O.ISING, [256, 64], 42)
-    oobs2, _, _ = O.cb_sweep(s2, O.ISING, [256, 64], {"glauber": O.GLAUBER, "heatbath": O.HEATBATH,
-                                                      "metropolis": O.METROPOLIS}[alg], 0.44, 42, nsweeps=3, h=h)
-    assert np.array_equal(oobs, oobs2)
+GENERAL_CASES = [  # alg, h, dims, beta: heat bath and fields (the general form), always / never classes at beta 3
+    ("heatbath", 0.0, [256, 64], 0.44), ("heatbath", 0.2, [128, 128], 0.3), ("heatbath", 0.0, [128, 16, 8], 0.2216),
+    ("heatbath", -0.1, [256, 12, 10], 3.0), ("metropolis", 0.3, [256, 64], 0.44), ("metropolis", -0.5, [128, 16, 8], 3.0),
+    ("glauber", 0.2, [1024, 96], 0.6), ("glauber", -0.2, [256, 12, 10], 0.25),
+]
+
+
+@pytest.mark.parametrize("layout", ["int8", "msc64"])
+@pytest.mark.parametrize("alg,h,L,beta", GENERAL_CASES)
+def test_planes_general_form_parity(gpu, alg, h, L, beta, layout):
+    """Every other Ising rule (heat bath; Metropolis and Glauber with a field) with bit-plane
+    uniforms on the packed words, against the oracle: flips, series and counters."""
+    sys_, a, obs, s, oobs, att, acc = _pair(gpu, L, beta, seed=11, stream=3, layout=layout, alg=alg, h=h)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
     sys_.close()
 
 
 def test_planes_calls_compose_and_switch(gpu):
     """3 + 5 sweeps equal 8; switching back to per-site words continues the same lattice
-    with the per-site stream; a heat-bath call in between runs on the int8 words."""
+    with the per-site stream; a heat-bath call in between (the general form) continues it."""
     L = [512, 256]
     sys_ = gpu.Ising(L)
     sys_.set_uniforms("planes")
@@ -168,8 +175,10 @@ def test_planes_argument_errors(gpu):
     s = gpu.Ising([128, 64])
     s.set_uniforms("planes")
     s.set_packing(False)
-    with pytest.raises(gpu.ArgumentError):
-        gpu.sweep_(s, gpu.Metropolis(gpu.Philox(1), beta=0.4), 1)
+    for kind in (gpu.Metropolis, gpu.HeatBath):
+        with pytest.raises(gpu.ArgumentError):
+            gpu.sweep_(s, kind(gpu.Philox(1), beta=0.4), 1)
+    s.set_uniforms("site")
     gpu.sweep_(s, gpu.HeatBath(gpu.Philox(1), beta=0.4), 1)  # per-site words: fine
     s.close()
 
@@ -206,23 +215,34 @@ def test_planes_refused_by_noalloc(gpu):
     s.set_uniforms("planes")
     r = gpu._lib.mcx_rng(1, 0, 0, 0)
     assert fn(s.handle, 0, 0.4, C.byref(r), 2, None, None) == 1  # MCX_ERR_INVALID_ARG
-    assert fn(s.handle, 2, 0.4, C.byref(r), 2, None, None) == 0  # heat bath: per-site words
+    assert fn(s.handle, 2, 0.4, C.byref(r), 2, None, None) == 1  # heat bath draws planes too
+    s.set_uniforms("site")
+    assert fn(s.handle, 2, 0.4, C.byref(r), 2, None, None) == 0
     s.close()
 
 
-@pytest.mark.parametrize("alg", ["metropolis", "glauber"])
-def test_planes_kaufman_l128(gpu, alg):
-    """16 independent 128^2 chains with plane uniforms (Metropolis or Glauber, beta 0.4407,
-    10^3 thermalisation + 5000 recorded sweeps): the mean energy per site within 3 standard
-    errors of the chain means of Kaufman's exact finite-torus value."""
+@pytest.mark.parametrize("alg,beta,start", [("metropolis", 0.4407, "random"), ("glauber", 0.3, "random"),
+                                             ("glauber", 0.6, "up"), ("heatbath", 0.3, "random"),
+                                             ("heatbath", 0.6, "up")])
+def test_planes_kaufman_l128(gpu, alg, beta, start):
+    """16 independent 128^2 chains with plane uniforms (10^3 thermalisation + 5000 recorded
+    sweeps): the mean energy per site within 3 standard errors of the chain means of
+    Kaufman's exact finite-torus value.  Metropolis at beta 0.4407; Glauber and heat bath
+    (the same flip probabilities, slower to relax) off beta_c: at 0.4407 both the per-site and
+    the plane form of the oracle's heat bath sit at -1.398 after these sweeps from a random
+    start, against the exact -1.4192."""
     from mcx.analysis import kaufman_ising2d
-    L, beta, nch = 128, 0.4407, 16
+    L, nch = 128, 16
     means = []
     for i in range(nch):
         c = gpu.Ising([L, L])
         c.set_uniforms("planes")
-        gpu.init_(c, "random", rng=gpu.Philox(42, i))
-        a = (gpu.Metropolis if alg == "metropolis" else gpu.Glauber)(gpu.Philox(42, i), beta=beta)
+        if start == "random":
+            gpu.init_(c, "random", rng=gpu.Philox(42, i))
+        else:
+            gpu.init_(c, start)
+        a = {"metropolis": gpu.Metropolis, "glauber": gpu.Glauber, "heatbath": gpu.HeatBath}[alg](gpu.Philox(42, i),
+                                                                                                beta=beta)
         gpu.sweep_(c, a, 1000)
         obs = gpu.sweep_(c, a, 5000, record=True)
         means.append((-obs[:, 0] / (L * L)).mean())
