@@ -84,7 +84,9 @@ def parse_args():
     ap.add_argument("--impl", choices=["mcx", "reference"], default="mcx")
     ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--uniforms", choices=["planes", "site"], default="planes",
-                    help="how the headline sweeps draw their Metropolis uniforms (mcx_lattice_set_uniforms)")
+                    help="how the headline sweeps draw their uniforms (mcx_lattice_set_uniforms)")
+    ap.add_argument("--algorithm", choices=["metropolis", "glauber", "heatbath"], default="metropolis",
+                    help="the headline workload's rule (the configured workload is Metropolis)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the parallel-tempering and serving lines")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU sample length")
@@ -119,14 +121,25 @@ CB_TRAFFIC_PER_LAUNCH = 16810240
 # The same for one k_msc_metro<2,*> launch (the headline workload's kernel: int8 lattices run
 # multi-sweep calls on a transient 64-sites-per-word copy), per uniforms form,
 # profiles/msc_metro_L4096.md and profiles/int_pipes_ising_strip_and_pt_persistent.md.
-MSC_TRAFFIC_PER_LAUNCH = {"site": 2136576, "planes": 2118656}
+MSC_TRAFFIC_PER_LAUNCH = {("site", "metropolis"): 2136576, ("planes", "metropolis"): 2118656,
+                          ("planes", "glauber"): 2123520, ("planes", "heatbath"): 2120960}
 
 # Per-launch integer-pipe work of the headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
-MSC_PIPES = {"site": {"warp_inst": 4710668, "alu_inst": 2143878, "fma_cycles": 6717168, "per": "launch"},
-             "planes": {"warp_inst": 2699982, "alu_inst": 1276356, "fma_cycles": 2403736, "per": "launch"}}
+MSC_PIPES = {("site", "metropolis"): {"warp_inst": 4710668, "alu_inst": 2143878, "fma_cycles": 6717168, "per": "launch"},
+             ("planes", "metropolis"): {"warp_inst": 2699982, "alu_inst": 1276356, "fma_cycles": 2403736,
+                                        "per": "launch"},
+             ("planes", "glauber"): {"warp_inst": 3616731, "alu_inst": 1978005, "fma_cycles": 2560230, "per": "launch"},
+             ("planes", "heatbath"): {"warp_inst": 3748500, "alu_inst": 2221129, "fma_cycles": 2761404, "per": "launch"}}
+
+
+def headline_kernel(uniforms, algorithm):
+    """The half-sweep kernel of the headline lattice for a uniforms form and rule."""
+    if uniforms == "planes":
+        return "k_msc_metro<2,true,%d>" % {"metropolis": 0, "glauber": 1, "heatbath": 2}[algorithm]
+    return "k_msc_metro<2,false,0>" if algorithm == "metropolis" else "k_ising_strip (int8 words)"
 PT_PIPES = {"warp_inst": 64528754 / 3, "alu_inst": 32555444 / 3, "fma_cycles": 67545556 / 3, "per": "sweep"}
 
 
@@ -326,8 +339,8 @@ def bench_headline_form(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, 
     launch_s = tot * 1e-3 / (2 * sweeps_per_step * steps)
     return {"workload": "ising2d_L4096_metropolis_%s_%s_uniforms" % (layout, uniforms),
             "attempts_per_ns": N * sweeps_per_step * steps / (tot * 1e6), "ms_per_step": tot / steps,
-            "sweeps_per_step": sweeps_per_step, "kernel": "k_msc_metro<2,%s>" % ("true" if uniforms == "planes" else "false"),
-            "roofline": int_roof(MSC_PIPES[uniforms], launch_s, sm_mhz, nsm)}
+            "sweeps_per_step": sweeps_per_step, "kernel": headline_kernel(uniforms, "metropolis"),
+            "roofline": int_roof(MSC_PIPES[(uniforms, "metropolis")], launch_s, sm_mhz, nsm)}
 
 
 def bench_int8_words(torch, mcx, ctx, flush, steps, warmup, sweeps_per_step, nsm, sm_mhz):
@@ -827,7 +840,8 @@ def run_mcx(args):
     lat = mcx.Ising(L, ctx=ctx)
     lat.set_uniforms(args.uniforms)
     mcx.init_(lat, "random", rng=mcx.Philox(SEED, rank))
-    alg = mcx.Metropolis(mcx.Philox(SEED, rank), beta=BETA)
+    alg = {"metropolis": mcx.Metropolis, "glauber": mcx.Glauber, "heatbath": mcx.HeatBath}[args.algorithm](
+        mcx.Philox(SEED, rank), beta=BETA)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def barrier():
@@ -931,19 +945,19 @@ def run_mcx(args):
         cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": "%d host threads x %d sequential random-site Metropolis attempts (spin_flip! order, "
                          "FP64 exp) on an L=%d lattice each, %.1f s" % (ncores, per, L_SIDE, t)}
-    tr = MSC_TRAFFIC_PER_LAUNCH[args.uniforms]
+    tr = MSC_TRAFFIC_PER_LAUNCH.get((args.uniforms, args.algorithm))
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
     if pt_res:
         pt_res["roofline"].update(int_roof(PT_PIPES, pt_res["persistent"]["ms_per_sweep"] * 1e-3, sm_mhz, nsm))
     for r in (other_form, msc_res):  # the legs' fractions at the clock sampled in the timed region
         if r:
-            r["roofline"] = int_roof(MSC_PIPES[r["workload"].split("_")[-2]], r["ms_per_step"] * 1e-3 / (2 * S),
-                                     sm_mhz, nsm)
+            r["roofline"] = int_roof(MSC_PIPES[(r["workload"].split("_")[-2], "metropolis")],
+                                     r["ms_per_step"] * 1e-3 / (2 * S), sm_mhz, nsm)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
-        "config": {"workload": "ising2d_L4096_metropolis_int8", "L": L_SIDE, "beta": BETA, "seed": SEED,
+        "config": {"workload": "ising2d_L4096_%s_int8" % args.algorithm, "L": L_SIDE, "beta": BETA, "seed": SEED,
                    "layout": "int8 colour-split storage; each call sweeps a transient 64-sites-per-word copy "
                              "(packed at its start, unpacked at its end; mcx_lattice_set_packing)",
                    "uniforms": args.uniforms + (" (top 8 bits of each site's 32-bit uniform from bit planes "
@@ -955,9 +969,10 @@ def run_mcx(args):
                    "parallelism": "replicas"},
         "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": tr, "peak_kind": peak_kind,
-                          "kernel": "k_msc_metro<2,%s>" % ("true" if args.uniforms == "planes" else "false"),
+                          "kernel": headline_kernel(args.uniforms, args.algorithm),
                           "alg_bytes_per_launch": alg_bytes},
-                         **int_roof(MSC_PIPES[args.uniforms], avg_launch_s, sm_mhz, nsm)),
+                         **(int_roof(MSC_PIPES[(args.uniforms, args.algorithm)], avg_launch_s, sm_mhz, nsm)
+                            if (args.uniforms, args.algorithm) in MSC_PIPES else {})),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N,
                 "d2h_bytes_per_step": S * 3 * 8 + 8},
         "gpu_launches": launches,
