@@ -1,12 +1,14 @@
 // mcx_msc.cu -- multi-spin-coded (MSC64) Ising sweeps: 64 same-colour sites per
 // uint64 word (bit b of word w of a colour row <-> entry k = 64w + b of the int8
 // colour-split layout; bit set = spin up).  Neighbour counts are formed for 64
-// sites at once with bit-sliced adders; every site still draws its own Philox word,
-// so results are bit-identical to the int8 kernels.  Only rules in the rank form of
-// k_msc_metro (Metropolis without a field) are swept on the words: the other rules
-// (heat bath, Glauber, a field) need a per-site table lookup, which on a GB300 ran
-// at 451-479 attempts/ns against 749-759 on the int8 words, so MSC64 lattices sweep
-// those on their int8 arrays (mcx_sweep unpacks before and packs after the call).
+// sites at once with bit-sliced adders.  With per-site uniforms every site draws its
+// own Philox word, so results are bit-identical to the int8 kernels, and only rules in
+// the rank form of k_msc_metro (Metropolis without a field) are swept on the words: the
+// other rules (heat bath, Glauber, a field) would need a per-site table lookup, which on
+// a GB300 ran at 451-479 attempts/ns against 749-759 on the int8 words, so MSC64 lattices
+// sweep those on their int8 arrays (mcx_sweep unpacks before and packs after the call).
+// With bit-plane uniforms (mcx_lattice_set_uniforms) every Ising rule is swept on the
+// words, in the rank, class or general form of k_msc_metro.
 #include "mcx_device.cuh"
 #include "mcx_internal.h"
 #include "mcx_sweep.cuh"

@@ -719,11 +719,11 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // ones (and those the cluster form does not take, up to kSmallLattice sites) in one
     // block; larger ones replay a captured chunk of kGraphChunk sweeps as often as it fits
     // and launch the rest directly
-    // MSC64 lattices sweep the packed words only under k_msc_metro's rank form; other rules
-    // run on their int8 arrays (unpacked before, packed after the call), which is faster
-    // than a per-site table lookup on the words
-    // A rank-form call with bit-plane uniforms always runs on the words: an int8 lattice's
-    // on its transient copy, whatever the call's length (the int8 kernels draw per-site words).
+    // With per-site uniforms MSC64 lattices sweep the packed words only under k_msc_metro's
+    // rank form; other rules run on their int8 arrays (unpacked before, packed after the
+    // call), which is faster than a per-site table lookup on the words.
+    // With bit-plane uniforms every Ising call runs on the words: an int8 lattice's on its
+    // transient copy, whatever the call's length (the int8 kernels draw per-site words).
     const bool pl_rule = msc_planes_ok(lat, alg, t);  // every Ising rule under bit-plane uniforms
     const bool msc_words = lat->layout == MCX_LAYOUT_MSC64 && (pl_rule || msc_rank_ok(lat, alg, t));
     const bool via_int8 = lat->layout == MCX_LAYOUT_MSC64 && !msc_words;
