@@ -423,8 +423,8 @@ def bench_c2_matrix(torch, mcx, ctx, sweeps=10000):
 def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_step=100):
     """Other single-lattice sweeps, device-timed, L2 flushed between steps: 3-D Ising 256^3
     (transient packed copy; per-site and bit-plane uniforms), Ising heat bath (int8 strip
-    kernel; bit planes on the packed copy) and Blume-Capel (D = 1) Metropolis / heat bath on
-    the 4096^2 lattice (column-strip half-sweeps)."""
+    kernel; bit planes on the packed copy) and Blume-Capel (D = 1) Metropolis (per-site and
+    plane proposal bits) / heat bath on the 4096^2 lattice (column-strip half-sweeps)."""
     lib = mcx._lib.load()
     def planes(lat):
         lat.set_uniforms("planes")
@@ -438,7 +438,9 @@ def bench_other_lattices(torch, mcx, ctx, flush, steps=3, warmup=3, sweeps_per_s
              ("ising2d_L4096_heatbath", lambda: mcx.Ising([L_SIDE, L_SIDE], ctx=ctx), mcx.HeatBath, BETA),
              ("bc2d_L4096_D1_metropolis", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.Metropolis,
               0.6),
-             ("bc2d_L4096_D1_heatbath", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.HeatBath, 0.6)]
+             ("bc2d_L4096_D1_heatbath", lambda: mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx), mcx.HeatBath, 0.6),
+             ("bc2d_L4096_D1_metropolis_plane_uniforms", lambda: planes(mcx.BlumeCapel([L_SIDE, L_SIDE], D=1.0, ctx=ctx)),
+              mcx.Metropolis, 0.6)]
     out = {}
     for name, make, kind, beta in cases:
         lat = make()

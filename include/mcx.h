@@ -72,7 +72,11 @@ typedef enum mcx_layout { MCX_LAYOUT_INT8 = 0, MCX_LAYOUT_MSC64 = 1 } mcx_layout
  *         for 64 sites at once; the low 24 bits come from a per-site block (like SITE,
  *         another counter purpose) and are drawn only for the sites whose top 8 bits equal
  *         their threshold's.  Applies to every Ising rule (Metropolis, Glauber, heat
- *         bath, with or without a field; all swept on 64-sites-per-word words). */
+ *         bath, with or without a field; all swept on 64-sites-per-word words).  On a
+ *         Blume-Capel lattice PLANES replaces the proposal word (whose top bit is the
+ *         proposal bit) by bit e & 63 of plane e >> 6, planes 2m and 2m+1 being words
+ *         0 | 1 << 32 and 2 | 3 << 32 of one Philox block (one block per 128 sites); the
+ *         acceptance words stay per site. */
 typedef enum mcx_uniforms { MCX_UNIFORMS_SITE = 0, MCX_UNIFORMS_PLANES = 1 } mcx_uniforms;
 
 /* Flat-histogram mode: Multicanonical (src/algorithms/multicanonical.jl) or
@@ -177,13 +181,14 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
  * of device memory on first use within the HBM budget.  Results are bit-identical either
  * way; the copy is faster.  Default on; off keeps every call on the int8 kernels. */
 MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow);
-/* Selects the uniforms of later sweeps (mcx_uniforms; default SITE).  PLANES needs an
- * Ising lattice with Lx a multiple of 128 (MCX_ERR_INVALID_ARG otherwise); on the int8
+/* Selects the uniforms of later sweeps (mcx_uniforms; default SITE).  PLANES needs Lx a
+ * multiple of 128 on an Ising lattice (MCX_ERR_INVALID_ARG otherwise); on the int8
  * layout its calls run on the transient 64-sites-per-word copy whatever their
  * length, so mcx_sweep returns MCX_ERR_INVALID_ARG with packing off and MCX_ERR_BUDGET /
  * MCX_ERR_OOM when the N/8-byte copy does not fit.  mcx_sweep_noalloc (int8 kernels
- * only) refuses such calls; mcx_sweep_batch runs them one mcx_sweep per lattice.  The two
- * forms give different chains with the same distribution. */
+ * only) refuses such Ising calls; mcx_sweep_batch runs them one mcx_sweep per lattice.
+ * Blume-Capel lattices of any size take PLANES on every launch form.  The two forms give
+ * different chains with the same distribution. */
 MCX_API mcx_status mcx_lattice_set_uniforms(mcx_lattice* lat, int32_t form);
 /* Times the admissible kernel shapes (sites per thread: 16, 8, 4) for this lattice
  * and algorithm on a scratch copy of the spins and keeps the fastest for later

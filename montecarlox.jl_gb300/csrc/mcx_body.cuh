@@ -55,24 +55,39 @@ __device__ __forceinline__ void ising_chunk(Chunk<DIM, V>& ch, uint32_t c0, cons
     }
 }
 
-// One Blume-Capel chunk (acceptance and proposal words from two Philox calls per word;
-// heat bath needs no proposal).  Deltas go to nacc and (dP, dM, dQ).
+// One Blume-Capel chunk (acceptance words from one Philox call per four sites; proposal
+// bits from the top bits of a second call's words, or with bit planes from one 64-bit
+// plane: bit e & 63 of plane e >> 6, planes 2m and 2m+1 being words 0 | 1 << 32 and
+// 2 | 3 << 32 of the block at counter m; heat bath needs no proposal).  c0 = e0 / 4 for the
+// chunk's first colour index e0 (a chunk of at most 16 aligned sites lies in one plane).
+// Deltas go to nacc and (dP, dM, dQ).
 template <int DIM, int V, bool HB>
 __device__ __forceinline__ void bc_chunk(Chunk<DIM, V>& ch, uint32_t c0, const SweepKey& key, uint32_t w2a,
-                                         uint32_t w2p, const unsigned long long* s_thr, int& nacc, int& dP, int& dM,
-                                         int& dQ) {
+                                         uint32_t w2p, bool planes, const unsigned long long* s_thr, int& nacc,
+                                         int& dP, int& dM, int& dQ) {
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
     BcLanes ln;
+    unsigned long long plane = 0;
+    if (!HB && planes) {
+        const unsigned long long e0 = 4ull * c0;
+        const uint4 b = philox10(make_uint4((uint32_t)(e0 >> 7), (uint32_t)key.sweep, w2p, key.stream), key.k0, key.k1);
+        plane = (e0 >> 6) & 1 ? ((unsigned long long)b.w << 32) | b.z : ((unsigned long long)b.y << 32) | b.x;
+    }
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
         uint32_t nbw[Z];
 #pragma unroll
         for (int d = 0; d < Z; ++d) nbw[d] = ch.nb[d][w];
         const uint4 ra = philox10(make_uint4(c0 + w, (uint32_t)key.sweep, w2a, key.stream), key.k0, key.k1);
-        uint4 rp = make_uint4(0, 0, 0, 0);
-        if (!HB) rp = philox10(make_uint4(c0 + w, (uint32_t)key.sweep, w2p, key.stream), key.k0, key.k1);
-        ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, ln);
+        uint32_t bits = 0;
+        if (!HB) {
+            if (planes)
+                bits = bc_plane_bits((uint32_t)(plane >> ((4u * (c0 + w)) & 63u)) & 0xFu);
+            else
+                bits = bc_site_bits(philox10(make_uint4(c0 + w, (uint32_t)key.sweep, w2p, key.stream), key.k0, key.k1));
+        }
+        ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, bits, s_thr, nacc, ln);
     }
     bc_lanes_fold<Z>(ln, dP, dM, dQ);
 }

@@ -239,15 +239,24 @@ struct BcLanes {
     uint32_t pn = 0, po = 0, qn = 0, qo = 0, cn = 0, co = 0;
 };
 
+// The proposal bits of four sites as bytes 0/1: the top bits of the four proposal words
+// (the reference's rand(rng, Bool)), or four consecutive bits of a bit plane (the
+// multiply copies bit i to bit 8 i; the copies do not overlap).
+__device__ __forceinline__ uint32_t bc_site_bits(uint4 rp) {
+    const uint32_t txy = __byte_perm(rp.x, rp.y, 0x0073u);  // bytes 0, 1: top bytes of x, y
+    const uint32_t tzw = __byte_perm(rp.z, rp.w, 0x0073u);
+    return (__byte_perm(txy, tzw, 0x5410u) >> 7) & 0x01010101u;
+}
+__device__ __forceinline__ uint32_t bc_plane_bits(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
+
 // Blume-Capel decision for the four sites of one word without per-site branches.
-// Metropolis / Glauber: proposal bits from the top bits of the proposal words (the
-// reference's rand(rng, Bool)), table entry (s_old+1)*2*NC + bit*NC + S formed
+// Metropolis / Glauber: proposal bits as bytes 0/1 (`bits`), table entry (s_old+1)*2*NC + bit*NC + S formed
 // byte-parallel, one 64-bit threshold compare per site, the proposed spins and the
 // accepted bytes merged with byte masks.  Heat bath: sn = -1 + [u >= T1] + [u >= T12]
 // per site from the cumulative thresholds at 2S, 2S+1.  Returns the new word; counts
 // changed sites into nacc and the observable deltas into the byte lanes.
 template <int Z, bool HB>
-__device__ __forceinline__ uint32_t bc_word_swar(const uint32_t (&nbw)[Z], uint32_t own, uint4 ra, uint4 rp,
+__device__ __forceinline__ uint32_t bc_word_swar(const uint32_t (&nbw)[Z], uint32_t own, uint4 ra, uint32_t bits,
                                                  const unsigned long long* s_thr, int& nacc, BcLanes& ln) {
     constexpr int NC = 2 * Z + 1;
     uint32_t cnt = 0;
@@ -267,10 +276,7 @@ __device__ __forceinline__ uint32_t bc_word_swar(const uint32_t (&nbw)[Z], uint3
             nw |= ((c + 0xFFu) & 0xFFu) << (8 * b);
         }
     } else {
-        // proposal bits (top bit of each proposal word) as bytes 0/1, and as 0x00/0xFF masks
-        const uint32_t txy = __byte_perm(rp.x, rp.y, 0x0073u);  // bytes 0, 1: top bytes of x, y
-        const uint32_t tzw = __byte_perm(rp.z, rp.w, 0x0073u);
-        const uint32_t bits = (__byte_perm(txy, tzw, 0x5410u) >> 7) & 0x01010101u;
+        // proposal bits (bytes 0/1), and as 0x00/0xFF masks
         const uint32_t bm = bits * 0xFFu;
         const uint32_t idx = po * (uint32_t)(2 * NC) + bits * (uint32_t)NC + cnt;  // bytes <= 77
         uint32_t f = 0;

@@ -93,7 +93,8 @@ __device__ __forceinline__ void cluster_run(const ClusterArgs& ca) {
             const int8_t* const oth = c ? s[0] : s[1];
             int8_t* const up_halo = c ? up1 : up0;
             int8_t* const dn_halo = c ? dn1 : dn0;
-            const uint32_t w2a = ctr_word2(key.sweep, c, P_ACCEPT), w2p = ctr_word2(key.sweep, c, P_PROPOSE);
+            const uint32_t w2a = ctr_word2(key.sweep, c, P_ACCEPT),
+                           w2p = ctr_word2(key.sweep, c, a0.planes ? P_PLANES : P_PROPOSE);
             int nacc = 0, nup = 0, isum = 0, dP = 0, dM = 0, dQ = 0;
             for (ChunkIter it = it0; it.valid(); it.next()) {
                 const int lu = it.z + 1;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void cluster_run(const ClusterArgs& ca) {
                 ch.load(cur, oth, W, lr, k0, ri);
                 const uint32_t c0 = (uint32_t)(((unsigned long long)gr * W + k0) >> 2);
                 if constexpr (KIND == 0) ising_chunk<DIM, V, HB, T32>(ch, c0, key, w2a, s_thr, s_t32, nacc, nup, isum);
-                else bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, s_thr, nacc, dP, dM, dQ);
+                else bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, a0.planes != 0, s_thr, nacc, dP, dM, dQ);
                 store_row<V>(cur + lr * W + k0, ch.own);
                 const int uoff = it.y * W + k0;
                 if (it.z == 0) store_row<V>(up_halo + uoff, ch.own);

@@ -134,6 +134,7 @@ struct mcx_lattice {
     unsigned long long* d_sweep_base = nullptr;  // {first sweep, seed, stream, series offset} read by captured graphs
     struct Graph {
         int alg;
+        int uniforms;  // the captured arguments carry the form (Blume-Capel proposals)
         double beta;
         int64_t nsweeps;
         int V;

@@ -504,8 +504,8 @@ extern "C" MCX_API mcx_status mcx_lattice_set_uniforms(mcx_lattice* lat, int32_t
     if (!lat) return mcx::fail(MCX_ERR_INVALID_ARG, "lattice is NULL");
     if (form != MCX_UNIFORMS_SITE && form != MCX_UNIFORMS_PLANES)
         return mcx::fail(MCX_ERR_INVALID_ARG, "unknown uniforms form %d", (int)form);
-    if (form == MCX_UNIFORMS_PLANES && (lat->model != MCX_ISING || lat->L[0] % 128 != 0))
-        return mcx::fail(MCX_ERR_INVALID_ARG, "bit-plane uniforms need an Ising lattice with Lx a multiple of 128");
+    if (form == MCX_UNIFORMS_PLANES && lat->model == MCX_ISING && lat->L[0] % 128 != 0)
+        return mcx::fail(MCX_ERR_INVALID_ARG, "bit-plane uniforms of an Ising lattice need Lx a multiple of 128");
     lat->uniforms = form;
     return MCX_OK;
 }

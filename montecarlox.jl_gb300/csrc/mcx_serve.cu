@@ -74,9 +74,9 @@ __device__ __forceinline__ void srv_tile(const SrvJobDev& J, const SrvTile& tl, 
                 const uint32_t fb = ising_word<Z, HB>(nbw, ch.own[w], ra, s_thr, nacc, a1, a2);
                 ch.own[w] ^= fb * 0xFEu;
             } else {
-                uint4 rp = make_uint4(0, 0, 0, 0);
-                if (!HB) rp = philox10(make_uint4(c0 + w, (uint32_t)t, w2p, J.stream), J.k0, J.k1);
-                ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, rp, s_thr, nacc, ln);
+                uint32_t bits = 0;
+                if (!HB) bits = bc_site_bits(philox10(make_uint4(c0 + w, (uint32_t)t, w2p, J.stream), J.k0, J.k1));
+                ch.own[w] = bc_word_swar<Z, HB>(nbw, ch.own[w], ra, bits, s_thr, nacc, ln);
             }
         }
         if (MODEL != 0) bc_lanes_fold<Z>(ln, a1, a2, a3);

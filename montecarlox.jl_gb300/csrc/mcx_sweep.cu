@@ -243,7 +243,7 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
                                            long long (&v)[4]) {
     const SweepKey key = sweep_key(a);
     const uint32_t w2a = ctr_word2(key.sweep, a.colour, P_ACCEPT);
-    const uint32_t w2p = ctr_word2(key.sweep, a.colour, P_PROPOSE);
+    const uint32_t w2p = ctr_word2(key.sweep, a.colour, a.planes ? P_PLANES : P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
     for (; it.valid(); it.next()) {
         const int r = it.row();
@@ -252,7 +252,7 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
         Chunk<DIM, V> ch;
         ch.load(a.cur, a.oth, a.W, r, k0, ri);
         const uint32_t c0 = (uint32_t)(((unsigned long long)r * a.W + k0) >> 2);
-        bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, s_thr, nacc, dP, dM, dQ);
+        bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, a.planes != 0, s_thr, nacc, dP, dM, dQ);
         store_row<V>(a.cur + (long long)r * a.W + k0, ch.own);
     }
     v[0] += dP;
@@ -278,10 +278,11 @@ __global__ void __launch_bounds__(256, 2) k_bc_strip(const SweepArgs a) {
     } else if (tid < tpc * (a.W / V)) {
         const SweepKey key = sweep_key(a);
         const uint32_t w2a = ctr_word2(key.sweep, a.colour, P_ACCEPT);
-        const uint32_t w2p = ctr_word2(key.sweep, a.colour, P_PROPOSE);
+        const uint32_t w2p = ctr_word2(key.sweep, a.colour, a.planes ? P_PLANES : P_PROPOSE);
+        const bool planes = a.planes != 0;
         int nacc = 0, dP = 0, dM = 0, dQ = 0;
         strip_walk<DIM, V>(a, tid, tpc, [&](Chunk<DIM, V>& ch, uint32_t c0) {
-            bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, s_thr, nacc, dP, dM, dQ);
+            bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, planes, s_thr, nacc, dP, dM, dQ);
         });
         v[0] += dP;
         v[1] += dM;
@@ -302,7 +303,7 @@ __device__ __forceinline__ void bc_site_body(const SweepArgs& a, const unsigned 
     const unsigned long long sweep = key.sweep;
     const long long n = (long long)a.W * a.rows;
     const uint32_t w2a = ctr_word2(sweep, a.colour, P_ACCEPT);
-    const uint32_t w2p = ctr_word2(sweep, a.colour, P_PROPOSE);
+    const uint32_t w2p = ctr_word2(sweep, a.colour, a.planes ? P_PLANES : P_PROPOSE);
     int nacc = 0, dP = 0, dM = 0, dQ = 0;
     for (long long j = first; j < n; j += stride) {
         const int r = (int)(j / a.W), k = (int)(j - (long long)r * a.W);
@@ -319,8 +320,15 @@ __device__ __forceinline__ void bc_site_body(const SweepArgs& a, const unsigned 
             sn = (unsigned long long)u < s_thr[2 * S] ? -1 : ((unsigned long long)u < s_thr[2 * S + 1] ? 0 : 1);
             acc = sn != so;
         } else {
-            const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2p, key.stream), key.k0, key.k1), (int)(j & 3));
-            const int bit = (int)(pw >> 31);
+            int bit;
+            if (a.planes) {  // bit j & 63 of plane j >> 6: half (j >> 6) & 1 of the block at j >> 7
+                const uint4 b = philox10(make_uint4((uint32_t)(j >> 7), (uint32_t)sweep, w2p, key.stream), key.k0, key.k1);
+                const uint32_t half = (j >> 5) & 1 ? ((j >> 6) & 1 ? b.w : b.y) : ((j >> 6) & 1 ? b.z : b.x);
+                bit = (int)((half >> (j & 31)) & 1u);
+            } else {
+                const uint32_t pw = pick4(philox10(make_uint4((uint32_t)(j >> 2), (uint32_t)sweep, w2p, key.stream), key.k0, key.k1), (int)(j & 3));
+                bit = (int)(pw >> 31);
+            }
             acc = (unsigned long long)u < s_thr[(so + 1) * 2 * NC + bit * NC + S];
             sn = bc_propose(so, bit);
         }
@@ -399,6 +407,7 @@ __device__ __forceinline__ void lattice_small_run(const SweepArgs& a0, int8_t* g
     a.k0 = a0.k0;
     a.k1 = a0.k1;
     a.stream = a0.stream;
+    a.planes = a0.planes;
     a.sweep_base = nullptr;
     a.acc = a0.acc;
     const unsigned long long sweep0 = a0.sweep;
@@ -604,6 +613,7 @@ void fill_sweep_args(SweepArgs* a, const mcx_lattice* lat, const Table& t, const
     a->k1 = (uint32_t)(rng->seed >> 32);
     a->stream = rng->stream;
     for (int i = 0; i < t.n; ++i) a->thr[i] = t.thr[i];
+    a->planes = lat->model == MCX_BLUME_CAPEL && lat->uniforms == MCX_UNIFORMS_PLANES;
 }
 
 mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const mcx_rng* rng,
@@ -651,7 +661,7 @@ static cudaError_t launch_half(HalfSweepFn fn, int grid, cudaStream_t st, const 
 static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, const Table& t, int V,
                               cudaGraphExec_t* out) {
     for (auto& g : lat->graphs)
-        if (g.alg == (int)alg && g.beta == beta && g.V == V && g.series == lat->d_series) {
+        if (g.alg == (int)alg && g.uniforms == lat->uniforms && g.beta == beta && g.V == V && g.series == lat->d_series) {
             *out = g.exec;
             return MCX_OK;
         }
@@ -693,7 +703,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
         cudaGraphExecDestroy(lat->graphs.front().exec);
         lat->graphs.erase(lat->graphs.begin());
     }
-    lat->graphs.push_back({(int)alg, beta, kGraphChunk, V, lat->d_series, exec});
+    lat->graphs.push_back({(int)alg, lat->uniforms, beta, kGraphChunk, V, lat->d_series, exec});
     *out = exec;
     return MCX_OK;
 }

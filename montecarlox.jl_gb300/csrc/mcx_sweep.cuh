@@ -20,6 +20,9 @@ struct SweepArgs {
     unsigned long long* dst[3];  // this sweep's (pair, spin, spin2) delta slots
     unsigned long long* acc;     // accepted-move counter
     unsigned long long thr[kMaxTable];
+    // Blume-Capel with bit-plane uniforms: proposal bits from bit planes (the block at
+    // counter e >> 7 of purpose P_PLANES holds the planes of 128 same-colour sites)
+    int planes = 0;
 };
 
 struct SweepKey {

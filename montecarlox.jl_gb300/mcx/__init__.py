@@ -295,10 +295,10 @@ class DeviceLattice(AbstractSpinSystem):
         return self.N
 
     def set_uniforms(self, form="planes"):
-        """How the sweeps of this Ising lattice draw their uniforms (mcx_lattice_set_uniforms):
-        "site" (one Philox word per site, the default) or "planes" (bit planes for the top 8
-        bits, compared for 64 sites at once; Ising, Lx a multiple of 128).  Same distribution,
-        different chain."""
+        """How the sweeps of this lattice draw their uniforms (mcx_lattice_set_uniforms):
+        "site" (one Philox word per site, the default) or "planes" (Ising, Lx a multiple of
+        128: bit planes for the top 8 bits of every uniform, compared for 64 sites at once;
+        Blume-Capel: bit planes for the proposal bits).  Same distribution, different chain."""
         _check(L.load().mcx_lattice_set_uniforms(self.handle, {"site": 0, "planes": 1}[form]))
         self.uniforms = form
 

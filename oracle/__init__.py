@@ -51,6 +51,8 @@ def lib():
         L.orc_cb_sweep_u.argtypes = L.orc_cb_sweep.argtypes + [C.c_int]
         L.orc_plane_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_uint64]
         L.orc_plane_uniform.restype = C.c_uint32
+        L.orc_bc_plane_bit.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_uint64]
+        L.orc_bc_plane_bit.restype = C.c_int
         L.orc_seq_attempts.argtypes = [i8p, C.c_int, C.c_int, i32p, C.c_int, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int64,
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
@@ -184,6 +186,11 @@ def cb_sweep(s, model, L, alg, beta, seed, stream=0, sweep0=0, nsweeps=1, J=1.0,
 def plane_uniform(seed, stream, sweep, colour, e):
     """The bit-plane uniform of colour-class site ``e`` (linear index >> 1)."""
     return lib().orc_plane_uniform(seed, stream, sweep, colour, e)
+
+
+def bc_plane_bit(seed, stream, sweep, colour, e):
+    """The Blume-Capel proposal bit of colour-class site ``e`` under bit-plane uniforms."""
+    return int(lib().orc_bc_plane_bit(seed, stream, sweep, colour, e))
 
 
 def seq_attempts(s, model, L, alg, beta, seed, stream=0, attempt0=0, nattempts=1, J=1.0, D=0.0, h=0.0):

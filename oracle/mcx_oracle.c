@@ -91,6 +91,17 @@ uint32_t orc_plane_uniform(uint64_t seed, uint32_t stream, uint64_t sweep, int c
     return u | (out[e & 3] & 0xFFFFFFu);
 }
 
+/* The Blume-Capel proposal bit of colour-class site e under bit-plane uniforms: bit e & 63
+ * of plane e >> 6, where planes 2m and 2m+1 are words 0 | 1 << 32 and 2 | 3 << 32 of the
+ * block at counter m, purpose P_PLANES (one block per 128 same-colour sites). */
+int orc_bc_plane_bit(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, uint64_t e) {
+    uint32_t out[4];
+    orc_cb_block(seed, stream, sweep, colour, P_PLANES, (uint32_t)(e >> 7), out);
+    const uint64_t plane = (e >> 6) & 1 ? ((uint64_t)out[2] | ((uint64_t)out[3] << 32))
+                                        : ((uint64_t)out[0] | ((uint64_t)out[1] << 32));
+    return (int)((plane >> (e & 63)) & 1u);
+}
+
 static double u53(uint32_t hi, uint32_t lo) {
     uint64_t k = ((uint64_t)hi << 21) | (uint64_t)(lo >> 11);
     return (double)k * 0x1p-53;
@@ -342,7 +353,7 @@ static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, do
     int rc = model == ORC_ISING ? orc_table_ising(dim, alg, beta, J, h, thr, xm)
                                 : orc_table_bc(dim, alg, beta, J, D, h, thr);
     if (rc) return rc;
-    if (uniforms && (model != ORC_ISING || L[0] % 128 != 0)) return ORC_ERR_INVALID;
+    if (uniforms && model == ORC_ISING && L[0] % 128 != 0) return ORC_ERR_INVALID;
     const int planes = uniforms;  /* every Ising rule: flip iff (u ^ xm) < thr with the plane uniform */
     int64_t P, M, Q;
     orc_observables(s, dim, L, &P, &M, &Q);
@@ -375,7 +386,8 @@ static int cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, do
                         sn = (u < thr[2 * (S + z)]) ? -1 : ((u < thr[2 * (S + z) + 1]) ? 0 : 1);
                         if (sn == so) continue;
                     } else {
-                        int b = (int)(orc_site_word(seed, stream, t, c, P_PROPOSE, (uint64_t)i) >> 31);
+                        int b = planes ? orc_bc_plane_bit(seed, stream, t, c, (uint64_t)i >> 1)
+                                       : (int)(orc_site_word(seed, stream, t, c, P_PROPOSE, (uint64_t)i) >> 31);
                         int idx = (so + 1) * 2 * nc + b * nc + (S + z);
                         uint32_t u = orc_site_word(seed, stream, t, c, P_ACCEPT, (uint64_t)i);
                         if (!((uint64_t)u < thr[idx])) continue;
@@ -404,8 +416,8 @@ int orc_cb_sweep(int8_t* s, int model, int dim, const int32_t* L, int alg, doubl
     return cb_sweep(s, model, dim, L, alg, beta, J, D, h, seed, stream, sweep0, nsweeps, obs, attempts, accepts, 0);
 }
 
-/* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes; bit
- * planes need an Ising lattice with Lx a multiple of 128 and apply to every Ising rule). */
+/* The same sweeps with the uniforms form `uniforms` (0 per-site words, 1 bit planes: every
+ * Ising rule, Ising lattices with Lx a multiple of 128; the Blume-Capel proposal bits). */
 int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, double beta,
                    double J, double D, double h, uint64_t seed, uint32_t stream,
                    uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,

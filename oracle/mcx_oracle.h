@@ -57,6 +57,8 @@ int orc_cb_sweep_u(int8_t* s, int model, int dim, const int32_t* L, int alg, dou
                    double J, double D, double h, uint64_t seed, uint32_t stream,
                    uint64_t sweep0, int64_t nsweeps, int64_t* obs, uint64_t* attempts,
                    uint64_t* accepts, int uniforms);
+/* the Blume-Capel proposal bit of colour-class site e under bit-plane uniforms */
+int orc_bc_plane_bit(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, uint64_t e);
 /* the bit-plane uniform of colour-class site e (e = linear index >> 1) */
 uint32_t orc_plane_uniform(uint64_t seed, uint32_t stream, uint64_t sweep, int colour, uint64_t e);
 

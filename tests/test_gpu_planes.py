@@ -111,6 +111,53 @@ def test_planes_general_form_parity(gpu, alg, h, L, beta, layout):
     sys_.close()
 
 
+BC_CASES = [
+    # dims, rule, beta, D, sweeps: one block (8^2, 32^2), a thread-block cluster (128 x 96), the
+    # per-site kernel (W = 3), the strip kernel (2048^2, 3-D), captured sweep graphs (66 sweeps
+    # of 1024 x 544), heat bath (no proposal: the per-site chain)
+    ([8, 8], "metropolis", 0.5, 1.0, 4), ([32, 32], "glauber", 0.6, 0.5, 4), ([128, 96], "metropolis", 0.6, 1.0, 4),
+    ([6, 8], "metropolis", 0.5, 0.7, 4), ([2048, 2048], "metropolis", 0.6, 1.0, 2), ([32, 16, 8], "glauber", 0.35, 0.7, 4),
+    ([1024, 544], "metropolis", 0.6, 1.0, 66), ([2048, 1024], "heatbath", 0.6, 1.0, 3),
+]
+
+
+@pytest.mark.parametrize("L,alg,beta,D,nsweeps", BC_CASES)
+def test_bc_planes_parity(gpu, L, alg, beta, D, nsweeps):
+    """Blume-Capel with bit-plane proposal bits on every launch form, against the oracle."""
+    sys_ = gpu.BlumeCapel(L, D=D)
+    sys_.set_uniforms("planes")
+    gpu.init_(sys_, "random", rng=gpu.Philox(13, 1))
+    a = {"metropolis": gpu.Metropolis, "glauber": gpu.Glauber, "heatbath": gpu.HeatBath}[alg](gpu.Philox(13, 1),
+                                                                                            beta=beta)
+    obs = gpu.sweep_(sys_, a, nsweeps, record=True)
+    s = O.init_random(O.BC, L, 13, 1)
+    oalg = {"metropolis": O.METROPOLIS, "glauber": O.GLAUBER, "heatbath": O.HEATBATH}[alg]
+    oobs, att, acc = O.cb_sweep(s, O.BC, L, oalg, beta, 13, stream=1, nsweeps=nsweeps, D=D, uniforms=1)
+    assert np.array_equal(obs, oobs)
+    assert np.array_equal(sys_.spins, s)
+    assert (a.flips if alg == "heatbath" else a.accepted) == acc
+    sys_.close()
+
+
+def test_bc_planes_batch(gpu):
+    """Independent Blume-Capel chains with bit planes in one mcx_sweep_batch call (the one-block
+    batch form) against their oracle runs; a per-site lattice in the same batch keeps its words."""
+    systems, algs = [], []
+    for i, u in enumerate(("planes", "site", "planes")):
+        b = gpu.BlumeCapel([32, 32], D=0.6)
+        b.set_uniforms(u)
+        gpu.init_(b, "random", rng=gpu.Philox(40 + i, i))
+        systems.append(b)
+        algs.append(gpu.Metropolis(gpu.Philox(50 + i, i), beta=0.5 + 0.05 * i))
+    obs = gpu.sweep_batch_(systems, algs, 7, record=True)
+    for i, u in enumerate(("planes", "site", "planes")):
+        s = O.init_random(O.BC, [32, 32], 40 + i, i)
+        oo, _, acc = O.cb_sweep(s, O.BC, [32, 32], O.METROPOLIS, 0.5 + 0.05 * i, 50 + i, stream=i, nsweeps=7, D=0.6,
+                                uniforms=1 if u == "planes" else 0)
+        assert np.array_equal(obs[i], oo) and np.array_equal(systems[i].spins, s) and algs[i].accepted == acc
+        systems[i].close()
+
+
 def test_planes_calls_compose_and_switch(gpu):
     """3 + 5 sweeps equal 8; switching back to per-site words continues the same lattice
     with the per-site stream; a heat-bath call in between (the general form) continues it."""
@@ -168,9 +215,6 @@ def test_planes_argument_errors(gpu):
         with pytest.raises(gpu.ArgumentError):
             s.set_uniforms("planes")
         s.close()
-    bc = gpu.BlumeCapel([128, 8], D=0.5)
-    with pytest.raises(gpu.ArgumentError):
-        bc.set_uniforms("planes")
     # the int8 kernels draw per-site words: packing off leaves no way to run the plane form
     s = gpu.Ising([128, 64])
     s.set_uniforms("planes")

@@ -55,11 +55,55 @@ def test_planes_change_the_chain(alg, h):
     assert not np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("model,L", [(O.ISING, [64, 64]), (O.ISING, [96, 8]), (O.BC, [128, 4])])
-def test_planes_need_an_ising_lattice_with_lx_multiple_of_128(model, L):
-    s = O.init_random(model, L, 1)
+@pytest.mark.parametrize("L", [[64, 64], [96, 8]])
+def test_planes_need_an_ising_lattice_with_lx_multiple_of_128(L):
+    s = O.init_random(O.ISING, L, 1)
     with pytest.raises(ValueError):
-        O.cb_sweep(s, model, L, O.METROPOLIS, 0.4, 1, nsweeps=1, D=0.5, uniforms=1)
+        O.cb_sweep(s, O.ISING, L, O.METROPOLIS, 0.4, 1, nsweeps=1, uniforms=1)
+
+
+def test_bc_plane_bit_definition():
+    """Blume-Capel proposal bit e: bit e & 63 of plane e >> 6, planes 2m, 2m+1 = words
+    0 | 1 << 32 and 2 | 3 << 32 of the block at counter m."""
+    for seed, stream, sweep in ((7, 0, 0), (2 ** 40 + 3, 5, 2 ** 33 + 9)):
+        for colour in (0, 1):
+            for e in (0, 1, 31, 32, 63, 64, 100, 127, 128, 1000, 2 ** 20 + 77):
+                o = _block(seed, stream, sweep, colour, P_PLANES, e >> 7)
+                plane = (o[2] | (o[3] << 32)) if (e >> 6) & 1 else (o[0] | (o[1] << 32))
+                assert O.bc_plane_bit(seed, stream, sweep, colour, e) == (plane >> (e & 63)) & 1
+
+
+@pytest.mark.parametrize("alg,changes", [(O.METROPOLIS, True), (O.GLAUBER, True), (O.HEATBATH, False)])
+def test_bc_planes_replace_the_proposal_bits(alg, changes):
+    """On a Blume-Capel lattice (any size) bit planes replace the proposal words; heat bath
+    has no proposal and keeps its chain."""
+    L = [10, 6]
+    a = O.init_random(O.BC, L, 5)
+    b = a.copy()
+    oa = O.cb_sweep(a, O.BC, L, alg, 0.5, 5, nsweeps=3, D=0.7)
+    ob = O.cb_sweep(b, O.BC, L, alg, 0.5, 5, nsweeps=3, D=0.7, uniforms=1)
+    assert (not np.array_equal(a, b)) == changes
+    if not changes:
+        assert np.array_equal(oa[0], ob[0])
+
+
+@pytest.mark.parametrize("alg", [O.METROPOLIS, O.GLAUBER])
+def test_bc_planes_sample_the_same_equilibrium(alg):
+    """Blume-Capel 64 x 64, D = 1, beta = 0.4 (disordered): <E>/N and <Q>/N (the density of
+    non-zero spins) of the two forms agree within 4 combined sigma of 20-sweep bins."""
+    L = [64, 64]
+    res = []
+    for u in (0, 1):
+        s = O.init_random(O.BC, L, 31 + u)
+        O.cb_sweep(s, O.BC, L, alg, 0.4, 31 + u, nsweeps=200, D=1.0, record=False, uniforms=u)
+        obs, _, _ = O.cb_sweep(s, O.BC, L, alg, 0.4, 31 + u, sweep0=200, nsweeps=1200, D=1.0, uniforms=u)
+        e = (-obs[:, 0] + 1.0 * obs[:, 2]) / s.size  # E = -J sum s_i s_j + D sum s_i^2
+        q = obs[:, 2] / s.size
+        res.append([(x.reshape(60, 20).mean(axis=1).mean(), x.reshape(60, 20).mean(axis=1).std(ddof=1) / np.sqrt(60))
+                     for x in (e, q)])
+    for k in range(2):
+        (m0, s0), (m1, s1) = res[0][k], res[1][k]
+        assert abs(m0 - m1) < 4 * np.hypot(s0, s1), (k, m0, m1, s0, s1)
 
 
 def _energy_series(uniforms, beta, L, nsweeps, burn, seed, alg=O.METROPOLIS):
