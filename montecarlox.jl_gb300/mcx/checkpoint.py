@@ -86,8 +86,8 @@ def import_state(d, ctx=None):
             s = BlumeCapel(d["dims"], J=d["J"], D=d["D"], h=d["h"], ctx=ctx)
         else:
             s = Ising(d["dims"], J=d["J"], h=d["h"], layout=d["layout"], ctx=ctx)
-            if d.get("uniforms", "site") != "site":
-                s.set_uniforms(d["uniforms"])
+        if d.get("uniforms", "site") != "site":
+            s.set_uniforms(d["uniforms"])
         s.spins = d["spins"]
         return s
     if k == "graph":
