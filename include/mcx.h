@@ -187,8 +187,10 @@ MCX_API mcx_status mcx_lattice_set_packing(mcx_lattice* lat, int32_t allow);
  * length, so mcx_sweep returns MCX_ERR_INVALID_ARG with packing off and MCX_ERR_BUDGET /
  * MCX_ERR_OOM when the N/8-byte copy does not fit.  mcx_sweep_noalloc (int8 kernels
  * only) refuses such Ising calls; mcx_sweep_batch runs them one mcx_sweep per lattice.
- * Blume-Capel lattices of any size take PLANES on every launch form.  The two forms give
- * different chains with the same distribution. */
+ * Blume-Capel lattices of any size take PLANES on every launch form.  The form governs
+ * mcx_sweep and mcx_sweep_batch; the flat-histogram walkers (mcx_flathist_sweep) and
+ * mcx_spin_flip draw their own streams whatever it is.  The two forms give different
+ * chains with the same distribution. */
 MCX_API mcx_status mcx_lattice_set_uniforms(mcx_lattice* lat, int32_t form);
 /* Times the admissible kernel shapes (sites per thread: 16, 8, 4) for this lattice
  * and algorithm on a scratch copy of the spins and keeps the fastest for later
