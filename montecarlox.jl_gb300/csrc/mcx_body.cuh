@@ -61,12 +61,14 @@ __device__ __forceinline__ void ising_chunk(Chunk<DIM, V>& ch, uint32_t c0, cons
 // 2 | 3 << 32 of the block at counter m; heat bath needs no proposal).  c0 = e0 / 4 for the
 // chunk's first colour index e0 (a chunk of at most 16 aligned sites lies in one plane).
 // Deltas go to nacc and (dP, dM, dQ).
-template <int DIM, int V, bool HB>
+// PLM: 0 per-site proposals, 1 plane proposals (both compiled in), 2 as `planes` says.
+template <int DIM, int V, bool HB, int PLM = 2>
 __device__ __forceinline__ void bc_chunk(Chunk<DIM, V>& ch, uint32_t c0, const SweepKey& key, uint32_t w2a,
-                                         uint32_t w2p, bool planes, const unsigned long long* s_thr, int& nacc,
+                                         uint32_t w2p, bool planes_arg, const unsigned long long* s_thr, int& nacc,
                                          int& dP, int& dM, int& dQ) {
     constexpr int Z = 2 * DIM;
     constexpr int NW = V / 4;
+    const bool planes = PLM == 2 ? planes_arg : PLM == 1;
     BcLanes ln;
     unsigned long long plane = 0;
     if (!HB && planes) {

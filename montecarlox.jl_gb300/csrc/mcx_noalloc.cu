@@ -108,7 +108,7 @@ extern "C" MCX_API mcx_status mcx_sweep_noalloc(mcx_lattice* lat, mcx_algorithm 
     fill_sweep_args(&a, lat, t, rng);
     a.acc = counter;
     const int V = vec_width(lat->W);
-    const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+    const HalfSweepFn fn = pick_half_sweep(lat, alg, V, t);
     const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
     for (int64_t s = 0; s < nsweeps; ++s) {
         a.sweep = rng->counter + (uint64_t)s;

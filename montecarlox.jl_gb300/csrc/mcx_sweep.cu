@@ -261,7 +261,8 @@ __device__ __forceinline__ void bc_cb_body(const SweepArgs& a, const unsigned lo
     v[3] += nacc;
 }
 
-template <int DIM, int V, bool HB>
+// PL: the proposal bits from bit planes (the lattice's form, compiled in on this path).
+template <int DIM, int V, bool HB, bool PL = false>
 __global__ void __launch_bounds__(256, 2) k_bc_strip(const SweepArgs a) {
     constexpr int NT = bc_table_size<DIM, HB>();
     __shared__ __align__(16) unsigned long long s_thr[NT];
@@ -278,11 +279,10 @@ __global__ void __launch_bounds__(256, 2) k_bc_strip(const SweepArgs a) {
     } else if (tid < tpc * (a.W / V)) {
         const SweepKey key = sweep_key(a);
         const uint32_t w2a = ctr_word2(key.sweep, a.colour, P_ACCEPT);
-        const uint32_t w2p = ctr_word2(key.sweep, a.colour, a.planes ? P_PLANES : P_PROPOSE);
-        const bool planes = a.planes != 0;
+        const uint32_t w2p = ctr_word2(key.sweep, a.colour, PL ? P_PLANES : P_PROPOSE);
         int nacc = 0, dP = 0, dM = 0, dQ = 0;
         strip_walk<DIM, V>(a, tid, tpc, [&](Chunk<DIM, V>& ch, uint32_t c0) {
-            bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, planes, s_thr, nacc, dP, dM, dQ);
+            bc_chunk<DIM, V, HB, PL ? 1 : 0>(ch, c0, key, w2a, w2p, PL, s_thr, nacc, dP, dM, dQ);
         });
         v[0] += dP;
         v[1] += dM;
@@ -495,7 +495,7 @@ static HalfSweepFn pick_ising_word(bool hb, int V) {
 }
 
 template <int DIM>
-static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, const Table& t) {
+static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, const Table& t, bool planes) {
     const bool hb = alg == MCX_HEATBATH;
     if (model == MCX_ISING) {
         if (V == 16 || V == 8 || V == 4)
@@ -503,14 +503,18 @@ static HalfSweepFn pick_kernel_dim(mcx_model model, mcx_algorithm alg, int V, co
                                                                : pick_ising_word<DIM, false>(hb, V);
         return hb ? k_ising_cb_site<DIM, true> : k_ising_cb_site<DIM, false>;
     }
-    if (V == 16) return hb ? k_bc_strip<DIM, 16, true> : k_bc_strip<DIM, 16, false>;
-    if (V == 8) return hb ? k_bc_strip<DIM, 8, true> : k_bc_strip<DIM, 8, false>;
-    if (V == 4) return hb ? k_bc_strip<DIM, 4, true> : k_bc_strip<DIM, 4, false>;
+    // Metropolis / Glauber: the proposal form compiled in (plane or per-site proposal bits)
+    if (V == 16) return hb ? k_bc_strip<DIM, 16, true> : planes ? k_bc_strip<DIM, 16, false, true> : k_bc_strip<DIM, 16, false>;
+    if (V == 8) return hb ? k_bc_strip<DIM, 8, true> : planes ? k_bc_strip<DIM, 8, false, true> : k_bc_strip<DIM, 8, false>;
+    if (V == 4) return hb ? k_bc_strip<DIM, 4, true> : planes ? k_bc_strip<DIM, 4, false, true> : k_bc_strip<DIM, 4, false>;
     return hb ? k_bc_cb_site<DIM, true> : k_bc_cb_site<DIM, false>;
 }
 
-HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t) {
-    return dim == 2 ? pick_kernel_dim<2>(model, alg, V, t) : pick_kernel_dim<3>(model, alg, V, t);
+// The half-sweep kernel of `lat` (its dimension, model and, for Blume-Capel, uniforms form).
+HalfSweepFn pick_half_sweep(const mcx_lattice* lat, mcx_algorithm alg, int V, const Table& t) {
+    const bool planes = lat->model == MCX_BLUME_CAPEL && lat->uniforms == MCX_UNIFORMS_PLANES;
+    return lat->dim == 2 ? pick_kernel_dim<2>(lat->model, alg, V, t, planes)
+                         : pick_kernel_dim<3>(lat->model, alg, V, t, planes);
 }
 
 using SmallLatticeFn = void (*)(SweepArgs, int8_t*, int8_t*, long long, long long, long long*);
@@ -673,7 +677,7 @@ static mcx_status sweep_graph(mcx_lattice* lat, mcx_algorithm alg, double beta, 
     fill_sweep_args(&a, lat, t, &r0);
     a.sweep_base = lat->d_sweep_base;
     a.acc = lat->d_acc;
-    const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+    const HalfSweepFn fn = pick_half_sweep(lat, alg, V, t);
     const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
     // Each half-sweep node after the first depends programmatically on the one before: its
     // blocks may be scheduled, and build their tables, while the previous half-sweep drains;
@@ -795,7 +799,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
             fill_sweep_args(&a, lat, t, rng);
             a.sweep_base = lat->d_sweep_base;
             a.acc = lat->d_acc;
-            const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+            const HalfSweepFn fn = pick_half_sweep(lat, alg, V, t);
             const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
             for (int64_t s = 0; s < rem; ++s) {
                 a.sweep = (uint64_t)s;
@@ -815,7 +819,7 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
         fill_sweep_args(&a, lat, t, rng);
         a.acc = lat->d_acc;
         const int V = lattice_width(lat);
-        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+        const HalfSweepFn fn = pick_half_sweep(lat, alg, V, t);
         const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         for (int64_t s = 0; s < nsweeps; ++s) {
             a.sweep = rng->counter + (uint64_t)s;
@@ -892,7 +896,7 @@ extern "C" MCX_API mcx_status mcx_autotune(mcx_lattice* lat, mcx_algorithm alg, 
         fill_sweep_args(&a, lat, t, &r);
         a.acc = acc;
         for (int j = 0; j < 3; ++j) a.dst[j] = dst + j;
-        const HalfSweepFn fn = pick_half_sweep(lat->dim, lat->model, alg, V, t);
+        const HalfSweepFn fn = pick_half_sweep(lat, alg, V, t);
         const int grid = half_sweep_grid(ctx, fn, lat->W, lat->rows, V);
         const int warm = 2, reps = 8;
         for (int k = 0; k < warm + reps && err == cudaSuccess; ++k) {

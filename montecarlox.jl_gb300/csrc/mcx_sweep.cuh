@@ -77,7 +77,7 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
 mcx_status cluster_sweep_batch(mcx_lattice** lats, int n, mcx_algorithm alg, const Table* tabs, const mcx_rng* rngs,
                                int64_t nsweeps, bool fits32, bool all_at_once, bool* done);
 
-HalfSweepFn pick_half_sweep(int dim, mcx_model model, mcx_algorithm alg, int V, const Table& t);
+HalfSweepFn pick_half_sweep(const mcx_lattice* lat, mcx_algorithm alg, int V, const Table& t);
 int vec_width(int64_t W);
 int lattice_width(const mcx_lattice* lat);
 int half_sweep_grid(const mcx_ctx* ctx, HalfSweepFn fn, int64_t W, int64_t rows, int V);
