@@ -93,8 +93,9 @@ __device__ __forceinline__ void cluster_run(const ClusterArgs& ca) {
             const int8_t* const oth = c ? s[0] : s[1];
             int8_t* const up_halo = c ? up1 : up0;
             int8_t* const dn_halo = c ? dn1 : dn0;
+            // Blume-Capel: T32 carries the proposal form (bit planes), compiled in
             const uint32_t w2a = ctr_word2(key.sweep, c, P_ACCEPT),
-                           w2p = ctr_word2(key.sweep, c, a0.planes ? P_PLANES : P_PROPOSE);
+                           w2p = ctr_word2(key.sweep, c, KIND == 2 && T32 ? P_PLANES : P_PROPOSE);
             int nacc = 0, nup = 0, isum = 0, dP = 0, dM = 0, dQ = 0;
             for (ChunkIter it = it0; it.valid(); it.next()) {
                 const int lu = it.z + 1;
@@ -124,7 +125,7 @@ __device__ __forceinline__ void cluster_run(const ClusterArgs& ca) {
                 ch.load(cur, oth, W, lr, k0, ri);
                 const uint32_t c0 = (uint32_t)(((unsigned long long)gr * W + k0) >> 2);
                 if constexpr (KIND == 0) ising_chunk<DIM, V, HB, T32>(ch, c0, key, w2a, s_thr, s_t32, nacc, nup, isum);
-                else bc_chunk<DIM, V, HB>(ch, c0, key, w2a, w2p, a0.planes != 0, s_thr, nacc, dP, dM, dQ);
+                else bc_chunk<DIM, V, HB, T32 ? 1 : 0>(ch, c0, key, w2a, w2p, T32, s_thr, nacc, dP, dM, dQ);
                 store_row<V>(cur + lr * W + k0, ch.own);
                 const int uoff = it.y * W + k0;
                 if (it.z == 0) store_row<V>(up_halo + uoff, ch.own);
@@ -211,7 +212,9 @@ typename K<0, 2, 4, false, false>::Fn pick_cluster_dim(bool ising, bool hb, bool
         if (hb) return t32 ? pick_cluster_v<K, 0, DIM, true, true>(V) : pick_cluster_v<K, 0, DIM, true, false>(V);
         return t32 ? pick_cluster_v<K, 0, DIM, false, true>(V) : pick_cluster_v<K, 0, DIM, false, false>(V);
     }
-    return hb ? pick_cluster_v<K, 2, DIM, true, false>(V) : pick_cluster_v<K, 2, DIM, false, false>(V);
+    // Blume-Capel: t32 selects the bit-plane proposal form (Metropolis / Glauber)
+    return hb ? pick_cluster_v<K, 2, DIM, true, false>(V)
+              : t32 ? pick_cluster_v<K, 2, DIM, false, true>(V) : pick_cluster_v<K, 2, DIM, false, false>(V);
 }
 
 template <template <int, int, int, bool, bool> class K>
@@ -283,7 +286,9 @@ mcx_status cluster_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, co
     *done = false;
     if (!cluster_eligible(lat) || nsweeps < 1 || lat->cluster_size < 0) return MCX_OK;
     const bool hb = alg == MCX_HEATBATH, ising = lat->model == MCX_ISING;
-    const bool t32 = ising && ising_table_fits32(t.thr, t.n, 2 * lat->dim, hb);
+    // Ising: the 32-bit table form; Blume-Capel: bit-plane proposals
+    const bool t32 = ising ? ising_table_fits32(t.thr, t.n, 2 * lat->dim, hb)
+                           : !hb && lat->uniforms == MCX_UNIFORMS_PLANES;
     const long long unitB = (long long)cut_rows(lat) * lat->W;
     ClusterArgs ca;
     fill_cluster_args(&ca, lat, t, rng, nsweeps, 0);

@@ -978,9 +978,12 @@ extern "C" MCX_API mcx_status mcx_sweep_batch(mcx_lattice** lats, int32_t n, mcx
     if (nsweeps == 0) return MCX_OK;
     if (n == 1)  // the single-lattice forms
         return mcx_sweep(lats[0], alg, betas[0], &rngs[0], nsweeps, obs_series ? obs_series[0] : nullptr, counters);
-    bool planes = false;  // bit-plane uniforms run on the words, one mcx_sweep per lattice
+    // bit-plane uniforms run one mcx_sweep per lattice (Ising: on the words; Blume-Capel: the
+    // batch kernels compile the per-site proposal form in)
+    bool planes = false;
     for (int i = 0; i < n; ++i)
-        planes = planes || msc_planes_ok(lats[i], alg, tabs[i]);
+        planes = planes || msc_planes_ok(lats[i], alg, tabs[i]) ||
+                 (lats[i]->model == MCX_BLUME_CAPEL && lats[i]->uniforms == MCX_UNIFORMS_PLANES && alg != MCX_HEATBATH);
     if (planes) {
         for (int i = 0; i < n; ++i)
             MCX_CHECK(mcx_sweep(lats[i], alg, betas[i], &rngs[i], nsweeps, obs_series ? obs_series[i] : nullptr,
