@@ -295,3 +295,51 @@ def test_planes_kaufman_l128(gpu, alg, beta, start):
     exact = kaufman_ising2d(L, L, beta)[1] / (L * L)
     se = means.std(ddof=1) / math.sqrt(nch)
     assert abs(means.mean() - exact) < 3 * se, (means.mean(), exact, se)
+
+
+@pytest.mark.parametrize("alg", ["metropolis", "glauber", "heatbath"])
+def test_planes_antiferromagnet(gpu, alg):
+    """J = -1: the thresholds fit neither the rank nor the class form (some classes always
+    flip), so every rule takes the general form; against the oracle on both layouts."""
+    L = [256, 32]
+    for layout in ("int8", "msc64"):
+        sys_ = gpu.Ising(L, J=-1.0, layout=layout)
+        sys_.set_uniforms("planes")
+        gpu.init_(sys_, "random", rng=gpu.Philox(17))
+        a = {"metropolis": gpu.Metropolis, "glauber": gpu.Glauber, "heatbath": gpu.HeatBath}[alg](gpu.Philox(17),
+                                                                                                beta=0.5)
+        obs = gpu.sweep_(sys_, a, 3, record=True)
+        s = O.init_random(O.ISING, L, 17)
+        oalg = {"metropolis": O.METROPOLIS, "glauber": O.GLAUBER, "heatbath": O.HEATBATH}[alg]
+        oobs, _, acc = O.cb_sweep(s, O.ISING, L, oalg, 0.5, 17, nsweeps=3, J=-1.0, uniforms=1)
+        assert np.array_equal(obs, oobs) and np.array_equal(sys_.spins, s)
+        assert (a.flips if alg == "heatbath" else a.accepted) == acc
+        sys_.close()
+
+
+def test_bc_planes_noalloc(gpu):
+    """mcx_sweep_noalloc on a Blume-Capel lattice with bit-plane proposals equals mcx_sweep on a
+    twin lattice, bit for bit, over two calls."""
+    import ctypes as C
+    import torch
+    lib = gpu._lib.load()
+    fn = lib.mcx_sweep_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(gpu._lib.mcx_rng), C.c_int64, C.c_void_p,
+                   C.c_void_p]
+    a = gpu.BlumeCapel([256, 64], D=0.8)
+    b = gpu.BlumeCapel([256, 64], D=0.8)
+    for x in (a, b):
+        x.set_uniforms("planes")
+        gpu.init_(x, "random", rng=gpu.Philox(21))
+    ra = gpu._lib.mcx_rng(5, 0, 2, 0)
+    rb = gpu._lib.mcx_rng(5, 0, 2, 0)
+    for n in (5, 9):
+        oa = np.zeros((n, 3), np.int64)
+        gpu._check(lib.mcx_sweep(a.handle, 0, 0.6, C.byref(ra), n, oa.ctypes.data, None))
+        ob = torch.full((n, 3), -1, dtype=torch.int64, device="cuda")
+        gpu._check(fn(b.handle, 0, 0.6, C.byref(rb), n, ob.data_ptr(), None))
+        torch.cuda.synchronize()
+        assert np.array_equal(oa, ob.cpu().numpy()) and np.array_equal(a.spins, b.spins)
+    a.close()
+    b.close()
