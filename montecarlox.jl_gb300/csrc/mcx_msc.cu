@@ -90,6 +90,7 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
     }
 }
 
+// k_msc_metro (named for its first rule; FORM selects the rule family): FORM 0, a
 // Metropolis-type rule in rank form (no field): every class with at most Z/2 aligned
 // neighbours is always accepted, and the threshold t_k of a site with Z/2 + k aligned
 // neighbours is the same for both spin states and non-increasing in k.  Aligned
