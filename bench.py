@@ -121,15 +121,15 @@ CB_TRAFFIC_PER_LAUNCH = 16810240
 # The same for one k_msc_metro<2,*> launch (the headline workload's kernel: int8 lattices run
 # multi-sweep calls on a transient 64-sites-per-word copy), per uniforms form,
 # profiles/msc_metro_L4096.md and profiles/int_pipes_ising_strip_and_pt_persistent.md.
-MSC_TRAFFIC_PER_LAUNCH = {("site", "metropolis"): 2136576, ("planes", "metropolis"): 2118656,
+MSC_TRAFFIC_PER_LAUNCH = {("site", "metropolis"): 2136064, ("planes", "metropolis"): 2118400,
                           ("planes", "glauber"): 2123520, ("planes", "heatbath"): 2120960}
 
 # Per-launch integer-pipe work of the headline kernels from one ncu capture each
 # (profiles/int_pipes_ising_strip_and_pt_persistent.md): warp instructions, ALU-pipe warp
 # instructions (2 cycles each on a sub-partition's ALU pipe) and FMA-pipe active cycles.
 CB_PIPES = {"warp_inst": 7033664, "alu_inst": 3798288, "fma_cycles": 7453376, "per": "launch"}
-MSC_PIPES = {("site", "metropolis"): {"warp_inst": 4710668, "alu_inst": 2143878, "fma_cycles": 6717168, "per": "launch"},
-             ("planes", "metropolis"): {"warp_inst": 2699982, "alu_inst": 1276356, "fma_cycles": 2403736,
+MSC_PIPES = {("site", "metropolis"): {"warp_inst": 4686044, "alu_inst": 2143878, "fma_cycles": 6684336, "per": "launch"},
+             ("planes", "metropolis"): {"warp_inst": 2712288, "alu_inst": 1276356, "fma_cycles": 2420152,
                                         "per": "launch"},
              ("planes", "glauber"): {"warp_inst": 3616731, "alu_inst": 1978005, "fma_cycles": 2560230, "per": "launch"},
              ("planes", "heatbath"): {"warp_inst": 3748500, "alu_inst": 2221129, "fma_cycles": 2761404, "per": "launch"}}
