@@ -43,6 +43,16 @@ def test_plane_uniform_bits_are_balanced():
     assert ((counts - exp) ** 2 / exp).sum() < 255 + 6 * np.sqrt(2 * 255)
 
 
+def test_plane_uniforms_of_neighbouring_sites_are_uncorrelated():
+    """Sites e and e + 1 (and e + 64, the same bit of the next plane word) take their top bits
+    from neighbouring bits of the same Philox words: their correlation is within 4 sigma of 0."""
+    us = np.array([O.plane_uniform(13, 2, 9, 0, e) for e in range(1 << 14)], np.float64)
+    x = (us - us.mean()) / us.std()
+    for lag in (1, 2, 64):
+        r = float((x[:-lag] * x[lag:]).mean())
+        assert abs(r) < 4 / np.sqrt(x.size - lag), (lag, r)
+
+
 @pytest.mark.parametrize("alg,h", [(O.METROPOLIS, 0.0), (O.GLAUBER, 0.0), (O.HEATBATH, 0.0), (O.METROPOLIS, 0.2),
                                    (O.GLAUBER, -0.2), (O.HEATBATH, 0.3)])
 def test_planes_change_the_chain(alg, h):
