@@ -104,15 +104,14 @@ __device__ __forceinline__ void count_bits(const unsigned long long (&x)[Z], uns
 // plane where its bit and its threshold's differ, and only the sites tied after 8 planes
 // (probability 2^-8 each) draw the low 24 bits from a per-site block.
 //
-// FORM 1 (bit planes only): the class form, a threshold below 2^32 for every aligned count,
-// the same for both spin states (Glauber without a field); K = Z + 1 classes, none always
-// accepted.  FORM 2 (bit planes only): any Ising rule (heat bath, a field): a site flips iff
+// FORM 1: the class form, a threshold below 2^32 for every aligned count, the same for both
+// spin states (Glauber without a field); K = Z + 1 classes, none always accepted.  FORM 2 (bit planes only): any Ising rule (heat bath, a field): a site flips iff
 // (u ^ x) < t_c for its class c = (aligned count, spin), x all ones for up spins under heat
 // bath; the word keeps its eight planes from before the wait, and each plane's per-site
 // threshold bit is selected from the class leaves by the bit-sliced count and the spin.
 template <int DIM, bool PL, int FORM>
 __global__ void __launch_bounds__(288, 3) k_msc_metro(const MscArgs a) {
-    static_assert(PL || FORM == 0, "the class and general forms are swept with bit-plane uniforms only");
+    static_assert(PL || FORM != 2, "the general form is swept with bit-plane uniforms only");
     constexpr bool ALL = FORM == 1, GEN = FORM == 2;
     constexpr int Z = 2 * DIM;
     constexpr int K = GEN ? 1 : ALL ? Z + 1 : Z / 2;
@@ -342,16 +341,19 @@ static bool msc_rank_form(const Table& t, int Z) {
     return true;
 }
 
-// Whether `alg` with table `t` is swept on the packed words (k_msc_metro's rank form).
-bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
-    return lat->model == MCX_ISING && alg != MCX_HEATBATH && msc_rank_form(t, 2 * lat->dim);
-}
-
 // The class form: one threshold below 2^32 per aligned count, equal for both spin states.
 static bool msc_class_form(const Table& t, int Z) {
     for (int al = 0; al <= Z; ++al)
         if (t.thr[al] != t.thr[al + Z + 1] || t.thr[al] >= (1ull << 32)) return false;
     return true;
+}
+
+// Whether `alg` with table `t` is swept on the packed words with per-site uniforms: the rank
+// form of k_msc_metro (Metropolis without a field) or its class form (Glauber without a
+// field: each site's word compared with all z+1 class thresholds).
+bool msc_rank_ok(const mcx_lattice* lat, mcx_algorithm alg, const Table& t) {
+    return lat->model == MCX_ISING && alg != MCX_HEATBATH &&
+           (msc_rank_form(t, 2 * lat->dim) || msc_class_form(t, 2 * lat->dim));
 }
 
 // Whether a call of `alg` on `lat` draws bit-plane uniforms (and so runs on the packed words):
@@ -464,7 +466,9 @@ mcx_status msc_sweep(mcx_lattice* lat, mcx_algorithm alg, const Table& t, const 
     using Fn = void (*)(const MscArgs);
     const Fn fns[2][4] = {{k_msc_metro<2, false, 0>, k_msc_metro<2, true, 0>, k_msc_metro<2, true, 1>, k_msc_metro<2, true, 2>},
                           {k_msc_metro<3, false, 0>, k_msc_metro<3, true, 0>, k_msc_metro<3, true, 1>, k_msc_metro<3, true, 2>}};
-    const Fn fn = fns[lat->dim == 3][pl ? 1 + form : 0];
+    const Fn site_fns[2][2] = {{k_msc_metro<2, false, 0>, k_msc_metro<2, false, 1>},
+                               {k_msc_metro<3, false, 0>, k_msc_metro<3, false, 1>}};
+    const Fn fn = pl ? fns[lat->dim == 3][1 + form] : site_fns[lat->dim == 3][form];  // site: form 0 or 1
     const int grid = occupancy_grid(ctx, (const void*)fn, (long long)a.nw * a.rows, 288, 0);  // one wave
     // every launch after the first depends programmatically on the one before (the
     // kernels read the lattice after pdl_wait)
