@@ -176,7 +176,7 @@ MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, double beta,
                              mcx_rng* rng, int64_t nsweeps, int64_t* obs_series,
                              mcx_counters* counters);
 /* Whether mcx_sweep may run calls of 16 sweeps or more of this int8 Ising lattice on a
- * transient 64-sites-per-word copy (Metropolis without a field, Lx a multiple of 128,
+ * transient 64-sites-per-word copy (Metropolis or Glauber without a field, Lx a multiple of 128,
  * above 524,288 sites): packed at the start of the call, unpacked at its end, N/8 bytes
  * of device memory on first use within the HBM budget.  Results are bit-identical either
  * way; the copy is faster.  Default on; off keeps every call on the int8 kernels. */

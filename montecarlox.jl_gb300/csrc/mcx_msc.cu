@@ -3,10 +3,11 @@
 // colour-split layout; bit set = spin up).  Neighbour counts are formed for 64
 // sites at once with bit-sliced adders.  With per-site uniforms every site draws its
 // own Philox word, so results are bit-identical to the int8 kernels, and only rules in
-// the rank form of k_msc_metro (Metropolis without a field) are swept on the words: the
-// other rules (heat bath, Glauber, a field) would need a per-site table lookup, which on
-// a GB300 ran at 451-479 attempts/ns against 749-759 on the int8 words, so MSC64 lattices
-// sweep those on their int8 arrays (mcx_sweep unpacks before and packs after the call).
+// the rank or the class form of k_msc_metro (Metropolis or Glauber without a field) are
+// swept on the words: the other rules (heat bath, a field) would need a per-site table
+// lookup, which on a GB300 ran at 451-479 attempts/ns against 749-759 on the int8 words, so
+// MSC64 lattices sweep those on their int8 arrays (mcx_sweep unpacks before and packs after
+// the call).
 // With bit-plane uniforms (mcx_lattice_set_uniforms) every Ising rule is swept on the
 // words, in the rank, class or general form of k_msc_metro.
 #include "mcx_device.cuh"
@@ -363,8 +364,8 @@ bool msc_planes_ok(const mcx_lattice* lat, mcx_algorithm, const Table&) {
 }
 
 // Whether a multi-sweep call on an int8 Ising lattice may run on a transient MSC64 copy
-// (packed at the start of the call, unpacked at its end): Metropolis-type rule in the rank
-// form of k_msc_metro, rows of a multiple of 64 same-colour sites.  Same stream, same
+// (packed at the start of the call, unpacked at its end): a rule in the rank or the class form
+// of k_msc_metro, rows of a multiple of 64 same-colour sites.  Same stream, same
 // results; the copy is allocated on first use (within the HBM budget, else the call
 // stays on the int8 kernels).
 // Allocates the transient copy once (MCX_OK, MCX_ERR_BUDGET or MCX_ERR_OOM; sets no error).

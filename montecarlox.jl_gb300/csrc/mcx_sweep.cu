@@ -734,8 +734,9 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     // block; larger ones replay a captured chunk of kGraphChunk sweeps as often as it fits
     // and launch the rest directly
     // With per-site uniforms MSC64 lattices sweep the packed words only under k_msc_metro's
-    // rank form; other rules run on their int8 arrays (unpacked before, packed after the
-    // call), which is faster than a per-site table lookup on the words.
+    // rank or class form (Metropolis or Glauber without a field); other rules run on their
+    // int8 arrays (unpacked before, packed after the call), which is faster than a per-site
+    // table lookup on the words.
     // With bit-plane uniforms every Ising call runs on the words: an int8 lattice's on its
     // transient copy, whatever the call's length (the int8 kernels draw per-site words).
     const bool pl_rule = msc_planes_ok(lat, alg, t);  // every Ising rule under bit-plane uniforms
@@ -747,9 +748,10 @@ extern "C" MCX_API mcx_status mcx_sweep(mcx_lattice* lat, mcx_algorithm alg, dou
     if (via_int8) MCX_CHECK(msc_unpack(lat));
     MCX_CUDA(cudaMemsetAsync(lat->d_series, 0, (size_t)nsweeps * 3 * sizeof(int64_t), ctx->stream));
     MCX_CUDA(cudaMemsetAsync(lat->d_acc, 0, sizeof(unsigned long long), ctx->stream));
-    // large int8 Ising lattices under a rank-form Metropolis rule run calls of kMscMinSweeps
-    // sweeps or more on a transient 64-sites-per-word copy (k_msc_metro: 25 % faster than the
-    // int8 words; packing and unpacking cost about two sweeps' worth of one-pass copies)
+    // large int8 Ising lattices under Metropolis or Glauber without a field run calls of
+    // kMscMinSweeps sweeps or more on a transient 64-sites-per-word copy (k_msc_metro: 1.8x
+    // and 1.46x the int8 words; packing and unpacking cost about two sweeps' worth of
+    // one-pass copies)
     const bool transient = planes || (int8 && lat->N > kClusterLattice && nsweeps >= kMscMinSweeps &&
                                       msc_transient_ok(lat, alg, t));
     bool clustered = false;
